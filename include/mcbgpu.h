@@ -1,0 +1,161 @@
+/*
+ * mcbgpu.h — C ABI of the GB300 (sm_103a) de Pina hot path (libmcbgpu.so).
+ *
+ * Three groups of entry points:
+ *
+ * 1. The reference's own GPU-layer free functions (gpu/common.cuh:18-27), under
+ *    their original names, with the reference's behaviour (print + exit on a CUDA
+ *    error, utils.h:36-47), plus status-returning mcbgpu_* forms of the same calls.
+ *
+ * 2. The gpu_struct object (gpu/gpu_struct.cuh:44-84) as a handle: create /
+ *    initialize_memory / copy_support_vector / process_shortest_path / clear_memory.
+ *    process_shortest_path computes, for every FVS tree and every position of the
+ *    reference's level-ordered layout, the parity of the support vector over the
+ *    non-tree edges on the root path (gpu/kernel_init_edges.cu:33-75 followed by
+ *    gpu/kernel_multi_search.cu:63-108) and copies the labels to the caller's
+ *    per-chunk host rows, as the reference does (gpu/gpu_struct.cu:158-193).
+ *
+ * 3. The device-resident main loop (mcb/mcb_cycle_deg_two_remove.cpp:317-398):
+ *    candidates in rank order, each with its sorted list of cycle coordinates,
+ *    are uploaded once; the support vectors S_j live in HBM; the search for the
+ *    first odd candidate, the cycle vector and the independence update run on the
+ *    device.  Two forms give identical results:
+ *      - per iteration: mcbgpu_select / mcbgpu_cycle_vector / mcbgpu_update, one
+ *        call each per iteration e, as the reference loop calls them;
+ *      - blocked: mcbgpu_solver_run, which runs 64 iterations per pass (the search
+ *        finds the 64 rank-ordered independent candidates for S_e..S_{e+63} in
+ *        one sweep and the update applies the 64 iterations' changes to every later
+ *        S_j in one sweep; GF(2) arithmetic is exact, so the selected sequence is
+ *        the reference's).
+ *
+ * All mcbgpu_* functions return MCBGPU_OK (0) or a negative MCBGPU_E* code and
+ * never exit; mcbgpu_last_error() describes the last failure of the calling
+ * thread.  Streams are passed as `void *` (a cudaStream_t; NULL = legacy default).
+ * One handle must not be used from two threads at once.
+ */
+#ifndef MCBGPU_H
+#define MCBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MCBGPU_OK = 0,
+    MCBGPU_E_ARG = -1,        /* invalid argument / size */
+    MCBGPU_E_CUDA = -2,       /* a CUDA runtime call failed */
+    MCBGPU_E_NOMEM = -3,      /* device or host allocation failed */
+    MCBGPU_E_STATE = -4,      /* call out of order */
+    MCBGPU_E_DEVICE = -5,     /* a kernel reported an error status (see mcbgpu_last_error) */
+    MCBGPU_E_NO_CANDIDATE = -6 /* no odd candidate for some S_e (input has no cycle basis in its candidate set) */
+};
+
+const char *mcbgpu_last_error(void);
+int mcbgpu_version(void); /* ABI version, currently 1 */
+
+/* ---- 1. reference free functions (gpu/common.cuh:18-27) ------------------- */
+/* gpu/common.cu:9-12 */
+void init_cuda(void);
+/* gpu/common.cu:14-30: grid = #SMs, block = max threads; returns min(end-start, #SMs) */
+size_t configure_grid(int start, int end);
+/* gpu/common.cu:32-41: pinned host buffer of chunk*nodes uint32 */
+unsigned *allocate_pinned_memory(int chunk, int nodes);
+/* gpu/common.cu:43-46 */
+void free_pinned_memory(unsigned *ptr);
+/* gpu/common.cu:48-67: how many trees of `num_nodes` fit next to the map and S */
+size_t calculate_chunk_size(size_t num_nodes, size_t num_edges, size_t size_vector, size_t nstream);
+
+int mcbgpu_init_cuda(int *device, int *sm_count, size_t *total_global_mem);
+int mcbgpu_allocate_pinned(size_t bytes, void **out);
+int mcbgpu_free_pinned(void *ptr);
+
+/* ---- 2. gpu_struct (gpu/gpu_struct.cuh:44-84) ----------------------------- */
+typedef struct mcbgpu_struct mcbgpu_struct;
+
+/* gpu_struct::gpu_struct (gpu/gpu_struct.cuh:44-60, gpu_struct.cu:3-17).
+ * num_edges = 2m' (size of the non-tree-edge map), size_vector = ceil(N/64).
+ * All fvs_size trees are kept resident in HBM (the reference's chunk streaming,
+ * gpu_struct.cu:132-156, is not needed on a 288 GB device); chunk_size only fixes
+ * the host row layout of compressed_trees (ceil(F/chunk) rows of chunk trees). */
+int mcbgpu_struct_create(mcbgpu_struct **out, int num_edges, int num_non_tree_edges, int size_vector,
+                         int original_nodes, int fvs_size, int chunk_size, int nstreams);
+/* gpu_struct::initialize_memory (gpu_struct.cu:76-101): the map (num_edges int32)
+ * and, per host row i, edge_offset[i] (chunk*n int32), tree_rows[i]
+ * (chunk*(n+1) uint32) and tree_cols[i] (chunk*n uint32) as compressed_trees holds
+ * them (include/compressed_trees.h:112-128). */
+int mcbgpu_struct_initialize_memory(mcbgpu_struct *s, const int32_t *non_tree_edges_map,
+                                    const int32_t *const *edge_offset_rows,
+                                    const uint32_t *const *tree_rows_rows,
+                                    const uint32_t *const *tree_cols_rows);
+/* gpu_struct::copy_support_vector (gpu_struct.cu:104-114): upload S (size_vector
+ * words); *ms = elapsed milliseconds (may be NULL). */
+int mcbgpu_struct_copy_support_vector(mcbgpu_struct *s, const uint64_t *support_vector, float *ms);
+/* gpu_struct::process_shortest_path (gpu_struct.cu:169-193): labels of every
+ * position of every tree for the current S, written as uint32 0/1 into
+ * precompute_rows[i] (chunk*n per host row, the layout of
+ * compressed_trees::precompute_value).  precompute_rows may be NULL to keep the
+ * labels on the device only.  multiple_transfer is accepted for signature parity;
+ * trees are always resident. */
+int mcbgpu_struct_process_shortest_path(mcbgpu_struct *s, uint32_t *const *precompute_rows,
+                                        int multiple_transfer, float *ms);
+/* gpu_struct::clear_memory (gpu_struct.cu:19-28); also frees the handle. */
+int mcbgpu_struct_clear_memory(mcbgpu_struct *s);
+
+/* ---- 3. device-resident main loop ------------------------------------------ */
+typedef struct mcbgpu_solver mcbgpu_solver;
+
+/* num_coords = N, num_candidates = K (rank order), nnz = total coordinates. */
+int mcbgpu_solver_create(mcbgpu_solver **out, int32_t num_coords, int64_t num_candidates, int64_t nnz);
+/* Upload the rank-ordered candidates: weight[K], offsets[K+1] (int64, offsets[0]
+ * = 0, offsets[K] = nnz) and coords[nnz] (each candidate's list sorted ascending,
+ * values in [0, N)).  Resets every S_j to the unit vector e_j (the reference's
+ * initial support vectors, mcb/mcb_cycle_deg_two_remove.cpp:274-278).  Asynchronous
+ * on `stream` with respect to the device; host buffers must stay valid until the
+ * stream has passed this point. */
+int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t *offsets,
+                         const int32_t *coords, void *stream);
+/* Reset S to the unit vectors without re-uploading the candidates. */
+int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream);
+
+/* Per-iteration form.  The caller runs e = 0, 1, ... in order.
+ * select: rank of the first candidate with <C, S_e> = 1 (the scan of
+ *   mcb/mcb_cycle_deg_two_remove.cpp:329-358); written to *rank (host, after a
+ *   stream sync) if rank != NULL, and kept on the device for the next two calls.
+ * cycle_vector: C_e of the selected candidate as ceil(N/64) words
+ *   (include/cycles.h:144-195) into `words` (host, may be NULL: device only).
+ * update: for every j > e with <C_e, S_j> odd, S_j ^= S_e (mcb/mcb_cycle_deg_two_remove.cpp:371-390). */
+int mcbgpu_select(mcbgpu_solver *s, int32_t e, int64_t *rank, void *stream);
+int mcbgpu_cycle_vector(mcbgpu_solver *s, int32_t e, uint64_t *words, void *stream);
+int mcbgpu_update(mcbgpu_solver *s, int32_t e, void *stream);
+
+/* Blocked form: iterations [0, min(max_iterations, N)) (max_iterations < 0: all),
+ * enqueued on `stream` without host synchronisation.  Results via
+ * mcbgpu_solver_results. */
+int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream);
+/* Per-iteration form over all iterations, enqueued without host synchronisation
+ * (select + update per iteration). */
+int mcbgpu_solver_run_plain(mcbgpu_solver *s, int64_t max_iterations, void *stream);
+/* Synchronises `stream`; copies selected[e] (rank chosen at iteration e) for the
+ * iterations run, the 64-bit total weight, and checks the device status word. */
+int mcbgpu_solver_results(mcbgpu_solver *s, int64_t *selected, int64_t count, int64_t *total_weight,
+                          void *stream);
+/* Copy S_j (ceil(N/64) words) to the host (synchronous). */
+int mcbgpu_solver_get_support(mcbgpu_solver *s, int32_t j, uint64_t *words, void *stream);
+/* Kernel launches issued by this handle so far (for accounting). */
+int64_t mcbgpu_solver_launches(const mcbgpu_solver *s);
+/* Device bytes held by the handle. */
+int64_t mcbgpu_solver_device_bytes(const mcbgpu_solver *s);
+int mcbgpu_solver_destroy(mcbgpu_solver *s);
+
+/* One-shot call with host buffers: create, upload, blocked run, results, destroy.
+ * selected[N] receives the rank chosen at each iteration. */
+int mcbgpu_solve(int32_t num_coords, int64_t num_candidates, const int32_t *weight, const int64_t *offsets,
+                 const int32_t *coords, int64_t *selected, int64_t *total_weight);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,120 @@
+/*
+ * mcbhost.h — C ABI of the host-side preprocessing library (libmcbhost.so).
+ *
+ * This is the host half of the minimum-cycle-basis driver: everything the
+ * reference's mcb driver does before its de Pina main loop, re-implemented in C++
+ * so that its outputs are identical to the reference's:
+ *   - symmetric Matrix-Market input          (include/FileReader.h:27-67)
+ *   - CSR with both directions, (row,col)-sorted (include/CsrGraph.h:113-174)
+ *   - degree-two chain contraction + relabel  (include/CsrGraphDegreeTwoRemoval.cpp:12-126,
+ *                                              include/CsrGraphMulti.h:229-300)
+ *   - MGA feedback vertex set                 (include/FVS.cpp:166-214)
+ *   - DFS spanning tree -> coordinate order   (include/CsrGraphMultiSpanningTree.cpp:11-135,
+ *                                              mcb/mcb_cycle_deg_two_remove.cpp:175-187)
+ *   - one Dijkstra tree per FVS root and the candidate cycles
+ *                                             (include/Dijkstra.h:78-254,
+ *                                              include/work_per_thread.h:92-147)
+ *   - candidate collection and sort = the tie-break order
+ *                                             (mcb/mcb_cycle_deg_two_remove.cpp:244-265)
+ * It also builds, per candidate, the sorted list of cycle coordinates that
+ * cycle::get_cycle_vector would set (include/cycles.h:144-195), and, on request,
+ * the reference's level-ordered per-tree GPU layout (include/Dijkstra.h:151-203).
+ *
+ * All functions return 0 on success and a negative MCBH_E* code on failure; no
+ * function calls exit().  Vertex ids are 0-based.
+ */
+#ifndef MCBHOST_H
+#define MCBHOST_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MCBH_OK = 0,
+    MCBH_E_ARG = -1,       /* bad argument */
+    MCBH_E_IO = -2,        /* cannot open / parse the input file */
+    MCBH_E_FORMAT = -3,    /* unsupported Matrix-Market banner */
+    MCBH_E_GRAPH = -4,     /* graph the reference cannot process (e.g. disconnected) */
+    MCBH_E_STATE = -5,     /* call out of order (e.g. accessor before prepare) */
+    MCBH_E_NOMEM = -6      /* allocation failed */
+};
+
+typedef struct mcbh_problem mcbh_problem;
+
+typedef struct mcbh_options {
+    int threads;          /* OpenMP threads for the per-root tree loop (<=0: all) */
+    int contract_chains;  /* 1: degree-two contraction (mcb_cpu / mcb_cuda);
+                             0: none, spanning-tree root 0 (mcb_cpu_baseline, mcb/mcb_cycle.cpp:110-113) */
+    int keep_trees;       /* keep per-tree vertex-indexed parent edge offsets (F x n int32) */
+    int ref_layout;       /* build the reference's level-ordered GPU layout (4 arrays of F x n) */
+    int cycle_lists;      /* build per-candidate sorted coordinate lists */
+} mcbh_options;
+
+typedef struct mcbh_info {
+    int32_t nodes;           /* input vertices */
+    int64_t edges2;          /* input directed edge slots (2m) */
+    int32_t single_cycle;    /* every vertex has degree two: the basis is the graph itself */
+    int32_t nodes_removed;   /* vertices removed by chain contraction */
+    int32_t reduced_nodes;   /* n' */
+    int64_t reduced_edges2;  /* 2m' */
+    int32_t source_vertex;   /* root of the initial DFS spanning tree */
+    int32_t fvs_size;        /* F */
+    int32_t num_coords;      /* N = m' - n' + 1 (non-tree edges = bit-vector coordinates) */
+    int64_t num_candidates;  /* K */
+    int64_t cycle_nnz;       /* total length of the per-candidate coordinate lists */
+    int64_t total_weight_input; /* sum of input edge weights (64-bit) */
+    double t_read, t_reduce, t_fvs, t_spanning, t_trees, t_collect; /* seconds */
+} mcbh_info;
+
+/* ---- construction ---------------------------------------------------------- */
+int mcbh_problem_from_mtx(const char *path, mcbh_problem **out);
+/* m undirected edges (u[i], v[i], w[i]), 0-based, inserted in that order. */
+int mcbh_problem_from_edges(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
+                            const int32_t *w, mcbh_problem **out);
+int mcbh_prepare(mcbh_problem *p, const mcbh_options *opt);
+void mcbh_problem_free(mcbh_problem *p);
+
+/* ---- accessors (caller-allocated outputs) --------------------------------- */
+int mcbh_get_info(const mcbh_problem *p, mcbh_info *info);
+/* reduced multigraph CSR, each of length 2m' (row_offsets: n'+1) */
+int mcbh_get_reduced_graph(const mcbh_problem *p, uint32_t *rows, uint32_t *cols, int32_t *weights,
+                           uint32_t *reverse_edge, uint32_t *row_offsets);
+int mcbh_get_fvs(const mcbh_problem *p, int32_t *fvs_array /* n' */, uint32_t *fvs_vertices /* F */);
+/* coord_edges[c] = edge offset of coordinate c (N); edge_coord[o] = coordinate of offset o or -1 (2m') */
+int mcbh_get_coords(const mcbh_problem *p, uint32_t *coord_edges, int32_t *edge_coord);
+/* candidates in rank order (K each); tree = FVS index of the root */
+int mcbh_get_candidates(const mcbh_problem *p, int32_t *root, int32_t *edge_offset, int32_t *weight,
+                        int32_t *tree);
+/* offsets (K+1) into coords (cycle_nnz); each list sorted ascending */
+int mcbh_get_cycle_lists(const mcbh_problem *p, int64_t *offsets, int32_t *coords);
+/* parent_edge[t*n' + v] = edge offset (parent -> v) in tree t, -1 at the root */
+int mcbh_get_tree_parents(const mcbh_problem *p, int32_t *parent_edge);
+/* reference GPU layout (include/Dijkstra.h:151-203), tree-major:
+ *   level_offsets F x (n'+1), parent_pos F x n', edge_offset F x n', nodes_index F x n' */
+int mcbh_get_ref_layout(const mcbh_problem *p, uint32_t *level_offsets, uint32_t *parent_pos,
+                        int32_t *edge_offset, uint32_t *nodes_index);
+
+/* ---- seeded synthetic inputs (splitmix64) ---------------------------------- */
+/* r x c grid, row-major ids, right then down edge per vertex; weights U[wlo,whi].
+ * Returns the number of edges written (call with u == NULL to size). */
+int64_t mcbh_gen_grid(int32_t r, int32_t c, int32_t wlo, int32_t whi, uint64_t seed,
+                      int32_t *u, int32_t *v, int32_t *w);
+/* connected random sparse graph: random spanning tree (random-permutation attach)
+ * plus uniform extra edges (no loops, no duplicates) up to m edges. */
+int64_t mcbh_gen_random(int32_t n, int64_t m, int32_t wlo, int32_t whi, uint64_t seed,
+                        int32_t *u, int32_t *v, int32_t *w);
+/* random geometric graph: n points in the unit square, k nearest neighbours,
+ * symmetrised, weight round(1000*length) (>= 1), plus the shortest bridging edges
+ * needed to connect the components (in order of component discovery). */
+int64_t mcbh_gen_rgg(int32_t n, int32_t k, uint64_t seed, int32_t *u, int32_t *v, int32_t *w);
+int mcbh_write_mtx(const char *path, int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
+                   const int32_t *w);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,11 @@
+"""minimumcyclebasis_gb300 — the de Pina minimum-cycle-basis hot path on GB300 (sm_103a).
+
+Host preparation (libmcbhost.so) reproduces the reference driver's reduced graph,
+FVS, coordinate order and candidate rank order; the main loop runs on the GPU
+(libmcbgpu.so) behind the C ABI in include/mcbgpu.h.
+"""
+from .host import Graph, Problem, grid_graph, random_graph, rgg_graph  # noqa: F401
+from .gpu import GpuStruct, Solver, device_info, solve  # noqa: F401
+
+__all__ = ["Graph", "Problem", "grid_graph", "random_graph", "rgg_graph", "GpuStruct", "Solver",
+           "device_info", "solve"]

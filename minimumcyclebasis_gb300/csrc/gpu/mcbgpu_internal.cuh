@@ -1,0 +1,121 @@
+// Shared helpers of libmcbgpu.so: error plumbing, the 1-D TMA bulk copy into
+// shared memory with a bounded mbarrier wait, and device status bits.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "mcbgpu.h"
+
+namespace mcbgpu {
+
+// Device status word bits (written by kernels, read by the host after a run).
+enum : unsigned {
+    ST_WAIT_TIMEOUT = 1u << 0,     // a bounded spin on a flag or mbarrier gave up
+    ST_NO_CANDIDATE = 1u << 1,     // the search found no odd candidate
+    ST_RANK_DEFICIT = 1u << 2,     // blocked search ran out of candidates before b pivots
+    ST_BAD_INPUT = 1u << 3,        // an index outside its array was seen and skipped
+};
+
+void set_error(const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define MCB_CUDA(call)                                              \
+    do {                                                            \
+        cudaError_t _e = (call);                                    \
+        if (_e != cudaSuccess) return ::mcbgpu::cuda_fail(_e, #call); \
+    } while (0)
+
+// ---- PTX wrappers -----------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// 1-D bulk copy global -> shared (TMA engine), completion counted on `bar`.
+// dst, src and bytes must be multiples of 16.
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: returns false (and the caller must flag an error) after `limit`
+// polls.  try_wait itself suspends for a hardware-chosen interval per poll.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; i++)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int parity64(uint64_t x) { return __popcll(x) & 1; }
+
+// Stage `words_even` u64 words of global memory (16-byte aligned, an even count)
+// into shared memory with TMA bulk copies of at most 32 KB each.  Called once per
+// kernel by the whole CTA (mbarrier phase 0); every thread waits on the mbarrier
+// with a bounded poll.  Returns false in every thread if the wait timed out; in that
+// case thread 0 has waited a second bounded interval for the copies in flight.
+__device__ __forceinline__ bool stage_words_tma(uint64_t *dst_smem, const uint64_t *src, uint32_t words_even,
+                                               uint64_t *bar) {
+    const uint32_t bytes = words_even * 8u;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+        fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(bar, bytes);
+        const uint32_t CH = 32768;
+        for (uint32_t off = 0; off < bytes; off += CH) {
+            uint32_t n = bytes - off < CH ? bytes - off : CH;
+            tma_load_1d((char *)dst_smem + off, (const char *)src + off, n, bar);
+        }
+    }
+    bool ok = mbar_wait_bounded(bar, 0, 1u << 22);
+    if (!ok && threadIdx.x == 0) mbar_wait_bounded(bar, 0, 1u << 22);
+    return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+}  // namespace mcbgpu

@@ -1,0 +1,973 @@
+// Device-resident de Pina main loop (mcb/mcb_cycle_deg_two_remove.cpp:317-398).
+//
+// Data in HBM:
+//   S       N rows x P words (P = ceil(N/64) rounded up to 4 words, 32-byte rows);
+//           row j is the support vector S_j, which only ever has bits in [0, j]
+//           (it starts as e_j and only earlier S_i are XORed into it).
+//   cands   weight[K], off[K+1] (int64), coords[nnz] (int32, sorted ascending per
+//           candidate) in the reference's rank order.  <C_r, S> = parity of S over
+//           the coordinates of candidate r, which equals the reference's label test
+//           S[e(u,v)] ^ P_t[u] ^ P_t[v] (include/cycles.h:144-195 builds the same set).
+//
+// Per-iteration form (select / cycle_vector / update):
+//   search_kernel   S_e's prefix [0, e] is staged into shared memory by a TMA bulk
+//                   copy; persistent CTAs take 1024-candidate tiles in rank order,
+//                   compute each candidate's parity, and the first odd rank is found
+//                   with a ballot per warp and an atomicMin across CTAs.  CTAs stop
+//                   once their next tile starts above the best rank found.
+//   update_kernel   one warp per row j > e: <C_e, S_j> by gathering S_j at C_e's
+//                   coordinates, then S_j ^= S_e over the words of [0, e].
+//
+// Blocked form (64 iterations per pass; GF(2) arithmetic, so exact):
+//   T[c] (64-bit) = bits S^0_{e0+k}[c], k < 64  — transpose of the block's rows
+//   W_r = XOR of T over C_r's coordinates = <C_r, S^0_{e0+k}> for all 64 k at once
+//   The candidate chosen at iteration e0+k is always one whose W_r is independent
+//   of every earlier candidate's W (a "pivot"): if all earlier W's are even for the
+//   current mask, so is anything in their span.  So one rank-ordered sweep finds the
+//   first 64 pivots, the 64 iterations are then resolved on 64-bit masks, and every
+//   later row S_j receives the block's combined update in one pass.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "mcbgpu_internal.cuh"
+
+using namespace mcbgpu;
+
+namespace {
+
+constexpr int kTile = 1024;           // candidates per tile
+constexpr int kScanThreads = 256;     // 4 candidates per thread
+constexpr int kPer = kTile / kScanThreads;
+constexpr unsigned kSpinLimit = 1u << 24;
+constexpr unsigned long long kNone = 0xFFFFFFFFFFFFFFFFull;
+
+struct IterSlot {            // state of one per-iteration search
+    unsigned long long best; // first odd rank (kNone until found)
+    unsigned next_tile;
+    unsigned pad;
+};
+
+struct BlockState {
+    unsigned next_tile, frontier, rank, stop, epoch, b, npairs, pad;
+    unsigned long long total;      // running 64-bit total weight of the basis
+    unsigned long long basis[64];  // reduced row-echelon basis of the pivot W's
+    unsigned pivbit[64];
+    long long pivrank[64];
+    unsigned long long pivW[64];   // the pivots' W as found (not reduced)
+    unsigned long long mask[64];   // final S_{e0+k} as a combination of S^0_{e0+l}
+    unsigned long long gcol[64];   // gcol[k] bit i = <C_sel_k, S_{e0+i}>, i < k
+    int sel[64];                   // pivot chosen at iteration e0+k
+};
+
+// ---------------------------------------------------------------------------
+__global__ void init_identity_kernel(uint64_t *S, int N, int P) {
+    size_t total = (size_t)N * P;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        int j = (int)(i / P), w = (int)(i % P);
+        S[i] = (w == (j >> 6)) ? (1ull << (j & 63)) : 0ull;
+    }
+}
+
+__global__ void reset_state_kernel(IterSlot *slots, BlockState *bs, unsigned *status) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        slots[0].best = kNone;
+        slots[0].next_tile = 0;
+        slots[1].best = kNone;
+        slots[1].next_tile = 0;
+        bs->total = 0;  // epoch keeps counting across runs: old tile marks never match
+        *status = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-iteration search for the first candidate with <C_r, S_e> = 1.
+__global__ void __launch_bounds__(kScanThreads) search_kernel(const uint64_t *__restrict__ Se, int e,
+                                                              int words_even, const int64_t *__restrict__ off,
+                                                              const int32_t *__restrict__ coords, long long K,
+                                                              IterSlot *slot, unsigned *status) {
+    extern __shared__ __align__(16) uint64_t s_S[];
+    __shared__ uint64_t bar;
+    __shared__ unsigned s_tile, s_go;
+    __shared__ unsigned long long s_best;
+    if (!stage_words_tma(s_S, Se, (uint32_t)words_even, &bar)) {
+        if (threadIdx.x == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+        return;
+    }
+    const long long ntiles = (K + kTile - 1) / kTile;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned t = atomicAdd(&slot->next_tile, 1u);
+            // stop when out of tiles or when an earlier tile already found an odd one
+            const unsigned long long gb = *((volatile unsigned long long *)&slot->best);
+            s_tile = t;
+            s_go = ((long long)t < ntiles && (unsigned long long)((long long)t * kTile) <= gb) ? 1u : 0u;
+            s_best = kNone;
+        }
+        __syncthreads();
+        if (!s_go) break;
+        const long long tile = s_tile;
+        const long long r0 = tile * kTile;
+        unsigned long long mine = kNone;
+        for (int q = 0; q < kPer; q++) {
+            long long r = r0 + q * kScanThreads + threadIdx.x;
+            if (r >= K) break;
+            int64_t b = off[r], en = off[r + 1];
+            unsigned par = 0;
+            for (int64_t i = b; i < en; i++) {
+                int c = __ldg(coords + i);
+                if (c > e) break;
+                par ^= (unsigned)(s_S[c >> 6] >> (c & 63)) & 1u;
+            }
+            if (par) {
+                mine = (unsigned long long)r;
+                break;  // later q only give larger ranks
+            }
+        }
+        // warp-level min of odd ranks, then CTA-level
+        unsigned long long wmin = mine;
+        for (int d = 16; d > 0; d >>= 1) {
+            unsigned long long o = __shfl_xor_sync(0xffffffffu, wmin, d);
+            wmin = o < wmin ? o : wmin;
+        }
+        if ((threadIdx.x & 31) == 0 && wmin != kNone) atomicMin(&s_best, wmin);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_best != kNone) atomicMin(&slot->best, s_best);
+        __syncthreads();
+    }
+}
+
+// One warp per row j in (e, N): if <C_e, S_j> is odd, S_j ^= S_e (words [0, e/64]).
+// Block 0 also records the selection and resets the next iteration's slot.
+__global__ void update_kernel(uint64_t *S, int N, int P, int e, const int64_t *__restrict__ off,
+                              const int32_t *__restrict__ coords, const int32_t *__restrict__ weight,
+                              IterSlot *slot, IterSlot *next_slot, long long *selected,
+                              BlockState *bs, unsigned *status) {
+    const unsigned long long r = *((volatile unsigned long long *)&slot->best);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        next_slot->best = kNone;
+        next_slot->next_tile = 0;
+        if (r == kNone) {
+            atomicOr(status, ST_NO_CANDIDATE);
+            selected[e] = -1;
+        } else {
+            selected[e] = (long long)r;
+            bs->total += (unsigned long long)(long long)weight[r];
+        }
+    }
+    if (r == kNone) return;
+    const int64_t b = off[r], len = off[r + 1] - b;
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int we = (e >> 6) + 1;
+    const uint64_t *Se = S + (size_t)e * P;
+    for (int j = e + 1 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); j < N; j += warps) {
+        uint64_t *Sj = S + (size_t)j * P;
+        unsigned par = 0;
+        for (int64_t i = lane; i < len; i += 32) {
+            int c = coords[b + i];
+            par ^= (unsigned)(Sj[c >> 6] >> (c & 63)) & 1u;
+        }
+        par = __reduce_xor_sync(0xffffffffu, par);
+        if (par)
+            for (int w = lane; w < we; w += 32) Sj[w] ^= Se[w];
+    }
+}
+
+// C_e of the selected candidate as a bit vector (include/cycles.h:144-195).
+__global__ void cycle_vector_kernel(uint64_t *C, int W, const int64_t *__restrict__ off,
+                                    const int32_t *__restrict__ coords, const IterSlot *slot) {
+    const unsigned long long r = slot->best;
+    for (int w = threadIdx.x; w < W; w += blockDim.x) C[w] = 0;
+    __syncthreads();
+    if (r == kNone) return;
+    for (int64_t i = off[r] + threadIdx.x; i < off[r + 1]; i += blockDim.x) {
+        int c = coords[i];
+        atomicOr((unsigned long long *)&C[c >> 6], 1ull << (c & 63));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Blocked form.
+//
+// blk_transpose_kernel: T[64w + i] bit k = S[e0+k] bit (64w+i), for w < Wb.
+// One warp per word column; also resets the block state (runs first in the block).
+__global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int e0, int b, int Wb,
+                                     uint64_t *__restrict__ T, BlockState *bs) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        bs->next_tile = 0;
+        bs->frontier = 0;
+        bs->rank = 0;
+        bs->stop = 0;
+        bs->epoch = bs->epoch + 1;
+        bs->b = (unsigned)b;
+        bs->npairs = 0;
+    }
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < Wb; w += warps) {
+        uint64_t lo = lane < b ? S[(size_t)(e0 + lane) * P + w] : 0ull;
+        uint64_t hi = (32 + lane) < b ? S[(size_t)(e0 + 32 + lane) * P + w] : 0ull;
+        uint64_t a = 0, c = 0;
+        for (int i = 0; i < 64; i++) {
+            unsigned blo = __ballot_sync(0xffffffffu, (unsigned)(lo >> i) & 1u);
+            unsigned bhi = __ballot_sync(0xffffffffu, (unsigned)(hi >> i) & 1u);
+            uint64_t v = (uint64_t)blo | ((uint64_t)bhi << 32);
+            if (i < 32) {
+                if (lane == i) a = v;
+            } else {
+                if (lane == i - 32) c = v;
+            }
+        }
+        T[(size_t)w * 64 + lane] = a;
+        T[(size_t)w * 64 + 32 + lane] = c;
+    }
+}
+
+// Reduce W by the basis held as Four-Russians tables: tab[g][pat] = XOR of the basis
+// vectors whose pivot bits form `pat` within byte g (0 for non-pivot bits).
+__device__ __forceinline__ uint64_t fr_reduce(uint64_t W, const uint64_t (*tab)[256]) {
+    uint64_t r = W;
+#pragma unroll
+    for (int g = 0; g < 8; g++) r ^= tab[g][(W >> (8 * g)) & 255];
+    return r;
+}
+
+// Build tab from the basis held in shared memory (rank vectors, pivot bits).
+__device__ void fr_build(uint64_t (*tab)[256], const uint64_t *basis, const unsigned *pivbit, unsigned rank) {
+    __shared__ uint64_t byBit[64];
+    if (threadIdx.x < 64) byBit[threadIdx.x] = 0;
+    __syncthreads();
+    for (unsigned q = threadIdx.x; q < rank; q += blockDim.x) byBit[pivbit[q]] = basis[q];
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 8 * 256; idx += blockDim.x) {
+        int g = idx >> 8, pat = idx & 255;
+        uint64_t v = 0;
+        for (int i = 0; i < 8; i++)
+            if (pat & (1 << i)) v ^= byBit[8 * g + i];
+        tab[g][pat] = v;
+    }
+    __syncthreads();
+}
+
+// The pivot sweep.  Candidates are taken in tiles of 1024, in rank order, by a
+// persistent grid.  A tile's W's are reduced against the latest basis the CTA has
+// seen; if all reduce to zero the tile holds no pivot (its W's are in the span of
+// pivots of earlier ranks) and it is marked EMPTY at once.  Otherwise the CTA waits
+// until every earlier tile is EMPTY or RESOLVED (the frontier), re-reduces against
+// the then-final basis and extracts its pivots in rank order, publishes the basis,
+// and marks the tile RESOLVED.  The sweep stops once the basis has rank b.
+__global__ void __launch_bounds__(kScanThreads) blk_scan_kernel(
+    const uint64_t *__restrict__ T, int bound, const int64_t *__restrict__ off,
+    const int32_t *__restrict__ coords, long long K, BlockState *bs, unsigned *tstatus, unsigned *status) {
+    __shared__ uint64_t tab[8][256];
+    __shared__ uint64_t sW[kTile];
+    __shared__ uint64_t sR[kTile];
+    __shared__ uint64_t sbasis[64];
+    __shared__ unsigned spiv[64];
+    __shared__ unsigned s_tile, s_stop, s_rank, s_min, s_fail;
+    const unsigned epoch = *((volatile unsigned *)&bs->epoch);
+    const unsigned b = *((volatile unsigned *)&bs->b);
+    const long long ntiles = (K + kTile - 1) / kTile;
+    unsigned snap = 0xFFFFFFFFu;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_stop = ld_acquire_u32(&bs->stop);
+            s_tile = s_stop ? 0u : atomicAdd(&bs->next_tile, 1u);
+            s_rank = ld_acquire_u32(&bs->rank);
+        }
+        __syncthreads();
+        if (s_stop) break;
+        const unsigned tile = s_tile;
+        if ((long long)tile >= ntiles) break;  // nobody waits on tiles past the end
+        // refresh the snapshot of the basis when it grew
+        if (s_rank != snap) {
+            unsigned rk = s_rank;
+            for (unsigned q = threadIdx.x; q < rk; q += blockDim.x) {
+                sbasis[q] = __ldcg(&bs->basis[q]);
+                spiv[q] = __ldcg(&bs->pivbit[q]);
+            }
+            __syncthreads();
+            fr_build(tab, sbasis, spiv, rk);
+            snap = rk;
+        }
+        const long long r0 = (long long)tile * kTile;
+        int any = 0;
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+            const int li = q * kScanThreads + threadIdx.x;
+            const long long r = r0 + li;
+            uint64_t W = 0;
+            if (r < K) {
+                const int64_t e1 = off[r + 1];
+                for (int64_t i = off[r]; i < e1; i++) {
+                    int c = __ldg(coords + i);
+                    if (c >= bound) break;
+                    W ^= __ldg(T + c);
+                }
+            }
+            sW[li] = W;
+            uint64_t R = fr_reduce(W, tab);
+            sR[li] = R;
+            any |= (R != 0);
+        }
+        if (!__syncthreads_or(any)) {
+            if (threadIdx.x == 0) st_release_u32(&tstatus[tile], (epoch << 2) | 1u);
+            continue;
+        }
+        // wait until all earlier tiles are done
+        if (threadIdx.x == 0) {
+            s_fail = 0;
+            unsigned f = ld_acquire_u32(&bs->frontier);
+            unsigned spins = 0;
+            while (f < tile) {
+                unsigned st = ld_acquire_u32(&tstatus[f]);
+                if ((st >> 2) == epoch && (st & 3u)) {
+                    f++;
+                    continue;
+                }
+                if (++spins > kSpinLimit) {
+                    s_fail = 1;
+                    break;
+                }
+                __nanosleep(64);
+            }
+            if (!s_fail) {
+                __threadfence();
+                atomicMax(&bs->frontier, f);
+                s_rank = ld_acquire_u32(&bs->rank);
+            }
+        }
+        __syncthreads();
+        if (s_fail) {
+            if (threadIdx.x == 0) {
+                atomicOr(status, ST_WAIT_TIMEOUT);
+                st_release_u32(&bs->stop, 1u);
+                st_release_u32(&tstatus[tile], (epoch << 2) | 2u);
+            }
+            break;
+        }
+        // the basis is now stable: reload it, re-reduce, extract pivots in order
+        unsigned rk = s_rank;
+        for (unsigned q = threadIdx.x; q < rk; q += blockDim.x) {
+            sbasis[q] = __ldcg(&bs->basis[q]);
+            spiv[q] = __ldcg(&bs->pivbit[q]);
+        }
+        __syncthreads();
+        fr_build(tab, sbasis, spiv, rk);
+        for (int q = 0; q < kPer; q++) {
+            const int li = q * kScanThreads + threadIdx.x;
+            sR[li] = fr_reduce(sW[li], tab);
+        }
+        __syncthreads();
+        const unsigned rk0 = rk;
+        while (rk < b) {
+            if (threadIdx.x == 0) s_min = 0xFFFFFFFFu;
+            __syncthreads();
+            for (int q = 0; q < kPer; q++) {
+                const int li = q * kScanThreads + threadIdx.x;
+                unsigned bal = __ballot_sync(0xffffffffu, sR[li] != 0);
+                if (bal) {
+                    if ((threadIdx.x & 31) == 0) atomicMin(&s_min, (unsigned)(q * kScanThreads + (threadIdx.x & ~31) + __ffs(bal) - 1));
+                    break;
+                }
+            }
+            __syncthreads();
+            const unsigned mi = s_min;
+            if (mi == 0xFFFFFFFFu) break;
+            const uint64_t v = sR[mi];
+            const unsigned p = (unsigned)(__ffsll((long long)v) - 1);
+            __syncthreads();
+            // keep the basis reduced: clear bit p from the other vectors
+            for (unsigned q = threadIdx.x; q < rk; q += blockDim.x)
+                if ((sbasis[q] >> p) & 1ull) sbasis[q] ^= v;
+            if (threadIdx.x == 0) {
+                sbasis[rk] = v;
+                spiv[rk] = p;
+                bs->pivrank[rk] = r0 + mi;
+                bs->pivW[rk] = sW[mi];
+            }
+            for (int q = 0; q < kPer; q++) {
+                const int li = q * kScanThreads + threadIdx.x;
+                if ((sR[li] >> p) & 1ull) sR[li] ^= v;
+            }
+            rk++;
+            __syncthreads();
+        }
+        // publish
+        for (unsigned q = threadIdx.x; q < rk; q += blockDim.x) {
+            bs->basis[q] = sbasis[q];
+            bs->pivbit[q] = spiv[q];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (rk != rk0) st_release_u32(&bs->rank, rk);
+            if (rk >= b) st_release_u32(&bs->stop, 1u);
+            st_release_u32(&tstatus[tile], (epoch << 2) | 2u);
+        }
+        snap = 0xFFFFFFFFu;  // the reduced vectors changed: rebuild next time
+        __syncthreads();
+    }
+}
+
+// Resolve the block's b iterations on masks (one warp).  Pivot index = rank order.
+// m_k starts as e_k; iteration k takes the first pivot p with <W_p, m_k> odd; every
+// later m_j with <W_p, m_j> odd gets m_j ^= m_k (the reference's update restricted
+// to the block, mcb/mcb_cycle_deg_two_remove.cpp:371-390).
+__global__ void blk_resolve_kernel(BlockState *bs, int e0, const int64_t *__restrict__ off,
+                                   const int32_t *__restrict__ coords, const int32_t *__restrict__ weight,
+                                   long long *selected, unsigned *pairs, unsigned pair_cap, unsigned *status) {
+    const int lane = threadIdx.x;
+    const int b = (int)bs->b;
+    const unsigned rank = bs->rank;
+    if (rank < (unsigned)b) {
+        if (lane == 0) atomicOr(status, ST_RANK_DEFICIT);
+        return;
+    }
+    uint64_t w0 = bs->pivW[lane], w1 = bs->pivW[32 + lane];
+    if (lane >= b) w0 = 0;
+    if (32 + lane >= b) w1 = 0;
+    uint64_t m0 = 1ull << lane, m1 = 1ull << (32 + lane);
+    bool used0 = lane >= b, used1 = 32 + lane >= b;
+    __shared__ int s_sel[64];
+    __shared__ uint64_t s_g[64];
+    for (int k = 0; k < b; k++) {
+        const uint64_t mk = __shfl_sync(0xffffffffu, k < 32 ? m0 : m1, k & 31);
+        const unsigned o0 = __ballot_sync(0xffffffffu, !used0 && parity64(w0 & mk));
+        const unsigned o1 = __ballot_sync(0xffffffffu, !used1 && parity64(w1 & mk));
+        int p;
+        if (o0)
+            p = __ffs(o0) - 1;
+        else if (o1)
+            p = 32 + __ffs(o1) - 1;
+        else {
+            if (lane == 0) atomicOr(status, ST_NO_CANDIDATE);
+            return;
+        }
+        if (p < 32 && lane == p) used0 = true;
+        if (p >= 32 && lane == p - 32) used1 = true;
+        const uint64_t wp = __shfl_sync(0xffffffffu, p < 32 ? w0 : w1, p & 31);
+        // gcol[k] bit i = <W_p, m_i> for i < k (rows i are final)
+        const unsigned g0 = __ballot_sync(0xffffffffu, lane < k && parity64(wp & m0));
+        const unsigned g1 = __ballot_sync(0xffffffffu, 32 + lane < k && parity64(wp & m1));
+        if (lane == 0) {
+            s_sel[k] = p;
+            s_g[k] = (uint64_t)g0 | ((uint64_t)g1 << 32);
+        }
+        if (lane > k && parity64(wp & m0)) m0 ^= mk;
+        if (32 + lane > k && parity64(wp & m1)) m1 ^= mk;
+    }
+    __syncwarp();
+    bs->mask[lane] = m0;
+    bs->mask[32 + lane] = m1;
+    // selections, weights, and the (coordinate, k) pairs of the chosen cycles
+    unsigned long long wsum = 0;
+    unsigned base = 0;
+    for (int k0 = 0; k0 < b; k0 += 32) {
+        const int k = k0 + lane;
+        long long r = -1;
+        unsigned len = 0;
+        if (k < b) {
+            r = bs->pivrank[s_sel[k]];
+            selected[e0 + k] = r;
+            bs->sel[k] = s_sel[k];
+            bs->gcol[k] = s_g[k];
+            wsum += (unsigned long long)(long long)weight[r];
+            len = (unsigned)(off[r + 1] - off[r]);
+        }
+        unsigned incl = len;
+        for (int d = 1; d < 32; d <<= 1) {
+            unsigned t = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += t;
+        }
+        const unsigned start = base + incl - len;
+        if (k < b) {
+            if (start + len > pair_cap) {
+                atomicOr(status, ST_BAD_INPUT);
+            } else {
+                for (unsigned i = 0; i < len; i++) pairs[start + i] = ((unsigned)coords[off[r] + i] << 6) | (unsigned)k;
+            }
+        }
+        base += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    for (int d = 16; d > 0; d >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, d);
+    if (lane == 0) {
+        bs->npairs = base < pair_cap ? base : pair_cap;
+        bs->total += wsum;
+    }
+}
+
+// S_{e0+k} := XOR of S^0_{e0+l} over l in mask[k], in place, words [0, Wb).
+// Each CTA owns 32 word columns and keeps the original rows in shared memory.
+__global__ void blk_materialize_kernel(uint64_t *S, int P, int e0, int Wb, const BlockState *bs) {
+    __shared__ uint64_t s0[64][33];
+    __shared__ uint64_t sm[64];
+    const int b = (int)bs->b;
+    const int w0 = blockIdx.x * 32;
+    if (threadIdx.x < 64) sm[threadIdx.x] = threadIdx.x < b ? bs->mask[threadIdx.x] : 0;
+    for (int idx = threadIdx.x; idx < 64 * 32; idx += blockDim.x) {
+        int l = idx >> 5, w = idx & 31;
+        s0[l][w] = (l < b && w0 + w < Wb) ? S[(size_t)(e0 + l) * P + w0 + w] : 0ull;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 64 * 32; idx += blockDim.x) {
+        int k = idx >> 5, w = idx & 31;
+        if (k >= b || w0 + w >= Wb) continue;
+        uint64_t m = sm[k], acc = 0;
+        while (m) {
+            int l = __ffsll((long long)m) - 1;
+            m &= m - 1;
+            acc ^= s0[l][w];
+        }
+        S[(size_t)(e0 + k) * P + w0 + w] = acc;
+    }
+}
+
+// tab[g][pat][w] = XOR of the final rows S_{e0+8g+i} for bits i of pat, w < Wb.
+__global__ void blk_tables_kernel(const uint64_t *__restrict__ S, int P, int e0, int b, int Wb, int Pt,
+                                  uint64_t *__restrict__ tab) {
+    const int total = 8 * Wb;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int g = idx / Wb, w = idx % Wb;
+        uint64_t v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = (8 * g + i < b) ? S[(size_t)(e0 + 8 * g + i) * P + w] : 0ull;
+        uint64_t *out = tab + (size_t)g * 256 * Pt + w;
+        uint64_t cur = 0;
+        out[0] = 0;
+        // Gray-code order: one XOR per entry
+        for (int i = 1; i < 256; i++) {
+            int flip = __ffs(i) - 1;
+            cur ^= v[flip];
+            int gray = i ^ (i >> 1);
+            out[(size_t)gray * Pt] = cur;
+        }
+    }
+}
+
+// One warp per row j >= e0+b: D_j (64 bits) = <C_sel_k, S_j>, then
+// beta_k = D_k ^ <beta_{<k}, gcol_k> (the sequential effect of the block's updates),
+// then S_j ^= XOR_k beta_k S_{e0+k} through the tables.
+__global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int Pt,
+                                  const uint64_t *__restrict__ tab, const BlockState *bs,
+                                  const unsigned *__restrict__ pairs) {
+    __shared__ uint64_t sg[64];
+    const int b = (int)bs->b;
+    const unsigned np = bs->npairs;
+    if (threadIdx.x < 64) sg[threadIdx.x] = threadIdx.x < b ? bs->gcol[threadIdx.x] : 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int j = e0 + b + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); j < N; j += warps) {
+        uint64_t *Sj = S + (size_t)j * P;
+        uint64_t D = 0;
+        for (unsigned i = lane; i < np; i += 32) {
+            unsigned pr = pairs[i];
+            unsigned c = pr >> 6, k = pr & 63u;
+            D ^= ((Sj[c >> 6] >> (c & 63)) & 1ull) << k;
+        }
+        for (int d = 16; d > 0; d >>= 1) D ^= __shfl_xor_sync(0xffffffffu, D, d);
+        uint64_t beta = 0;
+        for (int k = 0; k < b; k++) {
+            uint64_t bk = ((D >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]);
+            beta |= bk << k;
+        }
+        if (!beta) continue;
+        const uint64_t *t0 = tab + ((size_t)0 * 256 + ((beta >> 0) & 255)) * Pt;
+        const uint64_t *t1 = tab + ((size_t)1 * 256 + ((beta >> 8) & 255)) * Pt;
+        const uint64_t *t2 = tab + ((size_t)2 * 256 + ((beta >> 16) & 255)) * Pt;
+        const uint64_t *t3 = tab + ((size_t)3 * 256 + ((beta >> 24) & 255)) * Pt;
+        const uint64_t *t4 = tab + ((size_t)4 * 256 + ((beta >> 32) & 255)) * Pt;
+        const uint64_t *t5 = tab + ((size_t)5 * 256 + ((beta >> 40) & 255)) * Pt;
+        const uint64_t *t6 = tab + ((size_t)6 * 256 + ((beta >> 48) & 255)) * Pt;
+        const uint64_t *t7 = tab + ((size_t)7 * 256 + ((beta >> 56) & 255)) * Pt;
+        for (int w = lane; w < Wb; w += 32)
+            Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+struct mcbgpu_solver {
+    int N = 0, W = 0, P = 0, words_cap = 0;
+    long long K = 0, nnz = 0;
+    int max_len = 0;
+    int sm_count = 0;
+    int32_t *d_weight = nullptr;
+    int64_t *d_off = nullptr;
+    int32_t *d_coords = nullptr;
+    uint64_t *d_S = nullptr;
+    uint64_t *d_C = nullptr;       // cycle vector buffer (W words)
+    uint64_t *d_T = nullptr;       // 64 * P words
+    uint64_t *d_tab = nullptr;     // 8 * 256 * P words
+    unsigned *d_tstatus = nullptr; // tiles + 1
+    unsigned *d_pairs = nullptr;
+    unsigned pair_cap = 0;
+    IterSlot *d_slots = nullptr;   // 2
+    BlockState *d_bs = nullptr;
+    long long *d_selected = nullptr;
+    unsigned *d_status = nullptr;
+    bool uploaded = false;
+    long long iters_run = 0;
+    long long launches = 0;
+    long long device_bytes = 0;
+};
+
+namespace {
+
+void free_solver(mcbgpu_solver *s) {
+    if (!s) return;
+    cudaFree(s->d_weight);
+    cudaFree(s->d_off);
+    cudaFree(s->d_coords);
+    cudaFree(s->d_S);
+    cudaFree(s->d_C);
+    cudaFree(s->d_T);
+    cudaFree(s->d_tab);
+    cudaFree(s->d_tstatus);
+    cudaFree(s->d_pairs);
+    cudaFree(s->d_slots);
+    cudaFree(s->d_bs);
+    cudaFree(s->d_selected);
+    cudaFree(s->d_status);
+    delete s;
+}
+
+int check_status(mcbgpu_solver *s, cudaStream_t st) {
+    unsigned v = 0;
+    MCB_CUDA(cudaMemcpyAsync(&v, s->d_status, sizeof v, cudaMemcpyDeviceToHost, st));
+    MCB_CUDA(cudaStreamSynchronize(st));
+    if (v & (ST_NO_CANDIDATE | ST_RANK_DEFICIT)) {
+        set_error("no odd candidate for some support vector (status 0x%x)", v);
+        return MCBGPU_E_NO_CANDIDATE;
+    }
+    if (v) {
+        set_error("device status 0x%x", v);
+        return MCBGPU_E_DEVICE;
+    }
+    return MCBGPU_OK;
+}
+
+int search_smem_words(const mcbgpu_solver *s, int e) {
+    int we = (e >> 6) + 1;
+    return (we + 1) & ~1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz) {
+    if (!out || N < 0 || K < 0 || nnz < 0 || N >= (1 << 26)) {
+        set_error("mcbgpu_solver_create: invalid sizes (N must be < 2^26)");
+        return MCBGPU_E_ARG;
+    }
+    *out = nullptr;
+    mcbgpu_solver *s = new mcbgpu_solver();
+    s->N = N;
+    s->K = K;
+    s->nnz = nnz;
+    s->W = (N + 63) / 64;
+    s->P = ((s->W + 3) / 4) * 4;
+    if (s->P == 0) s->P = 4;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    const size_t ntiles = (size_t)((K + kTile - 1) / kTile) + 2;
+    long long bytes = 0;
+#define ALLOC(ptr, sz)                                                         \
+    do {                                                                       \
+        size_t _b = (size_t)(sz);                                              \
+        if (_b < 16) _b = 16;                                                  \
+        if (e == cudaSuccess) e = cudaMalloc((void **)&(ptr), _b);             \
+        bytes += (long long)_b;                                                \
+    } while (0)
+    ALLOC(s->d_weight, sizeof(int32_t) * (size_t)K);
+    ALLOC(s->d_off, sizeof(int64_t) * (size_t)(K + 1));
+    ALLOC(s->d_coords, sizeof(int32_t) * (size_t)nnz);
+    ALLOC(s->d_S, sizeof(uint64_t) * (size_t)N * s->P);
+    ALLOC(s->d_C, sizeof(uint64_t) * (size_t)s->P);
+    ALLOC(s->d_T, sizeof(uint64_t) * 64 * (size_t)s->P);
+    ALLOC(s->d_tab, sizeof(uint64_t) * 8 * 256 * (size_t)s->P);
+    ALLOC(s->d_tstatus, sizeof(unsigned) * ntiles);
+    ALLOC(s->d_slots, sizeof(IterSlot) * 2);
+    ALLOC(s->d_bs, sizeof(BlockState));
+    ALLOC(s->d_selected, sizeof(long long) * (size_t)(N > 0 ? N : 1));
+    ALLOC(s->d_status, sizeof(unsigned));
+#undef ALLOC
+    if (e == cudaSuccess) e = cudaMemset(s->d_tstatus, 0, sizeof(unsigned) * ntiles);
+    if (e == cudaSuccess) e = cudaMemset(s->d_bs, 0, sizeof(BlockState));
+    if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(unsigned));
+    if (e != cudaSuccess) {
+        free_solver(s);
+        return cuda_fail(e, "mcbgpu_solver_create");
+    }
+    s->device_bytes = bytes;
+    *out = s;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream) {
+    if (!s) {
+        set_error("mcbgpu_solver_reset: NULL handle");
+        return MCBGPU_E_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->N > 0) {
+        int grid = s->sm_count > 0 ? s->sm_count * 4 : 256;
+        init_identity_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P);
+        MCB_CUDA(cudaGetLastError());
+        s->launches++;
+    }
+    reset_state_kernel<<<1, 32, 0, st>>>(s->d_slots, s->d_bs, s->d_status);
+    MCB_CUDA(cudaGetLastError());
+    s->launches++;
+    s->iters_run = 0;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t *offsets, const int32_t *coords,
+                         void *stream) {
+    if (!s || (s->K > 0 && (!weight || !offsets)) || (s->nnz > 0 && !coords)) {
+        set_error("mcbgpu_solver_upload: NULL argument");
+        return MCBGPU_E_ARG;
+    }
+    // validate on the host so the kernels index in bounds by construction
+    if (s->K > 0) {
+        if (offsets[0] != 0 || offsets[s->K] != s->nnz) {
+            set_error("mcbgpu_solver_upload: offsets must start at 0 and end at nnz");
+            return MCBGPU_E_ARG;
+        }
+        int max_len = 0;
+        for (long long r = 0; r < s->K; r++) {
+            int64_t b = offsets[r], e = offsets[r + 1];
+            if (e < b) {
+                set_error("mcbgpu_solver_upload: offsets decrease at candidate %lld", r);
+                return MCBGPU_E_ARG;
+            }
+            if (e - b > max_len) max_len = (int)(e - b);
+            int prev = -1;
+            for (int64_t i = b; i < e; i++) {
+                int c = coords[i];
+                if (c <= prev || c >= s->N) {
+                    set_error("mcbgpu_solver_upload: candidate %lld: coordinates must be ascending in [0, N)", r);
+                    return MCBGPU_E_ARG;
+                }
+                prev = c;
+            }
+        }
+        s->max_len = max_len;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned cap = (unsigned)(64 * (size_t)(s->max_len > 0 ? s->max_len : 1));
+    if (cap > s->pair_cap) {
+        cudaFree(s->d_pairs);
+        s->d_pairs = nullptr;
+        MCB_CUDA(cudaMalloc((void **)&s->d_pairs, sizeof(unsigned) * cap));
+        s->device_bytes += (long long)sizeof(unsigned) * cap;
+        s->pair_cap = cap;
+    }
+    if (s->K > 0) {
+        MCB_CUDA(cudaMemcpyAsync(s->d_weight, weight, sizeof(int32_t) * (size_t)s->K, cudaMemcpyHostToDevice, st));
+        MCB_CUDA(cudaMemcpyAsync(s->d_off, offsets, sizeof(int64_t) * (size_t)(s->K + 1), cudaMemcpyHostToDevice, st));
+    }
+    if (s->nnz > 0)
+        MCB_CUDA(cudaMemcpyAsync(s->d_coords, coords, sizeof(int32_t) * (size_t)s->nnz, cudaMemcpyHostToDevice, st));
+    s->uploaded = true;
+    return mcbgpu_solver_reset(s, stream);
+}
+
+int mcbgpu_select(mcbgpu_solver *s, int32_t e, int64_t *rank, void *stream) {
+    if (!s || e < 0 || e >= s->N) {
+        set_error("mcbgpu_select: invalid iteration");
+        return MCBGPU_E_ARG;
+    }
+    if (!s->uploaded) {
+        set_error("mcbgpu_select: candidates not uploaded");
+        return MCBGPU_E_STATE;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const int we = search_smem_words(s, e);
+    const size_t smem = (size_t)we * 8;
+    if (smem > 200 * 1024) {
+        set_error("mcbgpu_select: support vector prefix too large for shared memory");
+        return MCBGPU_E_ARG;
+    }
+    if (smem > 48 * 1024) MCB_CUDA(cudaFuncSetAttribute(search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the S row pitch is a multiple of 4 words, so reading `we` (even) words is in bounds
+    int grid = s->sm_count > 0 ? s->sm_count * 4 : 256;
+    long long ntiles = (s->K + kTile - 1) / kTile;
+    if (ntiles < grid) grid = (int)(ntiles > 0 ? ntiles : 1);
+    IterSlot *slot = s->d_slots + (e & 1);
+    search_kernel<<<grid, kScanThreads, smem, st>>>(s->d_S + (size_t)e * s->P, e, we, s->d_off, s->d_coords, s->K,
+                                                     slot, s->d_status);
+    MCB_CUDA(cudaGetLastError());
+    s->launches++;
+    if (rank) {
+        unsigned long long r = 0;
+        MCB_CUDA(cudaMemcpyAsync(&r, &slot->best, sizeof r, cudaMemcpyDeviceToHost, st));
+        MCB_CUDA(cudaStreamSynchronize(st));
+        *rank = r == kNone ? -1 : (int64_t)r;
+        if (r == kNone) {
+            set_error("mcbgpu_select: no odd candidate at iteration %d", e);
+            return MCBGPU_E_NO_CANDIDATE;
+        }
+    }
+    return MCBGPU_OK;
+}
+
+int mcbgpu_cycle_vector(mcbgpu_solver *s, int32_t e, uint64_t *words, void *stream) {
+    if (!s || e < 0 || e >= s->N) {
+        set_error("mcbgpu_cycle_vector: invalid iteration");
+        return MCBGPU_E_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    cycle_vector_kernel<<<1, 256, 0, st>>>(s->d_C, s->W, s->d_off, s->d_coords, s->d_slots + (e & 1));
+    MCB_CUDA(cudaGetLastError());
+    s->launches++;
+    if (words) {
+        MCB_CUDA(cudaMemcpyAsync(words, s->d_C, sizeof(uint64_t) * (size_t)s->W, cudaMemcpyDeviceToHost, st));
+        MCB_CUDA(cudaStreamSynchronize(st));
+    }
+    return MCBGPU_OK;
+}
+
+int mcbgpu_update(mcbgpu_solver *s, int32_t e, void *stream) {
+    if (!s || e < 0 || e >= s->N) {
+        set_error("mcbgpu_update: invalid iteration");
+        return MCBGPU_E_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int rows = s->N - e - 1;
+    int grid = (rows + 7) / 8;
+    int cap = s->sm_count > 0 ? s->sm_count * 8 : 1024;
+    if (grid > cap) grid = cap;
+    if (grid < 1) grid = 1;
+    update_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P, e, s->d_off, s->d_coords, s->d_weight,
+                                        s->d_slots + (e & 1), s->d_slots + ((e + 1) & 1), s->d_selected, s->d_bs,
+                                        s->d_status);
+    MCB_CUDA(cudaGetLastError());
+    s->launches++;
+    if (e + 1 > s->iters_run) s->iters_run = e + 1;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_run_plain(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
+    if (!s) {
+        set_error("mcbgpu_solver_run_plain: NULL handle");
+        return MCBGPU_E_ARG;
+    }
+    int64_t iters = (max_iterations >= 0 && max_iterations < s->N) ? max_iterations : s->N;
+    for (int64_t e = 0; e < iters; e++) {
+        int rc = mcbgpu_select(s, (int32_t)e, nullptr, stream);
+        if (rc) return rc;
+        rc = mcbgpu_update(s, (int32_t)e, stream);
+        if (rc) return rc;
+    }
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
+    if (!s) {
+        set_error("mcbgpu_solver_run: NULL handle");
+        return MCBGPU_E_ARG;
+    }
+    if (!s->uploaded) {
+        set_error("mcbgpu_solver_run: candidates not uploaded");
+        return MCBGPU_E_STATE;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t iters = (max_iterations >= 0 && max_iterations < s->N) ? max_iterations : s->N;
+    const int sms = s->sm_count > 0 ? s->sm_count : 148;
+    long long ntiles = (s->K + kTile - 1) / kTile;
+    int scan_grid = sms * 3;
+    if (ntiles + 1 < scan_grid) scan_grid = (int)(ntiles + 1);
+    for (int64_t e0 = 0; e0 < iters; e0 += 64) {
+        const int b = (int)std::min<int64_t>(64, iters - e0);
+        const int Wb = (int)((e0 + b + 63) / 64);
+        {
+            int warps = Wb;
+            int grid = (warps + 7) / 8;
+            blk_transpose_kernel<<<grid, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs);
+        }
+        blk_scan_kernel<<<scan_grid, kScanThreads, 0, st>>>(s->d_T, (int)(e0 + b), s->d_off, s->d_coords, s->K,
+                                                            s->d_bs, s->d_tstatus, s->d_status);
+        blk_resolve_kernel<<<1, 32, 0, st>>>(s->d_bs, (int)e0, s->d_off, s->d_coords, s->d_weight, s->d_selected,
+                                             s->d_pairs, s->pair_cap, s->d_status);
+        blk_materialize_kernel<<<(Wb + 31) / 32, 256, 0, st>>>(s->d_S, s->P, (int)e0, Wb, s->d_bs);
+        s->launches += 4;
+        if (e0 + b < s->N) {
+            int tgrid = (8 * Wb + 255) / 256;
+            blk_tables_kernel<<<tgrid, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->P, s->d_tab);
+            int rows = (int)(s->N - (e0 + b));
+            int grid = (rows + 7) / 8;
+            if (grid > sms * 8) grid = sms * 8;
+            blk_update_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P, (int)e0, Wb, s->P, s->d_tab, s->d_bs,
+                                                    s->d_pairs);
+            s->launches += 2;
+        }
+        MCB_CUDA(cudaGetLastError());
+    }
+    s->iters_run = iters;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_results(mcbgpu_solver *s, int64_t *selected, int64_t count, int64_t *total_weight, void *stream) {
+    if (!s) {
+        set_error("mcbgpu_solver_results: NULL handle");
+        return MCBGPU_E_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (count > s->iters_run) count = s->iters_run;
+    if (selected && count > 0)
+        MCB_CUDA(cudaMemcpyAsync(selected, s->d_selected, sizeof(int64_t) * (size_t)count, cudaMemcpyDeviceToHost, st));
+    unsigned long long tot = 0;
+    MCB_CUDA(cudaMemcpyAsync(&tot, &s->d_bs->total, sizeof tot, cudaMemcpyDeviceToHost, st));
+    int rc = check_status(s, st);
+    if (total_weight) *total_weight = (int64_t)tot;
+    return rc;
+}
+
+int mcbgpu_solver_get_support(mcbgpu_solver *s, int32_t j, uint64_t *words, void *stream) {
+    if (!s || !words || j < 0 || j >= s->N) {
+        set_error("mcbgpu_solver_get_support: invalid argument");
+        return MCBGPU_E_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    MCB_CUDA(cudaMemcpyAsync(words, s->d_S + (size_t)j * s->P, sizeof(uint64_t) * (size_t)s->W,
+                             cudaMemcpyDeviceToHost, st));
+    MCB_CUDA(cudaStreamSynchronize(st));
+    return MCBGPU_OK;
+}
+
+int64_t mcbgpu_solver_launches(const mcbgpu_solver *s) { return s ? s->launches : 0; }
+int64_t mcbgpu_solver_device_bytes(const mcbgpu_solver *s) { return s ? s->device_bytes : 0; }
+
+int mcbgpu_solver_destroy(mcbgpu_solver *s) {
+    if (!s) return MCBGPU_OK;
+    cudaError_t e = cudaDeviceSynchronize();
+    free_solver(s);
+    if (e != cudaSuccess) return cuda_fail(e, "mcbgpu_solver_destroy");
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solve(int32_t N, int64_t K, const int32_t *weight, const int64_t *offsets, const int32_t *coords,
+                 int64_t *selected, int64_t *total_weight) {
+    if (K < 0 || !offsets) {
+        set_error("mcbgpu_solve: invalid argument");
+        return MCBGPU_E_ARG;
+    }
+    mcbgpu_solver *s = nullptr;
+    int rc = mcbgpu_solver_create(&s, N, K, offsets[K]);
+    if (rc) return rc;
+    rc = mcbgpu_solver_upload(s, weight, offsets, coords, nullptr);
+    if (!rc) rc = mcbgpu_solver_run(s, -1, nullptr);
+    if (!rc) rc = mcbgpu_solver_results(s, selected, N, total_weight, nullptr);
+    int rc2 = mcbgpu_solver_destroy(s);
+    return rc ? rc : rc2;
+}
+
+}  // extern "C"

@@ -1,0 +1,1137 @@
+// Host-side preprocessing for the minimum-cycle-basis driver (libmcbhost.so).
+//
+// Every stage reproduces the reference's result exactly, because the reference's
+// output (which of several equal-weight cycles enters the basis) depends on all of
+// them: edge offsets, the coordinate order of the non-tree edges, which vertices are
+// FVS roots, the shortest-path tree chosen among equal-length paths, and the order of
+// the candidate list.  Where the reference's result depends on a standard-library
+// behaviour (std::sort's permutation of equal keys, std::priority_queue's order of
+// equal distances, std::unordered_map's iteration order), this file calls the same
+// standard-library routine on the same sequence, which gives the same permutation.
+// The recursive DFS passes of the reference are restated as explicit-stack loops
+// that visit edges in the same order (the reference needs `ulimit -s unlimited`).
+#include "mcbhost.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <queue>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <utility>
+#include <vector>
+#include <omp.h>
+
+namespace {
+
+using u32 = uint32_t;
+using i64 = int64_t;
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// One directed edge slot while sorting.  Only (row, col) take part in comparisons,
+// so std::sort permutes these exactly as it permutes the reference's edge pointers.
+struct EdgeSlot {
+    u32 row, col;
+    int weight;
+    int chain;
+    int orig;
+    u32 rev;  // index of the reverse slot before sorting
+};
+struct RowColLess {
+    bool operator()(const EdgeSlot &a, const EdgeSlot &b) const {
+        return a.row == b.row ? a.col < b.col : a.row < b.row;
+    }
+};
+
+struct Graph {  // CSR over both directions, sorted by (row, col)
+    int n = 0;
+    std::vector<u32> rows, cols, ro, deg;
+    std::vector<int> w;
+    std::vector<u32> rev;  // multigraph only
+    size_t slots() const { return rows.size(); }
+};
+
+// include/CsrGraph.h:113-174: sort the 2m slots by (row, col), then row offsets.
+void finish_simple_csr(Graph &g, std::vector<EdgeSlot> &s) {
+    std::sort(s.begin(), s.end(), RowColLess());
+    g.rows.resize(s.size());
+    g.cols.resize(s.size());
+    g.w.resize(s.size());
+    for (size_t i = 0; i < s.size(); i++) {
+        g.rows[i] = s[i].row;
+        g.cols[i] = s[i].col;
+        g.w[i] = s[i].weight;
+    }
+    g.ro.assign(g.n + 1, 0);
+    g.deg.assign(g.n, 0);
+    for (size_t i = 0; i < s.size(); i++) g.ro[g.rows[i]]++;
+    u32 prev = 0;
+    for (int i = 0; i <= g.n; i++) {
+        u32 c = g.ro[i];
+        g.ro[i] = prev;
+        prev += c;
+    }
+    for (int i = 0; i < g.n; i++) g.deg[i] = g.ro[i + 1] - g.ro[i];
+}
+
+}  // namespace
+
+struct mcbh_problem {
+    // input
+    Graph in;
+    i64 m_in = 0;
+    bool prepared = false;
+    bool single_cycle = false;
+    i64 total_weight_input = 0;
+    // reduced multigraph
+    Graph rg;
+    std::vector<int> r_chain, r_orig;
+    int nodes_removed = 0;
+    int source_vertex = 0;
+    // FVS
+    std::vector<int> fvs_array;
+    std::vector<u32> fvs_vertices;
+    // coordinates
+    std::vector<u32> coord_edges;
+    std::vector<int> edge_coord;
+    // trees
+    std::vector<int> tree_parent;  // F x n'
+    std::vector<u32> lay_rows, lay_cols, lay_nodes;
+    std::vector<int> lay_edge;
+    // candidates in rank order
+    std::vector<int> c_root, c_edge, c_weight, c_tree;
+    std::vector<i64> c_off;
+    std::vector<int> c_coords;
+    mcbh_info info{};
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Degree-two chains (include/CsrGraphDegreeTwoRemoval.cpp:12-126).
+// The reference runs a recursive DFS from the first vertex of degree > 2; on the
+// way back from each edge it extends / opens / closes the current chain.  The
+// explicit stack below keeps the same edge order and runs the post-edge step when
+// a child frame returns.
+struct ChainResult {
+    std::vector<u32> removal;
+    std::vector<std::vector<u32>> chains;
+    int src = 0;
+    bool bad = false;  // the reference would dereference a null chain here
+};
+
+ChainResult mark_degree_two_chains(const Graph &g) {
+    ChainResult r;
+    const int n = g.n;
+    std::vector<char> visited(n, 0);
+    std::vector<int> parent(n, -1);
+    std::vector<u32> current;  // the chain being assembled
+    bool have_current = false;
+
+    auto chain_step = [&](u32 row, u32 offset) {
+        u32 column = g.cols[offset];
+        bool dc = g.deg[column] == 2, dr = g.deg[row] == 2;
+        if (dc && dr) {
+            if (!have_current) r.bad = true;
+            current.push_back(offset);
+            r.removal.push_back(offset);
+        } else if (dr) {
+            current.clear();
+            current.push_back(offset);
+            have_current = true;
+            r.removal.push_back(offset);
+        } else if (dc) {
+            if (!have_current) r.bad = true;
+            current.push_back(offset);
+            r.chains.push_back(current);
+            current.clear();
+            have_current = false;
+            r.removal.push_back(offset);
+        }
+    };
+
+    int src = -1;
+    for (int i = 0; i < n; i++)
+        if (g.deg[i] > 2) {
+            src = i;
+            break;
+        }
+    if (src < 0) {  // the reference leaves its source uninitialised here
+        r.src = 0;
+        return r;
+    }
+    r.src = src;
+
+    struct Frame {
+        u32 row, off;
+    };
+    std::vector<Frame> st;
+    visited[src] = 1;
+    st.push_back({(u32)src, g.ro[src]});
+    while (!st.empty()) {
+        Frame &f = st.back();
+        if (f.off == g.ro[f.row + 1]) {
+            st.pop_back();
+            if (!st.empty()) {  // back from dfs(column): finish that tree edge
+                Frame &p = st.back();
+                chain_step(p.row, p.off);
+                p.off++;
+            }
+            continue;
+        }
+        u32 row = f.row, offset = f.off;
+        u32 column = g.cols[offset];
+        if (!visited[column]) {
+            visited[column] = 1;
+            parent[column] = (int)row;
+            st.push_back({column, g.ro[column]});
+            continue;
+        }
+        if ((int)column == parent[row]) {
+            if (g.deg[column] == 2 || g.deg[row] == 2) r.removal.push_back(offset);
+            f.off++;
+            continue;
+        }
+        if (g.deg[column] == 2) {
+            r.removal.push_back(offset);
+            f.off++;
+            continue;
+        }
+        chain_step(row, offset);
+        f.off++;
+    }
+    return r;
+}
+
+// include/CsrGraphMulti.h:229-300 (get_modified_graph) and :96-168 (sort + reverse).
+void build_reduced(mcbh_problem &P, const ChainResult *cr) {
+    const Graph &g = P.in;
+    std::vector<char> filtered(g.slots(), 0);
+    std::vector<std::vector<u32>> new_edges;  // (row, col, weight)
+    if (cr) {
+        for (u32 o : cr->removal) filtered[o] = 1;
+        for (const auto &ch : cr->chains) {
+            // csr_graph::sum_edge_weights (include/CsrGraph.h:193-204)
+            u32 tot = 0;
+            for (u32 o : ch) tot += (u32)g.w[o];
+            u32 col = g.cols[ch.front()];
+            u32 row = g.rows[ch.back()];
+            new_edges.push_back({row, col, tot});
+        }
+    }
+    // Relabel in order of first appearance: kept slots first, then new edges.
+    std::vector<int> label(g.n, -1);
+    int cnt = 0;
+    for (size_t i = 0; i < g.slots(); i++)
+        if (!filtered[i]) {
+            if (label[g.rows[i]] < 0) label[g.rows[i]] = cnt++;
+            if (label[g.cols[i]] < 0) label[g.cols[i]] = cnt++;
+        }
+    for (const auto &e : new_edges) {
+        if (label[e[0]] < 0) label[e[0]] = cnt++;
+        if (label[e[1]] < 0) label[e[1]] = cnt++;
+    }
+    Graph &r = P.rg;
+    r.n = cnt;
+    std::vector<EdgeSlot> s;
+    s.reserve(2 * new_edges.size() + g.slots());
+    auto insert_pair = [&](u32 a, u32 b, int wt, int chain, int orig) {
+        u32 i0 = (u32)s.size();
+        s.push_back({a, b, wt, chain, orig, i0 + 1});
+        s.push_back({b, a, wt, chain, orig, i0});
+    };
+    for (size_t i = 0; i < new_edges.size(); i++)
+        insert_pair((u32)label[new_edges[i][0]], (u32)label[new_edges[i][1]], (int)new_edges[i][2], (int)i,
+                    -1);
+    for (size_t i = 0; i < g.slots(); i++)
+        if (!filtered[i] && g.rows[i] < g.cols[i])
+            insert_pair((u32)label[g.rows[i]], (u32)label[g.cols[i]], g.w[i], -1, (int)i);
+
+    // Sort slots by (row, col) with std::sort (unstable for parallel edges: the same
+    // permutation as the reference's sort of edge pointers), then remap reverses.
+    std::vector<EdgeSlot> sorted = s;
+    for (size_t i = 0; i < sorted.size(); i++) sorted[i].rev = (u32)i;  // remember origin
+    std::sort(sorted.begin(), sorted.end(), RowColLess());
+    std::vector<u32> newpos(s.size());
+    for (size_t i = 0; i < sorted.size(); i++) newpos[sorted[i].rev] = (u32)i;
+    const size_t S2 = sorted.size();
+    r.rows.resize(S2);
+    r.cols.resize(S2);
+    r.w.resize(S2);
+    r.rev.resize(S2);
+    P.r_chain.resize(S2);
+    P.r_orig.resize(S2);
+    for (size_t i = 0; i < S2; i++) {
+        u32 origin = sorted[i].rev;
+        r.rows[i] = sorted[i].row;
+        r.cols[i] = sorted[i].col;
+        r.w[i] = sorted[i].weight;
+        P.r_chain[i] = sorted[i].chain;
+        P.r_orig[i] = sorted[i].orig;
+        r.rev[i] = newpos[s[origin].rev];
+    }
+    r.ro.assign(r.n + 1, 0);
+    r.deg.assign(r.n, 0);
+    for (size_t i = 0; i < S2; i++) r.ro[r.rows[i]]++;
+    u32 prev = 0;
+    for (int i = 0; i <= r.n; i++) {
+        u32 c = r.ro[i];
+        r.ro[i] = prev;
+        prev += c;
+    }
+    for (int i = 0; i < r.n; i++) r.deg[i] = r.ro[i + 1] - r.ro[i];
+}
+
+// ---------------------------------------------------------------------------
+// FVS (include/FVS.cpp:166-262).  MGA's pruning step exits at once (it marks the
+// chosen vertex removed before testing it, FVS.cpp:94-104), so W and the degrees
+// never change and MGA picks every vertex, by largest degree, lowest id first.  The
+// list is then reversed and each vertex is dropped from the FVS if the rest stays
+// acyclic (test_fvs: BFS cycle check over non-FVS vertices, FVS.cpp:138-212).  Here
+// the same test is answered incrementally with a union-find over the non-FVS
+// forest: adding v closes a cycle iff v has a self-loop, or two of its edges
+// (parallel edges included) reach the same forest component.
+struct DSU {
+    std::vector<int> p;
+    explicit DSU(int n) : p(n) {
+        for (int i = 0; i < n; i++) p[i] = i;
+    }
+    int find(int x) {
+        while (p[x] != x) {
+            p[x] = p[p[x]];
+            x = p[x];
+        }
+        return x;
+    }
+};
+
+void compute_fvs(mcbh_problem &P) {
+    const Graph &g = P.rg;
+    const int n = g.n;
+    // MGA pick order: ratio W/deg ascending with strict '<' (lowest id wins ties).
+    // W = 1 for every vertex of the reduced graph (all have degree >= 1).
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        double ra = 1.0 / (double)g.deg[a], rb = 1.0 / (double)g.deg[b];
+        return ra < rb;
+    });
+    std::reverse(order.begin(), order.end());
+    std::vector<char> in_fvs(n, 1);
+    DSU dsu(n);
+    std::vector<int> seen_roots;
+    for (int v : order) {
+        bool cycle = false;
+        seen_roots.clear();
+        for (u32 o = g.ro[v]; o < g.ro[v + 1] && !cycle; o++) {
+            u32 c = g.cols[o];
+            if ((int)c == v) {
+                cycle = true;
+                break;
+            }
+            if (in_fvs[c]) continue;
+            int rt = dsu.find((int)c);
+            for (int x : seen_roots)
+                if (x == rt) {
+                    cycle = true;
+                    break;
+                }
+            seen_roots.push_back(rt);
+        }
+        if (!cycle) {
+            in_fvs[v] = 0;
+            for (int x : seen_roots) dsu.p[dsu.find(x)] = dsu.find(v);
+        }
+    }
+    P.fvs_array.assign(n, -1);
+    P.fvs_vertices.clear();
+    int cnt = 0;
+    for (int v = 0; v < n; v++)
+        if (in_fvs[v]) {
+            P.fvs_array[v] = cnt++;
+            P.fvs_vertices.push_back((u32)v);
+        }
+}
+
+// ---------------------------------------------------------------------------
+// Initial DFS spanning tree (include/CsrGraphMultiSpanningTree.cpp:11-135) and the
+// coordinate map (mcb/mcb_cycle_deg_two_remove.cpp:175-187).
+bool spanning_tree(mcbh_problem &P, int src) {
+    const Graph &g = P.rg;
+    const int n = g.n;
+    if (src < 0 || src >= n) return false;
+    std::vector<char> visited(n, 0);
+    std::vector<int> parent(n, -1);
+    std::vector<unsigned char> state(g.slots(), 0);  // 0 unseen, 1 tree, 2 non-tree
+    std::vector<u32> nte;
+    int tree_edges = 0;
+    struct Frame {
+        u32 row, off;
+    };
+    std::vector<Frame> st;
+    visited[src] = 1;
+    st.push_back({(u32)src, g.ro[src]});
+    while (!st.empty()) {
+        Frame &f = st.back();
+        if (f.off == g.ro[f.row + 1]) {
+            st.pop_back();
+            if (!st.empty()) st.back().off++;
+            continue;
+        }
+        u32 row = f.row, offset = f.off;
+        u32 column = g.cols[offset];
+        if (!visited[column]) {
+            visited[column] = 1;
+            tree_edges++;
+            parent[column] = (int)row;
+            state[offset] = 1;
+            st.push_back({column, g.ro[column]});
+            continue;
+        }
+        f.off++;
+        if ((int)column == parent[row]) {
+            u32 ri = g.rev[offset];
+            if (state[ri] == 1) {
+                state[offset] = 1;
+            } else if (state[ri] == 2) {
+                state[offset] = 2;
+            } else {
+                state[offset] = 2;
+                state[ri] = 2;
+                nte.push_back(row < column ? offset : ri);
+            }
+        } else if (state[offset] == 0) {
+            u32 ri = g.rev[offset];
+            state[offset] = 2;
+            state[ri] = 2;
+            nte.push_back(row < column ? offset : ri);
+        }
+    }
+    if (tree_edges != n - 1) return false;
+    P.coord_edges = nte;
+    P.edge_coord.assign(g.slots(), -1);
+    for (size_t i = 0; i < nte.size(); i++) P.edge_coord[nte[i]] = (int)i;
+    for (size_t i = 0; i < g.slots(); i++)
+        if (P.edge_coord[i] < 0 && P.edge_coord[g.rev[i]] >= 0) P.edge_coord[i] = P.edge_coord[g.rev[i]];
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Per-root shortest-path tree + candidates (include/Dijkstra.h:78-254,
+// include/work_per_thread.h:92-147).
+struct HeapLess {  // include/Dijkstra.h:37-41: min-heap on distance only
+    bool operator()(const std::pair<int, int> &a, const std::pair<int, int> &b) const {
+        return a.second > b.second;
+    }
+};
+
+struct LevelItem {  // include/Dijkstra.h:7-21
+    int offset, level;
+};
+struct LevelLess {
+    bool operator()(const LevelItem &a, const LevelItem &b) const { return a.level < b.level; }
+};
+
+struct LocalCandidate {
+    int edge;
+    int weight;
+    i64 coord_begin;
+    int coord_len;
+};
+
+struct RootOutput {
+    std::vector<LocalCandidate> cands;
+    std::vector<int> coords;
+    // unordered_map<u64, indices> with the reference's key and insertion sequence
+    // (include/cycle_searcher.h:23-61); only its iteration order is used.
+    std::unordered_map<unsigned long long, std::vector<int>> groups;
+};
+
+struct TreeWorkspace {
+    std::vector<int> dist, par, level, pedge;
+    std::vector<char> in_tree;
+    std::vector<u32> pop_order;
+    std::vector<unsigned char> is_tree;
+    std::vector<u32> nte;
+    std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>, HeapLess> pq;
+    std::vector<LevelItem> lv;
+    std::vector<int> tmp;
+    void init(int n, size_t slots) {
+        dist.assign(n, -1);
+        par.assign(n, -1);
+        level.assign(n, -1);
+        pedge.assign(n, -1);
+        in_tree.assign(n, 0);
+        is_tree.assign(slots, 0);
+        pop_order.clear();
+        pop_order.reserve(n);
+    }
+};
+
+void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput &out, bool want_lists,
+                  int *tree_parent, u32 *lay_rows, u32 *lay_cols, int *lay_edge, u32 *lay_nodes) {
+    const Graph &g = P.rg;
+    const int n = g.n;
+    const u32 src = P.fvs_vertices[tidx];
+    ws.init(n, g.slots());
+    // dijkstra::dijkstra_sp
+    std::vector<u32> tree_edges;
+    tree_edges.reserve(n);
+    ws.dist[src] = 0;
+    ws.level[src] = 0;
+    ws.pq.push(std::make_pair((int)src, 0));
+    while (!ws.pq.empty()) {
+        std::pair<int, int> val = ws.pq.top();
+        ws.pq.pop();
+        int x = val.first;
+        if (ws.in_tree[x]) continue;
+        if ((u32)x != src) tree_edges.push_back((u32)ws.pedge[x]);
+        ws.in_tree[x] = 1;
+        ws.pop_order.push_back((u32)x);
+        for (u32 o = g.ro[x]; o < g.ro[x + 1]; o++) {
+            u32 c = g.cols[o];
+            if (ws.in_tree[c]) continue;
+            int ew = g.w[o];
+            if (ws.dist[c] == -1 || ws.dist[x] + ew < ws.dist[c]) {
+                ws.dist[c] = ws.dist[x] + ew;
+                ws.pq.push(std::make_pair((int)c, ws.dist[c]));
+                ws.par[c] = x;
+                ws.pedge[c] = (int)o;
+                ws.level[c] = ws.level[x] + 1;
+            }
+        }
+    }
+    // dijkstra::compute_non_tree_edges
+    for (u32 o : tree_edges) ws.is_tree[o] = 1;
+    ws.nte.clear();
+    for (size_t i = 0; i < g.slots(); i++) {
+        if (ws.is_tree[i] == 1) continue;
+        unsigned char rs = ws.is_tree[g.rev[i]];
+        if (rs == 1) {
+            ws.is_tree[i] = 1;
+        } else if (rs == 2) {
+            ws.is_tree[i] = 2;
+        } else {
+            ws.is_tree[i] = 2;
+            ws.nte.push_back((u32)i);
+        }
+    }
+    // dijkstra::is_edge_cycle: accepted iff the two root paths meet only at the root
+    // and contain no FVS vertex with a smaller id than the root.  Computed here per
+    // vertex: the root child a vertex hangs under, and whether its root path holds
+    // such an FVS vertex (vertices are visited in pop order: parents first).
+    std::vector<int> &branch = ws.tmp;
+    branch.assign(n, -1);
+    std::vector<char> blocked(n, 0);
+    for (u32 x : ws.pop_order) {
+        bool self_bad = P.fvs_array[x] >= 0 && src > x;
+        if (x == src) {
+            branch[x] = -1;
+            blocked[x] = self_bad;
+        } else {
+            int p = ws.par[x];
+            branch[x] = ((u32)p == src) ? (int)x : branch[p];
+            blocked[x] = blocked[p] || self_bad;
+        }
+    }
+    for (u32 off : ws.nte) {
+        u32 a = g.rows[off], b = g.cols[off];
+        if (blocked[a] || blocked[b]) continue;
+        bool lca_root = (a == src) || (b == src) || (branch[a] != branch[b]);
+        if (!lca_root) continue;
+        int weight = ws.dist[a] + ws.dist[b] + g.w[off];
+        LocalCandidate lc;
+        lc.edge = (int)off;
+        lc.weight = weight;
+        lc.coord_begin = (i64)out.coords.size();
+        lc.coord_len = 0;
+        if (want_lists) {
+            size_t b0 = out.coords.size();
+            if (P.edge_coord[off] >= 0) out.coords.push_back(P.edge_coord[off]);
+            for (u32 x = a; x != src; x = (u32)ws.par[x]) {
+                int c = P.edge_coord[ws.pedge[x]];
+                if (c >= 0) out.coords.push_back(c);
+            }
+            for (u32 x = b; x != src; x = (u32)ws.par[x]) {
+                int c = P.edge_coord[ws.pedge[x]];
+                if (c >= 0) out.coords.push_back(c);
+            }
+            std::sort(out.coords.begin() + b0, out.coords.end());
+            lc.coord_len = (int)(out.coords.size() - b0);
+        }
+        int local = (int)out.cands.size();
+        out.cands.push_back(lc);
+        unsigned long long key = ((unsigned long long)std::min(a, b) << 32) | std::max(a, b);
+        auto it = out.groups.find(key);
+        if (it == out.groups.end())
+            out.groups.insert(std::make_pair(key, std::vector<int>(1, local)));
+        else
+            it->second.push_back(local);
+    }
+    if (tree_parent) {
+        int *tp = tree_parent + (size_t)tidx * n;
+        for (int v = 0; v < n; v++) tp[v] = ws.pedge[v];
+        tp[src] = -1;
+    }
+    if (lay_rows) {
+        // dijkstra::fill_tree_edges: (offset, level) items, root first, then tree
+        // edges in pop order; std::sort by level only.
+        ws.lv.clear();
+        ws.lv.push_back({-1, 0});
+        for (u32 o : tree_edges) ws.lv.push_back({(int)o, ws.level[g.cols[o]]});
+        std::sort(ws.lv.begin(), ws.lv.end(), LevelLess());
+        u32 *R = lay_rows + (size_t)tidx * (n + 1);
+        u32 *C = lay_cols + (size_t)tidx * n;
+        int *E = lay_edge + (size_t)tidx * n;
+        u32 *NI = lay_nodes + (size_t)tidx * n;
+        for (int i = 0; i <= n; i++) R[i] = 0;
+        for (size_t i = 0; i < ws.lv.size(); i++) {
+            R[ws.lv[i].level]++;
+            if (ws.lv[i].offset == -1) {
+                NI[src] = (u32)i;
+                C[i] = 0xFFFFFFFFu;
+                E[i] = -1;
+            } else {
+                u32 r = g.rows[ws.lv[i].offset], c = g.cols[ws.lv[i].offset];
+                NI[c] = (u32)i;
+                C[i] = NI[r];
+                E[i] = ws.lv[i].offset;
+            }
+        }
+        u32 prev = 0;
+        for (int i = 0; i <= n; i++) {
+            u32 t = R[i];
+            R[i] = prev;
+            prev += t;
+        }
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+extern "C" {
+
+static int read_mtx(const char *path, int &nodes, std::vector<int> &u, std::vector<int> &v,
+                    std::vector<int> &w) {
+    FILE *f = fopen(path, "r");
+    if (!f) return MCBH_E_IO;
+    char line[4096];
+    if (!fgets(line, sizeof line, f)) {
+        fclose(f);
+        return MCBH_E_IO;
+    }
+    // banner: %%MatrixMarket matrix coordinate <integer|real> <symmetric|general>
+    // (the combinations include/FileReader.h:39-44 accepts)
+    std::string b(line);
+    for (auto &ch : b) ch = (char)tolower(ch);
+    if (b.compare(0, 14, "%%matrixmarket") != 0) {
+        fclose(f);
+        return MCBH_E_FORMAT;
+    }
+    bool ok = b.find("matrix") != std::string::npos && b.find("coordinate") != std::string::npos &&
+              (b.find("integer") != std::string::npos || b.find("real") != std::string::npos) &&
+              (b.find("symmetric") != std::string::npos || b.find("general") != std::string::npos);
+    if (!ok) {
+        fclose(f);
+        return MCBH_E_FORMAT;
+    }
+    long M = 0, Ncol = 0, E = 0;
+    while (fgets(line, sizeof line, f)) {
+        if (line[0] == '%') continue;
+        if (sscanf(line, "%ld %ld %ld", &M, &Ncol, &E) == 3) break;
+    }
+    if (M <= 0 || E < 0) {
+        fclose(f);
+        return MCBH_E_IO;
+    }
+    nodes = (int)M;
+    u.resize(E);
+    v.resize(E);
+    w.resize(E);
+    for (long i = 0; i < E; i++) {
+        long a, c;
+        double wt;
+        if (fscanf(f, "%ld %ld %lf", &a, &c, &wt) != 3) {
+            fclose(f);
+            return MCBH_E_IO;
+        }
+        if (a < 1 || c < 1 || a > M || c > M) {
+            fclose(f);
+            return MCBH_E_IO;
+        }
+        u[i] = (int)(a - 1);
+        v[i] = (int)(c - 1);
+        w[i] = (int)wt;  // fscanf("%d") of the reference truncates the same way
+    }
+    fclose(f);
+    return MCBH_OK;
+}
+
+int mcbh_problem_from_edges(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v, const int32_t *w,
+                            mcbh_problem **out) {
+    if (!out || nodes <= 0 || m < 0 || (m > 0 && (!u || !v || !w))) return MCBH_E_ARG;
+    *out = nullptr;
+    mcbh_problem *P = new (std::nothrow) mcbh_problem();
+    if (!P) return MCBH_E_NOMEM;
+    double t0 = now_s();
+    P->in.n = nodes;
+    P->m_in = m;
+    std::vector<EdgeSlot> s;
+    try {
+        s.reserve(2 * (size_t)m);
+    } catch (...) {
+        delete P;
+        return MCBH_E_NOMEM;
+    }
+    for (int64_t i = 0; i < m; i++) {
+        if (u[i] < 0 || v[i] < 0 || u[i] >= nodes || v[i] >= nodes) {
+            delete P;
+            return MCBH_E_ARG;
+        }
+        // csr_graph::insert(a, b, w, false) pushes (a,b) then (b,a)
+        s.push_back({(u32)u[i], (u32)v[i], w[i], -1, -1, 0});
+        s.push_back({(u32)v[i], (u32)u[i], w[i], -1, -1, 0});
+        P->total_weight_input += w[i];
+    }
+    finish_simple_csr(P->in, s);
+    P->info.t_read = now_s() - t0;
+    *out = P;
+    return MCBH_OK;
+}
+
+int mcbh_problem_from_mtx(const char *path, mcbh_problem **out) {
+    if (!path || !out) return MCBH_E_ARG;
+    double t0 = now_s();
+    int nodes = 0;
+    std::vector<int> u, v, w;
+    int rc = read_mtx(path, nodes, u, v, w);
+    if (rc) return rc;
+    rc = mcbh_problem_from_edges(nodes, (int64_t)u.size(), u.data(), v.data(), w.data(), out);
+    if (rc == MCBH_OK) (*out)->info.t_read = now_s() - t0;
+    return rc;
+}
+
+void mcbh_problem_free(mcbh_problem *p) { delete p; }
+
+int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
+    if (!P || !opt) return MCBH_E_ARG;
+    if (P->prepared) return MCBH_E_STATE;
+    mcbh_info &I = P->info;
+    I.nodes = P->in.n;
+    I.edges2 = (int64_t)P->in.slots();
+    I.total_weight_input = P->total_weight_input;
+    try {
+        // mcb/mcb_cycle_deg_two_remove.cpp:104-113: a graph whose every vertex has
+        // degree two is one cycle.
+        int deg2 = 0;
+        for (int i = 0; i < P->in.n; i++) deg2 += P->in.deg[i] == 2;
+        if (opt->contract_chains && deg2 == P->in.n) {
+            P->single_cycle = true;
+            I.single_cycle = 1;
+            I.nodes_removed = P->in.n - 1;
+            I.fvs_size = 1;
+            I.num_coords = 1;
+            I.num_candidates = 1;
+            P->prepared = true;
+            return MCBH_OK;
+        }
+        double t0 = now_s();
+        if (opt->contract_chains) {
+            ChainResult cr = mark_degree_two_chains(P->in);
+            if (cr.bad) return MCBH_E_GRAPH;
+            int removed = 0;
+            for (auto &ch : cr.chains) removed += (int)ch.size() - 1;
+            P->nodes_removed = removed;
+            P->source_vertex = cr.src;
+            build_reduced(*P, &cr);
+        } else {
+            P->nodes_removed = 0;
+            P->source_vertex = 0;  // mcb/mcb_cycle.cpp:110
+            build_reduced(*P, nullptr);
+        }
+        I.nodes_removed = P->nodes_removed;
+        I.reduced_nodes = P->rg.n;
+        I.reduced_edges2 = (int64_t)P->rg.slots();
+        I.source_vertex = P->source_vertex;
+        I.t_reduce = now_s() - t0;
+
+        t0 = now_s();
+        compute_fvs(*P);
+        I.fvs_size = (int)P->fvs_vertices.size();
+        I.t_fvs = now_s() - t0;
+
+        t0 = now_s();
+        if (!spanning_tree(*P, P->source_vertex)) return MCBH_E_GRAPH;
+        I.num_coords = (int)P->coord_edges.size();
+        I.t_spanning = now_s() - t0;
+
+        t0 = now_s();
+        const int F = I.fvs_size;
+        const int n = P->rg.n;
+        if (opt->keep_trees) P->tree_parent.assign((size_t)F * n, -1);
+        if (opt->ref_layout) {
+            P->lay_rows.assign((size_t)F * (n + 1), 0);
+            P->lay_cols.assign((size_t)F * n, 0);
+            P->lay_edge.assign((size_t)F * n, -1);
+            P->lay_nodes.assign((size_t)F * n, 0);
+        }
+        std::vector<RootOutput> outs(F);
+        int threads = opt->threads > 0 ? opt->threads : omp_get_max_threads();
+        bool lists = opt->cycle_lists != 0;
+#pragma omp parallel num_threads(threads)
+        {
+            TreeWorkspace ws;
+#pragma omp for schedule(dynamic, 1)
+            for (int t = 0; t < F; t++)
+                process_root(*P, t, ws, outs[t], lists, opt->keep_trees ? P->tree_parent.data() : nullptr,
+                             opt->ref_layout ? P->lay_rows.data() : nullptr,
+                             opt->ref_layout ? P->lay_cols.data() : nullptr,
+                             opt->ref_layout ? P->lay_edge.data() : nullptr,
+                             opt->ref_layout ? P->lay_nodes.data() : nullptr);
+        }
+        I.t_trees = now_s() - t0;
+
+        t0 = now_s();
+        // mcb/mcb_cycle_deg_two_remove.cpp:244-258: roots in vertex-id order, each
+        // root's map in iteration order, each group in insertion order; then an
+        // unstable std::sort on total_length alone.
+        struct Item {
+            int weight;
+            int tree;
+            int local;
+        };
+        std::vector<Item> items;
+        size_t total = 0;
+        for (int t = 0; t < F; t++) total += outs[t].cands.size();
+        items.reserve(total);
+        for (int vtx = 0; vtx < n; vtx++) {
+            int t = P->fvs_array[vtx];
+            if (t < 0) continue;
+            for (auto it = outs[t].groups.begin(); it != outs[t].groups.end(); ++it)
+                for (int loc : it->second) items.push_back({outs[t].cands[loc].weight, t, loc});
+        }
+        std::sort(items.begin(), items.end(), [](const Item &a, const Item &b) { return a.weight < b.weight; });
+        const size_t K = items.size();
+        P->c_root.resize(K);
+        P->c_edge.resize(K);
+        P->c_weight.resize(K);
+        P->c_tree.resize(K);
+        int64_t nnz = 0;
+        if (lists) {
+            P->c_off.resize(K + 1);
+            P->c_off[0] = 0;
+            for (size_t r = 0; r < K; r++) {
+                nnz += outs[items[r].tree].cands[items[r].local].coord_len;
+                P->c_off[r + 1] = nnz;
+            }
+            P->c_coords.resize((size_t)nnz);
+        }
+#pragma omp parallel for num_threads(threads) schedule(static)
+        for (int64_t r = 0; r < (int64_t)K; r++) {
+            const Item &it = items[r];
+            const LocalCandidate &lc = outs[it.tree].cands[it.local];
+            P->c_root[r] = (int)P->fvs_vertices[it.tree];
+            P->c_edge[r] = lc.edge;
+            P->c_weight[r] = lc.weight;
+            P->c_tree[r] = it.tree;
+            if (lists)
+                std::memcpy(&P->c_coords[P->c_off[r]], &outs[it.tree].coords[lc.coord_begin],
+                            sizeof(int) * (size_t)lc.coord_len);
+        }
+        I.num_candidates = (int64_t)K;
+        I.cycle_nnz = nnz;
+        I.t_collect = now_s() - t0;
+    } catch (const std::bad_alloc &) {
+        return MCBH_E_NOMEM;
+    }
+    P->prepared = true;
+    return MCBH_OK;
+}
+
+int mcbh_get_info(const mcbh_problem *p, mcbh_info *info) {
+    if (!p || !info) return MCBH_E_ARG;
+    *info = p->info;
+    return MCBH_OK;
+}
+
+#define NEED_PREPARED(p)                                     \
+    do {                                                     \
+        if (!(p)) return MCBH_E_ARG;                         \
+        if (!(p)->prepared || (p)->single_cycle) return MCBH_E_STATE; \
+    } while (0)
+
+int mcbh_get_reduced_graph(const mcbh_problem *p, uint32_t *rows, uint32_t *cols, int32_t *weights,
+                           uint32_t *reverse_edge, uint32_t *row_offsets) {
+    NEED_PREPARED(p);
+    const Graph &g = p->rg;
+    if (rows) std::memcpy(rows, g.rows.data(), g.slots() * 4);
+    if (cols) std::memcpy(cols, g.cols.data(), g.slots() * 4);
+    if (weights) std::memcpy(weights, g.w.data(), g.slots() * 4);
+    if (reverse_edge) std::memcpy(reverse_edge, g.rev.data(), g.slots() * 4);
+    if (row_offsets) std::memcpy(row_offsets, g.ro.data(), (g.n + 1) * 4);
+    return MCBH_OK;
+}
+
+int mcbh_get_fvs(const mcbh_problem *p, int32_t *fvs_array, uint32_t *fvs_vertices) {
+    NEED_PREPARED(p);
+    if (fvs_array) std::memcpy(fvs_array, p->fvs_array.data(), p->fvs_array.size() * 4);
+    if (fvs_vertices) std::memcpy(fvs_vertices, p->fvs_vertices.data(), p->fvs_vertices.size() * 4);
+    return MCBH_OK;
+}
+
+int mcbh_get_coords(const mcbh_problem *p, uint32_t *coord_edges, int32_t *edge_coord) {
+    NEED_PREPARED(p);
+    if (coord_edges) std::memcpy(coord_edges, p->coord_edges.data(), p->coord_edges.size() * 4);
+    if (edge_coord) std::memcpy(edge_coord, p->edge_coord.data(), p->edge_coord.size() * 4);
+    return MCBH_OK;
+}
+
+int mcbh_get_candidates(const mcbh_problem *p, int32_t *root, int32_t *edge_offset, int32_t *weight,
+                        int32_t *tree) {
+    NEED_PREPARED(p);
+    size_t K = p->c_root.size();
+    if (root) std::memcpy(root, p->c_root.data(), K * 4);
+    if (edge_offset) std::memcpy(edge_offset, p->c_edge.data(), K * 4);
+    if (weight) std::memcpy(weight, p->c_weight.data(), K * 4);
+    if (tree) std::memcpy(tree, p->c_tree.data(), K * 4);
+    return MCBH_OK;
+}
+
+int mcbh_get_cycle_lists(const mcbh_problem *p, int64_t *offsets, int32_t *coords) {
+    NEED_PREPARED(p);
+    if (p->c_off.empty() && !p->c_root.empty()) return MCBH_E_STATE;
+    if (p->c_root.empty()) {
+        if (offsets) offsets[0] = 0;
+        return MCBH_OK;
+    }
+    if (offsets) std::memcpy(offsets, p->c_off.data(), p->c_off.size() * 8);
+    if (coords) std::memcpy(coords, p->c_coords.data(), p->c_coords.size() * 4);
+    return MCBH_OK;
+}
+
+int mcbh_get_tree_parents(const mcbh_problem *p, int32_t *parent_edge) {
+    NEED_PREPARED(p);
+    if (p->tree_parent.empty() && p->info.fvs_size > 0) return MCBH_E_STATE;
+    if (parent_edge) std::memcpy(parent_edge, p->tree_parent.data(), p->tree_parent.size() * 4);
+    return MCBH_OK;
+}
+
+int mcbh_get_ref_layout(const mcbh_problem *p, uint32_t *level_offsets, uint32_t *parent_pos,
+                        int32_t *edge_offset, uint32_t *nodes_index) {
+    NEED_PREPARED(p);
+    if (p->lay_rows.empty() && p->info.fvs_size > 0) return MCBH_E_STATE;
+    if (level_offsets) std::memcpy(level_offsets, p->lay_rows.data(), p->lay_rows.size() * 4);
+    if (parent_pos) std::memcpy(parent_pos, p->lay_cols.data(), p->lay_cols.size() * 4);
+    if (edge_offset) std::memcpy(edge_offset, p->lay_edge.data(), p->lay_edge.size() * 4);
+    if (nodes_index) std::memcpy(nodes_index, p->lay_nodes.data(), p->lay_nodes.size() * 4);
+    return MCBH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Seeded generators.  splitmix64 (Steele, Lea, Flood 2014; constants as published
+// by Vigna) drives every draw, so the same seed gives the same graph on any host.
+struct Rng {
+    uint64_t s;
+    uint64_t next() {
+        uint64_t z = (s += 0x9e3779b97f4a7c15ULL);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+        return z ^ (z >> 31);
+    }
+    uint64_t below(uint64_t n) { return next() % n; }
+    double unit() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+int64_t mcbh_gen_grid(int32_t r, int32_t c, int32_t wlo, int32_t whi, uint64_t seed, int32_t *u, int32_t *v,
+                      int32_t *w) {
+    if (r <= 0 || c <= 0 || whi < wlo) return MCBH_E_ARG;
+    int64_t m = (int64_t)r * (c - 1) + (int64_t)(r - 1) * c;
+    if (!u) return m;
+    Rng g{seed};
+    int64_t k = 0;
+    for (int32_t i = 0; i < r; i++)
+        for (int32_t j = 0; j < c; j++) {
+            int32_t id = i * c + j;
+            if (j + 1 < c) {
+                u[k] = id;
+                v[k] = id + 1;
+                w[k] = wlo + (int32_t)g.below((uint64_t)(whi - wlo + 1));
+                k++;
+            }
+            if (i + 1 < r) {
+                u[k] = id;
+                v[k] = id + c;
+                w[k] = wlo + (int32_t)g.below((uint64_t)(whi - wlo + 1));
+                k++;
+            }
+        }
+    return k;
+}
+
+int64_t mcbh_gen_random(int32_t n, int64_t m, int32_t wlo, int32_t whi, uint64_t seed, int32_t *u, int32_t *v,
+                        int32_t *w) {
+    if (n <= 1 || m < n - 1 || whi < wlo) return MCBH_E_ARG;
+    if (m > (int64_t)n * (n - 1) / 2) return MCBH_E_ARG;
+    if (!u) return m;
+    Rng g{seed};
+    std::vector<int32_t> perm(n);
+    for (int32_t i = 0; i < n; i++) perm[i] = i;
+    for (int32_t i = n - 1; i > 0; i--) std::swap(perm[i], perm[g.below((uint64_t)i + 1)]);
+    std::unordered_set<uint64_t> seen;
+    seen.reserve((size_t)m * 2);
+    int64_t k = 0;
+    auto key = [](int32_t a, int32_t b) {
+        return ((uint64_t)(uint32_t)std::min(a, b) << 32) | (uint32_t)std::max(a, b);
+    };
+    for (int32_t i = 1; i < n; i++) {
+        int32_t a = perm[i], b = perm[g.below((uint64_t)i)];
+        u[k] = a;
+        v[k] = b;
+        w[k] = wlo + (int32_t)g.below((uint64_t)(whi - wlo + 1));
+        seen.insert(key(a, b));
+        k++;
+    }
+    while (k < m) {
+        int32_t a = (int32_t)g.below((uint64_t)n), b = (int32_t)g.below((uint64_t)n);
+        if (a == b || seen.count(key(a, b))) continue;
+        seen.insert(key(a, b));
+        u[k] = a;
+        v[k] = b;
+        w[k] = wlo + (int32_t)g.below((uint64_t)(whi - wlo + 1));
+        k++;
+    }
+    return k;
+}
+
+int64_t mcbh_gen_rgg(int32_t n, int32_t kk, uint64_t seed, int32_t *u, int32_t *v, int32_t *w) {
+    if (n <= 1 || kk <= 0 || kk >= n) return MCBH_E_ARG;
+    Rng g{seed};
+    std::vector<double> x(n), y(n);
+    for (int32_t i = 0; i < n; i++) {
+        x[i] = g.unit();
+        y[i] = g.unit();
+    }
+    // bucket grid with ~2 points per cell
+    int G = std::max(1, (int)std::sqrt((double)n / 2.0));
+    std::vector<std::vector<int32_t>> cell((size_t)G * G);
+    auto cid = [&](double a) { return std::min(G - 1, (int)(a * G)); };
+    for (int32_t i = 0; i < n; i++) cell[(size_t)cid(y[i]) * G + cid(x[i])].push_back(i);
+    std::unordered_set<uint64_t> seen;
+    std::vector<std::pair<int32_t, int32_t>> edges;
+    auto key = [](int32_t a, int32_t b) {
+        return ((uint64_t)(uint32_t)std::min(a, b) << 32) | (uint32_t)std::max(a, b);
+    };
+    auto add = [&](int32_t a, int32_t b) {
+        if (a == b) return;
+        if (seen.insert(key(a, b)).second) edges.push_back({std::min(a, b), std::max(a, b)});
+    };
+    // k nearest neighbours by expanding rings (exact: a ring stops only when the
+    // k-th distance found is within the ring's guaranteed radius)
+    std::vector<std::pair<double, int32_t>> best;
+    for (int32_t i = 0; i < n; i++) {
+        int cx = cid(x[i]), cy = cid(y[i]);
+        best.clear();
+        for (int ring = 0;; ring++) {
+            for (int dy = -ring; dy <= ring; dy++)
+                for (int dx = -ring; dx <= ring; dx++) {
+                    if (std::max(std::abs(dx), std::abs(dy)) != ring) continue;
+                    int gx = cx + dx, gy = cy + dy;
+                    if (gx < 0 || gy < 0 || gx >= G || gy >= G) continue;
+                    for (int32_t j : cell[(size_t)gy * G + gx]) {
+                        if (j == i) continue;
+                        double d = (x[i] - x[j]) * (x[i] - x[j]) + (y[i] - y[j]) * (y[i] - y[j]);
+                        best.push_back({d, j});
+                    }
+                }
+            if ((int)best.size() >= kk) {
+                std::nth_element(best.begin(), best.begin() + (kk - 1), best.end());
+                double r = (double)ring / G;
+                if (best[kk - 1].first <= r * r || ring > G) break;
+            }
+            if (ring > G) break;
+        }
+        std::sort(best.begin(), best.end());
+        for (int t = 0; t < kk && t < (int)best.size(); t++) add(i, best[t].second);
+    }
+    // connect components: each later component to its nearest outside point
+    std::vector<int> comp(n, -1);
+    {
+        std::vector<std::vector<int32_t>> adj(n);
+        for (auto &e : edges) {
+            adj[e.first].push_back(e.second);
+            adj[e.second].push_back(e.first);
+        }
+        int nc = 0;
+        std::vector<int32_t> stk;
+        for (int32_t s = 0; s < n; s++) {
+            if (comp[s] >= 0) continue;
+            comp[s] = nc;
+            stk.push_back(s);
+            while (!stk.empty()) {
+                int32_t a = stk.back();
+                stk.pop_back();
+                for (int32_t b : adj[a])
+                    if (comp[b] < 0) {
+                        comp[b] = nc;
+                        stk.push_back(b);
+                    }
+            }
+            nc++;
+        }
+        if (nc > 1) {
+            DSU d(nc);
+            for (int32_t i = 0; i < n; i++) {
+                if (d.find(comp[i]) == d.find(0)) continue;
+                // nearest point in another (merged) component, brute force (rare)
+                double bd = 1e300;
+                int32_t bj = -1;
+                for (int32_t j = 0; j < n; j++) {
+                    if (d.find(comp[j]) == d.find(comp[i])) continue;
+                    double dd = (x[i] - x[j]) * (x[i] - x[j]) + (y[i] - y[j]) * (y[i] - y[j]);
+                    if (dd < bd) {
+                        bd = dd;
+                        bj = j;
+                    }
+                }
+                if (bj >= 0) {
+                    add(i, bj);
+                    d.p[d.find(comp[i])] = d.find(comp[bj]);
+                }
+            }
+        }
+    }
+    int64_t m = (int64_t)edges.size();
+    if (!u) return m;
+    for (int64_t k = 0; k < m; k++) {
+        int32_t a = edges[k].first, b = edges[k].second;
+        double len = std::sqrt((x[a] - x[b]) * (x[a] - x[b]) + (y[a] - y[b]) * (y[a] - y[b]));
+        u[k] = a;
+        v[k] = b;
+        w[k] = std::max(1, (int32_t)std::lround(1000.0 * len));
+    }
+    return m;
+}
+
+int mcbh_write_mtx(const char *path, int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
+                   const int32_t *w) {
+    if (!path || nodes <= 0 || m < 0) return MCBH_E_ARG;
+    FILE *f = fopen(path, "w");
+    if (!f) return MCBH_E_IO;
+    fprintf(f, "%%%%MatrixMarket matrix coordinate integer symmetric\n");
+    fprintf(f, "%d %d %lld\n", nodes, nodes, (long long)m);
+    for (int64_t i = 0; i < m; i++) fprintf(f, "%d %d %d\n", u[i] + 1, v[i] + 1, w[i]);
+    fclose(f);
+    return MCBH_OK;
+}
+
+}  // extern "C"

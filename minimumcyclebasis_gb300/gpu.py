@@ -1,0 +1,203 @@
+"""Python handles over libmcbgpu.so (include/mcbgpu.h).
+
+GpuStruct mirrors the reference's gpu_struct (gpu/gpu_struct.cuh:44-84): trees are
+uploaded once, a support vector is copied in, and process_shortest_path returns
+every tree's labels.  Solver holds the device-resident main loop: candidates in
+rank order, S in HBM, and either the per-iteration calls (select / cycle_vector /
+update, as the reference's loop makes them) or the blocked run.
+
+Streams are CUDA stream handles as integers (e.g. torch.cuda.current_stream().cuda_stream);
+0 is the legacy default stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._native import check_gpu, gpu_lib, ptr
+
+
+def _stream(s) -> C.c_void_p:
+    return C.c_void_p(int(s)) if s else None
+
+
+def device_info() -> dict:
+    lib = gpu_lib()
+    d, sm, mem = C.c_int(), C.c_int(), C.c_size_t()
+    check_gpu(lib.mcbgpu_init_cuda(C.byref(d), C.byref(sm), C.byref(mem)), "mcbgpu_init_cuda")
+    return {"device": d.value, "sm_count": sm.value, "total_global_mem": mem.value}
+
+
+class GpuStruct:
+    """gpu_struct drop-in: labels of every FVS tree for one support vector."""
+
+    def __init__(self, num_edges: int, num_coords: int, nodes: int, fvs_size: int, chunk_size: int = 720,
+                 nstreams: int = 1):
+        self.lib = gpu_lib()
+        self.n, self.F, self.chunk = nodes, fvs_size, chunk_size
+        self.size_vector = (num_coords + 63) // 64
+        self.rows = (fvs_size + chunk_size - 1) // chunk_size
+        h = C.c_void_p()
+        check_gpu(self.lib.mcbgpu_struct_create(C.byref(h), num_edges, num_coords, self.size_vector, nodes,
+                                                fvs_size, chunk_size, nstreams), "mcbgpu_struct_create")
+        self._h = h
+
+    def _rows_of(self, a: np.ndarray, per_tree: int):
+        """Split a tree-major array into the per-chunk host rows compressed_trees holds."""
+        ptrs = (C.c_void_p * max(self.rows, 1))()
+        keep = []
+        for r in range(self.rows):
+            t0 = r * self.chunk
+            part = np.ascontiguousarray(a[t0 * per_tree:min(self.F, t0 + self.chunk) * per_tree])
+            keep.append(part)
+            ptrs[r] = part.ctypes.data
+        return ptrs, keep
+
+    def initialize_memory(self, edge_coord: np.ndarray, level_offsets: np.ndarray, parent_pos: np.ndarray,
+                          edge_offset: np.ndarray) -> None:
+        n = self.n
+        eo, k1 = self._rows_of(np.asarray(edge_offset, np.int32), n)
+        lv, k2 = self._rows_of(np.asarray(level_offsets, np.uint32), n + 1)
+        pp, k3 = self._rows_of(np.asarray(parent_pos, np.uint32), n)
+        m = np.ascontiguousarray(edge_coord, np.int32)
+        check_gpu(self.lib.mcbgpu_struct_initialize_memory(self._h, ptr(m), eo, lv, pp),
+                  "mcbgpu_struct_initialize_memory")
+
+    def copy_support_vector(self, words: np.ndarray) -> float:
+        w = np.ascontiguousarray(words, np.uint64)
+        ms = C.c_float()
+        check_gpu(self.lib.mcbgpu_struct_copy_support_vector(self._h, ptr(w), C.byref(ms)),
+                  "mcbgpu_struct_copy_support_vector")
+        return ms.value
+
+    def process_shortest_path(self, fetch: bool = True):
+        """Returns (labels F x n uint32 in position order, milliseconds)."""
+        ms = C.c_float()
+        if not fetch:
+            check_gpu(self.lib.mcbgpu_struct_process_shortest_path(self._h, None, 0, C.byref(ms)),
+                      "mcbgpu_struct_process_shortest_path")
+            return None, ms.value
+        out = np.zeros(self.F * self.n, np.uint32)
+        ptrs = (C.c_void_p * max(self.rows, 1))()
+        for r in range(self.rows):
+            ptrs[r] = out.ctypes.data + r * self.chunk * self.n * 4
+        check_gpu(self.lib.mcbgpu_struct_process_shortest_path(self._h, ptrs, 0, C.byref(ms)),
+                  "mcbgpu_struct_process_shortest_path")
+        return out.reshape(self.F, self.n), ms.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            check_gpu(self.lib.mcbgpu_struct_clear_memory(self._h), "mcbgpu_struct_clear_memory")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """Device-resident de Pina loop over rank-ordered candidates."""
+
+    def __init__(self, num_coords: int, weight: np.ndarray, offsets: np.ndarray, coords: np.ndarray,
+                 stream=0, upload: bool = True):
+        self.lib = gpu_lib()
+        self.N = int(num_coords)
+        self.K = int(weight.shape[0])
+        self.weight = np.ascontiguousarray(weight, np.int32)
+        self.offsets = np.ascontiguousarray(offsets, np.int64)
+        self.coords = np.ascontiguousarray(coords, np.int32)
+        h = C.c_void_p()
+        check_gpu(self.lib.mcbgpu_solver_create(C.byref(h), self.N, self.K, int(self.offsets[-1])),
+                  "mcbgpu_solver_create")
+        self._h = h
+        if upload:
+            self.upload(stream)
+
+    @classmethod
+    def from_problem(cls, prob, stream=0) -> "Solver":
+        _, _, w, _ = prob.candidates()
+        off, co = prob.cycle_lists()
+        return cls(prob.N, w, off, co, stream)
+
+    def upload(self, stream=0, weight=None, offsets=None, coords=None) -> None:
+        w = self.weight if weight is None else weight
+        o = self.offsets if offsets is None else offsets
+        c = self.coords if coords is None else coords
+        check_gpu(self.lib.mcbgpu_solver_upload(self._h, ptr(w), ptr(o), ptr(c), _stream(stream)),
+                  "mcbgpu_solver_upload")
+
+    def reset(self, stream=0) -> None:
+        check_gpu(self.lib.mcbgpu_solver_reset(self._h, _stream(stream)), "mcbgpu_solver_reset")
+
+    # per-iteration form
+    def select(self, e: int, stream=0, fetch: bool = True):
+        r = C.c_int64()
+        check_gpu(self.lib.mcbgpu_select(self._h, e, C.byref(r) if fetch else None, _stream(stream)),
+                  "mcbgpu_select")
+        return r.value if fetch else None
+
+    def cycle_vector(self, e: int, stream=0) -> np.ndarray:
+        out = np.zeros((self.N + 63) // 64, np.uint64)
+        check_gpu(self.lib.mcbgpu_cycle_vector(self._h, e, ptr(out), _stream(stream)), "mcbgpu_cycle_vector")
+        return out
+
+    def update(self, e: int, stream=0) -> None:
+        check_gpu(self.lib.mcbgpu_update(self._h, e, _stream(stream)), "mcbgpu_update")
+
+    # whole-loop forms
+    def run(self, max_iterations: int = -1, stream=0) -> None:
+        check_gpu(self.lib.mcbgpu_solver_run(self._h, max_iterations, _stream(stream)), "mcbgpu_solver_run")
+
+    def run_plain(self, max_iterations: int = -1, stream=0) -> None:
+        check_gpu(self.lib.mcbgpu_solver_run_plain(self._h, max_iterations, _stream(stream)),
+                  "mcbgpu_solver_run_plain")
+
+    def results(self, count: int | None = None, stream=0):
+        """(selected ranks int64[count], total weight) after synchronising `stream`."""
+        count = self.N if count is None else count
+        sel = np.full(max(count, 1), -1, np.int64)
+        tot = C.c_int64()
+        check_gpu(self.lib.mcbgpu_solver_results(self._h, ptr(sel), count, C.byref(tot), _stream(stream)),
+                  "mcbgpu_solver_results")
+        return sel[:count], tot.value
+
+    def support_vector(self, j: int, stream=0) -> np.ndarray:
+        out = np.zeros((self.N + 63) // 64, np.uint64)
+        check_gpu(self.lib.mcbgpu_solver_get_support(self._h, j, ptr(out), _stream(stream)),
+                  "mcbgpu_solver_get_support")
+        return out
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.mcbgpu_solver_launches(self._h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.lib.mcbgpu_solver_device_bytes(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            check_gpu(self.lib.mcbgpu_solver_destroy(self._h), "mcbgpu_solver_destroy")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve(num_coords: int, weight: np.ndarray, offsets: np.ndarray, coords: np.ndarray):
+    """One-shot C-ABI call with host buffers: (selected[N], total weight)."""
+    lib = gpu_lib()
+    w = np.ascontiguousarray(weight, np.int32)
+    o = np.ascontiguousarray(offsets, np.int64)
+    c = np.ascontiguousarray(coords, np.int32)
+    sel = np.full(max(num_coords, 1), -1, np.int64)
+    tot = C.c_int64()
+    check_gpu(lib.mcbgpu_solve(num_coords, w.shape[0], ptr(w), ptr(o), ptr(c), ptr(sel), C.byref(tot)),
+              "mcbgpu_solve")
+    return sel[:num_coords], tot.value

@@ -1,0 +1,219 @@
+"""Host-side problem preparation (the mcb driver's steps before its main loop).
+
+Mirrors the reference driver's sequence (mcb/mcb_cycle_deg_two_remove.cpp:60-265):
+read a symmetric Matrix-Market graph, contract degree-two chains, compute the MGA
+feedback vertex set, the DFS spanning tree and its coordinate order, one Dijkstra
+tree per FVS root with its candidate cycles, and the sorted candidate list.  The
+work is done by libmcbhost.so; this module returns its arrays as numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._native import MCBHInfo, MCBHOptions, check_host, host_lib, ptr
+
+
+@dataclass
+class Graph:
+    """An undirected weighted graph as an edge list (0-based)."""
+    nodes: int
+    u: np.ndarray
+    v: np.ndarray
+    w: np.ndarray
+
+    @property
+    def m(self) -> int:
+        return int(self.u.shape[0])
+
+    def write_mtx(self, path: str) -> None:
+        check_host(host_lib().mcbh_write_mtx(path.encode(), self.nodes, self.m, ptr(self.u), ptr(self.v),
+                                             ptr(self.w)), "mcbh_write_mtx")
+
+
+def _edges(m: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    return np.empty(m, np.int32), np.empty(m, np.int32), np.empty(m, np.int32)
+
+
+def grid_graph(rows: int, cols: int, wlo: int = 1, whi: int = 100, seed: int = 1) -> Graph:
+    """rows x cols grid, row-major ids, right and down edges, weights U[wlo, whi]."""
+    lib = host_lib()
+    m = lib.mcbh_gen_grid(rows, cols, wlo, whi, seed, None, None, None)
+    if m < 0:
+        raise ValueError("bad grid parameters")
+    u, v, w = _edges(m)
+    lib.mcbh_gen_grid(rows, cols, wlo, whi, seed, ptr(u), ptr(v), ptr(w))
+    return Graph(rows * cols, u, v, w)
+
+
+def random_graph(n: int, m: int, wlo: int = 1, whi: int = 1000, seed: int = 1) -> Graph:
+    """Connected random sparse graph: random spanning tree plus uniform extra edges."""
+    lib = host_lib()
+    mm = lib.mcbh_gen_random(n, m, wlo, whi, seed, None, None, None)
+    if mm < 0:
+        raise ValueError("bad random-graph parameters")
+    u, v, w = _edges(mm)
+    lib.mcbh_gen_random(n, m, wlo, whi, seed, ptr(u), ptr(v), ptr(w))
+    return Graph(n, u, v, w)
+
+
+def rgg_graph(n: int, k: int = 4, seed: int = 1) -> Graph:
+    """Random geometric graph: k nearest neighbours in the unit square, w = round(1000*len)."""
+    lib = host_lib()
+    mm = lib.mcbh_gen_rgg(n, k, seed, None, None, None)
+    if mm < 0:
+        raise ValueError("bad rgg parameters")
+    u, v, w = _edges(mm)
+    lib.mcbh_gen_rgg(n, k, seed, ptr(u), ptr(v), ptr(w))
+    return Graph(n, u, v, w)
+
+
+class Problem:
+    """A graph prepared for the de Pina main loop.
+
+    Construct with Problem.from_mtx(path) or Problem.from_graph(graph), then
+    prepare(...).  Arrays are read back lazily and cached.
+    """
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+        self.prepared = False
+        self._cache: dict = {}
+
+    @classmethod
+    def from_mtx(cls, path: str) -> "Problem":
+        h = C.c_void_p()
+        check_host(host_lib().mcbh_problem_from_mtx(path.encode(), C.byref(h)), "mcbh_problem_from_mtx")
+        return cls(h)
+
+    @classmethod
+    def from_graph(cls, g: Graph) -> "Problem":
+        h = C.c_void_p()
+        u = np.ascontiguousarray(g.u, np.int32)
+        v = np.ascontiguousarray(g.v, np.int32)
+        w = np.ascontiguousarray(g.w, np.int32)
+        check_host(host_lib().mcbh_problem_from_edges(g.nodes, g.m, ptr(u), ptr(v), ptr(w), C.byref(h)),
+                   "mcbh_problem_from_edges")
+        return cls(h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            host_lib().mcbh_problem_free(h)
+            self._h = None
+
+    def prepare(self, threads: int = 0, contract_chains: bool = True, keep_trees: bool = False,
+                ref_layout: bool = False, cycle_lists: bool = True) -> "Problem":
+        opt = MCBHOptions(threads, int(contract_chains), int(keep_trees), int(ref_layout), int(cycle_lists))
+        check_host(host_lib().mcbh_prepare(self._h, C.byref(opt)), "mcbh_prepare")
+        self.prepared = True
+        self._opts = opt
+        return self
+
+    @property
+    def info(self) -> MCBHInfo:
+        i = MCBHInfo()
+        check_host(host_lib().mcbh_get_info(self._h, C.byref(i)), "mcbh_get_info")
+        return i
+
+    # sizes
+    @property
+    def n(self) -> int:
+        return self.info.reduced_nodes
+
+    @property
+    def N(self) -> int:
+        return self.info.num_coords
+
+    @property
+    def K(self) -> int:
+        return self.info.num_candidates
+
+    @property
+    def F(self) -> int:
+        return self.info.fvs_size
+
+    def _get(self, key, fn):
+        if key not in self._cache:
+            self._cache[key] = fn()
+        return self._cache[key]
+
+    def reduced_graph(self):
+        def f():
+            i = self.info
+            m2, n = i.reduced_edges2, i.reduced_nodes
+            rows = np.empty(m2, np.uint32)
+            cols = np.empty(m2, np.uint32)
+            w = np.empty(m2, np.int32)
+            rev = np.empty(m2, np.uint32)
+            ro = np.empty(n + 1, np.uint32)
+            check_host(host_lib().mcbh_get_reduced_graph(self._h, ptr(rows), ptr(cols), ptr(w), ptr(rev), ptr(ro)),
+                       "mcbh_get_reduced_graph")
+            return rows, cols, w, rev, ro
+        return self._get("graph", f)
+
+    def fvs(self):
+        def f():
+            i = self.info
+            fa = np.empty(i.reduced_nodes, np.int32)
+            fv = np.empty(i.fvs_size, np.uint32)
+            check_host(host_lib().mcbh_get_fvs(self._h, ptr(fa), ptr(fv)), "mcbh_get_fvs")
+            return fa, fv
+        return self._get("fvs", f)
+
+    def coords(self):
+        def f():
+            i = self.info
+            ce = np.empty(i.num_coords, np.uint32)
+            ec = np.empty(i.reduced_edges2, np.int32)
+            check_host(host_lib().mcbh_get_coords(self._h, ptr(ce), ptr(ec)), "mcbh_get_coords")
+            return ce, ec
+        return self._get("coords", f)
+
+    def candidates(self):
+        """(root, edge_offset, weight, tree) in rank order."""
+        def f():
+            K = self.info.num_candidates
+            a = [np.empty(K, np.int32) for _ in range(4)]
+            check_host(host_lib().mcbh_get_candidates(self._h, *[ptr(x) for x in a]), "mcbh_get_candidates")
+            return tuple(a)
+        return self._get("cands", f)
+
+    def cycle_lists(self):
+        """(offsets[K+1] int64, coords[nnz] int32)."""
+        def f():
+            i = self.info
+            off = np.empty(i.num_candidates + 1, np.int64)
+            co = np.empty(i.cycle_nnz, np.int32)
+            check_host(host_lib().mcbh_get_cycle_lists(self._h, ptr(off), ptr(co)), "mcbh_get_cycle_lists")
+            return off, co
+        return self._get("lists", f)
+
+    def tree_parents(self):
+        def f():
+            i = self.info
+            tp = np.empty(i.fvs_size * i.reduced_nodes, np.int32)
+            check_host(host_lib().mcbh_get_tree_parents(self._h, ptr(tp)), "mcbh_get_tree_parents")
+            return tp
+        return self._get("parents", f)
+
+    def ref_layout(self):
+        """(level_offsets F x (n+1), parent_pos F x n, edge_offset F x n, nodes_index F x n)."""
+        def f():
+            i = self.info
+            F, n = i.fvs_size, i.reduced_nodes
+            lv = np.empty(F * (n + 1), np.uint32)
+            pp = np.empty(F * n, np.uint32)
+            eo = np.empty(F * n, np.int32)
+            ni = np.empty(F * n, np.uint32)
+            check_host(host_lib().mcbh_get_ref_layout(self._h, ptr(lv), ptr(pp), ptr(eo), ptr(ni)),
+                       "mcbh_get_ref_layout")
+            return lv, pp, eo, ni
+        return self._get("layout", f)
+
+    def total_weight(self, selected: np.ndarray) -> int:
+        """64-bit total weight of the selected candidate ranks."""
+        _, _, w, _ = self.candidates()
+        return int(w[np.asarray(selected, np.int64)].astype(np.int64).sum())

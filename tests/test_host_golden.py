@@ -1,0 +1,99 @@
+"""Host preparation vs the reference's own outputs (golden vectors made by
+tests/golden/make_golden.py from the reference binaries)."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from minimumcyclebasis_gb300 import Problem
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, np.int32).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_prepare_matches_reference(name):
+    fx = load_golden(name)
+    p = Problem.from_mtx(fx["mtx"]).prepare(threads=2)
+    i = p.info
+    G = fx["G"]
+    assert i.nodes == G["nodes"]
+    assert i.edges2 == G["edges2"]
+    assert i.nodes_removed == G["nodes_removed"]
+    assert i.reduced_nodes == G["reduced_nodes"]
+    assert i.reduced_edges2 == G["reduced_edges2"]
+    assert i.fvs_size == G["fvs_size"]
+    assert i.num_coords == G["num_coords"]
+    assert i.num_candidates == G["num_candidates"]
+    _, fv = p.fvs()
+    assert fv.tolist() == fx["fvs_vertices"]
+    ce, ec = p.coords()
+    assert ce.tolist() == fx["coord_edges"]
+    root, edge, w, tree = p.candidates()
+    assert sha(root) == fx["candidates_sha256"]["root"]
+    assert sha(edge) == fx["candidates_sha256"]["edge"]
+    assert sha(w) == fx["candidates_sha256"]["weight"]
+    if "candidates" in fx:
+        assert root.tolist() == fx["candidates"]["root"]
+        assert edge.tolist() == fx["candidates"]["edge"]
+        assert w.tolist() == fx["candidates"]["weight"]
+    # the stats CSV of the reference CPU driver agrees on the counts
+    csv = fx["mcb_cpu_csv"]
+    assert int(csv["Fvs_size"]) == i.fvs_size
+    assert int(csv["Initial_Cycles"]) == i.num_candidates
+    assert int(csv["Node_removed"]) == i.nodes_removed
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_cycle_lists_are_sorted_coordinate_sets(name):
+    fx = load_golden(name)
+    p = Problem.from_mtx(fx["mtx"]).prepare(threads=2, keep_trees=True)
+    off, co = p.cycle_lists()
+    assert off[0] == 0 and off[-1] == co.shape[0]
+    assert np.all(np.diff(off) >= 0)
+    assert co.size == 0 or (co.min() >= 0 and co.max() < p.N)
+    # strictly ascending inside each list
+    d = np.diff(co)
+    starts = np.zeros(co.shape[0], bool)
+    starts[off[:-1][off[:-1] < co.shape[0]]] = True
+    assert np.all((d > 0) | starts[1:])
+    # lists equal the reference's get_cycle_vector (include/cycles.h:144-195) on a sample
+    import oracle
+    rng = np.random.default_rng(0)
+    for r in rng.choice(p.K, size=min(p.K, 25), replace=False):
+        words = oracle.cycle_vector(p, int(r))
+        bits = [c for c in range(p.N) if (int(words[c >> 6]) >> (c & 63)) & 1]
+        assert bits == co[off[r]:off[r + 1]].tolist()
+
+
+def test_threads_do_not_change_the_order():
+    fx = load_golden("rand2000_w20_s11")
+    a = Problem.from_mtx(fx["mtx"]).prepare(threads=1)
+    b = Problem.from_mtx(fx["mtx"]).prepare(threads=8)
+    for x, y in zip(a.candidates(), b.candidates()):
+        assert np.array_equal(x, y)
+    for x, y in zip(a.cycle_lists(), b.cycle_lists()):
+        assert np.array_equal(x, y)
+
+
+def test_reference_layout_is_level_ordered():
+    fx = load_golden("grid8x8_s3")
+    p = Problem.from_mtx(fx["mtx"]).prepare(ref_layout=True, keep_trees=True)
+    lv, pp, eo, ni = p.ref_layout()
+    n, F = p.n, p.F
+    rows, cols, _, _, _ = p.reduced_graph()
+    tp = p.tree_parents()
+    for t in range(F):
+        L = lv[t * (n + 1):(t + 1) * (n + 1)]
+        P = pp[t * n:(t + 1) * n]
+        E = eo[t * n:(t + 1) * n]
+        NI = ni[t * n:(t + 1) * n]
+        assert L[0] == 0 and L[1] == 1 and L[n] == n
+        assert E[0] == -1
+        for pos in range(1, n):
+            assert P[pos] < pos
+            child = cols[E[pos]]
+            assert NI[child] == pos
+            assert tp[t * n + child] == E[pos]
