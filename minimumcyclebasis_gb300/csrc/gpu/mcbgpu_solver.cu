@@ -50,7 +50,9 @@ struct IterSlot {            // state of one per-iteration search
 };
 
 struct BlockState {
-    unsigned next_tile, frontier, rank, stop, epoch, b, npairs, pad;
+    unsigned rank, epoch, b, npairs;
+    long long last_pivot;          // rank of the previous block's last pivot
+    long long pred_tiles;          // tiles the streaming pass computes for this block
     unsigned long long total;      // running 64-bit total weight of the basis
     unsigned long long basis[64];  // reduced row-echelon basis of the pivot W's
     unsigned pivbit[64];
@@ -59,6 +61,11 @@ struct BlockState {
     unsigned long long mask[64];   // final S_{e0+k} as a combination of S^0_{e0+l}
     unsigned long long gcol[64];   // gcol[k] bit i = <C_sel_k, S_{e0+i}>, i < k
     int sel[64];                   // pivot chosen at iteration e0+k
+};
+
+// Grid barrier state of the cooperative pivot kernel (see grid_barrier).
+struct GridBar {
+    unsigned count, gen, abort, pad;
 };
 
 // ---------------------------------------------------------------------------
@@ -78,6 +85,27 @@ __global__ void reset_state_kernel(IterSlot *slots, BlockState *bs, unsigned *st
         slots[1].next_tile = 0;
         bs->total = 0;  // epoch keeps counting across runs: old tile marks never match
         *status = 0;
+    }
+}
+
+// Smallest first coordinate per tile of 1024 candidates (lists are ascending, so a
+// tile whose value is >= the block's bound has W = 0 for every candidate).
+__global__ void tile_minc_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ coords, long long K,
+                                 int32_t *tile_minc, long long ntiles) {
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int m = 0x7fffffff;
+        for (long long r = t * kTile + threadIdx.x; r < K && r < (t + 1) * kTile; r += blockDim.x)
+            if (off[r + 1] > off[r]) m = min(m, coords[off[r]]);
+        for (int d = 16; d > 0; d >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, d));
+        __shared__ int sm[32];
+        if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int v = sm[0];
+            for (int w = 1; w < (int)(blockDim.x >> 5); w++) v = min(v, sm[w]);
+            tile_minc[t] = v;
+        }
+        __syncthreads();
     }
 }
 
@@ -194,15 +222,21 @@ __global__ void cycle_vector_kernel(uint64_t *C, int W, const int64_t *__restric
 // blk_transpose_kernel: T[64w + i] bit k = S[e0+k] bit (64w+i), for w < Wb.
 // One warp per word column; also resets the block state (runs first in the block).
 __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int e0, int b, int Wb,
-                                     uint64_t *__restrict__ T, BlockState *bs) {
+                                     uint64_t *__restrict__ T, BlockState *bs, long long ntiles,
+                                     GridBar *gb, unsigned long long *gmin) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        bs->next_tile = 0;
-        bs->frontier = 0;
+        gb->count = 0;
+        gb->abort = 0;
+        gmin[0] = kNone;
         bs->rank = 0;
-        bs->stop = 0;
         bs->epoch = bs->epoch + 1;
         bs->b = (unsigned)b;
         bs->npairs = 0;
+        // stream 25% past the previous block's deepest pivot; the pivot kernel
+        // computes any further tile it needs
+        long long lp = e0 == 0 ? ntiles * kTile : bs->last_pivot + 1;
+        long long pred = (lp + lp / 4) / kTile + 8;
+        bs->pred_tiles = pred < ntiles ? pred : ntiles;
     }
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -251,164 +285,218 @@ __device__ void fr_build(uint64_t (*tab)[256], const uint64_t *basis, const unsi
     __syncthreads();
 }
 
-// The pivot sweep.  Candidates are taken in tiles of 1024, in rank order, by a
-// persistent grid.  A tile's W's are reduced against the latest basis the CTA has
-// seen; if all reduce to zero the tile holds no pivot (its W's are in the span of
-// pivots of earlier ranks) and it is marked EMPTY at once.  Otherwise the CTA waits
-// until every earlier tile is EMPTY or RESOLVED (the frontier), re-reduces against
-// the then-final basis and extracts its pivots in rank order, publishes the basis,
-// and marks the tile RESOLVED.  The sweep stops once the basis has rank b.
-__global__ void __launch_bounds__(kScanThreads) blk_scan_kernel(
-    const uint64_t *__restrict__ T, int bound, const int64_t *__restrict__ off,
-    const int32_t *__restrict__ coords, long long K, BlockState *bs, unsigned *tstatus, unsigned *status) {
-    __shared__ uint64_t tab[8][256];
-    __shared__ uint64_t sW[kTile];
-    __shared__ uint64_t sR[kTile];
-    __shared__ uint64_t sbasis[64];
-    __shared__ unsigned spiv[64];
-    __shared__ unsigned s_tile, s_stop, s_rank, s_min, s_fail;
-    const unsigned epoch = *((volatile unsigned *)&bs->epoch);
-    const unsigned b = *((volatile unsigned *)&bs->b);
-    const long long ntiles = (K + kTile - 1) / kTile;
-    unsigned snap = 0xFFFFFFFFu;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            s_stop = ld_acquire_u32(&bs->stop);
-            s_tile = s_stop ? 0u : atomicAdd(&bs->next_tile, 1u);
-            s_rank = ld_acquire_u32(&bs->rank);
-        }
-        __syncthreads();
-        if (s_stop) break;
-        const unsigned tile = s_tile;
-        if ((long long)tile >= ntiles) break;  // nobody waits on tiles past the end
-        // refresh the snapshot of the basis when it grew
-        if (s_rank != snap) {
-            unsigned rk = s_rank;
-            for (unsigned q = threadIdx.x; q < rk; q += blockDim.x) {
-                sbasis[q] = __ldcg(&bs->basis[q]);
-                spiv[q] = __ldcg(&bs->pivbit[q]);
-            }
-            __syncthreads();
-            fr_build(tab, sbasis, spiv, rk);
-            snap = rk;
-        }
-        const long long r0 = (long long)tile * kTile;
-        int any = 0;
-#pragma unroll
-        for (int q = 0; q < kPer; q++) {
-            const int li = q * kScanThreads + threadIdx.x;
-            const long long r = r0 + li;
-            uint64_t W = 0;
-            if (r < K) {
-                const int64_t e1 = off[r + 1];
-                for (int64_t i = off[r]; i < e1; i++) {
-                    int c = __ldg(coords + i);
-                    if (c >= bound) break;
-                    W ^= __ldg(T + c);
-                }
-            }
-            sW[li] = W;
-            uint64_t R = fr_reduce(W, tab);
-            sR[li] = R;
-            any |= (R != 0);
-        }
-        if (!__syncthreads_or(any)) {
-            if (threadIdx.x == 0) st_release_u32(&tstatus[tile], (epoch << 2) | 1u);
-            continue;
-        }
-        // wait until all earlier tiles are done
-        if (threadIdx.x == 0) {
-            s_fail = 0;
-            unsigned f = ld_acquire_u32(&bs->frontier);
+// ---- grid-wide barrier for the cooperative pivot kernel ----------------------
+// All CTAs of a cooperative launch are co-resident.  The wait is bounded: after
+// kSpinLimit polls a CTA raises `abort`, every waiter sees it and the kernel ends
+// with ST_WAIT_TIMEOUT instead of hanging.
+
+__device__ bool grid_barrier(GridBar *gb, unsigned nctas, unsigned &gen_local) {
+    __shared__ unsigned s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned ok = 1;
+        const unsigned g = gen_local;
+        __threadfence();
+        if (atomicAdd(&gb->count, 1u) == nctas - 1) {
+            atomicExch(&gb->count, 0u);
+            __threadfence();
+            st_release_u32(&gb->gen, g + 1);
+        } else {
             unsigned spins = 0;
-            while (f < tile) {
-                unsigned st = ld_acquire_u32(&tstatus[f]);
-                if ((st >> 2) == epoch && (st & 3u)) {
-                    f++;
-                    continue;
+            while (ld_acquire_u32(&gb->gen) == g) {
+                if (*((volatile unsigned *)&gb->abort)) {
+                    ok = 0;
+                    break;
                 }
                 if (++spins > kSpinLimit) {
-                    s_fail = 1;
+                    atomicExch(&gb->abort, 1u);
+                    ok = 0;
                     break;
                 }
-                __nanosleep(64);
-            }
-            if (!s_fail) {
-                __threadfence();
-                atomicMax(&bs->frontier, f);
-                s_rank = ld_acquire_u32(&bs->rank);
+                __nanosleep(20);
             }
         }
-        __syncthreads();
-        if (s_fail) {
-            if (threadIdx.x == 0) {
-                atomicOr(status, ST_WAIT_TIMEOUT);
-                st_release_u32(&bs->stop, 1u);
-                st_release_u32(&tstatus[tile], (epoch << 2) | 2u);
+        gen_local = g + 1;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// W of one tile of 1024 candidates into sW (shared), computed by the whole CTA:
+//   W_r = XOR of T[c] over the coordinates c < bound of candidate r.
+// The tile's coordinates are one contiguous run of `coords`; threads read it with
+// 16-byte loads (coalesced), find each element's candidate from the tile's offsets
+// held in shared memory, and fold runs of the same candidate into one shared
+// atomicXor.  A tile whose smallest coordinate is >= bound has W = 0 throughout.
+__device__ void compute_w_tile(long long tile, long long K, const int64_t *__restrict__ off,
+                               const int32_t *__restrict__ coords, const int32_t *__restrict__ tile_minc,
+                               const uint64_t *__restrict__ T, int bound, uint64_t *sW, int64_t *soff) {
+    const long long r0 = tile * kTile;
+    const int rn = (int)((K - r0) < kTile ? (K - r0) : kTile);
+    for (int i = threadIdx.x; i < kTile; i += blockDim.x) sW[i] = 0;
+    const bool skip = tile_minc[tile] >= bound;
+    if (!skip)
+        for (int i = threadIdx.x; i <= rn; i += blockDim.x) soff[i] = off[r0 + i];
+    __syncthreads();
+    if (skip) return;
+    const int64_t cb = soff[0], ce = soff[rn];
+    for (int64_t i4 = (cb & ~(int64_t)3) + 4 * (int64_t)threadIdx.x; i4 < ce; i4 += 4 * (int64_t)blockDim.x) {
+        const int4 v = *reinterpret_cast<const int4 *>(coords + i4);
+        const int vals[4] = {v.x, v.y, v.z, v.w};
+        int64_t first = i4 < cb ? cb : i4;
+        // candidate owning index `first`: last j with soff[j] <= first
+        int lo = 0, hi = rn - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (soff[mid] <= first)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        int j = lo;
+        uint64_t acc = 0;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int64_t i = i4 + e;
+            if (i < cb || i >= ce) continue;
+            while (soff[j + 1] <= i) {
+                if (acc) atomicXor((unsigned long long *)&sW[j], (unsigned long long)acc);
+                acc = 0;
+                j++;
             }
+            const int c = vals[e];
+            if (c < bound) acc ^= __ldg(T + c);
+        }
+        if (acc) atomicXor((unsigned long long *)&sW[j], (unsigned long long)acc);
+    }
+    __syncthreads();
+}
+
+// Streaming pass: W for tiles [0, bs->pred_tiles), written to Warr and tagged with
+// the block's epoch.  This is the bandwidth-bound part of the block's search.
+__global__ void __launch_bounds__(kScanThreads) blk_w_kernel(long long K, const int64_t *__restrict__ off,
+                                                             const int32_t *__restrict__ coords,
+                                                             const int32_t *__restrict__ tile_minc,
+                                                             const uint64_t *__restrict__ T, int bound,
+                                                             const BlockState *bs, uint64_t *Warr,
+                                                             unsigned *tile_epoch) {
+    __shared__ uint64_t sW[kTile];
+    __shared__ int64_t soff[kTile + 1];
+    const unsigned epoch = bs->epoch;
+    const long long ntiles = bs->pred_tiles;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        compute_w_tile(t, K, off, coords, tile_minc, T, bound, sW, soff);
+        const long long r0 = t * kTile;
+        for (int i = threadIdx.x; i < kTile; i += blockDim.x) Warr[r0 + i] = sW[i];
+        __syncthreads();
+        if (threadIdx.x == 0) tile_epoch[t] = epoch;
+    }
+}
+
+// Cooperative pivot extraction.  Step k finds the next pivot exactly: the first
+// candidate at or after the previous pivot whose W is not in the span of the
+// pivots found so far (every candidate before it is in that span, so the first
+// non-zero residual is the next rank-ordered independent W).  CTAs scan tiles from
+// the previous pivot onward (tile t by CTA t mod G), reducing W with their own
+// copy of the basis held as Four-Russians tables, and the first non-zero residual
+// is found with a ballot per warp and atomicMin across the grid; one grid barrier
+// per step.  Tiles outside the streamed range are computed here and cached.
+__global__ void __launch_bounds__(kScanThreads) blk_pivot_kernel(
+    long long K, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
+    const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T, int bound, BlockState *bs,
+    uint64_t *Warr, unsigned *tile_epoch, unsigned long long *gmin, GridBar *gb, unsigned *status) {
+    __shared__ uint64_t tab[8][256];
+    __shared__ uint64_t sW[kTile];
+    __shared__ int64_t soff[kTile + 1];
+    __shared__ uint64_t sbasis[64];
+    __shared__ unsigned spiv[64];
+    __shared__ unsigned s_go, s_found;
+    __shared__ unsigned long long s_min;
+    const unsigned epoch = bs->epoch;
+    const int b = (int)bs->b;
+    const long long ntiles = (K + kTile - 1) / kTile;
+    const unsigned G = gridDim.x;
+    unsigned gen = ld_acquire_u32(&gb->gen);
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&tab[0][0])[i] = 0;
+    __syncthreads();
+    long long s = 0;
+    int rank = 0;
+    bool ok = true;
+    for (int k = 0; k < b; k++) {
+        unsigned long long *slot = gmin + (k % 3);
+        if (blockIdx.x == 0 && threadIdx.x == 0) gmin[(k + 1) % 3] = kNone;
+        const long long t0 = s / kTile;
+        for (long long t = t0 + blockIdx.x; t < ntiles; t += G) {
+            if (threadIdx.x == 0) s_go = (unsigned long long)(t * kTile) <= *((volatile unsigned long long *)slot);
+            __syncthreads();
+            if (!s_go) break;
+            const long long r0 = t * kTile;
+            if (*((volatile unsigned *)&tile_epoch[t]) == epoch) {
+                for (int i = threadIdx.x; i < kTile; i += blockDim.x) sW[i] = (r0 + i < K) ? __ldcg(Warr + r0 + i) : 0;
+                __syncthreads();
+            } else {
+                compute_w_tile(t, K, off, coords, tile_minc, T, bound, sW, soff);
+                for (int i = threadIdx.x; i < kTile; i += blockDim.x) Warr[r0 + i] = sW[i];
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    __threadfence();
+                    tile_epoch[t] = epoch;
+                }
+            }
+            if (threadIdx.x == 0) {
+                s_min = kNone;
+                s_found = 0;
+            }
+            __syncthreads();
+            // rank order inside the tile = index order; warp w covers [32w, 32w+32) of each quarter
+#pragma unroll
+            for (int q = 0; q < kPer; q++) {
+                const int li = q * kScanThreads + threadIdx.x;
+                const bool nz = fr_reduce(sW[li], tab) != 0 && (r0 + li) >= s;
+                const unsigned bal = __ballot_sync(0xffffffffu, nz);
+                if (bal && (threadIdx.x & 31) == 0)
+                    atomicMin(&s_min, (unsigned long long)(r0 + q * kScanThreads + (threadIdx.x & ~31) + __ffs(bal) - 1));
+            }
+            __syncthreads();
+            if (s_min != kNone) {
+                if (threadIdx.x == 0) atomicMin(slot, s_min);
+                break;
+            }
+        }
+        if (!grid_barrier(gb, G, gen)) {
+            ok = false;
             break;
         }
-        // the basis is now stable: reload it, re-reduce, extract pivots in order
-        unsigned rk = s_rank;
-        for (unsigned q = threadIdx.x; q < rk; q += blockDim.x) {
-            sbasis[q] = __ldcg(&bs->basis[q]);
-            spiv[q] = __ldcg(&bs->pivbit[q]);
+        const unsigned long long p = *((volatile unsigned long long *)slot);
+        if (p == kNone) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, ST_RANK_DEFICIT);
+            ok = false;
+            break;
         }
-        __syncthreads();
-        fr_build(tab, sbasis, spiv, rk);
-        for (int q = 0; q < kPer; q++) {
-            const int li = q * kScanThreads + threadIdx.x;
-            sR[li] = fr_reduce(sW[li], tab);
-        }
-        __syncthreads();
-        const unsigned rk0 = rk;
-        while (rk < b) {
-            if (threadIdx.x == 0) s_min = 0xFFFFFFFFu;
-            __syncthreads();
-            for (int q = 0; q < kPer; q++) {
-                const int li = q * kScanThreads + threadIdx.x;
-                unsigned bal = __ballot_sync(0xffffffffu, sR[li] != 0);
-                if (bal) {
-                    if ((threadIdx.x & 31) == 0) atomicMin(&s_min, (unsigned)(q * kScanThreads + (threadIdx.x & ~31) + __ffs(bal) - 1));
-                    break;
-                }
-            }
-            __syncthreads();
-            const unsigned mi = s_min;
-            if (mi == 0xFFFFFFFFu) break;
-            const uint64_t v = sR[mi];
-            const unsigned p = (unsigned)(__ffsll((long long)v) - 1);
-            __syncthreads();
-            // keep the basis reduced: clear bit p from the other vectors
-            for (unsigned q = threadIdx.x; q < rk; q += blockDim.x)
-                if ((sbasis[q] >> p) & 1ull) sbasis[q] ^= v;
-            if (threadIdx.x == 0) {
-                sbasis[rk] = v;
-                spiv[rk] = p;
-                bs->pivrank[rk] = r0 + mi;
-                bs->pivW[rk] = sW[mi];
-            }
-            for (int q = 0; q < kPer; q++) {
-                const int li = q * kScanThreads + threadIdx.x;
-                if ((sR[li] >> p) & 1ull) sR[li] ^= v;
-            }
-            rk++;
-            __syncthreads();
-        }
-        // publish
-        for (unsigned q = threadIdx.x; q < rk; q += blockDim.x) {
-            bs->basis[q] = sbasis[q];
-            bs->pivbit[q] = spiv[q];
-        }
+        const uint64_t Wp = __ldcg(Warr + p);
+        const uint64_t v = fr_reduce(Wp, tab);
+        const unsigned qb = (unsigned)(__ffsll((long long)v) - 1);
+        // keep the basis reduced: clear bit qb from the others, append v
+        if (threadIdx.x < (unsigned)rank && ((sbasis[threadIdx.x] >> qb) & 1ull)) sbasis[threadIdx.x] ^= v;
         __syncthreads();
         if (threadIdx.x == 0) {
-            __threadfence();
-            if (rk != rk0) st_release_u32(&bs->rank, rk);
-            if (rk >= b) st_release_u32(&bs->stop, 1u);
-            st_release_u32(&tstatus[tile], (epoch << 2) | 2u);
+            sbasis[rank] = v;
+            spiv[rank] = qb;
+            if (blockIdx.x == 0) {
+                bs->pivrank[rank] = (long long)p;
+                bs->pivW[rank] = Wp;
+            }
         }
-        snap = 0xFFFFFFFFu;  // the reduced vectors changed: rebuild next time
+        rank++;
         __syncthreads();
+        fr_build(tab, sbasis, spiv, (unsigned)rank);
+        s = (long long)p + 1;
+    }
+    if (!ok && threadIdx.x == 0 && (*((volatile unsigned *)&gb->abort))) atomicOr(status, ST_WAIT_TIMEOUT);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        bs->rank = (unsigned)rank;
+        bs->last_pivot = s - 1;
     }
 }
 
@@ -603,7 +691,12 @@ struct mcbgpu_solver {
     uint64_t *d_C = nullptr;       // cycle vector buffer (W words)
     uint64_t *d_T = nullptr;       // 64 * P words
     uint64_t *d_tab = nullptr;     // 8 * 256 * P words
-    unsigned *d_tstatus = nullptr; // tiles + 1
+    uint64_t *d_Warr = nullptr;    // W per candidate (tiles * 1024)
+    unsigned *d_tile_epoch = nullptr;
+    int32_t *d_tile_minc = nullptr;
+    unsigned long long *d_gmin = nullptr;  // 3 slots
+    GridBar *d_gbar = nullptr;
+    int pivot_grid = 0;
     unsigned *d_pairs = nullptr;
     unsigned pair_cap = 0;
     IterSlot *d_slots = nullptr;   // 2
@@ -627,7 +720,11 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_C);
     cudaFree(s->d_T);
     cudaFree(s->d_tab);
-    cudaFree(s->d_tstatus);
+    cudaFree(s->d_Warr);
+    cudaFree(s->d_tile_epoch);
+    cudaFree(s->d_tile_minc);
+    cudaFree(s->d_gmin);
+    cudaFree(s->d_gbar);
     cudaFree(s->d_pairs);
     cudaFree(s->d_slots);
     cudaFree(s->d_bs);
@@ -687,18 +784,30 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     } while (0)
     ALLOC(s->d_weight, sizeof(int32_t) * (size_t)K);
     ALLOC(s->d_off, sizeof(int64_t) * (size_t)(K + 1));
-    ALLOC(s->d_coords, sizeof(int32_t) * (size_t)nnz);
+    ALLOC(s->d_coords, sizeof(int32_t) * (size_t)(nnz + 4));  // 16-byte loads may read 3 past the end
     ALLOC(s->d_S, sizeof(uint64_t) * (size_t)N * s->P);
     ALLOC(s->d_C, sizeof(uint64_t) * (size_t)s->P);
     ALLOC(s->d_T, sizeof(uint64_t) * 64 * (size_t)s->P);
     ALLOC(s->d_tab, sizeof(uint64_t) * 8 * 256 * (size_t)s->P);
-    ALLOC(s->d_tstatus, sizeof(unsigned) * ntiles);
+    ALLOC(s->d_Warr, sizeof(uint64_t) * (size_t)kTile * ntiles);
+    ALLOC(s->d_tile_epoch, sizeof(unsigned) * ntiles);
+    ALLOC(s->d_tile_minc, sizeof(int32_t) * ntiles);
+    ALLOC(s->d_gmin, sizeof(unsigned long long) * 4);
+    ALLOC(s->d_gbar, sizeof(GridBar));
     ALLOC(s->d_slots, sizeof(IterSlot) * 2);
     ALLOC(s->d_bs, sizeof(BlockState));
     ALLOC(s->d_selected, sizeof(long long) * (size_t)(N > 0 ? N : 1));
     ALLOC(s->d_status, sizeof(unsigned));
 #undef ALLOC
-    if (e == cudaSuccess) e = cudaMemset(s->d_tstatus, 0, sizeof(unsigned) * ntiles);
+    if (e == cudaSuccess) e = cudaMemset(s->d_tile_epoch, 0, sizeof(unsigned) * ntiles);
+    if (e == cudaSuccess) e = cudaMemset(s->d_gbar, 0, sizeof(GridBar));
+    if (e == cudaSuccess) e = cudaMemset(s->d_coords, 0, sizeof(int32_t) * (size_t)(nnz + 4));
+    if (e == cudaSuccess) {
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blk_pivot_kernel, kScanThreads, 0);
+        if (per_sm > 1) per_sm = 1;
+        s->pivot_grid = per_sm * (s->sm_count > 0 ? s->sm_count : 1);
+    }
     if (e == cudaSuccess) e = cudaMemset(s->d_bs, 0, sizeof(BlockState));
     if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(unsigned));
     if (e != cudaSuccess) {
@@ -776,6 +885,13 @@ int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t 
     }
     if (s->nnz > 0)
         MCB_CUDA(cudaMemcpyAsync(s->d_coords, coords, sizeof(int32_t) * (size_t)s->nnz, cudaMemcpyHostToDevice, st));
+    const long long ntiles = (s->K + kTile - 1) / kTile;
+    if (ntiles > 0) {
+        int grid = (int)std::min<long long>(ntiles, (long long)(s->sm_count > 0 ? s->sm_count : 148) * 8);
+        tile_minc_kernel<<<grid, 256, 0, st>>>(s->d_off, s->d_coords, s->K, s->d_tile_minc, ntiles);
+        MCB_CUDA(cudaGetLastError());
+        s->launches++;
+    }
     s->uploaded = true;
     return mcbgpu_solver_reset(s, stream);
 }
@@ -883,22 +999,35 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
     const int64_t iters = (max_iterations >= 0 && max_iterations < s->N) ? max_iterations : s->N;
     const int sms = s->sm_count > 0 ? s->sm_count : 148;
     long long ntiles = (s->K + kTile - 1) / kTile;
-    int scan_grid = sms * 3;
-    if (ntiles + 1 < scan_grid) scan_grid = (int)(ntiles + 1);
     for (int64_t e0 = 0; e0 < iters; e0 += 64) {
         const int b = (int)std::min<int64_t>(64, iters - e0);
         const int Wb = (int)((e0 + b + 63) / 64);
+        const int bound = (int)(e0 + b);
+        blk_transpose_kernel<<<(Wb + 7) / 8, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles,
+                                                          s->d_gbar, s->d_gmin);
+        if (ntiles > 0)
+            blk_w_kernel<<<sms * 4, kScanThreads, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                                                          s->d_bs, s->d_Warr, s->d_tile_epoch);
         {
-            int warps = Wb;
-            int grid = (warps + 7) / 8;
-            blk_transpose_kernel<<<grid, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs);
+            long long K = s->K;
+            const int64_t *off = s->d_off;
+            const int32_t *co = s->d_coords;
+            const int32_t *tm = s->d_tile_minc;
+            const uint64_t *T = s->d_T;
+            BlockState *bs = s->d_bs;
+            uint64_t *Wa = s->d_Warr;
+            unsigned *te = s->d_tile_epoch;
+            unsigned long long *gm = s->d_gmin;
+            GridBar *gb = s->d_gbar;
+            unsigned *stt = s->d_status;
+            void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &gm, &gb, &stt};
+            MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kScanThreads),
+                                                 args, 0, st));
         }
-        blk_scan_kernel<<<scan_grid, kScanThreads, 0, st>>>(s->d_T, (int)(e0 + b), s->d_off, s->d_coords, s->K,
-                                                            s->d_bs, s->d_tstatus, s->d_status);
         blk_resolve_kernel<<<1, 32, 0, st>>>(s->d_bs, (int)e0, s->d_off, s->d_coords, s->d_weight, s->d_selected,
                                              s->d_pairs, s->pair_cap, s->d_status);
         blk_materialize_kernel<<<(Wb + 31) / 32, 256, 0, st>>>(s->d_S, s->P, (int)e0, Wb, s->d_bs);
-        s->launches += 4;
+        s->launches += 5;
         if (e0 + b < s->N) {
             int tgrid = (8 * Wb + 255) / 256;
             blk_tables_kernel<<<tgrid, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->P, s->d_tab);

@@ -18,7 +18,7 @@ def big():
 
 
 def dot(words, coords):
-    return int(sum((int(words[c >> 6]) >> (c & 63)) & 1 for c in coords) & 1)
+    return int(sum((int(words[c >> 6]) >> (c & 63)) & 1 for c in np.asarray(coords).tolist()) & 1)
 
 
 def test_blocked_equals_plain_and_invariants(big):
@@ -31,11 +31,11 @@ def test_blocked_equals_plain_and_invariants(big):
     assert tot == int(w[sel].astype(np.int64).sum())
     off, co = p.cycle_lists()
     rng = np.random.default_rng(3)
-    for j in rng.choice(p.N, 12, replace=False):
-        Sj = s.support_vector(int(j))
+    for j in rng.choice(p.N, 12, replace=False).tolist():
+        Sj = s.support_vector(j)
         cj = co[off[sel[j]]:off[sel[j] + 1]]
         assert dot(Sj, cj) == 1
-        for i in rng.choice(int(j), min(int(j), 20), replace=False) if j > 0 else []:
+        for i in (rng.choice(j, min(j, 20), replace=False).tolist() if j > 0 else []):
             ci = co[off[sel[i]]:off[sel[i] + 1]]
             assert dot(Sj, ci) == 0
     s.reset()
