@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""Benchmark of the de Pina minimum-cycle-basis hot path on GB300.
+
+Workload (the plain-GPU configuration): a connected random sparse graph with
+50,000 vertices and 100,000 edges (random spanning tree by random-permutation
+attach plus uniform extra edges), int32 weights U[1,1000], seed 1 — synthetic,
+generated by the repository's seeded generator.  Host preparation (chain
+contraction, FVS, shortest-path trees, candidate ranking) is done once, untimed.
+
+One step = one complete de Pina solve (all N = m - n + 1 iterations) on the GPU:
+reset S to the unit vectors, then the blocked device loop.  Inputs (the rank-ordered
+candidates and their cycle-coordinate lists, 1.5 GB) stay resident in HBM; they are
+larger than the 129 MB L2, so no flush is needed between steps.
+
+  value       mean seconds per solve (CUDA events on the solver's stream)
+  e2e         seconds per solve through the C ABI with pinned host buffers: upload
+              (H2D of weights, offsets, coordinates) + solve + results (D2H)
+  roofline    the kernel class with the largest time share, algorithmic bytes per
+              launch / mean event-timed launch duration vs the measured HBM peak
+  cpu_baseline  the reference's CPU main loop (oracle port of mcb/mcb_non_cpu_rd.cpp)
+              on this host's cores over the first P iterations, extrapolated to N
+
+`--impl reference` times only that CPU implementation and prints its own line.
+Under torchrun (N > 1) every rank solves its own replica (the loop does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MCB solve time (s) & search HBM GB/s: batched+learned vs plain GPU, exact"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() and args.impl != "reference" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def prepare(args, keep_trees):
+    from minimumcyclebasis_gb300 import Problem, random_graph
+    t0 = time.time()
+    g = random_graph(args.n, 2 * args.n, 1, 1000, args.seed)
+    p = Problem.from_graph(g).prepare(threads=0, keep_trees=keep_trees)
+    i = p.info
+    log("prepared in %.1fs: n'=%d F=%d N=%d K=%d nnz=%d" % (time.time() - t0, i.reduced_nodes, i.fvs_size,
+                                                             i.num_coords, i.num_candidates, i.cycle_nnz))
+    return p
+
+
+def config_of(p, args, extra=None):
+    i = p.info
+    c = {"workload": "random sparse graph n=%d m=%d (avg degree 4), int32 w U[1,1000], seed %d; full de Pina solve"
+                     % (args.n, 2 * args.n, args.seed),
+         "reduced_nodes": i.reduced_nodes, "fvs": i.fvs_size, "N": i.num_coords, "K": i.num_candidates,
+         "cycle_nnz": i.cycle_nnz, "form": args.mode,
+         "l2": ("inputs (cycle lists %.2f GB) larger than the 129 MB L2; no flush" % (i.cycle_nnz * 4 / 1e9))
+         if i.cycle_nnz * 4 > 129e6 else "small case: inputs fit in L2"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def cpu_baseline(p, iters, threads):
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    sel, _, sec = oracle.solve(p, threads=threads, max_iter=iters)
+    n = p.N
+    done = len(sel)
+    value = sec / max(done, 1) * n
+    return {"value": value, "unit": "s", "cores": threads, "kind": "port",
+            "sample": "first %d of %d de Pina iterations of the reference CPU main loop (oracle port of "
+                      "mcb/mcb_non_cpu_rd.cpp:264-342), %.2f s, extrapolated x%d/%d (per-iteration label "
+                      "precompute over all FVS trees dominates and is constant)" % (done, n, sec, n, done)}
+
+
+def run_reference(args, world, rank, pg):
+    if rank != 0:
+        return None
+    p = prepare(args, keep_trees=True)
+    threads = args.cpu_threads or os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(p, max(2, args.cpu_iters // 8), threads)
+    vals = []
+    t0 = time.time()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(p, args.cpu_iters, threads))
+    wall = time.time() - t0
+    v = statistics.mean(x["value"] for x in vals)
+    cb = dict(vals[-1])
+    cb["value"] = v
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / max(args.steps, 1) * 1000.0, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": config_of(p, args, {"form": "reference CPU loop (oracle port), bounded sample"}),
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def pinned_like(a):
+    """A pinned host copy of numpy array `a` (cudaMallocHost through the C ABI)."""
+    import ctypes as C
+
+    import numpy as np
+
+    from minimumcyclebasis_gb300._native import check_gpu, gpu_lib
+    lib = gpu_lib()
+    ptr = C.c_void_p()
+    check_gpu(lib.mcbgpu_allocate_pinned(max(a.nbytes, 1), C.byref(ptr)), "mcbgpu_allocate_pinned")
+    buf = (C.c_char * max(a.nbytes, 1)).from_address(ptr.value)
+    out = np.frombuffer(buf, dtype=a.dtype, count=a.size)
+    out[...] = a
+    return out, ptr
+
+
+def run_gpu(args, world, rank, local, pg):
+    import numpy as np
+    import torch
+
+    from minimumcyclebasis_gb300 import Solver
+    from minimumcyclebasis_gb300.build import build_all
+
+    build_all()
+    torch.cuda.set_device(local)
+    want_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
+    p = prepare(args, keep_trees=want_cpu)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    _, _, w, _ = p.candidates()
+    off, co = p.cycle_lists()
+    solver = Solver(p.N, w, off, co, stream=sh)
+    run = solver.run if args.mode == "blocked" else solver.run_plain
+
+    def solve_once():
+        solver.reset(sh)
+        run(args.max_iterations, sh)
+
+    for i in range(args.warmup):
+        solve_once()
+        if i == 0:
+            sel, tot = solver.results(stream=sh)
+            assert (sel >= 0).all(), "warm-up solve failed"
+            log("warm-up total weight %d" % tot)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    launches0 = solver.launches
+    solver.set_profiling(True)
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            solve_once()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = solver.launches - launches0
+    stats = solver.kernel_stats()
+    solver.set_profiling(False)
+    sel, tot = solver.results(stream=sh)
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+        pg.barrier()
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pw, pw_h = pinned_like(w)
+        po, po_h = pinned_like(off)
+        pc, pc_h = pinned_like(co)
+        psel, psel_h = pinned_like(np.zeros(max(p.N, 1), np.int64))
+        import ctypes as C
+
+        from minimumcyclebasis_gb300._native import check_gpu, gpu_lib
+        lib = gpu_lib()
+        tot_c = C.c_int64()
+
+        def e2e_once():
+            solver.upload(sh, pw, po, pc)
+            run(args.max_iterations, sh)
+            check_gpu(lib.mcbgpu_solver_results(solver._h, C.c_void_p(psel.ctypes.data), p.N, C.byref(tot_c),
+                                                C.c_void_p(sh)), "mcbgpu_solver_results")
+
+        e2e_once()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_once()
+        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+        assert np.array_equal(psel[:p.N], sel) and tot_c.value == tot, "e2e results differ"
+        e2e = {"value": e2e_s, "unit": "s", "steps": args.e2e_steps,
+               "h2d_bytes_per_step": int(w.nbytes + off.nbytes + co.nbytes),
+               "d2h_bytes_per_step": int(8 * p.N + 8 + 4)}
+        for h in (pw_h, po_h, pc_h, psel_h):
+            lib.mcbgpu_free_pinned(h)
+
+    # roofline of the kernel class with the largest time share
+    peak, peak_kind = measured_peaks()
+    top = max(stats.items(), key=lambda kv: kv[1]["ms"])
+    name, st = top
+    per_launch_s = st["ms"] / 1e3 / max(st["launches"], 1)
+    per_launch_b = st["bytes"] / max(st["launches"], 1)
+    achieved = per_launch_b / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(name)
+    total_ms = sum(v["ms"] for v in stats.values())
+    roofline = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "bytes_per_launch": per_launch_b, "launch_ms": per_launch_s * 1e3, "share": st["ms"] / total_ms,
+                "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                                "GBps": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 and v["bytes"] else None}
+                            for k, v in sorted(stats.items(), key=lambda kv: -kv[1]["ms"])}}
+
+    cb = None
+    if want_cpu:
+        cb = cpu_baseline(p, args.cpu_iters, args.cpu_threads)
+    if rank != 0:
+        return None
+    return {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": config_of(p, args, {"total_weight": tot, "solves_per_s_all_ranks": world * 1e3 / ms}),
+            "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
+            "cpu_baseline": cb}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--n", type=int, default=50000, help="graph vertices (edges = 2n)")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--mode", choices=["blocked", "plain"], default="blocked")
+    ap.add_argument("--max-iterations", type=int, default=-1)
+    ap.add_argument("--cpu-iters", type=int, default=40, help="iterations in the CPU baseline sample")
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        out = run_reference(args, world, rank, pg)
+    else:
+        out = run_gpu(args, world, rank, local, pg)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

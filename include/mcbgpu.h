@@ -144,6 +144,19 @@ int mcbgpu_solver_results(mcbgpu_solver *s, int64_t *selected, int64_t count, in
                           void *stream);
 /* Copy S_j (ceil(N/64) words) to the host (synchronous). */
 int mcbgpu_solver_get_support(mcbgpu_solver *s, int32_t j, uint64_t *words, void *stream);
+/* Optional live profile.  set_profiling(1) clears the records; from then on every
+ * kernel launch of the handle is bracketed by CUDA events on its stream, and the
+ * kernels add their algorithmic HBM bytes to per-class counters.  kernel_stats
+ * synchronises the device, fills one entry per kernel class launched since, and
+ * clears the records. */
+typedef struct mcbgpu_kernel_stat {
+    const char *name;
+    int64_t launches;
+    double ms;     /* summed event time of the launches */
+    double bytes;  /* summed algorithmic bytes (0 where a kernel does not count) */
+} mcbgpu_kernel_stat;
+int mcbgpu_solver_set_profiling(mcbgpu_solver *s, int enable);
+int mcbgpu_solver_kernel_stats(mcbgpu_solver *s, mcbgpu_kernel_stat *out, int max_entries, int *count);
 /* Kernel launches issued by this handle so far (for accounting). */
 int64_t mcbgpu_solver_launches(const mcbgpu_solver *s);
 /* Device bytes held by the handle. */

@@ -19,6 +19,10 @@ i32, i64, u64 = C.c_int32, C.c_int64, C.c_uint64
 f32p = C.POINTER(C.c_float)
 
 
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("launches", i64), ("ms", C.c_double), ("bytes", C.c_double)]
+
+
 class MCBHOptions(C.Structure):
     _fields_ = [("threads", C.c_int), ("contract_chains", C.c_int), ("keep_trees", C.c_int),
                 ("ref_layout", C.c_int), ("cycle_lists", C.c_int)]
@@ -78,6 +82,8 @@ GPU_SYMBOLS = {
     "mcbgpu_solver_run_plain": (C.c_int, [vp, i64, vp]),
     "mcbgpu_solver_results": (C.c_int, [vp, vp, i64, C.POINTER(i64), vp]),
     "mcbgpu_solver_get_support": (C.c_int, [vp, i32, vp, vp]),
+    "mcbgpu_solver_set_profiling": (C.c_int, [vp, C.c_int]),
+    "mcbgpu_solver_kernel_stats": (C.c_int, [vp, vp, C.c_int, C.POINTER(C.c_int)]),
     "mcbgpu_solver_launches": (i64, [vp]),
     "mcbgpu_solver_device_bytes": (i64, [vp]),
     "mcbgpu_solver_destroy": (C.c_int, [vp]),

@@ -43,6 +43,15 @@ constexpr int kPer = kTile / kScanThreads;
 constexpr unsigned kSpinLimit = 1u << 24;
 constexpr unsigned long long kNone = 0xFFFFFFFFFFFFFFFFull;
 
+// Kernel classes for the optional per-launch profile (events + algorithmic bytes).
+enum KernelClass {
+    KC_INIT, KC_TILE_MINC, KC_TRANSPOSE, KC_WSTREAM, KC_PIVOT, KC_RESOLVE, KC_MATERIALIZE, KC_TABLES,
+    KC_BLK_UPDATE, KC_SEARCH, KC_UPDATE, KC_CYCLE, KC_RESET, KC_VALIDATE, KC_COUNT
+};
+const char *const kKernelNames[KC_COUNT] = {
+    "init_identity", "tile_minc", "blk_transpose", "blk_w", "blk_pivot", "blk_resolve", "blk_materialize",
+    "blk_tables", "blk_update", "search", "update", "cycle_vector", "reset_state", "validate"};
+
 struct IterSlot {            // state of one per-iteration search
     unsigned long long best; // first odd rank (kNone until found)
     unsigned next_tile;
@@ -68,6 +77,10 @@ struct GridBar {
     unsigned count, gen, abort, pad;
 };
 
+struct PivotReport {  // one CTA's first non-zero residual in a pivot step
+    unsigned long long rank, w;
+};
+
 // ---------------------------------------------------------------------------
 __global__ void init_identity_kernel(uint64_t *S, int N, int P) {
     size_t total = (size_t)N * P;
@@ -85,6 +98,32 @@ __global__ void reset_state_kernel(IterSlot *slots, BlockState *bs, unsigned *st
         slots[1].next_tile = 0;
         bs->total = 0;  // epoch keeps counting across runs: old tile marks never match
         *status = 0;
+    }
+}
+
+// Validates the uploaded candidate lists before any kernel indexes with them:
+// offsets non-decreasing from 0 to nnz, coordinates strictly ascending inside each
+// list and inside [0, N).  Records the longest list.  One thread per candidate.
+__global__ void validate_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ coords, long long K,
+                                long long nnz, int N, unsigned *bad, unsigned *max_len) {
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < K; r += (long long)gridDim.x * blockDim.x) {
+        const int64_t b = off[r], e = off[r + 1];
+        if (r == 0 && b != 0) atomicOr(bad, 1u);
+        if (r == K - 1 && e != nnz) atomicOr(bad, 1u);
+        if (e < b || b < 0 || e > nnz) {
+            atomicOr(bad, 1u);
+            continue;
+        }
+        int prev = -1;
+        for (int64_t i = b; i < e; i++) {
+            const int c = coords[i];
+            if (c <= prev || c >= N) {
+                atomicOr(bad, 2u);
+                break;
+            }
+            prev = c;
+        }
+        if (e - b > 0) atomicMax(max_len, (unsigned)(e - b));
     }
 }
 
@@ -114,7 +153,9 @@ __global__ void tile_minc_kernel(const int64_t *__restrict__ off, const int32_t 
 __global__ void __launch_bounds__(kScanThreads) search_kernel(const uint64_t *__restrict__ Se, int e,
                                                               int words_even, const int64_t *__restrict__ off,
                                                               const int32_t *__restrict__ coords, long long K,
-                                                              IterSlot *slot, unsigned *status) {
+                                                              IterSlot *slot, unsigned *status,
+                                                              unsigned long long *bytes) {
+    unsigned long long nb = 0;
     extern __shared__ __align__(16) uint64_t s_S[];
     __shared__ uint64_t bar;
     __shared__ unsigned s_tile, s_go;
@@ -143,8 +184,10 @@ __global__ void __launch_bounds__(kScanThreads) search_kernel(const uint64_t *__
             if (r >= K) break;
             int64_t b = off[r], en = off[r + 1];
             unsigned par = 0;
+            nb += 8;
             for (int64_t i = b; i < en; i++) {
                 int c = __ldg(coords + i);
+                nb += 4;
                 if (c > e) break;
                 par ^= (unsigned)(s_S[c >> 6] >> (c & 63)) & 1u;
             }
@@ -164,6 +207,8 @@ __global__ void __launch_bounds__(kScanThreads) search_kernel(const uint64_t *__
         if (threadIdx.x == 0 && s_best != kNone) atomicMin(&slot->best, s_best);
         __syncthreads();
     }
+    for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
+    if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
 }
 
 // One warp per row j in (e, N): if <C_e, S_j> is odd, S_j ^= S_e (words [0, e/64]).
@@ -329,7 +374,8 @@ __device__ bool grid_barrier(GridBar *gb, unsigned nctas, unsigned &gen_local) {
 // 16-byte loads (coalesced), find each element's candidate from the tile's offsets
 // held in shared memory, and fold runs of the same candidate into one shared
 // atomicXor.  A tile whose smallest coordinate is >= bound has W = 0 throughout.
-__device__ void compute_w_tile(long long tile, long long K, const int64_t *__restrict__ off,
+// Returns, in thread 0, the tile's algorithmic HBM bytes (offsets + coordinates read).
+__device__ unsigned long long compute_w_tile(long long tile, long long K, const int64_t *__restrict__ off,
                                const int32_t *__restrict__ coords, const int32_t *__restrict__ tile_minc,
                                const uint64_t *__restrict__ T, int bound, uint64_t *sW, int64_t *soff) {
     const long long r0 = tile * kTile;
@@ -339,7 +385,7 @@ __device__ void compute_w_tile(long long tile, long long K, const int64_t *__res
     if (!skip)
         for (int i = threadIdx.x; i <= rn; i += blockDim.x) soff[i] = off[r0 + i];
     __syncthreads();
-    if (skip) return;
+    if (skip) return 4;
     const int64_t cb = soff[0], ce = soff[rn];
     for (int64_t i4 = (cb & ~(int64_t)3) + 4 * (int64_t)threadIdx.x; i4 < ce; i4 += 4 * (int64_t)blockDim.x) {
         const int4 v = *reinterpret_cast<const int4 *>(coords + i4);
@@ -371,6 +417,7 @@ __device__ void compute_w_tile(long long tile, long long K, const int64_t *__res
         if (acc) atomicXor((unsigned long long *)&sW[j], (unsigned long long)acc);
     }
     __syncthreads();
+    return 8ull * (unsigned long long)(rn + 1) + 4ull * (unsigned long long)(ce - cb);
 }
 
 // Streaming pass: W for tiles [0, bs->pred_tiles), written to Warr and tagged with
@@ -380,210 +427,307 @@ __global__ void __launch_bounds__(kScanThreads) blk_w_kernel(long long K, const 
                                                              const int32_t *__restrict__ tile_minc,
                                                              const uint64_t *__restrict__ T, int bound,
                                                              const BlockState *bs, uint64_t *Warr,
-                                                             unsigned *tile_epoch) {
+                                                             unsigned *tile_epoch, unsigned long long *bytes) {
     __shared__ uint64_t sW[kTile];
     __shared__ int64_t soff[kTile + 1];
     const unsigned epoch = bs->epoch;
     const long long ntiles = bs->pred_tiles;
+    unsigned long long nb = (blockIdx.x == 0 && threadIdx.x == 0) ? 8ull * (unsigned long long)bound : 0ull;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        compute_w_tile(t, K, off, coords, tile_minc, T, bound, sW, soff);
+        if (tile_minc[t] >= bound) {  // every W of the tile is 0: tag it, write nothing
+            if (threadIdx.x == 0) {
+                tile_epoch[t] = (epoch << 1) | 1u;
+                nb += 8;
+            }
+            continue;
+        }
+        const unsigned long long tb = compute_w_tile(t, K, off, coords, tile_minc, T, bound, sW, soff);
         const long long r0 = t * kTile;
         for (int i = threadIdx.x; i < kTile; i += blockDim.x) Warr[r0 + i] = sW[i];
         __syncthreads();
-        if (threadIdx.x == 0) tile_epoch[t] = epoch;
+        if (threadIdx.x == 0) {
+            tile_epoch[t] = epoch << 1;
+            nb += tb + 8ull * kTile + 8;
+        }
     }
+    if (threadIdx.x == 0 && nb) atomicAdd(bytes, nb);
 }
 
 // Cooperative pivot extraction.  Step k finds the next pivot exactly: the first
 // candidate at or after the previous pivot whose W is not in the span of the
 // pivots found so far (every candidate before it is in that span, so the first
-// non-zero residual is the next rank-ordered independent W).  CTAs scan tiles from
-// the previous pivot onward (tile t by CTA t mod G), reducing W with their own
-// copy of the basis held as Four-Russians tables, and the first non-zero residual
-// is found with a ballot per warp and atomicMin across the grid; one grid barrier
-// per step.  Tiles outside the streamed range are computed here and cached.
+// non-zero residual is the next rank-ordered independent W).
+//
+// CTA c owns tiles c, c+G, c+2G, ... and keeps the W of its current tile in shared
+// memory across steps.  Each step it reduces that tile against its own copy of the
+// basis (Four-Russians tables), moving on to its next tile when the current one has
+// no non-zero residual at or after the scan start, and reports its first non-zero
+// residual (rank, W) in a per-CTA slot; an atomicMin on the running minimum lets CTAs
+// stop scanning past it.  After one grid barrier every CTA reads all reports in one
+// pass, takes the smallest rank, and applies the same basis update to its tables.
+// Tiles outside the streamed range are computed here and cached in Warr.
 __global__ void __launch_bounds__(kScanThreads) blk_pivot_kernel(
     long long K, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
     const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T, int bound, BlockState *bs,
-    uint64_t *Warr, unsigned *tile_epoch, unsigned long long *gmin, GridBar *gb, unsigned *status) {
+    uint64_t *Warr, unsigned *tile_epoch, unsigned long long *gmin, PivotReport *reports, GridBar *gb,
+    unsigned *status, unsigned long long *bytes) {
+    unsigned long long nb = 0;
     __shared__ uint64_t tab[8][256];
     __shared__ uint64_t sW[kTile];
     __shared__ int64_t soff[kTile + 1];
     __shared__ uint64_t sbasis[64];
     __shared__ unsigned spiv[64];
-    __shared__ unsigned s_go, s_found;
-    __shared__ unsigned long long s_min;
+    __shared__ unsigned s_go;
+    __shared__ unsigned long long s_min, s_chg;
+    __shared__ unsigned long long s_wr[kScanThreads / 32];
+    __shared__ unsigned long long s_ww[kScanThreads / 32];
     const unsigned epoch = bs->epoch;
     const int b = (int)bs->b;
     const long long ntiles = (K + kTile - 1) / kTile;
-    const unsigned G = gridDim.x;
+    const long long G = gridDim.x, c = blockIdx.x;
     unsigned gen = ld_acquire_u32(&gb->gen);
     for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&tab[0][0])[i] = 0;
-    __syncthreads();
+    long long cur = -1;  // owned tile whose W is in sW
     long long s = 0;
     int rank = 0;
     bool ok = true;
+    __syncthreads();
     for (int k = 0; k < b; k++) {
         unsigned long long *slot = gmin + (k % 3);
-        if (blockIdx.x == 0 && threadIdx.x == 0) gmin[(k + 1) % 3] = kNone;
+        PivotReport *rep = reports + (size_t)(k & 1) * G;
+        if (c == 0 && threadIdx.x == 0) gmin[(k + 1) % 3] = kNone;
         const long long t0 = s / kTile;
-        for (long long t = t0 + blockIdx.x; t < ntiles; t += G) {
+        long long t = t0 + ((c - t0 % G) + G) % G;  // first owned tile at or after t0
+        unsigned long long found_r = kNone, found_w = 0;
+        for (; t < ntiles; t += G) {
             if (threadIdx.x == 0) s_go = (unsigned long long)(t * kTile) <= *((volatile unsigned long long *)slot);
             __syncthreads();
             if (!s_go) break;
             const long long r0 = t * kTile;
-            if (*((volatile unsigned *)&tile_epoch[t]) == epoch) {
-                for (int i = threadIdx.x; i < kTile; i += blockDim.x) sW[i] = (r0 + i < K) ? __ldcg(Warr + r0 + i) : 0;
-                __syncthreads();
-            } else {
-                compute_w_tile(t, K, off, coords, tile_minc, T, bound, sW, soff);
-                for (int i = threadIdx.x; i < kTile; i += blockDim.x) Warr[r0 + i] = sW[i];
-                __syncthreads();
-                if (threadIdx.x == 0) {
-                    __threadfence();
-                    tile_epoch[t] = epoch;
+            if (t != cur) {
+                const unsigned tag = *((volatile unsigned *)&tile_epoch[t]);
+                if ((tag >> 1) == epoch) {
+                    if (tag & 1u) {
+                        for (int i = threadIdx.x; i < kTile; i += blockDim.x) sW[i] = 0;
+                    } else {
+                        for (int i = threadIdx.x; i < kTile; i += blockDim.x)
+                            sW[i] = (r0 + i < K) ? __ldcg(Warr + r0 + i) : 0;
+                        nb += 8ull * kTile;
+                    }
+                    __syncthreads();
+                } else {
+                    const unsigned long long tb = compute_w_tile(t, K, off, coords, tile_minc, T, bound, sW, soff);
+                    for (int i = threadIdx.x; i < kTile; i += blockDim.x) Warr[r0 + i] = sW[i];
+                    __syncthreads();
+                    if (threadIdx.x == 0) {
+                        __threadfence();
+                        tile_epoch[t] = epoch << 1;
+                    }
+                    nb += tb + 8ull * kTile;
                 }
+                cur = t;
             }
-            if (threadIdx.x == 0) {
-                s_min = kNone;
-                s_found = 0;
-            }
+            if (threadIdx.x == 0) s_min = kNone;
             __syncthreads();
-            // rank order inside the tile = index order; warp w covers [32w, 32w+32) of each quarter
 #pragma unroll
             for (int q = 0; q < kPer; q++) {
                 const int li = q * kScanThreads + threadIdx.x;
-                const bool nz = fr_reduce(sW[li], tab) != 0 && (r0 + li) >= s;
+                const bool nz = (r0 + li) >= s && fr_reduce(sW[li], tab) != 0;
                 const unsigned bal = __ballot_sync(0xffffffffu, nz);
                 if (bal && (threadIdx.x & 31) == 0)
                     atomicMin(&s_min, (unsigned long long)(r0 + q * kScanThreads + (threadIdx.x & ~31) + __ffs(bal) - 1));
             }
             __syncthreads();
             if (s_min != kNone) {
-                if (threadIdx.x == 0) atomicMin(slot, s_min);
+                found_r = s_min;
+                found_w = sW[found_r - r0];
                 break;
             }
         }
-        if (!grid_barrier(gb, G, gen)) {
+        if (threadIdx.x == 0) {
+            rep[c].rank = found_r;
+            rep[c].w = found_w;
+            if (found_r != kNone) atomicMin(slot, found_r);
+        }
+        if (!grid_barrier(gb, (unsigned)G, gen)) {
             ok = false;
             break;
         }
-        const unsigned long long p = *((volatile unsigned long long *)slot);
+        // smallest reported rank and its W (one coalesced pass over the reports)
+        unsigned long long br = kNone, bw = 0;
+        for (long long i = threadIdx.x; i < G; i += blockDim.x) {
+            const unsigned long long r = __ldcg(&rep[i].rank);
+            if (r < br) {
+                br = r;
+                bw = __ldcg(&rep[i].w);
+            }
+        }
+        for (int d = 16; d > 0; d >>= 1) {
+            const unsigned long long orr = __shfl_xor_sync(0xffffffffu, br, d);
+            const unsigned long long ow = __shfl_xor_sync(0xffffffffu, bw, d);
+            if (orr < br) {
+                br = orr;
+                bw = ow;
+            }
+        }
+        if ((threadIdx.x & 31) == 0) {
+            s_wr[threadIdx.x >> 5] = br;
+            s_ww[threadIdx.x >> 5] = bw;
+        }
+        if (threadIdx.x == 0) s_chg = 0;
+        __syncthreads();
+        unsigned long long p = kNone, Wp = 0;
+        for (int w = 0; w < kScanThreads / 32; w++)
+            if (s_wr[w] < p) {
+                p = s_wr[w];
+                Wp = s_ww[w];
+            }
         if (p == kNone) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, ST_RANK_DEFICIT);
+            if (c == 0 && threadIdx.x == 0) atomicOr(status, ST_RANK_DEFICIT);
             ok = false;
             break;
         }
-        const uint64_t Wp = __ldcg(Warr + p);
         const uint64_t v = fr_reduce(Wp, tab);
         const unsigned qb = (unsigned)(__ffsll((long long)v) - 1);
-        // keep the basis reduced: clear bit qb from the others, append v
-        if (threadIdx.x < (unsigned)rank && ((sbasis[threadIdx.x] >> qb) & 1ull)) sbasis[threadIdx.x] ^= v;
+        // vectors that change when bit qb is cleared from them, plus the new one
+        if (threadIdx.x < (unsigned)rank && ((sbasis[threadIdx.x] >> qb) & 1ull))
+            atomicOr(&s_chg, 1ull << spiv[threadIdx.x]);
         __syncthreads();
+        const unsigned long long chg = s_chg | (1ull << qb);
+        for (int idx = threadIdx.x; idx < 8 * 256; idx += blockDim.x) {
+            const int g = idx >> 8, pat = idx & 255;
+            if (__popc(pat & (unsigned)((chg >> (8 * g)) & 255)) & 1) (&tab[0][0])[idx] ^= v;
+        }
+        if (threadIdx.x < (unsigned)rank && ((sbasis[threadIdx.x] >> qb) & 1ull)) sbasis[threadIdx.x] ^= v;
         if (threadIdx.x == 0) {
             sbasis[rank] = v;
             spiv[rank] = qb;
-            if (blockIdx.x == 0) {
+            if (c == 0) {
                 bs->pivrank[rank] = (long long)p;
                 bs->pivW[rank] = Wp;
             }
         }
         rank++;
-        __syncthreads();
-        fr_build(tab, sbasis, spiv, (unsigned)rank);
         s = (long long)p + 1;
+        __syncthreads();
     }
     if (!ok && threadIdx.x == 0 && (*((volatile unsigned *)&gb->abort))) atomicOr(status, ST_WAIT_TIMEOUT);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (threadIdx.x == 0 && nb) atomicAdd(bytes, nb);
+    if (c == 0 && threadIdx.x == 0) {
         bs->rank = (unsigned)rank;
         bs->last_pivot = s - 1;
     }
 }
 
-// Resolve the block's b iterations on masks (one warp).  Pivot index = rank order.
+// Resolve the block's b iterations on masks.  Pivot index = rank order.
 // m_k starts as e_k; iteration k takes the first pivot p with <W_p, m_k> odd; every
 // later m_j with <W_p, m_j> odd gets m_j ^= m_k (the reference's update restricted
-// to the block, mcb/mcb_cycle_deg_two_remove.cpp:371-390).
-__global__ void blk_resolve_kernel(BlockState *bs, int e0, const int64_t *__restrict__ off,
-                                   const int32_t *__restrict__ coords, const int32_t *__restrict__ weight,
-                                   long long *selected, unsigned *pairs, unsigned pair_cap, unsigned *status) {
-    const int lane = threadIdx.x;
+// to the block, mcb/mcb_cycle_deg_two_remove.cpp:371-390).  Warp 0 runs the 64
+// steps; then all threads record the selections and build the (coordinate, k) list
+// of the chosen cycles for the update kernel.
+__global__ void __launch_bounds__(256) blk_resolve_kernel(BlockState *bs, int e0, const int64_t *__restrict__ off,
+                                                          const int32_t *__restrict__ coords,
+                                                          const int32_t *__restrict__ weight, long long *selected,
+                                                          unsigned *pairs, unsigned pair_cap, unsigned *status) {
+    __shared__ uint64_t s_w[64];
+    __shared__ long long s_r[64];
+    __shared__ int s_sel[64];
+    __shared__ int64_t s_beg[64];
+    __shared__ unsigned s_pre[65];
+    __shared__ unsigned s_fail;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int b = (int)bs->b;
     const unsigned rank = bs->rank;
     if (rank < (unsigned)b) {
-        if (lane == 0) atomicOr(status, ST_RANK_DEFICIT);
+        if (tid == 0) atomicOr(status, ST_RANK_DEFICIT);
         return;
     }
-    uint64_t w0 = bs->pivW[lane], w1 = bs->pivW[32 + lane];
-    if (lane >= b) w0 = 0;
-    if (32 + lane >= b) w1 = 0;
-    uint64_t m0 = 1ull << lane, m1 = 1ull << (32 + lane);
-    bool used0 = lane >= b, used1 = 32 + lane >= b;
-    __shared__ int s_sel[64];
-    __shared__ uint64_t s_g[64];
-    for (int k = 0; k < b; k++) {
-        const uint64_t mk = __shfl_sync(0xffffffffu, k < 32 ? m0 : m1, k & 31);
-        const unsigned o0 = __ballot_sync(0xffffffffu, !used0 && parity64(w0 & mk));
-        const unsigned o1 = __ballot_sync(0xffffffffu, !used1 && parity64(w1 & mk));
-        int p;
-        if (o0)
-            p = __ffs(o0) - 1;
-        else if (o1)
-            p = 32 + __ffs(o1) - 1;
-        else {
-            if (lane == 0) atomicOr(status, ST_NO_CANDIDATE);
-            return;
-        }
-        if (p < 32 && lane == p) used0 = true;
-        if (p >= 32 && lane == p - 32) used1 = true;
-        const uint64_t wp = __shfl_sync(0xffffffffu, p < 32 ? w0 : w1, p & 31);
-        // gcol[k] bit i = <W_p, m_i> for i < k (rows i are final)
-        const unsigned g0 = __ballot_sync(0xffffffffu, lane < k && parity64(wp & m0));
-        const unsigned g1 = __ballot_sync(0xffffffffu, 32 + lane < k && parity64(wp & m1));
-        if (lane == 0) {
-            s_sel[k] = p;
-            s_g[k] = (uint64_t)g0 | ((uint64_t)g1 << 32);
-        }
-        if (lane > k && parity64(wp & m0)) m0 ^= mk;
-        if (32 + lane > k && parity64(wp & m1)) m1 ^= mk;
+    if (tid < 64) {
+        s_w[tid] = tid < b ? bs->pivW[tid] : 0ull;
+        s_r[tid] = tid < b ? bs->pivrank[tid] : -1;
     }
-    __syncwarp();
-    bs->mask[lane] = m0;
-    bs->mask[32 + lane] = m1;
-    // selections, weights, and the (coordinate, k) pairs of the chosen cycles
+    if (tid == 0) s_fail = 0;
+    __syncthreads();
+    if (tid < 32) {
+        const uint64_t w0 = s_w[lane], w1 = s_w[32 + lane];
+        uint64_t m0 = 1ull << lane, m1 = 1ull << (32 + lane);
+        bool used0 = lane >= b, used1 = 32 + lane >= b;
+        for (int k = 0; k < b; k++) {
+            const uint64_t mk = __shfl_sync(0xffffffffu, k < 32 ? m0 : m1, k & 31);
+            const unsigned o0 = __ballot_sync(0xffffffffu, !used0 && parity64(w0 & mk));
+            const unsigned o1 = __ballot_sync(0xffffffffu, !used1 && parity64(w1 & mk));
+            int p;
+            if (o0)
+                p = __ffs(o0) - 1;
+            else if (o1)
+                p = 32 + __ffs(o1) - 1;
+            else {
+                if (lane == 0) s_fail = 1;
+                break;
+            }
+            if (p < 32 && lane == p) used0 = true;
+            if (p >= 32 && lane == p - 32) used1 = true;
+            const uint64_t wp = s_w[p];
+            // gcol[k] bit i = <W_p, m_i> for i < k (rows i are final)
+            const unsigned g0 = __ballot_sync(0xffffffffu, lane < k && parity64(wp & m0));
+            const unsigned g1 = __ballot_sync(0xffffffffu, 32 + lane < k && parity64(wp & m1));
+            if (lane == 0) {
+                s_sel[k] = p;
+                bs->gcol[k] = (uint64_t)g0 | ((uint64_t)g1 << 32);
+            }
+            if (lane > k && parity64(wp & m0)) m0 ^= mk;
+            if (32 + lane > k && parity64(wp & m1)) m1 ^= mk;
+        }
+        bs->mask[lane] = m0;
+        bs->mask[32 + lane] = m1;
+    }
+    __syncthreads();
+    if (s_fail) {
+        if (tid == 0) atomicOr(status, ST_NO_CANDIDATE);
+        return;
+    }
+    // selections, weights, chosen cycles' coordinate ranges
+    unsigned len = 0;
     unsigned long long wsum = 0;
-    unsigned base = 0;
-    for (int k0 = 0; k0 < b; k0 += 32) {
-        const int k = k0 + lane;
-        long long r = -1;
-        unsigned len = 0;
-        if (k < b) {
-            r = bs->pivrank[s_sel[k]];
-            selected[e0 + k] = r;
-            bs->sel[k] = s_sel[k];
-            bs->gcol[k] = s_g[k];
-            wsum += (unsigned long long)(long long)weight[r];
+    if (tid < 64) {
+        if (tid < b) {
+            const long long r = s_r[s_sel[tid]];
+            selected[e0 + tid] = r;
+            bs->sel[tid] = s_sel[tid];
+            wsum = (unsigned long long)(long long)weight[r];
+            s_beg[tid] = off[r];
             len = (unsigned)(off[r + 1] - off[r]);
         }
         unsigned incl = len;
         for (int d = 1; d < 32; d <<= 1) {
-            unsigned t = __shfl_up_sync(0xffffffffu, incl, d);
+            const unsigned t = __shfl_up_sync(0xffffffffu, incl, d);
             if (lane >= d) incl += t;
         }
-        const unsigned start = base + incl - len;
-        if (k < b) {
-            if (start + len > pair_cap) {
-                atomicOr(status, ST_BAD_INPUT);
-            } else {
-                for (unsigned i = 0; i < len; i++) pairs[start + i] = ((unsigned)coords[off[r] + i] << 6) | (unsigned)k;
-            }
-        }
-        base += __shfl_sync(0xffffffffu, incl, 31);
+        s_pre[tid + 1] = incl;  // per-warp inclusive; fixed up below
+        for (int d = 16; d > 0; d >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, d);
+        if (lane == 0) atomicAdd(&bs->total, wsum);
     }
-    for (int d = 16; d > 0; d >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, d);
-    if (lane == 0) {
-        bs->npairs = base < pair_cap ? base : pair_cap;
-        bs->total += wsum;
+    __syncthreads();
+    if (tid == 0) {
+        s_pre[0] = 0;
+        const unsigned carry = s_pre[32];
+        for (int i = 33; i <= 64; i++) s_pre[i] += carry;
+        const unsigned total = s_pre[64];
+        bs->npairs = total < pair_cap ? total : pair_cap;
+        if (total > pair_cap) atomicOr(status, ST_BAD_INPUT);
+    }
+    __syncthreads();
+    const unsigned total = s_pre[64] < pair_cap ? s_pre[64] : pair_cap;
+    for (unsigned i = tid; i < total; i += blockDim.x) {
+        int lo = 0, hi = b - 1;  // last k with s_pre[k] <= i
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_pre[mid] <= i)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        pairs[i] = ((unsigned)coords[s_beg[lo] + (i - s_pre[lo])] << 6) | (unsigned)lo;
     }
 }
 
@@ -640,7 +784,8 @@ __global__ void blk_tables_kernel(const uint64_t *__restrict__ S, int P, int e0,
 // then S_j ^= XOR_k beta_k S_{e0+k} through the tables.
 __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int Pt,
                                   const uint64_t *__restrict__ tab, const BlockState *bs,
-                                  const unsigned *__restrict__ pairs) {
+                                  const unsigned *__restrict__ pairs, unsigned long long *bytes) {
+    unsigned long long nb = 0;
     __shared__ uint64_t sg[64];
     const int b = (int)bs->b;
     const unsigned np = bs->npairs;
@@ -662,6 +807,10 @@ __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int
             uint64_t bk = ((D >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]);
             beta |= bk << k;
         }
+        // algorithmic bytes: the words of S_j the pairs touch (at most its support
+        // [0, j]) plus, when it changes, read + write of its first Wb words
+        const unsigned wj = (unsigned)(j >> 6) + 1;
+        nb += 8ull * (np < wj ? np : wj) + (beta ? 16ull * (unsigned long long)Wb : 0ull);
         if (!beta) continue;
         const uint64_t *t0 = tab + ((size_t)0 * 256 + ((beta >> 0) & 255)) * Pt;
         const uint64_t *t1 = tab + ((size_t)1 * 256 + ((beta >> 8) & 255)) * Pt;
@@ -674,6 +823,7 @@ __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int
         for (int w = lane; w < Wb; w += 32)
             Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
     }
+    if (lane == 0 && nb) atomicAdd(bytes, nb);
 }
 
 }  // namespace
@@ -695,6 +845,7 @@ struct mcbgpu_solver {
     unsigned *d_tile_epoch = nullptr;
     int32_t *d_tile_minc = nullptr;
     unsigned long long *d_gmin = nullptr;  // 3 slots
+    PivotReport *d_reports = nullptr;      // 2 x pivot_grid
     GridBar *d_gbar = nullptr;
     int pivot_grid = 0;
     unsigned *d_pairs = nullptr;
@@ -703,11 +854,58 @@ struct mcbgpu_solver {
     BlockState *d_bs = nullptr;
     long long *d_selected = nullptr;
     unsigned *d_status = nullptr;
+    unsigned *d_check = nullptr;   // [bad flags, longest list]
     bool uploaded = false;
     long long iters_run = 0;
     long long launches = 0;
     long long device_bytes = 0;
+    // optional per-launch profile: events around every launch, per-class byte counters
+    struct ProfRec {
+        int cls;
+        cudaEvent_t a, b;
+    };
+    bool profiling = false;
+    std::vector<ProfRec> recs;
+    std::vector<cudaEvent_t> pool;
+    size_t pool_next = 0;
+    unsigned long long *d_bytes = nullptr;  // KC_COUNT counters
 };
+
+namespace {
+
+cudaEvent_t pool_event(mcbgpu_solver *s) {
+    if (s->pool_next == s->pool.size()) {
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        s->pool.push_back(e);
+    }
+    return s->pool[s->pool_next++];
+}
+
+// Counts a launch of class `cls`; when profiling, brackets it with events.
+struct Launch {
+    mcbgpu_solver *s;
+    int cls;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    Launch(mcbgpu_solver *s_, int cls_, cudaStream_t st_) : s(s_), cls(cls_), st(st_) {
+        if (s->profiling) {
+            a = pool_event(s);
+            cudaEventRecord(a, st);
+        }
+    }
+    ~Launch() {
+        if (s->profiling) {
+            cudaEvent_t b = pool_event(s);
+            cudaEventRecord(b, st);
+            s->recs.push_back({cls, a, b});
+        }
+        s->launches++;
+    }
+    unsigned long long *bytes() const { return s->d_bytes + cls; }
+};
+
+}  // namespace
 
 namespace {
 
@@ -724,12 +922,16 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_tile_epoch);
     cudaFree(s->d_tile_minc);
     cudaFree(s->d_gmin);
+    cudaFree(s->d_reports);
     cudaFree(s->d_gbar);
     cudaFree(s->d_pairs);
     cudaFree(s->d_slots);
     cudaFree(s->d_bs);
     cudaFree(s->d_selected);
     cudaFree(s->d_status);
+    cudaFree(s->d_check);
+    cudaFree(s->d_bytes);
+    for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
     delete s;
 }
 
@@ -798,7 +1000,10 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_bs, sizeof(BlockState));
     ALLOC(s->d_selected, sizeof(long long) * (size_t)(N > 0 ? N : 1));
     ALLOC(s->d_status, sizeof(unsigned));
+    ALLOC(s->d_bytes, sizeof(unsigned long long) * KC_COUNT);
+    ALLOC(s->d_check, sizeof(unsigned) * 2);
 #undef ALLOC
+    if (e == cudaSuccess) e = cudaMemset(s->d_bytes, 0, sizeof(unsigned long long) * KC_COUNT);
     if (e == cudaSuccess) e = cudaMemset(s->d_tile_epoch, 0, sizeof(unsigned) * ntiles);
     if (e == cudaSuccess) e = cudaMemset(s->d_gbar, 0, sizeof(GridBar));
     if (e == cudaSuccess) e = cudaMemset(s->d_coords, 0, sizeof(int32_t) * (size_t)(nnz + 4));
@@ -807,6 +1012,8 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blk_pivot_kernel, kScanThreads, 0);
         if (per_sm > 1) per_sm = 1;
         s->pivot_grid = per_sm * (s->sm_count > 0 ? s->sm_count : 1);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_reports, sizeof(PivotReport) * 2 * (size_t)s->pivot_grid);
+        bytes += (long long)sizeof(PivotReport) * 2 * s->pivot_grid;
     }
     if (e == cudaSuccess) e = cudaMemset(s->d_bs, 0, sizeof(BlockState));
     if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(unsigned));
@@ -827,13 +1034,17 @@ int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (s->N > 0) {
         int grid = s->sm_count > 0 ? s->sm_count * 4 : 256;
-        init_identity_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P);
+        {
+            Launch L(s, KC_INIT, st);
+            init_identity_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P);
+        }
         MCB_CUDA(cudaGetLastError());
-        s->launches++;
     }
-    reset_state_kernel<<<1, 32, 0, st>>>(s->d_slots, s->d_bs, s->d_status);
+    {
+        Launch L(s, KC_RESET, st);
+        reset_state_kernel<<<1, 32, 0, st>>>(s->d_slots, s->d_bs, s->d_status);
+    }
     MCB_CUDA(cudaGetLastError());
-    s->launches++;
     s->iters_run = 0;
     return MCBGPU_OK;
 }
@@ -844,33 +1055,31 @@ int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t 
         set_error("mcbgpu_solver_upload: NULL argument");
         return MCBGPU_E_ARG;
     }
-    // validate on the host so the kernels index in bounds by construction
-    if (s->K > 0) {
-        if (offsets[0] != 0 || offsets[s->K] != s->nnz) {
-            set_error("mcbgpu_solver_upload: offsets must start at 0 and end at nnz");
-            return MCBGPU_E_ARG;
-        }
-        int max_len = 0;
-        for (long long r = 0; r < s->K; r++) {
-            int64_t b = offsets[r], e = offsets[r + 1];
-            if (e < b) {
-                set_error("mcbgpu_solver_upload: offsets decrease at candidate %lld", r);
-                return MCBGPU_E_ARG;
-            }
-            if (e - b > max_len) max_len = (int)(e - b);
-            int prev = -1;
-            for (int64_t i = b; i < e; i++) {
-                int c = coords[i];
-                if (c <= prev || c >= s->N) {
-                    set_error("mcbgpu_solver_upload: candidate %lld: coordinates must be ascending in [0, N)", r);
-                    return MCBGPU_E_ARG;
-                }
-                prev = c;
-            }
-        }
-        s->max_len = max_len;
-    }
     cudaStream_t st = (cudaStream_t)stream;
+    s->uploaded = false;
+    if (s->K > 0) {
+        MCB_CUDA(cudaMemcpyAsync(s->d_weight, weight, sizeof(int32_t) * (size_t)s->K, cudaMemcpyHostToDevice, st));
+        MCB_CUDA(cudaMemcpyAsync(s->d_off, offsets, sizeof(int64_t) * (size_t)(s->K + 1), cudaMemcpyHostToDevice, st));
+    }
+    if (s->nnz > 0)
+        MCB_CUDA(cudaMemcpyAsync(s->d_coords, coords, sizeof(int32_t) * (size_t)s->nnz, cudaMemcpyHostToDevice, st));
+    // the lists are checked on the device before any other kernel reads them
+    unsigned chk[2] = {0, 0};
+    MCB_CUDA(cudaMemsetAsync(s->d_check, 0, sizeof chk, st));
+    if (s->K > 0) {
+        Launch L(s, KC_VALIDATE, st);
+        int grid = (int)std::min<long long>((s->K + 255) / 256, (long long)(s->sm_count > 0 ? s->sm_count : 148) * 16);
+        validate_kernel<<<grid, 256, 0, st>>>(s->d_off, s->d_coords, s->K, s->nnz, s->N, s->d_check, s->d_check + 1);
+    }
+    MCB_CUDA(cudaGetLastError());
+    MCB_CUDA(cudaMemcpyAsync(chk, s->d_check, sizeof chk, cudaMemcpyDeviceToHost, st));
+    MCB_CUDA(cudaStreamSynchronize(st));
+    if (chk[0]) {
+        set_error("mcbgpu_solver_upload: %s", (chk[0] & 1u) ? "offsets must be non-decreasing from 0 to nnz"
+                                                             : "coordinates must be ascending in [0, N)");
+        return MCBGPU_E_ARG;
+    }
+    s->max_len = (int)chk[1];
     unsigned cap = (unsigned)(64 * (size_t)(s->max_len > 0 ? s->max_len : 1));
     if (cap > s->pair_cap) {
         cudaFree(s->d_pairs);
@@ -879,18 +1088,14 @@ int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t 
         s->device_bytes += (long long)sizeof(unsigned) * cap;
         s->pair_cap = cap;
     }
-    if (s->K > 0) {
-        MCB_CUDA(cudaMemcpyAsync(s->d_weight, weight, sizeof(int32_t) * (size_t)s->K, cudaMemcpyHostToDevice, st));
-        MCB_CUDA(cudaMemcpyAsync(s->d_off, offsets, sizeof(int64_t) * (size_t)(s->K + 1), cudaMemcpyHostToDevice, st));
-    }
-    if (s->nnz > 0)
-        MCB_CUDA(cudaMemcpyAsync(s->d_coords, coords, sizeof(int32_t) * (size_t)s->nnz, cudaMemcpyHostToDevice, st));
     const long long ntiles = (s->K + kTile - 1) / kTile;
     if (ntiles > 0) {
         int grid = (int)std::min<long long>(ntiles, (long long)(s->sm_count > 0 ? s->sm_count : 148) * 8);
-        tile_minc_kernel<<<grid, 256, 0, st>>>(s->d_off, s->d_coords, s->K, s->d_tile_minc, ntiles);
+        {
+            Launch L(s, KC_TILE_MINC, st);
+            tile_minc_kernel<<<grid, 256, 0, st>>>(s->d_off, s->d_coords, s->K, s->d_tile_minc, ntiles);
+        }
         MCB_CUDA(cudaGetLastError());
-        s->launches++;
     }
     s->uploaded = true;
     return mcbgpu_solver_reset(s, stream);
@@ -918,10 +1123,12 @@ int mcbgpu_select(mcbgpu_solver *s, int32_t e, int64_t *rank, void *stream) {
     long long ntiles = (s->K + kTile - 1) / kTile;
     if (ntiles < grid) grid = (int)(ntiles > 0 ? ntiles : 1);
     IterSlot *slot = s->d_slots + (e & 1);
-    search_kernel<<<grid, kScanThreads, smem, st>>>(s->d_S + (size_t)e * s->P, e, we, s->d_off, s->d_coords, s->K,
-                                                     slot, s->d_status);
+    {
+        Launch L(s, KC_SEARCH, st);
+        search_kernel<<<grid, kScanThreads, smem, st>>>(s->d_S + (size_t)e * s->P, e, we, s->d_off, s->d_coords,
+                                                         s->K, slot, s->d_status, L.bytes());
+    }
     MCB_CUDA(cudaGetLastError());
-    s->launches++;
     if (rank) {
         unsigned long long r = 0;
         MCB_CUDA(cudaMemcpyAsync(&r, &slot->best, sizeof r, cudaMemcpyDeviceToHost, st));
@@ -941,9 +1148,11 @@ int mcbgpu_cycle_vector(mcbgpu_solver *s, int32_t e, uint64_t *words, void *stre
         return MCBGPU_E_ARG;
     }
     cudaStream_t st = (cudaStream_t)stream;
-    cycle_vector_kernel<<<1, 256, 0, st>>>(s->d_C, s->W, s->d_off, s->d_coords, s->d_slots + (e & 1));
+    {
+        Launch L(s, KC_CYCLE, st);
+        cycle_vector_kernel<<<1, 256, 0, st>>>(s->d_C, s->W, s->d_off, s->d_coords, s->d_slots + (e & 1));
+    }
     MCB_CUDA(cudaGetLastError());
-    s->launches++;
     if (words) {
         MCB_CUDA(cudaMemcpyAsync(words, s->d_C, sizeof(uint64_t) * (size_t)s->W, cudaMemcpyDeviceToHost, st));
         MCB_CUDA(cudaStreamSynchronize(st));
@@ -962,11 +1171,13 @@ int mcbgpu_update(mcbgpu_solver *s, int32_t e, void *stream) {
     int cap = s->sm_count > 0 ? s->sm_count * 8 : 1024;
     if (grid > cap) grid = cap;
     if (grid < 1) grid = 1;
-    update_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P, e, s->d_off, s->d_coords, s->d_weight,
-                                        s->d_slots + (e & 1), s->d_slots + ((e + 1) & 1), s->d_selected, s->d_bs,
-                                        s->d_status);
+    {
+        Launch L(s, KC_UPDATE, st);
+        update_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P, e, s->d_off, s->d_coords, s->d_weight,
+                                            s->d_slots + (e & 1), s->d_slots + ((e + 1) & 1), s->d_selected,
+                                            s->d_bs, s->d_status);
+    }
     MCB_CUDA(cudaGetLastError());
-    s->launches++;
     if (e + 1 > s->iters_run) s->iters_run = e + 1;
     return MCBGPU_OK;
 }
@@ -1003,12 +1214,18 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         const int b = (int)std::min<int64_t>(64, iters - e0);
         const int Wb = (int)((e0 + b + 63) / 64);
         const int bound = (int)(e0 + b);
-        blk_transpose_kernel<<<(Wb + 7) / 8, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles,
-                                                          s->d_gbar, s->d_gmin);
-        if (ntiles > 0)
-            blk_w_kernel<<<sms * 4, kScanThreads, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
-                                                          s->d_bs, s->d_Warr, s->d_tile_epoch);
         {
+            Launch L(s, KC_TRANSPOSE, st);
+            blk_transpose_kernel<<<(Wb + 7) / 8, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles,
+                                                              s->d_gbar, s->d_gmin);
+        }
+        if (ntiles > 0) {
+            Launch L(s, KC_WSTREAM, st);
+            blk_w_kernel<<<sms * 4, kScanThreads, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                                                          s->d_bs, s->d_Warr, s->d_tile_epoch, L.bytes());
+        }
+        {
+            Launch L(s, KC_PIVOT, st);
             long long K = s->K;
             const int64_t *off = s->d_off;
             const int32_t *co = s->d_coords;
@@ -1020,23 +1237,33 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             unsigned long long *gm = s->d_gmin;
             GridBar *gb = s->d_gbar;
             unsigned *stt = s->d_status;
-            void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &gm, &gb, &stt};
+            PivotReport *rp = s->d_reports;
+            unsigned long long *nb = L.bytes();
+            void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &gm, &rp, &gb, &stt, &nb};
             MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kScanThreads),
                                                  args, 0, st));
         }
-        blk_resolve_kernel<<<1, 32, 0, st>>>(s->d_bs, (int)e0, s->d_off, s->d_coords, s->d_weight, s->d_selected,
-                                             s->d_pairs, s->pair_cap, s->d_status);
-        blk_materialize_kernel<<<(Wb + 31) / 32, 256, 0, st>>>(s->d_S, s->P, (int)e0, Wb, s->d_bs);
-        s->launches += 5;
+        {
+            Launch L(s, KC_RESOLVE, st);
+            blk_resolve_kernel<<<1, 256, 0, st>>>(s->d_bs, (int)e0, s->d_off, s->d_coords, s->d_weight, s->d_selected,
+                                                  s->d_pairs, s->pair_cap, s->d_status);
+        }
+        {
+            Launch L(s, KC_MATERIALIZE, st);
+            blk_materialize_kernel<<<(Wb + 31) / 32, 256, 0, st>>>(s->d_S, s->P, (int)e0, Wb, s->d_bs);
+        }
         if (e0 + b < s->N) {
-            int tgrid = (8 * Wb + 255) / 256;
-            blk_tables_kernel<<<tgrid, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->P, s->d_tab);
+            {
+                Launch L(s, KC_TABLES, st);
+                int tgrid = (8 * Wb + 255) / 256;
+                blk_tables_kernel<<<tgrid, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->P, s->d_tab);
+            }
+            Launch L(s, KC_BLK_UPDATE, st);
             int rows = (int)(s->N - (e0 + b));
             int grid = (rows + 7) / 8;
             if (grid > sms * 8) grid = sms * 8;
             blk_update_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P, (int)e0, Wb, s->P, s->d_tab, s->d_bs,
-                                                    s->d_pairs);
-            s->launches += 2;
+                                                    s->d_pairs, L.bytes());
         }
         MCB_CUDA(cudaGetLastError());
     }
@@ -1069,6 +1296,53 @@ int mcbgpu_solver_get_support(mcbgpu_solver *s, int32_t j, uint64_t *words, void
     MCB_CUDA(cudaMemcpyAsync(words, s->d_S + (size_t)j * s->P, sizeof(uint64_t) * (size_t)s->W,
                              cudaMemcpyDeviceToHost, st));
     MCB_CUDA(cudaStreamSynchronize(st));
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_set_profiling(mcbgpu_solver *s, int enable) {
+    if (!s) {
+        set_error("mcbgpu_solver_set_profiling: NULL handle");
+        return MCBGPU_E_ARG;
+    }
+    MCB_CUDA(cudaDeviceSynchronize());
+    s->recs.clear();
+    s->pool_next = 0;
+    MCB_CUDA(cudaMemset(s->d_bytes, 0, sizeof(unsigned long long) * KC_COUNT));
+    s->profiling = enable != 0;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_kernel_stats(mcbgpu_solver *s, mcbgpu_kernel_stat *out, int max_entries, int *count) {
+    if (!s || (!out && max_entries > 0)) {
+        set_error("mcbgpu_solver_kernel_stats: invalid argument");
+        return MCBGPU_E_ARG;
+    }
+    MCB_CUDA(cudaDeviceSynchronize());
+    double ms[KC_COUNT] = {0};
+    long long n[KC_COUNT] = {0};
+    for (const auto &r : s->recs) {
+        float t = 0;
+        MCB_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+        ms[r.cls] += t;
+        n[r.cls]++;
+    }
+    unsigned long long bytes[KC_COUNT];
+    MCB_CUDA(cudaMemcpy(bytes, s->d_bytes, sizeof bytes, cudaMemcpyDeviceToHost));
+    int c = 0;
+    for (int k = 0; k < KC_COUNT; k++) {
+        if (!n[k]) continue;
+        if (c < max_entries) {
+            out[c].name = kKernelNames[k];
+            out[c].launches = n[k];
+            out[c].ms = ms[k];
+            out[c].bytes = (double)bytes[k];
+        }
+        c++;
+    }
+    if (count) *count = c;
+    s->recs.clear();
+    s->pool_next = 0;
+    MCB_CUDA(cudaMemset(s->d_bytes, 0, sizeof(unsigned long long) * KC_COUNT));
     return MCBGPU_OK;
 }
 

@@ -170,6 +170,18 @@ class Solver:
                   "mcbgpu_solver_get_support")
         return out
 
+    def set_profiling(self, enable: bool = True) -> None:
+        check_gpu(self.lib.mcbgpu_solver_set_profiling(self._h, int(enable)), "mcbgpu_solver_set_profiling")
+
+    def kernel_stats(self) -> dict:
+        """{kernel: {launches, ms, bytes}} since set_profiling(True) (or the last call)."""
+        from ._native import KernelStat
+        arr = (KernelStat * 32)()
+        cnt = C.c_int()
+        check_gpu(self.lib.mcbgpu_solver_kernel_stats(self._h, arr, 32, C.byref(cnt)), "mcbgpu_solver_kernel_stats")
+        return {arr[i].name.decode(): {"launches": arr[i].launches, "ms": arr[i].ms, "bytes": arr[i].bytes}
+                for i in range(min(cnt.value, 32))}
+
     @property
     def launches(self) -> int:
         return int(self.lib.mcbgpu_solver_launches(self._h))
