@@ -104,6 +104,25 @@ int mcbgpu_struct_process_shortest_path(mcbgpu_struct *s, uint32_t *const *preco
 /* gpu_struct::clear_memory (gpu_struct.cu:19-28); also frees the handle. */
 int mcbgpu_struct_clear_memory(mcbgpu_struct *s);
 
+/* No counterpart in the reference.  The labels of process_shortest_path, computed
+ * without allocating: for callers that cannot call cudaMalloc (a host framework
+ * that owns all device memory through its own pool, or a latency-critical loop
+ * that must not take the synchronisation cudaMalloc / cudaFree can imply).  All
+ * pointers are device memory owned by the caller, tree-major as in
+ * initialize_memory (level_offsets F x (nodes+1), parent_pos and edge_offset
+ * F x nodes), the map (num_edges), S (ceil(N/64) words); labels receives F x nodes
+ * uint32 0/1.  Working memory is a static device array inside the library
+ * (16 MiB of per-CTA label slabs + a status word) that every GPU loading the
+ * library keeps until exit; trees of more than 16 Mi vertices are rejected.  The
+ * first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * and should come before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU (other streams, other threads) race.  The call synchronises
+ * `stream` to read the kernel's status. */
+int mcbgpu_label_forest_noalloc(const uint32_t *level_offsets, const uint32_t *parent_pos,
+                                const int32_t *edge_offset, const int32_t *non_tree_edges_map, int num_edges,
+                                const uint64_t *support_vector, int num_coords, int fvs_size, int nodes,
+                                uint32_t *labels, void *stream);
+
 /* ---- 3. device-resident main loop ------------------------------------------ */
 typedef struct mcbgpu_solver mcbgpu_solver;
 

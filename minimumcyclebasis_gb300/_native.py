@@ -72,6 +72,7 @@ GPU_SYMBOLS = {
     "mcbgpu_struct_copy_support_vector": (C.c_int, [vp, vp, f32p]),
     "mcbgpu_struct_process_shortest_path": (C.c_int, [vp, vp, C.c_int, f32p]),
     "mcbgpu_struct_clear_memory": (C.c_int, [vp]),
+    "mcbgpu_label_forest_noalloc": (C.c_int, [vp, vp, vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, vp]),
     "mcbgpu_solver_create": (C.c_int, [C.POINTER(vp), i32, i64, i64]),
     "mcbgpu_solver_upload": (C.c_int, [vp, vp, vp, vp, vp]),
     "mcbgpu_solver_reset": (C.c_int, [vp, vp]),

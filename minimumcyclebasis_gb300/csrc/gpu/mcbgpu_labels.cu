@@ -14,6 +14,7 @@
 // parent-position reads are coalesced), and the finished labels are written out as
 // the reference's uint32 0/1 array.  All trees stay resident in HBM.
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "mcbgpu_internal.cuh"
@@ -259,3 +260,129 @@ int mcbgpu_struct_clear_memory(mcbgpu_struct *s) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free label pass.
+//
+// Some callers cannot allocate device memory: code that runs inside a host
+// framework which owns every byte of device memory through its own pool and does
+// not let plugins call cudaMalloc, and latency-critical loops that must not take the
+// device-wide synchronisation that cudaMalloc / cudaFree can imply.  For them,
+// mcbgpu_label_forest_noalloc computes the same labels as
+// mcbgpu_struct_process_shortest_path from buffers the caller already owns, and
+// keeps its working memory in the file-scope array below, which is part of the
+// library image: every GPU that loads libmcbgpu.so holds it until the process exits.
+//
+// Layout of the array: a 256-byte header whose first word is the kernel's status,
+// then kNoAllocSlabBytes of label slabs, one slab of `nodes` bytes per CTA.
+namespace {
+
+constexpr size_t kNoAllocHeaderBytes = 256;
+constexpr size_t kNoAllocSlabBytes = (size_t)16 << 20;  // 16 MiB
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocHeaderBytes + kNoAllocSlabBytes];
+
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+
+// Same level sweep as label_forest_kernel; the byte labels of the tree being swept
+// live in this CTA's slab of the static scratch, S is read from global memory, and
+// each CTA walks trees blockIdx.x, blockIdx.x + gridDim.x, ...
+__global__ void __launch_bounds__(kLabelThreads) label_forest_noalloc_kernel(
+    const uint32_t *__restrict__ level_off, const uint32_t *__restrict__ parent_pos,
+    const int32_t *__restrict__ edge_off, const int32_t *__restrict__ map, int num_edges,
+    const uint64_t *__restrict__ S, int num_coords, int n, int F, uint32_t *__restrict__ labels_out,
+    uint8_t *slabs, unsigned *status) {
+    uint8_t *lab = slabs + (size_t)blockIdx.x * n;
+    for (int t = blockIdx.x; t < F; t += gridDim.x) {
+        const uint32_t *R = level_off + (size_t)t * (n + 1);
+        const uint32_t *Cp = parent_pos + (size_t)t * n;
+        const int32_t *E = edge_off + (size_t)t * n;
+        if (threadIdx.x == 0) lab[0] = 0;
+        __syncthreads();
+        for (int k = 1; k < n; k++) {
+            const uint32_t beg = R[k], end = R[k + 1];
+            if (beg >= end || end > (uint32_t)n) break;
+            for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
+                const int eo = E[i];
+                uint32_t bit = 0;
+                if (eo >= 0 && eo < num_edges) {
+                    const int c = map[eo];
+                    if (c >= 0 && c < num_coords) bit = (uint32_t)(S[c >> 6] >> (c & 63)) & 1u;
+                }
+                const uint32_t p = Cp[i];
+                uint8_t pl = 0;
+                if (p < i)
+                    pl = lab[p];
+                else
+                    atomicOr(status, ST_BAD_INPUT);
+                lab[i] = (uint8_t)(bit ^ pl);
+            }
+            __syncthreads();
+        }
+        uint32_t *out = labels_out + (size_t)t * n;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = lab[i];
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+extern "C" int mcbgpu_label_forest_noalloc(const uint32_t *level_offsets, const uint32_t *parent_pos,
+                                           const int32_t *edge_offset, const int32_t *non_tree_edges_map,
+                                           int num_edges, const uint64_t *support_vector, int num_coords,
+                                           int fvs_size, int nodes, uint32_t *labels, void *stream) {
+    if (!level_offsets || !parent_pos || !edge_offset || !non_tree_edges_map || !support_vector || !labels ||
+        num_edges <= 0 || num_coords < 0 || fvs_size < 0 || nodes <= 0) {
+        set_error("mcbgpu_label_forest_noalloc: invalid argument");
+        return MCBGPU_E_ARG;
+    }
+    if ((size_t)nodes > kNoAllocSlabBytes) {
+        set_error("mcbgpu_label_forest_noalloc: a tree of %d vertices needs more than the %zu-byte static scratch",
+                  nodes, kNoAllocSlabBytes);
+        return MCBGPU_E_ARG;
+    }
+    int dev = 0;
+    MCB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("mcbgpu_label_forest_noalloc: device %d out of range", dev);
+        return MCBGPU_E_ARG;
+    }
+    unsigned char *base = nullptr;
+    {
+        // once per device, with that device current: the device address of the array
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+            g_noalloc_addr[dev] = (unsigned char *)p;
+        }
+        base = g_noalloc_addr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned *status = reinterpret_cast<unsigned *>(base);
+    uint8_t *slabs = base + kNoAllocHeaderBytes;
+    MCB_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+    if (fvs_size > 0) {
+        int sms = 0;
+        MCB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        size_t grid = (size_t)(sms > 0 ? sms : 1) * 2;
+        const size_t fit = kNoAllocSlabBytes / (size_t)nodes;
+        if (grid > fit) grid = fit;
+        if (grid > (size_t)fvs_size) grid = (size_t)fvs_size;
+        label_forest_noalloc_kernel<<<(unsigned)grid, kLabelThreads, 0, st>>>(
+            level_offsets, parent_pos, edge_offset, non_tree_edges_map, num_edges, support_vector, num_coords,
+            nodes, fvs_size, labels, slabs, status);
+        MCB_CUDA(cudaGetLastError());
+    }
+    unsigned h = 0;
+    MCB_CUDA(cudaMemcpyAsync(&h, status, sizeof h, cudaMemcpyDeviceToHost, st));
+    MCB_CUDA(cudaStreamSynchronize(st));
+    if (h) {
+        set_error("mcbgpu_label_forest_noalloc: kernel status 0x%x", h);
+        return MCBGPU_E_DEVICE;
+    }
+    return MCBGPU_OK;
+}
