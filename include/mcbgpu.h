@@ -176,6 +176,15 @@ typedef struct mcbgpu_kernel_stat {
 } mcbgpu_kernel_stat;
 int mcbgpu_solver_set_profiling(mcbgpu_solver *s, int enable);
 int mcbgpu_solver_kernel_stats(mcbgpu_solver *s, mcbgpu_kernel_stat *out, int max_entries, int *count);
+/* Counters of the blocked search, summed over the blocks run since the last reset:
+ * [0] pivot steps (grid barriers), [1] local pivots reported, [2] merge candidates,
+ * [3] W tiles loaded, [4] W tiles computed inside the pivot kernel, [5] blocks,
+ * [6] / [7] / [8] SM clock cycles of CTA 0 in the scan / barrier / merge parts,
+ * [9]-[13] where a bounded barrier wait gave up (CTA+1, step, rank, generation,
+ * arrivals), [14]/[15] most/fewest barriers of a CTA in one launch, [16]-[19] first
+ * step at which two CTAs disagreed on the merged result (flag, step, CTA, block).
+ * Synchronises the device. */
+int mcbgpu_solver_diagnostics(mcbgpu_solver *s, int64_t *out, int n, int reset);
 /* Kernel launches issued by this handle so far (for accounting). */
 int64_t mcbgpu_solver_launches(const mcbgpu_solver *s);
 /* Device bytes held by the handle. */

@@ -16,6 +16,7 @@ enum : unsigned {
     ST_NO_CANDIDATE = 1u << 1,     // the search found no odd candidate
     ST_RANK_DEFICIT = 1u << 2,     // blocked search ran out of candidates before b pivots
     ST_BAD_INPUT = 1u << 3,        // an index outside its array was seen and skipped
+    ST_DIVERGED = 1u << 4,         // CTAs of a cooperative kernel disagreed on a shared result
 };
 
 void set_error(const char *fmt, ...);
@@ -91,6 +92,30 @@ __device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
 
 __device__ __forceinline__ int parity64(uint64_t x) { return __popcll(x) & 1; }
 
+// CTA barriers in the non-aligned form (`barrier.sync`, not the `.aligned` form
+// that __syncthreads() emits).  The aligned form lets the hardware assume that
+// every warp arrives converged; after lane-divergent loops (per-candidate
+// coordinate walks with early exits, per-thread mbarrier polls) a warp can arrive
+// in pieces, and on sm_103a an aligned barrier was observed to release while one
+// warp of the CTA was still short of it.  The non-aligned form counts threads, so
+// a barrier completes only when every thread of the CTA has reached it.  Every
+// kernel of this library uses these instead of __syncthreads().
+__device__ __forceinline__ void cta_sync() { asm volatile("barrier.sync 0;" ::: "memory"); }
+
+// cta_sync that also returns whether `v` holds in every thread of the CTA.
+__device__ __forceinline__ bool cta_sync_and(bool v) {
+    unsigned r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "barrier.red.and.pred q, 0, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(v ? 1u : 0u)
+        : "memory");
+    return r != 0;
+}
+
 // Stage `words_even` u64 words of global memory (16-byte aligned, an even count)
 // into shared memory with TMA bulk copies of at most 32 KB each.  Called once per
 // kernel by the whole CTA (mbarrier phase 0); every thread waits on the mbarrier
@@ -104,7 +129,7 @@ __device__ __forceinline__ bool stage_words_tma(uint64_t *dst_smem, const uint64
         fence_mbar_init();
         fence_proxy_async_smem();
     }
-    __syncthreads();
+    cta_sync();
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(bar, bytes);
         const uint32_t CH = 32768;
@@ -115,7 +140,7 @@ __device__ __forceinline__ bool stage_words_tma(uint64_t *dst_smem, const uint64
     }
     bool ok = mbar_wait_bounded(bar, 0, 1u << 22);
     if (!ok && threadIdx.x == 0) mbar_wait_bounded(bar, 0, 1u << 22);
-    return __syncthreads_and(ok ? 1 : 0) != 0;
+    return cta_sync_and(ok);
 }
 
 }  // namespace mcbgpu

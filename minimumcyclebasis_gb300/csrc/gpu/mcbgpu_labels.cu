@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kLabelThreads) label_forest_kernel(
     const int32_t *E = edge_off + (size_t)t * n;
     // level 0: the root (edge offset -1 -> label 0)
     if (threadIdx.x == 0) lab[0] = 0;
-    __syncthreads();
+    cta_sync();
     for (int k = 1; k < n; k++) {
         uint32_t beg = R[k], end = R[k + 1];
         if (beg >= end || end > (uint32_t)n) break;
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kLabelThreads) label_forest_kernel(
                 atomicOr(status, ST_BAD_INPUT);  // parent positions precede children
             lab[i] = (uint8_t)(bit ^ pl);
         }
-        __syncthreads();
+        cta_sync();
     }
     uint32_t *out = labels_out + (size_t)t * n;
     for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = lab[i];
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kLabelThreads) label_forest_noalloc_kernel(
         const uint32_t *Cp = parent_pos + (size_t)t * n;
         const int32_t *E = edge_off + (size_t)t * n;
         if (threadIdx.x == 0) lab[0] = 0;
-        __syncthreads();
+        cta_sync();
         for (int k = 1; k < n; k++) {
             const uint32_t beg = R[k], end = R[k + 1];
             if (beg >= end || end > (uint32_t)n) break;
@@ -319,11 +319,11 @@ __global__ void __launch_bounds__(kLabelThreads) label_forest_noalloc_kernel(
                     atomicOr(status, ST_BAD_INPUT);
                 lab[i] = (uint8_t)(bit ^ pl);
             }
-            __syncthreads();
+            cta_sync();
         }
         uint32_t *out = labels_out + (size_t)t * n;
         for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = lab[i];
-        __syncthreads();
+        cta_sync();
     }
 }
 

@@ -41,7 +41,11 @@ constexpr int kTile = 1024;           // candidates per tile
 constexpr int kScanThreads = 256;     // 4 candidates per thread
 constexpr int kPer = kTile / kScanThreads;
 constexpr unsigned kSpinLimit = 1u << 24;
+constexpr int kLmax = 8;       // local pivots a CTA reports per pivot step
+constexpr int kWinTiles = 8;   // tiles a CTA scans per pivot step
+constexpr int kUpdRows = 8;    // rows per warp group in the block update
 constexpr unsigned long long kNone = 0xFFFFFFFFFFFFFFFFull;
+constexpr unsigned kNoIndex = 0xFFFFFFFFu;
 
 // Kernel classes for the optional per-launch profile (events + algorithmic bytes).
 enum KernelClass {
@@ -62,6 +66,7 @@ struct BlockState {
     unsigned rank, epoch, b, npairs;
     long long last_pivot;          // rank of the previous block's last pivot
     long long pred_tiles;          // tiles the streaming pass computes for this block
+    long long max_tile;            // deepest tile the previous block's pivot search touched
     unsigned long long total;      // running 64-bit total weight of the basis
     unsigned long long basis[64];  // reduced row-echelon basis of the pivot W's
     unsigned pivbit[64];
@@ -138,13 +143,13 @@ __global__ void tile_minc_kernel(const int64_t *__restrict__ off, const int32_t 
         for (int d = 16; d > 0; d >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, d));
         __shared__ int sm[32];
         if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
-        __syncthreads();
+        cta_sync();
         if (threadIdx.x == 0) {
             int v = sm[0];
             for (int w = 1; w < (int)(blockDim.x >> 5); w++) v = min(v, sm[w]);
             tile_minc[t] = v;
         }
-        __syncthreads();
+        cta_sync();
     }
 }
 
@@ -174,7 +179,7 @@ __global__ void __launch_bounds__(kScanThreads) search_kernel(const uint64_t *__
             s_go = ((long long)t < ntiles && (unsigned long long)((long long)t * kTile) <= gb) ? 1u : 0u;
             s_best = kNone;
         }
-        __syncthreads();
+        cta_sync();
         if (!s_go) break;
         const long long tile = s_tile;
         const long long r0 = tile * kTile;
@@ -203,9 +208,9 @@ __global__ void __launch_bounds__(kScanThreads) search_kernel(const uint64_t *__
             wmin = o < wmin ? o : wmin;
         }
         if ((threadIdx.x & 31) == 0 && wmin != kNone) atomicMin(&s_best, wmin);
-        __syncthreads();
+        cta_sync();
         if (threadIdx.x == 0 && s_best != kNone) atomicMin(&slot->best, s_best);
-        __syncthreads();
+        cta_sync();
     }
     for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
     if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
@@ -253,7 +258,7 @@ __global__ void cycle_vector_kernel(uint64_t *C, int W, const int64_t *__restric
                                     const int32_t *__restrict__ coords, const IterSlot *slot) {
     const unsigned long long r = slot->best;
     for (int w = threadIdx.x; w < W; w += blockDim.x) C[w] = 0;
-    __syncthreads();
+    cta_sync();
     if (r == kNone) return;
     for (int64_t i = off[r] + threadIdx.x; i < off[r + 1]; i += blockDim.x) {
         int c = coords[i];
@@ -268,7 +273,7 @@ __global__ void cycle_vector_kernel(uint64_t *C, int W, const int64_t *__restric
 // One warp per word column; also resets the block state (runs first in the block).
 __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int e0, int b, int Wb,
                                      uint64_t *__restrict__ T, BlockState *bs, long long ntiles,
-                                     GridBar *gb, unsigned long long *gmin) {
+                                     GridBar *gb, unsigned long long *gmin, long long window_tiles) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         gb->count = 0;
         gb->abort = 0;
@@ -279,9 +284,14 @@ __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int 
         bs->npairs = 0;
         // stream 25% past the previous block's deepest pivot; the pivot kernel
         // computes any further tile it needs
-        long long lp = e0 == 0 ? ntiles * kTile : bs->last_pivot + 1;
-        long long pred = (lp + lp / 4) / kTile + 8;
+        long long pred = ntiles;
+        if (e0 != 0) {
+            const long long lp = bs->last_pivot + 1;
+            const long long a = (lp + lp / 4) / kTile + 1, m = bs->max_tile + 1;
+            pred = (a > m ? a : m) + window_tiles;
+        }
         bs->pred_tiles = pred < ntiles ? pred : ntiles;
+        bs->max_tile = 0;
     }
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -317,9 +327,9 @@ __device__ __forceinline__ uint64_t fr_reduce(uint64_t W, const uint64_t (*tab)[
 __device__ void fr_build(uint64_t (*tab)[256], const uint64_t *basis, const unsigned *pivbit, unsigned rank) {
     __shared__ uint64_t byBit[64];
     if (threadIdx.x < 64) byBit[threadIdx.x] = 0;
-    __syncthreads();
-    for (unsigned q = threadIdx.x; q < rank; q += blockDim.x) byBit[pivbit[q]] = basis[q];
-    __syncthreads();
+    cta_sync();
+    for (unsigned q = threadIdx.x; q < rank; q += blockDim.x) byBit[pivbit[q] & 63] = basis[q];
+    cta_sync();
     for (int idx = threadIdx.x; idx < 8 * 256; idx += blockDim.x) {
         int g = idx >> 8, pat = idx & 255;
         uint64_t v = 0;
@@ -327,7 +337,7 @@ __device__ void fr_build(uint64_t (*tab)[256], const uint64_t *basis, const unsi
             if (pat & (1 << i)) v ^= byBit[8 * g + i];
         tab[g][pat] = v;
     }
-    __syncthreads();
+    cta_sync();
 }
 
 // ---- grid-wide barrier for the cooperative pivot kernel ----------------------
@@ -335,101 +345,110 @@ __device__ void fr_build(uint64_t (*tab)[256], const uint64_t *basis, const unsi
 // kSpinLimit polls a CTA raises `abort`, every waiter sees it and the kernel ends
 // with ST_WAIT_TIMEOUT instead of hanging.
 
+// Arrive: acq_rel add on the counter (releases this CTA's writes, and the last
+// arriver acquires everyone's); the last arriver then releases `gen`, which the
+// others acquire.  Lane 0 of warp 0 does the atomics and loads; the whole warp
+// runs the wait loop together (values broadcast by shuffle), so it reaches the
+// CTA barrier converged.  Lane 0 ends with an acquire fence and the CTA barrier
+// carries the ordering to the other threads.
+__device__ __forceinline__ unsigned atomic_add_acq_rel(unsigned *p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
 __device__ bool grid_barrier(GridBar *gb, unsigned nctas, unsigned &gen_local) {
     __shared__ unsigned s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned ok = 1;
+    cta_sync();
+    if (threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
         const unsigned g = gen_local;
-        __threadfence();
-        if (atomicAdd(&gb->count, 1u) == nctas - 1) {
-            atomicExch(&gb->count, 0u);
+        unsigned last = 0;
+        if (lane == 0) {
             __threadfence();
-            st_release_u32(&gb->gen, g + 1);
-        } else {
-            unsigned spins = 0;
-            while (ld_acquire_u32(&gb->gen) == g) {
-                if (*((volatile unsigned *)&gb->abort)) {
+            last = atomic_add_acq_rel(&gb->count, 1u) == nctas - 1;
+            if (last) {
+                atomicExch(&gb->count, 0u);
+                __threadfence();
+                st_release_u32(&gb->gen, g + 1);
+            }
+        }
+        last = __shfl_sync(0xffffffffu, last, 0);
+        unsigned ok = 1;
+        if (!last) {
+            for (unsigned spins = 0;; spins++) {
+                unsigned cur = g, ab = 0;
+                if (lane == 0) {
+                    cur = ld_acquire_u32(&gb->gen);
+                    ab = *((volatile unsigned *)&gb->abort);
+                }
+                cur = __shfl_sync(0xffffffffu, cur, 0);
+                ab = __shfl_sync(0xffffffffu, ab, 0);
+                if (cur != g) break;
+                if (ab) {
                     ok = 0;
                     break;
                 }
-                if (++spins > kSpinLimit) {
-                    atomicExch(&gb->abort, 1u);
+                if (spins > kSpinLimit) {
+                    if (lane == 0) atomicExch(&gb->abort, 1u);
                     ok = 0;
                     break;
                 }
                 __nanosleep(20);
             }
         }
+        __syncwarp();
+        if (lane == 0) {
+            fence_acq_rel_gpu();
+            s_ok = ok;
+        }
         gen_local = g + 1;
-        s_ok = ok;
     }
-    __syncthreads();
+    cta_sync();
     return s_ok != 0;
 }
 
-// W of one tile of 1024 candidates into sW (shared), computed by the whole CTA:
-//   W_r = XOR of T[c] over the coordinates c < bound of candidate r.
-// The tile's coordinates are one contiguous run of `coords`; threads read it with
-// 16-byte loads (coalesced), find each element's candidate from the tile's offsets
-// held in shared memory, and fold runs of the same candidate into one shared
-// atomicXor.  A tile whose smallest coordinate is >= bound has W = 0 throughout.
-// Returns, in thread 0, the tile's algorithmic HBM bytes (offsets + coordinates read).
-__device__ unsigned long long compute_w_tile(long long tile, long long K, const int64_t *__restrict__ off,
-                               const int32_t *__restrict__ coords, const int32_t *__restrict__ tile_minc,
-                               const uint64_t *__restrict__ T, int bound, uint64_t *sW, int64_t *soff) {
-    const long long r0 = tile * kTile;
-    const int rn = (int)((K - r0) < kTile ? (K - r0) : kTile);
-    for (int i = threadIdx.x; i < kTile; i += blockDim.x) sW[i] = 0;
-    const bool skip = tile_minc[tile] >= bound;
-    if (!skip)
-        for (int i = threadIdx.x; i <= rn; i += blockDim.x) soff[i] = off[r0 + i];
-    __syncthreads();
-    if (skip) return 4;
-    const int64_t cb = soff[0], ce = soff[rn];
-    for (int64_t i4 = (cb & ~(int64_t)3) + 4 * (int64_t)threadIdx.x; i4 < ce; i4 += 4 * (int64_t)blockDim.x) {
-        const int4 v = *reinterpret_cast<const int4 *>(coords + i4);
-        const int vals[4] = {v.x, v.y, v.z, v.w};
-        int64_t first = i4 < cb ? cb : i4;
-        // candidate owning index `first`: last j with soff[j] <= first
-        int lo = 0, hi = rn - 1;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (soff[mid] <= first)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        int j = lo;
-        uint64_t acc = 0;
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            const int64_t i = i4 + e;
-            if (i < cb || i >= ce) continue;
-            while (soff[j + 1] <= i) {
-                if (acc) atomicXor((unsigned long long *)&sW[j], (unsigned long long)acc);
-                acc = 0;
-                j++;
-            }
-            const int c = vals[e];
-            if (c < bound) acc ^= __ldg(T + c);
-        }
-        if (acc) atomicXor((unsigned long long *)&sW[j], (unsigned long long)acc);
+// W of one candidate: XOR of T over its coordinates below `bound`.  The list is
+// ascending, so reading stops at the first coordinate >= bound; loads are issued
+// four at a time.  *nread counts the coordinates read.
+__device__ __forceinline__ uint64_t w_of_candidate(long long r, const int64_t *__restrict__ off,
+                                                   const int32_t *__restrict__ coords,
+                                                   const uint64_t *__restrict__ T, int bound, unsigned &nread) {
+    int64_t i = __ldg(off + r);
+    const int64_t e = __ldg(off + r + 1);
+    uint64_t W = 0;
+    for (; i + 4 <= e; i += 4) {
+        const int c0 = __ldg(coords + i), c1 = __ldg(coords + i + 1), c2 = __ldg(coords + i + 2),
+                  c3 = __ldg(coords + i + 3);
+        nread += 4;
+        if (c0 >= bound) return W;
+        W ^= __ldg(T + c0);
+        if (c1 >= bound) return W;
+        W ^= __ldg(T + c1);
+        if (c2 >= bound) return W;
+        W ^= __ldg(T + c2);
+        if (c3 >= bound) return W;
+        W ^= __ldg(T + c3);
     }
-    __syncthreads();
-    return 8ull * (unsigned long long)(rn + 1) + 4ull * (unsigned long long)(ce - cb);
+    for (; i < e; i++) {
+        const int c = __ldg(coords + i);
+        nread++;
+        if (c >= bound) break;
+        W ^= __ldg(T + c);
+    }
+    return W;
 }
 
-// Streaming pass: W for tiles [0, bs->pred_tiles), written to Warr and tagged with
-// the block's epoch.  This is the bandwidth-bound part of the block's search.
-__global__ void __launch_bounds__(kScanThreads) blk_w_kernel(long long K, const int64_t *__restrict__ off,
-                                                             const int32_t *__restrict__ coords,
-                                                             const int32_t *__restrict__ tile_minc,
-                                                             const uint64_t *__restrict__ T, int bound,
-                                                             const BlockState *bs, uint64_t *Warr,
-                                                             unsigned *tile_epoch, unsigned long long *bytes) {
-    __shared__ uint64_t sW[kTile];
-    __shared__ int64_t soff[kTile + 1];
+// Streaming pass: W for tiles [0, bs->pred_tiles), one candidate per thread (1024
+// threads = one tile per CTA pass), written to Warr and tagged with the block's
+// epoch.  This is the bandwidth-bound part of the block's search.
+__global__ void __launch_bounds__(kTile) blk_w_kernel(long long K, const int64_t *__restrict__ off,
+                                                    const int32_t *__restrict__ coords,
+                                                    const int32_t *__restrict__ tile_minc,
+                                                    const uint64_t *__restrict__ T, int bound, const BlockState *bs,
+                                                    uint64_t *Warr, unsigned *tile_epoch, unsigned long long *bytes) {
     const unsigned epoch = bs->epoch;
     const long long ntiles = bs->pred_tiles;
     unsigned long long nb = (blockIdx.x == 0 && threadIdx.x == 0) ? 8ull * (unsigned long long)bound : 0ull;
@@ -441,182 +460,427 @@ __global__ void __launch_bounds__(kScanThreads) blk_w_kernel(long long K, const 
             }
             continue;
         }
-        const unsigned long long tb = compute_w_tile(t, K, off, coords, tile_minc, T, bound, sW, soff);
-        const long long r0 = t * kTile;
-        for (int i = threadIdx.x; i < kTile; i += blockDim.x) Warr[r0 + i] = sW[i];
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            tile_epoch[t] = epoch << 1;
-            nb += tb + 8ull * kTile + 8;
+        const long long r = t * kTile + threadIdx.x;
+        uint64_t W = 0;
+        unsigned nread = 0;
+        if (r < K) {
+            W = w_of_candidate(r, off, coords, T, bound, nread);
+            nb += 8 + 8 + 4ull * nread;  // offset, W write, coordinates read
         }
+        Warr[r] = W;
+        cta_sync();
+        if (threadIdx.x == 0) tile_epoch[t] = epoch << 1;
     }
-    if (threadIdx.x == 0 && nb) atomicAdd(bytes, nb);
+    for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
+    if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
 }
 
-// Cooperative pivot extraction.  Step k finds the next pivot exactly: the first
-// candidate at or after the previous pivot whose W is not in the span of the
-// pivots found so far (every candidate before it is in that span, so the first
-// non-zero residual is the next rank-ordered independent W).
+// Cooperative pivot extraction, several pivots per grid barrier.
 //
-// CTA c owns tiles c, c+G, c+2G, ... and keeps the W of its current tile in shared
-// memory across steps.  Each step it reduces that tile against its own copy of the
-// basis (Four-Russians tables), moving on to its next tile when the current one has
-// no non-zero residual at or after the scan start, and reports its first non-zero
-// residual (rank, W) in a per-CTA slot; an atomicMin on the running minimum lets CTAs
-// stop scanning past it.  After one grid barrier every CTA reads all reports in one
-// pass, takes the smallest rank, and applies the same basis update to its tables.
-// Tiles outside the streamed range are computed here and cached in Warr.
+// Definitions: B = the pivots found so far (a reduced row-echelon basis, held by
+// every CTA as Four-Russians tables); s = scan start: every candidate before s has
+// its W in span(B).  A pivot is a candidate whose W is not in the span of all
+// earlier W's.
+//
+// Step, part 1 (no communication): CTA c scans its own tiles t = c (mod G) from s
+// on, up to kWinTiles of them.  It keeps a local basis B ∪ L_c and, in rank order,
+// turns every candidate whose residual against B ∪ L_c is non-zero into a local
+// pivot (appended to L_c).  It stops early after kLmax local pivots.  It reports
+// its local pivots (rank, W) and `end`: every candidate of its tiles below `end`
+// has been processed.
+// Part 2, after one grid barrier, in every CTA identically: D = min over CTAs of
+// `end`.  Every candidate z below D is in span(B ∪ L_c' before z) for its CTA c',
+// so span(W's below r) = span(B ∪ reported local pivots below r) for any r <= D.
+// Hence the global pivots below D are exactly the reported local pivots below D
+// that, taken in rank order, are not in the span of B and the ones accepted
+// before them.  Accept them that way (first non-zero residual against the global
+// tables, add, repeat), then s = D.
+// The reductions below leave one value per warp in a shared slot array (plain
+// stores by lane 0, no shared atomics) and every thread combines the slots after
+// the barrier.  A caller must pass a barrier between reading one call's slots and
+// the next call that writes the same slots.
+constexpr int kWarps = kScanThreads / 32;
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+    for (int d = 16; d > 0; d >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, d);
+        v = o < v ? o : v;
+    }
+    return v;
+}
+
+// Minimum over the CTA (every thread gets it).
+__device__ __forceinline__ unsigned long long block_min_u64(unsigned long long v, unsigned long long *slots) {
+    v = warp_min_u64(v);
+    if ((threadIdx.x & 31) == 0) slots[threadIdx.x >> 5] = v;
+    cta_sync();
+    unsigned long long m = slots[0];
+#pragma unroll
+    for (int w = 1; w < kWarps; w++) m = slots[w] < m ? slots[w] : m;
+    return m;
+}
+
+// Adds v (already reduced against the basis, v != 0) to an RREF basis held as
+// vectors + pivot bits + Four-Russians tables.  Called by the whole CTA; `slots`
+// holds kWarps words.
+__device__ void basis_add(uint64_t (*tab)[256], uint64_t *basis, unsigned *piv, int &rank, uint64_t v,
+                          unsigned long long *slots) {
+    const unsigned qb = (unsigned)(__ffsll((long long)v) - 1) & 63u;
+    const bool mine = threadIdx.x < (unsigned)rank && ((basis[threadIdx.x] >> qb) & 1ull);
+    unsigned long long m = mine ? (1ull << (piv[threadIdx.x] & 63u)) : 0ull;
+    for (int d = 16; d > 0; d >>= 1) m |= __shfl_xor_sync(0xffffffffu, m, d);
+    if ((threadIdx.x & 31) == 0) slots[threadIdx.x >> 5] = m;
+    cta_sync();
+    unsigned long long chg = 1ull << qb;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) chg |= slots[w];
+    for (int idx = threadIdx.x; idx < 8 * 256; idx += blockDim.x) {
+        const int g = idx >> 8, pat = idx & 255;
+        if (__popc(pat & (unsigned)((chg >> (8 * g)) & 255)) & 1) (&tab[0][0])[idx] ^= v;
+    }
+    if (mine) basis[threadIdx.x] ^= v;
+    if (threadIdx.x == 0 && rank < 64) {
+        basis[rank] = v;
+        piv[rank] = qb;
+    }
+    rank++;
+    cta_sync();
+}
+
+// First index (rank order) in the tile with rank >= s and a non-zero residual, or
+// kNoIndex.  `slots` holds kWarps words.
+__device__ unsigned tile_first_nonzero(const uint64_t *sW, const uint64_t (*tab)[256], long long r0, long long s,
+                                       unsigned *slots) {
+    unsigned best = kNoIndex;
+#pragma unroll
+    for (int q = 0; q < kPer; q++) {
+        const int li = q * kScanThreads + threadIdx.x;
+        const bool nz = (r0 + li) >= s && fr_reduce(sW[li], tab) != 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, nz);
+        if (bal && best == kNoIndex) best = (unsigned)(q * kScanThreads + (threadIdx.x & ~31) + __ffs(bal) - 1);
+    }
+    if ((threadIdx.x & 31) == 0) slots[threadIdx.x >> 5] = best;
+    cta_sync();
+    unsigned r = slots[0];
+#pragma unroll
+    for (int w = 1; w < kWarps; w++) r = slots[w] < r ? slots[w] : r;
+    return r;
+}
+
 __global__ void __launch_bounds__(kScanThreads) blk_pivot_kernel(
     long long K, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
     const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T, int bound, BlockState *bs,
-    uint64_t *Warr, unsigned *tile_epoch, unsigned long long *gmin, PivotReport *reports, GridBar *gb,
-    unsigned *status, unsigned long long *bytes) {
+    uint64_t *Warr, unsigned *tile_epoch, PivotReport *reports, GridBar *gb, unsigned *status,
+    unsigned long long *bytes, unsigned long long *diag, unsigned long long *dbg) {
+    // dynamic shared memory: global tables | local tables | tile W's | merge buffers | report staging
+    extern __shared__ __align__(16) unsigned char dsm[];
+    const unsigned G = gridDim.x;
+    uint64_t(*gtab)[256] = reinterpret_cast<uint64_t(*)[256]>(dsm);
+    uint64_t(*ltab)[256] = reinterpret_cast<uint64_t(*)[256]>(dsm + 16384);
+    uint64_t *sW = reinterpret_cast<uint64_t *>(dsm + 32768);
+    unsigned long long *mr = reinterpret_cast<unsigned long long *>(dsm + 32768 + 8 * kTile);  // 2 G kLmax
+    uint64_t *mw = reinterpret_cast<uint64_t *>(mr + 2 * (size_t)G * kLmax);                      // 3 G kLmax
+    unsigned long long *lr = mr + 5 * (size_t)G * kLmax;  // G (2 kLmax + 2)
+    __shared__ uint64_t gbasis[64], lbasis[64];
+    __shared__ unsigned gpiv[64], lpiv[64];
+    __shared__ unsigned s_first[kWarps], s_wcnt[kWarps];
+    __shared__ unsigned long long s_chg[kWarps], s_dmin[kWarps];
+    __shared__ unsigned s_tag;
+    __shared__ uint64_t s_newv[64];
+    __shared__ unsigned s_newq[64];
+    __shared__ int s_nnew;
+    __shared__ unsigned long long sr_rank[kLmax], sr_w[kLmax];
+
+    unsigned long long n_loaded = 0, n_computed = 0, n_local = 0, n_cand = 0;
+    long long cyc_scan = 0, cyc_bar = 0, cyc_merge = 0;
+    unsigned long long nbar = 0;
     unsigned long long nb = 0;
-    __shared__ uint64_t tab[8][256];
-    __shared__ uint64_t sW[kTile];
-    __shared__ int64_t soff[kTile + 1];
-    __shared__ uint64_t sbasis[64];
-    __shared__ unsigned spiv[64];
-    __shared__ unsigned s_go;
-    __shared__ unsigned long long s_min, s_chg;
-    __shared__ unsigned long long s_wr[kScanThreads / 32];
-    __shared__ unsigned long long s_ww[kScanThreads / 32];
     const unsigned epoch = bs->epoch;
     const int b = (int)bs->b;
     const long long ntiles = (K + kTile - 1) / kTile;
-    const long long G = gridDim.x, c = blockIdx.x;
+    const long long c = blockIdx.x;
     unsigned gen = ld_acquire_u32(&gb->gen);
-    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&tab[0][0])[i] = 0;
-    long long cur = -1;  // owned tile whose W is in sW
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&gtab[0][0])[i] = 0;
+    long long cur = -1;  // tile whose W is in sW
+    long long maxt = 0;  // deepest tile this CTA touched
     long long s = 0;
-    int rank = 0;
+    int grank = 0;
     bool ok = true;
-    __syncthreads();
-    for (int k = 0; k < b; k++) {
-        unsigned long long *slot = gmin + (k % 3);
-        PivotReport *rep = reports + (size_t)(k & 1) * G;
-        if (c == 0 && threadIdx.x == 0) gmin[(k + 1) % 3] = kNone;
+    unsigned k = 0;
+    cta_sync();
+    while (grank < b) {
+        unsigned long long *rep_rank =
+            reinterpret_cast<unsigned long long *>(reports) + (size_t)(k & 1) * G * (2 * kLmax + 2);
+        unsigned long long *rep_w = rep_rank + (size_t)G * kLmax;
+        unsigned long long *rep_end = rep_w + (size_t)G * kLmax;
+        unsigned long long *rep_n = rep_end + G;
+        // ---- part 1: local pivots over this CTA's window ----
+        const long long c0 = clock64();
+        for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&ltab[0][0])[i] = (&gtab[0][0])[i];
+        if (threadIdx.x < 64) {
+            lbasis[threadIdx.x] = gbasis[threadIdx.x];
+            lpiv[threadIdx.x] = gpiv[threadIdx.x];
+        }
+        int lrank = grank;
+        cta_sync();
         const long long t0 = s / kTile;
-        long long t = t0 + ((c - t0 % G) + G) % G;  // first owned tile at or after t0
-        unsigned long long found_r = kNone, found_w = 0;
-        for (; t < ntiles; t += G) {
-            if (threadIdx.x == 0) s_go = (unsigned long long)(t * kTile) <= *((volatile unsigned long long *)slot);
-            __syncthreads();
-            if (!s_go) break;
+        long long t = t0 + (((long long)c - t0 % G) + G) % G;
+        int nloc = 0;
+        long long end = K;
+        for (int m = 0; m < kWinTiles; m++, t += G) {
+            if (t >= ntiles) {
+                end = K;
+                break;
+            }
             const long long r0 = t * kTile;
+            maxt = t > maxt ? t : maxt;
             if (t != cur) {
-                const unsigned tag = *((volatile unsigned *)&tile_epoch[t]);
+                // one thread reads the tag and the CTA branches on the shared copy
+                if (threadIdx.x == 0) s_tag = ld_acquire_u32(&tile_epoch[t]);
+                cta_sync();
+                const unsigned tag = s_tag;
                 if ((tag >> 1) == epoch) {
                     if (tag & 1u) {
                         for (int i = threadIdx.x; i < kTile; i += blockDim.x) sW[i] = 0;
                     } else {
                         for (int i = threadIdx.x; i < kTile; i += blockDim.x)
                             sW[i] = (r0 + i < K) ? __ldcg(Warr + r0 + i) : 0;
-                        nb += 8ull * kTile;
+                        if (threadIdx.x == 0) nb += 8ull * kTile;
                     }
-                    __syncthreads();
+                    n_loaded++;
+                    cta_sync();
                 } else {
-                    const unsigned long long tb = compute_w_tile(t, K, off, coords, tile_minc, T, bound, sW, soff);
-                    for (int i = threadIdx.x; i < kTile; i += blockDim.x) Warr[r0 + i] = sW[i];
-                    __syncthreads();
+                    const bool zero = tile_minc[t] >= bound;
+                    unsigned nread = 0;
+                    for (int i = threadIdx.x; i < kTile; i += blockDim.x) {
+                        uint64_t W = 0;
+                        if (!zero && r0 + i < K) W = w_of_candidate(r0 + i, off, coords, T, bound, nread);
+                        sW[i] = W;
+                        Warr[r0 + i] = W;
+                    }
+                    cta_sync();
                     if (threadIdx.x == 0) {
                         __threadfence();
                         tile_epoch[t] = epoch << 1;
                     }
-                    nb += tb + 8ull * kTile;
+                    nb += 4ull * nread + (threadIdx.x == 0 ? 16ull * kTile : 0ull);
+                    n_computed++;
                 }
                 cur = t;
             }
-            if (threadIdx.x == 0) s_min = kNone;
-            __syncthreads();
-#pragma unroll
-            for (int q = 0; q < kPer; q++) {
-                const int li = q * kScanThreads + threadIdx.x;
-                const bool nz = (r0 + li) >= s && fr_reduce(sW[li], tab) != 0;
-                const unsigned bal = __ballot_sync(0xffffffffu, nz);
-                if (bal && (threadIdx.x & 31) == 0)
-                    atomicMin(&s_min, (unsigned long long)(r0 + q * kScanThreads + (threadIdx.x & ~31) + __ffs(bal) - 1));
+            bool trunc = false;
+            for (;;) {
+                const unsigned li = tile_first_nonzero(sW, ltab, r0, s, s_first);
+                if (li >= (unsigned)kTile) break;
+                const uint64_t w = sW[li];
+                const uint64_t x = fr_reduce(w, ltab);
+                if (threadIdx.x == 0) {
+                    sr_rank[nloc] = (unsigned long long)(r0 + li);
+                    sr_w[nloc] = w;
+                }
+                cta_sync();
+                basis_add(ltab, lbasis, lpiv, lrank, x, s_chg);
+                nloc++;
+                if (nloc == kLmax) {
+                    end = r0 + li + 1;
+                    trunc = true;
+                    break;
+                }
             }
-            __syncthreads();
-            if (s_min != kNone) {
-                found_r = s_min;
-                found_w = sW[found_r - r0];
-                break;
-            }
+            if (trunc) break;
+            end = (r0 + kTile < K) ? r0 + kTile : K;
         }
+        n_local += nloc;
         if (threadIdx.x == 0) {
-            rep[c].rank = found_r;
-            rep[c].w = found_w;
-            if (found_r != kNone) atomicMin(slot, found_r);
+            for (int j = 0; j < nloc; j++) {
+                rep_rank[c * kLmax + j] = sr_rank[j];
+                rep_w[c * kLmax + j] = sr_w[j];
+            }
+            rep_end[c] = (unsigned long long)end;
+            rep_n[c] = (unsigned long long)nloc;
         }
-        if (!grid_barrier(gb, (unsigned)G, gen)) {
+        const long long c1 = clock64();
+        nbar++;
+        if (!grid_barrier(gb, G, gen)) {
+            if (threadIdx.x == 0) {  // where the wait gave up
+                atomicExch(&diag[9], (unsigned long long)c + 1);
+                atomicExch(&diag[10], (unsigned long long)k);
+                atomicExch(&diag[11], (unsigned long long)grank);
+                atomicExch(&diag[12], (unsigned long long)gen);
+                atomicExch(&diag[13], (unsigned long long)*((volatile unsigned *)&gb->count));
+            }
             ok = false;
             break;
         }
-        // smallest reported rank and its W (one coalesced pass over the reports)
-        unsigned long long br = kNone, bw = 0;
-        for (long long i = threadIdx.x; i < G; i += blockDim.x) {
-            const unsigned long long r = __ldcg(&rep[i].rank);
-            if (r < br) {
-                br = r;
-                bw = __ldcg(&rep[i].w);
+        const long long c2 = clock64();
+        cyc_scan += c1 - c0;
+        cyc_bar += c2 - c1;
+        if (k > 0 && c == 0 && threadIdx.x < G) {  // compare the previous step's merge results
+            const unsigned long long *prev = dbg + (size_t)((k - 1) & 1) * G;
+            if (__ldcg(prev + threadIdx.x) != __ldcg(prev)) {
+                atomicOr(status, ST_DIVERGED);
+                if (atomicCAS(&diag[16], 0ull, 1ull) == 0ull) {
+                    diag[17] = (unsigned long long)(k - 1);
+                    diag[18] = (unsigned long long)threadIdx.x;
+                    diag[19] = epoch;
+                }
             }
         }
-        for (int d = 16; d > 0; d >>= 1) {
-            const unsigned long long orr = __shfl_xor_sync(0xffffffffu, br, d);
-            const unsigned long long ow = __shfl_xor_sync(0xffffffffu, bw, d);
-            if (orr < br) {
-                br = orr;
-                bw = ow;
+        // ---- part 2: merge (identical in every CTA) ----
+        // all reports into shared memory with independent loads (one round trip)
+        const unsigned words = G * (2 * kLmax + 2);
+        for (unsigned i = threadIdx.x; i < words; i += blockDim.x) lr[i] = __ldcg(rep_rank + i);
+        cta_sync();
+        const unsigned long long *l_rank = lr, *l_w = lr + (size_t)G * kLmax, *l_end = l_w + (size_t)G * kLmax,
+                                 *l_n = l_end + G;
+        unsigned long long dmin = kNone;
+        for (unsigned i = threadIdx.x; i < G; i += blockDim.x) dmin = l_end[i] < dmin ? l_end[i] : dmin;
+        const unsigned long long D = block_min_u64(dmin, s_dmin);
+        // the reports below D, CTA by CTA (a CTA's ranks ascend): per-CTA counts,
+        // block prefix sum, copy
+        unsigned cnt = 0;
+        const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        for (unsigned cb = 0; cb < G; cb += blockDim.x) {
+            const unsigned cc = cb + threadIdx.x;
+            unsigned n = 0;
+            if (cc < G) {
+                const unsigned ln = l_n[cc] < (unsigned long long)kLmax ? (unsigned)l_n[cc] : (unsigned)kLmax;
+                while (n < ln && l_rank[(size_t)cc * kLmax + n] < D) n++;
             }
-        }
-        if ((threadIdx.x & 31) == 0) {
-            s_wr[threadIdx.x >> 5] = br;
-            s_ww[threadIdx.x >> 5] = bw;
-        }
-        if (threadIdx.x == 0) s_chg = 0;
-        __syncthreads();
-        unsigned long long p = kNone, Wp = 0;
-        for (int w = 0; w < kScanThreads / 32; w++)
-            if (s_wr[w] < p) {
-                p = s_wr[w];
-                Wp = s_ww[w];
+            unsigned incl = n;
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= (unsigned)d) incl += v;
             }
-        if (p == kNone) {
+            if (lane == 31) s_wcnt[wid] = incl;
+            cta_sync();
+            unsigned before = 0, all = 0;
+#pragma unroll
+            for (int x = 0; x < kWarps; x++) {
+                const unsigned v = s_wcnt[x];
+                before += (unsigned)x < wid ? v : 0u;
+                all += v;
+            }
+            const unsigned o = cnt + before + incl - n;
+            for (unsigned j = 0; j < n && o + j < G * kLmax; j++) {
+                mr[o + j] = l_rank[(size_t)cc * kLmax + j];
+                mw[o + j] = l_w[(size_t)cc * kLmax + j];
+            }
+            cnt += all;
+            cta_sync();
+        }
+        if (cnt > G * kLmax) cnt = G * kLmax;
+        n_cand += cnt;
+        // rank order: each candidate's position = number of smaller ranks (ranks are distinct)
+        unsigned long long *sr = mr + cnt;  // sorted ranks
+        uint64_t *sz = mw + cnt;            // sorted residuals against the global basis
+        uint64_t *sw = sz + cnt;            // sorted W
+        for (unsigned i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const unsigned long long r = mr[i];
+            unsigned pos = 0;
+            for (unsigned j = 0; j < cnt; j++) pos += mr[j] < r;
+            sr[pos] = r;
+            sw[pos] = mw[i];
+            sz[pos] = fr_reduce(mw[i], gtab);
+        }
+        cta_sync();
+        // greedy echelon in rank order (warp 0): a candidate is a new global pivot iff
+        // its residual is not in the span of the new pivots before it
+        if (threadIdx.x < 32) {
+            int nn = 0;
+            for (unsigned base = 0; base < cnt && grank + nn < b; base += 32) {
+                uint64_t z = base + lane < cnt ? sz[base + lane] : 0ull;
+                for (int j = 0; j < nn; j++)
+                    if ((z >> s_newq[j]) & 1ull) z ^= s_newv[j];
+                for (;;) {
+                    const unsigned bal = __ballot_sync(0xffffffffu, z != 0);
+                    if (!bal || grank + nn >= b) break;
+                    const int pl = __ffs(bal) - 1;
+                    const uint64_t v = __shfl_sync(0xffffffffu, z, pl);
+                    const unsigned qb = (unsigned)(__ffsll((long long)v) - 1);
+                    if (lane == 0) {
+                        s_newv[nn] = v;
+                        s_newq[nn] = qb;
+                        if (c == 0) {
+                            bs->pivrank[grank + nn] = (long long)sr[base + pl];
+                            bs->pivW[grank + nn] = sw[base + pl];
+                        }
+                    }
+                    nn++;
+                    if ((z >> qb) & 1ull) z ^= v;
+                }
+                __syncwarp();
+            }
+            if (lane == 0) s_nnew = nn;
+        }
+        cta_sync();
+        const int nnew = s_nnew;
+        if (nnew > 0) {
+            // bring the new vectors to reduced form among themselves (latest first),
+            // clear their pivot bits from the old basis vectors, append, rebuild tables
+            if (threadIdx.x == 0)
+                for (int j = nnew - 1; j >= 0; j--)
+                    for (int jj = j + 1; jj < nnew; jj++)
+                        if ((s_newv[j] >> s_newq[jj]) & 1ull) s_newv[j] ^= s_newv[jj];
+            cta_sync();
+            if (threadIdx.x < (unsigned)grank) {
+                uint64_t v = gbasis[threadIdx.x];
+                for (int j = 0; j < nnew; j++)
+                    if ((v >> s_newq[j]) & 1ull) v ^= s_newv[j];
+                gbasis[threadIdx.x] = v;
+            }
+            if (threadIdx.x < (unsigned)nnew && grank + threadIdx.x < 64) {
+                gbasis[grank + threadIdx.x] = s_newv[threadIdx.x];
+                gpiv[grank + threadIdx.x] = s_newq[threadIdx.x];
+            }
+            grank += nnew;
+            cta_sync();
+            fr_build(gtab, gbasis, gpiv, (unsigned)grank);
+        }
+        if (nnew == 0 && D >= (unsigned long long)K) {
             if (c == 0 && threadIdx.x == 0) atomicOr(status, ST_RANK_DEFICIT);
             ok = false;
             break;
         }
-        const uint64_t v = fr_reduce(Wp, tab);
-        const unsigned qb = (unsigned)(__ffsll((long long)v) - 1);
-        // vectors that change when bit qb is cleared from them, plus the new one
-        if (threadIdx.x < (unsigned)rank && ((sbasis[threadIdx.x] >> qb) & 1ull))
-            atomicOr(&s_chg, 1ull << spiv[threadIdx.x]);
-        __syncthreads();
-        const unsigned long long chg = s_chg | (1ull << qb);
-        for (int idx = threadIdx.x; idx < 8 * 256; idx += blockDim.x) {
-            const int g = idx >> 8, pat = idx & 255;
-            if (__popc(pat & (unsigned)((chg >> (8 * g)) & 255)) & 1) (&tab[0][0])[idx] ^= v;
+        s = (long long)D;
+        if (threadIdx.x == 0) {  // self-check: every CTA must reach the same merge result
+            unsigned long long h = 1469598103934665603ull;
+            h = (h ^ (unsigned long long)grank) * 1099511628211ull;
+            h = (h ^ D) * 1099511628211ull;
+            h = (h ^ (unsigned long long)cnt) * 1099511628211ull;
+            dbg[(size_t)(k & 1) * G + c] = h;
         }
-        if (threadIdx.x < (unsigned)rank && ((sbasis[threadIdx.x] >> qb) & 1ull)) sbasis[threadIdx.x] ^= v;
-        if (threadIdx.x == 0) {
-            sbasis[rank] = v;
-            spiv[rank] = qb;
-            if (c == 0) {
-                bs->pivrank[rank] = (long long)p;
-                bs->pivW[rank] = Wp;
-            }
-        }
-        rank++;
-        s = (long long)p + 1;
-        __syncthreads();
+        k++;
+        cyc_merge += clock64() - c2;
     }
     if (!ok && threadIdx.x == 0 && (*((volatile unsigned *)&gb->abort))) atomicOr(status, ST_WAIT_TIMEOUT);
-    if (threadIdx.x == 0 && nb) atomicAdd(bytes, nb);
-    if (c == 0 && threadIdx.x == 0) {
-        bs->rank = (unsigned)rank;
-        bs->last_pivot = s - 1;
+    for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
+    if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
+    if (threadIdx.x == 0) {
+        atomicMax(&diag[14], nbar);
+        atomicMin(&diag[15], nbar);
+        atomicMax((unsigned long long *)&bs->max_tile, (unsigned long long)maxt);
+        atomicAdd(&diag[1], n_local);
+        atomicAdd(&diag[3], n_loaded);
+        atomicAdd(&diag[4], n_computed);
     }
+    if (c == 0 && threadIdx.x == 0) {
+        bs->rank = (unsigned)grank;
+        bs->last_pivot = grank > 0 ? bs->pivrank[grank - 1] : 0;
+        atomicAdd(&diag[0], (unsigned long long)k);
+        atomicAdd(&diag[2], n_cand);
+        atomicAdd(&diag[5], 1ull);
+        atomicAdd(&diag[6], (unsigned long long)cyc_scan);
+        atomicAdd(&diag[7], (unsigned long long)cyc_bar);
+        atomicAdd(&diag[8], (unsigned long long)cyc_merge);
+    }
+}
+
+// Dynamic shared memory of blk_pivot_kernel for a grid of G CTAs: two sets of
+// Four-Russians tables, one tile of W's, the merge buffers (5 x G x kLmax words)
+// and the report staging (G x (2 kLmax + 2) words).
+size_t pivot_smem_bytes(int G) {
+    return 32768 + 8 * (size_t)kTile + 8 * 5 * (size_t)G * kLmax + 8 * (size_t)G * (2 * kLmax + 2);
 }
 
 // Resolve the block's b iterations on masks.  Pivot index = rank order.
@@ -647,7 +911,7 @@ __global__ void __launch_bounds__(256) blk_resolve_kernel(BlockState *bs, int e0
         s_r[tid] = tid < b ? bs->pivrank[tid] : -1;
     }
     if (tid == 0) s_fail = 0;
-    __syncthreads();
+    cta_sync();
     if (tid < 32) {
         const uint64_t w0 = s_w[lane], w1 = s_w[32 + lane];
         uint64_t m0 = 1ull << lane, m1 = 1ull << (32 + lane);
@@ -681,7 +945,7 @@ __global__ void __launch_bounds__(256) blk_resolve_kernel(BlockState *bs, int e0
         bs->mask[lane] = m0;
         bs->mask[32 + lane] = m1;
     }
-    __syncthreads();
+    cta_sync();
     if (s_fail) {
         if (tid == 0) atomicOr(status, ST_NO_CANDIDATE);
         return;
@@ -707,7 +971,7 @@ __global__ void __launch_bounds__(256) blk_resolve_kernel(BlockState *bs, int e0
         for (int d = 16; d > 0; d >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, d);
         if (lane == 0) atomicAdd(&bs->total, wsum);
     }
-    __syncthreads();
+    cta_sync();
     if (tid == 0) {
         s_pre[0] = 0;
         const unsigned carry = s_pre[32];
@@ -716,7 +980,7 @@ __global__ void __launch_bounds__(256) blk_resolve_kernel(BlockState *bs, int e0
         bs->npairs = total < pair_cap ? total : pair_cap;
         if (total > pair_cap) atomicOr(status, ST_BAD_INPUT);
     }
-    __syncthreads();
+    cta_sync();
     const unsigned total = s_pre[64] < pair_cap ? s_pre[64] : pair_cap;
     for (unsigned i = tid; i < total; i += blockDim.x) {
         int lo = 0, hi = b - 1;  // last k with s_pre[k] <= i
@@ -743,7 +1007,7 @@ __global__ void blk_materialize_kernel(uint64_t *S, int P, int e0, int Wb, const
         int l = idx >> 5, w = idx & 31;
         s0[l][w] = (l < b && w0 + w < Wb) ? S[(size_t)(e0 + l) * P + w0 + w] : 0ull;
     }
-    __syncthreads();
+    cta_sync();
     for (int idx = threadIdx.x; idx < 64 * 32; idx += blockDim.x) {
         int k = idx >> 5, w = idx & 31;
         if (k >= b || w0 + w >= Wb) continue;
@@ -779,9 +1043,11 @@ __global__ void blk_tables_kernel(const uint64_t *__restrict__ S, int P, int e0,
     }
 }
 
-// One warp per row j >= e0+b: D_j (64 bits) = <C_sel_k, S_j>, then
-// beta_k = D_k ^ <beta_{<k}, gcol_k> (the sequential effect of the block's updates),
-// then S_j ^= XOR_k beta_k S_{e0+k} through the tables.
+// Rows j >= e0+b, kUpdRows rows per warp.  D_j (64 bits) = <C_sel_k, S_j> (lanes split the
+// chosen cycles' (coordinate, k) pairs, one row at a time); then lane i computes,
+// for row i of the group, beta_k = D_k ^ <beta_{<k}, gcol_k> (the sequential effect
+// of the block's 64 updates); then S_j ^= XOR_k beta_k S_{e0+k} through the tables,
+// lanes split the row's words.
 __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int Pt,
                                   const uint64_t *__restrict__ tab, const BlockState *bs,
                                   const unsigned *__restrict__ pairs, unsigned long long *bytes) {
@@ -790,39 +1056,52 @@ __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int
     const int b = (int)bs->b;
     const unsigned np = bs->npairs;
     if (threadIdx.x < 64) sg[threadIdx.x] = threadIdx.x < b ? bs->gcol[threadIdx.x] : 0;
-    __syncthreads();
+    cta_sync();
     const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int j = e0 + b + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); j < N; j += warps) {
-        uint64_t *Sj = S + (size_t)j * P;
-        uint64_t D = 0;
-        for (unsigned i = lane; i < np; i += 32) {
-            unsigned pr = pairs[i];
-            unsigned c = pr >> 6, k = pr & 63u;
-            D ^= ((Sj[c >> 6] >> (c & 63)) & 1ull) << k;
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long first = e0 + b;
+    for (long long g0 = first + kUpdRows * (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); g0 < N;
+         g0 += kUpdRows * warps) {
+        const int rows = (int)((N - g0) < kUpdRows ? (N - g0) : kUpdRows);
+        uint64_t Dmine = 0;
+        for (int r = 0; r < rows; r++) {
+            const uint64_t *Sj = S + (size_t)(g0 + r) * P;
+            uint64_t D = 0;
+#pragma unroll 4
+            for (unsigned i = lane; i < np; i += 32) {
+                const unsigned pr = __ldg(pairs + i);
+                const unsigned c = pr >> 6, k = pr & 63u;
+                D ^= ((Sj[c >> 6] >> (c & 63)) & 1ull) << k;
+            }
+            for (int d = 16; d > 0; d >>= 1) D ^= __shfl_xor_sync(0xffffffffu, D, d);
+            if (lane == r) Dmine = D;
         }
-        for (int d = 16; d > 0; d >>= 1) D ^= __shfl_xor_sync(0xffffffffu, D, d);
         uint64_t beta = 0;
-        for (int k = 0; k < b; k++) {
-            uint64_t bk = ((D >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]);
-            beta |= bk << k;
+        if (lane < rows) {
+            for (int k = 0; k < b; k++) beta |= ((((Dmine >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]))) << k;
+            // algorithmic bytes: the words of S_j the pairs touch (its support is [0, j])
+            // plus, when it changes, read + write of its first Wb words
+            const long long j = g0 + lane;
+            const unsigned wj = (unsigned)(j >> 6) + 1;
+            nb += 8ull * (np < wj ? np : wj) + (beta ? 16ull * (unsigned long long)Wb : 0ull);
         }
-        // algorithmic bytes: the words of S_j the pairs touch (at most its support
-        // [0, j]) plus, when it changes, read + write of its first Wb words
-        const unsigned wj = (unsigned)(j >> 6) + 1;
-        nb += 8ull * (np < wj ? np : wj) + (beta ? 16ull * (unsigned long long)Wb : 0ull);
-        if (!beta) continue;
-        const uint64_t *t0 = tab + ((size_t)0 * 256 + ((beta >> 0) & 255)) * Pt;
-        const uint64_t *t1 = tab + ((size_t)1 * 256 + ((beta >> 8) & 255)) * Pt;
-        const uint64_t *t2 = tab + ((size_t)2 * 256 + ((beta >> 16) & 255)) * Pt;
-        const uint64_t *t3 = tab + ((size_t)3 * 256 + ((beta >> 24) & 255)) * Pt;
-        const uint64_t *t4 = tab + ((size_t)4 * 256 + ((beta >> 32) & 255)) * Pt;
-        const uint64_t *t5 = tab + ((size_t)5 * 256 + ((beta >> 40) & 255)) * Pt;
-        const uint64_t *t6 = tab + ((size_t)6 * 256 + ((beta >> 48) & 255)) * Pt;
-        const uint64_t *t7 = tab + ((size_t)7 * 256 + ((beta >> 56) & 255)) * Pt;
-        for (int w = lane; w < Wb; w += 32)
-            Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
+        for (int r = 0; r < rows; r++) {
+            const uint64_t bt = __shfl_sync(0xffffffffu, beta, r);
+            if (!bt) continue;
+            uint64_t *Sj = S + (size_t)(g0 + r) * P;
+            const uint64_t *t0 = tab + ((size_t)0 * 256 + ((bt >> 0) & 255)) * Pt;
+            const uint64_t *t1 = tab + ((size_t)1 * 256 + ((bt >> 8) & 255)) * Pt;
+            const uint64_t *t2 = tab + ((size_t)2 * 256 + ((bt >> 16) & 255)) * Pt;
+            const uint64_t *t3 = tab + ((size_t)3 * 256 + ((bt >> 24) & 255)) * Pt;
+            const uint64_t *t4 = tab + ((size_t)4 * 256 + ((bt >> 32) & 255)) * Pt;
+            const uint64_t *t5 = tab + ((size_t)5 * 256 + ((bt >> 40) & 255)) * Pt;
+            const uint64_t *t6 = tab + ((size_t)6 * 256 + ((bt >> 48) & 255)) * Pt;
+            const uint64_t *t7 = tab + ((size_t)7 * 256 + ((bt >> 56) & 255)) * Pt;
+            for (int w = lane; w < Wb; w += 32)
+                Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
+        }
     }
+    for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
     if (lane == 0 && nb) atomicAdd(bytes, nb);
 }
 
@@ -869,6 +1148,7 @@ struct mcbgpu_solver {
     std::vector<cudaEvent_t> pool;
     size_t pool_next = 0;
     unsigned long long *d_bytes = nullptr;  // KC_COUNT counters
+    unsigned long long *d_diag = nullptr;   // pivot-kernel counters (see mcbgpu_solver_diagnostics)
 };
 
 namespace {
@@ -931,6 +1211,7 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_status);
     cudaFree(s->d_check);
     cudaFree(s->d_bytes);
+    cudaFree(s->d_diag);
     for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
     delete s;
 }
@@ -1002,18 +1283,26 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_status, sizeof(unsigned));
     ALLOC(s->d_bytes, sizeof(unsigned long long) * KC_COUNT);
     ALLOC(s->d_check, sizeof(unsigned) * 2);
+    ALLOC(s->d_diag, sizeof(unsigned long long) * (32 + 8 * 1024));
 #undef ALLOC
+    if (e == cudaSuccess) e = cudaMemset(s->d_diag, 0, sizeof(unsigned long long) * 32);
     if (e == cudaSuccess) e = cudaMemset(s->d_bytes, 0, sizeof(unsigned long long) * KC_COUNT);
     if (e == cudaSuccess) e = cudaMemset(s->d_tile_epoch, 0, sizeof(unsigned) * ntiles);
     if (e == cudaSuccess) e = cudaMemset(s->d_gbar, 0, sizeof(GridBar));
     if (e == cudaSuccess) e = cudaMemset(s->d_coords, 0, sizeof(int32_t) * (size_t)(nnz + 4));
     if (e == cudaSuccess) {
+        const int G = s->sm_count > 0 ? s->sm_count : 1;  // one CTA per SM
+        const size_t smem = pivot_smem_bytes(G);
+        e = cudaFuncSetAttribute(blk_pivot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blk_pivot_kernel, kScanThreads, 0);
-        if (per_sm > 1) per_sm = 1;
-        s->pivot_grid = per_sm * (s->sm_count > 0 ? s->sm_count : 1);
-        if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_reports, sizeof(PivotReport) * 2 * (size_t)s->pivot_grid);
-        bytes += (long long)sizeof(PivotReport) * 2 * s->pivot_grid;
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blk_pivot_kernel, kScanThreads, smem);
+        if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
+        s->pivot_grid = G;
+        // two step-parity halves of: ranks + W's (G x kLmax each), ends, counts (G each)
+        const size_t rb = sizeof(unsigned long long) * 2 * (size_t)G * (2 * kLmax + 2);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_reports, rb);
+        bytes += (long long)rb;
     }
     if (e == cudaSuccess) e = cudaMemset(s->d_bs, 0, sizeof(BlockState));
     if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(unsigned));
@@ -1217,11 +1506,12 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         {
             Launch L(s, KC_TRANSPOSE, st);
             blk_transpose_kernel<<<(Wb + 7) / 8, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles,
-                                                              s->d_gbar, s->d_gmin);
+                                                              s->d_gbar, s->d_gmin,
+                                                              (long long)s->pivot_grid * kWinTiles);
         }
         if (ntiles > 0) {
             Launch L(s, KC_WSTREAM, st);
-            blk_w_kernel<<<sms * 4, kScanThreads, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+            blk_w_kernel<<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
                                                           s->d_bs, s->d_Warr, s->d_tile_epoch, L.bytes());
         }
         {
@@ -1234,14 +1524,15 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             BlockState *bs = s->d_bs;
             uint64_t *Wa = s->d_Warr;
             unsigned *te = s->d_tile_epoch;
-            unsigned long long *gm = s->d_gmin;
             GridBar *gb = s->d_gbar;
             unsigned *stt = s->d_status;
             PivotReport *rp = s->d_reports;
             unsigned long long *nb = L.bytes();
-            void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &gm, &rp, &gb, &stt, &nb};
+            unsigned long long *dg = s->d_diag;
+            unsigned long long *db = s->d_diag + 32;
+            void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db};
             MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kScanThreads),
-                                                 args, 0, st));
+                                                 args, pivot_smem_bytes(s->pivot_grid), st));
         }
         {
             Launch L(s, KC_RESOLVE, st);
@@ -1260,8 +1551,9 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             }
             Launch L(s, KC_BLK_UPDATE, st);
             int rows = (int)(s->N - (e0 + b));
-            int grid = (rows + 7) / 8;
+            int grid = (rows + 8 * kUpdRows - 1) / (8 * kUpdRows);  // 8 warps x kUpdRows rows per CTA pass
             if (grid > sms * 8) grid = sms * 8;
+            if (grid < 1) grid = 1;
             blk_update_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P, (int)e0, Wb, s->P, s->d_tab, s->d_bs,
                                                     s->d_pairs, L.bytes());
         }
@@ -1343,6 +1635,22 @@ int mcbgpu_solver_kernel_stats(mcbgpu_solver *s, mcbgpu_kernel_stat *out, int ma
     s->recs.clear();
     s->pool_next = 0;
     MCB_CUDA(cudaMemset(s->d_bytes, 0, sizeof(unsigned long long) * KC_COUNT));
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_diagnostics(mcbgpu_solver *s, int64_t *out, int n, int reset) {
+    if (!s || (!out && n > 0) || n > 32) {
+        set_error("mcbgpu_solver_diagnostics: invalid argument");
+        return MCBGPU_E_ARG;
+    }
+    unsigned long long v[32];
+    MCB_CUDA(cudaDeviceSynchronize());
+    MCB_CUDA(cudaMemcpy(v, s->d_diag, sizeof v, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) out[i] = (int64_t)v[i];
+    if (reset) {
+        MCB_CUDA(cudaMemset(s->d_diag, 0, sizeof v));
+        MCB_CUDA(cudaMemset(s->d_diag + 15, 0xff, sizeof(unsigned long long)));
+    }
     return MCBGPU_OK;
 }
 

@@ -182,6 +182,16 @@ class Solver:
         return {arr[i].name.decode(): {"launches": arr[i].launches, "ms": arr[i].ms, "bytes": arr[i].bytes}
                 for i in range(min(cnt.value, 32))}
 
+    def diagnostics(self, reset: bool = True) -> dict:
+        """Counters of the blocked search since the last reset."""
+        out = np.zeros(32, np.int64)
+        check_gpu(self.lib.mcbgpu_solver_diagnostics(self._h, ptr(out), 32, int(reset)), "mcbgpu_solver_diagnostics")
+        keys = ["pivot_steps", "local_pivots", "merge_candidates", "tiles_loaded", "tiles_computed", "blocks",
+                "cycles_scan", "cycles_barrier", "cycles_merge", "timeout_cta_plus1", "timeout_step", "timeout_rank",
+                "timeout_gen", "timeout_count", "max_barriers_per_cta", "min_barriers_per_cta", "diverged",
+                "div_step", "div_cta", "div_epoch"]
+        return dict(zip(keys, out.tolist()))
+
     @property
     def launches(self) -> int:
         return int(self.lib.mcbgpu_solver_launches(self._h))
