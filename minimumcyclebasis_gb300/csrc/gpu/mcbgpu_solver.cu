@@ -410,33 +410,32 @@ __device__ bool grid_barrier(GridBar *gb, unsigned nctas, unsigned &gen_local) {
     return s_ok != 0;
 }
 
-// W of one candidate: XOR of T over its coordinates below `bound`.  The list is
-// ascending, so reading stops at the first coordinate >= bound; loads are issued
-// four at a time.  *nread counts the coordinates read.
+// W of one candidate: XOR of T over its coordinates below `bound`.  Coordinates
+// are read kWChunk at a time (independent loads), then their T words are gathered
+// (independent loads), so a list costs two memory round trips per kWChunk
+// coordinates.  The list is ascending: a chunk whose last coordinate is >= bound
+// ends the walk, and its coordinates >= bound gather nothing.  `nread` counts the
+// coordinates read.
+constexpr int kWChunk = 8;
+
 __device__ __forceinline__ uint64_t w_of_candidate(long long r, const int64_t *__restrict__ off,
                                                    const int32_t *__restrict__ coords,
                                                    const uint64_t *__restrict__ T, int bound, unsigned &nread) {
     int64_t i = __ldg(off + r);
     const int64_t e = __ldg(off + r + 1);
     uint64_t W = 0;
-    for (; i + 4 <= e; i += 4) {
-        const int c0 = __ldg(coords + i), c1 = __ldg(coords + i + 1), c2 = __ldg(coords + i + 2),
-                  c3 = __ldg(coords + i + 3);
-        nread += 4;
-        if (c0 >= bound) return W;
-        W ^= __ldg(T + c0);
-        if (c1 >= bound) return W;
-        W ^= __ldg(T + c1);
-        if (c2 >= bound) return W;
-        W ^= __ldg(T + c2);
-        if (c3 >= bound) return W;
-        W ^= __ldg(T + c3);
-    }
-    for (; i < e; i++) {
-        const int c = __ldg(coords + i);
-        nread++;
-        if (c >= bound) break;
-        W ^= __ldg(T + c);
+    while (i < e) {
+        int cv[kWChunk];
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) cv[q] = i + q < e ? __ldg(coords + i + q) : 0x7fffffff;
+        uint64_t tv[kWChunk];
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) tv[q] = cv[q] < bound ? __ldg(T + cv[q]) : 0ull;
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) W ^= tv[q];
+        nread += (unsigned)(e - i < kWChunk ? e - i : kWChunk);
+        if (cv[kWChunk - 1] >= bound) break;
+        i += kWChunk;
     }
     return W;
 }
@@ -499,7 +498,9 @@ __global__ void __launch_bounds__(kTile) blk_w_kernel(long long K, const int64_t
 // stores by lane 0, no shared atomics) and every thread combines the slots after
 // the barrier.  A caller must pass a barrier between reading one call's slots and
 // the next call that writes the same slots.
-constexpr int kWarps = kScanThreads / 32;
+constexpr int kPivotThreads = 512;        // threads of a pivot-kernel CTA
+constexpr int kWarps = kPivotThreads / 32;
+constexpr int kWinW = kWinTiles * kTile;  // W's in a CTA's window
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
     for (int d = 16; d > 0; d >>= 1) {
@@ -547,17 +548,19 @@ __device__ void basis_add(uint64_t (*tab)[256], uint64_t *basis, unsigned *piv, 
     cta_sync();
 }
 
-// First index (rank order) in the tile with rank >= s and a non-zero residual, or
-// kNoIndex.  `slots` holds kWarps words.
-__device__ unsigned tile_first_nonzero(const uint64_t *sW, const uint64_t (*tab)[256], long long r0, long long s,
-                                       unsigned *slots) {
+// First window position p in [from, valid) whose W has a non-zero residual against
+// tab, or kNoIndex.  Window positions are in rank order.  `slots` holds kWarps words.
+__device__ unsigned window_first_nonzero(const uint64_t *win, const uint64_t (*tab)[256], unsigned from,
+                                         unsigned valid, unsigned *slots) {
     unsigned best = kNoIndex;
-#pragma unroll
-    for (int q = 0; q < kPer; q++) {
-        const int li = q * kScanThreads + threadIdx.x;
-        const bool nz = (r0 + li) >= s && fr_reduce(sW[li], tab) != 0;
+    for (unsigned base = from & ~(unsigned)(kPivotThreads - 1); base < valid; base += kPivotThreads) {
+        const unsigned p = base + threadIdx.x;
+        const bool nz = p >= from && p < valid && fr_reduce(win[p], tab) != 0;
         const unsigned bal = __ballot_sync(0xffffffffu, nz);
-        if (bal && best == kNoIndex) best = (unsigned)(q * kScanThreads + (threadIdx.x & ~31) + __ffs(bal) - 1);
+        if (bal) {  // warp-uniform: this warp's first hit
+            best = base + (threadIdx.x & ~31u) + (unsigned)(__ffs(bal) - 1);
+            break;
+        }
     }
     if ((threadIdx.x & 31) == 0) slots[threadIdx.x >> 5] = best;
     cta_sync();
@@ -567,25 +570,32 @@ __device__ unsigned tile_first_nonzero(const uint64_t *sW, const uint64_t (*tab)
     return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) blk_pivot_kernel(
+// Index of the j-th set bit of a window mask.
+__device__ __forceinline__ int nth_bit(unsigned mask, unsigned j) {
+    for (unsigned q = 0; q < j; q++) mask &= mask - 1;
+    return __ffs(mask) - 1;
+}
+
+__global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
     long long K, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
     const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T, int bound, BlockState *bs,
     uint64_t *Warr, unsigned *tile_epoch, PivotReport *reports, GridBar *gb, unsigned *status,
     unsigned long long *bytes, unsigned long long *diag, unsigned long long *dbg) {
-    // dynamic shared memory: global tables | local tables | tile W's | merge buffers | report staging
-    extern __shared__ __align__(16) unsigned char dsm[];
+    // dynamic shared memory: global tables | local tables | window W's | merge buffers | report staging
+    extern __shared__ __align__(128) unsigned char dsm[];
     const unsigned G = gridDim.x;
     uint64_t(*gtab)[256] = reinterpret_cast<uint64_t(*)[256]>(dsm);
     uint64_t(*ltab)[256] = reinterpret_cast<uint64_t(*)[256]>(dsm + 16384);
-    uint64_t *sW = reinterpret_cast<uint64_t *>(dsm + 32768);
-    unsigned long long *mr = reinterpret_cast<unsigned long long *>(dsm + 32768 + 8 * kTile);  // 2 G kLmax
-    uint64_t *mw = reinterpret_cast<uint64_t *>(mr + 2 * (size_t)G * kLmax);                      // 3 G kLmax
+    uint64_t *win = reinterpret_cast<uint64_t *>(dsm + 32768);                                      // kWinW
+    unsigned long long *mr = reinterpret_cast<unsigned long long *>(dsm + 32768 + 8 * (size_t)kWinW);  // 2 G kLmax
+    uint64_t *mw = reinterpret_cast<uint64_t *>(mr + 2 * (size_t)G * kLmax);                          // 3 G kLmax
     unsigned long long *lr = mr + 5 * (size_t)G * kLmax;  // G (2 kLmax + 2)
     __shared__ uint64_t gbasis[64], lbasis[64];
     __shared__ unsigned gpiv[64], lpiv[64];
     __shared__ unsigned s_first[kWarps], s_wcnt[kWarps];
     __shared__ unsigned long long s_chg[kWarps], s_dmin[kWarps];
-    __shared__ unsigned s_tag;
+    __shared__ unsigned s_tag[kWinTiles];
+    __shared__ __align__(8) uint64_t s_bar;  // completion of the window's bulk copies
     __shared__ uint64_t s_newv[64];
     __shared__ unsigned s_newq[64];
     __shared__ int s_nnew;
@@ -601,8 +611,12 @@ __global__ void __launch_bounds__(kScanThreads) blk_pivot_kernel(
     const long long c = blockIdx.x;
     unsigned gen = ld_acquire_u32(&gb->gen);
     for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&gtab[0][0])[i] = 0;
-    long long cur = -1;  // tile whose W is in sW
-    long long maxt = 0;  // deepest tile this CTA touched
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        fence_mbar_init();
+    }
+    unsigned mphase = 0;  // uses of s_bar so far
+    long long maxt = 0;   // deepest tile this CTA touched
     long long s = 0;
     int grank = 0;
     bool ok = true;
@@ -622,73 +636,100 @@ __global__ void __launch_bounds__(kScanThreads) blk_pivot_kernel(
             lpiv[threadIdx.x] = gpiv[threadIdx.x];
         }
         int lrank = grank;
-        cta_sync();
+        // window: this CTA's tiles tf, tf + G, ... (t = c mod G) from the scan start on
         const long long t0 = s / kTile;
-        long long t = t0 + (((long long)c - t0 % G) + G) % G;
-        int nloc = 0;
-        long long end = K;
-        for (int m = 0; m < kWinTiles; m++, t += G) {
-            if (t >= ntiles) {
-                end = K;
+        const long long tf = t0 + (((long long)c - t0 % G) + G) % G;
+        const int nwin = tf >= ntiles ? 0 : (int)min((long long)kWinTiles, (ntiles - 1 - tf) / G + 1);
+        if (threadIdx.x < (unsigned)nwin) s_tag[threadIdx.x] = ld_acquire_u32(&tile_epoch[tf + (long long)threadIdx.x * G]);
+        cta_sync();
+        unsigned copymask = 0, zeromask = 0, missmask = 0;
+        for (int m = 0; m < nwin; m++) {
+            const unsigned tag = s_tag[m];
+            if ((tag >> 1) != epoch) missmask |= 1u << m;
+            else if (tag & 1u) zeromask |= 1u << m;
+            else copymask |= 1u << m;
+        }
+        maxt = nwin > 0 && tf + (long long)(nwin - 1) * G > maxt ? tf + (long long)(nwin - 1) * G : maxt;
+        // tiles the streaming pass computed: one bulk copy each into the window
+        if (copymask && threadIdx.x == 0) {
+            fence_proxy_async_smem();  // the previous step's reads of the window come first
+            mbar_arrive_expect_tx(&s_bar, (unsigned)__popc(copymask) * 8u * kTile);
+            for (unsigned mm = copymask; mm; mm &= mm - 1) {
+                const int m = __ffs(mm) - 1;
+                tma_load_1d(win + (size_t)m * kTile, Warr + (size_t)(tf + (long long)m * G) * kTile, 8u * kTile, &s_bar);
+            }
+            nb += 8ull * kTile * (unsigned)__popc(copymask);
+        }
+        for (unsigned mm = zeromask; mm; mm &= mm - 1) {
+            const int m = __ffs(mm) - 1;
+            for (int i = threadIdx.x; i < kTile; i += blockDim.x) win[(size_t)m * kTile + i] = 0;
+        }
+        n_loaded += (unsigned)__popc(copymask | zeromask);
+        if (missmask) {  // tiles beyond the streaming pass: W's computed here by the whole CTA
+            const unsigned nm = (unsigned)__popc(missmask);
+            unsigned nread = 0;
+            for (unsigned idx = threadIdx.x; idx < nm * kTile; idx += blockDim.x) {
+                const int m = nth_bit(missmask, idx / kTile);
+                const unsigned i = idx % kTile;
+                const long long t = tf + (long long)m * G;
+                const long long r = t * kTile + i;
+                uint64_t W = 0;
+                if (r < K && tile_minc[t] < bound) W = w_of_candidate(r, off, coords, T, bound, nread);
+                win[(size_t)m * kTile + i] = W;
+                Warr[r] = W;
+            }
+            fence_proxy_async_global();  // a later step may bulk-copy these tiles
+            nb += 4ull * nread + (threadIdx.x == 0 ? 16ull * kTile * nm : 0ull);
+            n_computed += nm;
+        }
+        if (copymask) {
+            bool done = mbar_wait_bounded(&s_bar, mphase & 1u, 1u << 22);
+            mphase++;
+            if (!cta_sync_and(done)) {
+                if (threadIdx.x == 0) {
+                    mbar_wait_bounded(&s_bar, (mphase - 1) & 1u, 1u << 22);  // copies still in flight
+                    atomicOr(status, ST_WAIT_TIMEOUT);
+                    atomicExch(&gb->abort, 1u);
+                }
+                ok = false;
                 break;
             }
-            const long long r0 = t * kTile;
-            maxt = t > maxt ? t : maxt;
-            if (t != cur) {
-                // one thread reads the tag and the CTA branches on the shared copy
-                if (threadIdx.x == 0) s_tag = ld_acquire_u32(&tile_epoch[t]);
-                cta_sync();
-                const unsigned tag = s_tag;
-                if ((tag >> 1) == epoch) {
-                    if (tag & 1u) {
-                        for (int i = threadIdx.x; i < kTile; i += blockDim.x) sW[i] = 0;
-                    } else {
-                        for (int i = threadIdx.x; i < kTile; i += blockDim.x)
-                            sW[i] = (r0 + i < K) ? __ldcg(Warr + r0 + i) : 0;
-                        if (threadIdx.x == 0) nb += 8ull * kTile;
-                    }
-                    n_loaded++;
-                    cta_sync();
-                } else {
-                    const bool zero = tile_minc[t] >= bound;
-                    unsigned nread = 0;
-                    for (int i = threadIdx.x; i < kTile; i += blockDim.x) {
-                        uint64_t W = 0;
-                        if (!zero && r0 + i < K) W = w_of_candidate(r0 + i, off, coords, T, bound, nread);
-                        sW[i] = W;
-                        Warr[r0 + i] = W;
-                    }
-                    cta_sync();
-                    if (threadIdx.x == 0) {
-                        __threadfence();
-                        tile_epoch[t] = epoch << 1;
-                    }
-                    nb += 4ull * nread + (threadIdx.x == 0 ? 16ull * kTile : 0ull);
-                    n_computed++;
-                }
-                cur = t;
+        }
+        cta_sync();
+        if (missmask && threadIdx.x == 0) {
+            __threadfence();
+            for (unsigned mm = missmask; mm; mm &= mm - 1)
+                tile_epoch[tf + (long long)(__ffs(mm) - 1) * G] = epoch << 1;
+        }
+        // local echelon over the window in rank order
+        const unsigned valid = (unsigned)nwin * kTile;
+        unsigned from = (nwin > 0 && tf == t0) ? (unsigned)(s - t0 * kTile) : 0u;
+        int nloc = 0;
+        long long end = K;
+        bool trunc = false;
+        for (;;) {
+            const unsigned p = window_first_nonzero(win, ltab, from, valid, s_first);
+            if (p >= valid) break;
+            const uint64_t w = win[p];
+            const uint64_t x = fr_reduce(w, ltab);
+            const long long rank = (tf + (long long)(p / kTile) * G) * kTile + (p % kTile);
+            if (threadIdx.x == 0) {
+                sr_rank[nloc] = (unsigned long long)rank;
+                sr_w[nloc] = w;
             }
-            bool trunc = false;
-            for (;;) {
-                const unsigned li = tile_first_nonzero(sW, ltab, r0, s, s_first);
-                if (li >= (unsigned)kTile) break;
-                const uint64_t w = sW[li];
-                const uint64_t x = fr_reduce(w, ltab);
-                if (threadIdx.x == 0) {
-                    sr_rank[nloc] = (unsigned long long)(r0 + li);
-                    sr_w[nloc] = w;
-                }
-                cta_sync();
-                basis_add(ltab, lbasis, lpiv, lrank, x, s_chg);
-                nloc++;
-                if (nloc == kLmax) {
-                    end = r0 + li + 1;
-                    trunc = true;
-                    break;
-                }
+            cta_sync();
+            basis_add(ltab, lbasis, lpiv, lrank, x, s_chg);
+            nloc++;
+            from = p + 1;
+            if (nloc == kLmax) {
+                end = rank + 1;
+                trunc = true;
+                break;
             }
-            if (trunc) break;
-            end = (r0 + kTile < K) ? r0 + kTile : K;
+        }
+        if (!trunc && nwin == kWinTiles) {  // a shorter window reached the last tile: end = K
+            const long long tl = tf + (long long)(kWinTiles - 1) * G;
+            end = (tl + 1) * kTile < K ? (tl + 1) * kTile : K;
         }
         n_local += nloc;
         if (threadIdx.x == 0) {
@@ -785,7 +826,9 @@ __global__ void __launch_bounds__(kScanThreads) blk_pivot_kernel(
         }
         cta_sync();
         // greedy echelon in rank order (warp 0): a candidate is a new global pivot iff
-        // its residual is not in the span of the new pivots before it
+        // its residual is not in the span of the new pivots before it; then the new
+        // vectors are brought to reduced form among themselves, latest first (lane l
+        // holds vectors l and l + 32)
         if (threadIdx.x < 32) {
             int nn = 0;
             for (unsigned base = 0; base < cnt && grank + nn < b; base += 32) {
@@ -811,18 +854,23 @@ __global__ void __launch_bounds__(kScanThreads) blk_pivot_kernel(
                 }
                 __syncwarp();
             }
+            uint64_t va = lane < (unsigned)nn ? s_newv[lane] : 0ull;
+            uint64_t vb = lane + 32 < (unsigned)nn ? s_newv[lane + 32] : 0ull;
+            for (int j = nn - 1; j >= 1; j--) {
+                const uint64_t vj = __shfl_sync(0xffffffffu, j < 32 ? va : vb, j & 31);
+                const unsigned qj = s_newq[j];
+                if ((int)lane < j && ((va >> qj) & 1ull)) va ^= vj;
+                if ((int)lane + 32 < j && ((vb >> qj) & 1ull)) vb ^= vj;
+            }
+            __syncwarp();
+            if (lane < (unsigned)nn) s_newv[lane] = va;
+            if (lane + 32 < (unsigned)nn) s_newv[lane + 32] = vb;
             if (lane == 0) s_nnew = nn;
         }
         cta_sync();
         const int nnew = s_nnew;
         if (nnew > 0) {
-            // bring the new vectors to reduced form among themselves (latest first),
-            // clear their pivot bits from the old basis vectors, append, rebuild tables
-            if (threadIdx.x == 0)
-                for (int j = nnew - 1; j >= 0; j--)
-                    for (int jj = j + 1; jj < nnew; jj++)
-                        if ((s_newv[j] >> s_newq[jj]) & 1ull) s_newv[j] ^= s_newv[jj];
-            cta_sync();
+            // clear the new pivot bits from the old basis vectors, append, rebuild tables
             if (threadIdx.x < (unsigned)grank) {
                 uint64_t v = gbasis[threadIdx.x];
                 for (int j = 0; j < nnew; j++)
@@ -877,10 +925,10 @@ __global__ void __launch_bounds__(kScanThreads) blk_pivot_kernel(
 }
 
 // Dynamic shared memory of blk_pivot_kernel for a grid of G CTAs: two sets of
-// Four-Russians tables, one tile of W's, the merge buffers (5 x G x kLmax words)
-// and the report staging (G x (2 kLmax + 2) words).
+// Four-Russians tables, the window of kWinTiles tiles of W's, the merge buffers
+// (5 x G x kLmax words) and the report staging (G x (2 kLmax + 2) words).
 size_t pivot_smem_bytes(int G) {
-    return 32768 + 8 * (size_t)kTile + 8 * 5 * (size_t)G * kLmax + 8 * (size_t)G * (2 * kLmax + 2);
+    return 32768 + 8 * (size_t)kWinW + 8 * 5 * (size_t)G * kLmax + 8 * (size_t)G * (2 * kLmax + 2);
 }
 
 // Resolve the block's b iterations on masks.  Pivot index = rank order.
@@ -1296,7 +1344,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
         e = cudaFuncSetAttribute(blk_pivot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = 0;
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blk_pivot_kernel, kScanThreads, smem);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blk_pivot_kernel, kPivotThreads, smem);
         if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
         s->pivot_grid = G;
         // two step-parity halves of: ranks + W's (G x kLmax each), ends, counts (G each)
@@ -1531,7 +1579,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             unsigned long long *dg = s->d_diag;
             unsigned long long *db = s->d_diag + 32;
             void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db};
-            MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kScanThreads),
+            MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kPivotThreads),
                                                  args, pivot_smem_bytes(s->pivot_grid), st));
         }
         {
