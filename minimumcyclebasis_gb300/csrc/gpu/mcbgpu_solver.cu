@@ -41,9 +41,24 @@ constexpr int kTile = 1024;           // candidates per tile
 constexpr int kScanThreads = 256;     // 4 candidates per thread
 constexpr int kPer = kTile / kScanThreads;
 constexpr unsigned kSpinLimit = 1u << 24;
-constexpr int kLmax = 8;       // local pivots a CTA reports per pivot step
-constexpr int kWinTiles = 8;   // tiles a CTA scans per pivot step
-constexpr int kUpdRows = 8;    // rows per warp group in the block update
+// Shape parameters of the blocked search; each can be overridden at build time
+// (-DMCB_LMAX=... and so on) to sweep them.
+#ifndef MCB_LMAX
+#define MCB_LMAX 6
+#endif
+#ifndef MCB_WIN_TILES
+#define MCB_WIN_TILES 6
+#endif
+#ifndef MCB_UPD_ROWS
+#define MCB_UPD_ROWS 8
+#endif
+#ifndef MCB_W_CHUNK
+#define MCB_W_CHUNK 8
+#endif
+
+constexpr int kLmax = MCB_LMAX;           // local pivots a CTA reports per pivot step
+constexpr int kWinTiles = MCB_WIN_TILES;  // tiles a CTA scans per pivot step (<= 32)
+constexpr int kUpdRows = MCB_UPD_ROWS;    // rows per warp group in the block update (<= 32)
 constexpr unsigned long long kNone = 0xFFFFFFFFFFFFFFFFull;
 constexpr unsigned kNoIndex = 0xFFFFFFFFu;
 
@@ -68,8 +83,6 @@ struct BlockState {
     long long pred_tiles;          // tiles the streaming pass computes for this block
     long long max_tile;            // deepest tile the previous block's pivot search touched
     unsigned long long total;      // running 64-bit total weight of the basis
-    unsigned long long basis[64];  // reduced row-echelon basis of the pivot W's
-    unsigned pivbit[64];
     long long pivrank[64];
     unsigned long long pivW[64];   // the pivots' W as found (not reduced)
     unsigned long long mask[64];   // final S_{e0+k} as a combination of S^0_{e0+l}
@@ -416,7 +429,7 @@ __device__ bool grid_barrier(GridBar *gb, unsigned nctas, unsigned &gen_local) {
 // coordinates.  The list is ascending: a chunk whose last coordinate is >= bound
 // ends the walk, and its coordinates >= bound gather nothing.  `nread` counts the
 // coordinates read.
-constexpr int kWChunk = 8;
+constexpr int kWChunk = MCB_W_CHUNK;
 
 __device__ __forceinline__ uint64_t w_of_candidate(long long r, const int64_t *__restrict__ off,
                                                    const int32_t *__restrict__ coords,
@@ -940,7 +953,9 @@ size_t pivot_smem_bytes(int G) {
 __global__ void __launch_bounds__(256) blk_resolve_kernel(BlockState *bs, int e0, const int64_t *__restrict__ off,
                                                           const int32_t *__restrict__ coords,
                                                           const int32_t *__restrict__ weight, long long *selected,
-                                                          unsigned *pairs, unsigned pair_cap, unsigned *status) {
+                                                          unsigned *pairs, unsigned pair_cap, unsigned *sorted,
+                                                          unsigned *word_end, int P, unsigned *status) {
+    extern __shared__ unsigned hist[];  // P + 1 counters
     __shared__ uint64_t s_w[64];
     __shared__ long long s_r[64];
     __shared__ int s_sel[64];
@@ -1041,6 +1056,41 @@ __global__ void __launch_bounds__(256) blk_resolve_kernel(BlockState *bs, int e0
         }
         pairs[i] = ((unsigned)coords[s_beg[lo] + (i - s_pre[lo])] << 6) | (unsigned)lo;
     }
+    // counting sort of the pairs by S word (coordinate >> 6): consecutive pairs then
+    // read neighbouring words of a row, and word_end[w] = number of pairs whose word
+    // is below w bounds the pairs that can meet the support [0, j] of a row S_j
+    const unsigned nw = (unsigned)P + 1;
+    for (unsigned w = tid; w < nw; w += blockDim.x) hist[w] = 0;
+    cta_sync();
+    for (unsigned i = tid; i < total; i += blockDim.x) atomicAdd(&hist[pairs[i] >> 12], 1u);
+    cta_sync();
+    {
+        __shared__ unsigned s_part[8];
+        const unsigned per = (nw + blockDim.x - 1) / blockDim.x;
+        const unsigned a = tid * per < nw ? tid * per : nw, z = a + per < nw ? a + per : nw;
+        unsigned sum = 0;
+        for (unsigned w = a; w < z; w++) sum += hist[w];
+        unsigned incl = sum;
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += t;
+        }
+        if (lane == 31) s_part[tid >> 5] = incl;
+        cta_sync();
+        unsigned run = incl - sum;
+        for (int x = 0; x < (int)(tid >> 5); x++) run += s_part[x];
+        for (unsigned w = a; w < z; w++) {
+            const unsigned h = hist[w];
+            hist[w] = run;
+            word_end[w] = run;
+            run += h;
+        }
+    }
+    cta_sync();
+    for (unsigned i = tid; i < total; i += blockDim.x) {
+        const unsigned pr = pairs[i];
+        sorted[atomicAdd(&hist[pr >> 12], 1u)] = pr;
+    }
 }
 
 // S_{e0+k} := XOR of S^0_{e0+l} over l in mask[k], in place, words [0, Wb).
@@ -1091,18 +1141,20 @@ __global__ void blk_tables_kernel(const uint64_t *__restrict__ S, int P, int e0,
     }
 }
 
-// Rows j >= e0+b, kUpdRows rows per warp.  D_j (64 bits) = <C_sel_k, S_j> (lanes split the
-// chosen cycles' (coordinate, k) pairs, one row at a time); then lane i computes,
-// for row i of the group, beta_k = D_k ^ <beta_{<k}, gcol_k> (the sequential effect
-// of the block's 64 updates); then S_j ^= XOR_k beta_k S_{e0+k} through the tables,
-// lanes split the row's words.
+// Rows j >= e0+b, kUpdRows consecutive rows per warp.  D_j (64 bits) = <C_sel_k, S_j>:
+// lanes split the chosen cycles' (coordinate, k) pairs, sorted by S word, and each
+// pair is applied to all rows of the group (independent gathers of neighbouring
+// words); pairs whose word lies above the group's last row are skipped (S_j has
+// support [0, j]).  Then lane i computes, for row i of the group, beta_k = D_k ^
+// <beta_{<k}, gcol_k> (the sequential effect of the block's 64 updates); then
+// S_j ^= XOR_k beta_k S_{e0+k} through the tables, lanes split the row's words.
 __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int Pt,
                                   const uint64_t *__restrict__ tab, const BlockState *bs,
-                                  const unsigned *__restrict__ pairs, unsigned long long *bytes) {
+                                  const unsigned *__restrict__ pairs, const unsigned *__restrict__ word_end,
+                                  unsigned long long *bytes) {
     unsigned long long nb = 0;
     __shared__ uint64_t sg[64];
     const int b = (int)bs->b;
-    const unsigned np = bs->npairs;
     if (threadIdx.x < 64) sg[threadIdx.x] = threadIdx.x < b ? bs->gcol[threadIdx.x] : 0;
     cta_sync();
     const int lane = threadIdx.x & 31;
@@ -1111,27 +1163,34 @@ __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int
     for (long long g0 = first + kUpdRows * (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); g0 < N;
          g0 += kUpdRows * warps) {
         const int rows = (int)((N - g0) < kUpdRows ? (N - g0) : kUpdRows);
+        const long long jl = g0 + rows - 1;
+        const int wl = (int)(jl >> 6) + 1 < P ? (int)(jl >> 6) + 1 : P;
+        const unsigned np = __ldg(word_end + wl);
+        const uint64_t *Sg = S + (size_t)g0 * P;
+        uint64_t D[kUpdRows];
+#pragma unroll
+        for (int r = 0; r < kUpdRows; r++) D[r] = 0;
+        for (unsigned i = lane; i < np; i += 32) {
+            const unsigned pr = __ldg(pairs + i);
+            const unsigned c = pr >> 6, k = pr & 63u, w = c >> 6, sh = c & 63u;
+#pragma unroll
+            for (int r = 0; r < kUpdRows; r++)
+                if (r < rows) D[r] ^= ((Sg[(size_t)r * P + w] >> sh) & 1ull) << k;
+        }
         uint64_t Dmine = 0;
-        for (int r = 0; r < rows; r++) {
-            const uint64_t *Sj = S + (size_t)(g0 + r) * P;
-            uint64_t D = 0;
-#pragma unroll 4
-            for (unsigned i = lane; i < np; i += 32) {
-                const unsigned pr = __ldg(pairs + i);
-                const unsigned c = pr >> 6, k = pr & 63u;
-                D ^= ((Sj[c >> 6] >> (c & 63)) & 1ull) << k;
-            }
-            for (int d = 16; d > 0; d >>= 1) D ^= __shfl_xor_sync(0xffffffffu, D, d);
-            if (lane == r) Dmine = D;
+#pragma unroll
+        for (int r = 0; r < kUpdRows; r++) {
+            uint64_t d = D[r];
+            for (int o = 16; o > 0; o >>= 1) d ^= __shfl_xor_sync(0xffffffffu, d, o);
+            if (lane == r) Dmine = d;
         }
         uint64_t beta = 0;
         if (lane < rows) {
             for (int k = 0; k < b; k++) beta |= ((((Dmine >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]))) << k;
-            // algorithmic bytes: the words of S_j the pairs touch (its support is [0, j])
-            // plus, when it changes, read + write of its first Wb words
-            const long long j = g0 + lane;
-            const unsigned wj = (unsigned)(j >> 6) + 1;
-            nb += 8ull * (np < wj ? np : wj) + (beta ? 16ull * (unsigned long long)Wb : 0ull);
+            // algorithmic bytes: the S words the group's pairs touch (8 rows share each
+            // pair, counted once per row) plus, when the row changes, read + write of
+            // its first Wb words
+            nb += 8ull * np + (beta ? 16ull * (unsigned long long)Wb : 0ull);
         }
         for (int r = 0; r < rows; r++) {
             const uint64_t bt = __shfl_sync(0xffffffffu, beta, r);
@@ -1175,8 +1234,9 @@ struct mcbgpu_solver {
     PivotReport *d_reports = nullptr;      // 2 x pivot_grid
     GridBar *d_gbar = nullptr;
     int pivot_grid = 0;
-    unsigned *d_pairs = nullptr;
+    unsigned *d_pairs = nullptr;     // 2 x pair_cap
     unsigned pair_cap = 0;
+    unsigned *d_word_end = nullptr;  // P + 1: sorted pairs with S word < w
     IterSlot *d_slots = nullptr;   // 2
     BlockState *d_bs = nullptr;
     long long *d_selected = nullptr;
@@ -1253,6 +1313,7 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_reports);
     cudaFree(s->d_gbar);
     cudaFree(s->d_pairs);
+    cudaFree(s->d_word_end);
     cudaFree(s->d_slots);
     cudaFree(s->d_bs);
     cudaFree(s->d_selected);
@@ -1325,6 +1386,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_tile_minc, sizeof(int32_t) * ntiles);
     ALLOC(s->d_gmin, sizeof(unsigned long long) * 4);
     ALLOC(s->d_gbar, sizeof(GridBar));
+    ALLOC(s->d_word_end, sizeof(unsigned) * ((size_t)s->P + 1));
     ALLOC(s->d_slots, sizeof(IterSlot) * 2);
     ALLOC(s->d_bs, sizeof(BlockState));
     ALLOC(s->d_selected, sizeof(long long) * (size_t)(N > 0 ? N : 1));
@@ -1337,11 +1399,15 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     if (e == cudaSuccess) e = cudaMemset(s->d_bytes, 0, sizeof(unsigned long long) * KC_COUNT);
     if (e == cudaSuccess) e = cudaMemset(s->d_tile_epoch, 0, sizeof(unsigned) * ntiles);
     if (e == cudaSuccess) e = cudaMemset(s->d_gbar, 0, sizeof(GridBar));
+    if (e == cudaSuccess) e = cudaMemset(s->d_word_end, 0, sizeof(unsigned) * ((size_t)s->P + 1));
     if (e == cudaSuccess) e = cudaMemset(s->d_coords, 0, sizeof(int32_t) * (size_t)(nnz + 4));
     if (e == cudaSuccess) {
         const int G = s->sm_count > 0 ? s->sm_count : 1;  // one CTA per SM
         const size_t smem = pivot_smem_bytes(G);
         e = cudaFuncSetAttribute(blk_pivot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const size_t rsmem = sizeof(unsigned) * ((size_t)s->P + 1);
+        if (e == cudaSuccess && rsmem > 48 * 1024)
+            e = cudaFuncSetAttribute(blk_resolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
         int per_sm = 0;
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blk_pivot_kernel, kPivotThreads, smem);
@@ -1418,11 +1484,11 @@ int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t 
     }
     s->max_len = (int)chk[1];
     unsigned cap = (unsigned)(64 * (size_t)(s->max_len > 0 ? s->max_len : 1));
-    if (cap > s->pair_cap) {
+    if (cap > s->pair_cap) {  // two halves: pairs in cycle order, pairs sorted by S word
         cudaFree(s->d_pairs);
         s->d_pairs = nullptr;
-        MCB_CUDA(cudaMalloc((void **)&s->d_pairs, sizeof(unsigned) * cap));
-        s->device_bytes += (long long)sizeof(unsigned) * cap;
+        MCB_CUDA(cudaMalloc((void **)&s->d_pairs, sizeof(unsigned) * 2 * (size_t)cap));
+        s->device_bytes += (long long)sizeof(unsigned) * 2 * cap;
         s->pair_cap = cap;
     }
     const long long ntiles = (s->K + kTile - 1) / kTile;
@@ -1560,7 +1626,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         if (ntiles > 0) {
             Launch L(s, KC_WSTREAM, st);
             blk_w_kernel<<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
-                                                          s->d_bs, s->d_Warr, s->d_tile_epoch, L.bytes());
+                                                    s->d_bs, s->d_Warr, s->d_tile_epoch, L.bytes());
         }
         {
             Launch L(s, KC_PIVOT, st);
@@ -1584,8 +1650,9 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         }
         {
             Launch L(s, KC_RESOLVE, st);
-            blk_resolve_kernel<<<1, 256, 0, st>>>(s->d_bs, (int)e0, s->d_off, s->d_coords, s->d_weight, s->d_selected,
-                                                  s->d_pairs, s->pair_cap, s->d_status);
+            blk_resolve_kernel<<<1, 256, sizeof(unsigned) * ((size_t)s->P + 1), st>>>(
+                s->d_bs, (int)e0, s->d_off, s->d_coords, s->d_weight, s->d_selected, s->d_pairs, s->pair_cap,
+                s->d_pairs + s->pair_cap, s->d_word_end, s->P, s->d_status);
         }
         {
             Launch L(s, KC_MATERIALIZE, st);
@@ -1603,7 +1670,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             if (grid > sms * 8) grid = sms * 8;
             if (grid < 1) grid = 1;
             blk_update_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P, (int)e0, Wb, s->P, s->d_tab, s->d_bs,
-                                                    s->d_pairs, L.bytes());
+                                                    s->d_pairs + s->pair_cap, s->d_word_end, L.bytes());
         }
         MCB_CUDA(cudaGetLastError());
     }
