@@ -111,6 +111,23 @@ int64_t mcbh_gen_random(int32_t n, int64_t m, int32_t wlo, int32_t whi, uint64_t
  * symmetrised, weight round(1000*length) (>= 1), plus the shortest bridging edges
  * needed to connect the components (in order of component discovery). */
 int64_t mcbh_gen_rgg(int32_t n, int32_t k, uint64_t seed, int32_t *u, int32_t *v, int32_t *w);
+/* planar-like graph with degree-two chains: a triangulated grid of about `points`
+ * vertices (right and down edges, one diagonal per cell in a random direction),
+ * delete_pct% of its edges deleted while a random spanning tree is kept (the graph
+ * stays connected), then every kept edge subdivided with probability chain_pct% into
+ * a chain of 1..chain_max extra vertices; weights uniform in [wlo, whi] per final
+ * edge.  Returns the edge count; *nodes gets the vertex count.  Call with u = NULL
+ * first to size the arrays. */
+int64_t mcbh_gen_planar_chains(int32_t points, int32_t delete_pct, int32_t chain_pct, int32_t chain_max,
+                               int32_t wlo, int32_t whi, uint64_t seed, int32_t *u, int32_t *v, int32_t *w,
+                               int32_t *nodes);
+/* tree of blocks: `blocks` 2-connected random blocks (a Hamiltonian cycle plus
+ * uniform extra edges; size log-uniform in [nmin, nmax], average degree uniform in
+ * [deg_lo_x10, deg_hi_x10] / 10), block i > 0 sharing one random earlier vertex (an
+ * articulation point).  Returns the edge count; *nodes gets the vertex count. */
+int64_t mcbh_gen_block_tree(int32_t blocks, int32_t nmin, int32_t nmax, int32_t deg_lo_x10, int32_t deg_hi_x10,
+                            int32_t wlo, int32_t whi, uint64_t seed, int32_t *u, int32_t *v, int32_t *w,
+                            int32_t *nodes);
 int mcbh_write_mtx(const char *path, int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
                    const int32_t *w);
 

@@ -1122,6 +1122,150 @@ int64_t mcbh_gen_rgg(int32_t n, int32_t kk, uint64_t seed, int32_t *u, int32_t *
     return m;
 }
 
+}  // extern "C"
+
+namespace {
+
+struct EdgeList {
+    std::vector<int32_t> u, v, w;
+    int32_t nodes = 0;
+    void add(int32_t a, int32_t b, int32_t wt) {
+        u.push_back(a);
+        v.push_back(b);
+        w.push_back(wt);
+    }
+};
+
+int64_t emit(const EdgeList &g, int32_t *u, int32_t *v, int32_t *w, int32_t *nodes) {
+    if (nodes) *nodes = g.nodes;
+    const int64_t m = (int64_t)g.u.size();
+    if (!u) return m;
+    std::memcpy(u, g.u.data(), sizeof(int32_t) * (size_t)m);
+    std::memcpy(v, g.v.data(), sizeof(int32_t) * (size_t)m);
+    std::memcpy(w, g.w.data(), sizeof(int32_t) * (size_t)m);
+    return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t mcbh_gen_planar_chains(int32_t points, int32_t delete_pct, int32_t chain_pct, int32_t chain_max, int32_t wlo,
+                               int32_t whi, uint64_t seed, int32_t *u, int32_t *v, int32_t *w, int32_t *nodes) {
+    if (points < 4 || delete_pct < 0 || delete_pct >= 100 || chain_pct < 0 || chain_pct > 100 || chain_max < 1 ||
+        whi < wlo)
+        return MCBH_E_ARG;
+    Rng g{seed};
+    // triangulated grid: r x c points, right and down edges, one diagonal per cell
+    // in a random direction (a planar triangulation of a jittered grid)
+    const int32_t r = std::max(2, (int32_t)std::lround(std::sqrt((double)points)));
+    const int32_t c = std::max(2, (points + r - 1) / r);
+    std::vector<std::pair<int32_t, int32_t>> base;
+    base.reserve((size_t)3 * r * c);
+    for (int32_t i = 0; i < r; i++)
+        for (int32_t j = 0; j < c; j++) {
+            const int32_t id = i * c + j;
+            if (j + 1 < c) base.push_back({id, id + 1});
+            if (i + 1 < r) base.push_back({id, id + c});
+            if (i + 1 < r && j + 1 < c) {
+                if (g.next() & 1)
+                    base.push_back({id, id + c + 1});
+                else
+                    base.push_back({id + 1, id + c});
+            }
+        }
+    const int32_t n0 = r * c;
+    // delete delete_pct% of the edges, keeping a random spanning tree
+    const size_t E = base.size();
+    std::vector<size_t> order(E);
+    for (size_t i = 0; i < E; i++) order[i] = i;
+    for (size_t i = E - 1; i > 0; i--) std::swap(order[i], order[g.below((uint64_t)i + 1)]);
+    std::vector<char> keep(E, 0);
+    DSU d(n0);
+    size_t kept = 0;
+    for (size_t t = 0; t < E; t++) {
+        const auto &e = base[order[t]];
+        const int a = d.find(e.first), b = d.find(e.second);
+        if (a != b) {
+            d.p[a] = b;
+            keep[order[t]] = 1;
+            kept++;
+        }
+    }
+    const size_t target = (size_t)std::llround((double)E * (100 - delete_pct) / 100.0);
+    for (size_t t = 0; t < E && kept < target; t++)
+        if (!keep[order[t]]) {
+            keep[order[t]] = 1;
+            kept++;
+        }
+    // subdivide each kept edge with probability chain_pct% into a chain of
+    // 1..chain_max extra vertices; every final edge gets its own weight
+    EdgeList out;
+    out.nodes = n0;
+    for (size_t i = 0; i < E; i++) {
+        if (!keep[i]) continue;
+        int32_t a = base[i].first;
+        const int32_t b = base[i].second;
+        if ((int32_t)g.below(100) < chain_pct) {
+            const int32_t L = 1 + (int32_t)g.below((uint64_t)chain_max);
+            for (int32_t q = 0; q < L; q++) {
+                const int32_t x = out.nodes++;
+                out.add(a, x, wlo + (int32_t)g.below((uint64_t)(whi - wlo + 1)));
+                a = x;
+            }
+        }
+        out.add(a, b, wlo + (int32_t)g.below((uint64_t)(whi - wlo + 1)));
+    }
+    return emit(out, u, v, w, nodes);
+}
+
+int64_t mcbh_gen_block_tree(int32_t blocks, int32_t nmin, int32_t nmax, int32_t deg_lo_x10, int32_t deg_hi_x10,
+                            int32_t wlo, int32_t whi, uint64_t seed, int32_t *u, int32_t *v, int32_t *w,
+                            int32_t *nodes) {
+    if (blocks < 1 || nmin < 3 || nmax < nmin || deg_lo_x10 < 20 || deg_hi_x10 < deg_lo_x10 || whi < wlo)
+        return MCBH_E_ARG;
+    Rng g{seed};
+    EdgeList out;
+    std::vector<int32_t> gid;
+    std::unordered_set<uint64_t> seen;
+    auto key = [](int32_t a, int32_t b) {
+        return ((uint64_t)(uint32_t)std::min(a, b) << 32) | (uint32_t)std::max(a, b);
+    };
+    for (int32_t bi = 0; bi < blocks; bi++) {
+        // block size log-uniform in [nmin, nmax], average degree uniform in [lo, hi]
+        const double ln = std::log((double)nmin) + g.unit() * (std::log((double)nmax) - std::log((double)nmin));
+        const int32_t n = std::min(nmax, std::max(nmin, (int32_t)std::lround(std::exp(ln))));
+        const double deg = (deg_lo_x10 + g.unit() * (deg_hi_x10 - deg_lo_x10)) / 10.0;
+        int64_t m = std::max<int64_t>(n, std::llround(n * deg / 2.0));
+        m = std::min<int64_t>(m, (int64_t)n * (n - 1) / 2);
+        // global ids: local vertex 0 is an existing vertex (the articulation point),
+        // the others are new
+        gid.assign((size_t)n, 0);
+        if (bi == 0) {
+            for (int32_t q = 0; q < n; q++) gid[q] = out.nodes++;
+        } else {
+            gid[0] = (int32_t)g.below((uint64_t)out.nodes);
+            for (int32_t q = 1; q < n; q++) gid[q] = out.nodes++;
+        }
+        // a cycle through a random order of the vertices (the block is 2-connected:
+        // no cut vertex inside it), then uniform extra edges up to m
+        std::vector<int32_t> perm(n);
+        for (int32_t q = 0; q < n; q++) perm[q] = q;
+        for (int32_t q = n - 1; q > 0; q--) std::swap(perm[q], perm[g.below((uint64_t)q + 1)]);
+        seen.clear();
+        int64_t k = 0;
+        auto add = [&](int32_t a, int32_t b) {
+            if (a == b || !seen.insert(key(a, b)).second) return false;
+            out.add(gid[a], gid[b], wlo + (int32_t)g.below((uint64_t)(whi - wlo + 1)));
+            k++;
+            return true;
+        };
+        for (int32_t q = 0; q < n; q++) add(perm[q], perm[(q + 1) % n]);
+        while (k < m) add((int32_t)g.below((uint64_t)n), (int32_t)g.below((uint64_t)n));
+    }
+    return emit(out, u, v, w, nodes);
+}
+
 int mcbh_write_mtx(const char *path, int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
                    const int32_t *w) {
     if (!path || nodes <= 0 || m < 0) return MCBH_E_ARG;

@@ -70,6 +70,68 @@ def rgg_graph(n: int, k: int = 4, seed: int = 1) -> Graph:
     return Graph(n, u, v, w)
 
 
+def planar_chain_graph(points: int, delete_pct: int = 30, chain_pct: int = 30, chain_max: int = 8,
+                       wlo: int = 1, whi: int = 1000, seed: int = 1) -> Graph:
+    """Triangulated grid of about `points` vertices, delete_pct% of the edges deleted
+    (connectivity kept), each kept edge subdivided with probability chain_pct% into a
+    chain of 1..chain_max vertices; weights U[wlo, whi] per final edge."""
+    lib = host_lib()
+    nodes = C.c_int32()
+    mm = lib.mcbh_gen_planar_chains(points, delete_pct, chain_pct, chain_max, wlo, whi, seed, None, None, None,
+                                    C.byref(nodes))
+    if mm < 0:
+        raise ValueError("bad planar-chain parameters")
+    u, v, w = _edges(mm)
+    lib.mcbh_gen_planar_chains(points, delete_pct, chain_pct, chain_max, wlo, whi, seed, ptr(u), ptr(v), ptr(w),
+                               C.byref(nodes))
+    return Graph(int(nodes.value), u, v, w)
+
+
+def block_tree_graph(blocks: int, nmin: int = 50, nmax: int = 150, deg_lo: float = 2.5, deg_hi: float = 5.0,
+                     wlo: int = 1, whi: int = 255, seed: int = 1) -> Graph:
+    """`blocks` 2-connected random blocks (size log-uniform in [nmin, nmax], average
+    degree U[deg_lo, deg_hi]) glued at articulation vertices into a tree of blocks."""
+    lib = host_lib()
+    nodes = C.c_int32()
+    lo, hi = int(round(deg_lo * 10)), int(round(deg_hi * 10))
+    mm = lib.mcbh_gen_block_tree(blocks, nmin, nmax, lo, hi, wlo, whi, seed, None, None, None, C.byref(nodes))
+    if mm < 0:
+        raise ValueError("bad block-tree parameters")
+    u, v, w = _edges(mm)
+    lib.mcbh_gen_block_tree(blocks, nmin, nmax, lo, hi, wlo, whi, seed, ptr(u), ptr(v), ptr(w), C.byref(nodes))
+    return Graph(int(nodes.value), u, v, w)
+
+
+def _splitmix64(state: int) -> tuple[int, int]:
+    state = (state + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    z = state
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return state, z ^ (z >> 31)
+
+
+def batch_graphs(count: int, nmin: int = 50, nmax: int = 5000, deg_lo: float = 2.5, deg_hi: float = 5.0,
+                 wlo: int = 1, whi: int = 255, seed: int = 1) -> list[Graph]:
+    """`count` independent connected random graphs: n log-uniform in [nmin, nmax],
+    average degree U[deg_lo, deg_hi], weights U[wlo, whi]; graph i is drawn from its
+    own seed, derived from `seed` by splitmix64."""
+    import math
+    out = []
+    st = seed & 0xFFFFFFFFFFFFFFFF
+    for _ in range(count):
+        st, a = _splitmix64(st)
+        st, b = _splitmix64(st)
+        st, gseed = _splitmix64(st)
+        ua, ub = (a >> 11) / float(1 << 53), (b >> 11) / float(1 << 53)
+        n = int(round(math.exp(math.log(nmin) + ua * (math.log(nmax) - math.log(nmin)))))
+        n = max(nmin, min(nmax, n))
+        deg = deg_lo + ub * (deg_hi - deg_lo)
+        m = max(n - 1, int(round(n * deg / 2)))
+        m = min(m, n * (n - 1) // 2)
+        out.append(random_graph(n, m, wlo, whi, gseed))
+    return out
+
+
 class Problem:
     """A graph prepared for the de Pina main loop.
 

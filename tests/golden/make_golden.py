@@ -29,7 +29,8 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-from minimumcyclebasis_gb300 import grid_graph, random_graph, rgg_graph  # noqa: E402
+from minimumcyclebasis_gb300 import (batch_graphs, block_tree_graph, grid_graph, planar_chain_graph,  # noqa: E402
+                                     random_graph, rgg_graph)
 from minimumcyclebasis_gb300.build import build_all, build_reference  # noqa: E402
 
 # (name, generator, args, keep full candidate list in the fixture)
@@ -46,11 +47,25 @@ CASES = [
     ("rand1000_s5", "random", (1000, 2500, 1, 1000, 5), False),
     ("tree_plus_one_s4", "random", (64, 64, 1, 50, 4), True),
     ("rgg500_s3", "rgg", (500, 4, 3), True),
+    # the planar-with-chains family (triangulated grid, 30% of edges deleted,
+    # 30% of edges subdivided into chains of 1..8 vertices)
+    ("planar300_s5", "planar", (300, 30, 30, 8, 1, 1000, 5), True),
+    ("planar2000_s2", "planar", (2000, 30, 30, 8, 1, 1000, 2), False),
+    # a tree of 2-connected random blocks glued at articulation vertices
+    ("blocktree12_s2", "blocktree", (12, 20, 60, 2.5, 5.0, 1, 255, 2), True),
+    # members of a batch of independent graphs (n log-uniform, degree U[2.5, 5])
+    ("batch7_g0", "batch", (4, 50, 600, 2.5, 5.0, 1, 255, 7, 0), True),
+    ("batch7_g1", "batch", (4, 50, 600, 2.5, 5.0, 1, 255, 7, 1), True),
+    ("batch7_g2", "batch", (4, 50, 600, 2.5, 5.0, 1, 255, 7, 2), True),
+    ("batch7_g3", "batch", (4, 50, 600, 2.5, 5.0, 1, 255, 7, 3), True),
 ]
 
 
 def gen(kind, args):
-    return {"grid": grid_graph, "random": random_graph, "rgg": rgg_graph}[kind](*args)
+    if kind == "batch":
+        return batch_graphs(*args[:-1])[args[-1]]
+    return {"grid": grid_graph, "random": random_graph, "rgg": rgg_graph, "planar": planar_chain_graph,
+            "blocktree": block_tree_graph}[kind](*args)
 
 
 def parse_dump(text):
