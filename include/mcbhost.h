@@ -84,6 +84,11 @@ int mcbh_get_info(const mcbh_problem *p, mcbh_info *info);
 int mcbh_get_reduced_graph(const mcbh_problem *p, uint32_t *rows, uint32_t *cols, int32_t *weights,
                            uint32_t *reverse_edge, uint32_t *row_offsets);
 int mcbh_get_fvs(const mcbh_problem *p, int32_t *fvs_array /* n' */, uint32_t *fvs_vertices /* F */);
+/* input_vertex[v] = the input vertex (0-based) of reduced vertex v (n'); chain
+ * contraction keeps every vertex of degree > 2 and relabels it in order of first
+ * appearance (include/CsrGraphMulti.h:229-300).  No reference counterpart: the
+ * reference prints reduced ids only. */
+int mcbh_get_vertex_map(const mcbh_problem *p, int32_t *input_vertex);
 /* coord_edges[c] = edge offset of coordinate c (N); edge_coord[o] = coordinate of offset o or -1 (2m') */
 int mcbh_get_coords(const mcbh_problem *p, uint32_t *coord_edges, int32_t *edge_coord);
 /* candidates in rank order (K each); tree = FVS index of the root */

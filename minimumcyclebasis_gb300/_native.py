@@ -44,6 +44,7 @@ HOST_SYMBOLS = {
     "mcbh_get_info": (C.c_int, [vp, C.POINTER(MCBHInfo)]),
     "mcbh_get_reduced_graph": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "mcbh_get_fvs": (C.c_int, [vp, vp, vp]),
+    "mcbh_get_vertex_map": (i32, [vp, vp]),
     "mcbh_get_coords": (C.c_int, [vp, vp, vp]),
     "mcbh_get_candidates": (C.c_int, [vp, vp, vp, vp, vp]),
     "mcbh_get_cycle_lists": (C.c_int, [vp, vp, vp]),

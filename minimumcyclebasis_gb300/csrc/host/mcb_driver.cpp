@@ -1,0 +1,215 @@
+// mcb_gb300 — the minimum-cycle-basis driver on this library, a drop-in for the
+// reference's GPU driver binary (mcb/mcb_cycle_deg_two_remove.cpp, built as
+// mcb_cuda).
+//
+//   mcb_gb300 <input.mtx> <stats.csv> <threads> [chunk_size] [options]
+//
+// Same positional arguments as the reference (chunk_size is accepted and ignored:
+// every tree stays resident in HBM).  Like the reference it appends one row of
+// statistics to stats.csv, writing the header first when the file is new, in the
+// column order of the reference's GPU timings row (include/stats.h:256-338).
+// Differences: the CSV has no padding whitespace, and Total_Weight is the exact
+// 64-bit sum (the reference accumulates it in an int).
+//
+// Options:
+//   --cycles FILE        the basis in selection order, one block per cycle in the
+//                        format of cycle::print (include/cycles.h:197-207), reduced
+//                        vertex ids + 1 as the reference prints them, then
+//                        "Total Weight = W" (mcb/Test_deg_two_remove.cpp:334-341)
+//   --cycles-input FILE  the same with the input graph's vertex ids + 1
+//   --plain              the per-iteration de Pina loop instead of the blocked one
+//
+// Exit status 0 on success; on any error a message on stderr and status 1 (the
+// reference prints and exits on every error too).
+#include <cuda_runtime.h>
+#include <unistd.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mcbgpu.h"
+#include "mcbhost.h"
+
+namespace {
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+[[noreturn]] void fail(const char *what, const char *detail) {
+    std::fprintf(stderr, "mcb_gb300: %s%s%s\n", what, detail ? ": " : "", detail ? detail : "");
+    std::exit(1);
+}
+
+void check_host(int rc, const char *what) {
+    if (rc != MCBH_OK) {
+        char code[32];
+        std::snprintf(code, sizeof code, "error %d", rc);
+        fail(what, code);
+    }
+}
+
+void check_gpu(int rc, const char *what) {
+    if (rc != MCBGPU_OK) fail(what, mcbgpu_last_error());
+}
+
+struct Stats {  // the reference's GPU stats row (include/stats.h:256-338)
+    long long nodes = 0, edges = 0, new_edges = 0, nodes_removed = 0, fvs = 0, initial = 0, final_ = 0;
+    long long total_weight = 0;
+    int nchunks = 1, nstreams = 1;
+    double total_mb = 0, static_mb = 0, variable_mb = 0;
+    bool load_entire = true;
+    double t_trees = 0, t_collect = 0, t_inspection = 0, t_gpu = 0, t_hybrid = 0, t_main = 0;
+
+    void append(const char *path) const {
+        const bool exists = access(path, F_OK) == 0;
+        FILE *f = std::fopen(path, "a");
+        if (!f) fail("cannot open the statistics file", path);
+        if (!exists)
+            std::fprintf(f,
+                         "Total_Nodes,Total_Edges,New_Edges,Nodes_removed,Fvs_size,Initial_Cycles,Final_cycles,"
+                         "Total_Weight,nchunks,nstreams,total_memory_usage(mb),static_memory_usage(mb),"
+                         "variable_memory_usage(mb),load_entire_memory,Construction_trees(s),Collect_cycles(s),"
+                         "Inspection_time(s),Gpu_timings,Hybrid_Timings(s),Preprocessing Time(s),Main_loop(s),"
+                         "Total_time(s)\n");
+        std::fprintf(f, "%lld,%lld,%lld,%lld,%lld,%lld,%lld,%lld,%d,%d,%lf,%lf,%lf,%s,%lf,%lf,%lf,%lf,%lf,%lf,%lf,%lf\n",
+                     nodes, edges, new_edges, nodes_removed, fvs, initial, final_, total_weight, nchunks, nstreams,
+                     total_mb, static_mb, variable_mb, load_entire ? "YES" : "NO", t_trees, t_collect, t_inspection,
+                     t_gpu, t_hybrid, t_trees + t_collect, t_main, t_main + t_trees + t_collect);
+        std::fclose(f);
+    }
+};
+
+void write_cycles(const char *path, const std::vector<int64_t> &sel, const std::vector<int32_t> &root,
+                  const std::vector<int32_t> &edge, const std::vector<int32_t> &weight,
+                  const std::vector<uint32_t> &rows, const std::vector<uint32_t> &cols, const int32_t *vmap,
+                  long long total) {
+    FILE *f = std::fopen(path, "w");
+    if (!f) fail("cannot open the cycle file", path);
+    const char *bar = "=================================================================================";
+    auto id = [&](uint32_t v) { return (unsigned)(vmap ? vmap[v] : (int32_t)v) + 1u; };
+    for (int64_t r : sel) {
+        std::fprintf(f, "%s\nRoot is %u\nEdge is %u - %u\nTotal weight = %d\n%s\n", bar, id((uint32_t)root[r]),
+                     id(rows[edge[r]]), id(cols[edge[r]]), weight[r], bar);
+    }
+    std::fprintf(f, "Total Weight = %lld\n", total);
+    std::fclose(f);
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    std::vector<const char *> pos;
+    const char *cycles_path = nullptr, *cycles_input_path = nullptr;
+    bool plain = false;
+    for (int i = 1; i < argc; i++) {
+        if (!std::strcmp(argv[i], "--cycles") && i + 1 < argc)
+            cycles_path = argv[++i];
+        else if (!std::strcmp(argv[i], "--cycles-input") && i + 1 < argc)
+            cycles_input_path = argv[++i];
+        else if (!std::strcmp(argv[i], "--plain"))
+            plain = true;
+        else
+            pos.push_back(argv[i]);
+    }
+    if (pos.size() < 3) {
+        std::printf("Ist Argument should indicate the InputFile\n");
+        std::printf("2nd Argument should indicate the OutputFile\n");
+        std::printf("3th argument should indicate the number of threads.(Optional) (1 default)\n");
+        std::printf("4th Argument is chunk_size.(Optional) (720 default)\n");
+        std::printf("options: --cycles FILE, --cycles-input FILE, --plain\n");
+        return 1;
+    }
+    const char *input = pos[0], *stats_path = pos[1];
+    const int threads = std::atoi(pos[2]);
+    const double t0 = now_s();
+
+    mcbh_problem *p = nullptr;
+    check_host(mcbh_problem_from_mtx(input, &p), "cannot read the input graph");
+    mcbh_options opt{};
+    opt.threads = threads > 0 ? threads : 1;
+    opt.contract_chains = 1;
+    opt.cycle_lists = 1;
+    check_host(mcbh_prepare(p, &opt), "preprocessing failed");
+    mcbh_info info{};
+    check_host(mcbh_get_info(p, &info), "mcbh_get_info");
+
+    Stats st;
+    st.nodes = info.nodes;
+    st.edges = info.edges2;
+    if (info.single_cycle) {  // every vertex has degree two (mcb_cycle_deg_two_remove.cpp:104-111)
+        st.fvs = 1;
+        st.nodes_removed = info.nodes - 1;
+        st.final_ = 1;
+        st.initial = 1;
+        st.total_weight = info.total_weight_input;
+        st.append(stats_path);
+        mcbh_problem_free(p);
+        return 0;
+    }
+    st.nodes_removed = info.nodes_removed;
+    st.new_edges = info.reduced_edges2;
+    st.fvs = info.fvs_size;
+    st.initial = info.num_candidates;
+    st.t_trees = info.t_trees;
+    st.t_collect = info.t_collect;
+
+    const int32_t N = info.num_coords;
+    const int64_t K = info.num_candidates;
+    std::vector<int32_t> root(K), edge(K), weight(K), tree(K);
+    check_host(mcbh_get_candidates(p, root.data(), edge.data(), weight.data(), tree.data()), "mcbh_get_candidates");
+    std::vector<int64_t> off(K + 1);
+    std::vector<int32_t> coords(info.cycle_nnz > 0 ? info.cycle_nnz : 1);
+    check_host(mcbh_get_cycle_lists(p, off.data(), coords.data()), "mcbh_get_cycle_lists");
+
+    int dev = 0, sms = 0;
+    size_t mem = 0;
+    check_gpu(mcbgpu_init_cuda(&dev, &sms, &mem), "CUDA initialisation");
+    const double t1 = now_s();
+    mcbgpu_solver *s = nullptr;
+    check_gpu(mcbgpu_solver_create(&s, N, K, off[K]), "mcbgpu_solver_create");
+    check_gpu(mcbgpu_solver_upload(s, weight.data(), off.data(), coords.data(), nullptr), "mcbgpu_solver_upload");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, 0);
+    check_gpu(plain ? mcbgpu_solver_run_plain(s, -1, nullptr) : mcbgpu_solver_run(s, -1, nullptr), "solve");
+    cudaEventRecord(b, 0);
+    std::vector<int64_t> sel(N);
+    int64_t total = 0;
+    check_gpu(mcbgpu_solver_results(s, sel.data(), N, &total, nullptr), "mcbgpu_solver_results");
+    float gpu_ms = 0;
+    cudaEventElapsedTime(&gpu_ms, a, b);
+    const double t2 = now_s();
+
+    st.final_ = N;
+    st.total_weight = total;
+    st.total_mb = (double)mcbgpu_solver_device_bytes(s) / (1024.0 * 1024.0);
+    st.static_mb = (double)(sizeof(int32_t) * K + sizeof(int64_t) * (K + 1) + sizeof(int32_t) * off[K]) /
+                   (1024.0 * 1024.0);
+    st.variable_mb = st.total_mb - st.static_mb;
+    st.t_gpu = gpu_ms / 1000.0;
+    st.t_inspection = gpu_ms / 1000.0;
+    st.t_main = t2 - t1;
+    st.append(stats_path);
+
+    if (cycles_path || cycles_input_path) {
+        const int64_t e2 = info.reduced_edges2;
+        std::vector<uint32_t> rows(e2), cols(e2), rev(e2), ro(info.reduced_nodes + 1);
+        std::vector<int32_t> wts(e2), vmap(info.reduced_nodes);
+        check_host(mcbh_get_reduced_graph(p, rows.data(), cols.data(), wts.data(), rev.data(), ro.data()),
+                   "mcbh_get_reduced_graph");
+        check_host(mcbh_get_vertex_map(p, vmap.data()), "mcbh_get_vertex_map");
+        if (cycles_path) write_cycles(cycles_path, sel, root, edge, weight, rows, cols, nullptr, total);
+        if (cycles_input_path) write_cycles(cycles_input_path, sel, root, edge, weight, rows, cols, vmap.data(), total);
+    }
+    std::printf("mcb_gb300: %s: N=%d K=%lld total weight %lld, solve %.3f s, all %.3f s\n", input, N, (long long)K,
+                (long long)total, gpu_ms / 1000.0, now_s() - t0);
+    mcbgpu_solver_destroy(s);
+    mcbh_problem_free(p);
+    return 0;
+}

@@ -94,6 +94,7 @@ struct mcbh_problem {
     // reduced multigraph
     Graph rg;
     std::vector<int> r_chain, r_orig;
+    std::vector<int> r_vertex;  // reduced vertex -> input vertex
     int nodes_removed = 0;
     int source_vertex = 0;
     // FVS
@@ -241,6 +242,9 @@ void build_reduced(mcbh_problem &P, const ChainResult *cr) {
     }
     Graph &r = P.rg;
     r.n = cnt;
+    P.r_vertex.assign((size_t)cnt, -1);
+    for (int v = 0; v < g.n; v++)
+        if (label[v] >= 0) P.r_vertex[label[v]] = v;
     std::vector<EdgeSlot> s;
     s.reserve(2 * new_edges.size() + g.slots());
     auto insert_pair = [&](u32 a, u32 b, int wt, int chain, int orig) {
@@ -886,6 +890,12 @@ int mcbh_get_fvs(const mcbh_problem *p, int32_t *fvs_array, uint32_t *fvs_vertic
     NEED_PREPARED(p);
     if (fvs_array) std::memcpy(fvs_array, p->fvs_array.data(), p->fvs_array.size() * 4);
     if (fvs_vertices) std::memcpy(fvs_vertices, p->fvs_vertices.data(), p->fvs_vertices.size() * 4);
+    return MCBH_OK;
+}
+
+int mcbh_get_vertex_map(const mcbh_problem *p, int32_t *input_vertex) {
+    NEED_PREPARED(p);
+    if (input_vertex) std::memcpy(input_vertex, p->r_vertex.data(), p->r_vertex.size() * 4);
     return MCBH_OK;
 }
 

@@ -225,6 +225,14 @@ class Problem:
             return fa, fv
         return self._get("fvs", f)
 
+    def vertex_map(self) -> np.ndarray:
+        """Input vertex (0-based) of every reduced vertex."""
+        def f():
+            vm = np.empty(self.info.reduced_nodes, np.int32)
+            check_host(host_lib().mcbh_get_vertex_map(self._h, ptr(vm)), "mcbh_get_vertex_map")
+            return vm
+        return self._get("vertex_map", f)
+
     def coords(self):
         def f():
             i = self.info

@@ -16,10 +16,11 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session", autouse=True)
 def _built():
-    from minimumcyclebasis_gb300.build import build_host, build_gpu, build_oracle
+    from minimumcyclebasis_gb300.build import build_driver, build_gpu, build_host, build_oracle
     build_host()
     build_oracle()
     build_gpu()
+    build_driver()
     yield
 
 

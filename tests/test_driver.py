@@ -1,0 +1,83 @@
+"""The mcb_gb300 driver executable: the reference driver's command line, stats row
+and cycle listing (mcb/mcb_cycle_deg_two_remove.cpp, include/stats.h:256-338,
+include/cycles.h:197-207)."""
+import csv
+import os
+import subprocess
+
+import numpy as np
+import pytest
+from conftest import ROOT, load_golden
+
+from minimumcyclebasis_gb300 import Problem
+
+DRIVER = os.path.join(ROOT, "minimumcyclebasis_gb300", "lib", "mcb_gb300")
+COUNTS = ["Total_Nodes", "Total_Edges", "New_Edges", "Fvs_size", "Initial_Cycles", "Final_cycles", "Total_Weight"]
+
+
+def run(*args):
+    return subprocess.run([DRIVER, *map(str, args)], capture_output=True, text=True, timeout=600)
+
+
+def read_rows(path):
+    with open(path) as f:
+        return list(csv.DictReader(f))
+
+
+def test_usage_without_arguments():
+    r = run()
+    assert r.returncode == 1 and "InputFile" in r.stdout
+
+
+def test_single_cycle_graph(tmp_path):
+    # every vertex of degree two: the basis is the graph itself, no GPU involved
+    # (mcb/mcb_cycle_deg_two_remove.cpp:104-111)
+    n = 7
+    mtx = tmp_path / "ring.mtx"
+    w = [3, 1, 4, 1, 5, 9, 2]
+    mtx.write_text("%%%%MatrixMarket matrix coordinate integer symmetric\n%d %d %d\n" % (n, n, n) +
+                   "".join("%d %d %d\n" % (i + 1, (i + 1) % n + 1, w[i]) for i in range(n)))
+    out = tmp_path / "stats.csv"
+    r = run(mtx, out, 1)
+    assert r.returncode == 0, r.stderr
+    row = read_rows(out)[0]
+    assert int(row["Total_Nodes"]) == n and int(row["Total_Edges"]) == 2 * n
+    assert int(row["Nodes_removed"]) == n - 1 and int(row["Fvs_size"]) == 1
+    assert int(row["Initial_Cycles"]) == 1 and int(row["Final_cycles"]) == 1
+    assert int(row["Total_Weight"]) == sum(w)
+    # a second run appends a row under the same header
+    assert run(mtx, out, 1).returncode == 0
+    assert len(read_rows(out)) == 2
+
+
+def expected_cycles(fx, use_input_ids):
+    p = Problem.from_mtx(fx["mtx"]).prepare(threads=2, cycle_lists=False)
+    root, edge, weight, _ = p.candidates()
+    rows, cols = p.reduced_graph()[:2]
+    vmap = p.vertex_map() if use_input_ids else np.arange(p.info.reduced_nodes)
+    bar = "=" * 81
+    lines = []
+    for r in fx["selected_ranks"]:
+        lines += [bar, "Root is %d" % (vmap[root[r]] + 1), "Edge is %d - %d" % (vmap[rows[edge[r]]] + 1,
+                                                                              vmap[cols[edge[r]]] + 1),
+                  "Total weight = %d" % weight[r], bar]
+    lines.append("Total Weight = %d" % fx["total_weight"])
+    return lines
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["grid8x8_s3", "rand300_s0", "planar300_s5", "blocktree12_s2", "batch7_g1"])
+@pytest.mark.parametrize("plain", [False, True])
+def test_driver_matches_reference(tmp_path, name, plain):
+    fx = load_golden(name)
+    out, cyc, cyc_in = tmp_path / "stats.csv", tmp_path / "c.txt", tmp_path / "ci.txt"
+    args = [fx["mtx"], out, 4, 720, "--cycles", cyc, "--cycles-input", cyc_in] + (["--plain"] if plain else [])
+    r = run(*args)
+    assert r.returncode == 0, r.stderr
+    row = read_rows(out)[0]
+    ref = fx["mcb_cpu_csv"]
+    for col in COUNTS:
+        assert int(row[col]) == int(ref[col]), col
+    assert int(row["Nodes_removed"]) == int(ref["Node_removed"])
+    assert cyc.read_text().splitlines() == expected_cycles(fx, False)
+    assert cyc_in.read_text().splitlines() == expected_cycles(fx, True)
