@@ -182,8 +182,9 @@ int mcbgpu_solver_kernel_stats(mcbgpu_solver *s, mcbgpu_kernel_stat *out, int ma
  * [6] / [7] / [8] SM clock cycles of CTA 0 in the scan / barrier / merge parts,
  * [9]-[13] where a bounded barrier wait gave up (CTA+1, step, rank, generation,
  * arrivals), [14]/[15] most/fewest barriers of a CTA in one launch, [16]-[19] first
- * step at which two CTAs disagreed on the merged result (flag, step, CTA, block).
- * Synchronises the device. */
+ * step at which two CTAs disagreed on the merged result (flag, step, CTA, block),
+ * [20] / [21] / [22] SM clock cycles of CTA 0 in the block tail: resolve, the tail's
+ * grid barrier, final rows + tables.  Synchronises the device. */
 int mcbgpu_solver_diagnostics(mcbgpu_solver *s, int64_t *out, int n, int reset);
 /* Kernel launches issued by this handle so far (for accounting). */
 int64_t mcbgpu_solver_launches(const mcbgpu_solver *s);

@@ -64,12 +64,12 @@ constexpr unsigned kNoIndex = 0xFFFFFFFFu;
 
 // Kernel classes for the optional per-launch profile (events + algorithmic bytes).
 enum KernelClass {
-    KC_INIT, KC_TILE_MINC, KC_TRANSPOSE, KC_WSTREAM, KC_PIVOT, KC_RESOLVE, KC_MATERIALIZE, KC_TABLES,
+    KC_INIT, KC_TILE_MINC, KC_TRANSPOSE, KC_WSTREAM, KC_PIVOT,
     KC_BLK_UPDATE, KC_SEARCH, KC_UPDATE, KC_CYCLE, KC_RESET, KC_VALIDATE, KC_COUNT
 };
 const char *const kKernelNames[KC_COUNT] = {
-    "init_identity", "tile_minc", "blk_transpose", "blk_w", "blk_pivot", "blk_resolve", "blk_materialize",
-    "blk_tables", "blk_update", "search", "update", "cycle_vector", "reset_state", "validate"};
+    "init_identity", "tile_minc", "blk_transpose", "blk_w", "blk_pivot", "blk_update", "search", "update",
+    "cycle_vector", "reset_state", "validate"};
 
 struct IterSlot {            // state of one per-iteration search
     unsigned long long best; // first odd rank (kNone until found)
@@ -83,6 +83,7 @@ struct BlockState {
     long long pred_tiles;          // tiles the streaming pass computes for this block
     long long max_tile;            // deepest tile the previous block's pivot search touched
     unsigned long long total;      // running 64-bit total weight of the basis
+    unsigned tail_ok, pad_;        // the pivot kernel's CTA 0 resolved the block
     long long pivrank[64];
     unsigned long long pivW[64];   // the pivots' W as found (not reduced)
     unsigned long long mask[64];   // final S_{e0+k} as a combination of S^0_{e0+l}
@@ -589,11 +590,288 @@ __device__ __forceinline__ int nth_bit(unsigned mask, unsigned j) {
     return __ffs(mask) - 1;
 }
 
+// ---- block tail, run inside the pivot kernel after its last step -------------
+struct TailArgs {
+    uint64_t *S;
+    uint64_t *tab;
+    long long *selected;
+    const int32_t *weight;
+    unsigned *pairs, *sorted, *word_end;
+    unsigned pair_cap;
+    int P, e0, Wb, tables;  // tables = 0 for the last block (no later rows)
+};
+
+// Named CTA barrier 1 over the warps 1.. of the CTA (warp 0 is busy elsewhere);
+// non-aligned form, like cta_sync.
+__device__ __forceinline__ void helpers_sync(unsigned nthreads) {
+    asm volatile("barrier.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+
+// Resolve the block's b iterations on masks (one CTA of at least 64 + 32 threads).
+// Pivot index = rank order.  m_k starts as e_k; iteration k takes the first pivot p
+// with <W_p, m_k> odd; every later m_j with <W_p, m_j> odd gets m_j ^= m_k (the
+// reference's update restricted to the block, mcb/mcb_cycle_deg_two_remove.cpp:371-390).
+// Warp 0 runs the b sequential steps.  The selected cycles are the b pivots in some
+// order, so meanwhile the other warps gather the pivots' coordinates into (coordinate,
+// pivot) pairs and sort them by S word (counting sort; word_end[w] = number of pairs
+// whose word is below w).  At the end the pivot index of every pair is replaced by
+// the iteration that selected it.  `hist` is shared scratch of P + 1 words.  Returns
+// false (and sets a status bit) if the block cannot be resolved.
+#ifdef MCB_TAIL_PROFILE
+__device__ unsigned long long g_tail_prof[8];
+#define TAIL_STAMP(i) \
+    do { \
+        if (threadIdx.x == 0 || threadIdx.x == 32) atomicAdd(&g_tail_prof[i], (unsigned long long)(clock64() - t_start)); \
+    } while (0)
+#else
+#define TAIL_STAMP(i) \
+    do { \
+    } while (0)
+#endif
+
+__device__ bool resolve_block(BlockState *bs, int rank, const int64_t *__restrict__ off,
+                              const int32_t *__restrict__ coords, const TailArgs &ta, unsigned *hist,
+                              unsigned *status) {
+#ifdef MCB_TAIL_PROFILE
+    const long long t_start = clock64();
+#endif
+    const int e0 = ta.e0, P = ta.P;
+    const int32_t *__restrict__ weight = ta.weight;
+    unsigned *pairs = ta.pairs, *sorted = ta.sorted, *word_end = ta.word_end;
+    const unsigned pair_cap = ta.pair_cap;
+    __shared__ uint64_t s_w[64];
+    __shared__ long long s_r[64];
+    __shared__ int s_sel[64], s_kof[64];
+    __shared__ int64_t s_beg[64];
+    __shared__ unsigned s_pre[65];
+    __shared__ unsigned s_part[32];
+    __shared__ unsigned s_fail;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int b = (int)bs->b;
+    if (rank < b) {
+        if (tid == 0) atomicOr(status, ST_RANK_DEFICIT);
+        return false;
+    }
+    if (tid < 64) {
+        s_w[tid] = tid < b ? bs->pivW[tid] : 0ull;
+        s_r[tid] = tid < b ? bs->pivrank[tid] : -1;
+        s_kof[tid] = 0;
+    }
+    if (tid == 0) s_fail = 0;
+    cta_sync();
+    TAIL_STAMP(0);
+    if (tid < 32) {
+        // A[j][p] = <m_j, W_p> as 64 rows of 64 bits, lane l holding rows l and l + 32;
+        // m_j = e_j at the start, so A is the bit transpose of the W's.  Iteration k:
+        // p_k = the first unused p with A[k][p] = 1; every later row j with
+        // A[j][p_k] = 1 takes row k (m_j ^= m_k, and A[j] ^= A[k] with it).  Rows
+        // i < k are final, so gcol[k] bit i = A[i][p_k].
+        const uint64_t w0 = s_w[lane], w1 = s_w[32 + lane];
+        uint64_t a0 = 0, a1 = 0;
+        for (int j = 0; j < 64; j++) {
+            const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(w0 >> j) & 1u);
+            const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(w1 >> j) & 1u);
+            const uint64_t row = (uint64_t)lo | ((uint64_t)hi << 32);
+            if (lane == (j & 31)) {
+                if (j < 32)
+                    a0 = row;
+                else
+                    a1 = row;
+            }
+        }
+        uint64_t m0 = 1ull << lane, m1 = 1ull << (32 + lane);
+        uint64_t used = 0;
+        for (int k = 0; k < b; k++) {
+            const uint64_t ak = __shfl_sync(0xffffffffu, k < 32 ? a0 : a1, k & 31);
+            const uint64_t mk = __shfl_sync(0xffffffffu, k < 32 ? m0 : m1, k & 31);
+            const uint64_t cand = ak & ~used;
+            if (!cand) {
+                if (lane == 0) s_fail = 1;
+                break;
+            }
+            const int p = __ffsll((long long)cand) - 1;
+            used |= 1ull << p;
+            const bool h0 = (a0 >> p) & 1ull, h1 = (a1 >> p) & 1ull;
+            const unsigned g0 = __ballot_sync(0xffffffffu, lane < k && h0);
+            const unsigned g1 = __ballot_sync(0xffffffffu, 32 + lane < k && h1);
+            if (lane == 0) {
+                s_sel[k] = p;
+                s_kof[p] = k;
+                bs->gcol[k] = (uint64_t)g0 | ((uint64_t)g1 << 32);
+            }
+            if (lane > k && h0) {
+                a0 ^= ak;
+                m0 ^= mk;
+            }
+            if (32 + lane > k && h1) {
+                a1 ^= ak;
+                m1 ^= mk;
+            }
+        }
+        bs->mask[lane] = m0;
+        bs->mask[32 + lane] = m1;
+        TAIL_STAMP(1);
+    } else {
+        // warps 1..: the pivots' (coordinate, pivot) pairs, sorted by S word
+        const unsigned nh = blockDim.x - 32, t = tid - 32;
+        const unsigned nw = (unsigned)P + 1;
+        for (unsigned w = t; w < nw; w += nh) hist[w] = 0;
+        unsigned long long wsum = 0;
+        if (t < 64) {
+            unsigned len = 0;
+            if ((int)t < b) {
+                const long long r = s_r[t];
+                s_beg[t] = off[r];
+                len = (unsigned)(off[r + 1] - off[r]);
+                wsum = (unsigned long long)(long long)weight[r];
+            }
+            unsigned incl = len;
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += v;
+            }
+            s_pre[t + 1] = incl;  // per-warp inclusive; fixed up below
+            for (int d = 16; d > 0; d >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, d);
+            if (lane == 0) atomicAdd(&bs->total, wsum);
+        }
+        helpers_sync(nh);
+        if (t == 0) {
+            s_pre[0] = 0;
+            const unsigned carry = s_pre[32];
+            for (int i = 33; i <= 64; i++) s_pre[i] += carry;
+            const unsigned total = s_pre[64];
+            bs->npairs = total < pair_cap ? total : pair_cap;
+            if (total > pair_cap) atomicOr(status, ST_BAD_INPUT);
+        }
+        helpers_sync(nh);
+        const unsigned total = s_pre[64] < pair_cap ? s_pre[64] : pair_cap;
+        for (unsigned i = t; i < total; i += nh) {
+            int lo = 0, hi = b - 1;  // last pivot with s_pre[p] <= i
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_pre[mid] <= i)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const unsigned c = (unsigned)coords[s_beg[lo] + (i - s_pre[lo])];
+            pairs[i] = (c << 6) | (unsigned)lo;
+            atomicAdd(&hist[c >> 6], 1u);
+        }
+        helpers_sync(nh);
+        TAIL_STAMP(2);
+        {
+            const unsigned per = (nw + nh - 1) / nh;
+            const unsigned a = t * per < nw ? t * per : nw, z = a + per < nw ? a + per : nw;
+            unsigned sum = 0;
+            for (unsigned w = a; w < z; w++) sum += hist[w];
+            unsigned incl = sum;
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += v;
+            }
+            if (lane == 31) s_part[t >> 5] = incl;
+            helpers_sync(nh);
+            unsigned run = incl - sum;
+            for (int x = 0; x < (int)(t >> 5); x++) run += s_part[x];
+            for (unsigned w = a; w < z; w++) {
+                const unsigned h = hist[w];
+                hist[w] = run;
+                word_end[w] = run;
+                run += h;
+            }
+        }
+        helpers_sync(nh);
+        for (unsigned i = t; i < total; i += nh) {
+            const unsigned pr = pairs[i];
+            sorted[atomicAdd(&hist[pr >> 12], 1u)] = pr;
+        }
+        TAIL_STAMP(3);
+    }
+    cta_sync();
+    TAIL_STAMP(4);
+    if (s_fail) {
+        if (tid == 0) atomicOr(status, ST_NO_CANDIDATE);
+        return false;
+    }
+    // selections, and the iteration of every sorted pair in place of its pivot
+    if (tid < b) {
+        ta.selected[e0 + tid] = s_r[s_sel[tid]];
+        bs->sel[tid] = s_sel[tid];
+    }
+    const unsigned total = s_pre[64] < pair_cap ? s_pre[64] : pair_cap;
+    for (unsigned i = tid; i < total; i += blockDim.x) {
+        const unsigned pr = sorted[i];
+        sorted[i] = (pr & ~63u) | (unsigned)s_kof[pr & 63u];
+    }
+    TAIL_STAMP(5);
+    return true;
+}
+
+// S_{e0+k} := XOR of S^0_{e0+l} over l in mask[k], in place, words [0, Wb), and the
+// Four-Russians tables of the final rows: tab[g][pat][w] = XOR of S_{e0+8g+i} over
+// the bits i of pat.  Column groups of kMatCols words, group cg handled by CTA
+// cg mod G; `buf` is shared scratch of 2 x 64 x (kMatCols + 1) words.
+#ifndef MCB_MAT_COLS
+#define MCB_MAT_COLS 8
+#endif
+constexpr int kMatCols = MCB_MAT_COLS;
+
+__device__ void materialize_tables(const TailArgs &ta, const BlockState *bs, int b, uint64_t *buf) {
+    uint64_t(*s0)[kMatCols + 1] = reinterpret_cast<uint64_t(*)[kMatCols + 1]>(buf);
+    uint64_t(*s1)[kMatCols + 1] = s0 + 64;
+    __shared__ uint64_t sm[64];
+    if (threadIdx.x < 64) sm[threadIdx.x] = (int)threadIdx.x < b ? bs->mask[threadIdx.x] : 0ull;
+    const int Wb = ta.Wb, P = ta.P, e0 = ta.e0;
+    const int ng = (Wb + kMatCols - 1) / kMatCols;
+    for (int cg = blockIdx.x; cg < ng; cg += gridDim.x) {
+        const int w0 = cg * kMatCols;
+        cta_sync();  // the masks are in place; the previous group's tables are read
+        for (int idx = threadIdx.x; idx < 64 * kMatCols; idx += blockDim.x) {
+            const int l = idx / kMatCols, w = idx % kMatCols;
+            s0[l][w] = (l < b && w0 + w < Wb) ? ta.S[(size_t)(e0 + l) * P + w0 + w] : 0ull;
+        }
+        cta_sync();
+        for (int idx = threadIdx.x; idx < 64 * kMatCols; idx += blockDim.x) {
+            const int k = idx / kMatCols, w = idx % kMatCols;
+            uint64_t acc = 0;
+            if (k < b && w0 + w < Wb) {
+                for (uint64_t m = sm[k]; m; m &= m - 1) acc ^= s0[__ffsll((long long)m) - 1][w];
+                ta.S[(size_t)(e0 + k) * P + w0 + w] = acc;
+            }
+            s1[k][w] = acc;
+        }
+        if (!ta.tables) continue;
+        cta_sync();
+        // one thread per (word, table group, quarter of the patterns); Gray-code order
+        // inside the quarter: one XOR per entry
+        for (int idx = threadIdx.x; idx < kMatCols * 8 * 4; idx += blockDim.x) {
+            const int w = idx % kMatCols, g = (idx / kMatCols) >> 2, q = (idx / kMatCols) & 3;
+            if (w0 + w >= Wb) continue;
+            uint64_t v[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) v[i] = s1[8 * g + i][w];
+            uint64_t *out = ta.tab + (size_t)g * 256 * P + w0 + w;
+            const int t0 = q * 64;
+            const int g0 = t0 ^ (t0 >> 1);
+            uint64_t cur = 0;
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if ((g0 >> i) & 1) cur ^= v[i];
+            out[(size_t)g0 * P] = cur;
+            for (int t = t0 + 1; t < t0 + 64; t++) {
+                cur ^= v[__ffs(t) - 1];
+                out[(size_t)(t ^ (t >> 1)) * P] = cur;
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
     long long K, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
     const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T, int bound, BlockState *bs,
     uint64_t *Warr, unsigned *tile_epoch, PivotReport *reports, GridBar *gb, unsigned *status,
-    unsigned long long *bytes, unsigned long long *diag, unsigned long long *dbg) {
+    unsigned long long *bytes, unsigned long long *diag, unsigned long long *dbg, TailArgs ta) {
     // dynamic shared memory: global tables | local tables | window W's | merge buffers | report staging
     extern __shared__ __align__(128) unsigned char dsm[];
     const unsigned G = gridDim.x;
@@ -914,6 +1192,28 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
         k++;
         cyc_merge += clock64() - c2;
     }
+    // ---- block tail: CTA 0 resolves the block; then every CTA materialises its
+    // column groups of the final rows and their tables ----
+    long long cyc_resolve = 0, cyc_tailbar = 0, cyc_mat = 0;
+    if (ok) {
+        const long long c3 = clock64();
+        if (c == 0) {
+            const bool done = resolve_block(bs, grank, off, coords, ta, reinterpret_cast<unsigned *>(win), status);
+            if (threadIdx.x == 0) bs->tail_ok = done ? 1u : 0u;
+        }
+        const long long c4 = clock64();
+        nbar++;
+        if (!grid_barrier(gb, G, gen)) {
+            ok = false;
+        } else {
+            const long long c5 = clock64();
+            if (*((volatile unsigned *)&bs->tail_ok)) materialize_tables(ta, bs, b, win);
+            cta_sync();
+            cyc_tailbar = c5 - c4;
+            cyc_mat = clock64() - c5;
+        }
+        cyc_resolve = c4 - c3;
+    }
     if (!ok && threadIdx.x == 0 && (*((volatile unsigned *)&gb->abort))) atomicOr(status, ST_WAIT_TIMEOUT);
     for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
     if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
@@ -934,6 +1234,12 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
         atomicAdd(&diag[6], (unsigned long long)cyc_scan);
         atomicAdd(&diag[7], (unsigned long long)cyc_bar);
         atomicAdd(&diag[8], (unsigned long long)cyc_merge);
+        atomicAdd(&diag[20], (unsigned long long)cyc_resolve);
+        atomicAdd(&diag[21], (unsigned long long)cyc_tailbar);
+        atomicAdd(&diag[22], (unsigned long long)cyc_mat);
+#ifdef MCB_TAIL_PROFILE
+        for (int i = 0; i < 6; i++) diag[24 + i] = g_tail_prof[i];
+#endif
     }
 }
 
@@ -942,203 +1248,6 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
 // (5 x G x kLmax words) and the report staging (G x (2 kLmax + 2) words).
 size_t pivot_smem_bytes(int G) {
     return 32768 + 8 * (size_t)kWinW + 8 * 5 * (size_t)G * kLmax + 8 * (size_t)G * (2 * kLmax + 2);
-}
-
-// Resolve the block's b iterations on masks.  Pivot index = rank order.
-// m_k starts as e_k; iteration k takes the first pivot p with <W_p, m_k> odd; every
-// later m_j with <W_p, m_j> odd gets m_j ^= m_k (the reference's update restricted
-// to the block, mcb/mcb_cycle_deg_two_remove.cpp:371-390).  Warp 0 runs the 64
-// steps; then all threads record the selections and build the (coordinate, k) list
-// of the chosen cycles for the update kernel.
-__global__ void __launch_bounds__(256) blk_resolve_kernel(BlockState *bs, int e0, const int64_t *__restrict__ off,
-                                                          const int32_t *__restrict__ coords,
-                                                          const int32_t *__restrict__ weight, long long *selected,
-                                                          unsigned *pairs, unsigned pair_cap, unsigned *sorted,
-                                                          unsigned *word_end, int P, unsigned *status) {
-    extern __shared__ unsigned hist[];  // P + 1 counters
-    __shared__ uint64_t s_w[64];
-    __shared__ long long s_r[64];
-    __shared__ int s_sel[64];
-    __shared__ int64_t s_beg[64];
-    __shared__ unsigned s_pre[65];
-    __shared__ unsigned s_fail;
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int b = (int)bs->b;
-    const unsigned rank = bs->rank;
-    if (rank < (unsigned)b) {
-        if (tid == 0) atomicOr(status, ST_RANK_DEFICIT);
-        return;
-    }
-    if (tid < 64) {
-        s_w[tid] = tid < b ? bs->pivW[tid] : 0ull;
-        s_r[tid] = tid < b ? bs->pivrank[tid] : -1;
-    }
-    if (tid == 0) s_fail = 0;
-    cta_sync();
-    if (tid < 32) {
-        const uint64_t w0 = s_w[lane], w1 = s_w[32 + lane];
-        uint64_t m0 = 1ull << lane, m1 = 1ull << (32 + lane);
-        bool used0 = lane >= b, used1 = 32 + lane >= b;
-        for (int k = 0; k < b; k++) {
-            const uint64_t mk = __shfl_sync(0xffffffffu, k < 32 ? m0 : m1, k & 31);
-            const unsigned o0 = __ballot_sync(0xffffffffu, !used0 && parity64(w0 & mk));
-            const unsigned o1 = __ballot_sync(0xffffffffu, !used1 && parity64(w1 & mk));
-            int p;
-            if (o0)
-                p = __ffs(o0) - 1;
-            else if (o1)
-                p = 32 + __ffs(o1) - 1;
-            else {
-                if (lane == 0) s_fail = 1;
-                break;
-            }
-            if (p < 32 && lane == p) used0 = true;
-            if (p >= 32 && lane == p - 32) used1 = true;
-            const uint64_t wp = s_w[p];
-            // gcol[k] bit i = <W_p, m_i> for i < k (rows i are final)
-            const unsigned g0 = __ballot_sync(0xffffffffu, lane < k && parity64(wp & m0));
-            const unsigned g1 = __ballot_sync(0xffffffffu, 32 + lane < k && parity64(wp & m1));
-            if (lane == 0) {
-                s_sel[k] = p;
-                bs->gcol[k] = (uint64_t)g0 | ((uint64_t)g1 << 32);
-            }
-            if (lane > k && parity64(wp & m0)) m0 ^= mk;
-            if (32 + lane > k && parity64(wp & m1)) m1 ^= mk;
-        }
-        bs->mask[lane] = m0;
-        bs->mask[32 + lane] = m1;
-    }
-    cta_sync();
-    if (s_fail) {
-        if (tid == 0) atomicOr(status, ST_NO_CANDIDATE);
-        return;
-    }
-    // selections, weights, chosen cycles' coordinate ranges
-    unsigned len = 0;
-    unsigned long long wsum = 0;
-    if (tid < 64) {
-        if (tid < b) {
-            const long long r = s_r[s_sel[tid]];
-            selected[e0 + tid] = r;
-            bs->sel[tid] = s_sel[tid];
-            wsum = (unsigned long long)(long long)weight[r];
-            s_beg[tid] = off[r];
-            len = (unsigned)(off[r + 1] - off[r]);
-        }
-        unsigned incl = len;
-        for (int d = 1; d < 32; d <<= 1) {
-            const unsigned t = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= d) incl += t;
-        }
-        s_pre[tid + 1] = incl;  // per-warp inclusive; fixed up below
-        for (int d = 16; d > 0; d >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, d);
-        if (lane == 0) atomicAdd(&bs->total, wsum);
-    }
-    cta_sync();
-    if (tid == 0) {
-        s_pre[0] = 0;
-        const unsigned carry = s_pre[32];
-        for (int i = 33; i <= 64; i++) s_pre[i] += carry;
-        const unsigned total = s_pre[64];
-        bs->npairs = total < pair_cap ? total : pair_cap;
-        if (total > pair_cap) atomicOr(status, ST_BAD_INPUT);
-    }
-    cta_sync();
-    const unsigned total = s_pre[64] < pair_cap ? s_pre[64] : pair_cap;
-    for (unsigned i = tid; i < total; i += blockDim.x) {
-        int lo = 0, hi = b - 1;  // last k with s_pre[k] <= i
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_pre[mid] <= i)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        pairs[i] = ((unsigned)coords[s_beg[lo] + (i - s_pre[lo])] << 6) | (unsigned)lo;
-    }
-    // counting sort of the pairs by S word (coordinate >> 6): consecutive pairs then
-    // read neighbouring words of a row, and word_end[w] = number of pairs whose word
-    // is below w bounds the pairs that can meet the support [0, j] of a row S_j
-    const unsigned nw = (unsigned)P + 1;
-    for (unsigned w = tid; w < nw; w += blockDim.x) hist[w] = 0;
-    cta_sync();
-    for (unsigned i = tid; i < total; i += blockDim.x) atomicAdd(&hist[pairs[i] >> 12], 1u);
-    cta_sync();
-    {
-        __shared__ unsigned s_part[8];
-        const unsigned per = (nw + blockDim.x - 1) / blockDim.x;
-        const unsigned a = tid * per < nw ? tid * per : nw, z = a + per < nw ? a + per : nw;
-        unsigned sum = 0;
-        for (unsigned w = a; w < z; w++) sum += hist[w];
-        unsigned incl = sum;
-        for (int d = 1; d < 32; d <<= 1) {
-            const unsigned t = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= d) incl += t;
-        }
-        if (lane == 31) s_part[tid >> 5] = incl;
-        cta_sync();
-        unsigned run = incl - sum;
-        for (int x = 0; x < (int)(tid >> 5); x++) run += s_part[x];
-        for (unsigned w = a; w < z; w++) {
-            const unsigned h = hist[w];
-            hist[w] = run;
-            word_end[w] = run;
-            run += h;
-        }
-    }
-    cta_sync();
-    for (unsigned i = tid; i < total; i += blockDim.x) {
-        const unsigned pr = pairs[i];
-        sorted[atomicAdd(&hist[pr >> 12], 1u)] = pr;
-    }
-}
-
-// S_{e0+k} := XOR of S^0_{e0+l} over l in mask[k], in place, words [0, Wb).
-// Each CTA owns 32 word columns and keeps the original rows in shared memory.
-__global__ void blk_materialize_kernel(uint64_t *S, int P, int e0, int Wb, const BlockState *bs) {
-    __shared__ uint64_t s0[64][33];
-    __shared__ uint64_t sm[64];
-    const int b = (int)bs->b;
-    const int w0 = blockIdx.x * 32;
-    if (threadIdx.x < 64) sm[threadIdx.x] = threadIdx.x < b ? bs->mask[threadIdx.x] : 0;
-    for (int idx = threadIdx.x; idx < 64 * 32; idx += blockDim.x) {
-        int l = idx >> 5, w = idx & 31;
-        s0[l][w] = (l < b && w0 + w < Wb) ? S[(size_t)(e0 + l) * P + w0 + w] : 0ull;
-    }
-    cta_sync();
-    for (int idx = threadIdx.x; idx < 64 * 32; idx += blockDim.x) {
-        int k = idx >> 5, w = idx & 31;
-        if (k >= b || w0 + w >= Wb) continue;
-        uint64_t m = sm[k], acc = 0;
-        while (m) {
-            int l = __ffsll((long long)m) - 1;
-            m &= m - 1;
-            acc ^= s0[l][w];
-        }
-        S[(size_t)(e0 + k) * P + w0 + w] = acc;
-    }
-}
-
-// tab[g][pat][w] = XOR of the final rows S_{e0+8g+i} for bits i of pat, w < Wb.
-__global__ void blk_tables_kernel(const uint64_t *__restrict__ S, int P, int e0, int b, int Wb, int Pt,
-                                  uint64_t *__restrict__ tab) {
-    const int total = 8 * Wb;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
-        const int g = idx / Wb, w = idx % Wb;
-        uint64_t v[8];
-#pragma unroll
-        for (int i = 0; i < 8; i++) v[i] = (8 * g + i < b) ? S[(size_t)(e0 + 8 * g + i) * P + w] : 0ull;
-        uint64_t *out = tab + (size_t)g * 256 * Pt + w;
-        uint64_t cur = 0;
-        out[0] = 0;
-        // Gray-code order: one XOR per entry
-        for (int i = 1; i < 256; i++) {
-            int flip = __ffs(i) - 1;
-            cur ^= v[flip];
-            int gray = i ^ (i >> 1);
-            out[(size_t)gray * Pt] = cur;
-        }
-    }
 }
 
 // Rows j >= e0+b, kUpdRows consecutive rows per warp.  D_j (64 bits) = <C_sel_k, S_j>:
@@ -1405,9 +1514,9 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
         const int G = s->sm_count > 0 ? s->sm_count : 1;  // one CTA per SM
         const size_t smem = pivot_smem_bytes(G);
         e = cudaFuncSetAttribute(blk_pivot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        const size_t rsmem = sizeof(unsigned) * ((size_t)s->P + 1);
-        if (e == cudaSuccess && rsmem > 48 * 1024)
-            e = cudaFuncSetAttribute(blk_resolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+        // the block tail sorts the pairs in shared memory past the tables (P + 1 counters)
+        // and materialises 2 x 64 x (kMatCols + 1) words there
+        if (e == cudaSuccess && sizeof(unsigned) * ((size_t)s->P + 1) > smem - 32768) e = cudaErrorInvalidValue;
         int per_sm = 0;
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blk_pivot_kernel, kPivotThreads, smem);
@@ -1644,26 +1753,24 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             unsigned long long *nb = L.bytes();
             unsigned long long *dg = s->d_diag;
             unsigned long long *db = s->d_diag + 32;
-            void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db};
+            TailArgs ta;
+            ta.S = s->d_S;
+            ta.tab = s->d_tab;
+            ta.selected = s->d_selected;
+            ta.weight = s->d_weight;
+            ta.pairs = s->d_pairs;
+            ta.sorted = s->d_pairs + s->pair_cap;
+            ta.word_end = s->d_word_end;
+            ta.pair_cap = s->pair_cap;
+            ta.P = s->P;
+            ta.e0 = (int)e0;
+            ta.Wb = Wb;
+            ta.tables = e0 + b < s->N ? 1 : 0;
+            void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db, &ta};
             MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kPivotThreads),
                                                  args, pivot_smem_bytes(s->pivot_grid), st));
         }
-        {
-            Launch L(s, KC_RESOLVE, st);
-            blk_resolve_kernel<<<1, 256, sizeof(unsigned) * ((size_t)s->P + 1), st>>>(
-                s->d_bs, (int)e0, s->d_off, s->d_coords, s->d_weight, s->d_selected, s->d_pairs, s->pair_cap,
-                s->d_pairs + s->pair_cap, s->d_word_end, s->P, s->d_status);
-        }
-        {
-            Launch L(s, KC_MATERIALIZE, st);
-            blk_materialize_kernel<<<(Wb + 31) / 32, 256, 0, st>>>(s->d_S, s->P, (int)e0, Wb, s->d_bs);
-        }
         if (e0 + b < s->N) {
-            {
-                Launch L(s, KC_TABLES, st);
-                int tgrid = (8 * Wb + 255) / 256;
-                blk_tables_kernel<<<tgrid, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->P, s->d_tab);
-            }
             Launch L(s, KC_BLK_UPDATE, st);
             int rows = (int)(s->N - (e0 + b));
             int grid = (rows + 8 * kUpdRows - 1) / (8 * kUpdRows);  // 8 warps x kUpdRows rows per CTA pass

@@ -189,7 +189,8 @@ class Solver:
         keys = ["pivot_steps", "local_pivots", "merge_candidates", "tiles_loaded", "tiles_computed", "blocks",
                 "cycles_scan", "cycles_barrier", "cycles_merge", "timeout_cta_plus1", "timeout_step", "timeout_rank",
                 "timeout_gen", "timeout_count", "max_barriers_per_cta", "min_barriers_per_cta", "diverged",
-                "div_step", "div_cta", "div_epoch"]
+                "div_step", "div_cta", "div_epoch", "cycles_tail_resolve", "cycles_tail_barrier",
+                "cycles_tail_tables"]
         return dict(zip(keys, out.tolist()))
 
     @property
