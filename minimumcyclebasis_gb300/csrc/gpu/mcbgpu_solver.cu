@@ -56,6 +56,12 @@ constexpr unsigned kSpinLimit = 1u << 24;
 #define MCB_W_CHUNK 8
 #endif
 
+#ifndef MCB_EARLY_WIN
+#define MCB_EARLY_WIN 2  // window while the rank is below MCB_EARLY_RANK
+#endif
+#ifndef MCB_EARLY_RANK
+#define MCB_EARLY_RANK 48
+#endif
 constexpr int kLmax = MCB_LMAX;           // local pivots a CTA reports per pivot step
 constexpr int kWinTiles = MCB_WIN_TILES;  // tiles a CTA scans per pivot step (<= 32)
 constexpr int kUpdRows = MCB_UPD_ROWS;    // rows per warp group in the block update (<= 32)
@@ -465,12 +471,11 @@ __global__ void __launch_bounds__(kTile) blk_w_kernel(long long K, const int64_t
     const unsigned epoch = bs->epoch;
     const long long ntiles = bs->pred_tiles;
     unsigned long long nb = (blockIdx.x == 0 && threadIdx.x == 0) ? 8ull * (unsigned long long)bound : 0ull;
+    // no barrier per tile: a thread moves on to its next tile as soon as its own
+    // candidate is done; the tags (read only by the next kernel) are written at the end
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        if (tile_minc[t] >= bound) {  // every W of the tile is 0: tag it, write nothing
-            if (threadIdx.x == 0) {
-                tile_epoch[t] = (epoch << 1) | 1u;
-                nb += 8;
-            }
+        if (tile_minc[t] >= bound) {  // every W of the tile is 0: nothing to write
+            if (threadIdx.x == 0) nb += 8;
             continue;
         }
         const long long r = t * kTile + threadIdx.x;
@@ -481,9 +486,9 @@ __global__ void __launch_bounds__(kTile) blk_w_kernel(long long K, const int64_t
             nb += 8 + 8 + 4ull * nread;  // offset, W write, coordinates read
         }
         Warr[r] = W;
-        cta_sync();
-        if (threadIdx.x == 0) tile_epoch[t] = epoch << 1;
     }
+    for (long long t = blockIdx.x + (long long)threadIdx.x * gridDim.x; t < ntiles; t += (long long)blockDim.x * gridDim.x)
+        tile_epoch[t] = (epoch << 1) | (tile_minc[t] >= bound ? 1u : 0u);
     for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
     if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
 }
@@ -930,7 +935,8 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
         // window: this CTA's tiles tf, tf + G, ... (t = c mod G) from the scan start on
         const long long t0 = s / kTile;
         const long long tf = t0 + (((long long)c - t0 % G) + G) % G;
-        const int nwin = tf >= ntiles ? 0 : (int)min((long long)kWinTiles, (ntiles - 1 - tf) / G + 1);
+        const int wsz = grank < MCB_EARLY_RANK ? MCB_EARLY_WIN : kWinTiles;  // same in every CTA
+        const int nwin = tf >= ntiles ? 0 : (int)min((long long)wsz, (ntiles - 1 - tf) / G + 1);
         if (threadIdx.x < (unsigned)nwin) s_tag[threadIdx.x] = ld_acquire_u32(&tile_epoch[tf + (long long)threadIdx.x * G]);
         cta_sync();
         unsigned copymask = 0, zeromask = 0, missmask = 0;
@@ -1018,8 +1024,8 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
                 break;
             }
         }
-        if (!trunc && nwin == kWinTiles) {  // a shorter window reached the last tile: end = K
-            const long long tl = tf + (long long)(kWinTiles - 1) * G;
+        if (!trunc && nwin == wsz) {  // a shorter window reached the last tile: end = K
+            const long long tl = tf + (long long)(wsz - 1) * G;
             end = (tl + 1) * kTile < K ? (tl + 1) * kTile : K;
         }
         n_local += nloc;
