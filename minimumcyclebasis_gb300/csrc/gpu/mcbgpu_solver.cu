@@ -55,6 +55,9 @@ constexpr unsigned kSpinLimit = 1u << 24;
 #ifndef MCB_W_CHUNK
 #define MCB_W_CHUNK 8
 #endif
+#ifndef MCB_UPD_SPLIT
+#define MCB_UPD_SPLIT 1  // warps per row group in the block update (1, 2, 4 or 8)
+#endif
 
 #ifndef MCB_EARLY_WIN
 #define MCB_EARLY_WIN 2  // window while the rank is below MCB_EARLY_RANK
@@ -93,7 +96,7 @@ struct BlockState {
     long long pivrank[64];
     unsigned long long pivW[64];   // the pivots' W as found (not reduced)
     unsigned long long mask[64];   // final S_{e0+k} as a combination of S^0_{e0+l}
-    unsigned long long gcol[64];   // gcol[k] bit i = <C_sel_k, S_{e0+i}>, i < k
+    unsigned long long gcol[2][64];  // by block parity: gcol[k] bit i = <C_sel_k, S_{e0+i}>, i < k
     int sel[64];                   // pivot chosen at iteration e0+k
 };
 
@@ -604,6 +607,7 @@ struct TailArgs {
     unsigned *pairs, *sorted, *word_end;
     unsigned pair_cap;
     int P, e0, Wb, tables;  // tables = 0 for the last block (no later rows)
+    int par;                // block parity: which gcol / tables / sorted pairs to write
 };
 
 // Named CTA barrier 1 over the warps 1.. of the CTA (warp 0 is busy elsewhere);
@@ -702,7 +706,7 @@ __device__ bool resolve_block(BlockState *bs, int rank, const int64_t *__restric
             if (lane == 0) {
                 s_sel[k] = p;
                 s_kof[p] = k;
-                bs->gcol[k] = (uint64_t)g0 | ((uint64_t)g1 << 32);
+                bs->gcol[ta.par][k] = (uint64_t)g0 | ((uint64_t)g1 << 32);
             }
             if (lane > k && h0) {
                 a0 ^= ak;
@@ -1256,28 +1260,42 @@ size_t pivot_smem_bytes(int G) {
     return 32768 + 8 * (size_t)kWinW + 8 * 5 * (size_t)G * kLmax + 8 * (size_t)G * (2 * kLmax + 2);
 }
 
-// Rows j >= e0+b, kUpdRows consecutive rows per warp.  D_j (64 bits) = <C_sel_k, S_j>:
-// lanes split the chosen cycles' (coordinate, k) pairs, sorted by S word, and each
-// pair is applied to all rows of the group (independent gathers of neighbouring
-// words); pairs whose word lies above the group's last row are skipped (S_j has
-// support [0, j]).  Then lane i computes, for row i of the group, beta_k = D_k ^
-// <beta_{<k}, gcol_k> (the sequential effect of the block's 64 updates); then
-// S_j ^= XOR_k beta_k S_{e0+k} through the tables, lanes split the row's words.
-__global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int Pt,
-                                  const uint64_t *__restrict__ tab, const BlockState *bs,
-                                  const unsigned *__restrict__ pairs, const unsigned *__restrict__ word_end,
-                                  unsigned long long *bytes) {
+// Rows j >= e0+b in groups of kUpdRows consecutive rows, kUpdSplit warps per group.
+// D_j (64 bits) = <C_sel_k, S_j>: the group's warps split the chosen cycles'
+// (coordinate, k) pairs, sorted by S word, and each pair is applied to all rows of
+// the group (independent gathers of neighbouring words); pairs whose word lies above
+// the group's last row are skipped (S_j has support [0, j]).  The warps' partial D's
+// meet in shared memory (two buffers by iteration parity, one named barrier per
+// group and iteration).  Then lane i computes, for row i of the group, beta_k =
+// D_k ^ <beta_{<k}, gcol_k> (the sequential effect of the block's 64 updates); then
+// S_j ^= XOR_k beta_k S_{e0+k} through the tables, the group's warps split the
+// row's words.
+constexpr int kUpdThreads = 256;
+constexpr int kUpdSplit = MCB_UPD_SPLIT;
+constexpr int kUpdGroups = kUpdThreads / 32 / kUpdSplit;  // row groups per CTA
+
+// Rows [row_begin, row_end) of the block that starts at e0 with b iterations; gcol,
+// tab, pairs and word_end are that block's (they are double-buffered by block
+// parity, so the next block's tail can run while these rows are updated).
+__global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, long long row_begin, long long row_end,
+                                                                 int P, int b, int Wb, int Pt,
+                                                                 const uint64_t *__restrict__ tab,
+                                                                 const uint64_t *__restrict__ gcol,
+                                                                 const unsigned *__restrict__ pairs,
+                                                                 const unsigned *__restrict__ word_end,
+                                                                 unsigned long long *bytes) {
     unsigned long long nb = 0;
     __shared__ uint64_t sg[64];
-    const int b = (int)bs->b;
-    if (threadIdx.x < 64) sg[threadIdx.x] = threadIdx.x < b ? bs->gcol[threadIdx.x] : 0;
+    __shared__ uint64_t sD[2][kUpdGroups][kUpdSplit][kUpdRows];
+    if (threadIdx.x < 64) sg[threadIdx.x] = (int)threadIdx.x < b ? gcol[threadIdx.x] : 0;
     cta_sync();
-    const int lane = threadIdx.x & 31;
-    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
-    const long long first = e0 + b;
-    for (long long g0 = first + kUpdRows * (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); g0 < N;
-         g0 += kUpdRows * warps) {
-        const int rows = (int)((N - g0) < kUpdRows ? (N - g0) : kUpdRows);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gi = warp / kUpdSplit, h = warp % kUpdSplit;
+    const long long groups = (long long)gridDim.x * kUpdGroups;
+    int par = 0;
+    for (long long g0 = row_begin + kUpdRows * ((long long)blockIdx.x * kUpdGroups + gi); g0 < row_end;
+         g0 += kUpdRows * groups, par ^= 1) {
+        const int rows = (int)((row_end - g0) < kUpdRows ? (row_end - g0) : kUpdRows);
         const long long jl = g0 + rows - 1;
         const int wl = (int)(jl >> 6) + 1 < P ? (int)(jl >> 6) + 1 : P;
         const unsigned np = __ldg(word_end + wl);
@@ -1285,7 +1303,7 @@ __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int
         uint64_t D[kUpdRows];
 #pragma unroll
         for (int r = 0; r < kUpdRows; r++) D[r] = 0;
-        for (unsigned i = lane; i < np; i += 32) {
+        for (unsigned i = h * 32 + lane; i < np; i += 32 * kUpdSplit) {
             const unsigned pr = __ldg(pairs + i);
             const unsigned c = pr >> 6, k = pr & 63u, w = c >> 6, sh = c & 63u;
 #pragma unroll
@@ -1299,13 +1317,22 @@ __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int
             for (int o = 16; o > 0; o >>= 1) d ^= __shfl_xor_sync(0xffffffffu, d, o);
             if (lane == r) Dmine = d;
         }
+        if (kUpdSplit > 1) {
+            if (lane < kUpdRows) sD[par][gi][h][lane] = Dmine;
+            asm volatile("barrier.sync %0, %1;" ::"r"(1 + gi), "r"(32 * kUpdSplit) : "memory");
+            if (lane < kUpdRows) {
+                Dmine = 0;
+#pragma unroll
+                for (int q = 0; q < kUpdSplit; q++) Dmine ^= sD[par][gi][q][lane];
+            }
+        }
         uint64_t beta = 0;
         if (lane < rows) {
             for (int k = 0; k < b; k++) beta |= ((((Dmine >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]))) << k;
-            // algorithmic bytes: the S words the group's pairs touch (8 rows share each
-            // pair, counted once per row) plus, when the row changes, read + write of
-            // its first Wb words
-            nb += 8ull * np + (beta ? 16ull * (unsigned long long)Wb : 0ull);
+            // algorithmic bytes (counted by the group's first warp): the S words the
+            // group's pairs touch (8 rows share each pair, counted once per row) plus,
+            // when the row changes, read + write of its first Wb words
+            if (h == 0) nb += 8ull * np + (beta ? 16ull * (unsigned long long)Wb : 0ull);
         }
         for (int r = 0; r < rows; r++) {
             const uint64_t bt = __shfl_sync(0xffffffffu, beta, r);
@@ -1319,7 +1346,7 @@ __global__ void blk_update_kernel(uint64_t *S, int N, int P, int e0, int Wb, int
             const uint64_t *t5 = tab + ((size_t)5 * 256 + ((bt >> 40) & 255)) * Pt;
             const uint64_t *t6 = tab + ((size_t)6 * 256 + ((bt >> 48) & 255)) * Pt;
             const uint64_t *t7 = tab + ((size_t)7 * 256 + ((bt >> 56) & 255)) * Pt;
-            for (int w = lane; w < Wb; w += 32)
+            for (int w = h * 32 + lane; w < Wb; w += 32 * kUpdSplit)
                 Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
         }
     }
@@ -1349,9 +1376,11 @@ struct mcbgpu_solver {
     PivotReport *d_reports = nullptr;      // 2 x pivot_grid
     GridBar *d_gbar = nullptr;
     int pivot_grid = 0;
-    unsigned *d_pairs = nullptr;     // 2 x pair_cap
+    unsigned *d_pairs = nullptr;     // 3 x pair_cap: resolve scratch, sorted pairs of the two block parities
     unsigned pair_cap = 0;
-    unsigned *d_word_end = nullptr;  // P + 1: sorted pairs with S word < w
+    unsigned *d_word_end = nullptr;  // 2 x (P + 1): sorted pairs with S word < w, by block parity
+    cudaStream_t st2 = nullptr;      // the update of the rows beyond the next block
+    cudaEvent_t ev_fork = nullptr, ev_tail = nullptr, ev_upd[2] = {nullptr, nullptr};
     IterSlot *d_slots = nullptr;   // 2
     BlockState *d_bs = nullptr;
     long long *d_selected = nullptr;
@@ -1429,6 +1458,11 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_gbar);
     cudaFree(s->d_pairs);
     cudaFree(s->d_word_end);
+    if (s->st2) cudaStreamDestroy(s->st2);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_tail) cudaEventDestroy(s->ev_tail);
+    for (cudaEvent_t e : s->ev_upd)
+        if (e) cudaEventDestroy(e);
     cudaFree(s->d_slots);
     cudaFree(s->d_bs);
     cudaFree(s->d_selected);
@@ -1495,13 +1529,13 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_S, sizeof(uint64_t) * (size_t)N * s->P);
     ALLOC(s->d_C, sizeof(uint64_t) * (size_t)s->P);
     ALLOC(s->d_T, sizeof(uint64_t) * 64 * (size_t)s->P);
-    ALLOC(s->d_tab, sizeof(uint64_t) * 8 * 256 * (size_t)s->P);
+    ALLOC(s->d_tab, sizeof(uint64_t) * 2 * 8 * 256 * (size_t)s->P);
     ALLOC(s->d_Warr, sizeof(uint64_t) * (size_t)kTile * ntiles);
     ALLOC(s->d_tile_epoch, sizeof(unsigned) * ntiles);
     ALLOC(s->d_tile_minc, sizeof(int32_t) * ntiles);
     ALLOC(s->d_gmin, sizeof(unsigned long long) * 4);
     ALLOC(s->d_gbar, sizeof(GridBar));
-    ALLOC(s->d_word_end, sizeof(unsigned) * ((size_t)s->P + 1));
+    ALLOC(s->d_word_end, sizeof(unsigned) * 2 * ((size_t)s->P + 1));
     ALLOC(s->d_slots, sizeof(IterSlot) * 2);
     ALLOC(s->d_bs, sizeof(BlockState));
     ALLOC(s->d_selected, sizeof(long long) * (size_t)(N > 0 ? N : 1));
@@ -1514,7 +1548,11 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     if (e == cudaSuccess) e = cudaMemset(s->d_bytes, 0, sizeof(unsigned long long) * KC_COUNT);
     if (e == cudaSuccess) e = cudaMemset(s->d_tile_epoch, 0, sizeof(unsigned) * ntiles);
     if (e == cudaSuccess) e = cudaMemset(s->d_gbar, 0, sizeof(GridBar));
-    if (e == cudaSuccess) e = cudaMemset(s->d_word_end, 0, sizeof(unsigned) * ((size_t)s->P + 1));
+    if (e == cudaSuccess) e = cudaMemset(s->d_word_end, 0, sizeof(unsigned) * 2 * ((size_t)s->P + 1));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_tail, cudaEventDisableTiming);
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&s->ev_upd[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMemset(s->d_coords, 0, sizeof(int32_t) * (size_t)(nnz + 4));
     if (e == cudaSuccess) {
         const int G = s->sm_count > 0 ? s->sm_count : 1;  // one CTA per SM
@@ -1599,11 +1637,11 @@ int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t 
     }
     s->max_len = (int)chk[1];
     unsigned cap = (unsigned)(64 * (size_t)(s->max_len > 0 ? s->max_len : 1));
-    if (cap > s->pair_cap) {  // two halves: pairs in cycle order, pairs sorted by S word
+    if (cap > s->pair_cap) {  // resolve scratch + sorted pairs of the two block parities
         cudaFree(s->d_pairs);
         s->d_pairs = nullptr;
-        MCB_CUDA(cudaMalloc((void **)&s->d_pairs, sizeof(unsigned) * 2 * (size_t)cap));
-        s->device_bytes += (long long)sizeof(unsigned) * 2 * cap;
+        MCB_CUDA(cudaMalloc((void **)&s->d_pairs, sizeof(unsigned) * 3 * (size_t)cap));
+        s->device_bytes += (long long)sizeof(unsigned) * 3 * cap;
         s->pair_cap = cap;
     }
     const long long ntiles = (s->K + kTile - 1) / kTile;
@@ -1728,8 +1766,19 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
     const int64_t iters = (max_iterations >= 0 && max_iterations < s->N) ? max_iterations : s->N;
     const int sms = s->sm_count > 0 ? s->sm_count : 148;
     long long ntiles = (s->K + kTile - 1) / kTile;
+    // The update of a block is split: the next block's 64 rows on `st` (its
+    // transpose needs them), every later row on st2, where it overlaps the next
+    // block's transpose, streaming pass and pivot search.  Rows are updated block
+    // after block, so the next block's near rows wait for this block's far rows
+    // (ev_upd), and the buffers the far update reads (gcol, tables, sorted pairs,
+    // word_end) alternate by block parity.
+    MCB_CUDA(cudaEventRecord(s->ev_fork, st));
+    MCB_CUDA(cudaStreamWaitEvent(s->st2, s->ev_fork, 0));
+    bool far_pending = false;
+    int far_par = 0;
     for (int64_t e0 = 0; e0 < iters; e0 += 64) {
         const int b = (int)std::min<int64_t>(64, iters - e0);
+        const int par = (int)((e0 / 64) & 1);
         const int Wb = (int)((e0 + b + 63) / 64);
         const int bound = (int)(e0 + b);
         {
@@ -1761,32 +1810,55 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             unsigned long long *db = s->d_diag + 32;
             TailArgs ta;
             ta.S = s->d_S;
-            ta.tab = s->d_tab;
+            ta.tab = s->d_tab + (size_t)par * 8 * 256 * s->P;
             ta.selected = s->d_selected;
             ta.weight = s->d_weight;
             ta.pairs = s->d_pairs;
-            ta.sorted = s->d_pairs + s->pair_cap;
-            ta.word_end = s->d_word_end;
+            ta.sorted = s->d_pairs + (size_t)(1 + par) * s->pair_cap;
+            ta.word_end = s->d_word_end + (size_t)par * (s->P + 1);
             ta.pair_cap = s->pair_cap;
             ta.P = s->P;
             ta.e0 = (int)e0;
             ta.Wb = Wb;
             ta.tables = e0 + b < s->N ? 1 : 0;
+            ta.par = par;
             void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db, &ta};
             MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kPivotThreads),
                                                  args, pivot_smem_bytes(s->pivot_grid), st));
         }
         if (e0 + b < s->N) {
-            Launch L(s, KC_BLK_UPDATE, st);
-            int rows = (int)(s->N - (e0 + b));
-            int grid = (rows + 8 * kUpdRows - 1) / (8 * kUpdRows);  // 8 warps x kUpdRows rows per CTA pass
-            if (grid > sms * 8) grid = sms * 8;
-            if (grid < 1) grid = 1;
-            blk_update_kernel<<<grid, 256, 0, st>>>(s->d_S, s->N, s->P, (int)e0, Wb, s->P, s->d_tab, s->d_bs,
-                                                    s->d_pairs + s->pair_cap, s->d_word_end, L.bytes());
+            const long long near_end = std::min<long long>(e0 + b + 64, s->N), far_end = s->N;
+            const uint64_t *tab = s->d_tab + (size_t)par * 8 * 256 * s->P;
+            const uint64_t *gcol = reinterpret_cast<const uint64_t *>(&s->d_bs->gcol[par][0]);
+            const unsigned *pairs = s->d_pairs + (size_t)(1 + par) * s->pair_cap;
+            const unsigned *wend = s->d_word_end + (size_t)par * (s->P + 1);
+            auto grid_for = [&](long long rows) {
+                long long g = (rows + kUpdGroups * kUpdRows - 1) / (kUpdGroups * kUpdRows);
+                return (int)std::max<long long>(1, std::min<long long>(g, (long long)sms * 8));
+            };
+            if (near_end < far_end) {  // far rows: on st2 once this block's tail is done
+                MCB_CUDA(cudaEventRecord(s->ev_tail, st));
+                MCB_CUDA(cudaStreamWaitEvent(s->st2, s->ev_tail, 0));
+                Launch L(s, KC_BLK_UPDATE, s->st2);
+                blk_update_kernel<<<grid_for(far_end - near_end), kUpdThreads, 0, s->st2>>>(
+                    s->d_S, near_end, far_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes());
+            }
+            if (far_pending) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[far_par], 0));
+            {
+                Launch L(s, KC_BLK_UPDATE, st);
+                blk_update_kernel<<<grid_for(near_end - (e0 + b)), kUpdThreads, 0, st>>>(
+                    s->d_S, e0 + b, near_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes());
+            }
+            far_pending = near_end < far_end;
+            if (far_pending) {
+                far_par = par;
+                MCB_CUDA(cudaEventRecord(s->ev_upd[par], s->st2));
+            }
         }
         MCB_CUDA(cudaGetLastError());
     }
+    if (far_pending) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[far_par], 0));
+
     s->iters_run = iters;
     return MCBGPU_OK;
 }
