@@ -466,7 +466,10 @@ __device__ __forceinline__ uint64_t w_of_candidate(long long r, const int64_t *_
 // Streaming pass: W for tiles [0, bs->pred_tiles), one candidate per thread (1024
 // threads = one tile per CTA pass), written to Warr and tagged with the block's
 // epoch.  This is the bandwidth-bound part of the block's search.
-__global__ void __launch_bounds__(kTile) blk_w_kernel(long long K, const int64_t *__restrict__ off,
+#ifndef MCB_W_MINB
+#define MCB_W_MINB 1  // resident 1024-thread CTAs per SM the W pass is compiled for
+#endif
+__global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, const int64_t *__restrict__ off,
                                                     const int32_t *__restrict__ coords,
                                                     const int32_t *__restrict__ tile_minc,
                                                     const uint64_t *__restrict__ T, int bound, const BlockState *bs,
@@ -1525,7 +1528,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     } while (0)
     ALLOC(s->d_weight, sizeof(int32_t) * (size_t)K);
     ALLOC(s->d_off, sizeof(int64_t) * (size_t)(K + 1));
-    ALLOC(s->d_coords, sizeof(int32_t) * (size_t)(nnz + 4));  // 16-byte loads may read 3 past the end
+    ALLOC(s->d_coords, sizeof(int32_t) * (size_t)(nnz + 16));  // aligned 16-byte loads read up to 11 past the end
     ALLOC(s->d_S, sizeof(uint64_t) * (size_t)N * s->P);
     ALLOC(s->d_C, sizeof(uint64_t) * (size_t)s->P);
     ALLOC(s->d_T, sizeof(uint64_t) * 64 * (size_t)s->P);
@@ -1553,7 +1556,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_tail, cudaEventDisableTiming);
     for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&s->ev_upd[i], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaMemset(s->d_coords, 0, sizeof(int32_t) * (size_t)(nnz + 4));
+    if (e == cudaSuccess) e = cudaMemset(s->d_coords, 0, sizeof(int32_t) * (size_t)(nnz + 16));
     if (e == cudaSuccess) {
         const int G = s->sm_count > 0 ? s->sm_count : 1;  // one CTA per SM
         const size_t smem = pivot_smem_bytes(G);
