@@ -55,6 +55,9 @@ constexpr unsigned kSpinLimit = 1u << 24;
 #ifndef MCB_W_CHUNK
 #define MCB_W_CHUNK 8
 #endif
+#ifndef MCB_OTF_PAIRS
+#define MCB_OTF_PAIRS 1  // pivot kernel: walk two candidates per thread together on the fly
+#endif
 #ifndef MCB_UPD_SPLIT
 #define MCB_UPD_SPLIT 1  // warps per row group in the block update (1, 2, 4 or 8)
 #endif
@@ -461,6 +464,43 @@ __device__ __forceinline__ uint64_t w_of_candidate(long long r, const int64_t *_
         i += kWChunk;
     }
     return W;
+}
+
+// W of two candidates walked in lockstep (their loads overlap); rb < 0: only ra.
+__device__ __forceinline__ void w_of_two(long long ra, long long rb, const int64_t *__restrict__ off,
+                                         const int32_t *__restrict__ coords, const uint64_t *__restrict__ T,
+                                         int bound, unsigned &nread, uint64_t &Wa, uint64_t &Wb) {
+    int64_t ia = __ldg(off + ra), ea = __ldg(off + ra + 1);
+    int64_t ib = 0, eb = 0;
+    if (rb >= 0) {
+        ib = __ldg(off + rb);
+        eb = __ldg(off + rb + 1);
+    }
+    Wa = 0;
+    Wb = 0;
+    while (ia < ea || ib < eb) {
+        int ca[kWChunk], cb[kWChunk];
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) {
+            ca[q] = ia + q < ea ? __ldg(coords + ia + q) : 0x7fffffff;
+            cb[q] = ib + q < eb ? __ldg(coords + ib + q) : 0x7fffffff;
+        }
+        uint64_t ta[kWChunk], tb[kWChunk];
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) {
+            ta[q] = ca[q] < bound ? __ldg(T + ca[q]) : 0ull;
+            tb[q] = cb[q] < bound ? __ldg(T + cb[q]) : 0ull;
+        }
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) {
+            Wa ^= ta[q];
+            Wb ^= tb[q];
+        }
+        if (ia < ea) nread += (unsigned)(ea - ia < kWChunk ? ea - ia : kWChunk);
+        if (ib < eb) nread += (unsigned)(eb - ib < kWChunk ? eb - ib : kWChunk);
+        ia = ca[kWChunk - 1] >= bound ? ea : ia + kWChunk;
+        ib = cb[kWChunk - 1] >= bound ? eb : ib + kWChunk;
+    }
 }
 
 // Streaming pass: W for tiles [0, bs->pred_tiles), one candidate per thread (1024
@@ -879,6 +919,9 @@ __device__ void materialize_tables(const TailArgs &ta, const BlockState *bs, int
     }
 }
 
+#ifdef MCB_SCAN_PROFILE
+__device__ long long g_scan_prof[4];
+#endif
 __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
     long long K, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
     const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T, int bound, BlockState *bs,
@@ -942,6 +985,19 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
         // window: this CTA's tiles tf, tf + G, ... (t = c mod G) from the scan start on
         const long long t0 = s / kTile;
         const long long tf = t0 + (((long long)c - t0 % G) + G) % G;
+#ifdef MCB_SCAN_PROFILE
+        long long sp0 = clock64();
+#define SCAN_STAMP(i)                                                 \
+    do {                                                              \
+        const long long sp1 = clock64();                              \
+        if (threadIdx.x == 0 && c == 0) g_scan_prof[i] += sp1 - sp0; \
+        sp0 = sp1;                                                    \
+    } while (0)
+#else
+#define SCAN_STAMP(i) \
+    do {              \
+    } while (0)
+#endif
         const int wsz = grank < MCB_EARLY_RANK ? MCB_EARLY_WIN : kWinTiles;  // same in every CTA
         const int nwin = tf >= ntiles ? 0 : (int)min((long long)wsz, (ntiles - 1 - tf) / G + 1);
         if (threadIdx.x < (unsigned)nwin) s_tag[threadIdx.x] = ld_acquire_u32(&tile_epoch[tf + (long long)threadIdx.x * G]);
@@ -969,9 +1025,40 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
             for (int i = threadIdx.x; i < kTile; i += blockDim.x) win[(size_t)m * kTile + i] = 0;
         }
         n_loaded += (unsigned)__popc(copymask | zeromask);
+        SCAN_STAMP(0);
         if (missmask) {  // tiles beyond the streaming pass: W's computed here by the whole CTA
             const unsigned nm = (unsigned)__popc(missmask);
             unsigned nread = 0;
+#if MCB_OTF_PAIRS
+            // two candidates per thread walked together (positions idx and idx + half)
+            const unsigned tot = nm * kTile, half = (tot + 1) / 2;
+            for (unsigned idx = threadIdx.x; idx < half; idx += blockDim.x) {
+                const unsigned jdx = idx + half;
+                const int ma = nth_bit(missmask, idx / kTile);
+                const long long ta_ = tf + (long long)ma * G, ra = ta_ * kTile + idx % kTile;
+                const bool va = ra < K && tile_minc[ta_] < bound;
+                long long rb = -1;
+                int mb = 0;
+                if (jdx < tot) {
+                    mb = nth_bit(missmask, jdx / kTile);
+                    const long long tb_ = tf + (long long)mb * G;
+                    rb = tb_ * kTile + jdx % kTile;
+                    if (!(rb < K && tile_minc[tb_] < bound)) rb = -2;
+                }
+                uint64_t Wa = 0, Wb = 0;
+                if (va || rb >= 0) w_of_two(va ? ra : rb, va ? (rb >= 0 ? rb : -1) : -1, off, coords, T, bound, nread, Wa, Wb);
+                if (!va) {  // the walk ran on rb alone
+                    Wb = Wa;
+                    Wa = 0;
+                }
+                win[(size_t)ma * kTile + idx % kTile] = Wa;
+                Warr[ra] = Wa;
+                if (jdx < tot) {
+                    win[(size_t)mb * kTile + jdx % kTile] = rb >= 0 ? Wb : 0ull;
+                    Warr[(tf + (long long)mb * G) * kTile + jdx % kTile] = rb >= 0 ? Wb : 0ull;
+                }
+            }
+#else
             for (unsigned idx = threadIdx.x; idx < nm * kTile; idx += blockDim.x) {
                 const int m = nth_bit(missmask, idx / kTile);
                 const unsigned i = idx % kTile;
@@ -982,10 +1069,12 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
                 win[(size_t)m * kTile + i] = W;
                 Warr[r] = W;
             }
+#endif
             fence_proxy_async_global();  // a later step may bulk-copy these tiles
             nb += 4ull * nread + (threadIdx.x == 0 ? 16ull * kTile * nm : 0ull);
             n_computed += nm;
         }
+        SCAN_STAMP(1);
         if (copymask) {
             bool done = mbar_wait_bounded(&s_bar, mphase & 1u, 1u << 22);
             mphase++;
@@ -1005,6 +1094,7 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
             for (unsigned mm = missmask; mm; mm &= mm - 1)
                 tile_epoch[tf + (long long)(__ffs(mm) - 1) * G] = epoch << 1;
         }
+        SCAN_STAMP(2);
         // local echelon over the window in rank order
         const unsigned valid = (unsigned)nwin * kTile;
         unsigned from = (nwin > 0 && tf == t0) ? (unsigned)(s - t0 * kTile) : 0u;
@@ -1031,6 +1121,7 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
                 break;
             }
         }
+        SCAN_STAMP(3);
         if (!trunc && nwin == wsz) {  // a shorter window reached the last tile: end = K
             const long long tl = tf + (long long)(wsz - 1) * G;
             end = (tl + 1) * kTile < K ? (tl + 1) * kTile : K;
@@ -1250,6 +1341,9 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
         atomicAdd(&diag[20], (unsigned long long)cyc_resolve);
         atomicAdd(&diag[21], (unsigned long long)cyc_tailbar);
         atomicAdd(&diag[22], (unsigned long long)cyc_mat);
+#ifdef MCB_SCAN_PROFILE
+        for (int i = 0; i < 4; i++) diag[24 + i] = (unsigned long long)g_scan_prof[i];
+#endif
 #ifdef MCB_TAIL_PROFILE
         for (int i = 0; i < 6; i++) diag[24 + i] = g_tail_prof[i];
 #endif
