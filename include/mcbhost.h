@@ -76,6 +76,10 @@ int mcbh_problem_from_mtx(const char *path, mcbh_problem **out);
 int mcbh_problem_from_edges(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
                             const int32_t *w, mcbh_problem **out);
 int mcbh_prepare(mcbh_problem *p, const mcbh_options *opt);
+/* The edges of a Matrix-Market file as mcbh_problem_from_mtx reads them (0-based,
+ * file order).  Returns the edge count and sets *nodes; with u != NULL also fills
+ * u, v, w (cap entries available). */
+int64_t mcbh_read_mtx(const char *path, int32_t *nodes, int64_t cap, int32_t *u, int32_t *v, int32_t *w);
 void mcbh_problem_free(mcbh_problem *p);
 
 /* ---- accessors (caller-allocated outputs) --------------------------------- */
@@ -135,6 +139,16 @@ int64_t mcbh_gen_block_tree(int32_t blocks, int32_t nmin, int32_t nmax, int32_t 
                             int32_t *nodes);
 int mcbh_write_mtx(const char *path, int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
                    const int32_t *w);
+
+/* ---- biconnected components ------------------------------------------------ */
+/* Splits the edges of an undirected graph into biconnected components (Hopcroft-
+ * Tarjan; a bridge is a component of one edge, a self-loop one of its own).
+ * comp_of_edge[i] = component of edge i, components numbered in order of their
+ * first edge.  Returns the number of components.  The minimum cycle basis of a graph
+ * is the union of its components' bases, so every component can be solved on its
+ * own; this replaces the reference's bicc tool + per-component loop (bicc/,
+ * main.sh:19-32) inside one process. */
+int64_t mcbh_bcc_split(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v, int32_t *comp_of_edge);
 
 #ifdef __cplusplus
 }

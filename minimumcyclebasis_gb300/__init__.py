@@ -4,10 +4,10 @@ Host preparation (libmcbhost.so) reproduces the reference driver's reduced graph
 FVS, coordinate order and candidate rank order; the main loop runs on the GPU
 (libmcbgpu.so) behind the C ABI in include/mcbgpu.h.
 """
-from .host import (Graph, Problem, batch_graphs, block_tree_graph, grid_graph, planar_chain_graph,  # noqa: F401
-                   random_graph, rgg_graph)
+from .host import (Graph, Problem, batch_graphs, bcc_split, block_tree_graph, grid_graph,  # noqa: F401
+                   planar_chain_graph, random_graph, rgg_graph)
 from .gpu import GpuStruct, Solver, device_info, solve  # noqa: F401
 
 __all__ = ["Graph", "Problem", "grid_graph", "random_graph", "rgg_graph", "planar_chain_graph",
-           "block_tree_graph", "batch_graphs", "GpuStruct", "Solver",
+           "block_tree_graph", "batch_graphs", "bcc_split", "GpuStruct", "Solver",
            "device_info", "solve"]

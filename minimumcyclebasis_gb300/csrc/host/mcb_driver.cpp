@@ -18,6 +18,11 @@
 //                        "Total Weight = W" (mcb/Test_deg_two_remove.cpp:334-341)
 //   --cycles-input FILE  the same with the input graph's vertex ids + 1
 //   --plain              the per-iteration de Pina loop instead of the blocked one
+//   --bcc                split the graph into biconnected components first and solve
+//                        each one that has a cycle (in order of its first edge), one
+//                        stats row per component, the way the reference's bicc tool +
+//                        per-component loop (bicc/, main.sh:19-32) processes a graph;
+//                        the cycle listings give each component's basis in turn
 //
 // Exit status 0 on success; on any error a message on stderr and status 1 (the
 // reference prints and exits on every error too).
@@ -84,60 +89,37 @@ struct Stats {  // the reference's GPU stats row (include/stats.h:256-338)
     }
 };
 
-void write_cycles(const char *path, const std::vector<int64_t> &sel, const std::vector<int32_t> &root,
+// One cycle block per selected candidate, in the format of cycle::print.  vmap: the
+// vertex ids to print for each reduced vertex (0-based), or NULL for reduced ids.
+void write_cycles(FILE *f, const std::vector<int64_t> &sel, const std::vector<int32_t> &root,
                   const std::vector<int32_t> &edge, const std::vector<int32_t> &weight,
-                  const std::vector<uint32_t> &rows, const std::vector<uint32_t> &cols, const int32_t *vmap,
-                  long long total) {
-    FILE *f = std::fopen(path, "w");
-    if (!f) fail("cannot open the cycle file", path);
+                  const std::vector<uint32_t> &rows, const std::vector<uint32_t> &cols, const int32_t *vmap) {
     const char *bar = "=================================================================================";
     auto id = [&](uint32_t v) { return (unsigned)(vmap ? vmap[v] : (int32_t)v) + 1u; };
     for (int64_t r : sel) {
         std::fprintf(f, "%s\nRoot is %u\nEdge is %u - %u\nTotal weight = %d\n%s\n", bar, id((uint32_t)root[r]),
                      id(rows[edge[r]]), id(cols[edge[r]]), weight[r], bar);
     }
-    std::fprintf(f, "Total Weight = %lld\n", total);
-    std::fclose(f);
 }
 
-}  // namespace
-
-int main(int argc, char **argv) {
-    std::vector<const char *> pos;
-    const char *cycles_path = nullptr, *cycles_input_path = nullptr;
+struct Outputs {
+    const char *stats = nullptr;
+    FILE *cycles = nullptr, *cycles_input = nullptr;
     bool plain = false;
-    for (int i = 1; i < argc; i++) {
-        if (!std::strcmp(argv[i], "--cycles") && i + 1 < argc)
-            cycles_path = argv[++i];
-        else if (!std::strcmp(argv[i], "--cycles-input") && i + 1 < argc)
-            cycles_input_path = argv[++i];
-        else if (!std::strcmp(argv[i], "--plain"))
-            plain = true;
-        else
-            pos.push_back(argv[i]);
-    }
-    if (pos.size() < 3) {
-        std::printf("Ist Argument should indicate the InputFile\n");
-        std::printf("2nd Argument should indicate the OutputFile\n");
-        std::printf("3th argument should indicate the number of threads.(Optional) (1 default)\n");
-        std::printf("4th Argument is chunk_size.(Optional) (720 default)\n");
-        std::printf("options: --cycles FILE, --cycles-input FILE, --plain\n");
-        return 1;
-    }
-    const char *input = pos[0], *stats_path = pos[1];
-    const int threads = std::atoi(pos[2]);
-    const double t0 = now_s();
+    int threads = 1;
+};
 
-    mcbh_problem *p = nullptr;
-    check_host(mcbh_problem_from_mtx(input, &p), "cannot read the input graph");
+// Prepares and solves one problem; appends its stats row and its cycle blocks.
+// input_ids: the input vertex of every vertex of the problem's graph (NULL: the
+// problem's graph is the input graph).  Returns the basis weight.
+long long solve_one(mcbh_problem *p, const Outputs &o, const int32_t *input_ids) {
     mcbh_options opt{};
-    opt.threads = threads > 0 ? threads : 1;
+    opt.threads = o.threads > 0 ? o.threads : 1;
     opt.contract_chains = 1;
     opt.cycle_lists = 1;
     check_host(mcbh_prepare(p, &opt), "preprocessing failed");
     mcbh_info info{};
     check_host(mcbh_get_info(p, &info), "mcbh_get_info");
-
     Stats st;
     st.nodes = info.nodes;
     st.edges = info.edges2;
@@ -147,9 +129,8 @@ int main(int argc, char **argv) {
         st.final_ = 1;
         st.initial = 1;
         st.total_weight = info.total_weight_input;
-        st.append(stats_path);
-        mcbh_problem_free(p);
-        return 0;
+        st.append(o.stats);
+        return info.total_weight_input;
     }
     st.nodes_removed = info.nodes_removed;
     st.new_edges = info.reduced_edges2;
@@ -166,9 +147,13 @@ int main(int argc, char **argv) {
     std::vector<int32_t> coords(info.cycle_nnz > 0 ? info.cycle_nnz : 1);
     check_host(mcbh_get_cycle_lists(p, off.data(), coords.data()), "mcbh_get_cycle_lists");
 
-    int dev = 0, sms = 0;
-    size_t mem = 0;
-    check_gpu(mcbgpu_init_cuda(&dev, &sms, &mem), "CUDA initialisation");
+    static bool cuda_ready = false;  // first problem that needs the GPU
+    if (!cuda_ready) {
+        int dev = 0, sms = 0;
+        size_t mem = 0;
+        check_gpu(mcbgpu_init_cuda(&dev, &sms, &mem), "CUDA initialisation");
+        cuda_ready = true;
+    }
     const double t1 = now_s();
     mcbgpu_solver *s = nullptr;
     check_gpu(mcbgpu_solver_create(&s, N, K, off[K]), "mcbgpu_solver_create");
@@ -177,13 +162,15 @@ int main(int argc, char **argv) {
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     cudaEventRecord(a, 0);
-    check_gpu(plain ? mcbgpu_solver_run_plain(s, -1, nullptr) : mcbgpu_solver_run(s, -1, nullptr), "solve");
+    check_gpu(o.plain ? mcbgpu_solver_run_plain(s, -1, nullptr) : mcbgpu_solver_run(s, -1, nullptr), "solve");
     cudaEventRecord(b, 0);
     std::vector<int64_t> sel(N);
     int64_t total = 0;
     check_gpu(mcbgpu_solver_results(s, sel.data(), N, &total, nullptr), "mcbgpu_solver_results");
     float gpu_ms = 0;
     cudaEventElapsedTime(&gpu_ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
     const double t2 = now_s();
 
     st.final_ = N;
@@ -195,21 +182,118 @@ int main(int argc, char **argv) {
     st.t_gpu = gpu_ms / 1000.0;
     st.t_inspection = gpu_ms / 1000.0;
     st.t_main = t2 - t1;
-    st.append(stats_path);
+    st.append(o.stats);
+    mcbgpu_solver_destroy(s);
 
-    if (cycles_path || cycles_input_path) {
+    if (o.cycles || o.cycles_input) {
         const int64_t e2 = info.reduced_edges2;
         std::vector<uint32_t> rows(e2), cols(e2), rev(e2), ro(info.reduced_nodes + 1);
         std::vector<int32_t> wts(e2), vmap(info.reduced_nodes);
         check_host(mcbh_get_reduced_graph(p, rows.data(), cols.data(), wts.data(), rev.data(), ro.data()),
                    "mcbh_get_reduced_graph");
         check_host(mcbh_get_vertex_map(p, vmap.data()), "mcbh_get_vertex_map");
-        if (cycles_path) write_cycles(cycles_path, sel, root, edge, weight, rows, cols, nullptr, total);
-        if (cycles_input_path) write_cycles(cycles_input_path, sel, root, edge, weight, rows, cols, vmap.data(), total);
+        if (o.cycles) write_cycles(o.cycles, sel, root, edge, weight, rows, cols, nullptr);
+        if (o.cycles_input) {
+            if (input_ids)
+                for (auto &x : vmap) x = input_ids[x];
+            write_cycles(o.cycles_input, sel, root, edge, weight, rows, cols, vmap.data());
+        }
     }
-    std::printf("mcb_gb300: %s: N=%d K=%lld total weight %lld, solve %.3f s, all %.3f s\n", input, N, (long long)K,
-                (long long)total, gpu_ms / 1000.0, now_s() - t0);
-    mcbgpu_solver_destroy(s);
-    mcbh_problem_free(p);
+    return total;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    std::vector<const char *> pos;
+    const char *cycles_path = nullptr, *cycles_input_path = nullptr;
+    bool plain = false, bcc = false;
+    for (int i = 1; i < argc; i++) {
+        if (!std::strcmp(argv[i], "--cycles") && i + 1 < argc)
+            cycles_path = argv[++i];
+        else if (!std::strcmp(argv[i], "--cycles-input") && i + 1 < argc)
+            cycles_input_path = argv[++i];
+        else if (!std::strcmp(argv[i], "--plain"))
+            plain = true;
+        else if (!std::strcmp(argv[i], "--bcc"))
+            bcc = true;
+        else
+            pos.push_back(argv[i]);
+    }
+    if (pos.size() < 3) {
+        std::printf("Ist Argument should indicate the InputFile\n");
+        std::printf("2nd Argument should indicate the OutputFile\n");
+        std::printf("3th argument should indicate the number of threads.(Optional) (1 default)\n");
+        std::printf("4th Argument is chunk_size.(Optional) (720 default)\n");
+        std::printf("options: --cycles FILE, --cycles-input FILE, --plain, --bcc\n");
+        return 1;
+    }
+    const char *input = pos[0];
+    Outputs o;
+    o.stats = pos[1];
+    o.threads = std::atoi(pos[2]);
+    o.plain = plain;
+    if (cycles_path && !(o.cycles = std::fopen(cycles_path, "w"))) fail("cannot open the cycle file", cycles_path);
+    if (cycles_input_path && !(o.cycles_input = std::fopen(cycles_input_path, "w")))
+        fail("cannot open the cycle file", cycles_input_path);
+    const double t0 = now_s();
+    long long total = 0;
+    int solved = 0;
+    if (!bcc) {
+        mcbh_problem *p = nullptr;
+        check_host(mcbh_problem_from_mtx(input, &p), "cannot read the input graph");
+        total = solve_one(p, o, nullptr);
+        solved = 1;
+        mcbh_problem_free(p);
+    } else {
+        int32_t nodes = 0;
+        const int64_t m = mcbh_read_mtx(input, &nodes, 0, nullptr, nullptr, nullptr);
+        if (m < 0) fail("cannot read the input graph", nullptr);
+        std::vector<int32_t> u(m > 0 ? m : 1), v(m > 0 ? m : 1), w(m > 0 ? m : 1), comp(m > 0 ? m : 1);
+        check_host(mcbh_read_mtx(input, &nodes, m, u.data(), v.data(), w.data()) == m ? MCBH_OK : MCBH_E_IO,
+                   "cannot read the input graph");
+        const int64_t nc = mcbh_bcc_split(nodes, m, u.data(), v.data(), comp.data());
+        if (nc < 0) fail("biconnected split failed", nullptr);
+        // edges of every component in input order; vertices renumbered in order of
+        // first appearance (as bicc/Relabeller.cpp numbers a component file)
+        std::vector<int64_t> start(nc + 1, 0);
+        for (int64_t i = 0; i < m; i++) start[comp[i] + 1]++;
+        for (int64_t c = 0; c < nc; c++) start[c + 1] += start[c];
+        std::vector<int64_t> order(m > 0 ? m : 1), fill(start.begin(), start.end() - 1);
+        for (int64_t i = 0; i < m; i++) order[fill[comp[i]]++] = i;
+        std::vector<int32_t> local(nodes, -1);
+        for (int64_t c = 0; c < nc; c++) {
+            std::vector<int32_t> cu, cv, cw, ids;
+            for (int64_t k = start[c]; k < start[c + 1]; k++) {
+                const int64_t e = order[k];
+                for (int32_t x : {u[e], v[e]})
+                    if (local[x] < 0) {
+                        local[x] = (int32_t)ids.size();
+                        ids.push_back(x);
+                    }
+                cu.push_back(local[u[e]]);
+                cv.push_back(local[v[e]]);
+                cw.push_back(w[e]);
+            }
+            for (int32_t x : ids) local[x] = -1;
+            if ((int64_t)cu.size() < (int64_t)ids.size()) continue;  // a bridge: no cycle
+            mcbh_problem *p = nullptr;
+            check_host(mcbh_problem_from_edges((int32_t)ids.size(), (int64_t)cu.size(), cu.data(), cv.data(),
+                                               cw.data(), &p),
+                       "component");
+            total += solve_one(p, o, ids.data());
+            solved++;
+            mcbh_problem_free(p);
+        }
+    }
+    if (o.cycles) {
+        std::fprintf(o.cycles, "Total Weight = %lld\n", total);
+        std::fclose(o.cycles);
+    }
+    if (o.cycles_input) {
+        std::fprintf(o.cycles_input, "Total Weight = %lld\n", total);
+        std::fclose(o.cycles_input);
+    }
+    std::printf("mcb_gb300: %s: %d problem(s), total weight %lld, %.3f s\n", input, solved, total, now_s() - t0);
     return 0;
 }

@@ -725,6 +725,23 @@ int mcbh_problem_from_mtx(const char *path, mcbh_problem **out) {
     return rc;
 }
 
+int64_t mcbh_read_mtx(const char *path, int32_t *nodes, int64_t cap, int32_t *u, int32_t *v, int32_t *w) {
+    if (!path || !nodes) return MCBH_E_ARG;
+    int n = 0;
+    std::vector<int> a, b, c;
+    const int rc = read_mtx(path, n, a, b, c);
+    if (rc) return rc;
+    *nodes = n;
+    const int64_t m = (int64_t)a.size();
+    if (u) {
+        if (cap < m || !v || !w) return MCBH_E_ARG;
+        std::memcpy(u, a.data(), sizeof(int32_t) * (size_t)m);
+        std::memcpy(v, b.data(), sizeof(int32_t) * (size_t)m);
+        std::memcpy(w, c.data(), sizeof(int32_t) * (size_t)m);
+    }
+    return m;
+}
+
 void mcbh_problem_free(mcbh_problem *p) { delete p; }
 
 int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
@@ -1274,6 +1291,83 @@ int64_t mcbh_gen_block_tree(int32_t blocks, int32_t nmin, int32_t nmax, int32_t 
         while (k < m) add((int32_t)g.below((uint64_t)n), (int32_t)g.below((uint64_t)n));
     }
     return emit(out, u, v, w, nodes);
+}
+
+int64_t mcbh_bcc_split(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v, int32_t *comp_of_edge) {
+    if (nodes <= 0 || m < 0 || (m > 0 && (!u || !v || !comp_of_edge))) return MCBH_E_ARG;
+    for (int64_t i = 0; i < m; i++)
+        if (u[i] < 0 || u[i] >= nodes || v[i] < 0 || v[i] >= nodes) return MCBH_E_ARG;
+    // adjacency (edge ids) in input order
+    std::vector<int64_t> ro((size_t)nodes + 1, 0);
+    for (int64_t i = 0; i < m; i++) {
+        ro[(size_t)u[i] + 1]++;
+        if (v[i] != u[i]) ro[(size_t)v[i] + 1]++;
+    }
+    for (int32_t x = 0; x < nodes; x++) ro[(size_t)x + 1] += ro[x];
+    std::vector<int64_t> adj((size_t)ro[nodes]), fill(ro.begin(), ro.end() - 1);
+    for (int64_t i = 0; i < m; i++) {
+        adj[(size_t)fill[u[i]]++] = i;
+        if (v[i] != u[i]) adj[(size_t)fill[v[i]]++] = i;
+    }
+    // Hopcroft-Tarjan with an edge stack, as an explicit-stack DFS.  A self-loop is
+    // a component of its own.
+    std::vector<int64_t> disc((size_t)nodes, -1), low((size_t)nodes, 0);
+    std::vector<int64_t> estack;
+    std::vector<int32_t> raw(m > 0 ? (size_t)m : 1, -1);
+    int32_t ncomp = 0;
+    struct Frame {
+        int32_t v;
+        int64_t pe, it;  // parent edge, next adjacency slot
+    };
+    std::vector<Frame> st;
+    int64_t timer = 0;
+    for (int64_t i = 0; i < m; i++)
+        if (u[i] == v[i]) raw[i] = ncomp++;
+    for (int32_t s = 0; s < nodes; s++) {
+        if (disc[s] >= 0 || ro[s] == ro[(size_t)s + 1]) continue;
+        disc[s] = low[s] = timer++;
+        st.push_back({s, -1, ro[s]});
+        while (!st.empty()) {
+            Frame &f = st.back();
+            if (f.it < ro[(size_t)f.v + 1]) {
+                const int64_t e = adj[(size_t)f.it++];
+                if (e == f.pe || u[e] == v[e]) continue;
+                const int32_t w = u[e] == f.v ? v[e] : u[e];
+                if (disc[w] < 0) {
+                    estack.push_back(e);
+                    disc[w] = low[w] = timer++;
+                    st.push_back({w, e, ro[w]});
+                } else if (disc[w] < disc[f.v]) {
+                    estack.push_back(e);  // back edge
+                    low[f.v] = std::min(low[f.v], disc[w]);
+                }
+                continue;
+            }
+            const int32_t w = f.v;
+            const int64_t pe = f.pe;
+            st.pop_back();
+            if (st.empty()) break;
+            const int32_t p = st.back().v;
+            low[p] = std::min(low[p], low[w]);
+            if (low[w] >= disc[p]) {  // p separates w's subtree: pop one component
+                while (true) {
+                    const int64_t e = estack.back();
+                    estack.pop_back();
+                    raw[e] = ncomp;
+                    if (e == pe) break;
+                }
+                ncomp++;
+            }
+        }
+    }
+    // number components by their first input edge
+    std::vector<int32_t> ren((size_t)ncomp, -1);
+    int32_t next = 0;
+    for (int64_t i = 0; i < m; i++) {
+        if (ren[raw[i]] < 0) ren[raw[i]] = next++;
+        comp_of_edge[i] = ren[raw[i]];
+    }
+    return next;
 }
 
 int mcbh_write_mtx(const char *path, int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,

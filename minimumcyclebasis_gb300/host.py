@@ -132,6 +132,36 @@ def batch_graphs(count: int, nmin: int = 50, nmax: int = 5000, deg_lo: float = 2
     return out
 
 
+def bcc_split(g: Graph, keep_bridges: bool = False) -> list[Graph]:
+    """The biconnected components of g as graphs of their own, in order of their first
+    edge; a component's vertices are numbered in order of first appearance in its
+    edges (input order), as the reference's Relabeller numbers a component file
+    (bicc/Relabeller.cpp).  Components without a cycle (bridges) are dropped unless
+    keep_bridges.  The minimum cycle basis of g is the union of the components' bases."""
+    comp = np.empty(max(g.m, 1), np.int32)
+    nc = host_lib().mcbh_bcc_split(g.nodes, g.m, ptr(g.u), ptr(g.v), ptr(comp))
+    if nc < 0:
+        raise ValueError("bad graph for the biconnected split")
+    comp = comp[:g.m]
+    order = np.argsort(comp, kind="stable")
+    bounds = np.searchsorted(comp[order], np.arange(nc + 1))
+    out = []
+    for c in range(nc):
+        idx = order[bounds[c]:bounds[c + 1]]
+        u, v, w = g.u[idx], g.v[idx], g.w[idx]
+        verts = np.empty(2 * idx.size, np.int32)
+        verts[0::2], verts[1::2] = u, v
+        uniq, first = np.unique(verts, return_index=True)
+        rank = np.empty(uniq.size, np.int32)
+        rank[np.argsort(first, kind="stable")] = np.arange(uniq.size, dtype=np.int32)
+        relabel = dict(zip(uniq.tolist(), rank.tolist()))
+        cu = np.fromiter((relabel[x] for x in u.tolist()), np.int32, idx.size)
+        cv = np.fromiter((relabel[x] for x in v.tolist()), np.int32, idx.size)
+        if keep_bridges or idx.size >= uniq.size:
+            out.append(Graph(int(uniq.size), cu, cv, np.ascontiguousarray(w)))
+    return out
+
+
 class Problem:
     """A graph prepared for the de Pina main loop.
 

@@ -81,3 +81,36 @@ def test_driver_matches_reference(tmp_path, name, plain):
     assert int(row["Nodes_removed"]) == int(ref["Node_removed"])
     assert cyc.read_text().splitlines() == expected_cycles(fx, False)
     assert cyc_in.read_text().splitlines() == expected_cycles(fx, True)
+
+
+def test_bcc_mode_rings_and_bridge_without_gpu(tmp_path):
+    # two rings joined by a bridge: each ring is its own basis, the bridge carries none
+    edges = [(1, 2, 3), (2, 3, 4), (3, 1, 5), (3, 4, 7), (4, 5, 1), (5, 6, 2), (6, 4, 6)]
+    mtx = tmp_path / "g.mtx"
+    mtx.write_text("%%MatrixMarket matrix coordinate integer symmetric\n6 6 7\n" +
+                   "".join("%d %d %d\n" % e for e in edges))
+    out, cyc = tmp_path / "stats.csv", tmp_path / "c.txt"
+    r = run(mtx, out, 1, "--bcc", "--cycles", cyc)
+    assert r.returncode == 0, r.stderr
+    rows = read_rows(out)
+    assert [int(x["Total_Weight"]) for x in rows] == [12, 9]
+    assert cyc.read_text().splitlines()[-1] == "Total Weight = 21"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["blocktree12_s2", "rand300_w3_s2", "planar300_s5"])
+def test_bcc_mode_weight_matches_reference(tmp_path, name):
+    # per-component solves add up to the reference's whole-graph basis
+    fx = load_golden(name)
+    out, cyc = tmp_path / "stats.csv", tmp_path / "c.txt"
+    r = run(fx["mtx"], out, 4, "--bcc", "--cycles-input", cyc)
+    assert r.returncode == 0, r.stderr
+    rows = read_rows(out)
+    assert sum(int(x["Total_Weight"]) for x in rows) == fx["total_weight"]
+    assert sum(int(x["Final_cycles"]) for x in rows) == fx["G"]["num_coords"]
+    lines = cyc.read_text().splitlines()
+    assert lines[-1] == "Total Weight = %d" % fx["total_weight"]
+    weights = [int(x.split("= ")[1]) for x in lines if x.startswith("Total weight = ")]
+    rings = sum(int(x["Total_Weight"]) for x in rows if int(x["Initial_Cycles"]) == 1 and int(x["Fvs_size"]) == 1
+                and int(x["Final_cycles"]) == 1 and int(x["New_Edges"]) == 0)
+    assert sum(weights) + rings == fx["total_weight"]
