@@ -90,7 +90,7 @@ struct IterSlot {            // state of one per-iteration search
 };
 
 struct BlockState {
-    unsigned rank, epoch, b, npairs;
+    unsigned rank, epoch, b, pad0_;
     long long last_pivot;          // rank of the previous block's last pivot
     long long pred_tiles;          // tiles the streaming pass computes for this block
     long long max_tile;            // deepest tile the previous block's pivot search touched
@@ -100,16 +100,11 @@ struct BlockState {
     unsigned long long pivW[64];   // the pivots' W as found (not reduced)
     unsigned long long mask[64];   // final S_{e0+k} as a combination of S^0_{e0+l}
     unsigned long long gcol[2][64];  // by block parity: gcol[k] bit i = <C_sel_k, S_{e0+i}>, i < k
-    int sel[64];                   // pivot chosen at iteration e0+k
 };
 
 // Grid barrier state of the cooperative pivot kernel (see grid_barrier).
 struct GridBar {
     unsigned count, gen, abort, pad;
-};
-
-struct PivotReport {  // one CTA's first non-zero residual in a pivot step
-    unsigned long long rank, w;
 };
 
 // ---------------------------------------------------------------------------
@@ -299,15 +294,13 @@ __global__ void cycle_vector_kernel(uint64_t *C, int W, const int64_t *__restric
 // One warp per word column; also resets the block state (runs first in the block).
 __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int e0, int b, int Wb,
                                      uint64_t *__restrict__ T, BlockState *bs, long long ntiles,
-                                     GridBar *gb, unsigned long long *gmin, long long window_tiles) {
+                                     GridBar *gb, long long window_tiles) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         gb->count = 0;
         gb->abort = 0;
-        gmin[0] = kNone;
         bs->rank = 0;
         bs->epoch = bs->epoch + 1;
         bs->b = (unsigned)b;
-        bs->npairs = 0;
         // stream 25% past the previous block's deepest pivot; the pivot kernel
         // computes any further tile it needs
         long long pred = ntiles;
@@ -792,7 +785,6 @@ __device__ bool resolve_block(BlockState *bs, int rank, const int64_t *__restric
             const unsigned carry = s_pre[32];
             for (int i = 33; i <= 64; i++) s_pre[i] += carry;
             const unsigned total = s_pre[64];
-            bs->npairs = total < pair_cap ? total : pair_cap;
             if (total > pair_cap) atomicOr(status, ST_BAD_INPUT);
         }
         helpers_sync(nh);
@@ -849,7 +841,6 @@ __device__ bool resolve_block(BlockState *bs, int rank, const int64_t *__restric
     // selections, and the iteration of every sorted pair in place of its pivot
     if (tid < b) {
         ta.selected[e0 + tid] = s_r[s_sel[tid]];
-        bs->sel[tid] = s_sel[tid];
     }
     const unsigned total = s_pre[64] < pair_cap ? s_pre[64] : pair_cap;
     for (unsigned i = tid; i < total; i += blockDim.x) {
@@ -925,7 +916,7 @@ __device__ long long g_scan_prof[4];
 __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
     long long K, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
     const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T, int bound, BlockState *bs,
-    uint64_t *Warr, unsigned *tile_epoch, PivotReport *reports, GridBar *gb, unsigned *status,
+    uint64_t *Warr, unsigned *tile_epoch, unsigned long long *reports, GridBar *gb, unsigned *status,
     unsigned long long *bytes, unsigned long long *diag, unsigned long long *dbg, TailArgs ta) {
     // dynamic shared memory: global tables | local tables | window W's | merge buffers | report staging
     extern __shared__ __align__(128) unsigned char dsm[];
@@ -970,7 +961,7 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
     cta_sync();
     while (grank < b) {
         unsigned long long *rep_rank =
-            reinterpret_cast<unsigned long long *>(reports) + (size_t)(k & 1) * G * (2 * kLmax + 2);
+            reports + (size_t)(k & 1) * G * (2 * kLmax + 2);
         unsigned long long *rep_w = rep_rank + (size_t)G * kLmax;
         unsigned long long *rep_end = rep_w + (size_t)G * kLmax;
         unsigned long long *rep_n = rep_end + G;
@@ -1469,8 +1460,7 @@ struct mcbgpu_solver {
     uint64_t *d_Warr = nullptr;    // W per candidate (tiles * 1024)
     unsigned *d_tile_epoch = nullptr;
     int32_t *d_tile_minc = nullptr;
-    unsigned long long *d_gmin = nullptr;  // 3 slots
-    PivotReport *d_reports = nullptr;      // 2 x pivot_grid
+    unsigned long long *d_reports = nullptr;  // two step parities of G x (2 kLmax + 2) words
     GridBar *d_gbar = nullptr;
     int pivot_grid = 0;
     unsigned *d_pairs = nullptr;     // 3 x pair_cap: resolve scratch, sorted pairs of the two block parities
@@ -1550,7 +1540,6 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_Warr);
     cudaFree(s->d_tile_epoch);
     cudaFree(s->d_tile_minc);
-    cudaFree(s->d_gmin);
     cudaFree(s->d_reports);
     cudaFree(s->d_gbar);
     cudaFree(s->d_pairs);
@@ -1630,7 +1619,6 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_Warr, sizeof(uint64_t) * (size_t)kTile * ntiles);
     ALLOC(s->d_tile_epoch, sizeof(unsigned) * ntiles);
     ALLOC(s->d_tile_minc, sizeof(int32_t) * ntiles);
-    ALLOC(s->d_gmin, sizeof(unsigned long long) * 4);
     ALLOC(s->d_gbar, sizeof(GridBar));
     ALLOC(s->d_word_end, sizeof(unsigned) * 2 * ((size_t)s->P + 1));
     ALLOC(s->d_slots, sizeof(IterSlot) * 2);
@@ -1881,7 +1869,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         {
             Launch L(s, KC_TRANSPOSE, st);
             blk_transpose_kernel<<<(Wb + 7) / 8, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles,
-                                                              s->d_gbar, s->d_gmin,
+                                                              s->d_gbar,
                                                               (long long)s->pivot_grid * kWinTiles);
         }
         if (ntiles > 0) {
@@ -1901,7 +1889,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             unsigned *te = s->d_tile_epoch;
             GridBar *gb = s->d_gbar;
             unsigned *stt = s->d_status;
-            PivotReport *rp = s->d_reports;
+            unsigned long long *rp = s->d_reports;
             unsigned long long *nb = L.bytes();
             unsigned long long *dg = s->d_diag;
             unsigned long long *db = s->d_diag + 32;
