@@ -68,6 +68,15 @@ constexpr unsigned kSpinLimit = 1u << 24;
 #ifndef MCB_EARLY_RANK
 #define MCB_EARLY_RANK 48
 #endif
+#ifndef MCB_TAIL_WIN
+#define MCB_TAIL_WIN 8  // window once the rank is at least MCB_TAIL_RANK
+#endif
+#ifndef MCB_TAIL_RANK
+#define MCB_TAIL_RANK 60
+#endif
+#ifndef MCB_MERGE_FAST
+#define MCB_MERGE_FAST 1  // merge: skip the sort and echelon when no report lies below D
+#endif
 constexpr int kLmax = MCB_LMAX;           // local pivots a CTA reports per pivot step
 constexpr int kWinTiles = MCB_WIN_TILES;  // tiles a CTA scans per pivot step (<= 32)
 constexpr int kUpdRows = MCB_UPD_ROWS;    // rows per warp group in the block update (<= 32)
@@ -558,7 +567,8 @@ __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, c
 // the next call that writes the same slots.
 constexpr int kPivotThreads = 512;        // threads of a pivot-kernel CTA
 constexpr int kWarps = kPivotThreads / 32;
-constexpr int kWinW = kWinTiles * kTile;  // W's in a CTA's window
+constexpr int kWinMax = MCB_TAIL_WIN > kWinTiles ? MCB_TAIL_WIN : kWinTiles;  // largest window
+constexpr int kWinW = kWinMax * kTile;  // W's the window buffer holds
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
     for (int d = 16; d > 0; d >>= 1) {
@@ -931,7 +941,7 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
     __shared__ unsigned gpiv[64], lpiv[64];
     __shared__ unsigned s_first[kWarps], s_wcnt[kWarps];
     __shared__ unsigned long long s_chg[kWarps], s_dmin[kWarps];
-    __shared__ unsigned s_tag[kWinTiles];
+    __shared__ unsigned s_tag[kWinMax];
     __shared__ __align__(8) uint64_t s_bar;  // completion of the window's bulk copies
     __shared__ uint64_t s_newv[64];
     __shared__ unsigned s_newq[64];
@@ -989,7 +999,9 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
     do {              \
     } while (0)
 #endif
-        const int wsz = grank < MCB_EARLY_RANK ? MCB_EARLY_WIN : kWinTiles;  // same in every CTA
+        const int wsz = grank < MCB_EARLY_RANK ? MCB_EARLY_WIN
+                        : grank >= MCB_TAIL_RANK ? MCB_TAIL_WIN
+                                                 : kWinTiles;  // same in every CTA
         const int nwin = tf >= ntiles ? 0 : (int)min((long long)wsz, (ntiles - 1 - tf) / G + 1);
         if (threadIdx.x < (unsigned)nwin) s_tag[threadIdx.x] = ld_acquire_u32(&tile_epoch[tf + (long long)threadIdx.x * G]);
         cta_sync();
@@ -1198,63 +1210,66 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
         }
         if (cnt > G * kLmax) cnt = G * kLmax;
         n_cand += cnt;
-        // rank order: each candidate's position = number of smaller ranks (ranks are distinct)
-        unsigned long long *sr = mr + cnt;  // sorted ranks
-        uint64_t *sz = mw + cnt;            // sorted residuals against the global basis
-        uint64_t *sw = sz + cnt;            // sorted W
-        for (unsigned i = threadIdx.x; i < cnt; i += blockDim.x) {
-            const unsigned long long r = mr[i];
-            unsigned pos = 0;
-            for (unsigned j = 0; j < cnt; j++) pos += mr[j] < r;
-            sr[pos] = r;
-            sw[pos] = mw[i];
-            sz[pos] = fr_reduce(mw[i], gtab);
-        }
-        cta_sync();
-        // greedy echelon in rank order (warp 0): a candidate is a new global pivot iff
-        // its residual is not in the span of the new pivots before it; then the new
-        // vectors are brought to reduced form among themselves, latest first (lane l
-        // holds vectors l and l + 32)
-        if (threadIdx.x < 32) {
-            int nn = 0;
-            for (unsigned base = 0; base < cnt && grank + nn < b; base += 32) {
-                uint64_t z = base + lane < cnt ? sz[base + lane] : 0ull;
-                for (int j = 0; j < nn; j++)
-                    if ((z >> s_newq[j]) & 1ull) z ^= s_newv[j];
-                for (;;) {
-                    const unsigned bal = __ballot_sync(0xffffffffu, z != 0);
-                    if (!bal || grank + nn >= b) break;
-                    const int pl = __ffs(bal) - 1;
-                    const uint64_t v = __shfl_sync(0xffffffffu, z, pl);
-                    const unsigned qb = (unsigned)(__ffsll((long long)v) - 1);
-                    if (lane == 0) {
-                        s_newv[nn] = v;
-                        s_newq[nn] = qb;
-                        if (c == 0) {
-                            bs->pivrank[grank + nn] = (long long)sr[base + pl];
-                            bs->pivW[grank + nn] = sw[base + pl];
+        int nnew = 0;
+        if (!MCB_MERGE_FAST || cnt > 0) {  // no report below D: no new pivot (uniform)
+            // rank order: each candidate's position = number of smaller ranks (ranks are distinct)
+            unsigned long long *sr = mr + cnt;  // sorted ranks
+            uint64_t *sz = mw + cnt;            // sorted residuals against the global basis
+            uint64_t *sw = sz + cnt;            // sorted W
+            for (unsigned i = threadIdx.x; i < cnt; i += blockDim.x) {
+                const unsigned long long r = mr[i];
+                unsigned pos = 0;
+                for (unsigned j = 0; j < cnt; j++) pos += mr[j] < r;
+                sr[pos] = r;
+                sw[pos] = mw[i];
+                sz[pos] = fr_reduce(mw[i], gtab);
+            }
+            cta_sync();
+            // greedy echelon in rank order (warp 0): a candidate is a new global pivot iff
+            // its residual is not in the span of the new pivots before it; then the new
+            // vectors are brought to reduced form among themselves, latest first (lane l
+            // holds vectors l and l + 32)
+            if (threadIdx.x < 32) {
+                int nn = 0;
+                for (unsigned base = 0; base < cnt && grank + nn < b; base += 32) {
+                    uint64_t z = base + lane < cnt ? sz[base + lane] : 0ull;
+                    for (int j = 0; j < nn; j++)
+                        if ((z >> s_newq[j]) & 1ull) z ^= s_newv[j];
+                    for (;;) {
+                        const unsigned bal = __ballot_sync(0xffffffffu, z != 0);
+                        if (!bal || grank + nn >= b) break;
+                        const int pl = __ffs(bal) - 1;
+                        const uint64_t v = __shfl_sync(0xffffffffu, z, pl);
+                        const unsigned qb = (unsigned)(__ffsll((long long)v) - 1);
+                        if (lane == 0) {
+                            s_newv[nn] = v;
+                            s_newq[nn] = qb;
+                            if (c == 0) {
+                                bs->pivrank[grank + nn] = (long long)sr[base + pl];
+                                bs->pivW[grank + nn] = sw[base + pl];
+                            }
                         }
+                        nn++;
+                        if ((z >> qb) & 1ull) z ^= v;
                     }
-                    nn++;
-                    if ((z >> qb) & 1ull) z ^= v;
+                    __syncwarp();
+                }
+                uint64_t va = lane < (unsigned)nn ? s_newv[lane] : 0ull;
+                uint64_t vb = lane + 32 < (unsigned)nn ? s_newv[lane + 32] : 0ull;
+                for (int j = nn - 1; j >= 1; j--) {
+                    const uint64_t vj = __shfl_sync(0xffffffffu, j < 32 ? va : vb, j & 31);
+                    const unsigned qj = s_newq[j];
+                    if ((int)lane < j && ((va >> qj) & 1ull)) va ^= vj;
+                    if ((int)lane + 32 < j && ((vb >> qj) & 1ull)) vb ^= vj;
                 }
                 __syncwarp();
+                if (lane < (unsigned)nn) s_newv[lane] = va;
+                if (lane + 32 < (unsigned)nn) s_newv[lane + 32] = vb;
+                if (lane == 0) s_nnew = nn;
             }
-            uint64_t va = lane < (unsigned)nn ? s_newv[lane] : 0ull;
-            uint64_t vb = lane + 32 < (unsigned)nn ? s_newv[lane + 32] : 0ull;
-            for (int j = nn - 1; j >= 1; j--) {
-                const uint64_t vj = __shfl_sync(0xffffffffu, j < 32 ? va : vb, j & 31);
-                const unsigned qj = s_newq[j];
-                if ((int)lane < j && ((va >> qj) & 1ull)) va ^= vj;
-                if ((int)lane + 32 < j && ((vb >> qj) & 1ull)) vb ^= vj;
-            }
-            __syncwarp();
-            if (lane < (unsigned)nn) s_newv[lane] = va;
-            if (lane + 32 < (unsigned)nn) s_newv[lane + 32] = vb;
-            if (lane == 0) s_nnew = nn;
+            cta_sync();
+            nnew = s_nnew;
         }
-        cta_sync();
-        const int nnew = s_nnew;
         if (nnew > 0) {
             // clear the new pivot bits from the old basis vectors, append, rebuild tables
             if (threadIdx.x < (unsigned)grank) {
