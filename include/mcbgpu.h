@@ -197,6 +197,43 @@ int mcbgpu_solver_destroy(mcbgpu_solver *s);
 int mcbgpu_solve(int32_t num_coords, int64_t num_candidates, const int32_t *weight, const int64_t *offsets,
                  const int32_t *coords, int64_t *selected, int64_t *total_weight);
 
+/* ---- 4. batched main loop ---------------------------------------------------
+ * Many independent problems (the biconnected components of one graph, or many
+ * graphs) in one persistent launch per size class, one CTA per problem at a time.
+ * Replaces the reference's one-process-per-component loop (main.sh:19-32 runs the
+ * whole mcb driver once per bicc component file); every problem's result equals
+ * mcbgpu_solver_run's on the same inputs.
+ *
+ * create: count problems, problem i with num_coords[i] = N_i (at most
+ *   mcbgpu_batch_max_coords()) and num_candidates[i] = K_i; nnz = total coordinates.
+ * upload: the problems' candidates back to back in problem order: weight[sum K],
+ *   offsets[sum K + 1] (int64, one running sequence from 0 to nnz), coords[nnz]
+ *   (each list ascending in [0, N_i) of its problem).
+ * run: enqueued on `stream` without host synchronisation.
+ * results: selected[sum N] (problem i's iterations at offset N_0 + ... + N_{i-1},
+ *   each the candidate's rank within problem i), total_weight[count] (-1 for a
+ *   problem that failed), problem_status[count] (0 = solved; may be NULL); returns
+ *   MCBGPU_E_ARG if some problem's lists were malformed, MCBGPU_E_NO_CANDIDATE if
+ *   some problem's candidates do not span its cycle space. */
+typedef struct mcbgpu_batch mcbgpu_batch;
+int mcbgpu_batch_max_coords(void);
+int mcbgpu_batch_create(mcbgpu_batch **out, int32_t count, const int32_t *num_coords,
+                        const int64_t *num_candidates, int64_t nnz);
+int mcbgpu_batch_upload(mcbgpu_batch *b, const int32_t *weight, const int64_t *offsets, const int32_t *coords,
+                        void *stream);
+int mcbgpu_batch_run(mcbgpu_batch *b, void *stream);
+int mcbgpu_batch_results(mcbgpu_batch *b, int64_t *selected, int64_t *total_weight, uint32_t *problem_status,
+                         void *stream);
+/* S_j of problem `problem` after the run (ceil(N/64) words, synchronous). */
+int mcbgpu_batch_get_support(mcbgpu_batch *b, int32_t problem, int32_t j, uint64_t *words, void *stream);
+int64_t mcbgpu_batch_launches(const mcbgpu_batch *b);
+int64_t mcbgpu_batch_device_bytes(const mcbgpu_batch *b);
+int mcbgpu_batch_destroy(mcbgpu_batch *b);
+/* One-shot: create, upload, run, results, destroy. */
+int mcbgpu_batch_solve(int32_t count, const int32_t *num_coords, const int64_t *num_candidates,
+                       const int32_t *weight, const int64_t *offsets, const int32_t *coords, int64_t *selected,
+                       int64_t *total_weight);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,6 +95,16 @@ GPU_SYMBOLS = {
     "mcbgpu_solver_device_bytes": (i64, [vp]),
     "mcbgpu_solver_destroy": (C.c_int, [vp]),
     "mcbgpu_solve": (C.c_int, [i32, i64, vp, vp, vp, vp, C.POINTER(i64)]),
+    "mcbgpu_batch_max_coords": (C.c_int, []),
+    "mcbgpu_batch_create": (C.c_int, [C.POINTER(vp), i32, vp, vp, i64]),
+    "mcbgpu_batch_upload": (C.c_int, [vp, vp, vp, vp, vp]),
+    "mcbgpu_batch_run": (C.c_int, [vp, vp]),
+    "mcbgpu_batch_results": (C.c_int, [vp, vp, vp, vp, vp]),
+    "mcbgpu_batch_get_support": (C.c_int, [vp, i32, i32, vp, vp]),
+    "mcbgpu_batch_launches": (i64, [vp]),
+    "mcbgpu_batch_device_bytes": (i64, [vp]),
+    "mcbgpu_batch_destroy": (C.c_int, [vp]),
+    "mcbgpu_batch_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
 }
 
 

@@ -1,0 +1,683 @@
+// Batched de Pina solver: many independent problems (the biconnected components of
+// one graph, or many graphs) solved in one persistent launch per size class.
+//
+// The reference solves one graph per process and, for a graph split into
+// biconnected components, runs the whole driver once per component file
+// (main.sh:19-32 loops `run.sh` over bicc's output).  Here every problem is a
+// (N, candidates, coordinate lists) triple as mcbgpu_solver takes it; one CTA owns
+// one problem at a time and pulls the next from a device work counter (problems
+// in order of decreasing N, so the longest start first).
+//
+// Per problem the CTA runs the blocked loop of mcbgpu_solver_run (64 iterations per
+// block) with everything block-local in shared memory:
+//   1. T[c] = bits i of S_{e0+i}[c] for the block's rows (64x64 bit transposes of
+//      the rows' words by warp ballots; unit bits for c in [e0, bound));
+//   2. the rank-ordered scan: W_r = XOR of T over C_r's coordinates below the
+//      bound; the first b candidates whose W is independent of the earlier ones'
+//      (a reduced row echelon basis keyed by lead bit) are the pivots;
+//   3. resolve: the reference's loop restricted to the block on 64-bit masks
+//      (iteration k takes the first pivot with parity(W_p & m_k) = 1, later masks
+//      with odd parity absorb m_k), which selects the reference's candidate for
+//      every iteration (mcb/mcb_cycle_deg_two_remove.cpp:329-358);
+//   4. the block's final rows S_{e0+k} = XOR_{l in m_k} S^0_{e0+l}, computed from T;
+//   5. every later row j: D_j[k] = <C_sel_k, S_j>, beta = the sequential effect of
+//      the 64 updates (a 64x64 GF(2) matrix applied to D), S_j ^= XOR_{k in beta}
+//      S_{e0+k} (mcb/mcb_cycle_deg_two_remove.cpp:371-390 for 64 iterations).
+// There is no inter-CTA synchronisation: the only shared word is the work counter.
+#include <algorithm>
+#include <vector>
+
+#include "mcbgpu_internal.cuh"
+
+using namespace mcbgpu;
+
+namespace {
+
+constexpr int kBThreads = 512;
+constexpr int kBWarps = kBThreads / 32;
+constexpr int kBChunk = 8;               // coordinates loaded together in a W walk
+constexpr int kBatchMaxN = 12288;        // largest N a CTA holds (T and the final rows in shared memory)
+constexpr unsigned kPairSmem = 4096;     // pairs kept in shared memory (more go to the CTA's global scratch)
+constexpr int kClasses = 3;
+constexpr int kClassMaxN[kClasses] = {1024, 4096, kBatchMaxN};
+
+struct BatchGraph {
+    long long cand;  // first candidate (index into weight / offsets)
+    long long K;     // candidates
+    long long srow;  // first word of the problem's support vectors (N rows of P words)
+    long long sel;   // first entry of the problem in `selected`
+    int N, P;
+};
+
+__device__ __forceinline__ int ffs64(uint64_t x) { return __ffsll((long long)x) - 1; }
+
+__device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int d) {
+    const unsigned lo = __shfl_xor_sync(0xffffffffu, (unsigned)v, d);
+    const unsigned hi = __shfl_xor_sync(0xffffffffu, (unsigned)(v >> 32), d);
+    return ((uint64_t)hi << 32) | lo;
+}
+
+// W of one candidate from the block's T in shared memory.
+__device__ __forceinline__ uint64_t w_smem(long long r, const int64_t *__restrict__ off,
+                                           const int32_t *__restrict__ coords, const uint64_t *T, int bound) {
+    long long i = __ldg(off + r);
+    const long long e = __ldg(off + r + 1);
+    uint64_t W = 0;
+    while (i < e) {
+        int cv[kBChunk];
+#pragma unroll
+        for (int q = 0; q < kBChunk; q++) cv[q] = i + q < e ? __ldg(coords + i + q) : 0x7fffffff;
+#pragma unroll
+        for (int q = 0; q < kBChunk; q++)
+            if (cv[q] < bound) W ^= T[cv[q]];
+        if (cv[kBChunk - 1] >= bound) break;
+        i += kBChunk;
+    }
+    return W;
+}
+
+__global__ void __launch_bounds__(kBThreads) batch_solve_kernel(
+    const BatchGraph *__restrict__ graphs, const int *__restrict__ order, int count, unsigned *next,
+    const int32_t *__restrict__ weight, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
+    uint64_t *S, long long *selected, long long *total, unsigned *gstatus, unsigned *status, unsigned *pair_scratch,
+    unsigned pair_cap, int ncap) {
+    extern __shared__ __align__(16) uint64_t smem[];
+    const int wcap = (ncap + 63) >> 6;
+    uint64_t *T = smem;                                    // ncap words
+    uint64_t *F = smem + ncap;                             // 64 x (wcap + 1) words: the block's final rows
+    unsigned *sPairs = (unsigned *)(F + 64 * (wcap + 1));  // kPairSmem
+    unsigned *gPairs = pair_scratch + (size_t)blockIdx.x * pair_cap;
+
+    __shared__ uint64_t sB[64];     // reduced echelon basis, by lead bit
+    __shared__ uint64_t sPivW[64];  // W of the pivots, in rank order
+    __shared__ int sPivR[64];       // their ranks
+    __shared__ uint64_t sMask[64];  // final masks m_k
+    __shared__ uint64_t sGcol[64];  // bit i of gcol[k] = <C_sel_k, S_{e0+i}> (i < k)
+    __shared__ uint64_t sMrow[64];  // beta of a row = XOR of sMrow[k] over the k with D bit k
+    __shared__ int sSel[64];        // rank selected at iteration e0 + k
+    __shared__ unsigned sPre[65];   // pair offsets of the selected lists
+    __shared__ int sWmin[kBWarps];
+    __shared__ uint64_t sNewRes, sNewW;
+    __shared__ int sGi;
+    __shared__ unsigned sFail;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned full = 0xffffffffu;
+
+    for (;;) {
+        if (tid == 0) sGi = (int)atomicAdd(next, 1u);
+        cta_sync();
+        const int gi = sGi;
+        if (gi >= count) break;
+        const int gx = order[gi];
+        const BatchGraph g = graphs[gx];
+        const int N = g.N, P = g.P;
+        const long long K = g.K, cand = g.cand;
+        uint64_t *Sg = S + g.srow;
+
+        // the problem's coordinate lists: ascending, in [0, N); lengths fit the pair scratch
+        bool ok = N <= ncap;
+        for (long long r = tid; ok && r < K; r += kBThreads) {
+            const long long a = off[cand + r], e = off[cand + r + 1];
+            if (e - a > (long long)(pair_cap / 64)) ok = false;
+            int prev = -1;
+            for (long long i = a; ok && i < e; i++) {
+                const int c = coords[i];
+                if (c <= prev || c >= N) ok = false;
+                prev = c;
+            }
+        }
+        if (!cta_sync_and(ok)) {
+            if (tid == 0) {
+                gstatus[gx] |= ST_BAD_INPUT;
+                atomicOr(status, ST_BAD_INPUT);
+            }
+            continue;  // the loop head's barrier separates the problems
+        }
+        // S_j = e_j; only words [0, j/64] of row j are ever read or written
+        for (int j = warp; j < N; j += kBWarps) {
+            uint64_t *row = Sg + (size_t)j * P;
+            for (int w = lane; w <= (j >> 6); w += 32) row[w] = w == (j >> 6) ? 1ull << (j & 63) : 0ull;
+        }
+        long long tot = 0;
+        if (tid == 0) sFail = 0;
+        cta_sync();
+
+        for (int e0 = 0; e0 < N; e0 += 64) {
+            const int b = min(64, N - e0), bound = e0 + b, wl = e0 >> 6, Wb = wl + 1;
+            // ---- 1. T
+            for (int c = e0 + tid; c < bound; c += kBThreads) T[c] = 1ull << (c - e0);
+            for (int w = warp; w < wl; w += kBWarps) {
+                const uint64_t *r0 = Sg + (size_t)(e0 + lane) * P + w;
+                const uint64_t x0 = lane < b ? r0[0] : 0ull;
+                const uint64_t x1 = lane + 32 < b ? r0[(size_t)32 * P] : 0ull;
+                uint64_t v0 = 0, v1 = 0;
+#pragma unroll 8
+                for (int t = 0; t < 32; t++) {
+                    const unsigned lo = __ballot_sync(full, (x0 >> t) & 1), hi = __ballot_sync(full, (x1 >> t) & 1);
+                    if (lane == t) v0 = ((uint64_t)hi << 32) | lo;
+                }
+#pragma unroll 8
+                for (int t = 0; t < 32; t++) {
+                    const unsigned lo = __ballot_sync(full, (x0 >> (t + 32)) & 1),
+                                   hi = __ballot_sync(full, (x1 >> (t + 32)) & 1);
+                    if (lane == t) v1 = ((uint64_t)hi << 32) | lo;
+                }
+                T[(w << 6) + lane] = v0;
+                T[(w << 6) + 32 + lane] = v1;
+            }
+            cta_sync();
+
+            // ---- 2. pivots: the first b rank-ordered candidates with independent W
+            int npiv = 0;
+            uint64_t lead = 0;
+            for (long long base = 0; npiv < b; base += kBThreads) {
+                if (base >= K) {  // fewer than b independent candidates
+                    if (tid == 0) sFail = 1;
+                    break;
+                }
+                const long long r = base + tid;
+                const uint64_t W = r < K ? w_smem(cand + r, off, coords, T, bound) : 0ull;
+                uint64_t res = W;
+                for (uint64_t m = W & lead; m; m &= m - 1) res ^= sB[ffs64(m)];
+                for (;;) {
+                    const unsigned bal = __ballot_sync(full, res != 0);
+                    if (lane == 0) sWmin[warp] = bal ? warp * 32 + __ffs(bal) - 1 : 0x7fffffff;
+                    cta_sync();
+                    int best = 0x7fffffff;
+#pragma unroll
+                    for (int q = 0; q < kBWarps; q++) best = min(best, sWmin[q]);
+                    if (best == 0x7fffffff) break;
+                    if (tid == best) {
+                        sNewRes = res;
+                        sNewW = W;
+                    }
+                    cta_sync();
+                    const uint64_t nr = sNewRes;
+                    const int L = ffs64(nr);
+                    if (warp == 0) {  // keep the basis reduced: clear bit L from the older vectors
+                        if (((lead >> lane) & 1) && ((sB[lane] >> L) & 1)) sB[lane] ^= nr;
+                        if (((lead >> (lane + 32)) & 1) && ((sB[lane + 32] >> L) & 1)) sB[lane + 32] ^= nr;
+                        if (lane == 0) {
+                            sB[L] = nr;
+                            sPivW[npiv] = sNewW;
+                            sPivR[npiv] = (int)(base + best);
+                        }
+                    }
+                    lead |= 1ull << L;
+                    npiv++;
+                    if (tid == best)
+                        res = 0;
+                    else if ((res >> L) & 1)
+                        res ^= nr;
+                    if (npiv == b) break;
+                }
+                cta_sync();
+            }
+            cta_sync();
+            if (sFail) break;
+
+            // ---- 3. resolve (warp 0), gcol, the beta matrix, selected ranks, pair offsets
+            if (warp == 0) {
+                const uint64_t W0 = lane < b ? sPivW[lane] : 0ull, W1 = lane + 32 < b ? sPivW[lane + 32] : 0ull;
+                uint64_t m0 = lane < b ? 1ull << lane : 0ull, m1 = lane + 32 < b ? 1ull << (lane + 32) : 0ull;
+                int p0 = 0, p1 = 0;  // pivot of iteration lane / lane + 32
+                bool bad = false;
+                for (int k = 0; k < b; k++) {
+                    const uint64_t mk = __shfl_sync(full, k < 32 ? m0 : m1, k & 31);
+                    const unsigned o0 = __ballot_sync(full, parity64(W0 & mk));
+                    const unsigned o1 = __ballot_sync(full, parity64(W1 & mk));
+                    const int p = o0 ? __ffs(o0) - 1 : (o1 ? 31 + __ffs(o1) : -1);
+                    if (p < 0) {  // cannot happen for independent pivots; guards the indexing
+                        bad = true;
+                        break;
+                    }
+                    const uint64_t Wp = __shfl_sync(full, p < 32 ? W0 : W1, p & 31);
+                    if (lane == (k & 31)) {
+                        if (k < 32)
+                            p0 = p;
+                        else
+                            p1 = p;
+                    }
+                    if (lane > k && parity64(Wp & m0)) m0 ^= mk;
+                    if (lane + 32 > k && parity64(Wp & m1)) m1 ^= mk;
+                }
+                sMask[lane] = m0;
+                sMask[lane + 32] = m1;
+                if (bad) {
+                    if (lane == 0) sFail = 1;
+                } else {
+                    __syncwarp();
+                    // gcol[k] bit i = parity(W_{p_k} & m_i), i < k
+                    for (int h = 0; h < 2; h++) {
+                        const int k = lane + 32 * h;
+                        uint64_t gc = 0;
+                        if (k < b) {
+                            const uint64_t Wk = sPivW[h ? p1 : p0];
+                            for (int i = 0; i < k; i++) gc |= (uint64_t)parity64(Wk & sMask[i]) << i;
+                            sSel[k] = sPivR[h ? p1 : p0];
+                        }
+                        sGcol[k] = gc;
+                    }
+                    __syncwarp();
+                    // beta for D = e_k: beta_i = 0 (i < k), 1 (i = k), parity(beta & gcol[i]) (i > k)
+                    for (int h = 0; h < 2; h++) {
+                        const int k = lane + 32 * h;
+                        uint64_t bt = 0;
+                        if (k < b) {
+                            bt = 1ull << k;
+                            for (int i = k + 1; i < b; i++) bt |= (uint64_t)parity64(bt & sGcol[i]) << i;
+                        }
+                        sMrow[k] = bt;
+                    }
+                    // pair offsets of the selected lists
+                    long long l0 = 0, l1 = 0;
+                    if (lane < b) l0 = off[cand + sSel[lane] + 1] - off[cand + sSel[lane]];
+                    if (lane + 32 < b) l1 = off[cand + sSel[lane + 32] + 1] - off[cand + sSel[lane + 32]];
+                    unsigned s0 = (unsigned)l0, s1 = (unsigned)l1;
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const unsigned a0 = __shfl_up_sync(full, s0, d), a1 = __shfl_up_sync(full, s1, d);
+                        if (lane >= d) {
+                            s0 += a0;
+                            s1 += a1;
+                        }
+                    }
+                    const unsigned t0 = __shfl_sync(full, s0, 31);
+                    sPre[lane + 1] = s0;
+                    sPre[lane + 33] = t0 + s1;
+                    if (lane == 0) sPre[0] = 0;
+                    if (lane == 0)
+                        for (int k = 0; k < b; k++) tot += weight[cand + sSel[k]];
+                }
+            }
+            cta_sync();
+            if (sFail) break;
+            const unsigned np = sPre[b];
+            unsigned *pairs = np <= kPairSmem ? sPairs : gPairs;
+
+            // ---- 4. final rows of the block (shared F and global S), 5. pairs
+            for (int item = warp; item < b * wl; item += kBWarps) {
+                const int k = item / wl, w = item - k * wl;
+                const uint64_t mk = sMask[k];
+                const unsigned lo = __ballot_sync(full, parity64(T[(w << 6) + lane] & mk));
+                const unsigned hi = __ballot_sync(full, parity64(T[(w << 6) + 32 + lane] & mk));
+                if (lane == 0) {
+                    const uint64_t v = ((uint64_t)hi << 32) | lo;
+                    F[k * Wb + w] = v;
+                    Sg[(size_t)(e0 + k) * P + w] = v;
+                }
+            }
+            for (int k = tid; k < b; k += kBThreads) {
+                F[k * Wb + wl] = sMask[k];
+                Sg[(size_t)(e0 + k) * P + wl] = sMask[k];
+            }
+            for (int k = warp; k < b; k += kBWarps) {
+                const long long a = off[cand + sSel[k]], e = off[cand + sSel[k] + 1];
+                const unsigned o = sPre[k];
+                for (long long i = a + lane; i < e; i += 32)
+                    pairs[o + (unsigned)(i - a)] = ((unsigned)coords[i] << 6) | (unsigned)k;
+            }
+            cta_sync();
+
+            // ---- 6. later rows: one warp per row
+            for (int j = bound + warp; j < N; j += kBWarps) {
+                uint64_t *Sj = Sg + (size_t)j * P;
+                uint64_t acc = 0;
+                for (unsigned i = lane; i < np; i += 32) {
+                    const unsigned pr = pairs[i];
+                    const int c = (int)(pr >> 6);
+                    const bool bit = c < e0 ? ((Sj[c >> 6] >> (c & 63)) & 1) : c == j;
+                    if (bit) acc ^= sMrow[pr & 63];
+                }
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) acc ^= shfl_xor64(acc, d);
+                if (!acc) continue;
+                for (int w = lane; w < Wb; w += 32) {
+                    uint64_t x = 0;
+                    for (uint64_t bb = acc; bb; bb &= bb - 1) x ^= F[ffs64(bb) * Wb + w];
+                    Sj[w] ^= x;
+                }
+            }
+            if (tid == 0)
+                for (int k = 0; k < b; k++) selected[g.sel + e0 + k] = sSel[k];
+            cta_sync();
+        }
+        if (tid == 0) {
+            if (sFail) {
+                gstatus[gx] |= ST_RANK_DEFICIT;
+                atomicOr(status, ST_RANK_DEFICIT);
+            }
+        }
+        if (warp == 0) {
+            // tot lives in lane 0 of warp 0
+            if (lane == 0) total[gx] = sFail ? -1 : tot;
+        }
+    }
+}
+
+}  // namespace
+
+struct mcbgpu_batch {
+    int count = 0;
+    int sm_count = 0;
+    long long total_K = 0, nnz = 0, total_N = 0, s_words = 0;
+    unsigned pair_cap = 0;   // pair scratch words per CTA (64 x the longest list)
+    int pair_slabs = 0;      // CTA slabs per class
+    std::vector<BatchGraph> graphs;
+    std::vector<int> order;            // problems grouped by class, by decreasing N within a class
+    int class_off[kClasses + 1] = {};  // class c holds order[class_off[c], class_off[c + 1])
+    int class_ncap[kClasses] = {};     // largest N of the class (rounded up to 64)
+    int class_grid[kClasses] = {};
+    BatchGraph *d_graphs = nullptr;
+    int *d_order = nullptr;
+    unsigned *d_next = nullptr;  // one work counter per class
+    int32_t *d_weight = nullptr;
+    int64_t *d_off = nullptr;
+    int32_t *d_coords = nullptr;
+    uint64_t *d_S = nullptr;
+    long long *d_selected = nullptr;
+    long long *d_total = nullptr;
+    unsigned *d_gstatus = nullptr;
+    unsigned *d_status = nullptr;
+    unsigned *d_pairs = nullptr;
+    cudaStream_t st[kClasses] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[kClasses] = {};
+    bool uploaded = false;
+    long long launches = 0;
+    long long device_bytes = 0;
+};
+
+namespace {
+
+size_t batch_smem_bytes(int ncap) {
+    const size_t wcap = (size_t)(ncap + 63) / 64;
+    return 8 * (size_t)ncap + 8 * 64 * (wcap + 1) + 4 * (size_t)kPairSmem;
+}
+
+void free_batch(mcbgpu_batch *b) {
+    if (!b) return;
+    cudaFree(b->d_graphs);
+    cudaFree(b->d_order);
+    cudaFree(b->d_next);
+    cudaFree(b->d_weight);
+    cudaFree(b->d_off);
+    cudaFree(b->d_coords);
+    cudaFree(b->d_S);
+    cudaFree(b->d_selected);
+    cudaFree(b->d_total);
+    cudaFree(b->d_gstatus);
+    cudaFree(b->d_status);
+    cudaFree(b->d_pairs);
+    for (int c = 0; c < kClasses; c++) {
+        if (b->st[c]) cudaStreamDestroy(b->st[c]);
+        if (b->ev_join[c]) cudaEventDestroy(b->ev_join[c]);
+    }
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    delete b;
+}
+
+int class_of(int N) {
+    int c = 0;
+    while (c < kClasses - 1 && N > kClassMaxN[c]) c++;
+    return c;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcbgpu_batch_max_coords(void) { return kBatchMaxN; }
+
+int mcbgpu_batch_create(mcbgpu_batch **out, int32_t count, const int32_t *num_coords,
+                        const int64_t *num_candidates, int64_t nnz) {
+    if (!out || count < 0 || nnz < 0 || (count > 0 && (!num_coords || !num_candidates))) {
+        set_error("mcbgpu_batch_create: invalid arguments");
+        return MCBGPU_E_ARG;
+    }
+    *out = nullptr;
+    for (int i = 0; i < count; i++) {
+        if (num_coords[i] < 0 || num_coords[i] > kBatchMaxN || num_candidates[i] < 0 ||
+            num_candidates[i] >= (1ll << 31)) {
+            set_error("mcbgpu_batch_create: problem %d has N = %d, K = %lld (the batch takes N <= %d and "
+                      "K < 2^31; solve larger problems with mcbgpu_solver)",
+                      i, (int)num_coords[i], (long long)num_candidates[i], kBatchMaxN);
+            return MCBGPU_E_ARG;
+        }
+    }
+    mcbgpu_batch *b = new mcbgpu_batch();
+    b->count = count;
+    b->nnz = nnz;
+    b->graphs.resize(count);
+    for (int i = 0; i < count; i++) {
+        BatchGraph &g = b->graphs[i];
+        g.N = num_coords[i];
+        g.P = (g.N + 63) / 64;
+        g.K = num_candidates[i];
+        g.cand = b->total_K;
+        g.sel = b->total_N;
+        g.srow = b->s_words;
+        b->total_K += g.K;
+        b->total_N += g.N;
+        b->s_words += (long long)g.N * g.P;
+    }
+    // problems with no coordinate need no work; the rest by class, each by decreasing N
+    std::vector<int> idx;
+    for (int i = 0; i < count; i++)
+        if (b->graphs[i].N > 0) idx.push_back(i);
+    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return b->graphs[x].N > b->graphs[y].N; });
+    for (int c = 0; c < kClasses; c++) {
+        b->class_off[c] = (int)b->order.size();
+        for (int i : idx)
+            if (class_of(b->graphs[i].N) == c) {
+                b->order.push_back(i);
+                b->class_ncap[c] = std::max(b->class_ncap[c], (b->graphs[i].N + 63) & ~63);
+            }
+    }
+    b->class_off[kClasses] = (int)b->order.size();
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    long long bytes = 0;
+#define ALLOC(ptr, sz)                                             \
+    do {                                                           \
+        size_t _b = (size_t)(sz);                                  \
+        if (_b < 16) _b = 16;                                      \
+        if (e == cudaSuccess) e = cudaMalloc((void **)&(ptr), _b); \
+        bytes += (long long)_b;                                    \
+    } while (0)
+    ALLOC(b->d_graphs, sizeof(BatchGraph) * (size_t)count);
+    ALLOC(b->d_order, sizeof(int) * b->order.size());
+    ALLOC(b->d_next, sizeof(unsigned) * kClasses);
+    ALLOC(b->d_weight, sizeof(int32_t) * (size_t)b->total_K);
+    ALLOC(b->d_off, sizeof(int64_t) * (size_t)(b->total_K + 1));
+    ALLOC(b->d_coords, sizeof(int32_t) * (size_t)nnz);
+    ALLOC(b->d_S, sizeof(uint64_t) * (size_t)b->s_words);
+    ALLOC(b->d_selected, sizeof(long long) * (size_t)b->total_N);
+    ALLOC(b->d_total, sizeof(long long) * (size_t)count);
+    ALLOC(b->d_gstatus, sizeof(unsigned) * (size_t)count);
+    ALLOC(b->d_status, sizeof(unsigned));
+#undef ALLOC
+    if (e == cudaSuccess && count > 0)
+        e = cudaMemcpy(b->d_graphs, b->graphs.data(), sizeof(BatchGraph) * (size_t)count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !b->order.empty())
+        e = cudaMemcpy(b->d_order, b->order.data(), sizeof(int) * b->order.size(), cudaMemcpyHostToDevice);
+    for (int c = 0; c < kClasses && e == cudaSuccess; c++) {
+        e = cudaStreamCreateWithFlags(&b->st[c], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join[c], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    // one persistent grid per class: as many CTAs as are resident at once, at most one per problem
+    // the attribute is per kernel, shared by all handles: always the largest class's need
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(batch_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)batch_smem_bytes(kBatchMaxN));
+    for (int c = 0; c < kClasses && e == cudaSuccess; c++) {
+        const int n = b->class_off[c + 1] - b->class_off[c];
+        if (n == 0) continue;
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_solve_kernel, kBThreads,
+                                                          batch_smem_bytes(b->class_ncap[c]));
+        if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
+        b->class_grid[c] = (int)std::min<long long>(n, (long long)per_sm * std::max(b->sm_count, 1));
+    }
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return cuda_fail(e, "mcbgpu_batch_create");
+    }
+    b->device_bytes = bytes;
+    *out = b;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_batch_upload(mcbgpu_batch *b, const int32_t *weight, const int64_t *offsets, const int32_t *coords,
+                        void *stream) {
+    if (!b || (b->total_K > 0 && (!weight || !offsets)) || (b->nnz > 0 && !coords)) {
+        set_error("mcbgpu_batch_upload: NULL argument");
+        return MCBGPU_E_ARG;
+    }
+    b->uploaded = false;
+    // offsets: non-decreasing from 0 to nnz; the longest list sizes the pair scratch
+    long long max_len = 0;
+    if (b->total_K > 0) {
+        if (offsets[0] != 0 || offsets[b->total_K] != b->nnz) {
+            set_error("mcbgpu_batch_upload: offsets must run from 0 to nnz");
+            return MCBGPU_E_ARG;
+        }
+        for (long long r = 0; r < b->total_K; r++) {
+            const long long len = offsets[r + 1] - offsets[r];
+            if (len < 0) {
+                set_error("mcbgpu_batch_upload: offsets must be non-decreasing");
+                return MCBGPU_E_ARG;
+            }
+            max_len = std::max(max_len, len);
+        }
+    }
+    if (max_len > kBatchMaxN) {  // a list has at most N distinct coordinates
+        set_error("mcbgpu_batch_upload: a coordinate list is longer than N");
+        return MCBGPU_E_ARG;
+    }
+    const unsigned cap = (unsigned)(64 * std::max<long long>(max_len, 1));
+    int slabs = 1;
+    for (int c = 0; c < kClasses; c++) slabs = std::max(slabs, b->class_grid[c]);
+    if (cap > b->pair_cap) {  // one slab per CTA of the widest class grid, for each class
+        cudaFree(b->d_pairs);
+        b->d_pairs = nullptr;
+        b->pair_cap = 0;
+        const size_t n = (size_t)cap * (size_t)slabs * kClasses;
+        MCB_CUDA(cudaMalloc((void **)&b->d_pairs, sizeof(unsigned) * n));
+        b->device_bytes += (long long)(sizeof(unsigned) * n);
+        b->pair_cap = cap;
+        b->pair_slabs = slabs;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (b->total_K > 0) {
+        MCB_CUDA(cudaMemcpyAsync(b->d_weight, weight, sizeof(int32_t) * (size_t)b->total_K, cudaMemcpyHostToDevice,
+                                 st));
+        MCB_CUDA(cudaMemcpyAsync(b->d_off, offsets, sizeof(int64_t) * (size_t)(b->total_K + 1),
+                                 cudaMemcpyHostToDevice, st));
+    }
+    if (b->nnz > 0)
+        MCB_CUDA(cudaMemcpyAsync(b->d_coords, coords, sizeof(int32_t) * (size_t)b->nnz, cudaMemcpyHostToDevice, st));
+    b->uploaded = true;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_batch_run(mcbgpu_batch *b, void *stream) {
+    if (!b || !b->uploaded) {
+        set_error("mcbgpu_batch_run: %s", b ? "upload first" : "NULL handle");
+        return b ? MCBGPU_E_STATE : MCBGPU_E_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    MCB_CUDA(cudaMemsetAsync(b->d_next, 0, sizeof(unsigned) * kClasses, st));
+    MCB_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(unsigned), st));
+    if (b->count > 0) {
+        MCB_CUDA(cudaMemsetAsync(b->d_gstatus, 0, sizeof(unsigned) * (size_t)b->count, st));
+        MCB_CUDA(cudaMemsetAsync(b->d_total, 0, sizeof(long long) * (size_t)b->count, st));
+    }
+    MCB_CUDA(cudaEventRecord(b->ev_fork, st));
+    for (int c = 0; c < kClasses; c++) {
+        const int n = b->class_off[c + 1] - b->class_off[c];
+        if (n == 0) continue;
+        MCB_CUDA(cudaStreamWaitEvent(b->st[c], b->ev_fork, 0));
+        batch_solve_kernel<<<b->class_grid[c], kBThreads, batch_smem_bytes(b->class_ncap[c]), b->st[c]>>>(
+            b->d_graphs, b->d_order + b->class_off[c], n, b->d_next + c, b->d_weight, b->d_off, b->d_coords, b->d_S,
+            b->d_selected, b->d_total, b->d_gstatus, b->d_status,
+            b->d_pairs + (size_t)c * b->pair_cap * (size_t)b->pair_slabs, b->pair_cap, b->class_ncap[c]);
+        MCB_CUDA(cudaGetLastError());
+        b->launches++;
+        MCB_CUDA(cudaEventRecord(b->ev_join[c], b->st[c]));
+        MCB_CUDA(cudaStreamWaitEvent(st, b->ev_join[c], 0));
+    }
+    return MCBGPU_OK;
+}
+
+int mcbgpu_batch_results(mcbgpu_batch *b, int64_t *selected, int64_t *total_weight, uint32_t *problem_status,
+                         void *stream) {
+    if (!b) {
+        set_error("mcbgpu_batch_results: NULL handle");
+        return MCBGPU_E_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned v = 0;
+    MCB_CUDA(cudaMemcpyAsync(&v, b->d_status, sizeof v, cudaMemcpyDeviceToHost, st));
+    if (selected && b->total_N > 0)
+        MCB_CUDA(cudaMemcpyAsync(selected, b->d_selected, sizeof(long long) * (size_t)b->total_N,
+                                 cudaMemcpyDeviceToHost, st));
+    if (total_weight && b->count > 0)
+        MCB_CUDA(cudaMemcpyAsync(total_weight, b->d_total, sizeof(long long) * (size_t)b->count,
+                                 cudaMemcpyDeviceToHost, st));
+    if (problem_status && b->count > 0)
+        MCB_CUDA(cudaMemcpyAsync(problem_status, b->d_gstatus, sizeof(unsigned) * (size_t)b->count,
+                                 cudaMemcpyDeviceToHost, st));
+    MCB_CUDA(cudaStreamSynchronize(st));
+    if (v & ST_RANK_DEFICIT) {
+        set_error("a problem's candidates do not span its cycle space (status 0x%x)", v);
+        return MCBGPU_E_NO_CANDIDATE;
+    }
+    if (v) {
+        set_error("a problem's coordinate lists are not ascending in [0, N) (status 0x%x)", v);
+        return MCBGPU_E_ARG;
+    }
+    return MCBGPU_OK;
+}
+
+int mcbgpu_batch_get_support(mcbgpu_batch *b, int32_t problem, int32_t j, uint64_t *words, void *stream) {
+    if (!b || problem < 0 || problem >= b->count || !words || j < 0 || j >= b->graphs[problem].N) {
+        set_error("mcbgpu_batch_get_support: invalid arguments");
+        return MCBGPU_E_ARG;
+    }
+    const BatchGraph &g = b->graphs[problem];
+    cudaStream_t st = (cudaStream_t)stream;
+    // words beyond j / 64 are never written: report them as zero
+    for (int w = 0; w < g.P; w++) words[w] = 0;
+    MCB_CUDA(cudaMemcpyAsync(words, b->d_S + g.srow + (size_t)j * g.P, sizeof(uint64_t) * (size_t)(j / 64 + 1),
+                             cudaMemcpyDeviceToHost, st));
+    MCB_CUDA(cudaStreamSynchronize(st));
+    return MCBGPU_OK;
+}
+
+int64_t mcbgpu_batch_launches(const mcbgpu_batch *b) { return b ? b->launches : 0; }
+int64_t mcbgpu_batch_device_bytes(const mcbgpu_batch *b) { return b ? b->device_bytes : 0; }
+
+int mcbgpu_batch_destroy(mcbgpu_batch *b) {
+    free_batch(b);
+    return MCBGPU_OK;
+}
+
+int mcbgpu_batch_solve(int32_t count, const int32_t *num_coords, const int64_t *num_candidates,
+                       const int32_t *weight, const int64_t *offsets, const int32_t *coords, int64_t *selected,
+                       int64_t *total_weight) {
+    long long totK = 0;
+    for (int i = 0; i < count; i++) totK += num_candidates ? num_candidates[i] : 0;
+    const int64_t nnz = totK > 0 && offsets ? offsets[totK] : 0;
+    mcbgpu_batch *b = nullptr;
+    int rc = mcbgpu_batch_create(&b, count, num_coords, num_candidates, nnz);
+    if (rc) return rc;
+    rc = mcbgpu_batch_upload(b, weight, offsets, coords, nullptr);
+    if (!rc) rc = mcbgpu_batch_run(b, nullptr);
+    if (!rc) rc = mcbgpu_batch_results(b, selected, total_weight, nullptr, nullptr);
+    mcbgpu_batch_destroy(b);
+    return rc;
+}
+
+}  // extern "C"

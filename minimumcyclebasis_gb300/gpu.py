@@ -224,3 +224,106 @@ def solve(num_coords: int, weight: np.ndarray, offsets: np.ndarray, coords: np.n
     check_gpu(lib.mcbgpu_solve(num_coords, w.shape[0], ptr(w), ptr(o), ptr(c), ptr(sel), C.byref(tot)),
               "mcbgpu_solve")
     return sel[:num_coords], tot.value
+
+
+class BatchSolver:
+    """Many independent de Pina problems in one persistent launch per size class.
+
+    `problems` is a list of (num_coords, weight, offsets, coords) tuples, each as
+    Solver takes it (offsets local to the problem, starting at 0).  Every problem's
+    result equals Solver.run's on the same arrays; problems with N above
+    max_coords() are rejected (solve those with Solver)."""
+
+    def __init__(self, problems, stream=0, upload: bool = True):
+        self.lib = gpu_lib()
+        self.count = len(problems)
+        self.N = np.array([int(p[0]) for p in problems], np.int32)
+        self.K = np.array([len(p[1]) for p in problems], np.int64)
+        ws, offs, cos = [], [], []
+        base = 0
+        for n, w, o, c in problems:
+            o = np.asarray(o, np.int64)
+            ws.append(np.asarray(w, np.int32))
+            offs.append(o[:-1] + base)
+            cos.append(np.asarray(c, np.int32)[: int(o[-1])])
+            base += int(o[-1])
+        self.weight = np.ascontiguousarray(np.concatenate(ws) if ws else np.zeros(0, np.int32))
+        self.offsets = np.ascontiguousarray(np.concatenate(offs + [np.array([base], np.int64)]))
+        self.coords = np.ascontiguousarray(np.concatenate(cos) if cos else np.zeros(0, np.int32))
+        self.nnz = base
+        h = C.c_void_p()
+        check_gpu(self.lib.mcbgpu_batch_create(C.byref(h), self.count, ptr(self.N), ptr(self.K), self.nnz),
+                  "mcbgpu_batch_create")
+        self._h = h
+        if upload:
+            self.upload(stream)
+
+    @staticmethod
+    def max_coords() -> int:
+        return int(gpu_lib().mcbgpu_batch_max_coords())
+
+    @classmethod
+    def from_problems(cls, probs, stream=0) -> "BatchSolver":
+        """From prepared host Problems (none of them a single cycle)."""
+        items = []
+        for p in probs:
+            _, _, w, _ = p.candidates()
+            off, co = p.cycle_lists()
+            items.append((p.N, w, off, co))
+        return cls(items, stream)
+
+    def upload(self, stream=0) -> None:
+        check_gpu(self.lib.mcbgpu_batch_upload(self._h, ptr(self.weight), ptr(self.offsets), ptr(self.coords),
+                                               _stream(stream)), "mcbgpu_batch_upload")
+
+    def run(self, stream=0) -> None:
+        check_gpu(self.lib.mcbgpu_batch_run(self._h, _stream(stream)), "mcbgpu_batch_run")
+
+    def results(self, stream=0):
+        """([selected ranks per problem], total weights int64[count]) after synchronising `stream`."""
+        sel = np.full(max(int(self.N.sum()), 1), -1, np.int64)
+        tot = np.zeros(max(self.count, 1), np.int64)
+        check_gpu(self.lib.mcbgpu_batch_results(self._h, ptr(sel), ptr(tot), None, _stream(stream)),
+                  "mcbgpu_batch_results")
+        bounds = np.concatenate([[0], np.cumsum(self.N.astype(np.int64))])
+        return [sel[bounds[i]:bounds[i + 1]] for i in range(self.count)], tot[: self.count]
+
+    def status(self, stream=0) -> np.ndarray:
+        """Per-problem status words (0 = solved), without raising."""
+        st = np.zeros(max(self.count, 1), np.uint32)
+        self.lib.mcbgpu_batch_results(self._h, None, None, ptr(st), _stream(stream))
+        return st[: self.count]
+
+    def support_vector(self, problem: int, j: int, stream=0) -> np.ndarray:
+        out = np.zeros((int(self.N[problem]) + 63) // 64, np.uint64)
+        check_gpu(self.lib.mcbgpu_batch_get_support(self._h, problem, j, ptr(out), _stream(stream)),
+                  "mcbgpu_batch_get_support")
+        return out
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.mcbgpu_batch_launches(self._h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.lib.mcbgpu_batch_device_bytes(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            check_gpu(self.lib.mcbgpu_batch_destroy(self._h), "mcbgpu_batch_destroy")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_batch(problems):
+    """One-shot C-ABI call: ([selected per problem], total weights)."""
+    b = BatchSolver(problems)
+    b.run()
+    out = b.results()
+    b.close()
+    return out

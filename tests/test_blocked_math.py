@@ -73,3 +73,78 @@ def test_blocked_equals_sequential(graph, B):
     p = Problem.from_graph(graph).prepare(threads=2, keep_trees=True)
     ref, _, _ = oracle.solve(p, threads=2)
     assert blocked_select(p, B) == ref.tolist()
+
+
+def batch_select(prob):
+    """The formulation of the batched kernel (one CTA per problem): pivots through a
+    reduced row echelon basis keyed by lead bit, the first odd pivot without
+    excluding used ones, beta through the 64x64 matrix of unit responses, the final
+    rows from the transposed block T, D from (coordinate, iteration) pairs."""
+    N, K = prob.N, prob.K
+    off, co = prob.cycle_lists()
+    lists = [co[off[r]:off[r + 1]].tolist() for r in range(K)]
+    S = [1 << j for j in range(N)]
+    sel = []
+    for e0 in range(0, N, 64):
+        b = min(64, N - e0)
+        bound = e0 + b
+        T = [sum(((S[e0 + i] >> c) & 1) << i for i in range(b)) for c in range(bound)]
+        assert all(T[c] == 1 << (c - e0) for c in range(e0, bound))
+        basis, piv = {}, []  # lead bit -> vector with zeros at every other lead
+        for r in range(K):
+            W = 0
+            for c in lists[r]:
+                if c >= bound:
+                    break
+                W ^= T[c]
+            res = W
+            for lead in list(basis):
+                if (W >> lead) & 1:
+                    res ^= basis[lead]
+            if res:
+                L = (res & -res).bit_length() - 1
+                for lead in basis:
+                    if (basis[lead] >> L) & 1:
+                        basis[lead] ^= res
+                basis[L] = res
+                piv.append((r, W))
+                if len(piv) == b:
+                    break
+        m = [1 << k for k in range(b)]
+        pk = []
+        for k in range(b):
+            p = next(i for i in range(b) if parity(piv[i][1] & m[k]))
+            pk.append(p)
+            for j in range(k + 1, b):
+                if parity(piv[p][1] & m[j]):
+                    m[j] ^= m[k]
+        gcol = [sum(parity(piv[pk[k]][1] & m[i]) << i for i in range(k)) for k in range(b)]
+        Mrow = []
+        for k in range(b):
+            bt = 1 << k
+            for i in range(k + 1, b):
+                bt |= parity(bt & gcol[i]) << i
+            Mrow.append(bt)
+        F = [sum(parity(T[c] & m[k]) << c for c in range(e0)) | (m[k] << e0) for k in range(b)]
+        for k in range(b):
+            S[e0 + k] = F[k]
+        sel += [piv[p][0] for p in pk]
+        pairs = [(c, k) for k in range(b) for c in lists[piv[pk[k]][0]]]
+        for j in range(bound, N):
+            beta = 0
+            for c, k in pairs:
+                bit = (S[j] >> c) & 1 if c < e0 else int(c == j)
+                if bit:
+                    beta ^= Mrow[k]
+            for k in range(b):
+                if (beta >> k) & 1:
+                    S[j] ^= F[k]
+    return sel
+
+
+@pytest.mark.parametrize("graph", [grid_graph(6, 6, 1, 10, 3), random_graph(200, 400, 1, 20, 2),
+                                   grid_graph(12, 12, 1, 3, 9)])
+def test_batch_formulation_equals_sequential(graph):
+    p = Problem.from_graph(graph).prepare(threads=2, keep_trees=True)
+    ref, _, _ = oracle.solve(p, threads=2)
+    assert batch_select(p) == ref.tolist()
