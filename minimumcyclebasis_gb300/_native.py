@@ -101,6 +101,8 @@ GPU_SYMBOLS = {
     "mcbgpu_batch_run": (C.c_int, [vp, vp]),
     "mcbgpu_batch_results": (C.c_int, [vp, vp, vp, vp, vp]),
     "mcbgpu_batch_get_support": (C.c_int, [vp, i32, i32, vp, vp]),
+    "mcbgpu_batch_set_profiling": (C.c_int, [vp, C.c_int]),
+    "mcbgpu_batch_profile": (C.c_int, [vp, vp]),
     "mcbgpu_batch_launches": (i64, [vp]),
     "mcbgpu_batch_device_bytes": (i64, [vp]),
     "mcbgpu_batch_destroy": (C.c_int, [vp]),

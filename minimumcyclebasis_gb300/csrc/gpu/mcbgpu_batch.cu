@@ -35,9 +35,13 @@ namespace {
 
 constexpr int kBThreads = 512;
 constexpr int kBWarps = kBThreads / 32;
-constexpr int kBChunk = 8;               // coordinates loaded together in a W walk
+#ifndef MCB_BATCH_CHUNK
+#define MCB_BATCH_CHUNK 4
+#endif
+constexpr int kBChunk = MCB_BATCH_CHUNK;  // coordinates of each candidate loaded together in a W walk
 constexpr int kBatchMaxN = 12288;        // largest N a CTA holds (T and the final rows in shared memory)
-constexpr unsigned kPairSmem = 4096;     // pairs kept in shared memory (more go to the CTA's global scratch)
+constexpr unsigned kPairSmemMax = 8192;  // pairs kept in shared memory (more go to the CTA's global scratch)
+constexpr size_t kSmemBudget = 220 * 1024;  // dynamic shared memory per CTA at most (static adds 3.4 KB)
 constexpr int kClasses = 3;
 constexpr int kClassMaxN[kClasses] = {1024, 4096, kBatchMaxN};
 
@@ -57,35 +61,56 @@ __device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int d) {
     return ((uint64_t)hi << 32) | lo;
 }
 
-// W of one candidate from the block's T in shared memory.
-__device__ __forceinline__ uint64_t w_smem(long long r, const int64_t *__restrict__ off,
-                                           const int32_t *__restrict__ coords, const uint64_t *T, int bound) {
-    long long i = __ldg(off + r);
-    const long long e = __ldg(off + r + 1);
-    uint64_t W = 0;
-    while (i < e) {
-        int cv[kBChunk];
+// W of the kBQ consecutive candidates r0 .. r0 + kBQ - 1 (0 past K) from the block's
+// T in shared memory.  The lists are walked in lockstep, kBChunk coordinates of each
+// per step, so kBQ x kBChunk independent loads are in flight per thread.
+template <int kBQ>
+__device__ __forceinline__ void w_smem_q(long long r0, long long K, long long cand,
+                                         const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
+                                         const uint64_t *T, int bound, uint64_t (&W)[kBQ]) {
+    long long ia[kBQ], ea[kBQ];
 #pragma unroll
-        for (int q = 0; q < kBChunk; q++) cv[q] = i + q < e ? __ldg(coords + i + q) : 0x7fffffff;
-#pragma unroll
-        for (int q = 0; q < kBChunk; q++)
-            if (cv[q] < bound) W ^= T[cv[q]];
-        if (cv[kBChunk - 1] >= bound) break;
-        i += kBChunk;
+    for (int q = 0; q < kBQ; q++) {
+        W[q] = 0;
+        ia[q] = ea[q] = 0;
+        if (r0 + q < K) {
+            ia[q] = __ldg(off + cand + r0 + q);
+            ea[q] = __ldg(off + cand + r0 + q + 1);
+        }
     }
-    return W;
+    for (;;) {
+        bool any = false;
+#pragma unroll
+        for (int q = 0; q < kBQ; q++) any |= ia[q] < ea[q];
+        if (!any) break;
+        int cv[kBQ][kBChunk];
+#pragma unroll
+        for (int q = 0; q < kBQ; q++)
+#pragma unroll
+            for (int t = 0; t < kBChunk; t++) cv[q][t] = ia[q] + t < ea[q] ? __ldg(coords + ia[q] + t) : 0x7fffffff;
+#pragma unroll
+        for (int q = 0; q < kBQ; q++) {
+#pragma unroll
+            for (int t = 0; t < kBChunk; t++)
+                if (cv[q][t] < bound) W[q] ^= T[cv[q][t]];
+            ia[q] = cv[q][kBChunk - 1] >= bound ? ea[q] : ia[q] + kBChunk;
+        }
+    }
 }
 
-__global__ void __launch_bounds__(kBThreads) batch_solve_kernel(
+// kBQ: candidates per thread in one scan round; kRowRegs: row words per lane in the
+// update (ceil(largest N of the class / 2048)).
+template <int kBQ, int kRowRegs, int kMinBlocks>
+__global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
     const BatchGraph *__restrict__ graphs, const int *__restrict__ order, int count, unsigned *next,
     const int32_t *__restrict__ weight, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
     uint64_t *S, long long *selected, long long *total, unsigned *gstatus, unsigned *status, unsigned *pair_scratch,
-    unsigned pair_cap, int ncap) {
+    unsigned pair_cap, int ncap, unsigned pcap, long long *prof) {
     extern __shared__ __align__(16) uint64_t smem[];
-    const int wcap = (ncap + 63) >> 6;
-    uint64_t *T = smem;                                    // ncap words
-    uint64_t *F = smem + ncap;                             // 64 x (wcap + 1) words: the block's final rows
-    unsigned *sPairs = (unsigned *)(F + 64 * (wcap + 1));  // kPairSmem
+    const int wcap = ncap >> 6;                       // ncap is a multiple of 64
+    uint64_t *T = smem;                               // ncap words (the row buffers of the update alias it)
+    uint64_t *F = smem + ncap;                        // 64 x wcap words: the block's final rows
+    unsigned *sPairs = (unsigned *)(F + 64 * wcap);   // pcap pairs
     unsigned *gPairs = pair_scratch + (size_t)blockIdx.x * pair_cap;
 
     __shared__ uint64_t sB[64];     // reduced echelon basis, by lead bit
@@ -100,6 +125,7 @@ __global__ void __launch_bounds__(kBThreads) batch_solve_kernel(
     __shared__ uint64_t sNewRes, sNewW;
     __shared__ int sGi;
     __shared__ unsigned sFail;
+    __shared__ long long pc[6];  // profile (thread 0): cycles in T, scan, resolve, final rows, update; scanned
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned full = 0xffffffffu;
@@ -140,11 +166,17 @@ __global__ void __launch_bounds__(kBThreads) batch_solve_kernel(
             for (int w = lane; w <= (j >> 6); w += 32) row[w] = w == (j >> 6) ? 1ull << (j & 63) : 0ull;
         }
         long long tot = 0;
-        if (tid == 0) sFail = 0;
+        unsigned long long t_start = 0;
+        if (prof && tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
+        if (tid == 0) {
+            sFail = 0;
+            for (int q = 0; q < 6; q++) pc[q] = 0;
+        }
         cta_sync();
 
         for (int e0 = 0; e0 < N; e0 += 64) {
             const int b = min(64, N - e0), bound = e0 + b, wl = e0 >> 6, Wb = wl + 1;
+            long long c0 = prof ? clock64() : 0;
             // ---- 1. T
             for (int c = e0 + tid; c < bound; c += kBThreads) T[c] = 1ull << (c - e0);
             for (int w = warp; w < wl; w += kBWarps) {
@@ -167,30 +199,58 @@ __global__ void __launch_bounds__(kBThreads) batch_solve_kernel(
                 T[(w << 6) + 32 + lane] = v1;
             }
             cta_sync();
+            if (prof && tid == 0) {
+                const long long c = clock64();
+                pc[0] += c - c0;
+                c0 = c;
+            }
 
             // ---- 2. pivots: the first b rank-ordered candidates with independent W
             int npiv = 0;
             uint64_t lead = 0;
-            for (long long base = 0; npiv < b; base += kBThreads) {
+            for (long long base = 0; npiv < b; base += (long long)kBThreads * kBQ) {
                 if (base >= K) {  // fewer than b independent candidates
                     if (tid == 0) sFail = 1;
                     break;
                 }
-                const long long r = base + tid;
-                const uint64_t W = r < K ? w_smem(cand + r, off, coords, T, bound) : 0ull;
-                uint64_t res = W;
-                for (uint64_t m = W & lead; m; m &= m - 1) res ^= sB[ffs64(m)];
+                // thread tid holds ranks base + tid * kBQ + q: key tid * kBQ + q is rank order
+                uint64_t W[kBQ], res[kBQ];
+                w_smem_q<kBQ>(base + (long long)tid * kBQ, K, cand, off, coords, T, bound, W);
+#pragma unroll
+                for (int q = 0; q < kBQ; q++) {
+                    res[q] = W[q];
+                    for (uint64_t m = W[q] & lead; m; m &= m - 1) res[q] ^= sB[ffs64(m)];
+                }
                 for (;;) {
-                    const unsigned bal = __ballot_sync(full, res != 0);
-                    if (lane == 0) sWmin[warp] = bal ? warp * 32 + __ffs(bal) - 1 : 0x7fffffff;
+                    int myq = kBQ;
+#pragma unroll
+                    for (int q = kBQ - 1; q >= 0; q--)
+                        if (res[q]) myq = q;
+                    const unsigned bal = __ballot_sync(full, myq < kBQ);
+                    if (bal) {
+                        const int fl = __ffs(bal) - 1;
+                        const int fq = __shfl_sync(full, myq, fl);
+                        if (lane == 0) sWmin[warp] = (warp * 32 + fl) * kBQ + fq;
+                    } else if (lane == 0) {
+                        sWmin[warp] = 0x7fffffff;
+                    }
                     cta_sync();
                     int best = 0x7fffffff;
 #pragma unroll
                     for (int q = 0; q < kBWarps; q++) best = min(best, sWmin[q]);
                     if (best == 0x7fffffff) break;
-                    if (tid == best) {
-                        sNewRes = res;
-                        sNewW = W;
+                    {
+                        uint64_t sr = 0, sw = 0;  // selects, not an indexed access (keeps res / W in registers)
+#pragma unroll
+                        for (int q = 0; q < kBQ; q++) {
+                            const bool h = tid * kBQ + q == best;
+                            sr = h ? res[q] : sr;
+                            sw = h ? W[q] : sw;
+                        }
+                        if (tid == best / kBQ) {
+                            sNewRes = sr;
+                            sNewW = sw;
+                        }
                     }
                     cta_sync();
                     const uint64_t nr = sNewRes;
@@ -206,15 +266,24 @@ __global__ void __launch_bounds__(kBThreads) batch_solve_kernel(
                     }
                     lead |= 1ull << L;
                     npiv++;
-                    if (tid == best)
-                        res = 0;
-                    else if ((res >> L) & 1)
-                        res ^= nr;
+#pragma unroll
+                    for (int q = 0; q < kBQ; q++) {
+                        if (tid * kBQ + q == best)
+                            res[q] = 0;
+                        else if ((res[q] >> L) & 1)
+                            res[q] ^= nr;
+                    }
                     if (npiv == b) break;
                 }
                 cta_sync();
+                if (tid == 0) pc[5] += kBThreads * kBQ;
             }
             cta_sync();
+            if (prof && tid == 0) {
+                const long long c = clock64();
+                pc[1] += c - c0;
+                c0 = c;
+            }
             if (sFail) break;
 
             // ---- 3. resolve (warp 0), gcol, the beta matrix, selected ranks, pair offsets
@@ -291,9 +360,14 @@ __global__ void __launch_bounds__(kBThreads) batch_solve_kernel(
                 }
             }
             cta_sync();
+            if (prof && tid == 0) {
+                const long long c = clock64();
+                pc[2] += c - c0;
+                c0 = c;
+            }
             if (sFail) break;
             const unsigned np = sPre[b];
-            unsigned *pairs = np <= kPairSmem ? sPairs : gPairs;
+            unsigned *pairs = np <= pcap ? sPairs : gPairs;
 
             // ---- 4. final rows of the block (shared F and global S), 5. pairs
             for (int item = warp; item < b * wl; item += kBWarps) {
@@ -318,29 +392,57 @@ __global__ void __launch_bounds__(kBThreads) batch_solve_kernel(
                     pairs[o + (unsigned)(i - a)] = ((unsigned)coords[i] << 6) | (unsigned)k;
             }
             cta_sync();
+            if (prof && tid == 0) {
+                const long long c = clock64();
+                pc[3] += c - c0;
+                c0 = c;
+            }
 
-            // ---- 6. later rows: one warp per row
+            // ---- 6. later rows: one warp per row.  The row's words [0, Wb) are loaded
+            // once (coalesced) into registers and, below e0, into the warp's row buffer
+            // (T's storage, free until the next block); D_j from the pairs against the
+            // buffer, beta = D_j x Mrow, then S_j ^= XOR_{k in beta} F_k.
+            uint64_t *rowbuf = T + (size_t)warp * wcap;
             for (int j = bound + warp; j < N; j += kBWarps) {
                 uint64_t *Sj = Sg + (size_t)j * P;
-                uint64_t acc = 0;
+                uint64_t v[kRowRegs];
+#pragma unroll
+                for (int i = 0; i < kRowRegs; i++) {
+                    const int w = lane + 32 * i;
+                    v[i] = w < Wb ? Sj[w] : 0ull;
+                    if (w < wl) rowbuf[w] = v[i];
+                }
+                __syncwarp();
+                uint64_t D = 0;
                 for (unsigned i = lane; i < np; i += 32) {
                     const unsigned pr = pairs[i];
                     const int c = (int)(pr >> 6);
-                    const bool bit = c < e0 ? ((Sj[c >> 6] >> (c & 63)) & 1) : c == j;
-                    if (bit) acc ^= sMrow[pr & 63];
+                    const uint64_t bit = c < e0 ? (rowbuf[c >> 6] >> (c & 63)) & 1ull : (uint64_t)(c == j);
+                    D ^= bit << (pr & 63);
                 }
 #pragma unroll
-                for (int d = 16; d > 0; d >>= 1) acc ^= shfl_xor64(acc, d);
-                if (!acc) continue;
-                for (int w = lane; w < Wb; w += 32) {
-                    uint64_t x = 0;
-                    for (uint64_t bb = acc; bb; bb &= bb - 1) x ^= F[ffs64(bb) * Wb + w];
-                    Sj[w] ^= x;
+                for (int d = 16; d > 0; d >>= 1) D ^= shfl_xor64(D, d);
+                uint64_t beta = ((D >> lane) & 1) ? sMrow[lane] : 0ull;
+                if ((D >> (lane + 32)) & 1) beta ^= sMrow[lane + 32];
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) beta ^= shfl_xor64(beta, d);
+                if (beta) {
+#pragma unroll
+                    for (int i = 0; i < kRowRegs; i++) {
+                        const int w = lane + 32 * i;
+                        if (w < Wb) {
+                            uint64_t x = 0;
+                            for (uint64_t bb = beta; bb; bb &= bb - 1) x ^= F[ffs64(bb) * Wb + w];
+                            Sj[w] = v[i] ^ x;
+                        }
+                    }
                 }
+                __syncwarp();
             }
             if (tid == 0)
                 for (int k = 0; k < b; k++) selected[g.sel + e0 + k] = sSel[k];
             cta_sync();
+            if (prof && tid == 0) pc[4] += clock64() - c0;
         }
         if (tid == 0) {
             if (sFail) {
@@ -351,6 +453,16 @@ __global__ void __launch_bounds__(kBThreads) batch_solve_kernel(
         if (warp == 0) {
             // tot lives in lane 0 of warp 0
             if (lane == 0) total[gx] = sFail ? -1 : tot;
+        }
+        if (prof && tid == 0) {
+            unsigned long long t_end;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
+            unsigned smid;
+            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+            long long *o = prof + (size_t)gx * 8;
+            o[0] = (long long)(t_end - t_start);
+            for (int q = 0; q < 6; q++) o[1 + q] = pc[q];
+            o[7] = smid;
         }
     }
 }
@@ -380,6 +492,7 @@ struct mcbgpu_batch {
     unsigned *d_gstatus = nullptr;
     unsigned *d_status = nullptr;
     unsigned *d_pairs = nullptr;
+    long long *d_prof = nullptr;  // optional per-problem profile (count x 8)
     cudaStream_t st[kClasses] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[kClasses] = {};
     bool uploaded = false;
@@ -389,10 +502,14 @@ struct mcbgpu_batch {
 
 namespace {
 
-size_t batch_smem_bytes(int ncap) {
-    const size_t wcap = (size_t)(ncap + 63) / 64;
-    return 8 * (size_t)ncap + 8 * 64 * (wcap + 1) + 4 * (size_t)kPairSmem;
+// Pairs kept in shared memory next to T and F for a class of largest N = ncap.
+unsigned batch_pair_smem(int ncap) {
+    const size_t tf = 16 * (size_t)ncap;
+    const size_t room = kSmemBudget > tf ? (kSmemBudget - tf) / 4 : 0;
+    return (unsigned)std::min<size_t>(kPairSmemMax, room & ~(size_t)31);
 }
+
+size_t batch_smem_bytes(int ncap) { return 16 * (size_t)ncap + 4 * (size_t)batch_pair_smem(ncap); }
 
 void free_batch(mcbgpu_batch *b) {
     if (!b) return;
@@ -408,12 +525,27 @@ void free_batch(mcbgpu_batch *b) {
     cudaFree(b->d_gstatus);
     cudaFree(b->d_status);
     cudaFree(b->d_pairs);
+    cudaFree(b->d_prof);
     for (int c = 0; c < kClasses; c++) {
         if (b->st[c]) cudaStreamDestroy(b->st[c]);
         if (b->ev_join[c]) cudaEventDestroy(b->ev_join[c]);
     }
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     delete b;
+}
+
+using BatchKernel = void (*)(const BatchGraph *, const int *, int, unsigned *, const int32_t *, const int64_t *,
+                            const int32_t *, uint64_t *, long long *, long long *, unsigned *, unsigned *, unsigned *,
+                            unsigned, int, unsigned, long long *);
+
+// Class c's kernel: problems with N <= kClassMaxN[c] (row words per lane in the
+// update = kClassMaxN[c] / 2048, rounded up).
+BatchKernel class_kernel(int c) {
+    switch (c) {
+        case 0: return batch_solve_kernel<2, 1, 2>;
+        case 1: return batch_solve_kernel<4, 2, 1>;
+        default: return batch_solve_kernel<4, (kBatchMaxN / 64 + 31) / 32, 1>;
+    }
 }
 
 int class_of(int N) {
@@ -507,15 +639,15 @@ int mcbgpu_batch_create(mcbgpu_batch **out, int32_t count, const int32_t *num_co
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
     // one persistent grid per class: as many CTAs as are resident at once, at most one per problem
-    // the attribute is per kernel, shared by all handles: always the largest class's need
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(batch_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)batch_smem_bytes(kBatchMaxN));
+    // the attribute is per kernel, shared by all handles: the class's largest need
+    for (int c = 0; c < kClasses && e == cudaSuccess; c++)
+        e = cudaFuncSetAttribute(class_kernel(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)batch_smem_bytes(kClassMaxN[c]));
     for (int c = 0; c < kClasses && e == cudaSuccess; c++) {
         const int n = b->class_off[c + 1] - b->class_off[c];
         if (n == 0) continue;
         int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_solve_kernel, kBThreads,
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, class_kernel(c), kBThreads,
                                                           batch_smem_bytes(b->class_ncap[c]));
         if (e == cudaSuccess && per_sm < 1) e = cudaErrorInvalidConfiguration;
         b->class_grid[c] = (int)std::min<long long>(n, (long long)per_sm * std::max(b->sm_count, 1));
@@ -599,10 +731,11 @@ int mcbgpu_batch_run(mcbgpu_batch *b, void *stream) {
         const int n = b->class_off[c + 1] - b->class_off[c];
         if (n == 0) continue;
         MCB_CUDA(cudaStreamWaitEvent(b->st[c], b->ev_fork, 0));
-        batch_solve_kernel<<<b->class_grid[c], kBThreads, batch_smem_bytes(b->class_ncap[c]), b->st[c]>>>(
+        class_kernel(c)<<<b->class_grid[c], kBThreads, batch_smem_bytes(b->class_ncap[c]), b->st[c]>>>(
             b->d_graphs, b->d_order + b->class_off[c], n, b->d_next + c, b->d_weight, b->d_off, b->d_coords, b->d_S,
             b->d_selected, b->d_total, b->d_gstatus, b->d_status,
-            b->d_pairs + (size_t)c * b->pair_cap * (size_t)b->pair_slabs, b->pair_cap, b->class_ncap[c]);
+            b->d_pairs + (size_t)c * b->pair_cap * (size_t)b->pair_slabs, b->pair_cap, b->class_ncap[c],
+            batch_pair_smem(b->class_ncap[c]), b->d_prof);
         MCB_CUDA(cudaGetLastError());
         b->launches++;
         MCB_CUDA(cudaEventRecord(b->ev_join[c], b->st[c]));
@@ -653,6 +786,31 @@ int mcbgpu_batch_get_support(mcbgpu_batch *b, int32_t problem, int32_t j, uint64
     MCB_CUDA(cudaMemcpyAsync(words, b->d_S + g.srow + (size_t)j * g.P, sizeof(uint64_t) * (size_t)(j / 64 + 1),
                              cudaMemcpyDeviceToHost, st));
     MCB_CUDA(cudaStreamSynchronize(st));
+    return MCBGPU_OK;
+}
+
+int mcbgpu_batch_set_profiling(mcbgpu_batch *b, int enable) {
+    if (!b) {
+        set_error("mcbgpu_batch_set_profiling: NULL handle");
+        return MCBGPU_E_ARG;
+    }
+    if (enable && !b->d_prof) {
+        MCB_CUDA(cudaMalloc((void **)&b->d_prof, sizeof(long long) * 8 * (size_t)std::max(b->count, 1)));
+        MCB_CUDA(cudaMemset(b->d_prof, 0, sizeof(long long) * 8 * (size_t)std::max(b->count, 1)));
+    } else if (!enable && b->d_prof) {
+        MCB_CUDA(cudaFree(b->d_prof));
+        b->d_prof = nullptr;
+    }
+    return MCBGPU_OK;
+}
+
+int mcbgpu_batch_profile(mcbgpu_batch *b, int64_t *out) {
+    if (!b || !out || !b->d_prof) {
+        set_error("mcbgpu_batch_profile: %s", b && b->d_prof ? "NULL output" : "profiling is off");
+        return MCBGPU_E_ARG;
+    }
+    MCB_CUDA(cudaDeviceSynchronize());
+    MCB_CUDA(cudaMemcpy(out, b->d_prof, sizeof(long long) * 8 * (size_t)b->count, cudaMemcpyDeviceToHost));
     return MCBGPU_OK;
 }
 

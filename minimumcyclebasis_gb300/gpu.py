@@ -300,6 +300,15 @@ class BatchSolver:
                   "mcbgpu_batch_get_support")
         return out
 
+    def set_profiling(self, enable: bool = True) -> None:
+        check_gpu(self.lib.mcbgpu_batch_set_profiling(self._h, int(enable)), "mcbgpu_batch_set_profiling")
+
+    def profile(self) -> np.ndarray:
+        """Per problem: [ns, cycles in T, scan, resolve, final rows, update, candidates scanned, SM]."""
+        out = np.zeros((max(self.count, 1), 8), np.int64)
+        check_gpu(self.lib.mcbgpu_batch_profile(self._h, ptr(out)), "mcbgpu_batch_profile")
+        return out[: self.count]
+
     @property
     def launches(self) -> int:
         return int(self.lib.mcbgpu_batch_launches(self._h))
