@@ -23,6 +23,12 @@ larger than the 129 MB L2, so no flush is needed between steps.
   cpu_baseline  the reference's CPU main loop (oracle port of mcb/mcb_non_cpu_rd.cpp)
               on this host's cores over the first P iterations, extrapolated to N
 
+`--workload batch` measures the batched configuration instead: --batch-count graphs
+(n log-uniform in [50, 5000], average degree U[2.5, 5], w U[1, 255]) solved in one
+BatchSolver (one persistent launch per size class), the plain GPU form (the blocked
+single-problem solver, problem after problem) on a sample beside it, and the
+biconnected components of a --blocks block tree in a second batch.
+
 `--impl reference` times only that CPU implementation and prints its own line.
 Under torchrun (N > 1) every rank solves its own replica (the loop does not shard).
 """
@@ -325,6 +331,175 @@ def run_gpu(args, world, rank, local, pg):
             "cpu_baseline": cb}
 
 
+def run_batch(args, world, rank, local, pg):
+    """The batched configuration: `--batch-count` independent graphs (n log-uniform in
+    [50, 5000], average degree U[2.5, 5], w U[1, 255]) in one BatchSolver, plus the
+    biconnected components of a tree of `--blocks` random blocks in a second one.
+    One step = one batched solve of all the graphs' problems, inputs resident."""
+    import numpy as np
+    import torch
+
+    from minimumcyclebasis_gb300 import BatchSolver, Problem, Solver, batch_graphs, bcc_split, block_tree_graph
+    from minimumcyclebasis_gb300.build import build_all
+
+    build_all()
+    torch.cuda.set_device(local)
+    t0 = time.time()
+
+    def problems(graphs):
+        items, host_total, nsc = [], 0, 0
+        for g in graphs:
+            p = Problem.from_graph(g).prepare(threads=0)
+            if p.info.single_cycle:  # the graph is one cycle: its basis needs no search
+                host_total += int(g.w.astype(np.int64).sum())
+                nsc += 1
+                continue
+            if p.N == 0:
+                continue
+            _, _, w, _ = p.candidates()
+            off, co = p.cycle_lists()
+            items.append((p.N, w, off, co))
+        return items, host_total, nsc
+
+    graphs = batch_graphs(args.batch_count, seed=args.seed + rank)
+    items, host_total, nsc = problems(graphs)
+    bt = block_tree_graph(args.blocks, seed=args.seed + rank)
+    comps = bcc_split(bt)
+    bitems, bhost_total, bnsc = problems(comps)
+    log("prepared in %.1fs: %d batch problems (%d rings), %d block-tree components (%d rings)"
+        % (time.time() - t0, len(items), nsc, len(bitems), bnsc))
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    bs = BatchSolver(items, stream=sh)
+    bb = BatchSolver(bitems, stream=sh)
+    for _ in range(args.warmup):
+        bs.run(sh)
+        bb.run(sh)
+    sels, tots = bs.results(sh)
+    bsels, btots = bb.results(sh)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+
+    def timed(solver):
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            solver.run(sh)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / args.steps
+
+    launches0 = bs.launches
+    with ClockSampler(local) as clocks:
+        ms = timed(bs)
+    launches = bs.launches - launches0
+    ms_blocks = timed(bb)
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # the plain GPU form: one blocked single-problem solver per problem, in sequence,
+    # on every `plain_stride`-th problem (extrapolated to all)
+    stride = max(1, args.plain_stride)
+    plain_ms, checked = 0.0, 0
+    for i in range(0, len(items), stride):
+        s = Solver(*items[i], stream=sh)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        s.run(-1, sh)
+        ev1.record(stream)
+        sel, tot = s.results(stream=sh)
+        plain_ms += ev0.elapsed_time(ev1)
+        assert np.array_equal(sel, sels[i]) and tot == tots[i], "batched and single-problem results differ"
+        checked += 1
+        s.close()
+    plain_est_s = plain_ms / 1e3 * len(items) / max(checked, 1)
+
+    # per-problem profile: CTA time split and scanned candidates
+    bs.set_profiling(True)
+    bs.run(sh)
+    prof = bs.profile()
+    bs.set_profiling(False)
+    cyc = prof[:, 1:6].sum(0).astype(float)
+    Ns = np.array([it[0] for it in items])
+
+    # end to end: upload from pinned host buffers, run, results
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+
+        from minimumcyclebasis_gb300._native import check_gpu, gpu_lib
+        lib = gpu_lib()
+        pw, pw_h = pinned_like(bs.weight)
+        po, po_h = pinned_like(bs.offsets)
+        pc, pc_h = pinned_like(bs.coords)
+        psel, psel_h = pinned_like(np.zeros(max(int(Ns.sum()), 1), np.int64))
+        ptot, ptot_h = pinned_like(np.zeros(max(len(items), 1), np.int64))
+
+        def e2e_once():
+            check_gpu(lib.mcbgpu_batch_upload(bs._h, C.c_void_p(pw.ctypes.data), C.c_void_p(po.ctypes.data),
+                                              C.c_void_p(pc.ctypes.data), C.c_void_p(sh)), "mcbgpu_batch_upload")
+            bs.run(sh)
+            check_gpu(lib.mcbgpu_batch_results(bs._h, C.c_void_p(psel.ctypes.data), C.c_void_p(ptot.ctypes.data),
+                                               None, C.c_void_p(sh)), "mcbgpu_batch_results")
+
+        e2e_once()
+        t1 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_once()
+        e2e_s = (time.perf_counter() - t1) / args.e2e_steps
+        assert np.array_equal(ptot[:len(items)], tots), "e2e results differ"
+        e2e = {"value": e2e_s, "unit": "s", "steps": args.e2e_steps,
+               "h2d_bytes_per_step": int(bs.weight.nbytes + bs.offsets.nbytes + bs.coords.nbytes),
+               "d2h_bytes_per_step": int(8 * Ns.sum() + 8 * len(items) + 4)}
+        for h in (pw_h, po_h, pc_h, psel_h, ptot_h):
+            lib.mcbgpu_free_pinned(h)
+    if rank != 0:
+        return None
+    nnz = int(bs.offsets[-1])
+    scanned = int(prof[:, 6].sum())
+    K = int(bs.weight.shape[0])
+    # the scan reads, per scanned candidate, its two offsets and its coordinate list
+    # (lists are walked to the block's bound; the full list is the upper bound used here)
+    scan_bytes = scanned * (8 + 4.0 * nnz / max(K, 1))
+    peak, peak_kind = measured_peaks()
+    achieved = scan_bytes / (ms / 1e3) / 1e9
+    return {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": "batched: %d random graphs, n log-uniform [50,5000], avg degree U[2.5,5], "
+                                   "w U[1,255], seed %d; one batched solve of all of them" % (args.batch_count,
+                                                                                               args.seed),
+                       "problems": len(items), "rings_on_host": nsc, "N_max": int(Ns.max()), "N_sum": int(Ns.sum()),
+                       "K": K, "cycle_nnz": nnz, "form": "batched (one persistent launch per size class)",
+                       "total_weight": int(tots.sum()) + host_total,
+                       "l2": "inputs (%.2f GB) larger than the 129 MB L2; no flush" % ((nnz * 4 + K * 12) / 1e9)},
+            "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": int(launches),
+            "plain_gpu": {"value": plain_est_s, "unit": "s", "speedup": plain_est_s / (ms / 1e3),
+                          "sample": "blocked single-problem solver on every %d-th problem (%d solves, %.1f ms), "
+                                    "extrapolated to all %d; selected ranks and weights equal the batch's"
+                                    % (stride, checked, plain_ms, len(items))},
+            "block_tree": {"blocks": args.blocks, "nodes": int(bt.nodes), "components_on_gpu": len(bitems),
+                           "rings_on_host": bnsc, "value": ms_blocks / 1e3, "unit": "s",
+                           "total_weight": int(btots.sum()) + bhost_total},
+            "profile": {"cta_ms_sum": float(prof[:, 0].sum() / 1e6), "cta_ms_max": float(prof[:, 0].max() / 1e6),
+                        "cycle_share": dict(zip(["transpose", "scan", "resolve", "final_rows", "update"],
+                                                [round(float(c / cyc.sum()), 4) for c in cyc])),
+                        "scanned_candidates": scanned},
+            "roofline": {"kernel": "batch_solve", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "bytes_per_launch": scan_bytes, "launch_ms": ms,
+                         "note": "scan bytes (offsets + lists of the scanned candidates) per batched solve; the "
+                                 "kernel is latency-bound on the per-problem critical path"},
+            "cpu_baseline": None}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -340,10 +515,17 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["random", "batch"], default="random",
+                    help="random: the 50k-node graph (default); batch: the batched configuration")
+    ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--blocks", type=int, default=2000)
+    ap.add_argument("--plain-stride", type=int, default=16)
     args = ap.parse_args()
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
         out = run_reference(args, world, rank, pg)
+    elif args.workload == "batch":
+        out = run_batch(args, world, rank, local, pg)
     else:
         out = run_gpu(args, world, rank, local, pg)
     if out is not None:
