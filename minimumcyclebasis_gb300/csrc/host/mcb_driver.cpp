@@ -22,6 +22,7 @@
 //                        each one that has a cycle (in order of its first edge), one
 //                        stats row per component, the way the reference's bicc tool +
 //                        per-component loop (bicc/, main.sh:19-32) processes a graph;
+//                        the components go through one batched solve (mcbgpu_batch);
 //                        the cycle listings give each component's basis in turn
 //
 // Exit status 0 on success; on any error a message on stderr and status 1 (the
@@ -109,18 +110,38 @@ struct Outputs {
     int threads = 1;
 };
 
-// Prepares and solves one problem; appends its stats row and its cycle blocks.
-// input_ids: the input vertex of every vertex of the problem's graph (NULL: the
-// problem's graph is the input graph).  Returns the basis weight.
-long long solve_one(mcbh_problem *p, const Outputs &o, const int32_t *input_ids) {
+// One problem from preparation to output.
+struct Job {
+    mcbh_problem *p = nullptr;
+    std::vector<int32_t> ids;  // input vertex of every vertex of the problem's graph (empty: the input graph)
+    mcbh_info info{};
+    Stats st;
+    std::vector<int32_t> root, edge, weight, tree, coords;
+    std::vector<int64_t> off, sel;
+    long long total = 0;
+};
+
+void init_gpu_once() {
+    static bool ready = false;  // first problem that needs the GPU
+    if (!ready) {
+        int dev = 0, sms = 0;
+        size_t mem = 0;
+        check_gpu(mcbgpu_init_cuda(&dev, &sms, &mem), "CUDA initialisation");
+        ready = true;
+    }
+}
+
+// Host preparation: reduced graph, FVS, trees, the rank-ordered candidates and
+// their coordinate lists; the stats row's host columns.
+void prepare_job(Job &j, const Outputs &o) {
     mcbh_options opt{};
     opt.threads = o.threads > 0 ? o.threads : 1;
     opt.contract_chains = 1;
     opt.cycle_lists = 1;
-    check_host(mcbh_prepare(p, &opt), "preprocessing failed");
-    mcbh_info info{};
-    check_host(mcbh_get_info(p, &info), "mcbh_get_info");
-    Stats st;
+    check_host(mcbh_prepare(j.p, &opt), "preprocessing failed");
+    check_host(mcbh_get_info(j.p, &j.info), "mcbh_get_info");
+    const mcbh_info &info = j.info;
+    Stats &st = j.st;
     st.nodes = info.nodes;
     st.edges = info.edges2;
     if (info.single_cycle) {  // every vertex has degree two (mcb_cycle_deg_two_remove.cpp:104-111)
@@ -129,8 +150,8 @@ long long solve_one(mcbh_problem *p, const Outputs &o, const int32_t *input_ids)
         st.final_ = 1;
         st.initial = 1;
         st.total_weight = info.total_weight_input;
-        st.append(o.stats);
-        return info.total_weight_input;
+        j.total = info.total_weight_input;
+        return;
     }
     st.nodes_removed = info.nodes_removed;
     st.new_edges = info.reduced_edges2;
@@ -138,68 +159,124 @@ long long solve_one(mcbh_problem *p, const Outputs &o, const int32_t *input_ids)
     st.initial = info.num_candidates;
     st.t_trees = info.t_trees;
     st.t_collect = info.t_collect;
-
-    const int32_t N = info.num_coords;
     const int64_t K = info.num_candidates;
-    std::vector<int32_t> root(K), edge(K), weight(K), tree(K);
-    check_host(mcbh_get_candidates(p, root.data(), edge.data(), weight.data(), tree.data()), "mcbh_get_candidates");
-    std::vector<int64_t> off(K + 1);
-    std::vector<int32_t> coords(info.cycle_nnz > 0 ? info.cycle_nnz : 1);
-    check_host(mcbh_get_cycle_lists(p, off.data(), coords.data()), "mcbh_get_cycle_lists");
+    j.root.resize(K);
+    j.edge.resize(K);
+    j.weight.resize(K);
+    j.tree.resize(K);
+    check_host(mcbh_get_candidates(j.p, j.root.data(), j.edge.data(), j.weight.data(), j.tree.data()),
+               "mcbh_get_candidates");
+    j.off.resize(K + 1);
+    j.coords.resize(info.cycle_nnz > 0 ? info.cycle_nnz : 1);
+    check_host(mcbh_get_cycle_lists(j.p, j.off.data(), j.coords.data()), "mcbh_get_cycle_lists");
+}
 
-    static bool cuda_ready = false;  // first problem that needs the GPU
-    if (!cuda_ready) {
-        int dev = 0, sms = 0;
-        size_t mem = 0;
-        check_gpu(mcbgpu_init_cuda(&dev, &sms, &mem), "CUDA initialisation");
-        cuda_ready = true;
-    }
+bool needs_gpu(const Job &j) { return !j.info.single_cycle && j.info.num_coords > 0; }
+
+// One problem on the single-problem solver (blocked, or per iteration with --plain).
+void solve_single(Job &j, const Outputs &o) {
+    init_gpu_once();
+    const int32_t N = j.info.num_coords;
+    const int64_t K = j.info.num_candidates;
     const double t1 = now_s();
     mcbgpu_solver *s = nullptr;
-    check_gpu(mcbgpu_solver_create(&s, N, K, off[K]), "mcbgpu_solver_create");
-    check_gpu(mcbgpu_solver_upload(s, weight.data(), off.data(), coords.data(), nullptr), "mcbgpu_solver_upload");
+    check_gpu(mcbgpu_solver_create(&s, N, K, j.off[K]), "mcbgpu_solver_create");
+    check_gpu(mcbgpu_solver_upload(s, j.weight.data(), j.off.data(), j.coords.data(), nullptr), "mcbgpu_solver_upload");
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     cudaEventRecord(a, 0);
     check_gpu(o.plain ? mcbgpu_solver_run_plain(s, -1, nullptr) : mcbgpu_solver_run(s, -1, nullptr), "solve");
     cudaEventRecord(b, 0);
-    std::vector<int64_t> sel(N);
+    j.sel.assign(N, -1);
     int64_t total = 0;
-    check_gpu(mcbgpu_solver_results(s, sel.data(), N, &total, nullptr), "mcbgpu_solver_results");
+    check_gpu(mcbgpu_solver_results(s, j.sel.data(), N, &total, nullptr), "mcbgpu_solver_results");
     float gpu_ms = 0;
     cudaEventElapsedTime(&gpu_ms, a, b);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    const double t2 = now_s();
-
-    st.final_ = N;
-    st.total_weight = total;
-    st.total_mb = (double)mcbgpu_solver_device_bytes(s) / (1024.0 * 1024.0);
-    st.static_mb = (double)(sizeof(int32_t) * K + sizeof(int64_t) * (K + 1) + sizeof(int32_t) * off[K]) /
-                   (1024.0 * 1024.0);
-    st.variable_mb = st.total_mb - st.static_mb;
-    st.t_gpu = gpu_ms / 1000.0;
-    st.t_inspection = gpu_ms / 1000.0;
-    st.t_main = t2 - t1;
-    st.append(o.stats);
+    j.total = total;
+    j.st.t_gpu = j.st.t_inspection = gpu_ms / 1000.0;
+    j.st.t_main = now_s() - t1;
+    j.st.total_mb = (double)mcbgpu_solver_device_bytes(s) / (1024.0 * 1024.0);
     mcbgpu_solver_destroy(s);
+}
 
-    if (o.cycles || o.cycles_input) {
-        const int64_t e2 = info.reduced_edges2;
-        std::vector<uint32_t> rows(e2), cols(e2), rev(e2), ro(info.reduced_nodes + 1);
-        std::vector<int32_t> wts(e2), vmap(info.reduced_nodes);
-        check_host(mcbh_get_reduced_graph(p, rows.data(), cols.data(), wts.data(), rev.data(), ro.data()),
-                   "mcbh_get_reduced_graph");
-        check_host(mcbh_get_vertex_map(p, vmap.data()), "mcbh_get_vertex_map");
-        if (o.cycles) write_cycles(o.cycles, sel, root, edge, weight, rows, cols, nullptr);
-        if (o.cycles_input) {
-            if (input_ids)
-                for (auto &x : vmap) x = input_ids[x];
-            write_cycles(o.cycles_input, sel, root, edge, weight, rows, cols, vmap.data());
-        }
+// Several problems in one batched launch per size class.  The GPU time and the
+// main-loop time of the batch are shared out over its problems in proportion to N.
+void solve_batched(std::vector<Job *> &jobs) {
+    if (jobs.empty()) return;
+    init_gpu_once();
+    const double t1 = now_s();
+    std::vector<int32_t> N;
+    std::vector<int64_t> K, off{0};
+    std::vector<int32_t> weight, coords;
+    for (Job *j : jobs) {
+        const int64_t k = j->info.num_candidates, base = off.back();
+        N.push_back(j->info.num_coords);
+        K.push_back(k);
+        weight.insert(weight.end(), j->weight.begin(), j->weight.begin() + k);
+        for (int64_t r = 1; r <= k; r++) off.push_back(base + j->off[r]);
+        coords.insert(coords.end(), j->coords.begin(), j->coords.begin() + j->off[k]);
     }
-    return total;
+    mcbgpu_batch *b = nullptr;
+    check_gpu(mcbgpu_batch_create(&b, (int32_t)jobs.size(), N.data(), K.data(), off.back()), "mcbgpu_batch_create");
+    check_gpu(mcbgpu_batch_upload(b, weight.data(), off.data(), coords.data(), nullptr), "mcbgpu_batch_upload");
+    cudaEvent_t a, e;
+    cudaEventCreate(&a);
+    cudaEventCreate(&e);
+    cudaEventRecord(a, 0);
+    check_gpu(mcbgpu_batch_run(b, nullptr), "batched solve");
+    cudaEventRecord(e, 0);
+    int64_t nsum = 0;
+    for (int32_t n : N) nsum += n;
+    std::vector<int64_t> sel(nsum > 0 ? nsum : 1), tot(jobs.size());
+    check_gpu(mcbgpu_batch_results(b, sel.data(), tot.data(), nullptr, nullptr), "mcbgpu_batch_results");
+    float gpu_ms = 0;
+    cudaEventElapsedTime(&gpu_ms, a, e);
+    cudaEventDestroy(a);
+    cudaEventDestroy(e);
+    const double main_s = now_s() - t1, mb = (double)mcbgpu_batch_device_bytes(b) / (1024.0 * 1024.0);
+    mcbgpu_batch_destroy(b);
+    int64_t at = 0;
+    for (size_t i = 0; i < jobs.size(); i++) {
+        Job &j = *jobs[i];
+        const double share = nsum > 0 ? (double)N[i] / (double)nsum : 0.0;
+        j.sel.assign(sel.begin() + at, sel.begin() + at + N[i]);
+        at += N[i];
+        j.total = tot[i];
+        j.st.t_gpu = j.st.t_inspection = gpu_ms / 1000.0 * share;
+        j.st.t_main = main_s * share;
+        j.st.total_mb = mb * share;
+    }
+}
+
+// Appends the problem's stats row and its cycle blocks.
+void emit_job(Job &j, const Outputs &o) {
+    Stats &st = j.st;
+    if (!j.info.single_cycle) {
+        const int64_t K = j.info.num_candidates;
+        st.final_ = j.info.num_coords;
+        st.total_weight = j.total;
+        st.static_mb = (double)(sizeof(int32_t) * K + sizeof(int64_t) * (K + 1) +
+                                sizeof(int32_t) * (K > 0 ? j.off[K] : 0)) /
+                       (1024.0 * 1024.0);
+        st.variable_mb = st.total_mb > st.static_mb ? st.total_mb - st.static_mb : 0.0;
+    }
+    st.append(o.stats);
+    if (j.info.single_cycle || !(o.cycles || o.cycles_input)) return;
+    const int64_t e2 = j.info.reduced_edges2;
+    std::vector<uint32_t> rows(e2), cols(e2), rev(e2), ro(j.info.reduced_nodes + 1);
+    std::vector<int32_t> wts(e2), vmap(j.info.reduced_nodes);
+    check_host(mcbh_get_reduced_graph(j.p, rows.data(), cols.data(), wts.data(), rev.data(), ro.data()),
+               "mcbh_get_reduced_graph");
+    check_host(mcbh_get_vertex_map(j.p, vmap.data()), "mcbh_get_vertex_map");
+    if (o.cycles) write_cycles(o.cycles, j.sel, j.root, j.edge, j.weight, rows, cols, nullptr);
+    if (o.cycles_input) {
+        if (!j.ids.empty())
+            for (auto &x : vmap) x = j.ids[x];
+        write_cycles(o.cycles_input, j.sel, j.root, j.edge, j.weight, rows, cols, vmap.data());
+    }
 }
 
 }  // namespace
@@ -240,11 +317,14 @@ int main(int argc, char **argv) {
     long long total = 0;
     int solved = 0;
     if (!bcc) {
-        mcbh_problem *p = nullptr;
-        check_host(mcbh_problem_from_mtx(input, &p), "cannot read the input graph");
-        total = solve_one(p, o, nullptr);
+        Job j;
+        check_host(mcbh_problem_from_mtx(input, &j.p), "cannot read the input graph");
+        prepare_job(j, o);
+        if (needs_gpu(j)) solve_single(j, o);
+        emit_job(j, o);
+        total = j.total;
         solved = 1;
-        mcbh_problem_free(p);
+        mcbh_problem_free(j.p);
     } else {
         int32_t nodes = 0;
         const int64_t m = mcbh_read_mtx(input, &nodes, 0, nullptr, nullptr, nullptr);
@@ -262,6 +342,8 @@ int main(int argc, char **argv) {
         std::vector<int64_t> order(m > 0 ? m : 1), fill(start.begin(), start.end() - 1);
         for (int64_t i = 0; i < m; i++) order[fill[comp[i]]++] = i;
         std::vector<int32_t> local(nodes, -1);
+        std::vector<Job> jobs;
+        jobs.reserve(nc);
         for (int64_t c = 0; c < nc; c++) {
             std::vector<int32_t> cu, cv, cw, ids;
             for (int64_t k = start[c]; k < start[c + 1]; k++) {
@@ -277,13 +359,30 @@ int main(int argc, char **argv) {
             }
             for (int32_t x : ids) local[x] = -1;
             if ((int64_t)cu.size() < (int64_t)ids.size()) continue;  // a bridge: no cycle
-            mcbh_problem *p = nullptr;
+            jobs.emplace_back();
+            Job &j = jobs.back();
+            j.ids = ids;
             check_host(mcbh_problem_from_edges((int32_t)ids.size(), (int64_t)cu.size(), cu.data(), cv.data(),
-                                               cw.data(), &p),
+                                               cw.data(), &j.p),
                        "component");
-            total += solve_one(p, o, ids.data());
+            prepare_job(j, o);
+        }
+        // every component that fits the batch in one batched launch per size class
+        // (the per-iteration form with --plain), the rest on the single-problem solver
+        std::vector<Job *> batch;
+        for (Job &j : jobs) {
+            if (!needs_gpu(j)) continue;
+            if (!o.plain && j.info.num_coords <= mcbgpu_batch_max_coords())
+                batch.push_back(&j);
+            else
+                solve_single(j, o);
+        }
+        solve_batched(batch);
+        for (Job &j : jobs) {
+            emit_job(j, o);
+            total += j.total;
             solved++;
-            mcbh_problem_free(p);
+            mcbh_problem_free(j.p);
         }
     }
     if (o.cycles) {
