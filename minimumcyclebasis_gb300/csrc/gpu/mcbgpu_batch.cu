@@ -35,6 +35,12 @@ namespace {
 
 constexpr int kBThreads = 512;
 constexpr int kBWarps = kBThreads / 32;
+#ifndef MCB_BATCH_Q0
+#define MCB_BATCH_Q0 2  // candidates per thread per scan round, problems with N <= 1024
+#endif
+#ifndef MCB_BATCH_Q
+#define MCB_BATCH_Q 4   // the same for the larger classes
+#endif
 #ifndef MCB_BATCH_CHUNK
 #define MCB_BATCH_CHUNK 4
 #endif
@@ -125,7 +131,10 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
     __shared__ uint64_t sNewRes, sNewW;
     __shared__ int sGi;
     __shared__ unsigned sFail;
-    __shared__ long long pc[6];  // profile (thread 0): cycles in T, scan, resolve, final rows, update; scanned
+    // profile (thread 0): cycles in T, scan, resolve, final rows, update; candidates
+    // scanned; cycles of the scan's list walks; pivot rounds; cycles of warp 0 in the
+    // update's D + beta and in its row writes
+    __shared__ long long pc[10];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned full = 0xffffffffu;
@@ -170,7 +179,7 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
         if (prof && tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
         if (tid == 0) {
             sFail = 0;
-            for (int q = 0; q < 6; q++) pc[q] = 0;
+            for (int q = 0; q < 10; q++) pc[q] = 0;
         }
         cta_sync();
 
@@ -214,6 +223,8 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
                     break;
                 }
                 // thread tid holds ranks base + tid * kBQ + q: key tid * kBQ + q is rank order
+                const long long cw = prof ? clock64() : 0;
+                bool first_round = true;
                 uint64_t W[kBQ], res[kBQ];
                 w_smem_q<kBQ>(base + (long long)tid * kBQ, K, cand, off, coords, T, bound, W);
 #pragma unroll
@@ -235,6 +246,11 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
                         sWmin[warp] = 0x7fffffff;
                     }
                     cta_sync();
+                    if (prof && tid == 0) {
+                        if (first_round) pc[6] += clock64() - cw;
+                        pc[7]++;
+                    }
+                    first_round = false;
                     int best = 0x7fffffff;
 #pragma unroll
                     for (int q = 0; q < kBWarps; q++) best = min(best, sWmin[q]);
@@ -404,6 +420,7 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
             // buffer, beta = D_j x Mrow, then S_j ^= XOR_{k in beta} F_k.
             uint64_t *rowbuf = T + (size_t)warp * wcap;
             for (int j = bound + warp; j < N; j += kBWarps) {
+                const long long cu0 = prof ? clock64() : 0;
                 uint64_t *Sj = Sg + (size_t)j * P;
                 uint64_t v[kRowRegs];
 #pragma unroll
@@ -426,6 +443,8 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
                 if ((D >> (lane + 32)) & 1) beta ^= sMrow[lane + 32];
 #pragma unroll
                 for (int d = 16; d > 0; d >>= 1) beta ^= shfl_xor64(beta, d);
+                const long long cu1 = prof ? clock64() : 0;
+                if (prof && tid == 0) pc[8] += cu1 - cu0;
                 if (beta) {
 #pragma unroll
                     for (int i = 0; i < kRowRegs; i++) {
@@ -437,6 +456,7 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
                         }
                     }
                 }
+                if (prof && tid == 0) pc[9] += clock64() - cu1;
                 __syncwarp();
             }
             if (tid == 0)
@@ -459,10 +479,14 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
             asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
             unsigned smid;
             asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-            long long *o = prof + (size_t)gx * 8;
+            long long *o = prof + (size_t)gx * 12;
             o[0] = (long long)(t_end - t_start);
             for (int q = 0; q < 6; q++) o[1 + q] = pc[q];
             o[7] = smid;
+            o[8] = pc[6];
+            o[9] = pc[7];
+            o[10] = pc[8];
+            o[11] = pc[9];
         }
     }
 }
@@ -542,9 +566,9 @@ using BatchKernel = void (*)(const BatchGraph *, const int *, int, unsigned *, c
 // update = kClassMaxN[c] / 2048, rounded up).
 BatchKernel class_kernel(int c) {
     switch (c) {
-        case 0: return batch_solve_kernel<2, 1, 2>;
-        case 1: return batch_solve_kernel<4, 2, 1>;
-        default: return batch_solve_kernel<4, (kBatchMaxN / 64 + 31) / 32, 1>;
+        case 0: return batch_solve_kernel<MCB_BATCH_Q0, 1, 2>;
+        case 1: return batch_solve_kernel<MCB_BATCH_Q, 2, 1>;
+        default: return batch_solve_kernel<MCB_BATCH_Q, (kBatchMaxN / 64 + 31) / 32, 1>;
     }
 }
 
@@ -795,8 +819,8 @@ int mcbgpu_batch_set_profiling(mcbgpu_batch *b, int enable) {
         return MCBGPU_E_ARG;
     }
     if (enable && !b->d_prof) {
-        MCB_CUDA(cudaMalloc((void **)&b->d_prof, sizeof(long long) * 8 * (size_t)std::max(b->count, 1)));
-        MCB_CUDA(cudaMemset(b->d_prof, 0, sizeof(long long) * 8 * (size_t)std::max(b->count, 1)));
+        MCB_CUDA(cudaMalloc((void **)&b->d_prof, sizeof(long long) * 12 * (size_t)std::max(b->count, 1)));
+        MCB_CUDA(cudaMemset(b->d_prof, 0, sizeof(long long) * 12 * (size_t)std::max(b->count, 1)));
     } else if (!enable && b->d_prof) {
         MCB_CUDA(cudaFree(b->d_prof));
         b->d_prof = nullptr;
@@ -810,7 +834,7 @@ int mcbgpu_batch_profile(mcbgpu_batch *b, int64_t *out) {
         return MCBGPU_E_ARG;
     }
     MCB_CUDA(cudaDeviceSynchronize());
-    MCB_CUDA(cudaMemcpy(out, b->d_prof, sizeof(long long) * 8 * (size_t)b->count, cudaMemcpyDeviceToHost));
+    MCB_CUDA(cudaMemcpy(out, b->d_prof, sizeof(long long) * 12 * (size_t)b->count, cudaMemcpyDeviceToHost));
     return MCBGPU_OK;
 }
 

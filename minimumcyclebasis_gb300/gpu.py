@@ -304,8 +304,9 @@ class BatchSolver:
         check_gpu(self.lib.mcbgpu_batch_set_profiling(self._h, int(enable)), "mcbgpu_batch_set_profiling")
 
     def profile(self) -> np.ndarray:
-        """Per problem: [ns, cycles in T, scan, resolve, final rows, update, candidates scanned, SM]."""
-        out = np.zeros((max(self.count, 1), 8), np.int64)
+        """Per problem: [ns, cycles in T, scan, resolve, final rows, update, candidates scanned, SM,
+        cycles of the scan's list walks, pivot rounds, warp 0's update cycles in D + beta, in row writes]."""
+        out = np.zeros((max(self.count, 1), 12), np.int64)
         check_gpu(self.lib.mcbgpu_batch_profile(self._h, ptr(out)), "mcbgpu_batch_profile")
         return out[: self.count]
 
