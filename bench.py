@@ -133,6 +133,17 @@ def dist_setup(args):
     return world, rank, local, pg
 
 
+def max_over_ranks(x, pg):
+    """The largest of every rank's `x` (the slowest rank's time), on every rank."""
+    if not pg:
+        return x
+    import torch
+    dev = "cuda" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def prepare(args, keep_trees):
     from minimumcyclebasis_gb300 import Problem, random_graph
     t0 = time.time()
@@ -261,9 +272,7 @@ def run_gpu(args, world, rank, local, pg):
     stats = solver.kernel_stats()
     solver.set_profiling(False)
     if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, pg)
         pg.barrier()
 
     # end to end through the C ABI with pinned host buffers
@@ -398,9 +407,7 @@ def run_batch(args, world, rank, local, pg):
     launches = bs.launches - launches0
     ms_blocks = timed(bb)
     if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, pg)
 
     # the plain GPU form: one blocked single-problem solver per problem, in sequence,
     # on every `plain_stride`-th problem (extrapolated to all)
@@ -506,7 +513,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--n", type=int, default=50000, help="graph vertices (edges = 2n)")
+    ap.add_argument("--n", "--vertices", dest="n", type=int, default=50000, help="graph vertices (edges = 2n)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--mode", choices=["blocked", "plain"], default="blocked")
     ap.add_argument("--max-iterations", type=int, default=-1)
