@@ -58,6 +58,12 @@ constexpr unsigned kSpinLimit = 1u << 24;
 #ifndef MCB_OTF_PAIRS
 #define MCB_OTF_PAIRS 1  // pivot kernel: walk two candidates per thread together on the fly
 #endif
+#ifndef MCB_PAIR
+#define MCB_PAIR 1  // one streaming pass per two blocks (the second block's W by blk_wfix_kernel)
+#endif
+#ifndef MCB_PAIR_MARGIN
+#define MCB_PAIR_MARGIN 5  // percent more tiles in a paired streaming pass
+#endif
 #ifndef MCB_UPD_SPLIT
 #define MCB_UPD_SPLIT 1  // warps per row group in the block update (1, 2, 4 or 8)
 #endif
@@ -86,11 +92,11 @@ constexpr unsigned kNoIndex = 0xFFFFFFFFu;
 // Kernel classes for the optional per-launch profile (events + algorithmic bytes).
 enum KernelClass {
     KC_INIT, KC_TILE_MINC, KC_TRANSPOSE, KC_WSTREAM, KC_PIVOT,
-    KC_BLK_UPDATE, KC_SEARCH, KC_UPDATE, KC_CYCLE, KC_RESET, KC_VALIDATE, KC_COUNT
+    KC_BLK_UPDATE, KC_SEARCH, KC_UPDATE, KC_CYCLE, KC_RESET, KC_VALIDATE, KC_WFIX, KC_COUNT
 };
 const char *const kKernelNames[KC_COUNT] = {
     "init_identity", "tile_minc", "blk_transpose", "blk_w", "blk_pivot", "blk_update", "search", "update",
-    "cycle_vector", "reset_state", "validate"};
+    "cycle_vector", "reset_state", "validate", "blk_wfix"};
 
 struct IterSlot {            // state of one per-iteration search
     unsigned long long best; // first odd rank (kNone until found)
@@ -105,6 +111,7 @@ struct BlockState {
     long long max_tile;            // deepest tile the previous block's pivot search touched
     unsigned long long total;      // running 64-bit total weight of the basis
     unsigned tail_ok, pad_;        // the pivot kernel's CTA 0 resolved the block
+    long long pair_tiles;          // tiles the paired streaming pass computed for the next block
     long long pivrank[64];
     unsigned long long pivW[64];   // the pivots' W as found (not reduced)
     unsigned long long mask[64];   // final S_{e0+k} as a combination of S^0_{e0+l}
@@ -301,9 +308,43 @@ __global__ void cycle_vector_kernel(uint64_t *C, int W, const int64_t *__restric
 //
 // blk_transpose_kernel: T[64w + i] bit k = S[e0+k] bit (64w+i), for w < Wb.
 // One warp per word column; also resets the block state (runs first in the block).
+// With b2 > 0 (a paired block) also T12[c] = {T[c], T2[c]} for the paired streaming
+// pass, T2[64w + i] bit k = S[e0+64+k] bit (64w+i), w < Wb2: the next block's b2
+// rows as they are now.
+// Writes T[64w + i] (T may be NULL) and, with T12, the same into T12[2(64w + i) + half].
+__device__ __forceinline__ void transpose_rows(const uint64_t *__restrict__ S, int P, int r0, int b, int Wb,
+                                               uint64_t *__restrict__ T, uint64_t *__restrict__ T12, int half) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < Wb; w += warps) {
+        uint64_t lo = lane < b ? S[(size_t)(r0 + lane) * P + w] : 0ull;
+        uint64_t hi = (32 + lane) < b ? S[(size_t)(r0 + 32 + lane) * P + w] : 0ull;
+        uint64_t a = 0, c = 0;
+        for (int i = 0; i < 64; i++) {
+            unsigned blo = __ballot_sync(0xffffffffu, (unsigned)(lo >> i) & 1u);
+            unsigned bhi = __ballot_sync(0xffffffffu, (unsigned)(hi >> i) & 1u);
+            uint64_t v = (uint64_t)blo | ((uint64_t)bhi << 32);
+            if (i < 32) {
+                if (lane == i) a = v;
+            } else {
+                if (lane == i - 32) c = v;
+            }
+        }
+        if (T) {
+            T[(size_t)w * 64 + lane] = a;
+            T[(size_t)w * 64 + 32 + lane] = c;
+        }
+        if (T12) {
+            T12[2 * ((size_t)w * 64 + lane) + half] = a;
+            T12[2 * ((size_t)w * 64 + 32 + lane) + half] = c;
+        }
+    }
+}
+
 __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int e0, int b, int Wb,
                                      uint64_t *__restrict__ T, BlockState *bs, long long ntiles,
-                                     GridBar *gb, long long window_tiles) {
+                                     GridBar *gb, long long window_tiles, uint64_t *__restrict__ T12, int b2,
+                                     int Wb2) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         gb->count = 0;
         gb->abort = 0;
@@ -318,28 +359,13 @@ __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int 
             const long long a = (lp + lp / 4) / kTile + 1, m = bs->max_tile + 1;
             pred = (a > m ? a : m) + window_tiles;
         }
+        if (b2 > 0 && e0 != 0) pred += pred * MCB_PAIR_MARGIN / 100;  // the pass serves the next block too
         bs->pred_tiles = pred < ntiles ? pred : ntiles;
+        if (b2 > 0) bs->pair_tiles = bs->pred_tiles;  // read by the next block's blk_wfix_kernel
         bs->max_tile = 0;
     }
-    const int lane = threadIdx.x & 31;
-    const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < Wb; w += warps) {
-        uint64_t lo = lane < b ? S[(size_t)(e0 + lane) * P + w] : 0ull;
-        uint64_t hi = (32 + lane) < b ? S[(size_t)(e0 + 32 + lane) * P + w] : 0ull;
-        uint64_t a = 0, c = 0;
-        for (int i = 0; i < 64; i++) {
-            unsigned blo = __ballot_sync(0xffffffffu, (unsigned)(lo >> i) & 1u);
-            unsigned bhi = __ballot_sync(0xffffffffu, (unsigned)(hi >> i) & 1u);
-            uint64_t v = (uint64_t)blo | ((uint64_t)bhi << 32);
-            if (i < 32) {
-                if (lane == i) a = v;
-            } else {
-                if (lane == i - 32) c = v;
-            }
-        }
-        T[(size_t)w * 64 + lane] = a;
-        T[(size_t)w * 64 + 32 + lane] = c;
-    }
+    transpose_rows(S, P, e0, b, Wb, T, b2 > 0 ? T12 : nullptr, 0);
+    if (b2 > 0) transpose_rows(S, P, e0 + 64, b2, Wb2, nullptr, T12, 1);
 }
 
 // Reduce W by the basis held as Four-Russians tables: tab[g][pat] = XOR of the basis
@@ -505,20 +531,79 @@ __device__ __forceinline__ void w_of_two(long long ra, long long rb, const int64
     }
 }
 
+// W of one candidate for two blocks at once: W (rows of this block, coordinates
+// below bound) and W2 (the next block's rows as they are now, below bound2 >=
+// bound), one walk of the list; T12[c] = {T[c], T2[c]} (one 16-byte gather).
+__device__ __forceinline__ void w_of_candidate2(long long r, const int64_t *__restrict__ off,
+                                                const int32_t *__restrict__ coords,
+                                                const ulonglong2 *__restrict__ T12, int bound, int bound2,
+                                                unsigned &nread, uint64_t &W, uint64_t &W2) {
+    int64_t i = __ldg(off + r);
+    const int64_t e = __ldg(off + r + 1);
+    W = 0;
+    W2 = 0;
+    while (i < e) {
+        int cv[kWChunk];
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) cv[q] = i + q < e ? __ldg(coords + i + q) : 0x7fffffff;
+        uint64_t tv[kWChunk], tv2[kWChunk];
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) {
+            const ulonglong2 t = cv[q] < bound2 ? __ldg(T12 + cv[q]) : make_ulonglong2(0ull, 0ull);
+            tv[q] = cv[q] < bound ? t.x : 0ull;
+            tv2[q] = t.y;
+        }
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) {
+            W ^= tv[q];
+            W2 ^= tv2[q];
+        }
+        nread += (unsigned)(e - i < kWChunk ? e - i : kWChunk);
+        if (cv[kWChunk - 1] >= bound2) break;
+        i += kWChunk;
+    }
+}
+
 // Streaming pass: W for tiles [0, bs->pred_tiles), one candidate per thread (1024
 // threads = one tile per CTA pass), written to Warr and tagged with the block's
 // epoch.  This is the bandwidth-bound part of the block's search.
 #ifndef MCB_W_MINB
 #define MCB_W_MINB 1  // resident 1024-thread CTAs per SM the W pass is compiled for
 #endif
+// kPaired: also W2 of the next block (T2, bound2) into Warr2, for blk_wfix_kernel.
+template <bool kPaired>
 __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, const int64_t *__restrict__ off,
                                                     const int32_t *__restrict__ coords,
                                                     const int32_t *__restrict__ tile_minc,
                                                     const uint64_t *__restrict__ T, int bound, const BlockState *bs,
-                                                    uint64_t *Warr, unsigned *tile_epoch, unsigned long long *bytes) {
+                                                    uint64_t *Warr, unsigned *tile_epoch, unsigned long long *bytes,
+                                                    const ulonglong2 *__restrict__ T12, int bound2, uint64_t *Warr2) {
     const unsigned epoch = bs->epoch;
     const long long ntiles = bs->pred_tiles;
     unsigned long long nb = (blockIdx.x == 0 && threadIdx.x == 0) ? 8ull * (unsigned long long)bound : 0ull;
+    if (kPaired) {
+        for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            if (tile_minc[t] >= bound2) {  // both W's of the tile are 0
+                if (threadIdx.x == 0) nb += 8;
+                continue;
+            }
+            const long long r = t * kTile + threadIdx.x;
+            uint64_t W = 0, W2 = 0;
+            unsigned nread = 0;
+            if (r < K) {
+                w_of_candidate2(r, off, coords, T12, bound, bound2, nread, W, W2);
+                nb += 8 + 16 + 4ull * nread;  // offset, two W writes, coordinates read
+            }
+            Warr[r] = W;
+            Warr2[r] = W2;
+        }
+        for (long long t = blockIdx.x + (long long)threadIdx.x * gridDim.x; t < ntiles;
+             t += (long long)blockDim.x * gridDim.x)
+            tile_epoch[t] = (epoch << 1) | (tile_minc[t] >= bound ? 1u : 0u);
+        for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
+        if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
+        return;
+    }
     // no barrier per tile: a thread moves on to its next tile as soon as its own
     // candidate is done; the tags (read only by the next kernel) are written at the end
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -539,6 +624,81 @@ __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, c
         tile_epoch[t] = (epoch << 1) | (tile_minc[t] >= bound ? 1u : 0u);
     for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
     if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
+}
+
+// The second block of a pair: W of every candidate the paired pass covered, from
+// the two W's it wrote.  Warr2 holds W against this block's rows as they were
+// before the previous block's update; the update added to row i (S_{e1+i}) the
+// combination gamma_i = XOR_{k in beta_i} m_k of the previous block's starting
+// rows (beta_i: the row's update bits, m_k: the previous block's final masks), so
+// bit i of W gains parity(Wprev & gamma_i), with Wprev = the previous block's W
+// (Warr).  That 64x64 GF(2) product is applied through eight 256-entry tables.
+__global__ void __launch_bounds__(kTile) blk_wfix_kernel(const int32_t *__restrict__ tile_minc, int bound,
+                                                         const BlockState *bs, const uint64_t *__restrict__ beta,
+                                                         int b, int bprev, uint64_t *Warr,
+                                                         const uint64_t *__restrict__ Warr2, unsigned *tile_epoch,
+                                                         unsigned long long *bytes) {
+    __shared__ uint64_t s_m[64], s_g[64], s_col[64];
+    __shared__ uint64_t s_tab[8][256];
+    const unsigned epoch = bs->epoch;
+    const long long ntiles = bs->pair_tiles;
+    const int tid = threadIdx.x;
+    if (tid < 64) s_m[tid] = tid < bprev ? bs->mask[tid] : 0ull;
+    cta_sync();
+    if (tid < 64) {
+        uint64_t g = 0;
+        if (tid < b)
+            for (uint64_t bb = beta[tid]; bb; bb &= bb - 1) g ^= s_m[__ffsll((long long)bb) - 1];
+        s_g[tid] = g;
+    }
+    cta_sync();
+    if (tid < 64) {  // col_t bit i = bit t of gamma_i: a 64x64 bit transpose by ballots (warps 0, 1)
+        const int lane = tid & 31, half = tid >> 5;
+        const uint64_t g0 = s_g[lane], g1 = s_g[lane + 32];
+        for (int t = half * 32; t < half * 32 + 32; t++) {
+            const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(g0 >> t) & 1u);
+            const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(g1 >> t) & 1u);
+            if (lane == (t & 31)) s_col[t] = (uint64_t)lo | ((uint64_t)hi << 32);
+        }
+    }
+    if (tid < 8) s_tab[tid][0] = 0;
+    cta_sync();
+    // tab[g][v] for v in [2^u, 2^(u+1)) = tab[g][v - 2^u] ^ col[8g + u]
+    for (int u = 0; u < 8; u++) {
+        const int n = 8 << u;  // 8 groups x 2^u entries
+        for (int idx = tid; idx < n; idx += blockDim.x) {
+            const int grp = idx >> u, v = (1 << u) + (idx & ((1 << u) - 1));
+            s_tab[grp][v] = s_tab[grp][v - (1 << u)] ^ s_col[grp * 8 + u];
+        }
+        cta_sync();
+    }
+    unsigned long long nb = 0;
+    // four tiles per pass: their loads are in flight together
+    constexpr int kU = 4;
+    for (long long t0 = blockIdx.x; t0 < ntiles; t0 += (long long)kU * gridDim.x) {
+        uint64_t w[kU], x[kU];
+        bool live[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const long long t = t0 + (long long)u * gridDim.x;
+            live[u] = t < ntiles && tile_minc[t] < bound;  // else W = 0 for the whole tile: tagged below
+            const long long r = t * kTile + tid;
+            w[u] = live[u] ? Warr[r] : 0ull;
+            x[u] = live[u] ? Warr2[r] : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            if (!live[u]) continue;
+#pragma unroll
+            for (int grp = 0; grp < 8; grp++) x[u] ^= s_tab[grp][(w[u] >> (8 * grp)) & 255];
+            Warr[(t0 + (long long)u * gridDim.x) * kTile + tid] = x[u];
+            nb += 24;
+        }
+    }
+    for (long long t = blockIdx.x + (long long)tid * gridDim.x; t < ntiles; t += (long long)blockDim.x * gridDim.x)
+        tile_epoch[t] = (epoch << 1) | (tile_minc[t] >= bound ? 1u : 0u);
+    for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
+    if ((tid & 31) == 0 && nb) atomicAdd(bytes, nb);
 }
 
 // Cooperative pivot extraction, several pivots per grid barrier.
@@ -1386,7 +1546,7 @@ __global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, lo
                                                                  const uint64_t *__restrict__ gcol,
                                                                  const unsigned *__restrict__ pairs,
                                                                  const unsigned *__restrict__ word_end,
-                                                                 unsigned long long *bytes) {
+                                                                 unsigned long long *bytes, uint64_t *beta_out) {
     unsigned long long nb = 0;
     __shared__ uint64_t sg[64];
     __shared__ uint64_t sD[2][kUpdGroups][kUpdSplit][kUpdRows];
@@ -1436,6 +1596,7 @@ __global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, lo
             // group's pairs touch (8 rows share each pair, counted once per row) plus,
             // when the row changes, read + write of its first Wb words
             if (h == 0) nb += 8ull * np + (beta ? 16ull * (unsigned long long)Wb : 0ull);
+            if (beta_out && h == 0) beta_out[g0 - row_begin + lane] = beta;  // the next block's rows (paired pass)
         }
         for (int r = 0; r < rows; r++) {
             const uint64_t bt = __shfl_sync(0xffffffffu, beta, r);
@@ -1473,6 +1634,9 @@ struct mcbgpu_solver {
     uint64_t *d_T = nullptr;       // 64 * P words
     uint64_t *d_tab = nullptr;     // 8 * 256 * P words
     uint64_t *d_Warr = nullptr;    // W per candidate (tiles * 1024)
+    uint64_t *d_Warr2 = nullptr;   // a paired pass's W against the next block's rows
+    uint64_t *d_T12 = nullptr;     // {this block's, the next block's} rows transposed (paired pass)
+    uint64_t *d_beta = nullptr;    // 64 update bits of the next block's rows (paired pass)
     unsigned *d_tile_epoch = nullptr;
     int32_t *d_tile_minc = nullptr;
     unsigned long long *d_reports = nullptr;  // two step parities of G x (2 kLmax + 2) words
@@ -1553,6 +1717,9 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_T);
     cudaFree(s->d_tab);
     cudaFree(s->d_Warr);
+    cudaFree(s->d_Warr2);
+    cudaFree(s->d_T12);
+    cudaFree(s->d_beta);
     cudaFree(s->d_tile_epoch);
     cudaFree(s->d_tile_minc);
     cudaFree(s->d_reports);
@@ -1632,6 +1799,11 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_T, sizeof(uint64_t) * 64 * (size_t)s->P);
     ALLOC(s->d_tab, sizeof(uint64_t) * 2 * 8 * 256 * (size_t)s->P);
     ALLOC(s->d_Warr, sizeof(uint64_t) * (size_t)kTile * ntiles);
+    if (MCB_PAIR) {
+        ALLOC(s->d_Warr2, sizeof(uint64_t) * (size_t)kTile * ntiles);
+        ALLOC(s->d_T12, sizeof(uint64_t) * 2 * 64 * (size_t)s->P);
+        ALLOC(s->d_beta, sizeof(uint64_t) * 64);
+    }
     ALLOC(s->d_tile_epoch, sizeof(unsigned) * ntiles);
     ALLOC(s->d_tile_minc, sizeof(int32_t) * ntiles);
     ALLOC(s->d_gbar, sizeof(GridBar));
@@ -1874,23 +2046,45 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
     // word_end) alternate by block parity.
     MCB_CUDA(cudaEventRecord(s->ev_fork, st));
     MCB_CUDA(cudaStreamWaitEvent(s->st2, s->ev_fork, 0));
-    bool far_pending = false;
+    bool far_pending = false, far_rec[2] = {false, false};
     int far_par = 0;
+    // Blocks in pairs (MCB_PAIR): the first block's streaming pass also computes W
+    // against the second block's rows as they are before the first block's update;
+    // the second block corrects those W's (blk_wfix_kernel) instead of streaming the
+    // lists again.  So the second block's rows must be final up to the block before
+    // the pair when the pair starts: the second block of a pair updates the next
+    // 128 rows on `st`, not 64.
     for (int64_t e0 = 0; e0 < iters; e0 += 64) {
         const int b = (int)std::min<int64_t>(64, iters - e0);
         const int par = (int)((e0 / 64) & 1);
         const int Wb = (int)((e0 + b + 63) / 64);
         const int bound = (int)(e0 + b);
+        const bool lead = MCB_PAIR && par == 0 && e0 + 64 < iters;  // first block of a pair
+        const bool follow = MCB_PAIR && par == 1;                     // second block of a pair
+        const int b2 = lead ? (int)std::min<int64_t>(64, iters - e0 - 64) : 0;
+        const int bound2 = (int)(e0 + 64 + b2);
+        const int Wb2 = lead ? (bound2 + 63) / 64 : 0;
         {
             Launch L(s, KC_TRANSPOSE, st);
-            blk_transpose_kernel<<<(Wb + 7) / 8, 256, 0, st>>>(s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles,
-                                                              s->d_gbar,
-                                                              (long long)s->pivot_grid * kWinTiles);
+            blk_transpose_kernel<<<(std::max(Wb, Wb2) + 7) / 8, 256, 0, st>>>(
+                s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles, s->d_gbar, (long long)s->pivot_grid * kWinTiles,
+                s->d_T12, b2, Wb2);
         }
-        if (ntiles > 0) {
+        if (ntiles > 0 && follow) {
+            Launch L(s, KC_WFIX, st);
+            blk_wfix_kernel<<<sms, kTile, 0, st>>>(s->d_tile_minc, bound, s->d_bs, s->d_beta, b, 64, s->d_Warr,
+                                                       s->d_Warr2, s->d_tile_epoch, L.bytes());
+        } else if (ntiles > 0 && lead) {
             Launch L(s, KC_WSTREAM, st);
-            blk_w_kernel<<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
-                                                    s->d_bs, s->d_Warr, s->d_tile_epoch, L.bytes());
+            blk_w_kernel<true><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                                                          s->d_bs, s->d_Warr, s->d_tile_epoch, L.bytes(),
+                                                          reinterpret_cast<const ulonglong2 *>(s->d_T12), bound2,
+                                                          s->d_Warr2);
+        } else if (ntiles > 0) {
+            Launch L(s, KC_WSTREAM, st);
+            blk_w_kernel<false><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                                                           s->d_bs, s->d_Warr, s->d_tile_epoch, L.bytes(), nullptr, 0,
+                                                           nullptr);
         }
         {
             Launch L(s, KC_PIVOT, st);
@@ -1927,7 +2121,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                                                  args, pivot_smem_bytes(s->pivot_grid), st));
         }
         if (e0 + b < s->N) {
-            const long long near_end = std::min<long long>(e0 + b + 64, s->N), far_end = s->N;
+            const long long near_end = std::min<long long>(e0 + b + (follow ? 128 : 64), s->N), far_end = s->N;
             const uint64_t *tab = s->d_tab + (size_t)par * 8 * 256 * s->P;
             const uint64_t *gcol = reinterpret_cast<const uint64_t *>(&s->d_bs->gcol[par][0]);
             const unsigned *pairs = s->d_pairs + (size_t)(1 + par) * s->pair_cap;
@@ -1941,17 +2135,26 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 MCB_CUDA(cudaStreamWaitEvent(s->st2, s->ev_tail, 0));
                 Launch L(s, KC_BLK_UPDATE, s->st2);
                 blk_update_kernel<<<grid_for(far_end - near_end), kUpdThreads, 0, s->st2>>>(
-                    s->d_S, near_end, far_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes());
+                    s->d_S, near_end, far_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes(), nullptr);
             }
-            if (far_pending) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[far_par], 0));
+            // the near rows wait for the last far update that covers them: the previous
+            // block's, except in the first block of a pair, whose near rows (the second
+            // block's) the previous block's far update does not reach (it starts 128
+            // rows on), so that block waits for the far update before it
+            if (lead && far_rec[par])
+                MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[par], 0));
+            else if (!lead && far_pending)
+                MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[far_par], 0));
             {
                 Launch L(s, KC_BLK_UPDATE, st);
                 blk_update_kernel<<<grid_for(near_end - (e0 + b)), kUpdThreads, 0, st>>>(
-                    s->d_S, e0 + b, near_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes());
+                    s->d_S, e0 + b, near_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes(),
+                    lead ? s->d_beta : nullptr);
             }
             far_pending = near_end < far_end;
             if (far_pending) {
                 far_par = par;
+                far_rec[par] = true;
                 MCB_CUDA(cudaEventRecord(s->ev_upd[par], s->st2));
             }
         }

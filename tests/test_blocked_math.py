@@ -148,3 +148,81 @@ def test_batch_formulation_equals_sequential(graph):
     p = Problem.from_graph(graph).prepare(threads=2, keep_trees=True)
     ref, _, _ = oracle.solve(p, threads=2)
     assert batch_select(p) == ref.tolist()
+
+
+def test_paired_pass_correction_identity():
+    """W of a candidate against block B+1's rows after block B's update equals its W
+    against those rows before the update, plus parity(W_B & gamma_i) in bit i, with
+    gamma_i = XOR of block B's final masks m_k over the update bits beta_i of row i
+    (the correction blk_wfix_kernel applies)."""
+    p = Problem.from_graph(random_graph(200, 400, 1, 20, 2)).prepare(threads=2, keep_trees=True)
+    N, K = p.N, p.K
+    off, co = p.cycle_lists()
+    lists = [co[off[r]:off[r + 1]].tolist() for r in range(K)]
+    S = [1 << j for j in range(N)]
+    dot = lambda s, r: sum((s >> c) & 1 for c in lists[r]) & 1  # noqa: E731
+    Wof = lambda rows, r: sum(dot(rows[i], r) << i for i in range(len(rows)))  # noqa: E731
+    checked = 0
+    for e0 in range(0, N, 64):
+        b = min(64, N - e0)
+        W0 = {}
+        if e0 + 64 < N:
+            nxt = S[e0 + 64:e0 + 128]
+            W0 = {r: Wof(nxt, r) for r in range(0, K, 7)}
+        WB = {r: Wof(S[e0:e0 + b], r) for r in W0}
+        # the block as in blocked_select
+        echelon, piv = {}, []
+        for r in range(K):
+            W = Wof(S[e0:e0 + b], r)
+            x = W
+            while x:
+                q = (x & -x).bit_length() - 1
+                if q in echelon:
+                    x ^= echelon[q]
+                else:
+                    echelon[q] = x
+                    piv.append((r, W))
+                    break
+            if len(piv) == b:
+                break
+        m = [1 << k for k in range(b)]
+        g, chosen, used = [], [], set()
+        for k in range(b):
+            q = next(i for i in range(b) if i not in used and parity(piv[i][1] & m[k]))
+            used.add(q)
+            chosen.append(q)
+            g.append(sum(parity(piv[q][1] & m[i]) << i for i in range(k)))
+            for j in range(k + 1, b):
+                if parity(piv[q][1] & m[j]):
+                    m[j] ^= m[k]
+        S0 = [S[e0 + l] for l in range(b)]
+        for k in range(b):
+            S[e0 + k] = 0
+            for l in range(b):
+                if (m[k] >> l) & 1:
+                    S[e0 + k] ^= S0[l]
+        betas = []
+        for j in range(e0 + b, N):
+            D = sum(dot(S[j], piv[chosen[k]][0]) << k for k in range(b))
+            beta = 0
+            for k in range(b):
+                beta |= (((D >> k) & 1) ^ parity(beta & g[k])) << k
+            betas.append(beta)
+            for k in range(b):
+                if (beta >> k) & 1:
+                    S[j] ^= S[e0 + k]
+        if W0:
+            nb = min(64, N - e0 - 64)
+            gam = []
+            for i in range(nb):
+                x = 0
+                for k in range(b):
+                    if (betas[i] >> k) & 1:
+                        x ^= m[k]
+                gam.append(x)
+            for r, w0 in W0.items():
+                want = Wof(S[e0 + 64:e0 + 64 + nb], r)
+                corr = sum(parity(WB[r] & gam[i]) << i for i in range(nb))
+                assert want == w0 ^ corr
+                checked += 1
+    assert checked > 50
