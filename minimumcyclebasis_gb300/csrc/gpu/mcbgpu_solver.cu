@@ -92,11 +92,11 @@ constexpr unsigned kNoIndex = 0xFFFFFFFFu;
 // Kernel classes for the optional per-launch profile (events + algorithmic bytes).
 enum KernelClass {
     KC_INIT, KC_TILE_MINC, KC_TRANSPOSE, KC_WSTREAM, KC_PIVOT,
-    KC_BLK_UPDATE, KC_SEARCH, KC_UPDATE, KC_CYCLE, KC_RESET, KC_VALIDATE, KC_WFIX, KC_COUNT
+    KC_BLK_UPDATE, KC_SEARCH, KC_UPDATE, KC_CYCLE, KC_RESET, KC_VALIDATE, KC_WFIX, KC_BLK_UPDATE_NEAR, KC_COUNT
 };
 const char *const kKernelNames[KC_COUNT] = {
     "init_identity", "tile_minc", "blk_transpose", "blk_w", "blk_pivot", "blk_update", "search", "update",
-    "cycle_vector", "reset_state", "validate", "blk_wfix"};
+    "cycle_vector", "reset_state", "validate", "blk_wfix", "blk_update_near"};
 
 struct IterSlot {            // state of one per-iteration search
     unsigned long long best; // first odd rank (kNone until found)
@@ -2146,7 +2146,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             else if (!lead && far_pending)
                 MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[far_par], 0));
             {
-                Launch L(s, KC_BLK_UPDATE, st);
+                Launch L(s, KC_BLK_UPDATE_NEAR, st);
                 blk_update_kernel<<<grid_for(near_end - (e0 + b)), kUpdThreads, 0, st>>>(
                     s->d_S, e0 + b, near_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes(),
                     lead ? s->d_beta : nullptr);
