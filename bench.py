@@ -25,7 +25,7 @@ larger than the 129 MB L2, so no flush is needed between steps.
 
 `--workload batch` measures the batched configuration instead: --batch-count graphs
 (n log-uniform in [50, 5000], average degree U[2.5, 5], w U[1, 255]) solved in one
-BatchSolver (one persistent launch per size class), the plain GPU form (the blocked
+BatchSolver (one persistent launch, one CTA per problem), the plain GPU form (the blocked
 single-problem solver, problem after problem) on a sample beside it, and the
 biconnected components of a --blocks block tree in a second batch.
 
@@ -484,7 +484,7 @@ def run_batch(args, world, rank, local, pg):
                                    "w U[1,255], seed %d; one batched solve of all of them" % (args.batch_count,
                                                                                                args.seed),
                        "problems": len(items), "rings_on_host": nsc, "N_max": int(Ns.max()), "N_sum": int(Ns.sum()),
-                       "K": K, "cycle_nnz": nnz, "form": "batched (one persistent launch per size class)",
+                       "K": K, "cycle_nnz": nnz, "form": "batched (one persistent launch, one CTA per problem)",
                        "total_weight": int(tots.sum()) + host_total,
                        "l2": "inputs (%.2f GB) larger than the 129 MB L2; no flush" % ((nnz * 4 + K * 12) / 1e9)},
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": int(launches),

@@ -199,7 +199,7 @@ int mcbgpu_solve(int32_t num_coords, int64_t num_candidates, const int32_t *weig
 
 /* ---- 4. batched main loop ---------------------------------------------------
  * Many independent problems (the biconnected components of one graph, or many
- * graphs) in one persistent launch per size class, one CTA per problem at a time.
+ * graphs) in one persistent launch, one CTA per problem at a time.
  * Replaces the reference's one-process-per-component loop (main.sh:19-32 runs the
  * whole mcb driver once per bicc component file); every problem's result equals
  * mcbgpu_solver_run's on the same inputs.

@@ -1,5 +1,5 @@
 // Batched de Pina solver: many independent problems (the biconnected components of
-// one graph, or many graphs) solved in one persistent launch per size class.
+// one graph, or many graphs) solved in one persistent launch.
 //
 // The reference solves one graph per process and, for a graph split into
 // biconnected components, runs the whole driver once per component file
@@ -40,6 +40,9 @@ constexpr int kBWarps = kBThreads / 32;
 #endif
 #ifndef MCB_BATCH_Q
 #define MCB_BATCH_Q 4   // the same for the larger classes
+#endif
+#ifndef MCB_BATCH_SINGLE
+#define MCB_BATCH_SINGLE 1  // one launch for the whole batch (0: one launch per size class)
 #endif
 #ifndef MCB_BATCH_CHUNK
 #define MCB_BATCH_CHUNK 4
@@ -572,7 +575,14 @@ BatchKernel class_kernel(int c) {
     }
 }
 
-int class_of(int N) {
+// The launch a problem goes to.  With MCB_BATCH_SINGLE (the default) a batch is one
+// queue in order of decreasing N: on the small-problem kernel (two CTAs per SM) when
+// every problem has N <= kClassMaxN[0], else on the largest-class kernel.  One queue
+// keeps the longest problems first across the whole batch (4096 graphs of the
+// batched configuration: 156 ms against 218 ms with a launch per size class, whose
+// large-problem CTAs take every SM first).
+int class_of(int N, int maxN) {
+    if (MCB_BATCH_SINGLE) return maxN <= kClassMaxN[0] ? 0 : kClasses - 1;
     int c = 0;
     while (c < kClasses - 1 && N > kClassMaxN[c]) c++;
     return c;
@@ -621,10 +631,11 @@ int mcbgpu_batch_create(mcbgpu_batch **out, int32_t count, const int32_t *num_co
     for (int i = 0; i < count; i++)
         if (b->graphs[i].N > 0) idx.push_back(i);
     std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return b->graphs[x].N > b->graphs[y].N; });
+    const int maxN = idx.empty() ? 0 : b->graphs[idx[0]].N;
     for (int c = 0; c < kClasses; c++) {
         b->class_off[c] = (int)b->order.size();
         for (int i : idx)
-            if (class_of(b->graphs[i].N) == c) {
+            if (class_of(b->graphs[i].N, maxN) == c) {
                 b->order.push_back(i);
                 b->class_ncap[c] = std::max(b->class_ncap[c], (b->graphs[i].N + 63) & ~63);
             }

@@ -227,7 +227,7 @@ def solve(num_coords: int, weight: np.ndarray, offsets: np.ndarray, coords: np.n
 
 
 class BatchSolver:
-    """Many independent de Pina problems in one persistent launch per size class.
+    """Many independent de Pina problems in one persistent launch (one CTA per problem).
 
     `problems` is a list of (num_coords, weight, offsets, coords) tuples, each as
     Solver takes it (offsets local to the problem, starting at 0).  Every problem's
