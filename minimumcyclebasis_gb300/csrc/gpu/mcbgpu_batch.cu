@@ -64,12 +64,6 @@ struct BatchGraph {
 
 __device__ __forceinline__ int ffs64(uint64_t x) { return __ffsll((long long)x) - 1; }
 
-__device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int d) {
-    const unsigned lo = __shfl_xor_sync(0xffffffffu, (unsigned)v, d);
-    const unsigned hi = __shfl_xor_sync(0xffffffffu, (unsigned)(v >> 32), d);
-    return ((uint64_t)hi << 32) | lo;
-}
-
 // W of the kBQ consecutive candidates r0 .. r0 + kBQ - 1 (0 past K) from the block's
 // T in shared memory.  The lists are walked in lockstep, kBChunk coordinates of each
 // per step, so kBQ x kBChunk independent loads are in flight per thread.
@@ -440,12 +434,10 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
                     const uint64_t bit = c < e0 ? (rowbuf[c >> 6] >> (c & 63)) & 1ull : (uint64_t)(c == j);
                     D ^= bit << (pr & 63);
                 }
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) D ^= shfl_xor64(D, d);
+                D = warp_xor64(D);
                 uint64_t beta = ((D >> lane) & 1) ? sMrow[lane] : 0ull;
                 if ((D >> (lane + 32)) & 1) beta ^= sMrow[lane + 32];
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) beta ^= shfl_xor64(beta, d);
+                beta = warp_xor64(beta);
                 const long long cu1 = prof ? clock64() : 0;
                 if (prof && tid == 0) pc[8] += cu1 - cu0;
                 if (beta) {

@@ -98,6 +98,13 @@ __device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
 
 __device__ __forceinline__ int parity64(uint64_t x) { return __popcll(x) & 1; }
 
+// XOR of a 64-bit value over the full warp (two warp-reduce instructions).
+__device__ __forceinline__ uint64_t warp_xor64(uint64_t v) {
+    const unsigned lo = __reduce_xor_sync(0xffffffffu, (unsigned)v);
+    const unsigned hi = __reduce_xor_sync(0xffffffffu, (unsigned)(v >> 32));
+    return ((uint64_t)hi << 32) | lo;
+}
+
 // CTA barriers in the non-aligned form (`barrier.sync`, not the `.aligned` form
 // that __syncthreads() emits).  The aligned form lets the hardware assume that
 // every warp arrives converged; after lane-divergent loops (per-candidate

@@ -1576,8 +1576,7 @@ __global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, lo
         uint64_t Dmine = 0;
 #pragma unroll
         for (int r = 0; r < kUpdRows; r++) {
-            uint64_t d = D[r];
-            for (int o = 16; o > 0; o >>= 1) d ^= __shfl_xor_sync(0xffffffffu, d, o);
+            const uint64_t d = warp_xor64(D[r]);
             if (lane == r) Dmine = d;
         }
         if (kUpdSplit > 1) {
