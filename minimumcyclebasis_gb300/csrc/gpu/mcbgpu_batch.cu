@@ -44,6 +44,9 @@ constexpr int kBWarps = kBThreads / 32;
 #ifndef MCB_BATCH_SINGLE
 #define MCB_BATCH_SINGLE 1  // one launch for the whole batch (0: one launch per size class)
 #endif
+#ifndef MCB_BATCH_PREFETCH
+#define MCB_BATCH_PREFETCH 1  // bulk L2 prefetch of the next scan chunk's offsets and lists
+#endif
 #ifndef MCB_BATCH_CHUNK
 #define MCB_BATCH_CHUNK 4
 #endif
@@ -219,6 +222,17 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
                     if (tid == 0) sFail = 1;
                     break;
                 }
+#if MCB_BATCH_PREFETCH
+                if (tid == 0) {  // the next chunk's offsets and lists into L2 while this one is walked
+                    const long long nb = base + (long long)kBThreads * kBQ;
+                    if (nb < K) {
+                        const long long ne = min(nb + (long long)kBThreads * kBQ, K);
+                        prefetch_l2(off + cand + nb, 8ull * (unsigned long long)(ne - nb + 1));
+                        const long long c0 = off[cand + nb], c1 = off[cand + ne];
+                        prefetch_l2(coords + c0, 4ull * (unsigned long long)(c1 - c0));
+                    }
+                }
+#endif
                 // thread tid holds ranks base + tid * kBQ + q: key tid * kBQ + q is rank order
                 const long long cw = prof ? clock64() : 0;
                 bool first_round = true;

@@ -98,6 +98,17 @@ __device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
 
 __device__ __forceinline__ int parity64(uint64_t x) { return __popcll(x) & 1; }
 
+// Bulk prefetch of [p, p + bytes) into L2, shrunk to the 16-byte aligned span inside
+// it (nothing outside the range is touched).
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned long long bytes) {
+    const unsigned long long a = ((unsigned long long)p + 15ull) & ~15ull;
+    const unsigned long long e = ((unsigned long long)p + bytes) & ~15ull;
+    if (e <= a) return;
+    unsigned long long n = e - a;
+    if (n > (1ull << 20)) n = 1ull << 20;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)n) : "memory");
+}
+
 // XOR of a 64-bit value over the full warp (two warp-reduce instructions).
 __device__ __forceinline__ uint64_t warp_xor64(uint64_t v) {
     const unsigned lo = __reduce_xor_sync(0xffffffffu, (unsigned)v);
