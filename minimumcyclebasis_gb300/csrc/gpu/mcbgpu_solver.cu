@@ -58,6 +58,9 @@ constexpr unsigned kSpinLimit = 1u << 24;
 #ifndef MCB_OTF_PAIRS
 #define MCB_OTF_PAIRS 1  // pivot kernel: walk two candidates per thread together on the fly
 #endif
+#ifndef MCB_W_PREFETCH
+#define MCB_W_PREFETCH 1  // streaming pass: bulk L2 prefetch of the CTA's next tile
+#endif
 #ifndef MCB_PAIR
 #define MCB_PAIR 1  // one streaming pass per two blocks (the second block's W by blk_wfix_kernel)
 #endif
@@ -583,6 +586,16 @@ __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, c
     unsigned long long nb = (blockIdx.x == 0 && threadIdx.x == 0) ? 8ull * (unsigned long long)bound : 0ull;
     if (kPaired) {
         for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+#if MCB_W_PREFETCH
+            if (threadIdx.x == 0 && t + gridDim.x < ntiles) {  // this CTA's next tile into L2
+                const long long r0 = (t + gridDim.x) * kTile, r1 = min(r0 + kTile, K);
+                if (r0 < r1) {
+                    prefetch_l2(off + r0, 8ull * (unsigned long long)(r1 - r0 + 1));
+                    const long long c0 = off[r0], c1 = off[r1];
+                    prefetch_l2(coords + c0, 4ull * (unsigned long long)(c1 - c0));
+                }
+            }
+#endif
             if (tile_minc[t] >= bound2) {  // both W's of the tile are 0
                 if (threadIdx.x == 0) nb += 8;
                 continue;
