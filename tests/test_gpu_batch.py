@@ -1,5 +1,5 @@
-"""GPU parity of the batched solver (one persistent launch per size class, one CTA
-per problem): every problem's selected ranks and weight equal the reference's
+"""GPU parity of the batched solver (one persistent launch, one CTA per problem):
+every problem's selected ranks and weight equal the reference's
 golden vectors, the oracle's, or the single-problem blocked solver's, bit for bit."""
 import numpy as np
 import pytest
@@ -141,7 +141,7 @@ def test_per_problem_profile():
     pr = b.profile()
     assert pr.shape == (len(probs), 12)
     assert (pr[:, 0] > 0).all() and (pr[:, 2] > 0).all()  # wall time, scan cycles
-    assert (pr[:, 6] >= np.array([p.K for p in probs]) * 0).all()  # candidates scanned
+    assert (pr[:, 6] > 0).all()  # candidates scanned
     assert (pr[:, 9] >= np.array([(p.N + 63) // 64 for p in probs])).all()  # at least one pivot round per block
     b.set_profiling(False)
     sels, tots = b.results()
