@@ -318,7 +318,9 @@ def run_gpu(args, world, rank, local, pg):
     tpath = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(name)
+            tj = json.load(f)
+        if tj.get("vertices") == args.n:  # captured on this workload
+            traffic = tj.get(name)
     total_ms = sum(v["ms"] for v in stats.values())
     roofline = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
