@@ -61,12 +61,15 @@ constexpr unsigned kSpinLimit = 1u << 24;
 #ifndef MCB_W_PREFETCH
 #define MCB_W_PREFETCH 1  // streaming pass: bulk L2 prefetch of the CTA's next tile
 #endif
-#ifndef MCB_PAIR
-#define MCB_PAIR 1  // one streaming pass per two blocks (the second block's W by blk_wfix_kernel)
+#ifndef MCB_GROUP
+#define MCB_GROUP 2  // blocks per streaming pass (1..3); the later blocks' W by blk_wfix_kernel
 #endif
 #ifndef MCB_PAIR_MARGIN
-#define MCB_PAIR_MARGIN 5  // percent more tiles in a paired streaming pass
+#define MCB_PAIR_MARGIN 5  // percent more tiles per additional block of a grouped streaming pass
 #endif
+constexpr int kGroup = MCB_GROUP;
+static_assert(kGroup >= 1 && kGroup <= 3, "MCB_GROUP must be 1, 2 or 3");
+constexpr int kGStride = kGroup == 3 ? 4 : kGroup;  // words per coordinate in the grouped transpose
 #ifndef MCB_UPD_SPLIT
 #define MCB_UPD_SPLIT 1  // warps per row group in the block update (1, 2, 4 or 8)
 #endif
@@ -114,7 +117,7 @@ struct BlockState {
     long long max_tile;            // deepest tile the previous block's pivot search touched
     unsigned long long total;      // running 64-bit total weight of the basis
     unsigned tail_ok, pad_;        // the pivot kernel's CTA 0 resolved the block
-    long long pair_tiles;          // tiles the paired streaming pass computed for the next block
+    long long pair_tiles;          // tiles the grouped streaming pass computed for the group's later blocks
     long long pivrank[64];
     unsigned long long pivW[64];   // the pivots' W as found (not reduced)
     unsigned long long mask[64];   // final S_{e0+k} as a combination of S^0_{e0+l}
@@ -311,12 +314,13 @@ __global__ void cycle_vector_kernel(uint64_t *C, int W, const int64_t *__restric
 //
 // blk_transpose_kernel: T[64w + i] bit k = S[e0+k] bit (64w+i), for w < Wb.
 // One warp per word column; also resets the block state (runs first in the block).
-// With b2 > 0 (a paired block) also T12[c] = {T[c], T2[c]} for the paired streaming
-// pass, T2[64w + i] bit k = S[e0+64+k] bit (64w+i), w < Wb2: the next block's b2
-// rows as they are now.
-// Writes T[64w + i] (T may be NULL) and, with T12, the same into T12[2(64w + i) + half].
+// The first block of a group also writes Tg[kGStride c + j] for the grouped streaming
+// pass: slot 0 = T[c], slot j = bit k of S[e0+64j+k] bit c (the group's j-th later
+// block's bj rows as they are now), for words w < Wbj of that block.
+// transpose_rows writes T[64w + i] (T may be NULL) and, with Tg, the same into
+// Tg[kGStride (64w + i) + slot].
 __device__ __forceinline__ void transpose_rows(const uint64_t *__restrict__ S, int P, int r0, int b, int Wb,
-                                               uint64_t *__restrict__ T, uint64_t *__restrict__ T12, int half) {
+                                               uint64_t *__restrict__ T, uint64_t *__restrict__ Tg, int slot) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < Wb; w += warps) {
@@ -337,17 +341,17 @@ __device__ __forceinline__ void transpose_rows(const uint64_t *__restrict__ S, i
             T[(size_t)w * 64 + lane] = a;
             T[(size_t)w * 64 + 32 + lane] = c;
         }
-        if (T12) {
-            T12[2 * ((size_t)w * 64 + lane) + half] = a;
-            T12[2 * ((size_t)w * 64 + 32 + lane) + half] = c;
+        if (Tg) {
+            Tg[kGStride * ((size_t)w * 64 + lane) + slot] = a;
+            Tg[kGStride * ((size_t)w * 64 + 32 + lane) + slot] = c;
         }
     }
 }
 
 __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int e0, int b, int Wb,
                                      uint64_t *__restrict__ T, BlockState *bs, long long ntiles,
-                                     GridBar *gb, long long window_tiles, uint64_t *__restrict__ T12, int b2,
-                                     int Wb2) {
+                                     GridBar *gb, long long window_tiles, uint64_t *__restrict__ Tg, int b1,
+                                     int Wb1, int b2, int Wb2) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         gb->count = 0;
         gb->abort = 0;
@@ -362,13 +366,15 @@ __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int 
             const long long a = (lp + lp / 4) / kTile + 1, m = bs->max_tile + 1;
             pred = (a > m ? a : m) + window_tiles;
         }
-        if (b2 > 0 && e0 != 0) pred += pred * MCB_PAIR_MARGIN / 100;  // the pass serves the next block too
+        const int later = (b1 > 0 ? 1 : 0) + (b2 > 0 ? 1 : 0);  // the pass serves the group's later blocks too
+        if (later > 0 && e0 != 0) pred += pred * MCB_PAIR_MARGIN * later / 100;
         bs->pred_tiles = pred < ntiles ? pred : ntiles;
-        if (b2 > 0) bs->pair_tiles = bs->pred_tiles;  // read by the next block's blk_wfix_kernel
+        if (later > 0) bs->pair_tiles = bs->pred_tiles;  // read by the later blocks' blk_wfix_kernel
         bs->max_tile = 0;
     }
-    transpose_rows(S, P, e0, b, Wb, T, b2 > 0 ? T12 : nullptr, 0);
-    if (b2 > 0) transpose_rows(S, P, e0 + 64, b2, Wb2, nullptr, T12, 1);
+    transpose_rows(S, P, e0, b, Wb, T, b1 > 0 ? Tg : nullptr, 0);
+    if (b1 > 0) transpose_rows(S, P, e0 + 64, b1, Wb1, nullptr, Tg, 1);
+    if (b2 > 0) transpose_rows(S, P, e0 + 128, b2, Wb2, nullptr, Tg, 2);
 }
 
 // Reduce W by the basis held as Four-Russians tables: tab[g][pat] = XOR of the basis
@@ -534,35 +540,44 @@ __device__ __forceinline__ void w_of_two(long long ra, long long rb, const int64
     }
 }
 
-// W of one candidate for two blocks at once: W (rows of this block, coordinates
-// below bound) and W2 (the next block's rows as they are now, below bound2 >=
-// bound), one walk of the list; T12[c] = {T[c], T2[c]} (one 16-byte gather).
-__device__ __forceinline__ void w_of_candidate2(long long r, const int64_t *__restrict__ off,
-                                                const int32_t *__restrict__ coords,
-                                                const ulonglong2 *__restrict__ T12, int bound, int bound2,
-                                                unsigned &nread, uint64_t &W, uint64_t &W2) {
+// W of one candidate for the kG blocks of a group at once: W[0] against this block's
+// rows (coordinates below bd[0]), W[j] against the group's j-th later block's rows as
+// they are now (below bd[j], ascending), one walk of the list; Tg holds kGStride
+// words per coordinate (one 16- or 32-byte gather).
+template <int kG>
+__device__ __forceinline__ void w_of_group(long long r, const int64_t *__restrict__ off,
+                                           const int32_t *__restrict__ coords, const uint64_t *__restrict__ Tg,
+                                           const int (&bd)[3], unsigned &nread, uint64_t (&W)[kG]) {
     int64_t i = __ldg(off + r);
     const int64_t e = __ldg(off + r + 1);
-    W = 0;
-    W2 = 0;
+    const int last = bd[kG - 1];
+#pragma unroll
+    for (int g = 0; g < kG; g++) W[g] = 0;
     while (i < e) {
         int cv[kWChunk];
 #pragma unroll
         for (int q = 0; q < kWChunk; q++) cv[q] = i + q < e ? __ldg(coords + i + q) : 0x7fffffff;
-        uint64_t tv[kWChunk], tv2[kWChunk];
+        uint64_t tv[kWChunk][kG];
 #pragma unroll
         for (int q = 0; q < kWChunk; q++) {
-            const ulonglong2 t = cv[q] < bound2 ? __ldg(T12 + cv[q]) : make_ulonglong2(0ull, 0ull);
-            tv[q] = cv[q] < bound ? t.x : 0ull;
-            tv2[q] = t.y;
+            const bool in = cv[q] < last;
+            const ulonglong2 t01 = in ? __ldg(reinterpret_cast<const ulonglong2 *>(Tg + (size_t)kGStride * cv[q]))
+                                      : make_ulonglong2(0ull, 0ull);
+            tv[q][0] = cv[q] < bd[0] ? t01.x : 0ull;
+            tv[q][1] = cv[q] < bd[1] ? t01.y : 0ull;
+            if (kG == 3) {
+                const ulonglong2 t23 =
+                    in ? __ldg(reinterpret_cast<const ulonglong2 *>(Tg + (size_t)kGStride * cv[q] + 2))
+                       : make_ulonglong2(0ull, 0ull);
+                tv[q][kG - 1] = t23.x;
+            }
         }
 #pragma unroll
-        for (int q = 0; q < kWChunk; q++) {
-            W ^= tv[q];
-            W2 ^= tv2[q];
-        }
+        for (int q = 0; q < kWChunk; q++)
+#pragma unroll
+            for (int g = 0; g < kG; g++) W[g] ^= tv[q][g];
         nread += (unsigned)(e - i < kWChunk ? e - i : kWChunk);
-        if (cv[kWChunk - 1] >= bound2) break;
+        if (cv[kWChunk - 1] >= last) break;
         i += kWChunk;
     }
 }
@@ -573,18 +588,22 @@ __device__ __forceinline__ void w_of_candidate2(long long r, const int64_t *__re
 #ifndef MCB_W_MINB
 #define MCB_W_MINB 1  // resident 1024-thread CTAs per SM the W pass is compiled for
 #endif
-// kPaired: also W2 of the next block (T2, bound2) into Warr2, for blk_wfix_kernel.
-template <bool kPaired>
+// kG > 1 (the first block of a group): also W against each later block's rows as
+// they are now (Tg, bounds bd[1..]) into Wl[0..kG-2], for blk_wfix_kernel.
+template <int kG>
 __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, const int64_t *__restrict__ off,
                                                     const int32_t *__restrict__ coords,
                                                     const int32_t *__restrict__ tile_minc,
                                                     const uint64_t *__restrict__ T, int bound, const BlockState *bs,
                                                     uint64_t *Warr, unsigned *tile_epoch, unsigned long long *bytes,
-                                                    const ulonglong2 *__restrict__ T12, int bound2, uint64_t *Warr2) {
+                                                    const uint64_t *__restrict__ Tg, int bound1, int bound2,
+                                                    uint64_t *Wl1, uint64_t *Wl2) {
     const unsigned epoch = bs->epoch;
     const long long ntiles = bs->pred_tiles;
     unsigned long long nb = (blockIdx.x == 0 && threadIdx.x == 0) ? 8ull * (unsigned long long)bound : 0ull;
-    if (kPaired) {
+    if (kG > 1) {
+        const int bd[3] = {bound, bound1, bound2};
+        const int last = bd[kG - 1];
         for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
 #if MCB_W_PREFETCH
             if (threadIdx.x == 0 && t + gridDim.x < ntiles) {  // this CTA's next tile into L2
@@ -596,19 +615,22 @@ __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, c
                 }
             }
 #endif
-            if (tile_minc[t] >= bound2) {  // both W's of the tile are 0
+            if (tile_minc[t] >= last) {  // every W of the tile is 0
                 if (threadIdx.x == 0) nb += 8;
                 continue;
             }
             const long long r = t * kTile + threadIdx.x;
-            uint64_t W = 0, W2 = 0;
+            uint64_t W[kG];
+#pragma unroll
+            for (int g = 0; g < kG; g++) W[g] = 0;
             unsigned nread = 0;
             if (r < K) {
-                w_of_candidate2(r, off, coords, T12, bound, bound2, nread, W, W2);
-                nb += 8 + 16 + 4ull * nread;  // offset, two W writes, coordinates read
+                w_of_group<kG>(r, off, coords, Tg, bd, nread, W);
+                nb += 8 + 8ull * kG + 4ull * nread;  // offset, kG W writes, coordinates read
             }
-            Warr[r] = W;
-            Warr2[r] = W2;
+            Warr[r] = W[0];
+            Wl1[r] = W[1];
+            if (kG == 3) Wl2[r] = W[kG - 1];
         }
         for (long long t = blockIdx.x + (long long)threadIdx.x * gridDim.x; t < ntiles;
              t += (long long)blockDim.x * gridDim.x)
@@ -639,73 +661,89 @@ __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, c
     if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
 }
 
-// The second block of a pair: W of every candidate the paired pass covered, from
-// the two W's it wrote.  Warr2 holds W against this block's rows as they were
-// before the previous block's update; the update added to row i (S_{e1+i}) the
-// combination gamma_i = XOR_{k in beta_i} m_k of the previous block's starting
-// rows (beta_i: the row's update bits, m_k: the previous block's final masks), so
-// bit i of W gains parity(Wprev & gamma_i), with Wprev = the previous block's W
-// (Warr).  That 64x64 GF(2) product is applied through eight 256-entry tables.
+// A later block of a group (the j-th, j = kJ): W of every candidate the grouped pass
+// covered.  Wout holds W against this block's rows as they were before the group's
+// first kJ blocks updated them.  Block i of the group (i < kJ) added to this
+// block's row r the combination gamma_ir = XOR_{k in beta_ir} m_ik of block i's
+// starting rows (beta_ir: row r's update bits in block i, written by block i's near
+// update; m_ik: block i's final masks), so bit r of W gains parity(W_i & gamma_ir),
+// with W_i = block i's W (Win[i]).  Each of these 64x64 GF(2) products is applied
+// through eight 256-entry tables.  Block kJ - 1's masks are read from the block
+// state and kept in masks[kJ - 1] for the group's next block.
+template <int kJ>
 __global__ void __launch_bounds__(kTile) blk_wfix_kernel(const int32_t *__restrict__ tile_minc, int bound,
-                                                         const BlockState *bs, const uint64_t *__restrict__ beta,
-                                                         int b, int bprev, uint64_t *Warr,
-                                                         const uint64_t *__restrict__ Warr2, unsigned *tile_epoch,
+                                                         BlockState *bs, const uint64_t *__restrict__ beta,
+                                                         uint64_t *masks, int b, uint64_t *Win0, uint64_t *Win1,
+                                                         uint64_t *Wout, unsigned *tile_epoch,
                                                          unsigned long long *bytes) {
     __shared__ uint64_t s_m[64], s_g[64], s_col[64];
-    __shared__ uint64_t s_tab[8][256];
+    __shared__ uint64_t s_tab[kJ][8][256];
     const unsigned epoch = bs->epoch;
     const long long ntiles = bs->pair_tiles;
     const int tid = threadIdx.x;
-    if (tid < 64) s_m[tid] = tid < bprev ? bs->mask[tid] : 0ull;
-    cta_sync();
-    if (tid < 64) {
-        uint64_t g = 0;
-        if (tid < b)
-            for (uint64_t bb = beta[tid]; bb; bb &= bb - 1) g ^= s_m[__ffsll((long long)bb) - 1];
-        s_g[tid] = g;
-    }
-    cta_sync();
-    if (tid < 64) {  // col_t bit i = bit t of gamma_i: a 64x64 bit transpose by ballots (warps 0, 1)
-        const int lane = tid & 31, half = tid >> 5;
-        const uint64_t g0 = s_g[lane], g1 = s_g[lane + 32];
-        for (int t = half * 32; t < half * 32 + 32; t++) {
-            const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(g0 >> t) & 1u);
-            const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(g1 >> t) & 1u);
-            if (lane == (t & 31)) s_col[t] = (uint64_t)lo | ((uint64_t)hi << 32);
-        }
-    }
-    if (tid < 8) s_tab[tid][0] = 0;
-    cta_sync();
-    // tab[g][v] for v in [2^u, 2^(u+1)) = tab[g][v - 2^u] ^ col[8g + u]
-    for (int u = 0; u < 8; u++) {
-        const int n = 8 << u;  // 8 groups x 2^u entries
-        for (int idx = tid; idx < n; idx += blockDim.x) {
-            const int grp = idx >> u, v = (1 << u) + (idx & ((1 << u) - 1));
-            s_tab[grp][v] = s_tab[grp][v - (1 << u)] ^ s_col[grp * 8 + u];
+    for (int i = 0; i < kJ; i++) {
+        // block i's masks: the block state holds block kJ - 1's; earlier ones were kept
+        if (tid < 64) {
+            const uint64_t mk = i == kJ - 1 ? bs->mask[tid] : masks[i * 64 + tid];
+            s_m[tid] = mk;
+            if (i == kJ - 1 && blockIdx.x == 0) masks[i * 64 + tid] = mk;
         }
         cta_sync();
+        if (tid < 64) {  // beta of this block's row tid in block i: near rows of block i start
+            uint64_t g = 0;  // at block i + 1, so this block's rows sit (kJ - 1 - i) blocks in
+            if (tid < b)
+                for (uint64_t bb = beta[i * 192 + (kJ - 1 - i) * 64 + tid]; bb; bb &= bb - 1)
+                    g ^= s_m[__ffsll((long long)bb) - 1];
+            s_g[tid] = g;
+        }
+        cta_sync();
+        if (tid < 64) {  // col_t bit r = bit t of gamma_r: a 64x64 bit transpose by ballots (warps 0, 1)
+            const int lane = tid & 31, half = tid >> 5;
+            const uint64_t g0 = s_g[lane], g1 = s_g[lane + 32];
+            for (int t = half * 32; t < half * 32 + 32; t++) {
+                const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(g0 >> t) & 1u);
+                const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(g1 >> t) & 1u);
+                if (lane == (t & 31)) s_col[t] = (uint64_t)lo | ((uint64_t)hi << 32);
+            }
+        }
+        if (tid < 8) s_tab[i][tid][0] = 0;
+        cta_sync();
+        // tab[g][v] for v in [2^u, 2^(u+1)) = tab[g][v - 2^u] ^ col[8g + u]
+        for (int u = 0; u < 8; u++) {
+            const int n = 8 << u;  // 8 groups x 2^u entries
+            for (int idx = tid; idx < n; idx += blockDim.x) {
+                const int grp = idx >> u, v = (1 << u) + (idx & ((1 << u) - 1));
+                s_tab[i][grp][v] = s_tab[i][grp][v - (1 << u)] ^ s_col[grp * 8 + u];
+            }
+            cta_sync();
+        }
     }
     unsigned long long nb = 0;
     // four tiles per pass: their loads are in flight together
     constexpr int kU = 4;
     for (long long t0 = blockIdx.x; t0 < ntiles; t0 += (long long)kU * gridDim.x) {
-        uint64_t w[kU], x[kU];
+        uint64_t w0[kU], w1[kU], x[kU];
         bool live[kU];
 #pragma unroll
         for (int u = 0; u < kU; u++) {
             const long long t = t0 + (long long)u * gridDim.x;
             live[u] = t < ntiles && tile_minc[t] < bound;  // else W = 0 for the whole tile: tagged below
             const long long r = t * kTile + tid;
-            w[u] = live[u] ? Warr[r] : 0ull;
-            x[u] = live[u] ? Warr2[r] : 0ull;
+            w0[u] = live[u] ? Win0[r] : 0ull;
+            w1[u] = live[u] && kJ > 1 ? Win1[r] : 0ull;
+            x[u] = live[u] ? Wout[r] : 0ull;
         }
 #pragma unroll
         for (int u = 0; u < kU; u++) {
             if (!live[u]) continue;
 #pragma unroll
-            for (int grp = 0; grp < 8; grp++) x[u] ^= s_tab[grp][(w[u] >> (8 * grp)) & 255];
-            Warr[(t0 + (long long)u * gridDim.x) * kTile + tid] = x[u];
-            nb += 24;
+            for (int grp = 0; grp < 8; grp++) x[u] ^= s_tab[0][grp][(w0[u] >> (8 * grp)) & 255];
+            if (kJ > 1) {
+#pragma unroll
+                for (int grp = 0; grp < 8; grp++) x[u] ^= s_tab[kJ - 1][grp][(w1[u] >> (8 * grp)) & 255];
+            }
+            Wout[(t0 + (long long)u * gridDim.x) * kTile + tid] = x[u];
+            nb += 16 + 8ull * kJ;
         }
     }
     for (long long t = blockIdx.x + (long long)tid * gridDim.x; t < ntiles; t += (long long)blockDim.x * gridDim.x)
@@ -1646,9 +1684,11 @@ struct mcbgpu_solver {
     uint64_t *d_T = nullptr;       // 64 * P words
     uint64_t *d_tab = nullptr;     // 8 * 256 * P words
     uint64_t *d_Warr = nullptr;    // W per candidate (tiles * 1024)
-    uint64_t *d_Warr2 = nullptr;   // a paired pass's W against the next block's rows
-    uint64_t *d_T12 = nullptr;     // {this block's, the next block's} rows transposed (paired pass)
-    uint64_t *d_beta = nullptr;    // 64 update bits of the next block's rows (paired pass)
+    uint64_t *d_Warr2 = nullptr;   // W of a group's second block (the grouped pass, then its correction)
+    uint64_t *d_Warr3 = nullptr;   // W of a group's third block
+    uint64_t *d_Tg = nullptr;      // the group's blocks' rows transposed, kGStride words per coordinate
+    uint64_t *d_beta = nullptr;    // 3 x 192: update bits of the near rows of a group's first blocks
+    uint64_t *d_masks = nullptr;   // 2 x 64: final masks of a group's first blocks
     unsigned *d_tile_epoch = nullptr;
     int32_t *d_tile_minc = nullptr;
     unsigned long long *d_reports = nullptr;  // two step parities of G x (2 kLmax + 2) words
@@ -1658,7 +1698,7 @@ struct mcbgpu_solver {
     unsigned pair_cap = 0;
     unsigned *d_word_end = nullptr;  // 2 x (P + 1): sorted pairs with S word < w, by block parity
     cudaStream_t st2 = nullptr;      // the update of the rows beyond the next block
-    cudaEvent_t ev_fork = nullptr, ev_tail = nullptr, ev_upd[2] = {nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_tail = nullptr, ev_upd[4] = {}, ev_par[2] = {};
     IterSlot *d_slots = nullptr;   // 2
     BlockState *d_bs = nullptr;
     long long *d_selected = nullptr;
@@ -1730,8 +1770,10 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_tab);
     cudaFree(s->d_Warr);
     cudaFree(s->d_Warr2);
-    cudaFree(s->d_T12);
+    cudaFree(s->d_Warr3);
+    cudaFree(s->d_Tg);
     cudaFree(s->d_beta);
+    cudaFree(s->d_masks);
     cudaFree(s->d_tile_epoch);
     cudaFree(s->d_tile_minc);
     cudaFree(s->d_reports);
@@ -1741,6 +1783,8 @@ void free_solver(mcbgpu_solver *s) {
     if (s->st2) cudaStreamDestroy(s->st2);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev_tail) cudaEventDestroy(s->ev_tail);
+    for (cudaEvent_t e : s->ev_par)
+        if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : s->ev_upd)
         if (e) cudaEventDestroy(e);
     cudaFree(s->d_slots);
@@ -1811,10 +1855,12 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_T, sizeof(uint64_t) * 64 * (size_t)s->P);
     ALLOC(s->d_tab, sizeof(uint64_t) * 2 * 8 * 256 * (size_t)s->P);
     ALLOC(s->d_Warr, sizeof(uint64_t) * (size_t)kTile * ntiles);
-    if (MCB_PAIR) {
+    if (kGroup > 1) {
         ALLOC(s->d_Warr2, sizeof(uint64_t) * (size_t)kTile * ntiles);
-        ALLOC(s->d_T12, sizeof(uint64_t) * 2 * 64 * (size_t)s->P);
-        ALLOC(s->d_beta, sizeof(uint64_t) * 64);
+        if (kGroup > 2) ALLOC(s->d_Warr3, sizeof(uint64_t) * (size_t)kTile * ntiles);
+        ALLOC(s->d_Tg, sizeof(uint64_t) * kGStride * 64 * (size_t)s->P);
+        ALLOC(s->d_beta, sizeof(uint64_t) * 3 * 192);
+        ALLOC(s->d_masks, sizeof(uint64_t) * 2 * 64);
     }
     ALLOC(s->d_tile_epoch, sizeof(unsigned) * ntiles);
     ALLOC(s->d_tile_minc, sizeof(int32_t) * ntiles);
@@ -1836,7 +1882,8 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_tail, cudaEventDisableTiming);
-    for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&s->ev_upd[i], cudaEventDisableTiming);
+    for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&s->ev_upd[i], cudaEventDisableTiming);
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&s->ev_par[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMemset(s->d_coords, 0, sizeof(int32_t) * (size_t)(nnz + 16));
     if (e == cudaSuccess) {
         const int G = s->sm_count > 0 ? s->sm_count : 1;  // one CTA per SM
@@ -2050,54 +2097,75 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
     const int64_t iters = (max_iterations >= 0 && max_iterations < s->N) ? max_iterations : s->N;
     const int sms = s->sm_count > 0 ? s->sm_count : 148;
     long long ntiles = (s->K + kTile - 1) / kTile;
-    // The update of a block is split: the next block's 64 rows on `st` (its
+    // The update of a block is split: the next rows on `st` (the next block's
     // transpose needs them), every later row on st2, where it overlaps the next
-    // block's transpose, streaming pass and pivot search.  Rows are updated block
-    // after block, so the next block's near rows wait for this block's far rows
-    // (ev_upd), and the buffers the far update reads (gcol, tables, sorted pairs,
-    // word_end) alternate by block parity.
+    // block's transpose, streaming pass and pivot search.  Dependencies across the
+    // two streams:
+    //  - a block's near rows wait for the last far update that reaches them (far
+    //    updates run in order on st2, so the last one suffices);
+    //  - the buffers the far update reads (gcol, tables, sorted pairs, word_end)
+    //    alternate by block parity, so a block's pivot kernel (whose tail rewrites
+    //    them) waits for the far update two blocks back.
+    // Blocks in groups of kGroup (MCB_GROUP): the first block's streaming pass also
+    // computes W against each later block's rows as they are then; each later block
+    // corrects those W's (blk_wfix_kernel) instead of streaming the lists again.  So
+    // the later blocks' rows must be final up to the block before the group when the
+    // group starts: the last block of a group updates the next kGroup x 64 rows on
+    // `st`, and block i < kGroup - 1 of a group the rows of the group's later blocks
+    // (their update bits go to beta slab i for the corrections).
     MCB_CUDA(cudaEventRecord(s->ev_fork, st));
     MCB_CUDA(cudaStreamWaitEvent(s->st2, s->ev_fork, 0));
-    bool far_pending = false, far_rec[2] = {false, false};
-    int far_par = 0;
-    // Blocks in pairs (MCB_PAIR): the first block's streaming pass also computes W
-    // against the second block's rows as they are before the first block's update;
-    // the second block corrects those W's (blk_wfix_kernel) instead of streaming the
-    // lists again.  So the second block's rows must be final up to the block before
-    // the pair when the pair starts: the second block of a pair updates the next
-    // 128 rows on `st`, not 64.
+    struct FarRec {
+        long long start;  // first row of the far update
+        int slot;         // its event in ev_upd
+    };
+    FarRec fars[4];
+    int nfar = 0, ring = 0;
+    bool par_far[2] = {false, false};  // a far update of this parity was recorded in ev_par
+    uint64_t *Wpos[3] = {s->d_Warr, s->d_Warr2, s->d_Warr3};
     for (int64_t e0 = 0; e0 < iters; e0 += 64) {
         const int b = (int)std::min<int64_t>(64, iters - e0);
         const int par = (int)((e0 / 64) & 1);
+        const int pos = (int)((e0 / 64) % kGroup);  // position in its group
         const int Wb = (int)((e0 + b + 63) / 64);
         const int bound = (int)(e0 + b);
-        const bool lead = MCB_PAIR && par == 0 && e0 + 64 < iters;  // first block of a pair
-        const bool follow = MCB_PAIR && par == 1;                     // second block of a pair
-        const int b2 = lead ? (int)std::min<int64_t>(64, iters - e0 - 64) : 0;
-        const int bound2 = (int)(e0 + 64 + b2);
-        const int Wb2 = lead ? (bound2 + 63) / 64 : 0;
+        int bl[2] = {0, 0};  // a group's first block: b of the later blocks
+        if (pos == 0)
+            for (int jj = 1; jj < kGroup; jj++) bl[jj - 1] = (int)std::max<int64_t>(0, std::min<int64_t>(64, iters - e0 - 64 * jj));
+        const int nl = (bl[0] > 0 ? 1 : 0) + (bl[1] > 0 ? 1 : 0);
+        const int bd1 = (int)(e0 + 64 + bl[0]), bd2 = (int)(e0 + 128 + bl[1]);
+        const int Wb1 = bl[0] > 0 ? (bd1 + 63) / 64 : 0, Wb2 = bl[1] > 0 ? (bd2 + 63) / 64 : 0;
         {
             Launch L(s, KC_TRANSPOSE, st);
-            blk_transpose_kernel<<<(std::max(Wb, Wb2) + 7) / 8, 256, 0, st>>>(
+            blk_transpose_kernel<<<(std::max(Wb, std::max(Wb1, Wb2)) + 7) / 8, 256, 0, st>>>(
                 s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles, s->d_gbar, (long long)s->pivot_grid * kWinTiles,
-                s->d_T12, b2, Wb2);
+                s->d_Tg, bl[0], Wb1, bl[1], Wb2);
         }
-        if (ntiles > 0 && follow) {
+        if (ntiles > 0 && pos > 0) {
             Launch L(s, KC_WFIX, st);
-            blk_wfix_kernel<<<sms, kTile, 0, st>>>(s->d_tile_minc, bound, s->d_bs, s->d_beta, b, 64, s->d_Warr,
-                                                       s->d_Warr2, s->d_tile_epoch, L.bytes());
-        } else if (ntiles > 0 && lead) {
-            Launch L(s, KC_WSTREAM, st);
-            blk_w_kernel<true><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
-                                                          s->d_bs, s->d_Warr, s->d_tile_epoch, L.bytes(),
-                                                          reinterpret_cast<const ulonglong2 *>(s->d_T12), bound2,
-                                                          s->d_Warr2);
+            if (pos == 1)
+                blk_wfix_kernel<1><<<sms, kTile, 0, st>>>(s->d_tile_minc, bound, s->d_bs, s->d_beta, s->d_masks, b,
+                                                          Wpos[0], Wpos[1], Wpos[1], s->d_tile_epoch, L.bytes());
+            else
+                blk_wfix_kernel<2><<<sms, kTile, 0, st>>>(s->d_tile_minc, bound, s->d_bs, s->d_beta, s->d_masks, b,
+                                                          Wpos[0], Wpos[1], Wpos[2], s->d_tile_epoch, L.bytes());
         } else if (ntiles > 0) {
             Launch L(s, KC_WSTREAM, st);
-            blk_w_kernel<false><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
-                                                           s->d_bs, s->d_Warr, s->d_tile_epoch, L.bytes(), nullptr, 0,
-                                                           nullptr);
+            if (nl == 2)
+                blk_w_kernel<3><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                                                           s->d_bs, Wpos[0], s->d_tile_epoch, L.bytes(), s->d_Tg, bd1,
+                                                           bd2, Wpos[1], Wpos[2]);
+            else if (nl == 1)
+                blk_w_kernel<2><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                                                           s->d_bs, Wpos[0], s->d_tile_epoch, L.bytes(), s->d_Tg, bd1,
+                                                           bd1, Wpos[1], nullptr);
+            else
+                blk_w_kernel<1><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                                                           s->d_bs, Wpos[0], s->d_tile_epoch, L.bytes(), nullptr, 0, 0,
+                                                           nullptr, nullptr);
         }
+        // this block's tail rewrites the parity buffers the far update two blocks back reads
+        if (par_far[par]) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_par[par], 0));
         {
             Launch L(s, KC_PIVOT, st);
             long long K = s->K;
@@ -2106,7 +2174,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             const int32_t *tm = s->d_tile_minc;
             const uint64_t *T = s->d_T;
             BlockState *bs = s->d_bs;
-            uint64_t *Wa = s->d_Warr;
+            uint64_t *Wa = Wpos[pos];
             unsigned *te = s->d_tile_epoch;
             GridBar *gb = s->d_gbar;
             unsigned *stt = s->d_status;
@@ -2133,7 +2201,8 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                                                  args, pivot_smem_bytes(s->pivot_grid), st));
         }
         if (e0 + b < s->N) {
-            const long long near_end = std::min<long long>(e0 + b + (follow ? 128 : 64), s->N), far_end = s->N;
+            const int near_rows = kGroup == 1 ? 64 : pos == kGroup - 1 ? 64 * kGroup : 64 * (kGroup - 1 - pos);
+            const long long near_end = std::min<long long>(e0 + b + near_rows, s->N), far_end = s->N;
             const uint64_t *tab = s->d_tab + (size_t)par * 8 * 256 * s->P;
             const uint64_t *gcol = reinterpret_cast<const uint64_t *>(&s->d_bs->gcol[par][0]);
             const unsigned *pairs = s->d_pairs + (size_t)(1 + par) * s->pair_cap;
@@ -2142,6 +2211,10 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 long long g = (rows + kUpdGroups * kUpdRows - 1) / (kUpdGroups * kUpdRows);
                 return (int)std::max<long long>(1, std::min<long long>(g, (long long)sms * 8));
             };
+            // the last earlier far update that reaches the near rows [e0 + b, near_end)
+            int wait_slot = -1;
+            for (int q = 0; q < nfar; q++)
+                if (fars[q].start < near_end) wait_slot = fars[q].slot;  // fars[] in launch order
             if (near_end < far_end) {  // far rows: on st2 once this block's tail is done
                 MCB_CUDA(cudaEventRecord(s->ev_tail, st));
                 MCB_CUDA(cudaStreamWaitEvent(s->st2, s->ev_tail, 0));
@@ -2149,30 +2222,29 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 blk_update_kernel<<<grid_for(far_end - near_end), kUpdThreads, 0, s->st2>>>(
                     s->d_S, near_end, far_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes(), nullptr);
             }
-            // the near rows wait for the last far update that covers them: the previous
-            // block's, except in the first block of a pair, whose near rows (the second
-            // block's) the previous block's far update does not reach (it starts 128
-            // rows on), so that block waits for the far update before it
-            if (lead && far_rec[par])
-                MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[par], 0));
-            else if (!lead && far_pending)
-                MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[far_par], 0));
+            if (wait_slot >= 0) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[wait_slot], 0));
             {
                 Launch L(s, KC_BLK_UPDATE_NEAR, st);
                 blk_update_kernel<<<grid_for(near_end - (e0 + b)), kUpdThreads, 0, st>>>(
                     s->d_S, e0 + b, near_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes(),
-                    lead ? s->d_beta : nullptr);
+                    kGroup > 1 && pos < kGroup - 1 ? s->d_beta + (size_t)pos * 192 : nullptr);
             }
-            far_pending = near_end < far_end;
-            if (far_pending) {
-                far_par = par;
-                far_rec[par] = true;
-                MCB_CUDA(cudaEventRecord(s->ev_upd[par], s->st2));
+            if (near_end < far_end) {
+                const int slot = ring;
+                ring = (ring + 1) & 3;
+                MCB_CUDA(cudaEventRecord(s->ev_upd[slot], s->st2));
+                MCB_CUDA(cudaEventRecord(s->ev_par[par], s->st2));
+                par_far[par] = true;
+                if (nfar == 4) {  // keep the last three
+                    for (int q = 1; q < 4; q++) fars[q - 1] = fars[q];
+                    nfar = 3;
+                }
+                fars[nfar++] = {near_end, slot};
             }
         }
         MCB_CUDA(cudaGetLastError());
     }
-    if (far_pending) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[far_par], 0));
+    if (nfar > 0) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[fars[nfar - 1].slot], 0));
 
     s->iters_run = iters;
     return MCBGPU_OK;

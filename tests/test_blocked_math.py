@@ -226,3 +226,89 @@ def test_paired_pass_correction_identity():
                 assert want == w0 ^ corr
                 checked += 1
     assert checked > 50
+
+
+def test_grouped_pass_correction_identity_three_blocks():
+    """The grouped pass over three blocks B, B+1, B+2: W of a candidate against block
+    B+2's rows at its start equals W0 (against those rows at B's start) plus, for each
+    earlier block i in {B, B+1}, bit r: parity(W_i & gamma_ir), gamma_ir = XOR of block
+    i's final masks over row r's update bits in block i, W_i = the candidate's W in
+    block i (the two corrections blk_wfix_kernel<2> applies)."""
+    p = Problem.from_graph(random_graph(260, 520, 1, 20, 5)).prepare(threads=2, keep_trees=True)
+    N, K = p.N, p.K
+    off, co = p.cycle_lists()
+    lists = [co[off[r]:off[r + 1]].tolist() for r in range(K)]
+    S = [1 << j for j in range(N)]
+    dot = lambda s, r: sum((s >> c) & 1 for c in lists[r]) & 1  # noqa: E731
+    Wof = lambda rows, r: sum(dot(rows[i], r) << i for i in range(len(rows)))  # noqa: E731
+    sample = list(range(0, K, 11))
+    hist = []  # per block: (e0, W of the sample, masks, betas by row)
+    W0 = {}
+    checked = 0
+    for e0 in range(0, N, 64):
+        b = min(64, N - e0)
+        bi = e0 // 64
+        if bi % 3 == 0 and e0 + 128 < N:
+            W0 = {r: Wof(S[e0 + 128:e0 + 192], r) for r in sample}
+        if bi % 3 == 2 and W0:
+            nb = min(64, N - e0)
+            for r in sample:
+                want = Wof(S[e0:e0 + nb], r)
+                got = W0[r]
+                for (ei, Wi, mi, betas) in hist[-2:]:
+                    bi_ = min(64, N - ei)
+                    corr = 0
+                    for row in range(nb):
+                        beta = betas[e0 + row]
+                        gam = 0
+                        for k in range(bi_):
+                            if (beta >> k) & 1:
+                                gam ^= mi[k]
+                        corr |= parity(Wi[r] & gam) << row
+                    got ^= corr
+                assert got == want
+                checked += 1
+            W0 = {}
+        Wb = {r: Wof(S[e0:e0 + b], r) for r in sample}
+        echelon, piv = {}, []
+        for r in range(K):
+            W = Wof(S[e0:e0 + b], r)
+            x = W
+            while x:
+                q = (x & -x).bit_length() - 1
+                if q in echelon:
+                    x ^= echelon[q]
+                else:
+                    echelon[q] = x
+                    piv.append((r, W))
+                    break
+            if len(piv) == b:
+                break
+        m = [1 << k for k in range(b)]
+        g, chosen, used = [], [], set()
+        for k in range(b):
+            q = next(i for i in range(b) if i not in used and parity(piv[i][1] & m[k]))
+            used.add(q)
+            chosen.append(q)
+            g.append(sum(parity(piv[q][1] & m[i]) << i for i in range(k)))
+            for j in range(k + 1, b):
+                if parity(piv[q][1] & m[j]):
+                    m[j] ^= m[k]
+        S0 = [S[e0 + l] for l in range(b)]
+        for k in range(b):
+            S[e0 + k] = 0
+            for l in range(b):
+                if (m[k] >> l) & 1:
+                    S[e0 + k] ^= S0[l]
+        betas = {}
+        for j in range(e0 + b, N):
+            D = sum(dot(S[j], piv[chosen[k]][0]) << k for k in range(b))
+            beta = 0
+            for k in range(b):
+                beta |= (((D >> k) & 1) ^ parity(beta & g[k])) << k
+            betas[j] = beta
+            for k in range(b):
+                if (beta >> k) & 1:
+                    S[j] ^= S[e0 + k]
+        hist.append((e0, Wb, m, betas))
+    assert checked > 20
