@@ -61,6 +61,9 @@ constexpr unsigned kSpinLimit = 1u << 24;
 #ifndef MCB_W_PREFETCH
 #define MCB_W_PREFETCH 1  // streaming pass: bulk L2 prefetch of the CTA's next tile
 #endif
+#ifndef MCB_PIVOT_DIV
+#define MCB_PIVOT_DIV 1  // pivot kernel grid = SM count / MCB_PIVOT_DIV
+#endif
 #ifndef MCB_GROUP
 #define MCB_GROUP 2  // blocks per streaming pass (1..3); the later blocks' W by blk_wfix_kernel
 #endif
@@ -1886,7 +1889,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&s->ev_par[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMemset(s->d_coords, 0, sizeof(int32_t) * (size_t)(nnz + 16));
     if (e == cudaSuccess) {
-        const int G = s->sm_count > 0 ? s->sm_count : 1;  // one CTA per SM
+        const int G = s->sm_count > 0 ? std::max(1, s->sm_count / MCB_PIVOT_DIV) : 1;  // one CTA per SM
         const size_t smem = pivot_smem_bytes(G);
         e = cudaFuncSetAttribute(blk_pivot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         // the block tail sorts the pairs in shared memory past the tables (P + 1 counters)
