@@ -55,3 +55,24 @@ def test_error_string_without_gpu():
     lib = gpu_lib()
     assert lib.mcbgpu_version() == 1
     assert lib.mcbgpu_last_error() is not None
+
+
+def test_size_checks_before_any_device_call():
+    # argument checks run before the library touches the device, so they answer on
+    # a machine without a GPU
+    import ctypes as C
+
+    import numpy as np
+
+    from minimumcyclebasis_gb300._native import gpu_lib, ptr
+    lib = gpu_lib()
+    h = C.c_void_p()
+    big = np.array([lib.mcbgpu_batch_max_coords() + 1], np.int32)
+    k = np.array([1], np.int64)
+    assert lib.mcbgpu_batch_create(C.byref(h), 1, ptr(big), ptr(k), 1) == -1
+    assert b"mcbgpu_solver" in lib.mcbgpu_last_error()  # points to the single-problem solver
+    neg = np.array([-1], np.int32)
+    assert lib.mcbgpu_batch_create(C.byref(h), 1, ptr(neg), ptr(k), 1) == -1
+    assert lib.mcbgpu_batch_create(None, 0, None, None, 0) == -1
+    assert lib.mcbgpu_solver_create(C.byref(h), 1 << 26, 1, 1) == -1
+    assert lib.mcbgpu_batch_max_coords() == 12288
