@@ -144,10 +144,19 @@ def max_over_ranks(x, pg):
     return float(t.item())
 
 
+def make_graph(args):
+    from minimumcyclebasis_gb300 import planar_chain_graph, random_graph, rgg_graph
+    if args.graph == "rgg":  # the learned-proposal configuration's family
+        return rgg_graph(args.n, 4, args.seed)
+    if args.graph == "planar":  # the scale configuration's family, --n triangulated points
+        return planar_chain_graph(args.n, 30, 30, 8, 1, 1000, args.seed)
+    return random_graph(args.n, 2 * args.n, 1, 1000, args.seed)
+
+
 def prepare(args, keep_trees):
-    from minimumcyclebasis_gb300 import Problem, random_graph
+    from minimumcyclebasis_gb300 import Problem
     t0 = time.time()
-    g = random_graph(args.n, 2 * args.n, 1, 1000, args.seed)
+    g = make_graph(args)
     p = Problem.from_graph(g).prepare(threads=0, keep_trees=keep_trees)
     i = p.info
     log("prepared in %.1fs: n'=%d F=%d N=%d K=%d nnz=%d" % (time.time() - t0, i.reduced_nodes, i.fvs_size,
@@ -157,8 +166,13 @@ def prepare(args, keep_trees):
 
 def config_of(p, args, extra=None):
     i = p.info
-    c = {"workload": "random sparse graph n=%d m=%d (avg degree 4), int32 w U[1,1000], seed %d; full de Pina solve"
-                     % (args.n, 2 * args.n, args.seed),
+    names = {"random": "random sparse graph n=%d m=%d (avg degree 4), int32 w U[1,1000], seed %d"
+                       % (args.n, 2 * args.n, args.seed),
+             "rgg": "random geometric graph n=%d, k=4 nearest neighbours, w = round(1000 x length), seed %d"
+                    % (args.n, args.seed),
+             "planar": "planar-like graph from %d triangulated points, 30%% of edges deleted, 30%% subdivided into "
+                       "chains of 1-8, w U[1,1000], seed %d" % (args.n, args.seed)}
+    c = {"workload": names[args.graph] + "; full de Pina solve", "input_nodes": i.nodes,
          "reduced_nodes": i.reduced_nodes, "fvs": i.fvs_size, "N": i.num_coords, "K": i.num_candidates,
          "cycle_nnz": i.cycle_nnz, "form": args.mode,
          "l2": ("inputs (cycle lists %.2f GB) larger than the 129 MB L2; no flush" % (i.cycle_nnz * 4 / 1e9))
@@ -319,7 +333,7 @@ def run_gpu(args, world, rank, local, pg):
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
-        if tj.get("vertices") == args.n:  # captured on this workload
+        if tj.get("vertices") == args.n and tj.get("graph", "random") == args.graph:  # captured on this workload
             traffic = tj.get(name)
     total_ms = sum(v["ms"] for v in stats.values())
     roofline = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -524,6 +538,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--graph", choices=["random", "rgg", "planar"], default="random",
+                    help="graph family of the single-graph workload (random: the 50k plain-GPU configuration)")
     ap.add_argument("--workload", choices=["random", "batch"], default="random",
                     help="random: the 50k-node graph (default); batch: the batched configuration")
     ap.add_argument("--batch-count", type=int, default=4096)
