@@ -208,7 +208,9 @@ int mcbgpu_solve(int32_t num_coords, int64_t num_candidates, const int32_t *weig
  *   mcbgpu_batch_max_coords()) and num_candidates[i] = K_i; nnz = total coordinates.
  * upload: the problems' candidates back to back in problem order: weight[sum K],
  *   offsets[sum K + 1] (int64, one running sequence from 0 to nnz), coords[nnz]
- *   (each list ascending in [0, N_i) of its problem).
+ *   (each list ascending in [0, N_i) of its problem).  Synchronises `stream`: the
+ *   offsets are checked on the device (MCBGPU_E_ARG if they are not non-decreasing
+ *   from 0 to nnz).
  * run: enqueued on `stream` without host synchronisation.
  * results: selected[sum N] (problem i's iterations at offset N_0 + ... + N_{i-1},
  *   each the candidate's rank within problem i), total_weight[count] (-1 for a

@@ -502,6 +502,33 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
 
 }  // namespace
 
+namespace {
+
+// The uploaded offsets: non-decreasing from 0 to nnz (out[0] = 1 if not); out[1] =
+// the longest list (it sizes the pair scratch).
+__global__ void batch_validate_kernel(const int64_t *__restrict__ off, long long K, long long nnz, unsigned *out) {
+    unsigned long long mx = 0;
+    unsigned bad = 0;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < K; r += (long long)gridDim.x * blockDim.x) {
+        const long long a = off[r], e = off[r + 1];
+        if (e < a || a < 0 || e > nnz)
+            bad = 1;
+        else if ((unsigned long long)(e - a) > mx)
+            mx = (unsigned long long)(e - a);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (off[0] != 0 || off[K] != nnz)) bad = 1;
+    if (mx > 0xffffffffull) mx = 0xffffffffull;
+    unsigned m32 = (unsigned)mx;
+    m32 = __reduce_max_sync(0xffffffffu, m32);
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0) {
+        if (m32) atomicMax(out + 1, m32);
+        if (bad) atomicOr(out, 1u);
+    }
+}
+
+}  // namespace
+
 struct mcbgpu_batch {
     int count = 0;
     int sm_count = 0;
@@ -524,6 +551,7 @@ struct mcbgpu_batch {
     long long *d_total = nullptr;
     unsigned *d_gstatus = nullptr;
     unsigned *d_status = nullptr;
+    unsigned *d_check = nullptr;  // [bad offsets, longest list]
     unsigned *d_pairs = nullptr;
     long long *d_prof = nullptr;  // optional per-problem profile (count x 8)
     cudaStream_t st[kClasses] = {};
@@ -557,6 +585,7 @@ void free_batch(mcbgpu_batch *b) {
     cudaFree(b->d_total);
     cudaFree(b->d_gstatus);
     cudaFree(b->d_status);
+    cudaFree(b->d_check);
     cudaFree(b->d_pairs);
     cudaFree(b->d_prof);
     for (int c = 0; c < kClasses; c++) {
@@ -669,6 +698,7 @@ int mcbgpu_batch_create(mcbgpu_batch **out, int32_t count, const int32_t *num_co
     ALLOC(b->d_total, sizeof(long long) * (size_t)count);
     ALLOC(b->d_gstatus, sizeof(unsigned) * (size_t)count);
     ALLOC(b->d_status, sizeof(unsigned));
+    ALLOC(b->d_check, 2 * sizeof(unsigned));
 #undef ALLOC
     if (e == cudaSuccess && count > 0)
         e = cudaMemcpy(b->d_graphs, b->graphs.data(), sizeof(BatchGraph) * (size_t)count, cudaMemcpyHostToDevice);
@@ -709,22 +739,31 @@ int mcbgpu_batch_upload(mcbgpu_batch *b, const int32_t *weight, const int64_t *o
         return MCBGPU_E_ARG;
     }
     b->uploaded = false;
-    // offsets: non-decreasing from 0 to nnz; the longest list sizes the pair scratch
-    long long max_len = 0;
+    cudaStream_t st = (cudaStream_t)stream;
     if (b->total_K > 0) {
-        if (offsets[0] != 0 || offsets[b->total_K] != b->nnz) {
-            set_error("mcbgpu_batch_upload: offsets must run from 0 to nnz");
-            return MCBGPU_E_ARG;
-        }
-        for (long long r = 0; r < b->total_K; r++) {
-            const long long len = offsets[r + 1] - offsets[r];
-            if (len < 0) {
-                set_error("mcbgpu_batch_upload: offsets must be non-decreasing");
-                return MCBGPU_E_ARG;
-            }
-            max_len = std::max(max_len, len);
-        }
+        MCB_CUDA(cudaMemcpyAsync(b->d_weight, weight, sizeof(int32_t) * (size_t)b->total_K, cudaMemcpyHostToDevice,
+                                 st));
+        MCB_CUDA(cudaMemcpyAsync(b->d_off, offsets, sizeof(int64_t) * (size_t)(b->total_K + 1),
+                                 cudaMemcpyHostToDevice, st));
     }
+    if (b->nnz > 0)
+        MCB_CUDA(cudaMemcpyAsync(b->d_coords, coords, sizeof(int32_t) * (size_t)b->nnz, cudaMemcpyHostToDevice, st));
+    // offsets checked on the device (non-decreasing from 0 to nnz); the longest list
+    // sizes the pair scratch; the coordinate lists are checked by the solve itself
+    unsigned chk[2] = {0, 0};
+    if (b->total_K > 0) {
+        MCB_CUDA(cudaMemsetAsync(b->d_check, 0, sizeof chk, st));
+        const int grid = (int)std::min<long long>((b->total_K + 255) / 256, (long long)std::max(b->sm_count, 1) * 8);
+        batch_validate_kernel<<<grid, 256, 0, st>>>(b->d_off, b->total_K, b->nnz, b->d_check);
+        MCB_CUDA(cudaGetLastError());
+        MCB_CUDA(cudaMemcpyAsync(chk, b->d_check, sizeof chk, cudaMemcpyDeviceToHost, st));
+    }
+    MCB_CUDA(cudaStreamSynchronize(st));
+    if (chk[0]) {
+        set_error("mcbgpu_batch_upload: offsets must be non-decreasing from 0 to nnz");
+        return MCBGPU_E_ARG;
+    }
+    const long long max_len = chk[1];
     if (max_len > kBatchMaxN) {  // a list has at most N distinct coordinates
         set_error("mcbgpu_batch_upload: a coordinate list is longer than N");
         return MCBGPU_E_ARG;
@@ -742,15 +781,6 @@ int mcbgpu_batch_upload(mcbgpu_batch *b, const int32_t *weight, const int64_t *o
         b->pair_cap = cap;
         b->pair_slabs = slabs;
     }
-    cudaStream_t st = (cudaStream_t)stream;
-    if (b->total_K > 0) {
-        MCB_CUDA(cudaMemcpyAsync(b->d_weight, weight, sizeof(int32_t) * (size_t)b->total_K, cudaMemcpyHostToDevice,
-                                 st));
-        MCB_CUDA(cudaMemcpyAsync(b->d_off, offsets, sizeof(int64_t) * (size_t)(b->total_K + 1),
-                                 cudaMemcpyHostToDevice, st));
-    }
-    if (b->nnz > 0)
-        MCB_CUDA(cudaMemcpyAsync(b->d_coords, coords, sizeof(int32_t) * (size_t)b->nnz, cudaMemcpyHostToDevice, st));
     b->uploaded = true;
     return MCBGPU_OK;
 }
