@@ -454,9 +454,13 @@ struct LocalCandidate {
 struct RootOutput {
     std::vector<LocalCandidate> cands;
     std::vector<int> coords;
-    // unordered_map<u64, indices> with the reference's key and insertion sequence
-    // (include/cycle_searcher.h:23-61); only its iteration order is used.
-    std::unordered_map<unsigned long long, std::vector<int>> groups;
+    // unordered_map keyed as the reference's, with the same insertion sequence
+    // (include/cycle_searcher.h:23-61); only its iteration order is used, and that
+    // order depends on the keys and their sequence, not on the mapped values.  Each
+    // key maps to the first and last of its candidates, chained in insertion order
+    // through `next` (no allocation per key).
+    std::unordered_map<unsigned long long, std::pair<int, int>> groups;
+    std::vector<int> next;
 };
 
 struct TreeWorkspace {
@@ -573,12 +577,15 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
         }
         int local = (int)out.cands.size();
         out.cands.push_back(lc);
+        out.next.push_back(-1);
         unsigned long long key = ((unsigned long long)std::min(a, b) << 32) | std::max(a, b);
         auto it = out.groups.find(key);
-        if (it == out.groups.end())
-            out.groups.insert(std::make_pair(key, std::vector<int>(1, local)));
-        else
-            it->second.push_back(local);
+        if (it == out.groups.end()) {
+            out.groups.insert(std::make_pair(key, std::make_pair(local, local)));
+        } else {
+            out.next[it->second.second] = local;
+            it->second.second = local;
+        }
     }
     if (tree_parent) {
         int *tp = tree_parent + (size_t)tidx * n;
@@ -839,7 +846,8 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
             int t = P->fvs_array[vtx];
             if (t < 0) continue;
             for (auto it = outs[t].groups.begin(); it != outs[t].groups.end(); ++it)
-                for (int loc : it->second) items.push_back({outs[t].cands[loc].weight, t, loc});
+                for (int loc = it->second.first; loc >= 0; loc = outs[t].next[loc])
+                    items.push_back({outs[t].cands[loc].weight, t, loc});
         }
         std::sort(items.begin(), items.end(), [](const Item &a, const Item &b) { return a.weight < b.weight; });
         const size_t K = items.size();
