@@ -50,6 +50,22 @@ def test_single_cycle_graph(tmp_path):
     assert len(read_rows(out)) == 2
 
 
+def test_tree_has_an_empty_basis(tmp_path):
+    # no cycle at all: no candidate, no GPU work, weight 0; with --bcc every edge is a
+    # bridge, so no component is solved and no row is written
+    mtx = tmp_path / "path.mtx"
+    mtx.write_text("%%MatrixMarket matrix coordinate integer symmetric\n5 5 4\n1 2 1\n2 3 2\n3 4 3\n4 5 4\n")
+    out = tmp_path / "stats.csv"
+    r = run(mtx, out, 1)
+    assert r.returncode == 0, r.stderr
+    row = read_rows(out)[0]
+    assert int(row["Final_cycles"]) == 0 and int(row["Initial_Cycles"]) == 0 and int(row["Total_Weight"]) == 0
+    out2 = tmp_path / "stats_bcc.csv"
+    r = run(mtx, out2, 1, "--bcc")
+    assert r.returncode == 0, r.stderr
+    assert "0 problem(s)" in r.stdout and not out2.exists()
+
+
 def expected_cycles(fx, use_input_ids):
     p = Problem.from_mtx(fx["mtx"]).prepare(threads=2, cycle_lists=False)
     root, edge, weight, _ = p.candidates()
