@@ -29,7 +29,9 @@ BatchSolver (one persistent launch, one CTA per problem), the plain GPU form (th
 single-problem solver, problem after problem) on a sample beside it, and the
 biconnected components of a --blocks block tree in a second batch.
 
-`--impl reference` times only that CPU implementation and prints its own line.
+`--impl reference` times only that CPU implementation and prints its own line (with
+`--workload batch`: full solves of a time-bounded sample of the batch's graphs,
+extrapolated by each problem's label cost N * F * n').
 Under torchrun (N > 1) every rank solves its own replica (the loop does not shard).
 """
 from __future__ import annotations
@@ -47,6 +49,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MCB solve time (s) & search HBM GB/s: batched+learned vs plain GPU, exact"
+BATCH_WORKLOAD = ("batched: %d random graphs, n log-uniform [50,5000], avg degree U[2.5,5], w U[1,255], seed %d; "
+                  "one batched solve of all of them")
 
 
 def log(*a):
@@ -195,9 +199,93 @@ def cpu_baseline(p, iters, threads):
                       "precompute over all FVS trees dominates and is constant)" % (done, n, sec, n, done)}
 
 
+def label_cost(info):
+    """Per-solve work of the reference CPU loop on one problem: every iteration
+    relabels all FVS trees, N * F * n' label writes (the constant that the time
+    extrapolation of a sample scales by)."""
+    return float(info.num_coords) * info.fvs_size * info.reduced_nodes
+
+
+def batch_cpu_baseline(graphs, costs, threads, budget_s, want=None):
+    """Full solves of the reference CPU main loop (oracle port of
+    mcb/mcb_non_cpu_rd.cpp:264-342) on a strided sample of the batch's graphs, taken
+    in order until `budget_s` seconds of solve time are spent, skipping a problem
+    whose predicted time (its cost at the rate seen so far) is above half the budget;
+    extrapolated to the whole batch by the label cost N * F * n' of every problem
+    (the rate per unit of cost is flat in problem size).  `costs` maps each
+    graph index to its cost (graphs that are a single ring or a tree are absent);
+    `want` maps graph index to the GPU's (selected ranks, total weight) to compare."""
+    import numpy as np
+
+    import oracle
+    from minimumcyclebasis_gb300 import Problem
+    threads = threads or os.cpu_count() or 1
+    idx = sorted(costs)
+    stride = 16
+    order = [j for off in range(stride) for j in idx[(off * 7) % stride::stride]]
+    t_sum, c_sum, solved, checked, skipped = 0.0, 0.0, 0, 0, 0
+    rate0 = 1.2e-8 / threads  # seconds per unit of cost before any measurement
+    for j in order:
+        rate = t_sum / c_sum if c_sum > 0 and t_sum > 0.5 else rate0
+        if costs[j] * rate > budget_s / 2:
+            skipped += 1
+            continue
+        p = Problem.from_graph(graphs[j]).prepare(threads=threads, keep_trees=True)
+        sel, tot, sec = oracle.solve(p, threads=threads)
+        if want is not None and j in want:
+            assert np.array_equal(sel, want[j][0]) and tot == want[j][1], "oracle and GPU results differ"
+            checked += 1
+        t_sum += sec
+        c_sum += costs[j]
+        solved += 1
+        if t_sum >= budget_s:
+            break
+    total_cost = sum(costs.values())
+    value = t_sum / max(c_sum, 1.0) * total_cost
+    return {"value": value, "unit": "s", "cores": threads, "kind": "port",
+            "sample": "full solves of %d of the %d searched problems by the reference CPU main loop (oracle port "
+                      "of mcb/mcb_non_cpu_rd.cpp:264-342), %.2f s, extrapolated by the per-problem label cost "
+                      "N*F*n' (sample %.3g of %.3g; %d problems predicted above half the budget skipped)%s"
+                      % (solved, len(idx), t_sum, c_sum, total_cost, skipped,
+                         "; %d checked equal to the GPU's" % checked if want is not None else "")}
+
+
+def run_reference_batch(args, world, rank, pg):
+    import numpy as np
+
+    from minimumcyclebasis_gb300 import Problem, batch_graphs
+    threads = args.cpu_threads or os.cpu_count() or 1
+    graphs = batch_graphs(args.batch_count, seed=args.seed)
+    costs, Ns = {}, []
+    for j, g in enumerate(graphs):
+        info = Problem.from_graph(g).prepare(threads=threads).info
+        if not info.single_cycle and info.num_coords > 0:
+            costs[j] = label_cost(info)
+            Ns.append(info.num_coords)
+    for _ in range(args.warmup):
+        batch_cpu_baseline(graphs, costs, threads, args.cpu_budget / 8)
+    vals = []
+    t0 = time.time()
+    for _ in range(args.steps):
+        vals.append(batch_cpu_baseline(graphs, costs, threads, args.cpu_budget))
+    wall = time.time() - t0
+    v = statistics.mean(x["value"] for x in vals)
+    cb = dict(vals[-1])
+    cb["value"] = v
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / max(args.steps, 1) * 1000.0, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOAD % (args.batch_count, args.seed), "problems": len(costs),
+                       "N_max": int(max(Ns, default=0)), "N_sum": int(np.sum(Ns)),
+                       "form": "reference CPU loop (oracle port), bounded sample of full solves"},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def run_reference(args, world, rank, pg):
     if rank != 0:
         return None
+    if args.workload == "batch":
+        return run_reference_batch(args, world, rank, pg)
     p = prepare(args, keep_trees=True)
     threads = args.cpu_threads or os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -372,8 +460,8 @@ def run_batch(args, world, rank, local, pg):
     t0 = time.time()
 
     def problems(graphs):
-        items, host_total, nsc = [], 0, 0
-        for g in graphs:
+        items, host_total, nsc, costs = [], 0, 0, {}
+        for j, g in enumerate(graphs):
             p = Problem.from_graph(g).prepare(threads=0)
             if p.info.single_cycle:  # the graph is one cycle: its basis needs no search
                 host_total += int(g.w.astype(np.int64).sum())
@@ -384,13 +472,14 @@ def run_batch(args, world, rank, local, pg):
             _, _, w, _ = p.candidates()
             off, co = p.cycle_lists()
             items.append((p.N, w, off, co))
-        return items, host_total, nsc
+            costs[j] = label_cost(p.info)
+        return items, host_total, nsc, costs
 
     graphs = batch_graphs(args.batch_count, seed=args.seed + rank)
-    items, host_total, nsc = problems(graphs)
+    items, host_total, nsc, costs = problems(graphs)
     bt = block_tree_graph(args.blocks, seed=args.seed + rank)
     comps = bcc_split(bt)
-    bitems, bhost_total, bnsc = problems(comps)
+    bitems, bhost_total, bnsc, _ = problems(comps)
     log("prepared in %.1fs: %d batch problems (%d rings), %d block-tree components (%d rings)"
         % (time.time() - t0, len(items), nsc, len(bitems), bnsc))
     stream = torch.cuda.Stream()
@@ -485,6 +574,10 @@ def run_batch(args, world, rank, local, pg):
             lib.mcbgpu_free_pinned(h)
     if rank != 0:
         return None
+    cb = None
+    if world == 1 and not args.no_cpu_baseline:
+        want = {j: (sels[i], tots[i]) for i, j in enumerate(sorted(costs))}
+        cb = batch_cpu_baseline(graphs, costs, args.cpu_threads, args.cpu_budget, want)
     nnz = int(bs.offsets[-1])
     scanned = int(prof[:, 6].sum())
     K = int(bs.weight.shape[0])
@@ -496,9 +589,7 @@ def run_batch(args, world, rank, local, pg):
     return {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": "batched: %d random graphs, n log-uniform [50,5000], avg degree U[2.5,5], "
-                                   "w U[1,255], seed %d; one batched solve of all of them" % (args.batch_count,
-                                                                                               args.seed),
+            "config": {"workload": BATCH_WORKLOAD % (args.batch_count, args.seed),
                        "problems": len(items), "rings_on_host": nsc, "N_max": int(Ns.max()), "N_sum": int(Ns.sum()),
                        "K": K, "cycle_nnz": nnz, "form": "batched (one persistent launch, one CTA per problem)",
                        "total_weight": int(tots.sum()) + host_total,
@@ -520,7 +611,7 @@ def run_batch(args, world, rank, local, pg):
                          "bytes_per_launch": scan_bytes, "launch_ms": ms,
                          "note": "scan bytes (offsets + lists of the scanned candidates) per batched solve; the "
                                  "kernel is latency-bound on the per-problem critical path"},
-            "cpu_baseline": None}
+            "cpu_baseline": cb}
 
 
 def main():
@@ -535,6 +626,8 @@ def main():
     ap.add_argument("--max-iterations", type=int, default=-1)
     ap.add_argument("--cpu-iters", type=int, default=40, help="iterations in the CPU baseline sample")
     ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--cpu-budget", type=float, default=20.0,
+                    help="seconds of CPU solve time in the batched workload's baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
