@@ -57,6 +57,8 @@ def _headers() -> list[str]:
     hs = [os.path.join(INC, f) for f in os.listdir(INC) if f.endswith(".h")]
     gdir = os.path.join(CSRC, "gpu")
     hs += [os.path.join(gdir, f) for f in os.listdir(gdir) if f.endswith(".cuh")]
+    hdir = os.path.join(CSRC, "host")
+    hs += [os.path.join(hdir, f) for f in os.listdir(hdir) if f.endswith(".h")]
     return hs
 
 

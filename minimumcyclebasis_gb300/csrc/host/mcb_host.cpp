@@ -7,10 +7,13 @@
 // the candidate list.  Where the reference's result depends on a standard-library
 // behaviour (std::sort's permutation of equal keys, std::priority_queue's order of
 // equal distances, std::unordered_map's iteration order), this file calls the same
-// standard-library routine on the same sequence, which gives the same permutation.
+// standard-library routine on the same sequence, which gives the same permutation;
+// the tree searches' queue is the one exception: dist_heap.h restates its heap moves
+// (faster, same pop order, checked against std::priority_queue by a test).
 // The recursive DFS passes of the reference are restated as explicit-stack loops
 // that visit edges in the same order (the reference needs `ulimit -s unlimited`).
 #include "mcbhost.h"
+#include "dist_heap.h"
 
 #include <algorithm>
 #include <chrono>
@@ -19,7 +22,6 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
-#include <queue>
 #include <string>
 #include <unordered_map>
 #include <unordered_set>
@@ -103,6 +105,15 @@ struct mcbh_problem {
     // coordinates
     std::vector<u32> coord_edges;
     std::vector<int> edge_coord;
+    // slot pairs of the reduced graph: the lower slot of every pair in ascending
+    // order, and each slot's pair index
+    std::vector<u32> pair_first, slot_pair;
+    // the reduced graph's slots as (column, weight) records, for the tree searches
+    struct Arc {
+        u32 col;
+        int w;
+    };
+    std::vector<Arc> arcs;
     // trees
     std::vector<int> tree_parent;  // F x n'
     std::vector<u32> lay_rows, lay_cols, lay_nodes;
@@ -431,12 +442,6 @@ bool spanning_tree(mcbh_problem &P, int src) {
 // ---------------------------------------------------------------------------
 // Per-root shortest-path tree + candidates (include/Dijkstra.h:78-254,
 // include/work_per_thread.h:92-147).
-struct HeapLess {  // include/Dijkstra.h:37-41: min-heap on distance only
-    bool operator()(const std::pair<int, int> &a, const std::pair<int, int> &b) const {
-        return a.second > b.second;
-    }
-};
-
 struct LevelItem {  // include/Dijkstra.h:7-21
     int offset, level;
 };
@@ -463,22 +468,24 @@ struct RootOutput {
     std::vector<int> next;
 };
 
+// One vertex of a tree search: distance, parent vertex, slot into it from the
+// parent, and whether it is settled (one 16-byte record per vertex).
+struct VertexState {
+    int dist, par, pedge, done;
+};
+
 struct TreeWorkspace {
-    std::vector<int> dist, par, level, pedge;
-    std::vector<char> in_tree;
+    std::vector<VertexState> vs;
+    std::vector<int> level;
     std::vector<u32> pop_order;
-    std::vector<unsigned char> is_tree;
+    std::vector<unsigned char> pair_tree;
     std::vector<u32> nte;
-    std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>, HeapLess> pq;
+    DistHeap pq;  // include/Dijkstra.h:37-44: min-heap on distance only
     std::vector<LevelItem> lv;
     std::vector<int> tmp;
-    void init(int n, size_t slots) {
-        dist.assign(n, -1);
-        par.assign(n, -1);
-        level.assign(n, -1);
-        pedge.assign(n, -1);
-        in_tree.assign(n, 0);
-        is_tree.assign(slots, 0);
+    void init(int n, size_t pairs) {
+        vs.assign(n, VertexState{-1, -1, -1, 0});
+        pair_tree.assign(pairs, 0);
         pop_order.clear();
         pop_order.reserve(n);
     }
@@ -489,49 +496,46 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
     const Graph &g = P.rg;
     const int n = g.n;
     const u32 src = P.fvs_vertices[tidx];
-    ws.init(n, g.slots());
+    ws.init(n, P.pair_first.size());
     // dijkstra::dijkstra_sp
     std::vector<u32> tree_edges;
     tree_edges.reserve(n);
-    ws.dist[src] = 0;
-    ws.level[src] = 0;
+    // (the level of a vertex, set with its parent in the reference, is its final
+    // parent's level + 1: computed after the search, in settle order, where needed)
+    VertexState *vs = ws.vs.data();
+    const mcbh_problem::Arc *arcs = P.arcs.data();
+    vs[src].dist = 0;
     ws.pq.push(std::make_pair((int)src, 0));
     while (!ws.pq.empty()) {
         std::pair<int, int> val = ws.pq.top();
         ws.pq.pop();
         int x = val.first;
-        if (ws.in_tree[x]) continue;
-        if ((u32)x != src) tree_edges.push_back((u32)ws.pedge[x]);
-        ws.in_tree[x] = 1;
+        VertexState &sx = vs[x];
+        if (sx.done) continue;
+        if ((u32)x != src) tree_edges.push_back((u32)sx.pedge);
+        sx.done = 1;
         ws.pop_order.push_back((u32)x);
+        const int dx = sx.dist;
         for (u32 o = g.ro[x]; o < g.ro[x + 1]; o++) {
-            u32 c = g.cols[o];
-            if (ws.in_tree[c]) continue;
-            int ew = g.w[o];
-            if (ws.dist[c] == -1 || ws.dist[x] + ew < ws.dist[c]) {
-                ws.dist[c] = ws.dist[x] + ew;
-                ws.pq.push(std::make_pair((int)c, ws.dist[c]));
-                ws.par[c] = x;
-                ws.pedge[c] = (int)o;
-                ws.level[c] = ws.level[x] + 1;
+            const mcbh_problem::Arc a = arcs[o];
+            VertexState &sc = vs[a.col];
+            if (sc.done) continue;
+            const int nd = dx + a.w;
+            if (sc.dist == -1 || nd < sc.dist) {
+                sc.dist = nd;
+                ws.pq.push(std::make_pair((int)a.col, nd));
+                sc.par = x;
+                sc.pedge = (int)o;
             }
         }
     }
-    // dijkstra::compute_non_tree_edges
-    for (u32 o : tree_edges) ws.is_tree[o] = 1;
+    // dijkstra::compute_non_tree_edges: its scan over the slots in ascending order
+    // keeps, of every pair that holds no tree slot, the slot met first, i.e. the lower
+    // one; the same list from one pass over the pairs in order of their lower slot.
+    for (u32 o : tree_edges) ws.pair_tree[P.slot_pair[o]] = 1;
     ws.nte.clear();
-    for (size_t i = 0; i < g.slots(); i++) {
-        if (ws.is_tree[i] == 1) continue;
-        unsigned char rs = ws.is_tree[g.rev[i]];
-        if (rs == 1) {
-            ws.is_tree[i] = 1;
-        } else if (rs == 2) {
-            ws.is_tree[i] = 2;
-        } else {
-            ws.is_tree[i] = 2;
-            ws.nte.push_back((u32)i);
-        }
-    }
+    for (size_t k = 0; k < P.pair_first.size(); k++)
+        if (!ws.pair_tree[k]) ws.nte.push_back(P.pair_first[k]);
     // dijkstra::is_edge_cycle: accepted iff the two root paths meet only at the root
     // and contain no FVS vertex with a smaller id than the root.  Computed here per
     // vertex: the root child a vertex hangs under, and whether its root path holds
@@ -545,7 +549,7 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
             branch[x] = -1;
             blocked[x] = self_bad;
         } else {
-            int p = ws.par[x];
+            int p = vs[x].par;
             branch[x] = ((u32)p == src) ? (int)x : branch[p];
             blocked[x] = blocked[p] || self_bad;
         }
@@ -555,7 +559,7 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
         if (blocked[a] || blocked[b]) continue;
         bool lca_root = (a == src) || (b == src) || (branch[a] != branch[b]);
         if (!lca_root) continue;
-        int weight = ws.dist[a] + ws.dist[b] + g.w[off];
+        int weight = vs[a].dist + vs[b].dist + g.w[off];
         LocalCandidate lc;
         lc.edge = (int)off;
         lc.weight = weight;
@@ -564,12 +568,12 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
         if (want_lists) {
             size_t b0 = out.coords.size();
             if (P.edge_coord[off] >= 0) out.coords.push_back(P.edge_coord[off]);
-            for (u32 x = a; x != src; x = (u32)ws.par[x]) {
-                int c = P.edge_coord[ws.pedge[x]];
+            for (u32 x = a; x != src; x = (u32)vs[x].par) {
+                int c = P.edge_coord[vs[x].pedge];
                 if (c >= 0) out.coords.push_back(c);
             }
-            for (u32 x = b; x != src; x = (u32)ws.par[x]) {
-                int c = P.edge_coord[ws.pedge[x]];
+            for (u32 x = b; x != src; x = (u32)vs[x].par) {
+                int c = P.edge_coord[vs[x].pedge];
                 if (c >= 0) out.coords.push_back(c);
             }
             std::sort(out.coords.begin() + b0, out.coords.end());
@@ -589,12 +593,16 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
     }
     if (tree_parent) {
         int *tp = tree_parent + (size_t)tidx * n;
-        for (int v = 0; v < n; v++) tp[v] = ws.pedge[v];
+        for (int v = 0; v < n; v++) tp[v] = vs[v].pedge;
         tp[src] = -1;
     }
     if (lay_rows) {
         // dijkstra::fill_tree_edges: (offset, level) items, root first, then tree
         // edges in pop order; std::sort by level only.
+        ws.level.assign(n, -1);
+        ws.level[src] = 0;
+        for (u32 x : ws.pop_order)
+            if (x != src) ws.level[x] = ws.level[vs[x].par] + 1;
         ws.lv.clear();
         ws.lv.push_back({-1, 0});
         for (u32 o : tree_edges) ws.lv.push_back({(int)o, ws.level[g.cols[o]]});
@@ -812,6 +820,20 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
             P->lay_cols.assign((size_t)F * n, 0);
             P->lay_edge.assign((size_t)F * n, -1);
             P->lay_nodes.assign((size_t)F * n, 0);
+        }
+        {
+            const Graph &g = P->rg;
+            P->pair_first.clear();
+            P->pair_first.reserve(g.slots() / 2);
+            P->slot_pair.assign(g.slots(), 0);
+            P->arcs.resize(g.slots());
+            for (size_t i = 0; i < g.slots(); i++) P->arcs[i] = {g.cols[i], g.w[i]};
+            for (size_t i = 0; i < g.slots(); i++) {
+                if (i < g.rev[i]) {
+                    P->slot_pair[i] = P->slot_pair[g.rev[i]] = (u32)P->pair_first.size();
+                    P->pair_first.push_back((u32)i);
+                }
+            }
         }
         std::vector<RootOutput> outs(F);
         int threads = opt->threads > 0 ? opt->threads : omp_get_max_threads();
