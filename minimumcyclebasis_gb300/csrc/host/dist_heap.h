@@ -65,3 +65,46 @@ struct DistHeap {
         a[i] = v;
     }
 };
+
+// Monotone radix queue (Ahuja, Mehlhorn, Orlin and Tarjan, "Faster algorithms for
+// the shortest path problem", 1990): entries are (distance, vertex) with unsigned
+// distances that never fall below the last one taken out.  Bucket 0 holds the
+// entries at exactly that last distance; bucket i > 0 those whose distance first
+// differs from it in bit i - 1 (counting from bit 0).  Taking out refills bucket 0
+// from the lowest non-empty bucket by moving its entries down by their new
+// difference.  Equal distances come out in no particular order.
+struct RadixQueue {
+    std::vector<std::pair<unsigned, int>> b[33];
+    unsigned last = 0;
+    size_t count = 0;
+
+    bool empty() const { return count == 0; }
+    void clear() {
+        for (auto &v : b) v.clear();
+        last = 0;
+        count = 0;
+    }
+    static int bucket_of(unsigned key, unsigned ref) {
+        return key == ref ? 0 : 32 - __builtin_clz(key ^ ref);
+    }
+    void push(unsigned key, int vertex) {
+        b[bucket_of(key, last)].push_back(std::make_pair(key, vertex));
+        count++;
+    }
+    // the vertex of an entry at the smallest distance (the queue must not be empty)
+    std::pair<unsigned, int> pop() {
+        if (b[0].empty()) {
+            int i = 1;
+            while (b[i].empty()) i++;
+            unsigned m = b[i][0].first;
+            for (const auto &e : b[i]) m = e.first < m ? e.first : m;
+            last = m;
+            for (const auto &e : b[i]) b[bucket_of(e.first, last)].push_back(e);
+            b[i].clear();
+        }
+        const std::pair<unsigned, int> e = b[0].back();
+        b[0].pop_back();
+        count--;
+        return e;
+    }
+};

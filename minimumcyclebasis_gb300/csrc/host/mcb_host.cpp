@@ -16,6 +16,7 @@
 #include "dist_heap.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -114,6 +115,7 @@ struct mcbh_problem {
         int w;
     };
     std::vector<Arc> arcs;
+    bool fast_search_ok = false;  // every weight >= 1 and no distance can overflow
     // trees
     std::vector<int> tree_parent;  // F x n'
     std::vector<u32> lay_rows, lay_cols, lay_nodes;
@@ -469,13 +471,15 @@ struct RootOutput {
 };
 
 // One vertex of a tree search: distance, parent vertex, slot into it from the
-// parent, and whether it is settled (one 16-byte record per vertex).
+// parent, and flags (bit 0 settled; bit 1, fast search only: the parent has a rival
+// at the same distance), one 16-byte record per vertex.
 struct VertexState {
     int dist, par, pedge, done;
 };
 
 struct TreeWorkspace {
     std::vector<VertexState> vs;
+    RadixQueue rq;
     std::vector<int> level;
     std::vector<u32> pop_order;
     std::vector<unsigned char> pair_tree;
@@ -491,20 +495,16 @@ struct TreeWorkspace {
     }
 };
 
-void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput &out, bool want_lists,
-                  int *tree_parent, u32 *lay_rows, u32 *lay_cols, int *lay_edge, u32 *lay_nodes) {
+// dijkstra::dijkstra_sp (include/Dijkstra.h:78-124) as the reference runs it: the
+// binary heap decides which of two equally near vertices settles first.  (The level
+// of a vertex, set with its parent in the reference, is its final parent's level + 1:
+// computed after the search, in settle order, where needed.)
+void search_exact(const mcbh_problem &P, u32 src, TreeWorkspace &ws, std::vector<u32> &tree_edges) {
     const Graph &g = P.rg;
-    const int n = g.n;
-    const u32 src = P.fvs_vertices[tidx];
-    ws.init(n, P.pair_first.size());
-    // dijkstra::dijkstra_sp
-    std::vector<u32> tree_edges;
-    tree_edges.reserve(n);
-    // (the level of a vertex, set with its parent in the reference, is its final
-    // parent's level + 1: computed after the search, in settle order, where needed)
     VertexState *vs = ws.vs.data();
     const mcbh_problem::Arc *arcs = P.arcs.data();
     vs[src].dist = 0;
+    ws.pq.clear();
     ws.pq.push(std::make_pair((int)src, 0));
     while (!ws.pq.empty()) {
         std::pair<int, int> val = ws.pq.top();
@@ -529,6 +529,83 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
             }
         }
     }
+}
+
+// The same search with a monotone radix queue, for graphs whose weights are all at
+// least 1 and whose distances cannot overflow.  Every shortest-path parent of a
+// vertex is then strictly nearer than the vertex and settles before it, and the
+// parent the reference keeps is the first of them to settle (only a strictly shorter
+// path replaces a parent).  Parents at different distances settle in distance order
+// under any queue; only two parents at the same distance, each on a shortest path
+// through a different vertex, are ordered by the reference's heap.  The search
+// counts the vertices whose current parent has such a rival (cleared when a
+// strictly shorter path replaces the parent) and returns false if any is left; the
+// caller then runs search_exact.  Otherwise distances, parents and parent slots equal
+// the reference's; the settle order may differ among equal distances, which only
+// the level-ordered layout (built from search_exact alone) depends on.
+bool search_fast(const mcbh_problem &P, u32 src, TreeWorkspace &ws, std::vector<u32> &tree_edges) {
+    const Graph &g = P.rg;
+    VertexState *vs = ws.vs.data();
+    const mcbh_problem::Arc *arcs = P.arcs.data();
+    long long rivals = 0;
+    vs[src].dist = 0;
+    ws.rq.clear();
+    ws.rq.push(0u, (int)src);
+    while (!ws.rq.empty()) {
+        const int x = ws.rq.pop().second;
+        VertexState &sx = vs[x];
+        if (sx.done & 1) continue;
+        if ((u32)x != src) tree_edges.push_back((u32)sx.pedge);
+        sx.done |= 1;
+        ws.pop_order.push_back((u32)x);
+        const int dx = sx.dist;
+        for (u32 o = g.ro[x]; o < g.ro[x + 1]; o++) {
+            const mcbh_problem::Arc a = arcs[o];
+            VertexState &sc = vs[a.col];
+            if (sc.done & 1) continue;
+            const int nd = dx + a.w;
+            if (sc.dist == -1 || nd < sc.dist) {
+                sc.dist = nd;
+                ws.rq.push((unsigned)nd, (int)a.col);
+                sc.par = x;
+                sc.pedge = (int)o;
+                if (sc.done & 2) {
+                    sc.done = 0;
+                    rivals--;
+                }
+            } else if (nd == sc.dist && sc.par != x && !(sc.done & 2) && vs[sc.par].dist == dx) {
+                sc.done |= 2;
+                rivals++;
+            }
+        }
+    }
+    return rivals == 0;
+}
+
+void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput &out, bool want_lists,
+                  int *tree_parent, u32 *lay_rows, u32 *lay_cols, int *lay_edge, u32 *lay_nodes,
+                  int *fast_result) {
+    const Graph &g = P.rg;
+    const int n = g.n;
+    const u32 src = P.fvs_vertices[tidx];
+    ws.init(n, P.pair_first.size());
+    std::vector<u32> tree_edges;
+    tree_edges.reserve(n);
+    // fast_result: in, whether to try search_fast; out, 1 if it was kept, 0 if it
+    // was tried and fell back to search_exact, -1 if not tried
+    bool fast_done = false;
+    if (*fast_result && !lay_rows) {
+        fast_done = search_fast(P, src, ws, tree_edges);
+        *fast_result = fast_done ? 1 : 0;
+        if (!fast_done) {
+            ws.init(n, P.pair_first.size());
+            tree_edges.clear();
+        }
+    } else {
+        *fast_result = -1;
+    }
+    if (!fast_done) search_exact(P, src, ws, tree_edges);
+    VertexState *vs = ws.vs.data();
     // dijkstra::compute_non_tree_edges: its scan over the slots in ascending order
     // keeps, of every pair that holds no tree slot, the slot met first, i.e. the lower
     // one; the same list from one pass over the pairs in order of their lower slot.
@@ -827,7 +904,13 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
             P->pair_first.reserve(g.slots() / 2);
             P->slot_pair.assign(g.slots(), 0);
             P->arcs.resize(g.slots());
-            for (size_t i = 0; i < g.slots(); i++) P->arcs[i] = {g.cols[i], g.w[i]};
+            long long wmin = 1, wmax = 0;
+            for (size_t i = 0; i < g.slots(); i++) {
+                P->arcs[i] = {g.cols[i], g.w[i]};
+                wmin = std::min(wmin, (long long)g.w[i]);
+                wmax = std::max(wmax, (long long)g.w[i]);
+            }
+            P->fast_search_ok = wmin >= 1 && wmax * (long long)(g.n + 1) < 0x7fffffffLL;
             for (size_t i = 0; i < g.slots(); i++) {
                 if (i < g.rev[i]) {
                     P->slot_pair[i] = P->slot_pair[g.rev[i]] = (u32)P->pair_first.size();
@@ -838,16 +921,27 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
         std::vector<RootOutput> outs(F);
         int threads = opt->threads > 0 ? opt->threads : omp_get_max_threads();
         bool lists = opt->cycle_lists != 0;
+        // The radix-queue search is tried while at most a quarter of the roots tried
+        // so far had to fall back (graphs with many equal path lengths, e.g. small
+        // integer weights, fall back on most roots).  Which roots take which search
+        // changes no output.
+        std::atomic<int> fast_tries{0}, fast_fallbacks{0};
 #pragma omp parallel num_threads(threads)
         {
             TreeWorkspace ws;
 #pragma omp for schedule(dynamic, 1)
-            for (int t = 0; t < F; t++)
+            for (int t = 0; t < F; t++) {
+                const int tries = fast_tries.load(std::memory_order_relaxed);
+                int fast = P->fast_search_ok &&
+                           (tries < 64 || 4 * fast_fallbacks.load(std::memory_order_relaxed) <= tries);
                 process_root(*P, t, ws, outs[t], lists, opt->keep_trees ? P->tree_parent.data() : nullptr,
                              opt->ref_layout ? P->lay_rows.data() : nullptr,
                              opt->ref_layout ? P->lay_cols.data() : nullptr,
                              opt->ref_layout ? P->lay_edge.data() : nullptr,
-                             opt->ref_layout ? P->lay_nodes.data() : nullptr);
+                             opt->ref_layout ? P->lay_nodes.data() : nullptr, &fast);
+                if (fast >= 0) fast_tries.fetch_add(1, std::memory_order_relaxed);
+                if (fast == 0) fast_fallbacks.fetch_add(1, std::memory_order_relaxed);
+            }
         }
         I.t_trees = now_s() - t0;
 

@@ -1,7 +1,10 @@
 // DistHeap against std::priority_queue with a distance-only comparator (the queue of
 // the reference's tree searches): random push/pop sequences, distances drawn from
 // small ranges so that ties are dense, and Dijkstra-like monotone sequences.  Every
-// top() and size() must agree.  Exit status 0 and "ok" on success.
+// top() and size() must agree.  RadixQueue on monotone sequences (no push below the
+// last distance taken out): the same distances come out in the same order as from
+// std::priority_queue, and every pushed vertex comes out exactly once.  Exit status 0
+// and "ok" on success.
 #include <cstdint>
 #include <cstdio>
 #include <queue>
@@ -63,6 +66,40 @@ int main() {
             checked++;
         }
         if (!dh.empty()) return 1;
+    }
+    for (int trial = 0; trial < 3000; trial++) {
+        std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>, ByDistance> pq;
+        RadixQueue rq;
+        std::vector<int> out_count;
+        const int range = 1 + (int)(next_u64() % (trial % 2 ? 8 : 100000));
+        const int ops = 1 + (int)(next_u64() % 4000);
+        unsigned base = (unsigned)(next_u64() % 1000);
+        int id = 0;
+        for (int k = 0; k < ops || !pq.empty(); k++) {
+            if (k < ops && (pq.empty() || next_u64() % 3 != 0)) {
+                unsigned d = base + (unsigned)(next_u64() % range);
+                pq.push(std::make_pair(id, (int)d));
+                rq.push(d, id);
+                out_count.push_back(0);
+                id++;
+            } else {
+                if (rq.empty()) {
+                    std::printf("radix queue empty early: trial %d\n", trial);
+                    return 1;
+                }
+                std::pair<unsigned, int> e = rq.pop();
+                if ((int)e.first != pq.top().second || out_count[e.second]++ != 0) {
+                    std::printf("radix mismatch: trial %d op %d\n", trial, k);
+                    return 1;
+                }
+                base = e.first;
+                pq.pop();
+                checked++;
+            }
+        }
+        if (!rq.empty()) return 1;
+        for (int c : out_count)
+            if (c != 1) return 1;
     }
     std::printf("ok %lld pops\n", checked);
     return 0;

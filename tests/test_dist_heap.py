@@ -1,6 +1,7 @@
-"""The tree searches' heap (csrc/host/dist_heap.h) pops in the same order as
-std::priority_queue with the reference's distance-only comparator
-(include/Dijkstra.h:37-44): compiled with g++ and run on random sequences dense in ties."""
+"""The tree searches' queues (csrc/host/dist_heap.h): DistHeap pops in the same order
+as std::priority_queue with the reference's distance-only comparator
+(include/Dijkstra.h:37-44), and RadixQueue gives out the same distances in the same
+order on monotone sequences; compiled with g++ and run on random sequences dense in ties."""
 import os
 import shutil
 import subprocess
@@ -11,7 +12,7 @@ import pytest
 from conftest import ROOT
 
 
-def test_dist_heap_pops_like_the_standard_queue():
+def test_tree_search_queues_against_the_standard_queue():
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("g++ not found")

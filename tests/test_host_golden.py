@@ -97,3 +97,22 @@ def test_reference_layout_is_level_ordered():
             child = cols[E[pos]]
             assert NI[child] == pos
             assert tp[t * n + child] == E[pos]
+
+
+@pytest.mark.parametrize("family", ["random_w1000", "random_w30", "planar", "batch_w255"])
+def test_fast_and_exact_tree_searches_agree(family):
+    # the level-ordered layout is built from the reference's heap search alone;
+    # without it the radix-queue search runs (falling back where two parents tie)
+    from minimumcyclebasis_gb300 import batch_graphs, planar_chain_graph, random_graph
+    g = {"random_w1000": lambda: random_graph(3000, 6000, 1, 1000, 21),
+         "random_w30": lambda: random_graph(3000, 6000, 1, 30, 22),
+         "planar": lambda: planar_chain_graph(2500, 30, 30, 8, 1, 1000, 23),
+         "batch_w255": lambda: max(batch_graphs(24, nmin=1000, nmax=3000, seed=24), key=lambda x: x.nodes)}[family]()
+    exact = Problem.from_graph(g).prepare(threads=4, keep_trees=True, ref_layout=True)
+    fast = Problem.from_graph(g).prepare(threads=4, keep_trees=True)
+    assert exact.F > 64  # past the first roots, where the fast search is always tried
+    for x, y in zip(exact.candidates(), fast.candidates()):
+        assert np.array_equal(x, y)
+    for x, y in zip(exact.cycle_lists(), fast.cycle_lists()):
+        assert np.array_equal(x, y)
+    assert np.array_equal(exact.tree_parents(), fast.tree_parents())
