@@ -953,20 +953,37 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
             int weight;
             int tree;
             int local;
+            int len;
         };
-        std::vector<Item> items;
-        size_t total = 0;
-        for (int t = 0; t < F; t++) total += outs[t].cands.size();
-        items.reserve(total);
-        for (int vtx = 0; vtx < n; vtx++) {
-            int t = P->fvs_array[vtx];
-            if (t < 0) continue;
-            for (auto it = outs[t].groups.begin(); it != outs[t].groups.end(); ++it)
-                for (int loc = it->second.first; loc >= 0; loc = outs[t].next[loc])
-                    items.push_back({outs[t].cands[loc].weight, t, loc});
+        // the list in that order, each root's part filled in parallel
+        std::vector<int> root_of_rank;  // FVS roots in vertex-id order
+        for (int vtx = 0; vtx < n; vtx++)
+            if (P->fvs_array[vtx] >= 0) root_of_rank.push_back(P->fvs_array[vtx]);
+        std::vector<size_t> base(root_of_rank.size() + 1, 0);
+        for (size_t i = 0; i < root_of_rank.size(); i++) base[i + 1] = base[i] + outs[root_of_rank[i]].cands.size();
+        const size_t K = base.back();
+        if (K > 0xffffffffull) return MCBH_E_NOMEM;  // past the 32-bit index of the sort records
+        std::vector<Item> items(K);
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+        for (int64_t i = 0; i < (int64_t)root_of_rank.size(); i++) {
+            const int t = root_of_rank[i];
+            const RootOutput &o = outs[t];
+            size_t k = base[i];
+            for (auto it = o.groups.begin(); it != o.groups.end(); ++it)
+                for (int loc = it->second.first; loc >= 0; loc = o.next[loc])
+                    items[k++] = {o.cands[loc].weight, t, loc, o.cands[loc].coord_len};
         }
-        std::sort(items.begin(), items.end(), [](const Item &a, const Item &b) { return a.weight < b.weight; });
-        const size_t K = items.size();
+        // std::sort on the weight alone: its permutation follows from the outcomes of
+        // its comparisons, so sorting (weight, index) records gives the permutation
+        // that sorting the candidates themselves gives
+        struct Key {
+            int weight;
+            u32 index;
+        };
+        std::vector<Key> keys(K);
+#pragma omp parallel for num_threads(threads) schedule(static)
+        for (int64_t r = 0; r < (int64_t)K; r++) keys[r] = {items[r].weight, (u32)r};
+        std::sort(keys.begin(), keys.end(), [](const Key &a, const Key &b) { return a.weight < b.weight; });
         P->c_root.resize(K);
         P->c_edge.resize(K);
         P->c_weight.resize(K);
@@ -975,15 +992,17 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
         if (lists) {
             P->c_off.resize(K + 1);
             P->c_off[0] = 0;
+#pragma omp parallel for num_threads(threads) schedule(static)
+            for (int64_t r = 0; r < (int64_t)K; r++) P->c_off[r + 1] = items[keys[r].index].len;
             for (size_t r = 0; r < K; r++) {
-                nnz += outs[items[r].tree].cands[items[r].local].coord_len;
+                nnz += P->c_off[r + 1];
                 P->c_off[r + 1] = nnz;
             }
             P->c_coords.resize((size_t)nnz);
         }
 #pragma omp parallel for num_threads(threads) schedule(static)
         for (int64_t r = 0; r < (int64_t)K; r++) {
-            const Item &it = items[r];
+            const Item &it = items[keys[r].index];
             const LocalCandidate &lc = outs[it.tree].cands[it.local];
             P->c_root[r] = (int)P->fvs_vertices[it.tree];
             P->c_edge[r] = lc.edge;
