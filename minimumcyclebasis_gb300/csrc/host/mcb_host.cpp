@@ -606,9 +606,10 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
     }
     if (!fast_done) search_exact(P, src, ws, tree_edges);
     VertexState *vs = ws.vs.data();
-    // dijkstra::compute_non_tree_edges: its scan over the slots in ascending order
-    // keeps, of every pair that holds no tree slot, the slot met first, i.e. the lower
-    // one; the same list from one pass over the pairs in order of their lower slot.
+    // dijkstra::compute_non_tree_edges (include/Dijkstra.h:129-149): its scan over the
+    // slots in ascending order keeps, of every pair that holds no tree slot, the slot
+    // met first, i.e. the lower one; the same list from one pass over the pairs in
+    // order of their lower slot.
     for (u32 o : tree_edges) ws.pair_tree[P.slot_pair[o]] = 1;
     ws.nte.clear();
     for (size_t k = 0; k < P.pair_first.size(); k++)
