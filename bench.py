@@ -180,7 +180,9 @@ def config_of(p, args, extra=None):
          "reduced_nodes": i.reduced_nodes, "fvs": i.fvs_size, "N": i.num_coords, "K": i.num_candidates,
          "cycle_nnz": i.cycle_nnz, "form": args.mode,
          "l2": ("inputs (cycle lists %.2f GB) larger than the 129 MB L2; no flush" % (i.cycle_nnz * 4 / 1e9))
-         if i.cycle_nnz * 4 > 129e6 else "small case: inputs fit in L2"}
+         if i.cycle_nnz * 4 > 129e6 else "small case: inputs fit in L2",
+         "host_preparation_s": round(i.t_reduce + i.t_fvs + i.t_spanning + i.t_trees + i.t_collect, 3),
+         "host_threads": os.cpu_count()}
     if extra:
         c.update(extra)
     return c
@@ -480,6 +482,7 @@ def run_batch(args, world, rank, local, pg):
     bt = block_tree_graph(args.blocks, seed=args.seed + rank)
     comps = bcc_split(bt)
     bitems, bhost_total, bnsc, _ = problems(comps)
+    prep_s = time.time() - t0
     log("prepared in %.1fs: %d batch problems (%d rings), %d block-tree components (%d rings)"
         % (time.time() - t0, len(items), nsc, len(bitems), bnsc))
     stream = torch.cuda.Stream()
@@ -593,7 +596,8 @@ def run_batch(args, world, rank, local, pg):
                        "problems": len(items), "rings_on_host": nsc, "N_max": int(Ns.max()), "N_sum": int(Ns.sum()),
                        "K": K, "cycle_nnz": nnz, "form": "batched (one persistent launch, one CTA per problem)",
                        "total_weight": int(tots.sum()) + host_total,
-                       "l2": "inputs (%.2f GB) larger than the 129 MB L2; no flush" % ((nnz * 4 + K * 12) / 1e9)},
+                       "l2": "inputs (%.2f GB) larger than the 129 MB L2; no flush" % ((nnz * 4 + K * 12) / 1e9),
+                       "host_preparation_s": round(prep_s, 3), "host_threads": os.cpu_count()},
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": int(launches),
             "plain_gpu": {"value": plain_est_s, "unit": "s", "speedup": plain_est_s / (ms / 1e3),
                           "sample": "blocked single-problem solver on every %d-th problem (%d solves, %.1f ms), "
