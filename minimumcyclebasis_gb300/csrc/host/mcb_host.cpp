@@ -483,7 +483,6 @@ struct TreeWorkspace {
     std::vector<int> level;
     std::vector<u32> pop_order;
     std::vector<unsigned char> pair_tree;
-    std::vector<u32> nte;
     DistHeap pq;  // include/Dijkstra.h:37-44: min-heap on distance only
     std::vector<LevelItem> lv;
     std::vector<int> tmp;
@@ -606,36 +605,33 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
     }
     if (!fast_done) search_exact(P, src, ws, tree_edges);
     VertexState *vs = ws.vs.data();
-    // dijkstra::compute_non_tree_edges (include/Dijkstra.h:129-149): its scan over the
-    // slots in ascending order keeps, of every pair that holds no tree slot, the slot
-    // met first, i.e. the lower one; the same list from one pass over the pairs in
-    // order of their lower slot.
-    for (u32 o : tree_edges) ws.pair_tree[P.slot_pair[o]] = 1;
-    ws.nte.clear();
-    for (size_t k = 0; k < P.pair_first.size(); k++)
-        if (!ws.pair_tree[k]) ws.nte.push_back(P.pair_first[k]);
     // dijkstra::is_edge_cycle: accepted iff the two root paths meet only at the root
     // and contain no FVS vertex with a smaller id than the root.  Computed here per
-    // vertex: the root child a vertex hangs under, and whether its root path holds
-    // such an FVS vertex (vertices are visited in pop order: parents first).
+    // vertex (vertices in settle order: parents first): the root child a vertex hangs
+    // under, or kBlocked if its root path holds such an FVS vertex; -1 for the root
+    // (which is never blocked: its id is not smaller than its own).
+    constexpr int kBlocked = -2;
     std::vector<int> &branch = ws.tmp;
     branch.assign(n, -1);
-    std::vector<char> blocked(n, 0);
     for (u32 x : ws.pop_order) {
-        bool self_bad = P.fvs_array[x] >= 0 && src > x;
-        if (x == src) {
-            branch[x] = -1;
-            blocked[x] = self_bad;
-        } else {
-            int p = vs[x].par;
-            branch[x] = ((u32)p == src) ? (int)x : branch[p];
-            blocked[x] = blocked[p] || self_bad;
-        }
+        if (x == src) continue;
+        const int p = vs[x].par;
+        const int bp = ((u32)p == src) ? (int)x : branch[p];
+        branch[x] = (bp == kBlocked || (P.fvs_array[x] >= 0 && src > x)) ? kBlocked : bp;
     }
-    for (u32 off : ws.nte) {
-        u32 a = g.rows[off], b = g.cols[off];
-        if (blocked[a] || blocked[b]) continue;
-        bool lca_root = (a == src) || (b == src) || (branch[a] != branch[b]);
+    // dijkstra::compute_non_tree_edges (include/Dijkstra.h:129-149): its scan over the
+    // slots in ascending order keeps, of every pair that holds no tree slot, the slot
+    // met first, i.e. the lower one; the same sequence is the pairs without a tree
+    // slot in order of their lower slot.
+    for (u32 o : tree_edges) ws.pair_tree[P.slot_pair[o]] = 1;
+    const size_t npairs = P.pair_first.size();
+    for (size_t k = 0; k < npairs; k++) {
+        if (ws.pair_tree[k]) continue;
+        const u32 off = P.pair_first[k];
+        const u32 a = g.rows[off], b = g.cols[off];
+        const int ba = branch[a], bb = branch[b];
+        if (ba == kBlocked || bb == kBlocked) continue;
+        const bool lca_root = (a == src) || (b == src) || (ba != bb);
         if (!lca_root) continue;
         int weight = vs[a].dist + vs[b].dist + g.w[off];
         LocalCandidate lc;
