@@ -255,12 +255,13 @@ def batch_cpu_baseline(graphs, costs, threads, budget_s, want=None):
 def run_reference_batch(args, world, rank, pg):
     import numpy as np
 
-    from minimumcyclebasis_gb300 import Problem, batch_graphs
+    from minimumcyclebasis_gb300 import Problem, batch_graphs, prepare_many
     threads = args.cpu_threads or os.cpu_count() or 1
     graphs = batch_graphs(args.batch_count, seed=args.seed)
     costs, Ns = {}, []
-    for j, g in enumerate(graphs):
-        info = Problem.from_graph(g).prepare(threads=threads).info
+    ps = prepare_many([Problem.from_graph(g) for g in graphs], threads=threads, cycle_lists=False)
+    for j in range(len(graphs)):
+        info, ps[j] = ps[j].info, None
         if not info.single_cycle and info.num_coords > 0:
             costs[j] = label_cost(info)
             Ns.append(info.num_coords)
@@ -454,7 +455,8 @@ def run_batch(args, world, rank, local, pg):
     import numpy as np
     import torch
 
-    from minimumcyclebasis_gb300 import BatchSolver, Problem, Solver, batch_graphs, bcc_split, block_tree_graph
+    from minimumcyclebasis_gb300 import (BatchSolver, Problem, Solver, batch_graphs, bcc_split, block_tree_graph,
+                                         prepare_many)
     from minimumcyclebasis_gb300.build import build_all
 
     build_all()
@@ -463,8 +465,9 @@ def run_batch(args, world, rank, local, pg):
 
     def problems(graphs):
         items, host_total, nsc, costs = [], 0, 0, {}
+        ps = prepare_many([Problem.from_graph(g) for g in graphs])  # in parallel, one thread per graph
         for j, g in enumerate(graphs):
-            p = Problem.from_graph(g).prepare(threads=0)
+            p, ps[j] = ps[j], None  # each problem's host copy is freed once its arrays are taken
             if p.info.single_cycle:  # the graph is one cycle: its basis needs no search
                 host_total += int(g.w.astype(np.int64).sum())
                 nsc += 1

@@ -76,6 +76,13 @@ int mcbh_problem_from_mtx(const char *path, mcbh_problem **out);
 int mcbh_problem_from_edges(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
                             const int32_t *w, mcbh_problem **out);
 int mcbh_prepare(mcbh_problem *p, const mcbh_options *opt);
+/* mcbh_prepare on `count` independent problems (the components of a biconnected
+ * split, the graphs of a batch), in parallel over problems with one thread each,
+ * largest first; opt->threads is the number of problems prepared at once (<=0:
+ * all cores).  Every problem's result is the one mcbh_prepare gives it.  status[i]
+ * (optional) receives each problem's return code; the return value is the code of
+ * the first problem, in index order, that failed (MCBH_OK if none). */
+int mcbh_prepare_many(mcbh_problem **ps, int64_t count, const mcbh_options *opt, int32_t *status);
 /* The edges of a Matrix-Market file as mcbh_problem_from_mtx reads them (0-based,
  * file order).  Returns the edge count and sets *nodes; with u != NULL also fills
  * u, v, w (cap entries available). */

@@ -131,14 +131,17 @@ void init_gpu_once() {
     }
 }
 
-// Host preparation: reduced graph, FVS, trees, the rank-ordered candidates and
-// their coordinate lists; the stats row's host columns.
-void prepare_job(Job &j, const Outputs &o) {
+mcbh_options job_options(const Outputs &o) {
     mcbh_options opt{};
     opt.threads = o.threads > 0 ? o.threads : 1;
     opt.contract_chains = 1;
     opt.cycle_lists = 1;
-    check_host(mcbh_prepare(j.p, &opt), "preprocessing failed");
+    return opt;
+}
+
+// A prepared problem's rank-ordered candidates and their coordinate lists; the
+// stats row's host columns.
+void collect_job(Job &j) {
     check_host(mcbh_get_info(j.p, &j.info), "mcbh_get_info");
     const mcbh_info &info = j.info;
     Stats &st = j.st;
@@ -169,6 +172,13 @@ void prepare_job(Job &j, const Outputs &o) {
     j.off.resize(K + 1);
     j.coords.resize(info.cycle_nnz > 0 ? info.cycle_nnz : 1);
     check_host(mcbh_get_cycle_lists(j.p, j.off.data(), j.coords.data()), "mcbh_get_cycle_lists");
+}
+
+// Host preparation of one problem: reduced graph, FVS, trees, candidates.
+void prepare_job(Job &j, const Outputs &o) {
+    const mcbh_options opt = job_options(o);
+    check_host(mcbh_prepare(j.p, &opt), "preprocessing failed");
+    collect_job(j);
 }
 
 bool needs_gpu(const Job &j) { return !j.info.single_cycle && j.info.num_coords > 0; }
@@ -365,7 +375,14 @@ int main(int argc, char **argv) {
             check_host(mcbh_problem_from_edges((int32_t)ids.size(), (int64_t)cu.size(), cu.data(), cv.data(),
                                                cw.data(), &j.p),
                        "component");
-            prepare_job(j, o);
+        }
+        // the components are independent: prepared in parallel, one thread each
+        {
+            std::vector<mcbh_problem *> hs;
+            for (Job &j : jobs) hs.push_back(j.p);
+            const mcbh_options opt = job_options(o);
+            check_host(mcbh_prepare_many(hs.data(), (int64_t)hs.size(), &opt, nullptr), "preprocessing failed");
+            for (Job &j : jobs) collect_job(j);
         }
         // every component that fits the batch in one batched launch per size class
         // (the per-iteration form with --plain), the rest on the single-problem solver

@@ -1019,6 +1019,30 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
     return MCBH_OK;
 }
 
+int mcbh_prepare_many(mcbh_problem **ps, int64_t count, const mcbh_options *opt, int32_t *status) {
+    if (count < 0 || (count > 0 && (!ps || !opt))) return MCBH_E_ARG;
+    mcbh_options one = *opt;
+    one.threads = 1;
+    const int threads = opt->threads > 0 ? opt->threads : omp_get_max_threads();
+    // the largest problems first, so that the last ones to finish are small
+    std::vector<int64_t> order((size_t)count);
+    for (int64_t i = 0; i < count; i++) order[(size_t)i] = i;
+    auto size_of = [&](int64_t i) { return ps[i] ? (int64_t)ps[i]->in.slots() : 0; };
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return size_of(a) > size_of(b); });
+    std::vector<int> st((size_t)count, MCBH_OK);
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+    for (int64_t k = 0; k < count; k++) {
+        const int64_t i = order[(size_t)k];
+        st[(size_t)i] = ps[i] ? mcbh_prepare(ps[i], &one) : MCBH_E_ARG;
+    }
+    int first = MCBH_OK;
+    for (int64_t i = 0; i < count; i++) {
+        if (status) status[i] = st[(size_t)i];
+        if (first == MCBH_OK) first = st[(size_t)i];
+    }
+    return first;
+}
+
 int mcbh_get_info(const mcbh_problem *p, mcbh_info *info) {
     if (!p || !info) return MCBH_E_ARG;
     *info = p->info;

@@ -162,6 +162,25 @@ def bcc_split(g: Graph, keep_bridges: bool = False) -> list[Graph]:
     return out
 
 
+def prepare_many(problems: list, threads: int = 0, contract_chains: bool = True, keep_trees: bool = False,
+                 ref_layout: bool = False, cycle_lists: bool = True) -> list:
+    """Problem.prepare on independent problems at once (mcbh_prepare_many): one thread
+    per problem, `threads` problems in parallel (0: all cores), largest first.  Each
+    problem gets the result Problem.prepare gives it.  Raises on the first failure in
+    list order, after the others are prepared."""
+    n = len(problems)
+    opt = MCBHOptions(threads, int(contract_chains), int(keep_trees), int(ref_layout), int(cycle_lists))
+    handles = (C.c_void_p * max(n, 1))(*[p._h for p in problems])
+    status = np.zeros(max(n, 1), np.int32)
+    rc = host_lib().mcbh_prepare_many(C.cast(handles, C.c_void_p), n, C.byref(opt), ptr(status))
+    for p, st in zip(problems, status[:n]):
+        if st == 0:
+            p.prepared = True
+            p._opts = opt
+    check_host(rc, "mcbh_prepare_many")
+    return problems
+
+
 class Problem:
     """A graph prepared for the de Pina main loop.
 

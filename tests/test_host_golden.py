@@ -116,3 +116,27 @@ def test_fast_and_exact_tree_searches_agree(family):
     for x, y in zip(exact.cycle_lists(), fast.cycle_lists()):
         assert np.array_equal(x, y)
     assert np.array_equal(exact.tree_parents(), fast.tree_parents())
+
+
+def test_prepare_many_equals_prepare_and_flags_failures():
+    from minimumcyclebasis_gb300 import batch_graphs, prepare_many
+    from minimumcyclebasis_gb300._native import MCBError
+    from minimumcyclebasis_gb300.host import Graph
+    graphs = batch_graphs(20, nmin=50, nmax=800, seed=31)
+    one = [Problem.from_graph(g).prepare(threads=2) for g in graphs]
+    many = prepare_many([Problem.from_graph(g) for g in graphs], threads=4)
+    for a, b in zip(one, many):
+        assert b.prepared and a.info.single_cycle == b.info.single_cycle
+        if a.info.single_cycle:
+            continue
+        for x, y in zip(a.candidates(), b.candidates()):
+            assert np.array_equal(x, y)
+        for x, y in zip(a.cycle_lists(), b.cycle_lists()):
+            assert np.array_equal(x, y)
+    # a triangle and a K4 with no edge between them: the spanning tree fails
+    bad = Graph(7, np.array([0, 1, 2, 3, 3, 3, 4, 4, 5], np.int32), np.array([1, 2, 0, 4, 5, 6, 5, 6, 6], np.int32),
+                np.ones(9, np.int32))
+    probs = [Problem.from_graph(graphs[0]), Problem.from_graph(bad), Problem.from_graph(graphs[1])]
+    with pytest.raises(MCBError):
+        prepare_many(probs, threads=2)
+    assert probs[0].prepared and not probs[1].prepared and probs[2].prepared
