@@ -497,7 +497,11 @@ struct TreeWorkspace {
 // dijkstra::dijkstra_sp (include/Dijkstra.h:78-124) as the reference runs it: the
 // binary heap decides which of two equally near vertices settles first.  (The level
 // of a vertex, set with its parent in the reference, is its final parent's level + 1:
-// computed after the search, in settle order, where needed.)
+// computed after the search, in settle order, where needed.)  kPositive: every
+// weight is at least 1 and no distance overflows, so a settled vertex, nearer than
+// the one being settled, never passes the distance test and the reference's
+// "settled" test before it can be left out without changing the push sequence.
+template <bool kPositive>
 void search_exact(const mcbh_problem &P, u32 src, TreeWorkspace &ws, std::vector<u32> &tree_edges) {
     const Graph &g = P.rg;
     VertexState *vs = ws.vs.data();
@@ -518,9 +522,9 @@ void search_exact(const mcbh_problem &P, u32 src, TreeWorkspace &ws, std::vector
         for (u32 o = g.ro[x]; o < g.ro[x + 1]; o++) {
             const mcbh_problem::Arc a = arcs[o];
             VertexState &sc = vs[a.col];
-            if (sc.done) continue;
+            if (!kPositive && sc.done) continue;
             const int nd = dx + a.w;
-            if (sc.dist == -1 || nd < sc.dist) {
+            if (kPositive ? (unsigned)nd < (unsigned)sc.dist : (sc.dist == -1 || nd < sc.dist)) {
                 sc.dist = nd;
                 ws.pq.push(std::make_pair((int)a.col, nd));
                 sc.par = x;
@@ -558,12 +562,13 @@ bool search_fast(const mcbh_problem &P, u32 src, TreeWorkspace &ws, std::vector<
         sx.done |= 1;
         ws.pop_order.push_back((u32)x);
         const int dx = sx.dist;
+        // with weights >= 1 a settled vertex is nearer than dx < nd, so the distance
+        // test alone skips it; unreached (-1) compares as the largest unsigned value
         for (u32 o = g.ro[x]; o < g.ro[x + 1]; o++) {
             const mcbh_problem::Arc a = arcs[o];
             VertexState &sc = vs[a.col];
-            if (sc.done & 1) continue;
             const int nd = dx + a.w;
-            if (sc.dist == -1 || nd < sc.dist) {
+            if ((unsigned)nd < (unsigned)sc.dist) {
                 sc.dist = nd;
                 ws.rq.push((unsigned)nd, (int)a.col);
                 sc.par = x;
@@ -581,29 +586,80 @@ bool search_fast(const mcbh_problem &P, u32 src, TreeWorkspace &ws, std::vector<
     return rivals == 0;
 }
 
+// Which search one root takes, and what it cost.
+struct SearchChoice {
+    bool try_fast = false;  // in: try search_fast first
+    int result = -1;        // out: 1 search_fast kept, 0 it fell back, -1 not tried
+    double fast_s = 0, exact_s = 0;
+};
+
+// Chooses, root by root, between search_fast (with its fallback) and search_exact
+// from their measured costs: search_fast is tried while its mean cost per root, the
+// fallbacks' heap searches included, is below the heap search's mean, and on every
+// 32nd root regardless, so that the estimate follows the roots.  How often a root's
+// search falls back depends on the graph (1% of the roots at weights U[1,1000], a
+// quarter at U[1,255], nearly all with small integer weights) and on the root, and
+// what search_fast saves depends on the graph too.  Which roots take which search
+// changes no output, only the time.
+struct SearchPolicy {
+    std::atomic<long long> ok_n{0}, fail_n{0}, exact_n{0}, ok_ns{0}, fail_ns{0}, exact_ns{0};
+
+    bool want_fast(int t) const {
+        const auto rl = std::memory_order_relaxed;
+        const long long okn = ok_n.load(rl), failn = fail_n.load(rl), exn = exact_n.load(rl);
+        const long long tries = okn + failn;
+        if (tries < 32 || t % 32 == 0 || exn == 0) return true;
+        const double exact_mean = (double)exact_ns.load(rl) / (double)exn;
+        const double fast_mean =
+            ((double)ok_ns.load(rl) + (double)fail_ns.load(rl) + exact_mean * (double)failn) / (double)tries;
+        return fast_mean < exact_mean;
+    }
+    void record(const SearchChoice &c) {
+        const auto rl = std::memory_order_relaxed;
+        const long long f = (long long)(c.fast_s * 1e9), e = (long long)(c.exact_s * 1e9);
+        if (c.result == 1) {
+            ok_n.fetch_add(1, rl);
+            ok_ns.fetch_add(f, rl);
+            return;
+        }
+        if (c.result == 0) {
+            fail_n.fetch_add(1, rl);
+            fail_ns.fetch_add(f, rl);
+        }
+        exact_n.fetch_add(1, rl);
+        exact_ns.fetch_add(e, rl);
+    }
+};
+
 void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput &out, bool want_lists,
                   int *tree_parent, u32 *lay_rows, u32 *lay_cols, int *lay_edge, u32 *lay_nodes,
-                  int *fast_result) {
+                  SearchChoice &choice) {
     const Graph &g = P.rg;
     const int n = g.n;
     const u32 src = P.fvs_vertices[tidx];
     ws.init(n, P.pair_first.size());
     std::vector<u32> tree_edges;
     tree_edges.reserve(n);
-    // fast_result: in, whether to try search_fast; out, 1 if it was kept, 0 if it
-    // was tried and fell back to search_exact, -1 if not tried
     bool fast_done = false;
-    if (*fast_result && !lay_rows) {
+    choice.result = -1;
+    if (choice.try_fast && P.fast_search_ok && !lay_rows) {
+        const double t0 = now_s();
         fast_done = search_fast(P, src, ws, tree_edges);
-        *fast_result = fast_done ? 1 : 0;
+        choice.fast_s = now_s() - t0;
+        choice.result = fast_done ? 1 : 0;
         if (!fast_done) {
             ws.init(n, P.pair_first.size());
             tree_edges.clear();
         }
-    } else {
-        *fast_result = -1;
     }
-    if (!fast_done) search_exact(P, src, ws, tree_edges);
+    if (!fast_done) {
+        const double t0 = now_s();
+        if (P.fast_search_ok)
+            search_exact<true>(P, src, ws, tree_edges);
+        else
+            search_exact<false>(P, src, ws, tree_edges);
+        choice.exact_s = now_s() - t0;
+    }
     VertexState *vs = ws.vs.data();
     // dijkstra::is_edge_cycle: accepted iff the two root paths meet only at the root
     // and contain no FVS vertex with a smaller id than the root.  Computed here per
@@ -918,26 +974,20 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
         std::vector<RootOutput> outs(F);
         int threads = opt->threads > 0 ? opt->threads : omp_get_max_threads();
         bool lists = opt->cycle_lists != 0;
-        // The radix-queue search is tried while at most a quarter of the roots tried
-        // so far had to fall back (graphs with many equal path lengths, e.g. small
-        // integer weights, fall back on most roots).  Which roots take which search
-        // changes no output.
-        std::atomic<int> fast_tries{0}, fast_fallbacks{0};
+        SearchPolicy policy;
 #pragma omp parallel num_threads(threads)
         {
             TreeWorkspace ws;
 #pragma omp for schedule(dynamic, 1)
             for (int t = 0; t < F; t++) {
-                const int tries = fast_tries.load(std::memory_order_relaxed);
-                int fast = P->fast_search_ok &&
-                           (tries < 64 || 4 * fast_fallbacks.load(std::memory_order_relaxed) <= tries);
+                SearchChoice choice;
+                choice.try_fast = policy.want_fast(t);
                 process_root(*P, t, ws, outs[t], lists, opt->keep_trees ? P->tree_parent.data() : nullptr,
                              opt->ref_layout ? P->lay_rows.data() : nullptr,
                              opt->ref_layout ? P->lay_cols.data() : nullptr,
                              opt->ref_layout ? P->lay_edge.data() : nullptr,
-                             opt->ref_layout ? P->lay_nodes.data() : nullptr, &fast);
-                if (fast >= 0) fast_tries.fetch_add(1, std::memory_order_relaxed);
-                if (fast == 0) fast_fallbacks.fetch_add(1, std::memory_order_relaxed);
+                             opt->ref_layout ? P->lay_nodes.data() : nullptr, choice);
+                policy.record(choice);
             }
         }
         I.t_trees = now_s() - t0;
