@@ -1,0 +1,48 @@
+"""Host preparation against the reference's own host library on fresh graphs:
+oracle/_ref/ref_dump (built by oracle/Makefile from the reference's sources, where
+they are present) prints the reference's rank-ordered candidate list, which must
+equal ours entry for entry (root, edge offset, weight).  The families cover both
+tree searches (the radix-queue search with its fallback, and the heap search for
+weights of 0), dense ties (small integer weights), chains and parallel edges.
+Skipped where the reference harness is not built."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from minimumcyclebasis_gb300 import Problem, batch_graphs, grid_graph, planar_chain_graph, random_graph, rgg_graph
+
+REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+
+FAMILIES = {
+    "random_w1000": lambda: random_graph(3000, 6000, 1, 1000, 41),
+    "random_w20": lambda: random_graph(3000, 6000, 1, 20, 42),
+    "random_w0to3": lambda: random_graph(3000, 6000, 0, 3, 43),
+    "random_w0to1_dense": lambda: random_graph(1500, 6000, 0, 1, 44),
+    "planar_chains": lambda: planar_chain_graph(2500, 30, 30, 8, 1, 1000, 45),
+    "planar_chains_w5": lambda: planar_chain_graph(2500, 30, 30, 8, 1, 5, 46),
+    "rgg": lambda: rgg_graph(2500, 4, 47),
+    "grid_w3": lambda: grid_graph(40, 40, 1, 3, 48),
+    "batch_w255": lambda: max(batch_graphs(16, nmin=800, nmax=3000, seed=49), key=lambda x: x.nodes),
+}
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DUMP), reason="reference harness (oracle/_ref) not built here")
+@pytest.mark.parametrize("family", sorted(FAMILIES))
+def test_candidates_equal_the_reference_host_library(tmp_path, family):
+    g = FAMILIES[family]()
+    mtx = str(tmp_path / "g.mtx")
+    g.write_mtx(mtx)
+    r = subprocess.run([REF_DUMP, mtx, "4", "0", "noE"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ref = np.array([[int(x) for x in ln.split()[1:]] for ln in r.stdout.splitlines() if ln.startswith("C ")],
+                   dtype=np.int64).reshape(-1, 4)
+    p = Problem.from_mtx(mtx).prepare(threads=4)
+    root, edge, w, _ = p.candidates()
+    assert p.F > 64  # enough roots for both tree searches to be chosen
+    assert np.array_equal(ref[:, 0], np.arange(len(ref)))
+    assert np.array_equal(ref[:, 1], root)
+    assert np.array_equal(ref[:, 2], edge)
+    assert np.array_equal(ref[:, 3], w)
