@@ -22,6 +22,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
+#include <memory_resource>
 #include <new>
 #include <string>
 #include <unordered_map>
@@ -465,8 +467,11 @@ struct RootOutput {
     // (include/cycle_searcher.h:23-61); only its iteration order is used, and that
     // order depends on the keys and their sequence, not on the mapped values.  Each
     // key maps to the first and last of its candidates, chained in insertion order
-    // through `next` (no allocation per key).
-    std::unordered_map<unsigned long long, std::pair<int, int>> groups;
+    // through `next`.  Its nodes and buckets come from an arena of the root's own
+    // (the allocator takes no part in the bucket layout, so not in the order).
+    std::unique_ptr<std::pmr::monotonic_buffer_resource> arena =
+        std::make_unique<std::pmr::monotonic_buffer_resource>();
+    std::pmr::unordered_map<unsigned long long, std::pair<int, int>> groups{arena.get()};
     std::vector<int> next;
 };
 
