@@ -83,6 +83,12 @@ int mcbh_prepare(mcbh_problem *p, const mcbh_options *opt);
  * (optional) receives each problem's return code; the return value is the code of
  * the first problem, in index order, that failed (MCBH_OK if none). */
 int mcbh_prepare_many(mcbh_problem **ps, int64_t count, const mcbh_options *opt, int32_t *status);
+/* Re-verification of a basis: the GF(2) rank of the cycle vectors of the candidates
+ * at `ranks` (rank-ordered candidate indices, e.g. a solver's selected ranks), by
+ * Gaussian elimination over their N-bit coordinate vectors (count x N bits held on
+ * the host; O(count x N^2 / 64) word operations, OpenMP over rows).  A basis is
+ * independent iff *rank_out == count == N.  Needs the cycle lists (cycle_lists = 1). */
+int mcbh_gf2_rank(const mcbh_problem *p, const int64_t *ranks, int64_t count, int threads, int64_t *rank_out);
 /* The edges of a Matrix-Market file as mcbh_problem_from_mtx reads them (0-based,
  * file order).  Returns the edge count and sets *nodes; with u != NULL also fills
  * u, v, w (cap entries available). */

@@ -41,6 +41,7 @@ HOST_SYMBOLS = {
     "mcbh_problem_from_edges": (C.c_int, [i32, i64, vp, vp, vp, C.POINTER(vp)]),
     "mcbh_prepare": (C.c_int, [vp, C.POINTER(MCBHOptions)]),
     "mcbh_prepare_many": (C.c_int, [vp, i64, C.POINTER(MCBHOptions), vp]),
+    "mcbh_gf2_rank": (C.c_int, [vp, vp, i64, C.c_int, C.POINTER(i64)]),
     "mcbh_problem_free": (None, [vp]),
     "mcbh_get_info": (C.c_int, [vp, C.POINTER(MCBHInfo)]),
     "mcbh_get_reduced_graph": (C.c_int, [vp, vp, vp, vp, vp, vp]),

@@ -24,6 +24,9 @@
 //                        per-component loop (bicc/, main.sh:19-32) processes a graph;
 //                        the components go through one batched solve (mcbgpu_batch);
 //                        the cycle listings give each component's basis in turn
+//   --verify             re-verify every basis by Gaussian elimination over GF(2)
+//                        (mcbh_gf2_rank): the N selected cycles must have rank N;
+//                        "GF(2) rank R of N" on stderr per problem, an error if R < N
 //
 // Exit status 0 on success; on any error a message on stderr and status 1 (the
 // reference prints and exits on every error too).
@@ -107,6 +110,7 @@ struct Outputs {
     const char *stats = nullptr;
     FILE *cycles = nullptr, *cycles_input = nullptr;
     bool plain = false;
+    bool verify = false;
     int threads = 1;
 };
 
@@ -263,6 +267,15 @@ void solve_batched(std::vector<Job *> &jobs) {
 
 // Appends the problem's stats row and its cycle blocks.
 void emit_job(Job &j, const Outputs &o) {
+    if (o.verify && !j.info.single_cycle && j.info.num_coords > 0) {
+        int64_t rank = 0;
+        check_host(mcbh_gf2_rank(j.p, j.sel.data(), (int64_t)j.sel.size(), o.threads, &rank), "GF(2) verification");
+        std::fprintf(stderr, "GF(2) rank %lld of %d\n", (long long)rank, j.info.num_coords);
+        if (rank != j.info.num_coords) {
+            std::fprintf(stderr, "mcb_gb300: the basis is not independent\n");
+            std::exit(1);
+        }
+    }
     Stats &st = j.st;
     if (!j.info.single_cycle) {
         const int64_t K = j.info.num_candidates;
@@ -294,7 +307,7 @@ void emit_job(Job &j, const Outputs &o) {
 int main(int argc, char **argv) {
     std::vector<const char *> pos;
     const char *cycles_path = nullptr, *cycles_input_path = nullptr;
-    bool plain = false, bcc = false;
+    bool plain = false, bcc = false, verify = false;
     for (int i = 1; i < argc; i++) {
         if (!std::strcmp(argv[i], "--cycles") && i + 1 < argc)
             cycles_path = argv[++i];
@@ -304,6 +317,8 @@ int main(int argc, char **argv) {
             plain = true;
         else if (!std::strcmp(argv[i], "--bcc"))
             bcc = true;
+        else if (!std::strcmp(argv[i], "--verify"))
+            verify = true;
         else
             pos.push_back(argv[i]);
     }
@@ -312,7 +327,7 @@ int main(int argc, char **argv) {
         std::printf("2nd Argument should indicate the OutputFile\n");
         std::printf("3th argument should indicate the number of threads.(Optional) (1 default)\n");
         std::printf("4th Argument is chunk_size.(Optional) (720 default)\n");
-        std::printf("options: --cycles FILE, --cycles-input FILE, --plain, --bcc\n");
+        std::printf("options: --cycles FILE, --cycles-input FILE, --plain, --bcc, --verify\n");
         return 1;
     }
     const char *input = pos[0];
@@ -320,6 +335,7 @@ int main(int argc, char **argv) {
     o.stats = pos[1];
     o.threads = std::atoi(pos[2]);
     o.plain = plain;
+    o.verify = verify;
     if (cycles_path && !(o.cycles = std::fopen(cycles_path, "w"))) fail("cannot open the cycle file", cycles_path);
     if (cycles_input_path && !(o.cycles_input = std::fopen(cycles_input_path, "w")))
         fail("cannot open the cycle file", cycles_input_path);

@@ -35,6 +35,7 @@
 namespace {
 
 using u32 = uint32_t;
+using u64 = uint64_t;
 using i64 = int64_t;
 
 double now_s() {
@@ -1096,6 +1097,60 @@ int mcbh_prepare_many(mcbh_problem **ps, int64_t count, const mcbh_options *opt,
         if (first == MCBH_OK) first = st[(size_t)i];
     }
     return first;
+}
+
+int mcbh_gf2_rank(const mcbh_problem *p, const int64_t *ranks, int64_t count, int threads, int64_t *rank_out) {
+    if (!p || !rank_out || count < 0 || (count > 0 && !ranks)) return MCBH_E_ARG;
+    if (!p->prepared || p->single_cycle || p->c_off.empty()) return MCBH_E_STATE;
+    const int64_t K = (int64_t)p->c_weight.size();
+    const int64_t N = (int64_t)p->coord_edges.size();
+    for (int64_t i = 0; i < count; i++)
+        if (ranks[i] < 0 || ranks[i] >= K) return MCBH_E_ARG;
+    if (threads <= 0) threads = omp_get_max_threads();
+    const int64_t W = (N + 63) / 64;
+    try {
+        // one bit row per selected cycle: its coordinates (the cycle vector of
+        // include/cycles.h:144-195 over the N coordinates)
+        std::vector<u64> M((size_t)(count * W), 0);
+#pragma omp parallel for num_threads(threads) schedule(static)
+        for (int64_t i = 0; i < count; i++) {
+            u64 *row = &M[(size_t)(i * W)];
+            for (int64_t k = p->c_off[ranks[i]]; k < p->c_off[ranks[i] + 1]; k++) {
+                const int c = p->c_coords[(size_t)k];
+                row[c >> 6] ^= 1ull << (c & 63);
+            }
+        }
+        // Gaussian elimination over GF(2), column by column: the first remaining row
+        // with the column's bit becomes the pivot and is XORed into every later row
+        // that has the bit (only the words from the column's word on change)
+        int64_t rank = 0;
+        for (int64_t col = 0; col < N && rank < count; col++) {
+            const int64_t w = col >> 6;
+            const u64 bit = 1ull << (col & 63);
+            int64_t piv = -1;
+            for (int64_t r = rank; r < count; r++)
+                if (M[(size_t)(r * W + w)] & bit) {
+                    piv = r;
+                    break;
+                }
+            if (piv < 0) continue;
+            if (piv != rank)
+                std::swap_ranges(M.begin() + (size_t)(piv * W + w), M.begin() + (size_t)((piv + 1) * W),
+                                 M.begin() + (size_t)(rank * W + w));
+            const u64 *prow = &M[(size_t)(rank * W)];
+#pragma omp parallel for num_threads(threads) schedule(static) if ((count - rank) * (W - w) > 65536)
+            for (int64_t r = rank + 1; r < count; r++) {
+                u64 *row = &M[(size_t)(r * W)];
+                if (row[w] & bit)
+                    for (int64_t x = w; x < W; x++) row[x] ^= prow[x];
+            }
+            rank++;
+        }
+        *rank_out = rank;
+    } catch (const std::bad_alloc &) {
+        return MCBH_E_NOMEM;
+    }
+    return MCBH_OK;
 }
 
 int mcbh_get_info(const mcbh_problem *p, mcbh_info *info) {

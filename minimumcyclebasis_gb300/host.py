@@ -223,6 +223,14 @@ class Problem:
         self._opts = opt
         return self
 
+    def gf2_rank(self, ranks, threads: int = 0) -> int:
+        """GF(2) rank of the cycle vectors of the candidates at `ranks` (mcbh_gf2_rank):
+        a basis re-verified by elimination has rank == len(ranks) == N."""
+        r = np.ascontiguousarray(ranks, np.int64)
+        out = C.c_int64()
+        check_host(host_lib().mcbh_gf2_rank(self._h, ptr(r), len(r), threads, C.byref(out)), "mcbh_gf2_rank")
+        return int(out.value)
+
     @property
     def info(self) -> MCBHInfo:
         i = MCBHInfo()

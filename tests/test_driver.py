@@ -106,11 +106,25 @@ def test_bcc_mode_rings_and_bridge_without_gpu(tmp_path):
     mtx.write_text("%%MatrixMarket matrix coordinate integer symmetric\n6 6 7\n" +
                    "".join("%d %d %d\n" % e for e in edges))
     out, cyc = tmp_path / "stats.csv", tmp_path / "c.txt"
-    r = run(mtx, out, 1, "--bcc", "--cycles", cyc)
+    r = run(mtx, out, 1, "--bcc", "--cycles", cyc, "--verify")  # rings: nothing to eliminate
     assert r.returncode == 0, r.stderr
     rows = read_rows(out)
     assert [int(x["Total_Weight"]) for x in rows] == [12, 9]
     assert cyc.read_text().splitlines()[-1] == "Total Weight = 21"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["grid32x32_s1", "rand2000_w20_s11"])
+@pytest.mark.parametrize("bcc", [False, True])
+def test_driver_verify_reports_full_rank(tmp_path, name, bcc):
+    # --verify: every basis re-verified by GF(2) elimination, rank N of N
+    fx = load_golden(name)
+    r = run(fx["mtx"], tmp_path / "stats.csv", 4, "--verify", *(["--bcc"] if bcc else []))
+    assert r.returncode == 0, r.stderr
+    ranks = [ln.split() for ln in r.stderr.splitlines() if ln.startswith("GF(2) rank ")]
+    assert ranks and all(x[2] == x[4] for x in ranks)
+    if not bcc:
+        assert ranks == [["GF(2)", "rank", str(fx["G"]["num_coords"]), "of", str(fx["G"]["num_coords"])]]
 
 
 @pytest.mark.gpu

@@ -140,3 +140,36 @@ def test_prepare_many_equals_prepare_and_flags_failures():
     with pytest.raises(MCBError):
         prepare_many(probs, threads=2)
     assert probs[0].prepared and not probs[1].prepared and probs[2].prepared
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_reference_basis_is_gf2_independent(name):
+    # re-verification by elimination: the reference's N selected cycles have rank N;
+    # a basis with one cycle listed twice has rank N - 1
+    fx = load_golden(name)
+    p = Problem.from_mtx(fx["mtx"]).prepare(threads=2)
+    if p.info.single_cycle:
+        pytest.skip("one cycle: nothing to eliminate")
+    sel = np.array(fx["selected_ranks"], np.int64)
+    assert len(sel) == p.N and p.gf2_rank(sel, threads=2) == p.N
+    if p.N > 1:
+        dup = sel.copy()
+        dup[-1] = dup[0]
+        assert p.gf2_rank(dup, threads=2) == p.N - 1
+
+
+def test_gf2_rank_of_oracle_bases_and_bad_arguments():
+    import oracle
+    from minimumcyclebasis_gb300 import random_graph
+    from minimumcyclebasis_gb300._native import MCBError
+    for seed in (61, 62, 63):
+        p = Problem.from_graph(random_graph(400, 900, 1, 30, seed)).prepare(threads=2, keep_trees=True)
+        sel, _, _ = oracle.solve(p, threads=2)
+        assert p.gf2_rank(sel) == p.N
+        # the first N candidates in rank order are not in general a basis
+        assert p.gf2_rank(np.arange(p.N)) <= p.N
+    with pytest.raises(MCBError):
+        p.gf2_rank([p.info.num_candidates])  # past the last candidate
+    q = Problem.from_graph(random_graph(50, 80, 1, 9, 64))
+    with pytest.raises(MCBError):
+        q.gf2_rank([0])  # not prepared
