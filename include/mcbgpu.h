@@ -246,6 +246,25 @@ int mcbgpu_batch_solve(int32_t count, const int32_t *num_coords, const int64_t *
                        const int32_t *weight, const int64_t *offsets, const int32_t *coords, int64_t *selected,
                        int64_t *total_weight);
 
+/* ---- 5. shortest-path trees of many roots (the host's per-root tree searches,
+ * include/Dijkstra.h:78-124, on the device) -------------------------------------
+ * The graph is the reduced multigraph's CSR: row offsets (nodes + 1), and per slot
+ * its column, weight and reverse slot; every weight at least 1 and every distance
+ * below 2^31 (MCBGPU_E_ARG otherwise).  mcbgpu_trees_run computes, for `count` <=
+ * max_roots roots, every vertex's distance (count x nodes) and parent slot (the slot
+ * of the parent's row that enters the vertex, -1 at the root), and per root a tie
+ * flag: where it is 0 the parents equal those of the reference's heap search; where
+ * it is 1 some vertex has two equally near shortest-path parents, which only the
+ * heap's order decides, and the caller must search that root itself.
+ * Synchronises `stream`. */
+typedef struct mcbgpu_trees mcbgpu_trees;
+int mcbgpu_trees_create(mcbgpu_trees **out, int32_t nodes, int64_t slots, const uint32_t *row_offsets,
+                        const uint32_t *cols, const int32_t *weights, const uint32_t *rev, int32_t max_roots);
+int mcbgpu_trees_run(mcbgpu_trees *t, const uint32_t *roots, int32_t count, int32_t *dist, int32_t *parent_slot,
+                     uint8_t *tied, void *stream);
+int64_t mcbgpu_trees_device_bytes(const mcbgpu_trees *t);
+int mcbgpu_trees_destroy(mcbgpu_trees *t);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,7 +40,8 @@ enum {
     MCBH_E_FORMAT = -3,    /* unsupported Matrix-Market banner */
     MCBH_E_GRAPH = -4,     /* graph the reference cannot process (e.g. disconnected) */
     MCBH_E_STATE = -5,     /* call out of order (e.g. accessor before prepare) */
-    MCBH_E_NOMEM = -6      /* allocation failed */
+    MCBH_E_NOMEM = -6,     /* allocation failed */
+    MCBH_E_SUPPLIER = -7   /* a tree supplier's callback returned an error */
 };
 
 typedef struct mcbh_problem mcbh_problem;
@@ -68,6 +69,7 @@ typedef struct mcbh_info {
     int64_t cycle_nnz;       /* total length of the per-candidate coordinate lists */
     int64_t total_weight_input; /* sum of input edge weights (64-bit) */
     double t_read, t_reduce, t_fvs, t_spanning, t_trees, t_collect; /* seconds */
+    int32_t trees_supplied;  /* roots whose tree came from mcbh_prepare_with_trees's supplier */
 } mcbh_info;
 
 /* ---- construction ---------------------------------------------------------- */
@@ -76,6 +78,30 @@ int mcbh_problem_from_mtx(const char *path, mcbh_problem **out);
 int mcbh_problem_from_edges(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
                             const int32_t *w, mcbh_problem **out);
 int mcbh_prepare(mcbh_problem *p, const mcbh_options *opt);
+/* A supplier of per-root shortest-path trees for mcbh_prepare_with_trees (e.g. the
+ * GPU's, mcbgpu_trees_*).  begin (optional) receives the reduced graph once, before
+ * the first trees call: `nodes`, the slot count, row offsets (nodes + 1), and per slot
+ * its column, weight and reverse slot.  trees fills, for the `count` roots at `roots`,
+ * every vertex's distance (count x nodes), its parent slot (the slot of the parent's
+ * row that enters it; -1 at the root) and a per-root flag, nonzero where the supplier
+ * leaves the root to the host.  Both return 0 on success. */
+typedef struct mcbh_tree_source {
+    void *ctx;
+    int (*begin)(void *ctx, int32_t nodes, int64_t slots, const uint32_t *row_offsets, const uint32_t *cols,
+                 const int32_t *weights, const uint32_t *rev);
+    int (*trees)(void *ctx, const uint32_t *roots, int32_t count, int32_t *dist, int32_t *parent_slot,
+                 uint8_t *skip);
+    int32_t chunk; /* roots per trees call (<= 0: all at once) */
+} mcbh_tree_source;
+/* mcbh_prepare with the per-root tree searches taken from `source` where it offers a
+ * tree.  Each tree is checked before use (a shortest-path tree whose every parent is
+ * the one the reference's heap search keeps, i.e. no two equally near shortest-path
+ * parents); a root whose tree fails a check, or that the supplier skips, is searched
+ * on the host.  The result is identical to mcbh_prepare's.  Without effect (all roots
+ * searched on the host) when some weight is below 1 or opt->ref_layout is set (the
+ * layout follows the heap's settle order).  info.trees_supplied counts the adopted
+ * trees. */
+int mcbh_prepare_with_trees(mcbh_problem *p, const mcbh_options *opt, const mcbh_tree_source *source);
 /* mcbh_prepare on `count` independent problems (the components of a biconnected
  * split, the graphs of a batch), in parallel over problems with one thread each,
  * largest first; opt->threads is the number of problems prepared at once (<=0:

@@ -28,12 +28,21 @@ class MCBHOptions(C.Structure):
                 ("ref_layout", C.c_int), ("cycle_lists", C.c_int)]
 
 
+TREE_BEGIN = C.CFUNCTYPE(C.c_int, vp, i32, i64, vp, vp, vp, vp)
+TREE_TREES = C.CFUNCTYPE(C.c_int, vp, vp, i32, vp, vp, vp)
+
+
+class MCBHTreeSource(C.Structure):
+    _fields_ = [("ctx", vp), ("begin", TREE_BEGIN), ("trees", TREE_TREES), ("chunk", i32)]
+
+
 class MCBHInfo(C.Structure):
     _fields_ = [("nodes", i32), ("edges2", i64), ("single_cycle", i32), ("nodes_removed", i32),
                 ("reduced_nodes", i32), ("reduced_edges2", i64), ("source_vertex", i32), ("fvs_size", i32),
                 ("num_coords", i32), ("num_candidates", i64), ("cycle_nnz", i64), ("total_weight_input", i64),
                 ("t_read", C.c_double), ("t_reduce", C.c_double), ("t_fvs", C.c_double),
-                ("t_spanning", C.c_double), ("t_trees", C.c_double), ("t_collect", C.c_double)]
+                ("t_spanning", C.c_double), ("t_trees", C.c_double), ("t_collect", C.c_double),
+                ("trees_supplied", i32)]
 
 
 HOST_SYMBOLS = {
@@ -42,6 +51,7 @@ HOST_SYMBOLS = {
     "mcbh_prepare": (C.c_int, [vp, C.POINTER(MCBHOptions)]),
     "mcbh_prepare_many": (C.c_int, [vp, i64, C.POINTER(MCBHOptions), vp]),
     "mcbh_gf2_rank": (C.c_int, [vp, vp, i64, C.c_int, C.POINTER(i64)]),
+    "mcbh_prepare_with_trees": (C.c_int, [vp, C.POINTER(MCBHOptions), vp]),
     "mcbh_problem_free": (None, [vp]),
     "mcbh_get_info": (C.c_int, [vp, C.POINTER(MCBHInfo)]),
     "mcbh_get_reduced_graph": (C.c_int, [vp, vp, vp, vp, vp, vp]),
@@ -108,6 +118,10 @@ GPU_SYMBOLS = {
     "mcbgpu_batch_launches": (i64, [vp]),
     "mcbgpu_batch_device_bytes": (i64, [vp]),
     "mcbgpu_batch_destroy": (C.c_int, [vp]),
+    "mcbgpu_trees_create": (C.c_int, [C.POINTER(vp), i32, i64, vp, vp, vp, vp, i32]),
+    "mcbgpu_trees_run": (C.c_int, [vp, vp, i32, vp, vp, vp, vp]),
+    "mcbgpu_trees_device_bytes": (i64, [vp]),
+    "mcbgpu_trees_destroy": (C.c_int, [vp]),
     "mcbgpu_batch_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
 }
 

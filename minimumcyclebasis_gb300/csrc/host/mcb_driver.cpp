@@ -24,6 +24,12 @@
 //                        per-component loop (bicc/, main.sh:19-32) processes a graph;
 //                        the components go through one batched solve (mcbgpu_batch);
 //                        the cycle listings give each component's basis in turn
+//   --gpu-trees          the per-root shortest-path trees computed on the GPU
+//                        (mcbgpu_trees_*, 2048 roots per launch) and handed to the host
+//                        preparation, which checks each one and searches any root whose
+//                        tree it does not accept itself (the result does not change);
+//                        single-graph mode (with --bcc the components are prepared on
+//                        the host in parallel)
 //   --verify             re-verify every basis by Gaussian elimination over GF(2)
 //                        (mcbh_gf2_rank): the N selected cycles must have rank N;
 //                        "GF(2) rank R of N" on stderr per problem, an error if R < N
@@ -111,7 +117,27 @@ struct Outputs {
     FILE *cycles = nullptr, *cycles_input = nullptr;
     bool plain = false;
     bool verify = false;
+    bool gpu_trees = false;
     int threads = 1;
+};
+
+// The GPU as the host preparation's tree supplier (mcbh_tree_source).
+struct GpuTreeSupplier {
+    mcbgpu_trees *t = nullptr;
+    int32_t chunk = 2048;
+    ~GpuTreeSupplier() { mcbgpu_trees_destroy(t); }
+    static int begin(void *ctx, int32_t nodes, int64_t slots, const uint32_t *ro, const uint32_t *cols,
+                     const int32_t *w, const uint32_t *rev) {
+        GpuTreeSupplier *g = static_cast<GpuTreeSupplier *>(ctx);
+        mcbgpu_trees_destroy(g->t);
+        g->t = nullptr;
+        return mcbgpu_trees_create(&g->t, nodes, slots, ro, cols, w, rev, g->chunk) == MCBGPU_OK ? 0 : 1;
+    }
+    static int trees(void *ctx, const uint32_t *roots, int32_t count, int32_t *dist, int32_t *pslot,
+                     uint8_t *skip) {
+        GpuTreeSupplier *g = static_cast<GpuTreeSupplier *>(ctx);
+        return mcbgpu_trees_run(g->t, roots, count, dist, pslot, skip, nullptr) == MCBGPU_OK ? 0 : 1;
+    }
 };
 
 // One problem from preparation to output.
@@ -181,7 +207,19 @@ void collect_job(Job &j) {
 // Host preparation of one problem: reduced graph, FVS, trees, candidates.
 void prepare_job(Job &j, const Outputs &o) {
     const mcbh_options opt = job_options(o);
-    check_host(mcbh_prepare(j.p, &opt), "preprocessing failed");
+    if (o.gpu_trees) {
+        init_gpu_once();
+        GpuTreeSupplier g;
+        mcbh_tree_source src{&g, &GpuTreeSupplier::begin, &GpuTreeSupplier::trees, g.chunk};
+        const int rc = mcbh_prepare_with_trees(j.p, &opt, &src);
+        if (rc == MCBH_E_SUPPLIER) {
+            std::fprintf(stderr, "mcb_gb300: GPU trees: %s\n", mcbgpu_last_error());
+            std::exit(1);
+        }
+        check_host(rc, "preprocessing failed");
+    } else {
+        check_host(mcbh_prepare(j.p, &opt), "preprocessing failed");
+    }
     collect_job(j);
 }
 
@@ -307,7 +345,7 @@ void emit_job(Job &j, const Outputs &o) {
 int main(int argc, char **argv) {
     std::vector<const char *> pos;
     const char *cycles_path = nullptr, *cycles_input_path = nullptr;
-    bool plain = false, bcc = false, verify = false;
+    bool plain = false, bcc = false, verify = false, gpu_trees = false;
     for (int i = 1; i < argc; i++) {
         if (!std::strcmp(argv[i], "--cycles") && i + 1 < argc)
             cycles_path = argv[++i];
@@ -319,6 +357,8 @@ int main(int argc, char **argv) {
             bcc = true;
         else if (!std::strcmp(argv[i], "--verify"))
             verify = true;
+        else if (!std::strcmp(argv[i], "--gpu-trees"))
+            gpu_trees = true;
         else
             pos.push_back(argv[i]);
     }
@@ -327,7 +367,7 @@ int main(int argc, char **argv) {
         std::printf("2nd Argument should indicate the OutputFile\n");
         std::printf("3th argument should indicate the number of threads.(Optional) (1 default)\n");
         std::printf("4th Argument is chunk_size.(Optional) (720 default)\n");
-        std::printf("options: --cycles FILE, --cycles-input FILE, --plain, --bcc, --verify\n");
+        std::printf("options: --cycles FILE, --cycles-input FILE, --plain, --bcc, --verify, --gpu-trees\n");
         return 1;
     }
     const char *input = pos[0];
@@ -336,6 +376,7 @@ int main(int argc, char **argv) {
     o.threads = std::atoi(pos[2]);
     o.plain = plain;
     o.verify = verify;
+    o.gpu_trees = gpu_trees;
     if (cycles_path && !(o.cycles = std::fopen(cycles_path, "w"))) fail("cannot open the cycle file", cycles_path);
     if (cycles_input_path && !(o.cycles_input = std::fopen(cycles_input_path, "w")))
         fail("cannot open the cycle file", cycles_input_path);

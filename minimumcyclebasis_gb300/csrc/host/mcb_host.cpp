@@ -487,6 +487,7 @@ struct TreeWorkspace {
     std::vector<VertexState> vs;
     RadixQueue rq;
     std::vector<int> level;
+    std::vector<u32> chain;
     std::vector<u32> pop_order;
     std::vector<unsigned char> pair_tree;
     DistHeap pq;  // include/Dijkstra.h:37-44: min-heap on distance only
@@ -592,6 +593,60 @@ bool search_fast(const mcbh_problem &P, u32 src, TreeWorkspace &ws, std::vector<
     return rivals == 0;
 }
 
+// A root's tree supplied from outside (mcbh_prepare_with_trees: distances and parent
+// slots, e.g. computed on the GPU), adopted only if it is the tree the reference's
+// search builds.  With every weight at least 1 that is checked in two passes over the
+// slots: (1) it is a tree of shortest paths: the root at distance 0, every other
+// vertex entered by its parent slot from a vertex whose distance plus the slot's
+// weight is its own, and no slot giving any vertex a shorter path; (2) every parent
+// is the one the reference keeps: the nearest of the vertex's shortest-path
+// neighbours, through that neighbour's first such slot, with no other neighbour as
+// near (otherwise the heap's order decides, and the root is searched here).  Returns
+// false, leaving the workspace to be reinitialised, if a check fails.
+bool take_given_tree(const mcbh_problem &P, u32 src, TreeWorkspace &ws, const int32_t *dist, const int32_t *pedge,
+                     std::vector<u32> &tree_edges) {
+    const Graph &g = P.rg;
+    const int n = g.n;
+    const int64_t slots = (int64_t)g.slots();
+    VertexState *vs = ws.vs.data();
+    if (dist[src] != 0 || pedge[src] != -1) return false;
+    for (int v = 0; v < n; v++) {
+        if ((u32)v == src) continue;
+        const int64_t o = pedge[v];
+        if (o < 0 || o >= slots || g.cols[o] != (u32)v) return false;
+        const u32 p = g.rows[o];
+        if (dist[p] < 0 || (long long)dist[p] + g.w[o] != (long long)dist[v]) return false;
+    }
+    for (int c = 0; c < n; c++) {
+        const int dc = dist[c];
+        int bestd = -1;
+        u32 bestx = 0xffffffffu, bests = 0xffffffffu;
+        for (u32 o = g.ro[c]; o < g.ro[c + 1]; o++) {
+            const u32 x = g.cols[o];
+            const long long via = (long long)dc + g.w[o];
+            if ((long long)dist[x] > via) return false;  // a shorter path to x through c
+            if ((u32)c == src || (long long)dist[x] + g.w[o] != (long long)dc) continue;
+            if (bestd < 0 || dist[x] < bestd) {
+                bestd = dist[x];
+                bestx = x;
+                bests = g.rev[o];
+            } else if (dist[x] == bestd) {
+                if (x != bestx) return false;  // two neighbours equally near: the heap decides
+                bests = g.rev[o] < bests ? g.rev[o] : bests;
+            }
+        }
+        if ((u32)c != src && (int64_t)bests != (int64_t)pedge[c]) return false;
+    }
+    for (int v = 0; v < n; v++) {
+        vs[v].dist = dist[v];
+        vs[v].pedge = pedge[v];
+        vs[v].par = (u32)v == src ? -1 : (int)g.rows[pedge[v]];
+        vs[v].done = 1;
+        if ((u32)v != src) tree_edges.push_back((u32)pedge[v]);
+    }
+    return true;
+}
+
 // Which search one root takes, and what it cost.
 struct SearchChoice {
     bool try_fast = false;  // in: try search_fast first
@@ -637,9 +692,12 @@ struct SearchPolicy {
     }
 };
 
+// given_dist / given_pedge: a supplied tree for this root (or null), adopted after
+// take_given_tree's checks; *given_taken says whether it was.
 void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput &out, bool want_lists,
                   int *tree_parent, u32 *lay_rows, u32 *lay_cols, int *lay_edge, u32 *lay_nodes,
-                  SearchChoice &choice) {
+                  SearchChoice &choice, const int32_t *given_dist = nullptr, const int32_t *given_pedge = nullptr,
+                  bool *given_taken = nullptr) {
     const Graph &g = P.rg;
     const int n = g.n;
     const u32 src = P.fvs_vertices[tidx];
@@ -648,7 +706,18 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
     tree_edges.reserve(n);
     bool fast_done = false;
     choice.result = -1;
-    if (choice.try_fast && P.fast_search_ok && !lay_rows) {
+    if (given_taken) *given_taken = false;
+    if (given_dist && given_pedge && P.fast_search_ok && !lay_rows) {
+        if (take_given_tree(P, src, ws, given_dist, given_pedge, tree_edges)) {
+            fast_done = true;
+            choice.try_fast = false;
+            if (given_taken) *given_taken = true;
+        } else {
+            ws.init(n, P.pair_first.size());
+            tree_edges.clear();
+        }
+    }
+    if (!fast_done && choice.try_fast && P.fast_search_ok && !lay_rows) {
         const double t0 = now_s();
         fast_done = search_fast(P, src, ws, tree_edges);
         choice.fast_s = now_s() - t0;
@@ -675,11 +744,27 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
     constexpr int kBlocked = -2;
     std::vector<int> &branch = ws.tmp;
     branch.assign(n, -1);
-    for (u32 x : ws.pop_order) {
-        if (x == src) continue;
+    auto code_of = [&](u32 x) {
         const int p = vs[x].par;
         const int bp = ((u32)p == src) ? (int)x : branch[p];
-        branch[x] = (bp == kBlocked || (P.fvs_array[x] >= 0 && src > x)) ? kBlocked : bp;
+        return (bp == kBlocked || (P.fvs_array[x] >= 0 && src > x)) ? kBlocked : bp;
+    };
+    if (!ws.pop_order.empty()) {
+        for (u32 x : ws.pop_order)
+            if (x != src) branch[x] = code_of(x);
+    } else {
+        // a supplied tree has no settle order: each vertex's chain up to the first
+        // vertex already done, then down (distances fall strictly along a chain,
+        // checked, so every chain ends)
+        constexpr int kUnset = -3;
+        branch.assign(n, kUnset);
+        branch[src] = -1;
+        std::vector<u32> &chain = ws.chain;
+        for (int v = 0; v < n; v++) {
+            chain.clear();
+            for (u32 x = (u32)v; branch[x] == kUnset; x = (u32)vs[x].par) chain.push_back(x);
+            for (size_t i = chain.size(); i-- > 0;) branch[chain[i]] = code_of(chain[i]);
+        }
     }
     // dijkstra::compute_non_tree_edges (include/Dijkstra.h:129-149): its scan over the
     // slots in ascending order keeps, of every pair that holds no tree slot, the slot
@@ -895,7 +980,7 @@ int64_t mcbh_read_mtx(const char *path, int32_t *nodes, int64_t cap, int32_t *u,
 
 void mcbh_problem_free(mcbh_problem *p) { delete p; }
 
-int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
+static int prepare_impl(mcbh_problem *P, const mcbh_options *opt, const mcbh_tree_source *source) {
     if (!P || !opt) return MCBH_E_ARG;
     if (P->prepared) return MCBH_E_STATE;
     mcbh_info &I = P->info;
@@ -981,19 +1066,58 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
         int threads = opt->threads > 0 ? opt->threads : omp_get_max_threads();
         bool lists = opt->cycle_lists != 0;
         SearchPolicy policy;
+        I.trees_supplied = 0;
+        const bool supplied = source && source->trees && P->fast_search_ok && !opt->ref_layout && F > 0;
+        if (supplied) {
+            // trees from the supplier, `chunk` roots per call; each adopted after
+            // take_given_tree's checks, the others searched here
+            const Graph &g = P->rg;
+            if (source->begin && source->begin(source->ctx, g.n, (int64_t)g.slots(), g.ro.data(), g.cols.data(),
+                                               g.w.data(), g.rev.data()) != 0)
+                return MCBH_E_SUPPLIER;
+            const int chunk = source->chunk > 0 ? std::min(source->chunk, F) : F;
+            std::vector<int32_t> gd((size_t)chunk * n), gp((size_t)chunk * n);
+            std::vector<uint8_t> gt((size_t)chunk);
+            std::vector<TreeWorkspace> wss((size_t)threads);
+            std::atomic<int> taken_count{0};
+            for (int t0 = 0; t0 < F; t0 += chunk) {
+                const int cnt = std::min(chunk, F - t0);
+                std::fill(gt.begin(), gt.begin() + cnt, (uint8_t)1);
+                if (source->trees(source->ctx, &P->fvs_vertices[(size_t)t0], cnt, gd.data(), gp.data(), gt.data()) != 0)
+                    return MCBH_E_SUPPLIER;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+                for (int i = 0; i < cnt; i++) {
+                    const int t = t0 + i;
+                    SearchChoice choice;
+                    choice.try_fast = policy.want_fast(t);
+                    bool taken = false;
+                    const bool offer = gt[(size_t)i] == 0;
+                    process_root(*P, t, wss[(size_t)omp_get_thread_num()], outs[t], lists,
+                                 opt->keep_trees ? P->tree_parent.data() : nullptr, nullptr, nullptr, nullptr, nullptr,
+                                 choice, offer ? &gd[(size_t)i * n] : nullptr, offer ? &gp[(size_t)i * n] : nullptr,
+                                 &taken);
+                    if (taken)
+                        taken_count.fetch_add(1, std::memory_order_relaxed);
+                    else
+                        policy.record(choice);
+                }
+            }
+            I.trees_supplied = taken_count.load();
+        } else {
 #pragma omp parallel num_threads(threads)
-        {
-            TreeWorkspace ws;
+            {
+                TreeWorkspace ws;
 #pragma omp for schedule(dynamic, 1)
-            for (int t = 0; t < F; t++) {
-                SearchChoice choice;
-                choice.try_fast = policy.want_fast(t);
-                process_root(*P, t, ws, outs[t], lists, opt->keep_trees ? P->tree_parent.data() : nullptr,
-                             opt->ref_layout ? P->lay_rows.data() : nullptr,
-                             opt->ref_layout ? P->lay_cols.data() : nullptr,
-                             opt->ref_layout ? P->lay_edge.data() : nullptr,
-                             opt->ref_layout ? P->lay_nodes.data() : nullptr, choice);
-                policy.record(choice);
+                for (int t = 0; t < F; t++) {
+                    SearchChoice choice;
+                    choice.try_fast = policy.want_fast(t);
+                    process_root(*P, t, ws, outs[t], lists, opt->keep_trees ? P->tree_parent.data() : nullptr,
+                                 opt->ref_layout ? P->lay_rows.data() : nullptr,
+                                 opt->ref_layout ? P->lay_cols.data() : nullptr,
+                                 opt->ref_layout ? P->lay_edge.data() : nullptr,
+                                 opt->ref_layout ? P->lay_nodes.data() : nullptr, choice);
+                    policy.record(choice);
+                }
             }
         }
         I.t_trees = now_s() - t0;
@@ -1073,6 +1197,13 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) {
     }
     P->prepared = true;
     return MCBH_OK;
+}
+
+int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) { return prepare_impl(P, opt, nullptr); }
+
+int mcbh_prepare_with_trees(mcbh_problem *P, const mcbh_options *opt, const mcbh_tree_source *source) {
+    if (!source || !source->trees) return MCBH_E_ARG;
+    return prepare_impl(P, opt, source);
 }
 
 int mcbh_prepare_many(mcbh_problem **ps, int64_t count, const mcbh_options *opt, int32_t *status) {

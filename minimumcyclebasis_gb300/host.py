@@ -223,6 +223,51 @@ class Problem:
         self._opts = opt
         return self
 
+    def prepare_with_trees(self, trees, chunk: int = 0, threads: int = 0, keep_trees: bool = False,
+                           ref_layout: bool = False, cycle_lists: bool = True, begin=None) -> "Problem":
+        """prepare() with the per-root shortest-path trees taken from `trees(roots)` ->
+        (dist int32[count, n], parent_slot int32[count, n], skip uint8[count]) where it
+        offers one (mcbh_prepare_with_trees); every offered tree is checked, and a root
+        whose tree fails or is skipped is searched on the host, so the result is
+        prepare()'s.  `begin(nodes, row_offsets, cols, weights, rev)` (optional) sees
+        the reduced graph first.  info.trees_supplied counts the adopted trees."""
+        from ._native import TREE_BEGIN, TREE_TREES, MCBHTreeSource
+        state = {}
+
+        def c_begin(ctx, nodes, slots, ro, cols, w, rev):
+            try:
+                state["n"] = int(nodes)
+                if begin is not None:
+                    arr = lambda p_, t, k: np.ctypeslib.as_array(C.cast(p_, C.POINTER(t)), shape=(k,)).copy()
+                    begin(int(nodes), arr(ro, C.c_uint32, nodes + 1), arr(cols, C.c_uint32, slots),
+                          arr(w, C.c_int32, slots), arr(rev, C.c_uint32, slots))
+                return 0
+            except Exception:
+                return 1
+
+        def c_trees(ctx, roots, count, dist, pslot, skip):
+            try:
+                n = state["n"]
+                r = np.ctypeslib.as_array(C.cast(roots, C.POINTER(C.c_uint32)), shape=(count,)).copy()
+                d, ps, sk = trees(r)
+                np.ctypeslib.as_array(C.cast(dist, C.POINTER(C.c_int32)), shape=(count * n,))[:] = \
+                    np.asarray(d, np.int32).reshape(-1)
+                np.ctypeslib.as_array(C.cast(pslot, C.POINTER(C.c_int32)), shape=(count * n,))[:] = \
+                    np.asarray(ps, np.int32).reshape(-1)
+                np.ctypeslib.as_array(C.cast(skip, C.POINTER(C.c_uint8)), shape=(count,))[:] = \
+                    np.asarray(sk, np.uint8).reshape(-1)
+                return 0
+            except Exception:
+                return 1
+
+        cb_begin, cb_trees = TREE_BEGIN(c_begin), TREE_TREES(c_trees)
+        src = MCBHTreeSource(None, cb_begin, cb_trees, chunk)
+        opt = MCBHOptions(threads, 1, int(keep_trees), int(ref_layout), int(cycle_lists))
+        check_host(host_lib().mcbh_prepare_with_trees(self._h, C.byref(opt), C.byref(src)), "mcbh_prepare_with_trees")
+        self.prepared = True
+        self._opts = opt
+        return self
+
     def gf2_rank(self, ranks, threads: int = 0) -> int:
         """GF(2) rank of the cycle vectors of the candidates at `ranks` (mcbh_gf2_rank):
         a basis re-verified by elimination has rank == len(ranks) == N."""
