@@ -1,10 +1,11 @@
-"""Host preparation against the reference's own host library on fresh graphs:
+"""Host preparation and the oracle against the reference's own code on fresh graphs:
 oracle/_ref/ref_dump (built by oracle/Makefile from the reference's sources, where
 they are present) prints the reference's rank-ordered candidate list, which must
-equal ours entry for entry (root, edge offset, weight).  The families cover both
-tree searches (the radix-queue search with its fallback, and the heap search for
-weights of 0), dense ties (small integer weights), chains and parallel edges.
-Skipped where the reference harness is not built."""
+equal ours entry for entry (root, edge offset, weight), and the basis its de Pina
+loop selects, which the oracle must select too.  The families cover both tree
+searches (the radix-queue search with its fallback, and the heap search for weights
+of 0), dense ties (small integer weights), chains and parallel edges.  Skipped
+where the reference harness is not built."""
 import os
 import subprocess
 
@@ -46,3 +47,36 @@ def test_candidates_equal_the_reference_host_library(tmp_path, family):
     assert np.array_equal(ref[:, 1], root)
     assert np.array_equal(ref[:, 2], edge)
     assert np.array_equal(ref[:, 3], w)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DUMP), reason="reference harness (oracle/_ref) not built here")
+@pytest.mark.parametrize("family", ["random_w5", "random_w0to1", "planar_w3", "grid_w2"])
+def test_oracle_selects_the_reference_loop_basis(tmp_path, family):
+    import oracle
+    g = {"random_w5": lambda: random_graph(900, 1800, 1, 5, 51),
+         "random_w0to1": lambda: random_graph(700, 1600, 0, 1, 52),
+         "planar_w3": lambda: planar_chain_graph(900, 30, 30, 8, 1, 3, 53),
+         "grid_w2": lambda: grid_graph(24, 24, 1, 2, 54)}[family]()
+    mtx = str(tmp_path / "g.mtx")
+    g.write_mtx(mtx)
+    r = subprocess.run([REF_DUMP, mtx, "4", "-1", "noE", "noC"], capture_output=True, text=True, timeout=600)
+    sel_ref = [int(ln.split()[2]) for ln in r.stdout.splitlines() if ln.startswith("S ")]
+    total_ref = [int(ln.split()[1]) for ln in r.stdout.splitlines() if ln.startswith("W ")]
+    stop = [ln for ln in r.stdout.splitlines() if ln.startswith("X no odd candidate at iteration ")]
+    p = Problem.from_mtx(mtx).prepare(threads=4, keep_trees=True)
+    if stop:
+        # with weights of 0 the reference's candidate set need not span: its loop finds
+        # no odd candidate at some iteration, and the oracle stops at the same one
+        k = int(stop[0].split()[-1])
+        assert len(sel_ref) == k < p.N
+        with pytest.raises(RuntimeError, match="no odd candidate at iteration %d$" % k):
+            oracle.solve(p, threads=4)
+        sel, _, _ = oracle.solve(p, threads=4, max_iter=k)
+        assert sel.tolist() == sel_ref
+        assert p.gf2_rank(sel) == k
+        return
+    assert r.returncode == 0, r.stderr[-2000:]
+    sel, total, _ = oracle.solve(p, threads=4)
+    assert len(sel_ref) == p.N and sel.tolist() == sel_ref
+    assert total_ref == [total]
+    assert p.gf2_rank(sel) == p.N
