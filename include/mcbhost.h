@@ -77,6 +77,8 @@ int mcbh_problem_from_mtx(const char *path, mcbh_problem **out);
 /* m undirected edges (u[i], v[i], w[i]), 0-based, inserted in that order. */
 int mcbh_problem_from_edges(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v,
                             const int32_t *w, mcbh_problem **out);
+/* One preparation per problem: a second call, after success or failure, returns
+ * MCBH_E_STATE. */
 int mcbh_prepare(mcbh_problem *p, const mcbh_options *opt);
 /* A supplier of per-root shortest-path trees for mcbh_prepare_with_trees (e.g. the
  * GPU's, mcbgpu_trees_*).  begin (optional) receives the reduced graph once, before

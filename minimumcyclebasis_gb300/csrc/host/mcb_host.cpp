@@ -95,6 +95,7 @@ struct mcbh_problem {
     Graph in;
     i64 m_in = 0;
     bool prepared = false;
+    bool attempted = false;  // one preparation per problem, successful or not
     bool single_cycle = false;
     i64 total_weight_input = 0;
     // reduced multigraph
@@ -982,7 +983,8 @@ void mcbh_problem_free(mcbh_problem *p) { delete p; }
 
 static int prepare_impl(mcbh_problem *P, const mcbh_options *opt, const mcbh_tree_source *source) {
     if (!P || !opt) return MCBH_E_ARG;
-    if (P->prepared) return MCBH_E_STATE;
+    if (P->prepared || P->attempted) return MCBH_E_STATE;
+    P->attempted = true;
     mcbh_info &I = P->info;
     I.nodes = P->in.n;
     I.edges2 = (int64_t)P->in.slots();

@@ -107,8 +107,11 @@ def test_supplier_failure_and_unused_supplier():
 
     def failing(roots):
         raise RuntimeError("no trees")
-    with pytest.raises(MCBError):
-        Problem.from_graph(g).prepare_with_trees(failing, threads=2)
+    f = Problem.from_graph(g)
+    with pytest.raises(MCBError, match="-7"):
+        f.prepare_with_trees(failing, threads=2)
+    with pytest.raises(MCBError, match="-5"):  # no second preparation on a problem left half-prepared
+        f.prepare(threads=2)
     # the level-ordered layout follows the heap's settle order: the supplier is not asked
     asked = []
     q = Problem.from_graph(g).prepare_with_trees(lambda r: asked.append(1), threads=2, keep_trees=True,
