@@ -22,6 +22,8 @@
 //      different distances settle in distance order) unless two different
 //      neighbours tie at that nearest distance, which sets the root's flag so that
 //      the host searches that root itself.
+// CTA barriers are cta_sync / cta_sync_and (the non-aligned barrier): the loops
+// before them diverge within warps.
 #include <climits>
 #include <vector>
 
@@ -55,13 +57,13 @@ __device__ __forceinline__ int block_min(int v, int *red) {
     v = __reduce_min_sync(0xffffffffu, v);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) red[warp] = v;
-    __syncthreads();
+    cta_sync();
     if (warp == 0) {
         int x = lane < (int)(blockDim.x >> 5) ? red[lane] : INT_MAX;
         x = __reduce_min_sync(0xffffffffu, x);
         if (lane == 0) red[32] = x;
     }
-    __syncthreads();
+    cta_sync();
     return red[32];
 }
 
@@ -86,19 +88,19 @@ __global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (;;) {
         if (tid == 0) s_root = atomicAdd(a.next_root, 1);
-        __syncthreads();
+        cta_sync();
         const int r = s_root;
-        __syncthreads();  // every thread has read s_root before thread 0 writes it again
+        cta_sync();  // every thread has read s_root before thread 0 writes it again
         if (r >= a.count) return;
         const uint32_t src = a.roots[r];  // < n, checked by the host
         for (int v = tid; v < n; v += nt) dist[v] = INT_MAX;
         for (int k = tid; k < words; k += nt) dirty[k] = 0;
-        __syncthreads();
+        cta_sync();
         if (tid == 0) {
             dist[src] = 0;
             dirty[src >> 5] = 1u << (src & 31);
         }
-        __syncthreads();
+        cta_sync();
         // 1. distances
         bool converged = false;
         for (int round = 0; round <= n; round++) {
@@ -137,7 +139,7 @@ __global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
                     }
                 }
             }
-            __syncthreads();
+            cta_sync();
         }
         // 2. parents by the rule, and the root's tie flag
         int tie = converged ? 0 : 1;
@@ -145,7 +147,7 @@ __global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
             const int dc = vdist[c];
             int32_t slot = -1;
             if ((uint32_t)c != src && dc != INT_MAX) {
-                int bestd = INT_MAX;
+                int bestd = INT_MAX, rival = 0;  // rival: another neighbour as near as the best
                 uint32_t bestx = 0xffffffffu, bests = 0xffffffffu;
                 for (uint32_t o = a.ro[c]; o < a.ro[c + 1]; o++) {
                     const uint32_t x = a.cols[o];
@@ -155,22 +157,23 @@ __global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
                         bestd = dx;
                         bestx = x;
                         bests = a.rev[o];
+                        rival = 0;
                     } else if (dx == bestd) {
                         if (x == bestx)
                             bests = a.rev[o] < bests ? a.rev[o] : bests;
                         else
-                            tie = 1;
+                            rival = 1;
                     }
                 }
                 slot = bests == 0xffffffffu ? -1 : (int32_t)bests;
-                if (slot < 0) tie = 1;  // no shortest-path neighbour: cannot happen, left to the host
+                if (rival || slot < 0) tie = 1;  // (no shortest-path neighbour cannot happen; left to the host)
             } else if ((uint32_t)c != src) {
                 tie = 1;  // unreachable vertex (the graph is not connected): left to the host
             }
             a.dist_out[(size_t)r * n + c] = dc;
             a.pedge_out[(size_t)r * n + c] = slot;
         }
-        tie = __syncthreads_or(tie);
+        tie = cta_sync_and(tie == 0) ? 0 : 1;
         if (tid == 0) a.tied_out[r] = tie ? 1 : 0;
         if (!converged && tid == 0) atomicOr(a.status, ST_DIVERGED);
     }

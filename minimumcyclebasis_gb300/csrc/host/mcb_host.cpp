@@ -621,6 +621,7 @@ bool take_given_tree(const mcbh_problem &P, u32 src, TreeWorkspace &ws, const in
     for (int c = 0; c < n; c++) {
         const int dc = dist[c];
         int bestd = -1;
+        bool rival = false;  // another neighbour as near as the best: the heap decides
         u32 bestx = 0xffffffffu, bests = 0xffffffffu;
         for (u32 o = g.ro[c]; o < g.ro[c + 1]; o++) {
             const u32 x = g.cols[o];
@@ -631,12 +632,15 @@ bool take_given_tree(const mcbh_problem &P, u32 src, TreeWorkspace &ws, const in
                 bestd = dist[x];
                 bestx = x;
                 bests = g.rev[o];
+                rival = false;
             } else if (dist[x] == bestd) {
-                if (x != bestx) return false;  // two neighbours equally near: the heap decides
-                bests = g.rev[o] < bests ? g.rev[o] : bests;
+                if (x != bestx)
+                    rival = true;
+                else
+                    bests = g.rev[o] < bests ? g.rev[o] : bests;
             }
         }
-        if ((u32)c != src && (int64_t)bests != (int64_t)pedge[c]) return false;
+        if ((u32)c != src && (rival || (int64_t)bests != (int64_t)pedge[c])) return false;
     }
     for (int v = 0; v < n; v++) {
         vs[v].dist = dist[v];
