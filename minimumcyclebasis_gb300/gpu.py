@@ -337,3 +337,50 @@ def solve_batch(problems):
     out = b.results()
     b.close()
     return out
+
+
+class GpuTrees:
+    """Shortest-path trees of many roots on the GPU (mcbgpu_trees_*): distances,
+    parent slots by the reference's rule, and a per-root tie flag (1: the host must
+    search that root itself).  The graph is a prepared Problem's reduced graph."""
+
+    def __init__(self, nodes: int, row_offsets, cols, weights, rev, max_roots: int):
+        self.lib = gpu_lib()
+        self.n = int(nodes)
+        self.max_roots = int(max_roots)
+        ro = np.ascontiguousarray(row_offsets, np.uint32)
+        c = np.ascontiguousarray(cols, np.uint32)
+        w = np.ascontiguousarray(weights, np.int32)
+        r = np.ascontiguousarray(rev, np.uint32)
+        h = C.c_void_p()
+        check_gpu(self.lib.mcbgpu_trees_create(C.byref(h), self.n, len(c), ptr(ro), ptr(c), ptr(w), ptr(r),
+                                               self.max_roots), "mcbgpu_trees_create")
+        self._h = h
+
+    @classmethod
+    def from_problem(cls, p, max_roots: int) -> "GpuTrees":
+        rows, cols, w, rev, ro = p.reduced_graph()
+        return cls(p.n, ro, cols, w, rev, max_roots)
+
+    def run(self, roots, stream=0):
+        """(dist int32[count, n], parent_slot int32[count, n], tied uint8[count])."""
+        r = np.ascontiguousarray(roots, np.uint32)
+        k = len(r)
+        dist = np.empty((max(k, 1), self.n), np.int32)
+        ps = np.empty((max(k, 1), self.n), np.int32)
+        tied = np.empty(max(k, 1), np.uint8)
+        check_gpu(self.lib.mcbgpu_trees_run(self._h, ptr(r), k, ptr(dist), ptr(ps), ptr(tied), _stream(stream)),
+                  "mcbgpu_trees_run")
+        return dist[:k], ps[:k], tied[:k]
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.lib.mcbgpu_trees_device_bytes(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.mcbgpu_trees_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
