@@ -80,3 +80,54 @@ def test_oracle_selects_the_reference_loop_basis(tmp_path, family):
     assert len(sel_ref) == p.N and sel.tolist() == sel_ref
     assert total_ref == [total]
     assert p.gf2_rank(sel) == p.N
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DUMP), reason="reference harness (oracle/_ref) not built here")
+def test_small_random_multigraphs_match_the_reference(tmp_path):
+    # 150 seeded graphs of 4-40 vertices: a random tree plus extra edges with parallel
+    # edges, weights in {0..2}, {1..3}, {1..9} or {1..1000}; candidate lists and the
+    # selected basis (or the iteration where the candidates run out) must agree
+    import oracle
+    from minimumcyclebasis_gb300.host import Graph
+    from minimumcyclebasis_gb300._native import MCBError
+    rng = np.random.default_rng(2024)
+    compared = rejected = 0
+    for it in range(150):
+        n = int(rng.integers(4, 40))
+        perm = rng.permutation(n)
+        u = [int(perm[i]) for i in range(1, n)]
+        v = [int(perm[rng.integers(0, i)]) for i in range(1, n)]
+        for _ in range(int(rng.integers(1, 2 * n))):
+            a, b = (int(x) for x in rng.integers(0, n, 2))
+            if a != b:
+                u.append(a)
+                v.append(b)
+        lo, hi = [(0, 2), (1, 3), (1, 9), (1, 1000)][it % 4]
+        w = rng.integers(lo, hi + 1, len(u))
+        mtx = str(tmp_path / ("g%d.mtx" % it))
+        Graph(n, np.array(u, np.int32), np.array(v, np.int32), np.array(w, np.int32)).write_mtx(mtx)
+        r = subprocess.run([REF_DUMP, mtx, "2", "-1", "noE"], capture_output=True, text=True, timeout=120)
+        try:
+            p = Problem.from_mtx(mtx).prepare(threads=2, keep_trees=True)
+        except MCBError:
+            # an input the reference cannot process either (degree-two vertices on
+            # parallel edges crash it); the host reports MCBH_E_GRAPH instead
+            assert r.returncode != 0, it
+            rejected += 1
+            continue
+        if p.info.single_cycle:
+            continue
+        ref = np.array([[int(x) for x in ln.split()[1:]] for ln in r.stdout.splitlines() if ln.startswith("C ")],
+                       dtype=np.int64).reshape(-1, 4)
+        root, edge, wt, _ = p.candidates()
+        assert np.array_equal(ref[:, 1:], np.stack([root, edge, wt], 1)), it
+        sel_ref = [int(ln.split()[2]) for ln in r.stdout.splitlines() if ln.startswith("S ")]
+        stop = [ln for ln in r.stdout.splitlines() if ln.startswith("X no odd candidate")]
+        if stop:
+            with pytest.raises(RuntimeError, match="at iteration %d$" % len(sel_ref)):
+                oracle.solve(p, threads=2)
+        else:
+            sel, _, _ = oracle.solve(p, threads=2)
+            assert sel.tolist() == sel_ref, it
+        compared += 1
+    assert compared > 100 and rejected < 40
