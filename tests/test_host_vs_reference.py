@@ -110,8 +110,9 @@ def test_small_random_multigraphs_match_the_reference(tmp_path):
         try:
             p = Problem.from_mtx(mtx).prepare(threads=2, keep_trees=True)
         except MCBError:
-            # an input the reference cannot process either (degree-two vertices on
-            # parallel edges crash it); the host reports MCBH_E_GRAPH instead
+            # an input the reference cannot process either (most have a degree-two
+            # vertex whose two edges are parallel; they crash it); the host reports
+            # MCBH_E_GRAPH instead
             assert r.returncode != 0, it
             rejected += 1
             continue
