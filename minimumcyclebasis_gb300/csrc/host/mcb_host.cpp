@@ -113,6 +113,7 @@ struct mcbh_problem {
     // slot pairs of the reduced graph: the lower slot of every pair in ascending
     // order, and each slot's pair index
     std::vector<u32> pair_first, slot_pair;
+    std::vector<std::pair<u32, u32>> pair_ends;  // (row, column) of each pair's lower slot
     // the reduced graph's slots as (column, weight) records, for the tree searches
     struct Arc {
         u32 col;
@@ -779,12 +780,12 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
     const size_t npairs = P.pair_first.size();
     for (size_t k = 0; k < npairs; k++) {
         if (ws.pair_tree[k]) continue;
-        const u32 off = P.pair_first[k];
-        const u32 a = g.rows[off], b = g.cols[off];
+        const u32 a = P.pair_ends[k].first, b = P.pair_ends[k].second;
         const int ba = branch[a], bb = branch[b];
         if (ba == kBlocked || bb == kBlocked) continue;
         const bool lca_root = (a == src) || (b == src) || (ba != bb);
         if (!lca_root) continue;
+        const u32 off = P.pair_first[k];
         int weight = vs[a].dist + vs[b].dist + g.w[off];
         LocalCandidate lc;
         lc.edge = (int)off;
@@ -1052,6 +1053,8 @@ static int prepare_impl(mcbh_problem *P, const mcbh_options *opt, const mcbh_tre
             const Graph &g = P->rg;
             P->pair_first.clear();
             P->pair_first.reserve(g.slots() / 2);
+            P->pair_ends.clear();
+            P->pair_ends.reserve(g.slots() / 2);
             P->slot_pair.assign(g.slots(), 0);
             P->arcs.resize(g.slots());
             long long wmin = 1, wmax = 0;
@@ -1065,6 +1068,7 @@ static int prepare_impl(mcbh_problem *P, const mcbh_options *opt, const mcbh_tre
                 if (i < g.rev[i]) {
                     P->slot_pair[i] = P->slot_pair[g.rev[i]] = (u32)P->pair_first.size();
                     P->pair_first.push_back((u32)i);
+                    P->pair_ends.push_back(std::make_pair(g.rows[i], g.cols[i]));
                 }
             }
         }
