@@ -134,8 +134,12 @@ int mcbgpu_struct_create(mcbgpu_struct **out, int num_edges, int num_non_tree_ed
     if (s->words_even == 0) s->words_even = 2;
     const size_t Fn = (size_t)fvs_size * original_nodes;
     cudaError_t e = cudaSuccess;
-#define ALLOC(ptr, bytes)                                   \
-    if (e == cudaSuccess) e = cudaMalloc((void **)&(ptr), (bytes) ? (bytes) : 16);
+#define ALLOC(ptr, bytes)                                              \
+    do {                                                               \
+        size_t _b = (size_t)(bytes);                                   \
+        if (_b == 0) _b = 16;                                          \
+        if (e == cudaSuccess) e = cudaMalloc((void **)&(ptr), _b);     \
+    } while (0)
     ALLOC(s->d_map, sizeof(int32_t) * (size_t)num_edges);
     ALLOC(s->d_edge, sizeof(int32_t) * Fn);
     ALLOC(s->d_parent, sizeof(uint32_t) * Fn);
