@@ -33,7 +33,7 @@ namespace mcbgpu {
 namespace {
 
 constexpr int kTreeThreads = 1024;
-constexpr int kTreeSharedMaxN = 40960;  // 160 KB of distances + 5 KB of dirty bits
+constexpr int kTreeSharedMaxN = 53248;  // 208 KB of distances + 6.5 KB of dirty bits (of 227 KB)
 
 struct TreeArgs {
     const uint32_t *ro;

@@ -1,6 +1,6 @@
 """GPU shortest-path trees (mcbgpu_trees_*) against the host's: distances equal
 everywhere, the tie flag equal to the rule's, and parent slots equal wherever the
-root has no tie; the shared-memory form (n' <= 40960) and the global one; and the
+root has no tie; the shared-memory form (n' <= 53248) and the global one; and the
 host preparation fed by the GPU trees equals prepare().  Run only with
 MCB_RUN_GPU_TREES=1 until the kernel has been run on a GPU."""
 import os
@@ -49,9 +49,9 @@ def test_gpu_trees_equal_the_host_trees(family):
 
 
 def test_gpu_trees_global_form():
-    # more than 40960 vertices after contraction: distances in per-CTA global slices
-    p = Problem.from_graph(random_graph(52000, 104000, 1, 1000, 104)).prepare(threads=0, keep_trees=True)
-    assert p.n > 40960
+    # more than 53248 vertices after contraction: distances in per-CTA global slices
+    p = Problem.from_graph(random_graph(66000, 132000, 1, 1000, 104)).prepare(threads=0, keep_trees=True)
+    assert p.n > 53248
     gt = GpuTrees.from_problem(p, max_roots=16)
     _, roots = p.fvs()
     idx = list(range(0, p.F, p.F // 16))[:16]
