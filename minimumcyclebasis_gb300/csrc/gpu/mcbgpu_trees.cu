@@ -291,8 +291,11 @@ int mcbgpu_trees_create(mcbgpu_trees **out, int32_t nodes, int64_t slots, const 
         if (e == cudaSuccess) e = cudaMemcpy(t->d_rev, rev, 4 * (size_t)slots, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(t->d_w, weights, 4 * (size_t)slots, cudaMemcpyHostToDevice);
     }
+    // the kernel's attribute is process-wide: set to the largest shared form, so that
+    // handles of different sizes can be used in any order
     if (e == cudaSuccess && t->shared_form)
-        e = cudaFuncSetAttribute(trees_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t->smem);
+        e = cudaFuncSetAttribute(trees_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)((size_t)kTreeSharedMaxN * 4 + (size_t)(kTreeSharedMaxN / 32) * 4));
     if (e != cudaSuccess) {
         const int rc = cuda_fail(e, "mcbgpu_trees_create");
         trees_free(t);
