@@ -124,3 +124,19 @@ def test_supplier_failure_and_unused_supplier():
     b = Problem.from_graph(z).prepare_with_trees(lambda r: asked.append(1), threads=2, keep_trees=True)
     assert not asked and b.info.trees_supplied == 0
     same_result(a, b)
+
+
+@pytest.mark.parametrize("chunk", [1, 0, 10 ** 6])
+def test_chunk_sizes(chunk):
+    # one root per call, all at once (0), and a chunk larger than the root count
+    g = GRAPHS["random_w1000"]()
+    p, trees, tied = reference_trees(g)
+    calls = []
+
+    def f(roots):
+        calls.append(len(roots))
+        return supplier(trees)(roots)
+    q = Problem.from_graph(g).prepare_with_trees(f, chunk=chunk, threads=4, keep_trees=True)
+    same_result(p, q)
+    assert q.info.trees_supplied == p.F - tied
+    assert sum(calls) == p.F and max(calls) == (1 if chunk == 1 else p.F)
