@@ -33,7 +33,7 @@ TREE_TREES = C.CFUNCTYPE(C.c_int, vp, vp, i32, vp, vp, vp)
 
 
 class MCBHTreeSource(C.Structure):
-    _fields_ = [("ctx", vp), ("begin", TREE_BEGIN), ("trees", TREE_TREES), ("chunk", i32)]
+    _fields_ = [("ctx", vp), ("begin", TREE_BEGIN), ("trees", TREE_TREES), ("chunk", i32), ("trust", i32)]
 
 
 class MCBHInfo(C.Structure):

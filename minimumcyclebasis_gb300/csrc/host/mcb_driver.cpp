@@ -210,7 +210,7 @@ void prepare_job(Job &j, const Outputs &o) {
     if (o.gpu_trees) {
         init_gpu_once();
         GpuTreeSupplier g;
-        mcbh_tree_source src{&g, &GpuTreeSupplier::begin, &GpuTreeSupplier::trees, g.chunk};
+        mcbh_tree_source src{&g, &GpuTreeSupplier::begin, &GpuTreeSupplier::trees, g.chunk, 0};
         const int rc = mcbh_prepare_with_trees(j.p, &opt, &src);
         if (rc == MCBH_E_SUPPLIER) {
             std::fprintf(stderr, "mcb_gb300: GPU trees: %s\n", mcbgpu_last_error());

@@ -603,10 +603,12 @@ bool search_fast(const mcbh_problem &P, u32 src, TreeWorkspace &ws, std::vector<
 // weight is its own, and no slot giving any vertex a shorter path; (2) every parent
 // is the one the reference keeps: the nearest of the vertex's shortest-path
 // neighbours, through that neighbour's first such slot, with no other neighbour as
-// near (otherwise the heap's order decides, and the root is searched here).  Returns
-// false, leaving the workspace to be reinitialised, if a check fails.
+// near (otherwise the heap's order decides, and the root is searched here).  With
+// `structure_only` (a trusted supplier) only the first half of (1) is checked, which
+// is what keeps the later walks up the parent chains finite.  Returns false, leaving
+// the workspace to be reinitialised, if a check fails.
 bool take_given_tree(const mcbh_problem &P, u32 src, TreeWorkspace &ws, const int32_t *dist, const int32_t *pedge,
-                     std::vector<u32> &tree_edges) {
+                     std::vector<u32> &tree_edges, bool structure_only) {
     const Graph &g = P.rg;
     const int n = g.n;
     const int64_t slots = (int64_t)g.slots();
@@ -619,7 +621,7 @@ bool take_given_tree(const mcbh_problem &P, u32 src, TreeWorkspace &ws, const in
         const u32 p = g.rows[o];
         if (dist[p] < 0 || (long long)dist[p] + g.w[o] != (long long)dist[v]) return false;
     }
-    for (int c = 0; c < n; c++) {
+    for (int c = 0; c < n && !structure_only; c++) {
         const int dc = dist[c];
         int bestd = -1;
         bool rival = false;  // another neighbour as near as the best: the heap decides
@@ -703,7 +705,7 @@ struct SearchPolicy {
 void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput &out, bool want_lists,
                   int *tree_parent, u32 *lay_rows, u32 *lay_cols, int *lay_edge, u32 *lay_nodes,
                   SearchChoice &choice, const int32_t *given_dist = nullptr, const int32_t *given_pedge = nullptr,
-                  bool *given_taken = nullptr) {
+                  bool *given_taken = nullptr, bool given_trusted = false) {
     const Graph &g = P.rg;
     const int n = g.n;
     const u32 src = P.fvs_vertices[tidx];
@@ -714,7 +716,7 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
     choice.result = -1;
     if (given_taken) *given_taken = false;
     if (given_dist && given_pedge && P.fast_search_ok && !lay_rows) {
-        if (take_given_tree(P, src, ws, given_dist, given_pedge, tree_edges)) {
+        if (take_given_tree(P, src, ws, given_dist, given_pedge, tree_edges, given_trusted)) {
             fast_done = true;
             choice.try_fast = false;
             if (given_taken) *given_taken = true;
@@ -1105,7 +1107,7 @@ static int prepare_impl(mcbh_problem *P, const mcbh_options *opt, const mcbh_tre
                     process_root(*P, t, wss[(size_t)omp_get_thread_num()], outs[t], lists,
                                  opt->keep_trees ? P->tree_parent.data() : nullptr, nullptr, nullptr, nullptr, nullptr,
                                  choice, offer ? &gd[(size_t)i * n] : nullptr, offer ? &gp[(size_t)i * n] : nullptr,
-                                 &taken);
+                                 &taken, source->trust != 0);
                     if (taken)
                         taken_count.fetch_add(1, std::memory_order_relaxed);
                     else

@@ -224,13 +224,16 @@ class Problem:
         return self
 
     def prepare_with_trees(self, trees, chunk: int = 0, threads: int = 0, keep_trees: bool = False,
-                           ref_layout: bool = False, cycle_lists: bool = True, begin=None) -> "Problem":
+                           ref_layout: bool = False, cycle_lists: bool = True, begin=None,
+                           trust: bool = False) -> "Problem":
         """prepare() with the per-root shortest-path trees taken from `trees(roots)` ->
         (dist int32[count, n], parent_slot int32[count, n], skip uint8[count]) where it
         offers one (mcbh_prepare_with_trees); every offered tree is checked, and a root
         whose tree fails or is skipped is searched on the host, so the result is
         prepare()'s.  `begin(nodes, row_offsets, cols, weights, rev)` (optional) sees
-        the reduced graph first.  info.trees_supplied counts the adopted trees."""
+        the reduced graph first.  info.trees_supplied counts the adopted trees.  With
+        `trust`, only each tree's structure is checked (for a supplier validated
+        against the host's trees)."""
         from ._native import TREE_BEGIN, TREE_TREES, MCBHTreeSource
         state = {}
 
@@ -261,7 +264,7 @@ class Problem:
                 return 1
 
         cb_begin, cb_trees = TREE_BEGIN(c_begin), TREE_TREES(c_trees)
-        src = MCBHTreeSource(None, cb_begin, cb_trees, chunk)
+        src = MCBHTreeSource(None, cb_begin, cb_trees, chunk, int(trust))
         opt = MCBHOptions(threads, 1, int(keep_trees), int(ref_layout), int(cycle_lists))
         check_host(host_lib().mcbh_prepare_with_trees(self._h, C.byref(opt), C.byref(src)), "mcbh_prepare_with_trees")
         self.prepared = True

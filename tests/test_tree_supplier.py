@@ -140,3 +140,25 @@ def test_chunk_sizes(chunk):
     same_result(p, q)
     assert q.info.trees_supplied == p.F - tied
     assert sum(calls) == p.F and max(calls) == (1 if chunk == 1 else p.F)
+
+
+def test_trusted_supplier_skips_only_the_shortest_path_checks():
+    # trust: the reference's trees are adopted (ties included: the rule is not checked),
+    # and trees whose structure is broken are still searched on the host
+    g = GRAPHS["random_w30"]()
+    p, trees, tied = reference_trees(g)
+    assert tied > 0
+    q = Problem.from_graph(g).prepare_with_trees(supplier(trees), chunk=40, threads=2, keep_trees=True, trust=True)
+    same_result(p, q)
+    assert q.info.trees_supplied == p.F
+    roots = sorted(trees)
+    broken = set(roots[::4])
+
+    def corrupt(r, d, ps):
+        if r in broken:
+            v = next(x for x in range(len(d)) if x != r)
+            ps[v] = -1  # a vertex without a parent
+    q2 = Problem.from_graph(g).prepare_with_trees(supplier(trees, corrupt), chunk=40, threads=2, keep_trees=True,
+                                                  trust=True)
+    same_result(p, q2)
+    assert q2.info.trees_supplied == p.F - len(broken)
