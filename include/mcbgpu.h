@@ -98,7 +98,8 @@ int mcbgpu_struct_copy_support_vector(mcbgpu_struct *s, const uint64_t *support_
  * precompute_rows[i] (chunk*n per host row, the layout of
  * compressed_trees::precompute_value).  precompute_rows may be NULL to keep the
  * labels on the device only.  multiple_transfer is accepted for signature parity;
- * trees are always resident. */
+ * trees are always resident.  A tree whose levels end before position n gives
+ * MCBGPU_E_DEVICE, with 0 at the unreached positions. */
 int mcbgpu_struct_process_shortest_path(mcbgpu_struct *s, uint32_t *const *precompute_rows,
                                         int multiple_transfer, float *ms);
 /* gpu_struct::clear_memory (gpu_struct.cu:19-28); also frees the handle. */
@@ -117,7 +118,9 @@ int mcbgpu_struct_clear_memory(mcbgpu_struct *s);
  * first call on a device looks up the array's device address (cudaGetSymbolAddress)
  * and should come before any stream capture.  Calls share the array: calls that
  * overlap on the GPU (other streams, other threads) race.  The call synchronises
- * `stream` to read the kernel's status. */
+ * `stream` to read the kernel's status.  Every position of a tree must lie on one
+ * of its levels (true of every tree of a connected graph): a tree whose levels end
+ * before position `nodes` gives MCBGPU_E_DEVICE, with 0 at the unreached positions. */
 int mcbgpu_label_forest_noalloc(const uint32_t *level_offsets, const uint32_t *parent_pos,
                                 const int32_t *edge_offset, const int32_t *non_tree_edges_map, int num_edges,
                                 const uint64_t *support_vector, int num_coords, int fvs_size, int nodes,

@@ -94,11 +94,12 @@ typedef struct mcbh_tree_source {
     int (*trees)(void *ctx, const uint32_t *roots, int32_t count, int32_t *dist, int32_t *parent_slot,
                  uint8_t *skip);
     int32_t chunk; /* roots per trees call (<= 0: all at once) */
-    int32_t trust; /* nonzero: check only each tree's structure (every parent slot enters
-                      its vertex, distances add up along it), not that it is the tree the
-                      reference's search builds; for a supplier already validated against
-                      the host's trees.  0: the full check, and a result identical to
-                      mcbh_prepare's whatever the supplier returns. */
+    int32_t trust; /* nonzero: check that each tree is a tree of shortest paths (every
+                      parent slot enters its vertex, distances add up along it, no slot
+                      gives a shorter path), not that every parent is the one the
+                      reference's search keeps among equally near ones; for a supplier
+                      already validated against the host's trees.  0: the full check, and
+                      a result identical to mcbh_prepare's whatever the supplier returns. */
 } mcbh_tree_source;
 /* mcbh_prepare with the per-root tree searches taken from `source` where it offers a
  * tree.  Each tree is checked before use (a shortest-path tree whose every parent is

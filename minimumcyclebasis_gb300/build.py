@@ -115,9 +115,12 @@ def build_oracle(force: bool = False) -> str:
     return out
 
 
-def build_reference(ref: str = "/root/reference") -> bool:
-    """oracle/_ref: the reference's own CPU drivers, only where its sources exist."""
-    if not os.path.isdir(os.path.join(ref, "mcb")):
+def build_reference(ref: str | None = None) -> bool:
+    """oracle/_ref: the reference's own CPU drivers, built from the reference checkout
+    at `ref` (default: the MCB_REFERENCE environment variable), only where its sources
+    exist."""
+    ref = ref or os.environ.get("MCB_REFERENCE")
+    if not ref or not os.path.isdir(os.path.join(ref, "mcb")):
         return False
     _run(["make", "-s", "-C", ORACLE, "REF=" + ref, "-j4"])
     return True
@@ -136,5 +139,5 @@ def build_all(force: bool = False) -> dict:
 
 if __name__ == "__main__":
     r = build_all(force="--force" in sys.argv)
-    r["reference"] = build_reference()
+    r["reference"] = build_reference(sys.argv[sys.argv.index("--ref") + 1] if "--ref" in sys.argv else None)
     print(r)

@@ -56,9 +56,11 @@ __global__ void __launch_bounds__(kLabelThreads) label_forest_kernel(
     // level 0: the root (edge offset -1 -> label 0)
     if (threadIdx.x == 0) lab[0] = 0;
     cta_sync();
+    uint32_t covered = 1;  // positions [0, covered) have their labels
     for (int k = 1; k < n; k++) {
         uint32_t beg = R[k], end = R[k + 1];
         if (beg >= end || end > (uint32_t)n) break;
+        covered = end;
         for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
             int eo = E[i];
             uint32_t bit = 0;
@@ -76,8 +78,11 @@ __global__ void __launch_bounds__(kLabelThreads) label_forest_kernel(
         }
         cta_sync();
     }
+    // every position of a tree of a connected graph is on some level; a layout whose
+    // levels end early is flagged, and its unreached positions read 0
+    if (covered < (uint32_t)n && threadIdx.x == 0) atomicOr(status, ST_BAD_INPUT);
     uint32_t *out = labels_out + (size_t)t * n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = lab[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = (uint32_t)i < covered ? lab[i] : 0u;
 }
 
 }  // namespace
@@ -305,9 +310,11 @@ __global__ void __launch_bounds__(kLabelThreads) label_forest_noalloc_kernel(
         const int32_t *E = edge_off + (size_t)t * n;
         if (threadIdx.x == 0) lab[0] = 0;
         cta_sync();
+        uint32_t covered = 1;  // positions [0, covered) have this tree's labels
         for (int k = 1; k < n; k++) {
             const uint32_t beg = R[k], end = R[k + 1];
             if (beg >= end || end > (uint32_t)n) break;
+            covered = end;
             for (uint32_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
                 const int eo = E[i];
                 uint32_t bit = 0;
@@ -325,8 +332,11 @@ __global__ void __launch_bounds__(kLabelThreads) label_forest_noalloc_kernel(
             }
             cta_sync();
         }
+        // the slab keeps the previous tree's labels beyond `covered`: a layout whose
+        // levels end before position n is flagged, and those positions read 0
+        if (covered < (uint32_t)n && threadIdx.x == 0) atomicOr(status, ST_BAD_INPUT);
         uint32_t *out = labels_out + (size_t)t * n;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = lab[i];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = (uint32_t)i < covered ? lab[i] : 0u;
         cta_sync();
     }
 }

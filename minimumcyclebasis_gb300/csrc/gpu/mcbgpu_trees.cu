@@ -128,13 +128,21 @@ __global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
                     const int v = (k << 5) + b;
                     if (vdist[v] >= hi) continue;
                     atomicAnd(&dirty[k], ~(1u << b));
-                    const int dv = vdist[v];  // a later improvement sets the bit again
+                    // pairs with the fence between a writer's atomicMin and atomicOr:
+                    // a bit this atomicAnd cleared was set after its distance was
+                    // lowered, so the read below sees that distance; a later
+                    // improvement sets the bit again
+                    __threadfence_block();
+                    const int dv = vdist[v];
                     for (uint32_t o = a.ro[v]; o < a.ro[v + 1]; o++) {
                         const uint32_t x = a.cols[o];
                         const int nd = dv + a.w[o];
                         if (nd < vdist[x]) {
                             const int old = atomicMin(&dist[x], nd);
-                            if (nd < old) atomicOr(&dirty[x >> 5], 1u << (x & 31));
+                            if (nd < old) {
+                                __threadfence_block();  // the new distance before the dirty bit
+                                atomicOr(&dirty[x >> 5], 1u << (x & 31));
+                            }
                         }
                     }
                 }
@@ -198,6 +206,7 @@ struct mcbgpu_trees {
     uint8_t *d_tied = nullptr;
     unsigned *d_status = nullptr;
     long long bytes = 0;
+    long long diverged_runs = 0;  // runs in which some root did not converge within n + 1 rounds
 };
 
 static void trees_free(mcbgpu_trees *t) {
@@ -350,7 +359,13 @@ int mcbgpu_trees_run(mcbgpu_trees *t, const uint32_t *roots, int32_t count, int3
     unsigned status = 0;
     MCB_CUDA(cudaMemcpyAsync(&status, t->d_status, 4, cudaMemcpyDeviceToHost, st));
     MCB_CUDA(cudaStreamSynchronize(st));
-    (void)status;  // a root that did not converge carries its tie flag; the host searches it itself
+    // a root that did not converge carries its tie flag (the host searches it itself)
+    // and is counted; any other bit is an error
+    if (status & ST_DIVERGED) t->diverged_runs++;
+    if (status & ~(unsigned)ST_DIVERGED) {
+        set_error("mcbgpu_trees_run: kernel status 0x%x", status);
+        return MCBGPU_E_DEVICE;
+    }
     return MCBGPU_OK;
 }
 

@@ -377,6 +377,9 @@ int main(int argc, char **argv) {
     o.plain = plain;
     o.verify = verify;
     o.gpu_trees = gpu_trees;
+    if (bcc && gpu_trees)
+        std::fprintf(stderr, "note: --gpu-trees applies to the single-graph mode; with --bcc the components are "
+                             "prepared on the host\n");
     if (cycles_path && !(o.cycles = std::fopen(cycles_path, "w"))) fail("cannot open the cycle file", cycles_path);
     if (cycles_input_path && !(o.cycles_input = std::fopen(cycles_input_path, "w")))
         fail("cannot open the cycle file", cycles_input_path);

@@ -604,9 +604,11 @@ bool search_fast(const mcbh_problem &P, u32 src, TreeWorkspace &ws, std::vector<
 // is the one the reference keeps: the nearest of the vertex's shortest-path
 // neighbours, through that neighbour's first such slot, with no other neighbour as
 // near (otherwise the heap's order decides, and the root is searched here).  With
-// `structure_only` (a trusted supplier) only the first half of (1) is checked, which
-// is what keeps the later walks up the parent chains finite.  Returns false, leaving
-// the workspace to be reinitialised, if a check fails.
+// `structure_only` (a trusted supplier) the parent rule of (2) is not checked; (1)
+// is, in full: its first half keeps the later walks up the parent chains finite, its
+// second (no slot gives a shorter path) keeps a supplier that stopped short of the
+// true distances from yielding a heavier basis.  Returns false, leaving the
+// workspace to be reinitialised, if a check fails.
 bool take_given_tree(const mcbh_problem &P, u32 src, TreeWorkspace &ws, const int32_t *dist, const int32_t *pedge,
                      std::vector<u32> &tree_edges, bool structure_only) {
     const Graph &g = P.rg;
@@ -620,6 +622,11 @@ bool take_given_tree(const mcbh_problem &P, u32 src, TreeWorkspace &ws, const in
         if (o < 0 || o >= slots || g.cols[o] != (u32)v) return false;
         const u32 p = g.rows[o];
         if (dist[p] < 0 || (long long)dist[p] + g.w[o] != (long long)dist[v]) return false;
+    }
+    for (int c = 0; c < n && structure_only; c++) {
+        const long long dc = dist[c];
+        for (u32 o = g.ro[c]; o < g.ro[c + 1]; o++)
+            if ((long long)dist[g.cols[o]] > dc + g.w[o]) return false;  // a shorter path through c
     }
     for (int c = 0; c < n && !structure_only; c++) {
         const int dc = dist[c];

@@ -232,7 +232,8 @@ class Problem:
         whose tree fails or is skipped is searched on the host, so the result is
         prepare()'s.  `begin(nodes, row_offsets, cols, weights, rev)` (optional) sees
         the reduced graph first.  info.trees_supplied counts the adopted trees.  With
-        `trust`, only each tree's structure is checked (for a supplier validated
+        `trust`, each tree is checked to be a tree of shortest paths but not that its
+        parents are the reference's among equally near ones (for a supplier validated
         against the host's trees)."""
         from ._native import TREE_BEGIN, TREE_TREES, MCBHTreeSource
         state = {}

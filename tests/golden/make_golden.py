@@ -1,8 +1,9 @@
 """Generate the golden vectors under tests/golden/ from the reference itself.
 
-Run in a container where the reference is checked out (default /root/reference):
+Run in a container where the reference is checked out (its path from --ref or the
+MCB_REFERENCE environment variable):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref /path/to/MinimumCycleBasis
 
 It builds oracle/_ref (oracle/Makefile: the reference's own CPU drivers plus
 oracle/ref_dump.cpp, a small driver over the reference's host library), generates
@@ -101,8 +102,10 @@ def sha(a):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("MCB_REFERENCE"))
     a = ap.parse_args()
+    if not a.ref:
+        sys.exit("name the reference checkout with --ref or MCB_REFERENCE")
     build_all()
     if not build_reference(a.ref):
         sys.exit("reference sources not found at %s" % a.ref)

@@ -40,6 +40,38 @@ def test_label_forest_matches_oracle(name, chunk):
     gs.close()
 
 
+def test_label_forest_flags_levels_that_end_early():
+    # tree 1's levels stop after level 1: its deeper positions are on no level, the
+    # call reports bad input and those positions read 0; the other trees are intact
+    from minimumcyclebasis_gb300._native import MCBError
+    fx, p = prep("grid8x8_s3", ref_layout=True)
+    rows, cols, w, rev, ro = p.reduced_graph()
+    _, ec = p.coords()
+    lv, pp, eo, ni = p.ref_layout()
+    n, F = p.n, p.F
+    lv = lv.reshape(F, n + 1).copy()
+    cut = int(lv[1, 2])
+    assert 1 < cut < n
+    lv[1, 2:] = cut
+    gs = GpuStruct(rows.shape[0], p.N, n, F, chunk_size=720)
+    gs.initialize_memory(ec, lv.reshape(-1), pp, eo)
+    gs.copy_support_vector(oracle.support_vector_at(p, 0))
+    out = np.full(F * n, 7, np.uint32)
+    import ctypes as C
+    ptrs = (C.c_void_p * 1)(out.ctypes.data)
+    rc = gs.lib.mcbgpu_struct_process_shortest_path(gs._h, ptrs, 0, None)
+    assert rc != 0 and b"status 0x8" in gs.lib.mcbgpu_last_error()
+    out = out.reshape(F, n)
+    assert (out[1, cut:] == 0).all()
+    want = oracle.labels(p, oracle.support_vector_at(p, 0))
+    NI = ni.reshape(F, n).astype(np.int64)
+    got = np.take_along_axis(out, NI, axis=1)
+    keep = np.ones(F, bool)
+    keep[1] = False
+    assert np.array_equal(got[keep], want[keep].astype(np.uint32))
+    gs.close()
+
+
 @pytest.mark.parametrize("name", golden_names())
 def test_blocked_run_matches_reference(name):
     fx, p = prep(name)

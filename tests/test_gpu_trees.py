@@ -1,19 +1,14 @@
 """GPU shortest-path trees (mcbgpu_trees_*) against the host's: distances equal
 everywhere, the tie flag equal to the rule's, and parent slots equal wherever the
 root has no tie; the shared-memory form (n' <= 53248) and the global one; and the
-host preparation fed by the GPU trees equals prepare().  Run only with
-MCB_RUN_GPU_TREES=1 until the kernel has been run on a GPU."""
-import os
-
+host preparation fed by the GPU trees equals prepare()."""
 import numpy as np
 import pytest
 
 from minimumcyclebasis_gb300 import GpuTrees, Problem, planar_chain_graph, random_graph
 from test_parent_rule import distances_from_parents, rule_parents
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("MCB_RUN_GPU_TREES") != "1",
-                                 reason="GPU tree kernel not yet run on a GPU (MCB_RUN_GPU_TREES=1 runs it)")]
+pytestmark = pytest.mark.gpu
 
 GRAPHS = {
     "random_w1000": lambda: random_graph(600, 1200, 1, 1000, 101),

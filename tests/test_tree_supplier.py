@@ -162,3 +162,51 @@ def test_trusted_supplier_skips_only_the_shortest_path_checks():
                                                   trust=True)
     same_result(p, q2)
     assert q2.info.trees_supplied == p.F - len(broken)
+
+
+def hop_tree(src, rows, cols, w, rev, n):
+    """A breadth-first tree by hop count from `src` (parent slots entering each
+    vertex), with distances summed along its parent chains: a consistent tree that is
+    not, in general, a tree of shortest paths."""
+    ro = np.zeros(n + 1, np.int64)
+    np.add.at(ro, rows.astype(np.int64) + 1, 1)
+    ro = np.cumsum(ro)
+    d = np.full(n, -1, np.int64)
+    pe = np.full(n, -1, np.int64)
+    d[src] = 0
+    frontier = [src]
+    while frontier:
+        nxt = []
+        for x in frontier:
+            for o in range(ro[x], ro[x + 1]):
+                c = int(cols[o])
+                if d[c] < 0:
+                    d[c] = d[x] + int(w[o])
+                    pe[c] = o
+                    nxt.append(c)
+        frontier = nxt
+    return d.astype(np.int32), pe.astype(np.int32)
+
+
+def test_trusted_supplier_still_rejects_trees_that_are_not_shortest():
+    # a supplier that stopped short of the true distances hands over a consistent
+    # tree (distances add up along every parent chain) that is not a shortest-path
+    # tree; even when trusted, such a tree is searched again on the host
+    g = GRAPHS["random_w1000"]()
+    p, trees, _ = reference_trees(g)
+    rows, cols, w, rev, _ = p.reduced_graph()
+    roots = sorted(trees)
+    bad = {}
+    for r in roots[::3]:
+        d, pe = hop_tree(r, rows, cols, w.astype(np.int64), rev, p.n)
+        if not np.array_equal(d, trees[r][0]):
+            bad[r] = (d, pe)
+    assert bad
+
+    def swap(r, d, ps):
+        if r in bad:
+            d[:], ps[:] = bad[r]
+    q = Problem.from_graph(g).prepare_with_trees(supplier(trees, swap), chunk=40, threads=2, keep_trees=True,
+                                                 trust=True)
+    same_result(p, q)
+    assert q.info.trees_supplied == p.F - len(bad)
