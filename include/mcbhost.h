@@ -53,6 +53,10 @@ typedef struct mcbh_options {
     int keep_trees;       /* keep per-tree vertex-indexed parent edge offsets (F x n int32) */
     int ref_layout;       /* build the reference's level-ordered GPU layout (4 arrays of F x n) */
     int cycle_lists;      /* build per-candidate sorted coordinate lists */
+    int structure_only;   /* 1: stop after the spanning tree (chain contraction, FVS, coordinates):
+                             no per-root trees and no candidates here; they come from a device
+                             candidate generation through mcbh_search_trees (for the roots it
+                             leaves to the host) and mcbh_rank_candidates */
 } mcbh_options;
 
 typedef struct mcbh_info {
@@ -110,6 +114,29 @@ typedef struct mcbh_tree_source {
  * layout follows the heap's settle order).  info.trees_supplied counts the adopted
  * trees. */
 int mcbh_prepare_with_trees(mcbh_problem *p, const mcbh_options *opt, const mcbh_tree_source *source);
+/* ---- the host half of a device candidate generation ------------------------ */
+/* After mcbh_prepare with structure_only = 1.  The reference's per-root tree
+ * searches (include/Dijkstra.h:78-124, the heap order deciding ties) for the FVS
+ * indices trees[0..count): every vertex's distance and parent slot (count x n', -1
+ * at the root), OpenMP over roots.  For the roots a device search leaves to the host
+ * (two equally near shortest-path parents somewhere in the tree). */
+int mcbh_search_trees(const mcbh_problem *p, const int32_t *trees, int32_t count, int threads, int32_t *dist,
+                      int32_t *parent_slot);
+/* The lower slot of every reverse-slot pair of the reduced graph in ascending order
+ * (m' entries): pair k joins rows[pair_slot[k]] and cols[pair_slot[k]].  The order in
+ * which the reference's non-tree-edge scan meets the pairs (include/Dijkstra.h:129-149),
+ * which is each root's candidate insertion order. */
+int mcbh_get_pairs(const mcbh_problem *p, uint32_t *pair_slot);
+/* The rank order of candidates found elsewhere (a device candidate test): for FVS
+ * index t, its accepted pairs pair_index[tree_offsets[t] .. tree_offsets[t+1]) in
+ * ascending pair order, with their cycle weights.  Builds each root's group map with
+ * the reference's key and insertion sequence (include/cycle_searcher.h:23-61), walks
+ * the roots in vertex-id order and sorts on weight alone with std::sort's permutation
+ * (mcb/mcb_cycle_deg_two_remove.cpp:244-258): mcbh_get_candidates then returns the
+ * list mcbh_prepare gives for the same candidates.  No coordinate lists (cycle_nnz = 0;
+ * the device builds them).  Once per problem, after a structure_only preparation. */
+int mcbh_rank_candidates(mcbh_problem *p, const int64_t *tree_offsets, const uint32_t *pair_index,
+                         const int32_t *weight, int threads);
 /* mcbh_prepare on `count` independent problems (the components of a biconnected
  * split, the graphs of a batch), in parallel over problems with one thread each,
  * largest first; opt->threads is the number of problems prepared at once (<=0:

@@ -25,7 +25,7 @@ class KernelStat(C.Structure):
 
 class MCBHOptions(C.Structure):
     _fields_ = [("threads", C.c_int), ("contract_chains", C.c_int), ("keep_trees", C.c_int),
-                ("ref_layout", C.c_int), ("cycle_lists", C.c_int)]
+                ("ref_layout", C.c_int), ("cycle_lists", C.c_int), ("structure_only", C.c_int)]
 
 
 TREE_BEGIN = C.CFUNCTYPE(C.c_int, vp, i32, i64, vp, vp, vp, vp)
@@ -52,6 +52,9 @@ HOST_SYMBOLS = {
     "mcbh_prepare_many": (C.c_int, [vp, i64, C.POINTER(MCBHOptions), vp]),
     "mcbh_gf2_rank": (C.c_int, [vp, vp, i64, C.c_int, C.POINTER(i64)]),
     "mcbh_prepare_with_trees": (C.c_int, [vp, C.POINTER(MCBHOptions), vp]),
+    "mcbh_search_trees": (C.c_int, [vp, vp, i32, C.c_int, vp, vp]),
+    "mcbh_get_pairs": (C.c_int, [vp, vp]),
+    "mcbh_rank_candidates": (C.c_int, [vp, vp, vp, vp, C.c_int]),
     "mcbh_problem_free": (None, [vp]),
     "mcbh_get_info": (C.c_int, [vp, C.POINTER(MCBHInfo)]),
     "mcbh_get_reduced_graph": (C.c_int, [vp, vp, vp, vp, vp, vp]),

@@ -14,6 +14,7 @@
 // that visit edges in the same order (the reference needs `ulimit -s unlimited`).
 #include "mcbhost.h"
 #include "dist_heap.h"
+#include "weight_sort.h"
 
 #include <algorithm>
 #include <atomic>
@@ -121,6 +122,8 @@ struct mcbh_problem {
     };
     std::vector<Arc> arcs;
     bool fast_search_ok = false;  // every weight >= 1 and no distance can overflow
+    bool structure_only = false;  // prepared up to the spanning tree; candidates from mcbh_rank_candidates
+    bool ranked = false;          // mcbh_rank_candidates has filled the candidate arrays
     // trees
     std::vector<int> tree_parent;  // F x n'
     std::vector<u32> lay_rows, lay_cols, lay_nodes;
@@ -476,6 +479,19 @@ struct RootOutput {
         std::make_unique<std::pmr::monotonic_buffer_resource>();
     std::pmr::unordered_map<unsigned long long, std::pair<int, int>> groups{arena.get()};
     std::vector<int> next;
+
+    // candidate `local` (just appended to cands) joins the group of its vertex pair
+    void group(int local, u32 a, u32 b) {
+        next.push_back(-1);
+        const unsigned long long key = ((unsigned long long)std::min(a, b) << 32) | std::max(a, b);
+        auto it = groups.find(key);
+        if (it == groups.end()) {
+            groups.insert(std::make_pair(key, std::make_pair(local, local)));
+        } else {
+            next[it->second.second] = local;
+            it->second.second = local;
+        }
+    }
 };
 
 // One vertex of a tree search: distance, parent vertex, slot into it from the
@@ -707,6 +723,106 @@ struct SearchPolicy {
     }
 };
 
+// The slot pairs and the search records of the reduced graph, built once before the
+// per-root trees (pairs: the lower slot of every reverse pair in ascending order, the
+// order in which the reference's non-tree-edge scan meets them).
+void setup_searches(mcbh_problem &P) {
+    const Graph &g = P.rg;
+    P.pair_first.clear();
+    P.pair_first.reserve(g.slots() / 2);
+    P.pair_ends.clear();
+    P.pair_ends.reserve(g.slots() / 2);
+    P.slot_pair.assign(g.slots(), 0);
+    P.arcs.resize(g.slots());
+    long long wmin = 1, wmax = 0;
+    for (size_t i = 0; i < g.slots(); i++) {
+        P.arcs[i] = {g.cols[i], g.w[i]};
+        wmin = std::min(wmin, (long long)g.w[i]);
+        wmax = std::max(wmax, (long long)g.w[i]);
+    }
+    P.fast_search_ok = wmin >= 1 && wmax * (long long)(g.n + 1) < 0x7fffffffLL;
+    for (size_t i = 0; i < g.slots(); i++) {
+        if (i < g.rev[i]) {
+            P.slot_pair[i] = P.slot_pair[g.rev[i]] = (u32)P.pair_first.size();
+            P.pair_first.push_back((u32)i);
+            P.pair_ends.push_back(std::make_pair(g.rows[i], g.cols[i]));
+        }
+    }
+}
+
+// mcb/mcb_cycle_deg_two_remove.cpp:244-258: the candidates of every root (outs[t]
+// for FVS index t, with its group map) into the rank order: roots in vertex-id
+// order, each root's map in iteration order, each group in insertion order; then an
+// unstable std::sort on total_length alone.  Fills the problem's candidate arrays
+// and, with `lists`, its coordinate lists.
+int collect_candidates(mcbh_problem *P, std::vector<RootOutput> &outs, bool lists, int threads) {
+    mcbh_info &I = P->info;
+    const int n = P->rg.n;
+    struct Item {
+        int weight;
+        int tree;
+        int local;
+        int len;
+    };
+    // the list in that order, each root's part filled in parallel
+    std::vector<int> root_of_rank;  // FVS roots in vertex-id order
+    for (int vtx = 0; vtx < n; vtx++)
+        if (P->fvs_array[vtx] >= 0) root_of_rank.push_back(P->fvs_array[vtx]);
+    std::vector<size_t> base(root_of_rank.size() + 1, 0);
+    for (size_t i = 0; i < root_of_rank.size(); i++) base[i + 1] = base[i] + outs[root_of_rank[i]].cands.size();
+    const size_t K = base.back();
+    if (K > 0xffffffffull) return MCBH_E_NOMEM;  // past the 32-bit index of the sort records
+    std::vector<Item> items(K);
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+    for (int64_t i = 0; i < (int64_t)root_of_rank.size(); i++) {
+        const int t = root_of_rank[i];
+        const RootOutput &o = outs[t];
+        size_t k = base[i];
+        for (auto it = o.groups.begin(); it != o.groups.end(); ++it)
+            for (int loc = it->second.first; loc >= 0; loc = o.next[loc])
+                items[k++] = {o.cands[loc].weight, t, loc, o.cands[loc].coord_len};
+    }
+    // std::sort on the weight alone: its permutation follows from the outcomes of
+    // its comparisons, so sorting (weight, index) records gives the permutation
+    // that sorting the candidates themselves gives; weight_sort gives that
+    // permutation with the independent sub-ranges sorted in parallel
+    std::vector<WeightKey> keys(K);
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t r = 0; r < (int64_t)K; r++) keys[r] = {items[r].weight, (u32)r};
+    weight_sort(keys.data(), K, threads);
+    P->c_root.resize(K);
+    P->c_edge.resize(K);
+    P->c_weight.resize(K);
+    P->c_tree.resize(K);
+    int64_t nnz = 0;
+    if (lists) {
+        P->c_off.resize(K + 1);
+        P->c_off[0] = 0;
+#pragma omp parallel for num_threads(threads) schedule(static)
+        for (int64_t r = 0; r < (int64_t)K; r++) P->c_off[r + 1] = items[keys[r].index].len;
+        for (size_t r = 0; r < K; r++) {
+            nnz += P->c_off[r + 1];
+            P->c_off[r + 1] = nnz;
+        }
+        P->c_coords.resize((size_t)nnz);
+    }
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (int64_t r = 0; r < (int64_t)K; r++) {
+        const Item &it = items[keys[r].index];
+        const LocalCandidate &lc = outs[it.tree].cands[it.local];
+        P->c_root[r] = (int)P->fvs_vertices[it.tree];
+        P->c_edge[r] = lc.edge;
+        P->c_weight[r] = lc.weight;
+        P->c_tree[r] = it.tree;
+        if (lists)
+            std::memcpy(&P->c_coords[P->c_off[r]], &outs[it.tree].coords[lc.coord_begin],
+                        sizeof(int) * (size_t)lc.coord_len);
+    }
+    I.num_candidates = (int64_t)K;
+    I.cycle_nnz = nnz;
+    return MCBH_OK;
+}
+
 // given_dist / given_pedge: a supplied tree for this root (or null), adopted after
 // take_given_tree's checks; *given_taken says whether it was.
 void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput &out, bool want_lists,
@@ -815,17 +931,9 @@ void process_root(const mcbh_problem &P, int tidx, TreeWorkspace &ws, RootOutput
             std::sort(out.coords.begin() + b0, out.coords.end());
             lc.coord_len = (int)(out.coords.size() - b0);
         }
-        int local = (int)out.cands.size();
+        const int local = (int)out.cands.size();
         out.cands.push_back(lc);
-        out.next.push_back(-1);
-        unsigned long long key = ((unsigned long long)std::min(a, b) << 32) | std::max(a, b);
-        auto it = out.groups.find(key);
-        if (it == out.groups.end()) {
-            out.groups.insert(std::make_pair(key, std::make_pair(local, local)));
-        } else {
-            out.next[it->second.second] = local;
-            it->second.second = local;
-        }
+        out.group(local, a, b);
     }
     if (tree_parent) {
         int *tp = tree_parent + (size_t)tidx * n;
@@ -1048,6 +1156,14 @@ static int prepare_impl(mcbh_problem *P, const mcbh_options *opt, const mcbh_tre
         I.num_coords = (int)P->coord_edges.size();
         I.t_spanning = now_s() - t0;
 
+        setup_searches(*P);
+        if (opt->structure_only) {
+            // stop before the per-root trees: the candidates come from
+            // mcbh_rank_candidates (a device candidate generation)
+            P->structure_only = true;
+            P->prepared = true;
+            return MCBH_OK;
+        }
         t0 = now_s();
         const int F = I.fvs_size;
         const int n = P->rg.n;
@@ -1057,29 +1173,6 @@ static int prepare_impl(mcbh_problem *P, const mcbh_options *opt, const mcbh_tre
             P->lay_cols.assign((size_t)F * n, 0);
             P->lay_edge.assign((size_t)F * n, -1);
             P->lay_nodes.assign((size_t)F * n, 0);
-        }
-        {
-            const Graph &g = P->rg;
-            P->pair_first.clear();
-            P->pair_first.reserve(g.slots() / 2);
-            P->pair_ends.clear();
-            P->pair_ends.reserve(g.slots() / 2);
-            P->slot_pair.assign(g.slots(), 0);
-            P->arcs.resize(g.slots());
-            long long wmin = 1, wmax = 0;
-            for (size_t i = 0; i < g.slots(); i++) {
-                P->arcs[i] = {g.cols[i], g.w[i]};
-                wmin = std::min(wmin, (long long)g.w[i]);
-                wmax = std::max(wmax, (long long)g.w[i]);
-            }
-            P->fast_search_ok = wmin >= 1 && wmax * (long long)(g.n + 1) < 0x7fffffffLL;
-            for (size_t i = 0; i < g.slots(); i++) {
-                if (i < g.rev[i]) {
-                    P->slot_pair[i] = P->slot_pair[g.rev[i]] = (u32)P->pair_first.size();
-                    P->pair_first.push_back((u32)i);
-                    P->pair_ends.push_back(std::make_pair(g.rows[i], g.cols[i]));
-                }
-            }
         }
         std::vector<RootOutput> outs(F);
         int threads = opt->threads > 0 ? opt->threads : omp_get_max_threads();
@@ -1142,74 +1235,8 @@ static int prepare_impl(mcbh_problem *P, const mcbh_options *opt, const mcbh_tre
         I.t_trees = now_s() - t0;
 
         t0 = now_s();
-        // mcb/mcb_cycle_deg_two_remove.cpp:244-258: roots in vertex-id order, each
-        // root's map in iteration order, each group in insertion order; then an
-        // unstable std::sort on total_length alone.
-        struct Item {
-            int weight;
-            int tree;
-            int local;
-            int len;
-        };
-        // the list in that order, each root's part filled in parallel
-        std::vector<int> root_of_rank;  // FVS roots in vertex-id order
-        for (int vtx = 0; vtx < n; vtx++)
-            if (P->fvs_array[vtx] >= 0) root_of_rank.push_back(P->fvs_array[vtx]);
-        std::vector<size_t> base(root_of_rank.size() + 1, 0);
-        for (size_t i = 0; i < root_of_rank.size(); i++) base[i + 1] = base[i] + outs[root_of_rank[i]].cands.size();
-        const size_t K = base.back();
-        if (K > 0xffffffffull) return MCBH_E_NOMEM;  // past the 32-bit index of the sort records
-        std::vector<Item> items(K);
-#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
-        for (int64_t i = 0; i < (int64_t)root_of_rank.size(); i++) {
-            const int t = root_of_rank[i];
-            const RootOutput &o = outs[t];
-            size_t k = base[i];
-            for (auto it = o.groups.begin(); it != o.groups.end(); ++it)
-                for (int loc = it->second.first; loc >= 0; loc = o.next[loc])
-                    items[k++] = {o.cands[loc].weight, t, loc, o.cands[loc].coord_len};
-        }
-        // std::sort on the weight alone: its permutation follows from the outcomes of
-        // its comparisons, so sorting (weight, index) records gives the permutation
-        // that sorting the candidates themselves gives
-        struct Key {
-            int weight;
-            u32 index;
-        };
-        std::vector<Key> keys(K);
-#pragma omp parallel for num_threads(threads) schedule(static)
-        for (int64_t r = 0; r < (int64_t)K; r++) keys[r] = {items[r].weight, (u32)r};
-        std::sort(keys.begin(), keys.end(), [](const Key &a, const Key &b) { return a.weight < b.weight; });
-        P->c_root.resize(K);
-        P->c_edge.resize(K);
-        P->c_weight.resize(K);
-        P->c_tree.resize(K);
-        int64_t nnz = 0;
-        if (lists) {
-            P->c_off.resize(K + 1);
-            P->c_off[0] = 0;
-#pragma omp parallel for num_threads(threads) schedule(static)
-            for (int64_t r = 0; r < (int64_t)K; r++) P->c_off[r + 1] = items[keys[r].index].len;
-            for (size_t r = 0; r < K; r++) {
-                nnz += P->c_off[r + 1];
-                P->c_off[r + 1] = nnz;
-            }
-            P->c_coords.resize((size_t)nnz);
-        }
-#pragma omp parallel for num_threads(threads) schedule(static)
-        for (int64_t r = 0; r < (int64_t)K; r++) {
-            const Item &it = items[keys[r].index];
-            const LocalCandidate &lc = outs[it.tree].cands[it.local];
-            P->c_root[r] = (int)P->fvs_vertices[it.tree];
-            P->c_edge[r] = lc.edge;
-            P->c_weight[r] = lc.weight;
-            P->c_tree[r] = it.tree;
-            if (lists)
-                std::memcpy(&P->c_coords[P->c_off[r]], &outs[it.tree].coords[lc.coord_begin],
-                            sizeof(int) * (size_t)lc.coord_len);
-        }
-        I.num_candidates = (int64_t)K;
-        I.cycle_nnz = nnz;
+        const int rc = collect_candidates(P, outs, lists, threads);
+        if (rc != MCBH_OK) return rc;
         I.t_collect = now_s() - t0;
     } catch (const std::bad_alloc &) {
         return MCBH_E_NOMEM;
@@ -1223,6 +1250,99 @@ int mcbh_prepare(mcbh_problem *P, const mcbh_options *opt) { return prepare_impl
 int mcbh_prepare_with_trees(mcbh_problem *P, const mcbh_options *opt, const mcbh_tree_source *source) {
     if (!source || !source->trees) return MCBH_E_ARG;
     return prepare_impl(P, opt, source);
+}
+
+int mcbh_search_trees(const mcbh_problem *P, const int32_t *trees, int32_t count, int threads, int32_t *dist,
+                      int32_t *parent_slot) {
+    if (!P || count < 0 || (count > 0 && (!trees || !dist || !parent_slot))) return MCBH_E_ARG;
+    if (!P->prepared || P->single_cycle || P->arcs.empty()) return MCBH_E_STATE;
+    const int F = (int)P->fvs_vertices.size();
+    for (int32_t i = 0; i < count; i++)
+        if (trees[i] < 0 || trees[i] >= F) return MCBH_E_ARG;
+    const int n = P->rg.n;
+    if (threads <= 0) threads = omp_get_max_threads();
+    try {
+#pragma omp parallel num_threads(threads)
+        {
+            TreeWorkspace ws;
+            std::vector<u32> tree_edges;
+#pragma omp for schedule(dynamic, 1)
+            for (int32_t i = 0; i < count; i++) {
+                const u32 src = P->fvs_vertices[(size_t)trees[i]];
+                ws.init(n, 0);
+                tree_edges.clear();
+                if (P->fast_search_ok)
+                    search_exact<true>(*P, src, ws, tree_edges);
+                else
+                    search_exact<false>(*P, src, ws, tree_edges);
+                int32_t *d = dist + (size_t)i * n, *ps = parent_slot + (size_t)i * n;
+                for (int v = 0; v < n; v++) {
+                    d[v] = ws.vs[v].dist;
+                    ps[v] = (u32)v == src ? -1 : ws.vs[v].pedge;
+                }
+            }
+        }
+    } catch (const std::bad_alloc &) {
+        return MCBH_E_NOMEM;
+    }
+    return MCBH_OK;
+}
+
+int mcbh_get_pairs(const mcbh_problem *P, uint32_t *pair_slot) {
+    if (!P || !pair_slot) return MCBH_E_ARG;
+    if (!P->prepared || P->single_cycle || P->pair_first.size() * 2 != P->rg.slots()) return MCBH_E_STATE;
+    std::memcpy(pair_slot, P->pair_first.data(), sizeof(uint32_t) * P->pair_first.size());
+    return MCBH_OK;
+}
+
+int mcbh_rank_candidates(mcbh_problem *P, const int64_t *tree_offsets, const uint32_t *pair_index,
+                         const int32_t *weight, int threads) {
+    if (!P || !tree_offsets) return MCBH_E_ARG;
+    if (!P->prepared || !P->structure_only || P->ranked) return MCBH_E_STATE;
+    const int F = (int)P->fvs_vertices.size();
+    const int64_t total = tree_offsets[F];
+    if (tree_offsets[0] != 0 || total < 0 || (total > 0 && (!pair_index || !weight))) return MCBH_E_ARG;
+    for (int t = 0; t < F; t++)
+        if (tree_offsets[t + 1] < tree_offsets[t]) return MCBH_E_ARG;
+    const int64_t npairs = (int64_t)P->pair_first.size();
+    if (threads <= 0) threads = omp_get_max_threads();
+    const double t0 = now_s();
+    try {
+        std::vector<RootOutput> outs((size_t)F);
+        std::atomic<int> bad{0};
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+        for (int t = 0; t < F; t++) {
+            RootOutput &o = outs[(size_t)t];
+            const int64_t b = tree_offsets[t], e = tree_offsets[t + 1];
+            o.cands.reserve((size_t)(e - b));
+            o.next.reserve((size_t)(e - b));
+            int64_t prev = -1;
+            for (int64_t i = b; i < e; i++) {
+                const int64_t k = pair_index[i];
+                if (k <= prev || k >= npairs) {  // each root's pairs ascending, in range
+                    bad.store(1, std::memory_order_relaxed);
+                    break;
+                }
+                prev = k;
+                LocalCandidate lc;
+                lc.edge = (int)P->pair_first[(size_t)k];
+                lc.weight = weight[i];
+                lc.coord_begin = 0;
+                lc.coord_len = 0;
+                const int local = (int)o.cands.size();
+                o.cands.push_back(lc);
+                o.group(local, P->pair_ends[(size_t)k].first, P->pair_ends[(size_t)k].second);
+            }
+        }
+        if (bad.load()) return MCBH_E_ARG;
+        const int rc = collect_candidates(P, outs, false, threads);
+        if (rc != MCBH_OK) return rc;
+    } catch (const std::bad_alloc &) {
+        return MCBH_E_NOMEM;
+    }
+    P->ranked = true;
+    P->info.t_collect = now_s() - t0;
+    return MCBH_OK;
 }
 
 int mcbh_prepare_many(mcbh_problem **ps, int64_t count, const mcbh_options *opt, int32_t *status) {

@@ -216,11 +216,48 @@ class Problem:
             self._h = None
 
     def prepare(self, threads: int = 0, contract_chains: bool = True, keep_trees: bool = False,
-                ref_layout: bool = False, cycle_lists: bool = True) -> "Problem":
-        opt = MCBHOptions(threads, int(contract_chains), int(keep_trees), int(ref_layout), int(cycle_lists))
+                ref_layout: bool = False, cycle_lists: bool = True, structure_only: bool = False) -> "Problem":
+        """The driver's steps before its main loop (mcbh_prepare).  With
+        `structure_only`, only up to the spanning tree: the candidates then come from a
+        device generation (search_trees for the roots it leaves to the host, then
+        rank_candidates)."""
+        opt = MCBHOptions(threads, int(contract_chains), int(keep_trees), int(ref_layout), int(cycle_lists),
+                          int(structure_only))
         check_host(host_lib().mcbh_prepare(self._h, C.byref(opt)), "mcbh_prepare")
         self.prepared = True
         self._opts = opt
+        return self
+
+    def search_trees(self, trees, threads: int = 0):
+        """The reference's heap-ordered tree searches for FVS indices `trees`:
+        (dist int32[count, n], parent_slot int32[count, n]) (mcbh_search_trees)."""
+        t = np.ascontiguousarray(trees, np.int32)
+        n = self.n
+        dist = np.empty((max(len(t), 1), n), np.int32)
+        ps = np.empty((max(len(t), 1), n), np.int32)
+        check_host(host_lib().mcbh_search_trees(self._h, ptr(t), len(t), threads, ptr(dist), ptr(ps)),
+                   "mcbh_search_trees")
+        return dist[:len(t)], ps[:len(t)]
+
+    def pairs(self) -> np.ndarray:
+        """The lower slot of every reverse-slot pair, ascending (mcbh_get_pairs)."""
+        def f():
+            out = np.empty(self.info.reduced_edges2 // 2, np.uint32)
+            check_host(host_lib().mcbh_get_pairs(self._h, ptr(out)), "mcbh_get_pairs")
+            return out
+        return self._get("pairs", f)
+
+    def rank_candidates(self, tree_offsets, pair_index, weight, threads: int = 0) -> "Problem":
+        """The rank order of externally found candidates (mcbh_rank_candidates): per
+        FVS index t, its accepted pairs pair_index[tree_offsets[t]:tree_offsets[t+1]]
+        (ascending) and their weights.  Afterwards candidates() is what prepare()
+        gives for the same candidates."""
+        to = np.ascontiguousarray(tree_offsets, np.int64)
+        pi = np.ascontiguousarray(pair_index, np.uint32)
+        w = np.ascontiguousarray(weight, np.int32)
+        check_host(host_lib().mcbh_rank_candidates(self._h, ptr(to), ptr(pi), ptr(w), threads),
+                   "mcbh_rank_candidates")
+        self._cache.pop("cands", None)
         return self
 
     def prepare_with_trees(self, trees, chunk: int = 0, threads: int = 0, keep_trees: bool = False,
