@@ -1,27 +1,39 @@
 #!/usr/bin/env python3
 """Benchmark of the de Pina minimum-cycle-basis hot path on GB300.
 
-Workload (the plain-GPU configuration): a connected random sparse graph with
-50,000 vertices and 100,000 edges (random spanning tree by random-permutation
-attach plus uniform extra edges), int32 weights U[1,1000], seed 1 — synthetic,
-generated by the repository's seeded generator.  Host preparation (chain
-contraction, FVS, shortest-path trees, candidate ranking) is done once, untimed.
+Default workload (the scale configuration): a 1M-vertex planar-like graph, 263,000
+triangulated grid points with 30% of the edges deleted (connectivity kept) and every
+kept edge subdivided with probability 0.3 into a chain of 1-8 vertices, int32
+weights U[1,1000], seed 1 (1,005,883 vertices; 241,787 after chain contraction;
+N = 288,051 coordinates, S = 10.4 GB) - synthetic, from the repository's seeded
+generator.  `--graph random --n 50000` is the 50k-vertex plain-GPU configuration.
 
-One step = one complete de Pina solve (all N = m - n + 1 iterations) on the GPU:
-reset S to the unit vectors, then the blocked device loop.  Inputs (the rank-ordered
-candidates and their cycle-coordinate lists, 1.5 GB) stay resident in HBM; they are
-larger than the 129 MB L2, so no flush is needed between steps.
+Preparation (chain contraction, FVS and spanning tree on the host; per-root trees,
+candidate test and coordinate lists on the GPU; ranking on the host) is timed once
+as part of the graph-to-basis time (`e2e_with_preparation`).
+
+One step = one complete de Pina solve (all N iterations) on the GPU: reset S to the
+unit vectors, then the blocked device loop.  The rank-ordered candidates and their
+coordinate lists stay resident in HBM (7.7 GB at the default size, larger than the
+129 MB L2, so no flush is needed between steps).
 
   value       mean seconds per solve (CUDA events on the solver's stream)
+  plain_gpu   the per-iteration device form (one odd-candidate search and one update
+              per iteration, the reference loop's shape) timed on windows of
+              iterations spread over the solve (each reached by the blocked run),
+              integrated over all N iterations
   e2e         seconds per solve through the C ABI with pinned host buffers: upload
               (H2D of weights, offsets, coordinates) + solve + results (D2H)
+  e2e_with_preparation  seconds from the graph's edge arrays in host memory to the
+              basis: preparation + solve + results, once
   roofline    the kernel class with the largest time share, algorithmic bytes per
               launch / mean event-timed launch duration vs the measured HBM peak;
               the launch durations come from a second pass of the same K solves
-              with an event pair around every launch (the per-launch events cost
-              about 5% and stay out of the timed region)
+              with an event pair around every launch (out of the timed region)
   cpu_baseline  the reference's CPU main loop (oracle port of mcb/mcb_non_cpu_rd.cpp)
-              on this host's cores over the first P iterations, extrapolated to N
+              on this host's cores: a label pass over a sample of the FVS trees
+              and the full-width update over a sample of rows, extrapolated to the
+              whole solve (N label passes over all F trees, N(N-1)/2 row updates)
 
 `--workload batch` measures the batched configuration instead: --batch-count graphs
 (n log-uniform in [50, 5000], average degree U[2.5, 5], w U[1, 255]) solved in one
@@ -49,6 +61,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MCB solve time (s) & search HBM GB/s: batched+learned vs plain GPU, exact"
+# total basis weights of the seeded workloads (graph family, --n, --seed): the
+# blocked solver's result, equal to the per-iteration form's on the same candidates
+PINNED_WEIGHTS = {("planar", 263000, 1): 1008336977, ("random", 50000, 1): 180590671}
+DEFAULT_N = {"planar": 263000, "random": 50000, "rgg": 20000}
 BATCH_WORKLOAD = ("batched: %d random graphs, n log-uniform [50,5000], avg degree U[2.5,5], w U[1,255], seed %d; "
                   "one batched solve of all of them")
 
@@ -157,17 +173,6 @@ def make_graph(args):
     return random_graph(args.n, 2 * args.n, 1, 1000, args.seed)
 
 
-def prepare(args, keep_trees):
-    from minimumcyclebasis_gb300 import Problem
-    t0 = time.time()
-    g = make_graph(args)
-    p = Problem.from_graph(g).prepare(threads=0, keep_trees=keep_trees)
-    i = p.info
-    log("prepared in %.1fs: n'=%d F=%d N=%d K=%d nnz=%d" % (time.time() - t0, i.reduced_nodes, i.fvs_size,
-                                                             i.num_coords, i.num_candidates, i.cycle_nnz))
-    return p
-
-
 def config_of(p, args, extra=None):
     i = p.info
     names = {"random": "random sparse graph n=%d m=%d (avg degree 4), int32 w U[1,1000], seed %d"
@@ -178,27 +183,40 @@ def config_of(p, args, extra=None):
                        "chains of 1-8, w U[1,1000], seed %d" % (args.n, args.seed)}
     c = {"workload": names[args.graph] + "; full de Pina solve", "input_nodes": i.nodes,
          "reduced_nodes": i.reduced_nodes, "fvs": i.fvs_size, "N": i.num_coords, "K": i.num_candidates,
-         "cycle_nnz": i.cycle_nnz, "form": args.mode,
-         "l2": ("inputs (cycle lists %.2f GB) larger than the 129 MB L2; no flush" % (i.cycle_nnz * 4 / 1e9))
-         if i.cycle_nnz * 4 > 129e6 else "small case: inputs fit in L2",
-         "host_preparation_s": round(i.t_reduce + i.t_fvs + i.t_spanning + i.t_trees + i.t_collect, 3),
-         "host_threads": os.cpu_count()}
+         "form": args.mode, "host_threads": os.cpu_count()}
     if extra:
         c.update(extra)
     return c
 
 
-def cpu_baseline(p, iters, threads):
+def cpu_baseline(p, args, threads):
+    """The reference CPU main loop's cost on this host, from samples: a label pass
+    (worker_thread::precompute_supportVec, the loop's per-iteration relabelling of
+    every FVS tree) over `--cpu-sample-roots` trees spread over the FVS, and the
+    full-width dot/XOR update over 2048 rows; extrapolated to N passes over all F
+    trees and N(N-1)/2 row updates.  The list scan, which stops at the first odd
+    candidate, is left out, so this is a lower bound of the loop's time."""
+    import numpy as np
+
     import oracle
     threads = threads or os.cpu_count() or 1
-    sel, _, sec = oracle.solve(p, threads=threads, max_iter=iters)
-    n = p.N
-    done = len(sel)
-    value = sec / max(done, 1) * n
+    F, n, N = p.F, p.n, p.N
+    step = max(1, F // max(1, args.cpu_sample_roots))
+    idx = np.arange(0, F, step, dtype=np.int32)[:args.cpu_sample_roots]
+    t0 = time.perf_counter()
+    _, ps = p.search_trees(idx, threads=threads)
+    t_trees = time.perf_counter() - t0
+    lab = oracle.label_pass_seconds(p, ps, passes=3, threads=threads)
+    row = oracle.update_row_seconds(N, rows=2048, passes=3, threads=threads)
+    label_total = lab * F / len(idx) * N
+    update_total = row * N * (N - 1) / 2.0
+    value = label_total + update_total
     return {"value": value, "unit": "s", "cores": threads, "kind": "port",
-            "sample": "first %d of %d de Pina iterations of the reference CPU main loop (oracle port of "
-                      "mcb/mcb_non_cpu_rd.cpp:264-342), %.2f s, extrapolated x%d/%d (per-iteration label "
-                      "precompute over all FVS trees dominates and is constant)" % (done, n, sec, n, done)}
+            "sample": "reference CPU main loop (oracle port of mcb/mcb_non_cpu_rd.cpp:264-342) from samples: a label "
+                      "pass over %d of the %d FVS trees %.4f s (x %d/%d trees x %d iterations = %.4g s), the "
+                      "full-width update %.3g s per row (x N(N-1)/2 = %.4g s); list scan omitted (a lower bound); "
+                      "the sampled trees searched on the host in %.1f s, untimed"
+                      % (len(idx), F, lab, F, len(idx), N, label_total, row, update_total, t_trees)}
 
 
 def label_cost(info):
@@ -289,14 +307,17 @@ def run_reference(args, world, rank, pg):
         return None
     if args.workload == "batch":
         return run_reference_batch(args, world, rank, pg)
-    p = prepare(args, keep_trees=True)
+    from minimumcyclebasis_gb300 import Problem
     threads = args.cpu_threads or os.cpu_count() or 1
+    t0 = time.time()
+    p = Problem.from_graph(make_graph(args)).prepare(threads=threads, structure_only=True)
+    log("structure prepared in %.1fs: n'=%d F=%d N=%d" % (time.time() - t0, p.n, p.F, p.N))
     for _ in range(args.warmup):
-        cpu_baseline(p, max(2, args.cpu_iters // 8), threads)
+        cpu_baseline(p, argparse.Namespace(cpu_sample_roots=max(16, args.cpu_sample_roots // 8)), threads)
     vals = []
     t0 = time.time()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(p, args.cpu_iters, threads))
+        vals.append(cpu_baseline(p, args, threads))
     wall = time.time() - t0
     v = statistics.mean(x["value"] for x in vals)
     cb = dict(vals[-1])
@@ -304,7 +325,10 @@ def run_reference(args, world, rank, pg):
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall / max(args.steps, 1) * 1000.0, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": config_of(p, args, {"form": "reference CPU loop (oracle port), bounded sample"}),
+            "config": config_of(p, args, {"form": "reference CPU loop (oracle port), sampled",
+                                          "input": "graph prepared up to its spanning tree by this repository's "
+                                                   "host library (untimed); the sampled trees by its heap-ordered "
+                                                   "searches (untimed)"}),
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -324,34 +348,94 @@ def pinned_like(a):
     return out, ptr
 
 
+def plain_form(solver, N, stream, sh, windows=8, width=128):
+    """The per-iteration device form (mcbgpu_select + mcbgpu_update per iteration)
+    timed on `windows` windows of `width` iterations centred at (k + 1/2) N / windows,
+    each reached by the blocked run; integrated over N iterations (midpoint rule).
+    Each window's selections are checked against the blocked run's."""
+    import numpy as np
+    import torch
+    full_sel, _ = solver.results(stream=sh)
+    per_iter, starts = [], []
+    for k in range(windows):
+        e0 = int((k + 0.5) * N / windows) - width // 2
+        e0 = max(0, min(N - width, e0)) // 64 * 64
+        w = min(width, N - e0)
+        solver.reset(sh)
+        solver.run(e0, sh)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for e in range(e0, e0 + w):
+            solver.select(e, sh, fetch=False)
+            solver.update(e, sh)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        sel, _ = solver.results(e0 + w, stream=sh)
+        assert np.array_equal(sel[e0:e0 + w], full_sel[e0:e0 + w]), "per-iteration and blocked selections differ"
+        per_iter.append(ev0.elapsed_time(ev1) / 1e3 / w)
+        starts.append(e0)
+    total = float(np.mean(per_iter) * N)
+    return {"value": total, "unit": "s",
+            "sample": "per-iteration device form (select + update per iteration) on %d windows of %d iterations "
+                      "starting at %s, each reached by the blocked run; mean %.3f ms per iteration x %d iterations "
+                      "(midpoint rule); every window's selections equal the blocked run's"
+                      % (windows, width, starts, float(np.mean(per_iter)) * 1e3, N),
+            "ms_per_iteration": [round(x * 1e3, 4) for x in per_iter]}
+
+
 def run_gpu(args, world, rank, local, pg):
     import numpy as np
     import torch
 
-    from minimumcyclebasis_gb300 import Solver
+    from minimumcyclebasis_gb300 import Problem, Solver, prepare_on_device
     from minimumcyclebasis_gb300.build import build_all
 
     build_all()
     torch.cuda.set_device(local)
     want_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
-    p = prepare(args, keep_trees=want_cpu)
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
+    g = make_graph(args)
+    pin = PINNED_WEIGHTS.get((args.graph, args.n, args.seed))
+
+    # graph -> basis, once: preparation + solve + results
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    if args.prep == "device":
+        dp, gen = prepare_on_device(g, threads=0, stream=sh, keep_gen=True)
+        p, solver = dp.problem, dp.solver
+        prep_times = dict(dp.times)
+    else:
+        p = Problem.from_graph(g).prepare(threads=0)
+        i = p.info
+        prep_times = {"total": time.perf_counter() - t0, "trees": i.t_trees, "collect": i.t_collect}
+        solver = Solver.from_problem(p, stream=sh)
+    solver.run(args.max_iterations, sh)
+    sel0, tot0 = solver.results(stream=sh)
+    graph_to_basis = time.perf_counter() - t0
+    log("graph to basis %.2fs (preparation %.2fs), total weight %d" % (graph_to_basis, prep_times["total"], tot0))
+    if args.max_iterations < 0 and pin is not None:
+        assert tot0 == pin, "total weight %d differs from the pinned %d" % (tot0, pin)
+    # host copies of the lists, for the end-to-end steps from pinned host buffers
     _, _, w, _ = p.candidates()
-    off, co = p.cycle_lists()
-    solver = Solver(p.N, w, off, co, stream=sh)
-    run = solver.run if args.mode == "blocked" else solver.run_plain
+    if args.prep == "device":
+        off, co = gen.fetch_lists()
+        gen.close()
+        tied = dp.tied_roots
+    else:
+        off, co = p.cycle_lists()
+        tied = None
 
     def solve_once():
         solver.reset(sh)
-        run(args.max_iterations, sh)
+        solver.run(args.max_iterations, sh)
 
     for i in range(args.warmup):
         solve_once()
-        if i == 0:
-            sel, tot = solver.results(stream=sh)
-            assert (sel >= 0).all(), "warm-up solve failed"
-            log("warm-up total weight %d" % tot)
+    sel, tot = solver.results(stream=sh)
+    assert np.array_equal(sel, sel0) and tot == tot0, "warm-up solve differs from the first"
     torch.cuda.synchronize()
     if pg:
         pg.barrier()
@@ -368,6 +452,7 @@ def run_gpu(args, world, rank, local, pg):
     ms = ev0.elapsed_time(ev1) / args.steps
     launches = solver.launches - launches0
     sel, tot = solver.results(stream=sh)
+    assert np.array_equal(sel, sel0) and tot == tot0, "timed solves differ from the first"
     # per-kernel durations: the same K solves again, with an event pair around
     # every launch on the solver's stream (kept out of the timed region above)
     solver.set_profiling(True)
@@ -379,6 +464,11 @@ def run_gpu(args, world, rank, local, pg):
     if pg:
         ms = max_over_ranks(ms, pg)
         pg.barrier()
+
+    plain = None
+    if not args.no_plain and args.max_iterations < 0:
+        plain = plain_form(solver, p.N, stream, sh, windows=args.plain_windows, width=args.plain_width)
+        plain["speedup"] = plain["value"] / (ms / 1e3)
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
@@ -395,7 +485,7 @@ def run_gpu(args, world, rank, local, pg):
 
         def e2e_once():
             solver.upload(sh, pw, po, pc)
-            run(args.max_iterations, sh)
+            solver.run(args.max_iterations, sh)
             check_gpu(lib.mcbgpu_solver_results(solver._h, C.c_void_p(psel.ctypes.data), p.N, C.byref(tot_c),
                                                 C.c_void_p(sh)), "mcbgpu_solver_results")
 
@@ -405,7 +495,8 @@ def run_gpu(args, world, rank, local, pg):
         for _ in range(args.e2e_steps):
             e2e_once()
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-        assert np.array_equal(psel[:p.N], sel) and tot_c.value == tot, "e2e results differ"
+        iters = p.N if args.max_iterations < 0 else min(args.max_iterations, p.N)
+        assert np.array_equal(psel[:iters], sel[:iters]) and tot_c.value == tot, "e2e results differ"
         e2e = {"value": e2e_s, "unit": "s", "steps": args.e2e_steps,
                "h2d_bytes_per_step": int(w.nbytes + off.nbytes + co.nbytes),
                "d2h_bytes_per_step": int(8 * p.N + 8 + 4)}
@@ -424,8 +515,9 @@ def run_gpu(args, world, rank, local, pg):
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
-        if tj.get("vertices") == args.n and tj.get("graph", "random") == args.graph:  # captured on this workload
-            traffic = tj.get(name)
+        rec = tj.get("%s:%d" % (args.graph, args.n))
+        if rec:  # captured on this workload (or scaled to it; see the file)
+            traffic = rec.get(name)
     total_ms = sum(v["ms"] for v in stats.values())
     roofline = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
@@ -436,15 +528,23 @@ def run_gpu(args, world, rank, local, pg):
 
     cb = None
     if want_cpu:
-        cb = cpu_baseline(p, args.cpu_iters, args.cpu_threads)
+        cb = cpu_baseline(p, args, args.cpu_threads)
     if rank != 0:
         return None
+    extra = {"total_weight": tot, "total_weight_pinned": pin, "solves_per_s_all_ranks": world * 1e3 / ms,
+             "cycle_nnz": int(off[-1]), "preparation": args.prep,
+             "l2": ("inputs (cycle lists %.2f GB) larger than the 129 MB L2; no flush" % (int(off[-1]) * 4 / 1e9))
+             if int(off[-1]) * 4 > 129e6 else "small case: inputs fit in L2"}
     return {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": config_of(p, args, {"total_weight": tot, "solves_per_s_all_ranks": world * 1e3 / ms}),
-            "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
-            "cpu_baseline": cb}
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic", "config": config_of(p, args, extra),
+            "clocks": clocks.summary(), "e2e": e2e,
+            "e2e_with_preparation": {"value": graph_to_basis, "unit": "s", "runs": 1,
+                                     "preparation_s": {k: round(v, 3) for k, v in prep_times.items()},
+                                     "tied_roots_searched_on_host": tied,
+                                     "note": "graph edge arrays in host memory -> basis in host memory: "
+                                             "preparation + solve + results, measured once"},
+            "plain_gpu": plain, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cb}
 
 
 def run_batch(args, world, rank, local, pg):
@@ -627,25 +727,36 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--n", "--vertices", dest="n", type=int, default=50000, help="graph vertices (edges = 2n)")
+    ap.add_argument("--n", "--vertices", dest="n", type=int, default=None,
+                    help="graph size: planar: triangulated points (default 263000); random: vertices, edges = 2n "
+                         "(default 50000); rgg: vertices (default 20000)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--mode", choices=["blocked", "plain"], default="blocked")
     ap.add_argument("--max-iterations", type=int, default=-1)
-    ap.add_argument("--cpu-iters", type=int, default=40, help="iterations in the CPU baseline sample")
+    ap.add_argument("--cpu-sample-roots", type=int, default=2000,
+                    help="FVS trees in the CPU baseline's label-pass sample")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--cpu-budget", type=float, default=20.0,
                     help="seconds of CPU solve time in the batched workload's baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--graph", choices=["random", "rgg", "planar"], default="random",
-                    help="graph family of the single-graph workload (random: the 50k plain-GPU configuration)")
-    ap.add_argument("--workload", choices=["random", "batch"], default="random",
-                    help="random: the 50k-node graph (default); batch: the batched configuration")
+    ap.add_argument("--graph", choices=["random", "rgg", "planar"], default="planar",
+                    help="graph family of the single-graph workload (planar: the 1M-vertex scale configuration; "
+                         "random: the 50k plain-GPU configuration)")
+    ap.add_argument("--workload", choices=["graph", "batch"], default="graph",
+                    help="graph: one graph of --graph (default); batch: the batched configuration")
+    ap.add_argument("--prep", choices=["device", "host"], default="device",
+                    help="candidate generation on the GPU (default) or on the host")
+    ap.add_argument("--no-plain", action="store_true", help="skip the per-iteration form's timing")
+    ap.add_argument("--plain-windows", type=int, default=8)
+    ap.add_argument("--plain-width", type=int, default=128)
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--blocks", type=int, default=2000)
     ap.add_argument("--plain-stride", type=int, default=16)
     args = ap.parse_args()
+    if args.n is None:
+        args.n = DEFAULT_N[args.graph]
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
         out = run_reference(args, world, rank, pg)

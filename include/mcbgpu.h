@@ -139,6 +139,10 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t num_coords, int64_t num_ca
  * stream has passed this point. */
 int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t *offsets,
                          const int32_t *coords, void *stream);
+/* mcbgpu_solver_upload with the three arrays in device memory (e.g. the lists a
+ * device candidate generation built, mcbgpu_gen_get_lists): copied on the device. */
+int mcbgpu_solver_upload_device(mcbgpu_solver *s, const int32_t *weight, const int64_t *offsets,
+                                const int32_t *coords, void *stream);
 /* Reset S to the unit vectors without re-uploading the candidates. */
 int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream);
 
@@ -267,6 +271,55 @@ int mcbgpu_trees_run(mcbgpu_trees *t, const uint32_t *roots, int32_t count, int3
                      uint8_t *tied, void *stream);
 int64_t mcbgpu_trees_device_bytes(const mcbgpu_trees *t);
 int mcbgpu_trees_destroy(mcbgpu_trees *t);
+
+/* ---- 6. candidate generation on the device (the host preparation's per-root
+ * trees, candidate test and coordinate lists: include/Dijkstra.h:78-254,
+ * include/work_per_thread.h:92-147, include/cycles.h:144-195) -------------------
+ * For a problem prepared on the host up to its spanning tree (mcbhost.h,
+ * mcbh_options.structure_only): the reduced graph (row offsets, and per slot its
+ * row, column, weight >= 1, reverse slot and coordinate or -1), the FVS array
+ * (n', -1 off the FVS) and vertices (F), the pair list (mcbh_get_pairs), all checked
+ * at creation.  `chunk` roots are processed per call; the parent slots of all F
+ * trees stay on the device (4 F n' bytes) until mcbgpu_gen_release_trees.
+ * Per chunk, in order:
+ *   mcbgpu_gen_trees       the trees of FVS indices [t0, t0 + count); tied[i] = 1
+ *                          where the host must search root t0 + i itself
+ *                          (mcbh_search_trees), then hand its tree over with
+ *   mcbgpu_gen_put_trees   (distances and parent slots, count x n', host memory);
+ *   mcbgpu_gen_candidates  the candidate test of the chunk: counts[i] candidates of
+ *                          root t0 + i, *total for the chunk; then
+ *   mcbgpu_gen_fetch       their pair indices (ascending per root, roots in order)
+ *                          and weights into host memory (total entries each).
+ * After ranking (mcbh_rank_candidates on the host):
+ *   mcbgpu_gen_lists       the sorted coordinate lists of the first K ranked
+ *                          candidates (tree = FVS index, edge_offset = the candidate's
+ *                          slot, weight, in rank order, host memory) on the device;
+ *                          *nnz their total;
+ *   mcbgpu_gen_get_lists   the device weights (K), offsets (K + 1) and coordinates
+ *                          (nnz), valid until the next mcbgpu_gen_lists or destroy:
+ *                          pass them to mcbgpu_solver_upload_device.
+ * Synchronising calls (each reads the device status); an index out of range in a
+ * caller's array gives MCBGPU_E_DEVICE. */
+typedef struct mcbgpu_gen mcbgpu_gen;
+int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint32_t *row_offsets,
+                      const uint32_t *rows, const uint32_t *cols, const int32_t *weights, const uint32_t *rev,
+                      const int32_t *edge_coord, int32_t num_coords, const int32_t *fvs_array,
+                      const uint32_t *fvs_vertices, int32_t fvs_size, const uint32_t *pair_slot, int32_t chunk);
+int mcbgpu_gen_trees(mcbgpu_gen *g, int32_t t0, int32_t count, uint8_t *tied, void *stream);
+int mcbgpu_gen_put_trees(mcbgpu_gen *g, const int32_t *trees, int32_t count, const int32_t *dist,
+                         const int32_t *parent_slot, void *stream);
+int mcbgpu_gen_candidates(mcbgpu_gen *g, int64_t *counts, int64_t *total, void *stream);
+int mcbgpu_gen_fetch(mcbgpu_gen *g, int64_t total, uint32_t *pair_index, int32_t *weight, void *stream);
+int mcbgpu_gen_lists(mcbgpu_gen *g, int64_t K, const int32_t *tree, const int32_t *edge_offset,
+                     const int32_t *weight, int64_t *nnz, void *stream);
+int mcbgpu_gen_get_lists(const mcbgpu_gen *g, const int32_t **weight, const int64_t **offsets,
+                         const int32_t **coords);
+/* The lists copied into host memory: offsets (K + 1) and coordinates (nnz). */
+int mcbgpu_gen_copy_lists(const mcbgpu_gen *g, int64_t *offsets, int32_t *coords, void *stream);
+/* Frees the resident parent slots (after the lists are built). */
+int mcbgpu_gen_release_trees(mcbgpu_gen *g);
+int64_t mcbgpu_gen_device_bytes(const mcbgpu_gen *g);
+int mcbgpu_gen_destroy(mcbgpu_gen *g);
 
 #ifdef __cplusplus
 }

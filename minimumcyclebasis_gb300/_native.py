@@ -95,6 +95,7 @@ GPU_SYMBOLS = {
     "mcbgpu_label_forest_noalloc": (C.c_int, [vp, vp, vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, vp]),
     "mcbgpu_solver_create": (C.c_int, [C.POINTER(vp), i32, i64, i64]),
     "mcbgpu_solver_upload": (C.c_int, [vp, vp, vp, vp, vp]),
+    "mcbgpu_solver_upload_device": (C.c_int, [vp, vp, vp, vp, vp]),
     "mcbgpu_solver_reset": (C.c_int, [vp, vp]),
     "mcbgpu_select": (C.c_int, [vp, i32, C.POINTER(i64), vp]),
     "mcbgpu_cycle_vector": (C.c_int, [vp, i32, vp, vp]),
@@ -126,6 +127,17 @@ GPU_SYMBOLS = {
     "mcbgpu_trees_device_bytes": (i64, [vp]),
     "mcbgpu_trees_destroy": (C.c_int, [vp]),
     "mcbgpu_batch_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
+    "mcbgpu_gen_create": (C.c_int, [C.POINTER(vp), i32, i64, vp, vp, vp, vp, vp, vp, i32, vp, vp, i32, vp, i32]),
+    "mcbgpu_gen_trees": (C.c_int, [vp, i32, i32, vp, vp]),
+    "mcbgpu_gen_put_trees": (C.c_int, [vp, vp, i32, vp, vp, vp]),
+    "mcbgpu_gen_candidates": (C.c_int, [vp, vp, C.POINTER(i64), vp]),
+    "mcbgpu_gen_fetch": (C.c_int, [vp, i64, vp, vp, vp]),
+    "mcbgpu_gen_lists": (C.c_int, [vp, i64, vp, vp, vp, C.POINTER(i64), vp]),
+    "mcbgpu_gen_get_lists": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
+    "mcbgpu_gen_copy_lists": (C.c_int, [vp, vp, vp, vp]),
+    "mcbgpu_gen_release_trees": (C.c_int, [vp]),
+    "mcbgpu_gen_device_bytes": (i64, [vp]),
+    "mcbgpu_gen_destroy": (C.c_int, [vp]),
 }
 
 

@@ -26,7 +26,8 @@ CSRC = os.path.join(PKG, "csrc")
 ORACLE = os.path.join(ROOT, "oracle")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-GPU_SOURCES = ["mcbgpu_runtime.cu", "mcbgpu_labels.cu", "mcbgpu_solver.cu", "mcbgpu_batch.cu", "mcbgpu_trees.cu"]
+GPU_SOURCES = ["mcbgpu_runtime.cu", "mcbgpu_labels.cu", "mcbgpu_solver.cu", "mcbgpu_batch.cu", "mcbgpu_trees.cu",
+               "mcbgpu_gen.cu"]
 
 
 def _nvcc() -> str:

@@ -20,6 +20,11 @@ enum : unsigned {
 };
 
 void set_error(const char *fmt, ...);
+
+// An upper bound on every shortest-path distance of a graph with positive weights
+// (slot o < rev[o] is one undirected edge): a shortest path is simple, so at most
+// nodes - 1 edges; the sum of the nodes - 1 heaviest edges.
+long long path_length_bound(int32_t nodes, int64_t slots, const int32_t *weights, const uint32_t *rev);
 int cuda_fail(cudaError_t e, const char *what);
 
 #define MCB_CUDA(call)                                              \

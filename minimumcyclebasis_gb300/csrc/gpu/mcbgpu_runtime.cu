@@ -1,8 +1,11 @@
 // Runtime helpers of libmcbgpu.so: error strings and the reference's GPU-layer
 // free functions (gpu/common.cu:1-67, declared in gpu/common.cuh:18-27).
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
+#include <vector>
 
 #include "mcbgpu_internal.cuh"
 
@@ -20,6 +23,18 @@ void set_error(const char *fmt, ...) {
 int cuda_fail(cudaError_t e, const char *what) {
     set_error("%s: %s", what, cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? MCBGPU_E_NOMEM : MCBGPU_E_CUDA;
+}
+
+long long path_length_bound(int32_t nodes, int64_t slots, const int32_t *weights, const uint32_t *rev) {
+    std::vector<long long> w;
+    w.reserve((size_t)(slots / 2));
+    for (int64_t o = 0; o < slots; o++)
+        if ((uint64_t)o < rev[o]) w.push_back(weights[o]);
+    const size_t keep = std::min(w.size(), (size_t)(nodes > 1 ? nodes - 1 : 0));
+    std::nth_element(w.begin(), w.begin() + keep, w.end(), std::greater<long long>());
+    long long s = 0;
+    for (size_t i = 0; i < keep; i++) s += w[i];
+    return s;
 }
 
 // State kept by the reference's globals prop / device_id / dimGrid / dimBlock

@@ -1939,8 +1939,9 @@ int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream) {
     return MCBGPU_OK;
 }
 
-int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t *offsets, const int32_t *coords,
-                         void *stream) {
+// The upload of both entry points: `kind` says where the three arrays live.
+static int solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t *offsets, const int32_t *coords,
+                         void *stream, cudaMemcpyKind kind) {
     if (!s || (s->K > 0 && (!weight || !offsets)) || (s->nnz > 0 && !coords)) {
         set_error("mcbgpu_solver_upload: NULL argument");
         return MCBGPU_E_ARG;
@@ -1948,11 +1949,10 @@ int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t 
     cudaStream_t st = (cudaStream_t)stream;
     s->uploaded = false;
     if (s->K > 0) {
-        MCB_CUDA(cudaMemcpyAsync(s->d_weight, weight, sizeof(int32_t) * (size_t)s->K, cudaMemcpyHostToDevice, st));
-        MCB_CUDA(cudaMemcpyAsync(s->d_off, offsets, sizeof(int64_t) * (size_t)(s->K + 1), cudaMemcpyHostToDevice, st));
+        MCB_CUDA(cudaMemcpyAsync(s->d_weight, weight, sizeof(int32_t) * (size_t)s->K, kind, st));
+        MCB_CUDA(cudaMemcpyAsync(s->d_off, offsets, sizeof(int64_t) * (size_t)(s->K + 1), kind, st));
     }
-    if (s->nnz > 0)
-        MCB_CUDA(cudaMemcpyAsync(s->d_coords, coords, sizeof(int32_t) * (size_t)s->nnz, cudaMemcpyHostToDevice, st));
+    if (s->nnz > 0) MCB_CUDA(cudaMemcpyAsync(s->d_coords, coords, sizeof(int32_t) * (size_t)s->nnz, kind, st));
     // the lists are checked on the device before any other kernel reads them
     unsigned chk[2] = {0, 0};
     MCB_CUDA(cudaMemsetAsync(s->d_check, 0, sizeof chk, st));
@@ -1989,6 +1989,16 @@ int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t 
     }
     s->uploaded = true;
     return mcbgpu_solver_reset(s, stream);
+}
+
+int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t *offsets, const int32_t *coords,
+                         void *stream) {
+    return solver_upload(s, weight, offsets, coords, stream, cudaMemcpyHostToDevice);
+}
+
+int mcbgpu_solver_upload_device(mcbgpu_solver *s, const int32_t *weight, const int64_t *offsets,
+                                const int32_t *coords, void *stream) {
+    return solver_upload(s, weight, offsets, coords, stream, cudaMemcpyDeviceToDevice);
 }
 
 int mcbgpu_select(mcbgpu_solver *s, int32_t e, int64_t *rank, void *stream) {

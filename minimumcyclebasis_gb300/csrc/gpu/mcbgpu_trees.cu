@@ -1,196 +1,14 @@
 // Shortest-path trees of many roots of one graph (the host's per-root tree searches,
-// include/Dijkstra.h:78-124, as one persistent launch): for each root, the distances
-// to every vertex and every vertex's parent slot, chosen by the rule that makes any
-// exact search agree with the reference's heap search, plus a flag for the roots
-// where that rule cannot decide.
-//
-// Graph: the reduced multigraph's CSR (row offsets, columns, weights, reverse slots),
-// every weight at least 1 and every distance below 2^31 (checked at creation).
-//
-// One CTA per root, persistent over a root counter:
-//   1. distances, label-correcting by buckets: each round takes lo = the smallest
-//      distance among dirty vertices and relaxes (atomicMin) the arcs of every dirty
-//      vertex nearer than lo + delta, marking improved heads dirty.  The dirty vertex
-//      at lo is final after its round (weights >= 1), so a root needs at most n
-//      rounds; the loop stops there and flags the root if it has not converged.
-//      Distances and dirty bits live in shared memory up to kTreeSharedMaxN vertices,
-//      in a per-CTA global slice beyond.
-//   2. parents: for each vertex c, among its neighbours x on a shortest path
-//      (d[x] + w = d[c]) the nearest one, entered through its first slot to c (the
-//      smallest slot index of x's row among those arcs); the reference keeps exactly
-//      that parent (only a strictly shorter path replaces one, and parents at
-//      different distances settle in distance order) unless two different
-//      neighbours tie at that nearest distance, which sets the root's flag so that
-//      the host searches that root itself.
-// CTA barriers are cta_sync / cta_sync_and (the non-aligned barrier): the loops
-// before them diverge within warps.
+// include/Dijkstra.h:78-124, as one persistent launch), for a host tree supplier:
+// the kernel (mcbgpu_sssp.cuh) runs on a chunk of roots and the distances, parent
+// slots and tie flags are copied back to the host.
 #include <climits>
 #include <vector>
 
-#include "mcbgpu_internal.cuh"
-
-namespace mcbgpu {
-namespace {
-
-constexpr int kTreeThreads = 1024;
-constexpr int kTreeSharedMaxN = 53248;  // 208 KB of distances + 6.5 KB of dirty bits (of 227 KB)
-
-struct TreeArgs {
-    const uint32_t *ro;
-    const uint32_t *cols;
-    const int32_t *w;
-    const uint32_t *rev;
-    int32_t n;
-    int32_t delta;
-    const uint32_t *roots;
-    int32_t count;
-    int32_t *dist_out;   // count x n
-    int32_t *pedge_out;  // count x n
-    uint8_t *tied_out;   // count
-    int32_t *gdist;      // gridDim.x x n (global form only)
-    uint32_t *gdirty;    // gridDim.x x words (global form only)
-    int32_t *next_root;
-    unsigned *status;
-};
-
-__device__ __forceinline__ int block_min(int v, int *red) {
-    v = __reduce_min_sync(0xffffffffu, v);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) red[warp] = v;
-    cta_sync();
-    if (warp == 0) {
-        int x = lane < (int)(blockDim.x >> 5) ? red[lane] : INT_MAX;
-        x = __reduce_min_sync(0xffffffffu, x);
-        if (lane == 0) red[32] = x;
-    }
-    cta_sync();
-    return red[32];
-}
-
-template <bool kShared>
-__global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_red[33];
-    __shared__ int s_root;
-    const int n = a.n;
-    const int words = (n + 31) >> 5;
-    int32_t *dist;
-    uint32_t *dirty;
-    if (kShared) {
-        dist = reinterpret_cast<int32_t *>(smem);
-        dirty = reinterpret_cast<uint32_t *>(smem + (((size_t)n * 4 + 15) & ~(size_t)15));
-    } else {
-        dist = a.gdist + (size_t)blockIdx.x * n;
-        dirty = a.gdirty + (size_t)blockIdx.x * words;
-    }
-    volatile int32_t *vdist = dist;
-    volatile uint32_t *vdirty = dirty;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (;;) {
-        if (tid == 0) s_root = atomicAdd(a.next_root, 1);
-        cta_sync();
-        const int r = s_root;
-        cta_sync();  // every thread has read s_root before thread 0 writes it again
-        if (r >= a.count) return;
-        const uint32_t src = a.roots[r];  // < n, checked by the host
-        for (int v = tid; v < n; v += nt) dist[v] = INT_MAX;
-        for (int k = tid; k < words; k += nt) dirty[k] = 0;
-        cta_sync();
-        if (tid == 0) {
-            dist[src] = 0;
-            dirty[src >> 5] = 1u << (src & 31);
-        }
-        cta_sync();
-        // 1. distances
-        bool converged = false;
-        for (int round = 0; round <= n; round++) {
-            int m = INT_MAX;
-            for (int k = tid; k < words; k += nt) {
-                uint32_t bits = vdirty[k];
-                while (bits) {
-                    const int b = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    const int d = vdist[(k << 5) + b];
-                    m = d < m ? d : m;
-                }
-            }
-            const int lo = block_min(m, s_red);
-            if (lo == INT_MAX) {
-                converged = true;
-                break;
-            }
-            const int hi = lo > INT_MAX - a.delta ? INT_MAX : lo + a.delta;
-            for (int k = tid; k < words; k += nt) {
-                uint32_t bits = vdirty[k];
-                while (bits) {
-                    const int b = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    const int v = (k << 5) + b;
-                    if (vdist[v] >= hi) continue;
-                    atomicAnd(&dirty[k], ~(1u << b));
-                    // pairs with the fence between a writer's atomicMin and atomicOr:
-                    // a bit this atomicAnd cleared was set after its distance was
-                    // lowered, so the read below sees that distance; a later
-                    // improvement sets the bit again
-                    __threadfence_block();
-                    const int dv = vdist[v];
-                    for (uint32_t o = a.ro[v]; o < a.ro[v + 1]; o++) {
-                        const uint32_t x = a.cols[o];
-                        const int nd = dv + a.w[o];
-                        if (nd < vdist[x]) {
-                            const int old = atomicMin(&dist[x], nd);
-                            if (nd < old) {
-                                __threadfence_block();  // the new distance before the dirty bit
-                                atomicOr(&dirty[x >> 5], 1u << (x & 31));
-                            }
-                        }
-                    }
-                }
-            }
-            cta_sync();
-        }
-        // 2. parents by the rule, and the root's tie flag
-        int tie = converged ? 0 : 1;
-        for (int c = tid; c < n; c += nt) {
-            const int dc = vdist[c];
-            int32_t slot = -1;
-            if ((uint32_t)c != src && dc != INT_MAX) {
-                int bestd = INT_MAX, rival = 0;  // rival: another neighbour as near as the best
-                uint32_t bestx = 0xffffffffu, bests = 0xffffffffu;
-                for (uint32_t o = a.ro[c]; o < a.ro[c + 1]; o++) {
-                    const uint32_t x = a.cols[o];
-                    const int dx = vdist[x];
-                    if (dx == INT_MAX || (long long)dx + a.w[o] != (long long)dc) continue;
-                    if (dx < bestd) {
-                        bestd = dx;
-                        bestx = x;
-                        bests = a.rev[o];
-                        rival = 0;
-                    } else if (dx == bestd) {
-                        if (x == bestx)
-                            bests = a.rev[o] < bests ? a.rev[o] : bests;
-                        else
-                            rival = 1;
-                    }
-                }
-                slot = bests == 0xffffffffu ? -1 : (int32_t)bests;
-                if (rival || slot < 0) tie = 1;  // (no shortest-path neighbour cannot happen; left to the host)
-            } else if ((uint32_t)c != src) {
-                tie = 1;  // unreachable vertex (the graph is not connected): left to the host
-            }
-            a.dist_out[(size_t)r * n + c] = dc;
-            a.pedge_out[(size_t)r * n + c] = slot;
-        }
-        tie = cta_sync_and(tie == 0) ? 0 : 1;
-        if (tid == 0) a.tied_out[r] = tie ? 1 : 0;
-        if (!converged && tid == 0) atomicOr(a.status, ST_DIVERGED);
-    }
-}
-
-}  // namespace
-}  // namespace mcbgpu
+#include "mcbgpu_sssp.cuh"
 
 using namespace mcbgpu;
+using namespace mcbgpu::sssp;
 
 struct mcbgpu_trees {
     int32_t n = 0;
@@ -255,7 +73,7 @@ int mcbgpu_trees_create(mcbgpu_trees **out, int32_t nodes, int64_t slots, const 
         wsum += weights[o];
         wmax = weights[o] > wmax ? weights[o] : wmax;
     }
-    if (wmax * ((long long)nodes + 1) >= (long long)INT_MAX) {
+    if (path_length_bound(nodes, slots, weights, rev) + wmax >= (long long)INT_MAX) {
         set_error("mcbgpu_trees_create: distances could reach 2^31 (largest weight %lld, %d vertices)", wmax,
                   (int)nodes);
         return MCBGPU_E_ARG;

@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <memory_resource>
 #include <new>
@@ -735,12 +736,21 @@ void setup_searches(mcbh_problem &P) {
     P.slot_pair.assign(g.slots(), 0);
     P.arcs.resize(g.slots());
     long long wmin = 1, wmax = 0;
+    std::vector<long long> pair_w;
+    pair_w.reserve(g.slots() / 2);
     for (size_t i = 0; i < g.slots(); i++) {
         P.arcs[i] = {g.cols[i], g.w[i]};
         wmin = std::min(wmin, (long long)g.w[i]);
         wmax = std::max(wmax, (long long)g.w[i]);
+        if (i < g.rev[i]) pair_w.push_back(g.w[i]);
     }
-    P.fast_search_ok = wmin >= 1 && wmax * (long long)(g.n + 1) < 0x7fffffffLL;
+    // a shortest path is simple: at most n - 1 edges, so no distance exceeds the sum
+    // of the n - 1 heaviest edges, and no tentative one that plus the heaviest edge
+    const size_t keep = std::min(pair_w.size(), (size_t)std::max(g.n - 1, 0));
+    std::nth_element(pair_w.begin(), pair_w.begin() + keep, pair_w.end(), std::greater<long long>());
+    long long path_bound = 0;
+    for (size_t i = 0; i < keep; i++) path_bound += pair_w[i];
+    P.fast_search_ok = wmin >= 1 && path_bound + wmax < 0x7fffffffLL;
     for (size_t i = 0; i < g.slots(); i++) {
         if (i < g.rev[i]) {
             P.slot_pair[i] = P.slot_pair[g.rev[i]] = (u32)P.pair_first.size();

@@ -117,6 +117,24 @@ class Solver:
             self.upload(stream)
 
     @classmethod
+    def from_device_lists(cls, num_coords: int, K: int, nnz: int, d_weight: int, d_offsets: int, d_coords: int,
+                          stream=0) -> "Solver":
+        """A solver whose candidates are already in device memory (a device candidate
+        generation's lists): copied device to device (mcbgpu_solver_upload_device).
+        No host copies are kept, so upload() needs explicit arrays."""
+        self = cls.__new__(cls)
+        self.lib = gpu_lib()
+        self.N, self.K = int(num_coords), int(K)
+        self.weight = self.offsets = self.coords = None
+        h = C.c_void_p()
+        check_gpu(self.lib.mcbgpu_solver_create(C.byref(h), self.N, self.K, int(nnz)), "mcbgpu_solver_create")
+        self._h = h
+        check_gpu(self.lib.mcbgpu_solver_upload_device(h, C.c_void_p(d_weight), C.c_void_p(d_offsets),
+                                                       C.c_void_p(d_coords), _stream(stream)),
+                  "mcbgpu_solver_upload_device")
+        return self
+
+    @classmethod
     def from_problem(cls, prob, stream=0) -> "Solver":
         _, _, w, _ = prob.candidates()
         off, co = prob.cycle_lists()

@@ -33,6 +33,11 @@ def lib():
         L.mcbo_support_vector_at.restype = C.c_int64
         L.mcbo_support_vector_at.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, vp, vp, vp, vp, vp, vp, C.c_int,
                                              C.c_int64, vp]
+        L.mcbo_label_pass_seconds.restype = C.c_double
+        L.mcbo_label_pass_seconds.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int,
+                                              C.c_uint64]
+        L.mcbo_update_row_seconds.restype = C.c_double
+        L.mcbo_update_row_seconds.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64]
         _lib = L
     return _lib
 
@@ -112,3 +117,26 @@ def cycle_vector(prob, rank: int) -> np.ndarray:
                 setbit(int(ec[pe_x]))
             x = int(rows[pe_x]) if int(rows[pe_x]) != x else int(cols[pe_x])
     return words
+
+
+def label_pass_seconds(prob, parent_edge, passes: int = 2, threads: int = 0, seed: int = 1) -> float:
+    """Seconds per label pass of the loop over the trees whose parent edges are given
+    (count x n, e.g. a sample of the FVS roots from Problem.search_trees), with
+    random support vectors."""
+    rows, cols, _, _, _ = prob.reduced_graph()
+    _, ec = prob.coords()
+    pe = np.ascontiguousarray(parent_edge, np.int32)
+    F = pe.size // prob.n
+    sec = lib().mcbo_label_pass_seconds(prob.n, F, prob.N, _p(rows), _p(cols), _p(ec), _p(pe), passes, threads,
+                                        seed)
+    if sec < 0:
+        raise RuntimeError("oracle label_pass_seconds failed")
+    return sec
+
+
+def update_row_seconds(N: int, rows: int = 2048, passes: int = 3, threads: int = 0, seed: int = 1) -> float:
+    """Seconds per row of the loop's full-width independence update at N coordinates."""
+    sec = lib().mcbo_update_row_seconds(N, rows, passes, threads, seed)
+    if sec < 0:
+        raise RuntimeError("oracle update_row_seconds failed")
+    return sec

@@ -242,4 +242,73 @@ int64_t mcbo_support_vector_at(int n, int F, int N, int64_t K, const uint32_t *r
     return at;
 }
 
+// Cost samples of the loop above, for graphs whose F x n' trees do not fit the
+// host (the bench's CPU baseline extrapolates them to a whole solve):
+// seconds per label pass over the F trees given (their parent edges only; the
+// forest's BFS orders are built first and not timed), the mean of `passes` passes
+// with support vectors drawn from `seed`.
+double mcbo_label_pass_seconds(int n, int F, int N, const uint32_t *rows, const uint32_t *cols,
+                               const int32_t *edge_coord, const int32_t *parent_edge, int passes, int threads,
+                               uint64_t seed) {
+    if (n <= 0 || F <= 0 || N <= 0 || passes <= 0 || !rows || !cols || !edge_coord || !parent_edge) return -1.0;
+    if (threads <= 0) threads = omp_get_max_threads();
+    const int words = (N + 63) / 64;
+    Forest f;
+    f.n = n;
+    f.F = F;
+    f.rows = rows;
+    f.cols = cols;
+    f.edge_coord = edge_coord;
+    f.parent_edge = parent_edge;
+    f.build(threads);
+    std::vector<uint8_t> P((size_t)F * n);
+    std::vector<uint64_t> S(words);
+    uint64_t x = seed | 1;
+    double sum = 0;
+    for (int k = 0; k < passes; k++) {
+        for (auto &w : S) {
+            x ^= x << 13;
+            x ^= x >> 7;
+            x ^= x << 17;
+            w = x;
+        }
+        const double t0 = now_s();
+        f.labels(S.data(), P.data(), threads);
+        sum += now_s() - t0;
+    }
+    return sum / passes;
+}
+
+// Seconds per row of the independence update (dot product of C with the row over
+// all ceil(N/64) words, XOR of S_e into it when odd, as the loop above does for
+// every j > e), timed over `rows` rows with random contents, `passes` times.
+double mcbo_update_row_seconds(int N, int rows, int passes, int threads, uint64_t seed) {
+    if (N <= 0 || rows <= 0 || passes <= 0) return -1.0;
+    if (threads <= 0) threads = omp_get_max_threads();
+    const int words = (N + 63) / 64;
+    std::vector<uint64_t> S((size_t)rows * words), C(words), Se(words);
+    uint64_t x = seed | 1;
+    auto next = [&]() {
+        x ^= x << 13;
+        x ^= x >> 7;
+        x ^= x << 17;
+        return x;
+    };
+    for (auto &w : S) w = next();
+    for (auto &w : C) w = next();
+    for (auto &w : Se) w = next();
+    const double t0 = now_s();
+    for (int k = 0; k < passes; k++) {
+#pragma omp parallel for num_threads(threads) schedule(static)
+        for (int64_t j = 0; j < rows; j++) {
+            uint64_t *Sj = &S[(size_t)j * words];
+            uint64_t acc = 0;
+            for (int w = 0; w < words; w++) acc ^= C[w] & Sj[w];
+            if (__builtin_popcountll(acc) & 1)
+                for (int w = 0; w < words; w++) Sj[w] ^= Se[w];
+        }
+    }
+    return (now_s() - t0) / ((double)passes * rows);
+}
+
 }  // extern "C"

@@ -56,3 +56,18 @@ def test_reference_arm_of_the_batched_workload_prints_one_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is False
     assert d["config"]["workload"].startswith("batched: 16 random graphs")
     assert d["cpu_baseline"]["value"] == d["value"] and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_of_the_planar_workload_prints_one_line():
+    # the default graph family at a small size: the sampled label pass and row update
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "1500", "--steps", "1",
+           "--warmup", "1", "--cpu-sample-roots", "40", "--cpu-threads", "2"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["value"] > 0
+    assert d["config"]["workload"].startswith("planar-like graph from 1500 triangulated points")
+    assert "label pass over 40 of the" in d["cpu_baseline"]["sample"]
+    assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0

@@ -39,8 +39,8 @@ def test_reference_arm_under_torchrun_prints_one_line():
     env = dict(os.environ, MASTER_ADDR="127.0.0.1")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(free_port()), os.path.join(ROOT, "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--vertices", "300", "--cpu-iters", "3",
-           "--cpu-threads", "2"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--graph", "random", "--vertices",
+           "300", "--cpu-sample-roots", "20", "--cpu-threads", "2"]
     r = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
