@@ -291,10 +291,15 @@ int mcbgpu_trees_destroy(mcbgpu_trees *t);
  *   mcbgpu_gen_fetch       their pair indices (ascending per root, roots in order)
  *                          and weights into host memory (total entries each).
  * After ranking (mcbh_rank_candidates on the host):
- *   mcbgpu_gen_lists       the sorted coordinate lists of the first K ranked
- *                          candidates (tree = FVS index, edge_offset = the candidate's
- *                          slot, weight, in rank order, host memory) on the device;
- *                          *nnz their total;
+ *   mcbgpu_gen_rank        takes the K ranked candidates (tree = FVS index,
+ *                          edge_offset = the candidate's slot, weight; rank order,
+ *                          host memory) and walks their cycles once: list lengths
+ *                          and, with `features` (device, K x 16 bf16, may be NULL),
+ *                          each candidate's features for the learned proposal;
+ *   mcbgpu_gen_build_lists the sorted coordinate lists of the first K_keep ranked
+ *                          candidates on the device; *nnz their total (a proposal
+ *                          may keep a prefix; K_keep = K builds them all);
+ *   mcbgpu_gen_lists       mcbgpu_gen_rank without features + build of all K;
  *   mcbgpu_gen_get_lists   the device weights (K), offsets (K + 1) and coordinates
  *                          (nnz), valid until the next mcbgpu_gen_lists or destroy:
  *                          pass them to mcbgpu_solver_upload_device.
@@ -310,6 +315,9 @@ int mcbgpu_gen_put_trees(mcbgpu_gen *g, const int32_t *trees, int32_t count, con
                          const int32_t *parent_slot, void *stream);
 int mcbgpu_gen_candidates(mcbgpu_gen *g, int64_t *counts, int64_t *total, void *stream);
 int mcbgpu_gen_fetch(mcbgpu_gen *g, int64_t total, uint32_t *pair_index, int32_t *weight, void *stream);
+int mcbgpu_gen_rank(mcbgpu_gen *g, int64_t K, const int32_t *tree, const int32_t *edge_offset,
+                    const int32_t *weight, uint16_t *features, void *stream);
+int mcbgpu_gen_build_lists(mcbgpu_gen *g, int64_t K_keep, int64_t *nnz, void *stream);
 int mcbgpu_gen_lists(mcbgpu_gen *g, int64_t K, const int32_t *tree, const int32_t *edge_offset,
                      const int32_t *weight, int64_t *nnz, void *stream);
 int mcbgpu_gen_get_lists(const mcbgpu_gen *g, const int32_t **weight, const int64_t **offsets,
@@ -320,6 +328,31 @@ int mcbgpu_gen_copy_lists(const mcbgpu_gen *g, int64_t *offsets, int32_t *coords
 int mcbgpu_gen_release_trees(mcbgpu_gen *g);
 int64_t mcbgpu_gen_device_bytes(const mcbgpu_gen *g);
 int mcbgpu_gen_destroy(mcbgpu_gen *g);
+
+/* ---- 7. the learned proposal's network -----------------------------------------
+ * A two-layer perceptron over the 16 per-candidate features of mcbgpu_gen_rank
+ * (16 -> 64 ReLU -> 1): bf16 weights in the forward pass, fp32 accumulation (the
+ * first layer on the tensor cores), fp32 master parameters trained with Adam on the
+ * mean binary cross-entropy of (candidate, selected?) labels, positives weighted by
+ * pos_weight.  Parameters, in order: W1 (64 x 16, row = hidden unit), b1 (64), w2
+ * (64), b2 (1): mcbgpu_mlp_param_count() floats.  x (count x 16 bf16), labels
+ * (count bytes, nonzero = selected) and logits (count floats) are device memory;
+ * params and grads host memory.  Its scores order candidates for a proposal and
+ * never decide a result by themselves. */
+typedef struct mcbgpu_mlp mcbgpu_mlp;
+int mcbgpu_mlp_param_count(void);
+int mcbgpu_mlp_create(mcbgpu_mlp **out, const float *params);
+int mcbgpu_mlp_get_params(const mcbgpu_mlp *m, float *params);
+int mcbgpu_mlp_forward(mcbgpu_mlp *m, const uint16_t *x, int64_t count, float *logits, void *stream);
+/* The loss (*loss, mean) and its gradient (grads, mcbgpu_mlp_param_count() floats)
+ * at the current parameters. */
+int mcbgpu_mlp_gradients(mcbgpu_mlp *m, const uint16_t *x, const uint8_t *labels, int64_t count, float pos_weight,
+                         float *grads, float *loss, void *stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on the batch; *loss (may be NULL) the
+ * batch loss before the step. */
+int mcbgpu_mlp_train_step(mcbgpu_mlp *m, const uint16_t *x, const uint8_t *labels, int64_t count, float pos_weight,
+                          float lr, float *loss, void *stream);
+int mcbgpu_mlp_destroy(mcbgpu_mlp *m);
 
 #ifdef __cplusplus
 }

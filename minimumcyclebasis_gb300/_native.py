@@ -132,12 +132,21 @@ GPU_SYMBOLS = {
     "mcbgpu_gen_put_trees": (C.c_int, [vp, vp, i32, vp, vp, vp]),
     "mcbgpu_gen_candidates": (C.c_int, [vp, vp, C.POINTER(i64), vp]),
     "mcbgpu_gen_fetch": (C.c_int, [vp, i64, vp, vp, vp]),
+    "mcbgpu_gen_rank": (C.c_int, [vp, i64, vp, vp, vp, vp, vp]),
+    "mcbgpu_gen_build_lists": (C.c_int, [vp, i64, C.POINTER(i64), vp]),
     "mcbgpu_gen_lists": (C.c_int, [vp, i64, vp, vp, vp, C.POINTER(i64), vp]),
     "mcbgpu_gen_get_lists": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
     "mcbgpu_gen_copy_lists": (C.c_int, [vp, vp, vp, vp]),
     "mcbgpu_gen_release_trees": (C.c_int, [vp]),
     "mcbgpu_gen_device_bytes": (i64, [vp]),
     "mcbgpu_gen_destroy": (C.c_int, [vp]),
+    "mcbgpu_mlp_param_count": (C.c_int, []),
+    "mcbgpu_mlp_create": (C.c_int, [C.POINTER(vp), vp]),
+    "mcbgpu_mlp_get_params": (C.c_int, [vp, vp]),
+    "mcbgpu_mlp_forward": (C.c_int, [vp, vp, i64, vp, vp]),
+    "mcbgpu_mlp_gradients": (C.c_int, [vp, vp, vp, i64, C.c_float, vp, C.POINTER(C.c_float), vp]),
+    "mcbgpu_mlp_train_step": (C.c_int, [vp, vp, vp, i64, C.c_float, C.c_float, C.POINTER(C.c_float), vp]),
+    "mcbgpu_mlp_destroy": (C.c_int, [vp]),
 }
 
 

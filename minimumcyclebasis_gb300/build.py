@@ -27,7 +27,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 GPU_SOURCES = ["mcbgpu_runtime.cu", "mcbgpu_labels.cu", "mcbgpu_solver.cu", "mcbgpu_batch.cu", "mcbgpu_trees.cu",
-               "mcbgpu_gen.cu"]
+               "mcbgpu_gen.cu", "mcbgpu_mlp.cu"]
 
 
 def _nvcc() -> str:

@@ -244,20 +244,51 @@ __global__ void __launch_bounds__(kCandThreads) cand_write_kernel(GenGraph g, co
     }
 }
 
+__device__ __forceinline__ uint16_t to_bf16(float f) {
+    uint32_t u = __float_as_uint(f);
+    u += 0x7fffu + ((u >> 16) & 1u);  // round to nearest even (finite inputs)
+    return (uint16_t)(u >> 16);
+}
+
+// The learned proposal's 16 features of one candidate (bf16), from its walk: its
+// weight against the list's median weight, the two root distances and the edge
+// weight as shares of the weight, the path hop counts, the list length, its rank
+// quantile, the degrees of its root and ends.
+__device__ void candidate_features(uint16_t *f, float W, float wmed, float da, float db, float we, int ha, int hb,
+                                   int len, float quantile, int deg_root, int deg_ends) {
+    const float Wp = W > 0.0f ? W : 1.0f;
+    const float v[16] = {W / wmed,
+                         fminf(da, db) / Wp,
+                         fmaxf(da, db) / Wp,
+                         we / Wp,
+                         log2f(1.0f + (float)(ha + hb)) * 0.125f,
+                         log2f(1.0f + (float)len) * 0.125f,
+                         quantile,
+                         log2f(1.0f + (float)deg_root) * 0.25f,
+                         log2f(1.0f + (float)deg_ends) * 0.25f,
+                         fabsf((float)(ha - hb)) / (1.0f + (float)(ha + hb)),
+                         1.0f,
+                         0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int i = 0; i < 16; i++) f[i] = to_bf16(v[i]);
+}
+
 // Per rank: the coordinates of its cycle (its own edge's, then the root paths of its
-// two ends).  Without `out`, the count into len[r]; with it, the coordinates at
-// out[off[r] ...] in walk order.
+// two ends).  Without `out`, the count into len[r] (and with `feat`, the candidate's
+// features); with it, the coordinates at out[off[r] ...] in walk order.
 __global__ void __launch_bounds__(kWalkThreads) walk_kernel(GenGraph g, const int32_t *__restrict__ pedge, int64_t K,
                                                             const int32_t *__restrict__ tree,
                                                             const int32_t *__restrict__ eoff, int32_t *len,
                                                             const int64_t *__restrict__ off, int32_t *out,
-                                                            unsigned *status) {
+                                                            unsigned *status, uint16_t *feat,
+                                                            const int32_t *__restrict__ weight, float wmed) {
     const int n = g.n;
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < K; r += (int64_t)gridDim.x * blockDim.x) {
         const int32_t t = tree[r], o = eoff[r];
         if (t < 0 || t >= g.F || o < 0 || (int64_t)o >= g.slots) {
             atomicOr(status, ST_BAD_INPUT);
             if (!out) len[r] = 0;
+            if (feat) candidate_features(feat + r * 16, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0);
             continue;
         }
         const uint32_t src = g.roots[t];
@@ -276,6 +307,8 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(GenGraph g, const in
             c++;
         };
         emit(g.ec[o]);
+        float dist[2] = {0.0f, 0.0f};
+        int hops[2] = {0, 0};
         for (int side = 0; side < 2; side++) {
             uint32_t x = side ? g.cols[o] : g.rows[o];
             for (int steps = 0; x != src; steps++) {
@@ -285,10 +318,19 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(GenGraph g, const in
                     break;
                 }
                 emit(g.ec[q]);
+                dist[side] += (float)g.w[q];
+                hops[side]++;
                 x = g.rows[q];
             }
         }
         if (!out) len[r] = c;
+        if (feat) {
+            const uint32_t a = g.rows[o], b = g.cols[o];
+            const int deg_root = (int)(g.ro[src + 1] - g.ro[src]);
+            const int deg_ends = (int)(g.ro[a + 1] - g.ro[a] + g.ro[b + 1] - g.ro[b]);
+            candidate_features(feat + r * 16, (float)weight[r], wmed, dist[0], dist[1], (float)g.w[o], hops[0],
+                               hops[1], c, (float)r / (float)K, deg_root, deg_ends);
+        }
     }
 }
 
@@ -457,7 +499,7 @@ struct mcbgpu_gen {
     int64_t cand_cap = 0;
     int32_t cur_t0 = -1, cur_count = 0;
     // lists
-    int64_t K = 0, nnz = 0;
+    int64_t K = 0, K_lists = 0, nnz = 0;
     int32_t *d_tree = nullptr, *d_eoff = nullptr, *d_len = nullptr, *d_coords = nullptr, *d_weight = nullptr;
     int64_t *d_off = nullptr, *d_bsum = nullptr, *d_longs = nullptr;
     unsigned *d_nlong = nullptr;
@@ -769,40 +811,66 @@ int mcbgpu_gen_fetch(mcbgpu_gen *g, int64_t total, uint32_t *pair_index, int32_t
     return check_status(g, st, "mcbgpu_gen_fetch");
 }
 
-int mcbgpu_gen_lists(mcbgpu_gen *g, int64_t K, const int32_t *tree, const int32_t *edge_offset,
-                     const int32_t *weight, int64_t *nnz, void *stream) {
-    if (!g || K < 0 || (K > 0 && (!tree || !edge_offset || !weight)) || !nnz) {
-        set_error("mcbgpu_gen_lists: invalid arguments");
+int mcbgpu_gen_rank(mcbgpu_gen *g, int64_t K, const int32_t *tree, const int32_t *edge_offset,
+                    const int32_t *weight, uint16_t *features, void *stream) {
+    if (!g || K < 0 || (K > 0 && (!tree || !edge_offset || !weight))) {
+        set_error("mcbgpu_gen_rank: invalid arguments");
         return MCBGPU_E_ARG;
     }
     if (!g->d_pedge) {
-        set_error("mcbgpu_gen_lists: the trees were released");
+        set_error("mcbgpu_gen_rank: the trees were released");
         return MCBGPU_E_STATE;
     }
     cudaStream_t st = (cudaStream_t)stream;
     gen_free_lists(g);
     g->K = K;
+    g->K_lists = 0;
     g->nnz = 0;
+    const size_t k1 = (size_t)(K > 0 ? K : 1);
     const int64_t nblk = (K + (int64_t)kScanThreads * kScanItems - 1) / ((int64_t)kScanThreads * kScanItems);
-    MCB_CUDA(cudaMalloc((void **)&g->d_tree, 4 * (size_t)(K > 0 ? K : 1)));
-    MCB_CUDA(cudaMalloc((void **)&g->d_eoff, 4 * (size_t)(K > 0 ? K : 1)));
-    MCB_CUDA(cudaMalloc((void **)&g->d_len, 4 * (size_t)(K > 0 ? K : 1)));
-    MCB_CUDA(cudaMalloc((void **)&g->d_weight, 4 * (size_t)(K > 0 ? K : 1)));
+    MCB_CUDA(cudaMalloc((void **)&g->d_tree, 4 * k1));
+    MCB_CUDA(cudaMalloc((void **)&g->d_eoff, 4 * k1));
+    MCB_CUDA(cudaMalloc((void **)&g->d_len, 4 * k1));
+    MCB_CUDA(cudaMalloc((void **)&g->d_weight, 4 * k1));
     MCB_CUDA(cudaMalloc((void **)&g->d_off, 8 * (size_t)(K + 1)));
     MCB_CUDA(cudaMalloc((void **)&g->d_bsum, 8 * (size_t)(nblk + 1)));
-    if (K == 0) {
-        MCB_CUDA(cudaMemsetAsync(g->d_off, 0, 8, st));
-        *nnz = 0;
-        return MCBGPU_OK;
-    }
+    if (K == 0) return MCBGPU_OK;
     MCB_CUDA(cudaMemcpyAsync(g->d_tree, tree, 4 * (size_t)K, cudaMemcpyHostToDevice, st));
     MCB_CUDA(cudaMemcpyAsync(g->d_eoff, edge_offset, 4 * (size_t)K, cudaMemcpyHostToDevice, st));
     MCB_CUDA(cudaMemcpyAsync(g->d_weight, weight, 4 * (size_t)K, cudaMemcpyHostToDevice, st));
+    const float wmed = (float)(weight[K / 2] > 0 ? weight[K / 2] : 1);  // the list is sorted by weight
     const GenGraph gg = graph_of(g);
     const int wgrid = (int)std::min<long long>((K + kWalkThreads - 1) / kWalkThreads, (long long)g->sm_count * 16);
     walk_kernel<<<wgrid, kWalkThreads, 0, st>>>(gg, g->d_pedge, K, g->d_tree, g->d_eoff, g->d_len, nullptr, nullptr,
-                                                g->d_status);
+                                                g->d_status, features, g->d_weight, wmed);
     MCB_CUDA(cudaGetLastError());
+    return check_status(g, st, "mcbgpu_gen_rank");
+}
+
+int mcbgpu_gen_build_lists(mcbgpu_gen *g, int64_t K_keep, int64_t *nnz, void *stream) {
+    if (!g || !nnz || K_keep < 0 || K_keep > g->K || !g->d_len) {
+        set_error("mcbgpu_gen_build_lists: invalid arguments (mcbgpu_gen_rank first)");
+        return MCBGPU_E_ARG;
+    }
+    if (!g->d_pedge) {
+        set_error("mcbgpu_gen_build_lists: the trees were released");
+        return MCBGPU_E_STATE;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaFree(g->d_coords);
+    cudaFree(g->d_longs);
+    g->d_coords = nullptr;
+    g->d_longs = nullptr;
+    g->K_lists = K_keep;
+    g->nnz = 0;
+    if (K_keep == 0) {
+        MCB_CUDA(cudaMemsetAsync(g->d_off, 0, 8, st));
+        MCB_CUDA(cudaStreamSynchronize(st));
+        *nnz = 0;
+        return MCBGPU_OK;
+    }
+    const int64_t K = K_keep;
+    const int64_t nblk = (K + (int64_t)kScanThreads * kScanItems - 1) / ((int64_t)kScanThreads * kScanItems);
     block_sums_kernel<<<(unsigned)nblk, kScanThreads, 0, st>>>(g->d_len, K, g->d_bsum);
     MCB_CUDA(cudaGetLastError());
     scan_small_kernel<<<1, kScanThreads, 0, st>>>(g->d_bsum, (int)nblk, g->d_bsum);
@@ -811,11 +879,13 @@ int mcbgpu_gen_lists(mcbgpu_gen *g, int64_t K, const int32_t *tree, const int32_
     MCB_CUDA(cudaGetLastError());
     int64_t total = 0;
     MCB_CUDA(cudaMemcpyAsync(&total, g->d_off + K, 8, cudaMemcpyDeviceToHost, st));
-    int rc = check_status(g, st, "mcbgpu_gen_lists (lengths)");
+    int rc = check_status(g, st, "mcbgpu_gen_build_lists (offsets)");
     if (rc) return rc;
     MCB_CUDA(cudaMalloc((void **)&g->d_coords, 4 * (size_t)(total > 0 ? total : 1)));
+    const GenGraph gg = graph_of(g);
+    const int wgrid = (int)std::min<long long>((K + kWalkThreads - 1) / kWalkThreads, (long long)g->sm_count * 16);
     walk_kernel<<<wgrid, kWalkThreads, 0, st>>>(gg, g->d_pedge, K, g->d_tree, g->d_eoff, g->d_len, g->d_off,
-                                                g->d_coords, g->d_status);
+                                                g->d_coords, g->d_status, nullptr, nullptr, 1.0f);
     MCB_CUDA(cudaGetLastError());
     const unsigned long long cap_long = (unsigned long long)(K < 65536 ? K : 65536);
     MCB_CUDA(cudaMalloc((void **)&g->d_longs, 8 * (size_t)cap_long));
@@ -827,25 +897,37 @@ int mcbgpu_gen_lists(mcbgpu_gen *g, int64_t K, const int32_t *tree, const int32_
     MCB_CUDA(cudaMemcpyAsync(&nlong, g->d_nlong, 4, cudaMemcpyDeviceToHost, st));
     MCB_CUDA(cudaStreamSynchronize(st));
     if (nlong > cap_long) {
-        set_error("mcbgpu_gen_lists: %u lists longer than %d entries (at most %llu)", nlong, kSortWarpMax, cap_long);
+        set_error("mcbgpu_gen_build_lists: %u lists longer than %d entries (at most %llu)", nlong, kSortWarpMax,
+                  cap_long);
         return MCBGPU_E_ARG;
     }
     if (nlong > 0) {
-        sort_long_kernel<<<std::min<unsigned>(nlong, (unsigned)g->sm_count), 1024, sizeof(int32_t) * kSortLongMax, st>>>(
-            g->d_off, g->d_coords, g->d_longs, (int)nlong, g->d_status);
+        sort_long_kernel<<<std::min<unsigned>(nlong, (unsigned)g->sm_count), 1024, sizeof(int32_t) * kSortLongMax,
+                           st>>>(g->d_off, g->d_coords, g->d_longs, (int)nlong, g->d_status);
         MCB_CUDA(cudaGetLastError());
     }
-    rc = check_status(g, st, "mcbgpu_gen_lists");
+    rc = check_status(g, st, "mcbgpu_gen_build_lists");
     if (rc) return rc;
     g->nnz = total;
     *nnz = total;
     return MCBGPU_OK;
 }
 
+int mcbgpu_gen_lists(mcbgpu_gen *g, int64_t K, const int32_t *tree, const int32_t *edge_offset,
+                     const int32_t *weight, int64_t *nnz, void *stream) {
+    if (!nnz) {
+        set_error("mcbgpu_gen_lists: NULL nnz");
+        return MCBGPU_E_ARG;
+    }
+    int rc = mcbgpu_gen_rank(g, K, tree, edge_offset, weight, nullptr, stream);
+    if (rc) return rc;
+    return mcbgpu_gen_build_lists(g, K, nnz, stream);
+}
+
 int mcbgpu_gen_get_lists(const mcbgpu_gen *g, const int32_t **weight, const int64_t **offsets,
                          const int32_t **coords) {
-    if (!g || !weight || !offsets || !coords || !g->d_off) {
-        set_error("mcbgpu_gen_get_lists: no lists (mcbgpu_gen_lists first)");
+    if (!g || !weight || !offsets || !coords || !g->d_off || (g->K_lists > 0 && !g->d_coords)) {
+        set_error("mcbgpu_gen_get_lists: no lists (mcbgpu_gen_build_lists first)");
         return MCBGPU_E_STATE;
     }
     *weight = g->d_weight;
@@ -855,12 +937,12 @@ int mcbgpu_gen_get_lists(const mcbgpu_gen *g, const int32_t **weight, const int6
 }
 
 int mcbgpu_gen_copy_lists(const mcbgpu_gen *g, int64_t *offsets, int32_t *coords, void *stream) {
-    if (!g || !offsets || (g->nnz > 0 && !coords) || !g->d_off) {
+    if (!g || !offsets || (g->nnz > 0 && !coords) || !g->d_off || (g->K_lists > 0 && !g->d_coords)) {
         set_error("mcbgpu_gen_copy_lists: invalid arguments or no lists");
         return MCBGPU_E_ARG;
     }
     cudaStream_t st = (cudaStream_t)stream;
-    MCB_CUDA(cudaMemcpyAsync(offsets, g->d_off, 8 * (size_t)(g->K + 1), cudaMemcpyDeviceToHost, st));
+    MCB_CUDA(cudaMemcpyAsync(offsets, g->d_off, 8 * (size_t)(g->K_lists + 1), cudaMemcpyDeviceToHost, st));
     if (g->nnz > 0)
         MCB_CUDA(cudaMemcpyAsync(coords, g->d_coords, 4 * (size_t)g->nnz, cudaMemcpyDeviceToHost, st));
     MCB_CUDA(cudaStreamSynchronize(st));

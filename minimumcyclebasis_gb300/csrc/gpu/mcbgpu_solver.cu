@@ -114,7 +114,8 @@ struct IterSlot {            // state of one per-iteration search
 };
 
 struct BlockState {
-    unsigned rank, epoch, b, pad0_;
+    unsigned rank, epoch, b;
+    unsigned failed;               // a block ran out of candidates: every later block's kernels return at once
     long long last_pivot;          // rank of the previous block's last pivot
     long long pred_tiles;          // tiles the streaming pass computes for this block
     long long max_tile;            // deepest tile the previous block's pivot search touched
@@ -148,6 +149,7 @@ __global__ void reset_state_kernel(IterSlot *slots, BlockState *bs, unsigned *st
         slots[1].best = kNone;
         slots[1].next_tile = 0;
         bs->total = 0;  // epoch keeps counting across runs: old tile marks never match
+        bs->failed = 0;
         *status = 0;
     }
 }
@@ -355,6 +357,13 @@ __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int 
                                      uint64_t *__restrict__ T, BlockState *bs, long long ntiles,
                                      GridBar *gb, long long window_tiles, uint64_t *__restrict__ Tg, int b1,
                                      int Wb1, int b2, int Wb2) {
+    if (*(volatile const unsigned *)&bs->failed) {  // set by an earlier block's pivot kernel (same stream)
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            bs->pred_tiles = 0;  // the streaming pass and its correction then cover no tile
+            bs->pair_tiles = 0;
+        }
+        return;
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         gb->count = 0;
         gb->abort = 0;
@@ -1162,6 +1171,9 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
     __shared__ int s_nnew;
     __shared__ unsigned long long sr_rank[kLmax], sr_w[kLmax];
 
+    // an earlier block ran out of candidates (flag written by an earlier launch, so
+    // every CTA reads the same value and none waits at a grid barrier)
+    if (*(volatile const unsigned *)&bs->failed) return;
     unsigned long long n_loaded = 0, n_computed = 0, n_local = 0, n_cand = 0;
     long long cyc_scan = 0, cyc_bar = 0, cyc_merge = 0;
     unsigned long long nbar = 0;
@@ -1501,7 +1513,10 @@ __global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
             fr_build(gtab, gbasis, gpiv, (unsigned)grank);
         }
         if (nnew == 0 && D >= (unsigned long long)K) {
-            if (c == 0 && threadIdx.x == 0) atomicOr(status, ST_RANK_DEFICIT);
+            if (c == 0 && threadIdx.x == 0) {
+                atomicOr(status, ST_RANK_DEFICIT);
+                bs->failed = 1;
+            }
             ok = false;
             break;
         }

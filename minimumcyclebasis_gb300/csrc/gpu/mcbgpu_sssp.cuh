@@ -11,13 +11,16 @@
 // every weight at least 1 and every distance below 2^31 (checked at creation).
 //
 // One CTA per root, persistent over a root counter:
-//   1. distances, label-correcting by buckets: each round takes lo = the smallest
-//      distance among dirty vertices and relaxes (atomicMin) the arcs of every dirty
-//      vertex nearer than lo + delta, marking improved heads dirty.  The dirty vertex
-//      at lo is final after its round (weights >= 1), so a root needs at most n
-//      rounds; the loop stops there and flags the root if it has not converged.
-//      Distances and dirty bits live in shared memory up to kTreeSharedMaxN vertices,
-//      in a per-CTA global slice beyond.
+//   1. distances, label-correcting by buckets: each round takes lo = (a lower
+//      bound of) the smallest distance among dirty vertices and relaxes (atomicMin)
+//      the arcs of every dirty vertex nearer than lo + delta, marking improved heads
+//      dirty.  The dirty vertex at lo is final after its round (weights >= 1), so a
+//      root needs at most 2 (n + 1) rounds; the loop stops there and flags the root
+//      if it has not converged.  Distances and dirty bits live in shared memory up
+//      to kTreeSharedMaxN vertices, in a per-CTA global slice beyond.  delta (the
+//      bucket width) trades rounds (each a pass over the dirty bits and a barrier)
+//      against relaxations repeated inside a bucket; the callers time a few widths
+//      and CTA shapes on their first roots and keep the fastest.
 //   2. parents: for each vertex c, among its neighbours x on a shortest path
 //      (d[x] + w = d[c]) the nearest one, entered through its first slot to c (the
 //      smallest slot index of x's row among those arcs); the reference keeps exactly
@@ -40,8 +43,9 @@ namespace sssp {
 // kernel, registered with its own module
 namespace {
 
-constexpr int kTreeThreads = 1024;
+constexpr int kTreeThreads = 1024;      // the shared-memory form's CTA
 constexpr int kTreeSharedMaxN = 53248;  // 208 KB of distances + 6.5 KB of dirty bits (of 227 KB)
+constexpr int kTreeMaxCtasPerSm = 8;    // the global form's per-CTA slices are sized for this many
 
 struct TreeArgs {
     const uint32_t *ro;
@@ -61,24 +65,13 @@ struct TreeArgs {
     unsigned *status;
 };
 
-__device__ __forceinline__ int block_min(int v, int *red) {
-    v = __reduce_min_sync(0xffffffffu, v);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) red[warp] = v;
-    cta_sync();
-    if (warp == 0) {
-        int x = lane < (int)(blockDim.x >> 5) ? red[lane] : INT_MAX;
-        x = __reduce_min_sync(0xffffffffu, x);
-        if (lane == 0) red[32] = x;
-    }
-    cta_sync();
-    return red[32];
-}
-
-template <bool kShared>
-__global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
+// Threads per CTA: the shared-memory form runs one 1024-thread CTA per SM (its
+// distances fill the shared memory); the global form runs kThreads-thread CTAs,
+// several per SM, so that the bucket rounds of different roots overlap.
+template <bool kShared, int kThreads>
+__global__ void __launch_bounds__(kThreads) trees_kernel(TreeArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_red[33];
+    __shared__ int s_next[3];
     __shared__ int s_root;
     const int n = a.n;
     const int words = (n + 31) >> 5;
@@ -93,7 +86,7 @@ __global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
     }
     volatile int32_t *vdist = dist;
     volatile uint32_t *vdirty = dirty;
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
     for (;;) {
         if (tid == 0) s_root = atomicAdd(a.next_root, 1);
         cta_sync();
@@ -103,38 +96,47 @@ __global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
         const uint32_t src = a.roots[r];  // < n, checked by the host
         for (int v = tid; v < n; v += nt) dist[v] = INT_MAX;
         for (int k = tid; k < words; k += nt) dirty[k] = 0;
+        if (tid == 0) {
+            s_next[0] = INT_MAX;
+            s_next[1] = INT_MAX;
+        }
         cta_sync();
         if (tid == 0) {
             dist[src] = 0;
             dirty[src >> 5] = 1u << (src & 31);
         }
         cta_sync();
-        // 1. distances
+        // 1. distances.  One pass per round over the dirty bits: vertices nearer than
+        // hi = lo + delta are relaxed, the others skipped; the next round's lo is the
+        // smallest distance of a skipped vertex or of an improvement made in this
+        // round (at most the smallest distance left dirty, so no vertex is missed;
+        // an underestimate only costs a round).  The dirty vertex at the true lo is
+        // final once relaxed (weights >= 1), so at most 2 (n + 1) rounds; the loop
+        // stops there and flags the root if it has not converged.  The round's
+        // minimum goes to s_next[round % 3]: the slot read after this round's
+        // barrier, reset two rounds later, when every thread has read it.
         bool converged = false;
-        for (int round = 0; round <= n; round++) {
-            int m = INT_MAX;
-            for (int k = tid; k < words; k += nt) {
-                uint32_t bits = vdirty[k];
-                while (bits) {
-                    const int b = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    const int d = vdist[(k << 5) + b];
-                    m = d < m ? d : m;
-                }
-            }
-            const int lo = block_min(m, s_red);
+        int lo = 0;
+        for (int round = 0; round <= 2 * n + 1; round++) {
             if (lo == INT_MAX) {
                 converged = true;
                 break;
             }
             const int hi = lo > INT_MAX - a.delta ? INT_MAX : lo + a.delta;
+            const int slot = round % 3;
+            if (tid == 0) s_next[(round + 1) % 3] = INT_MAX;
+            int mynext = INT_MAX;
             for (int k = tid; k < words; k += nt) {
                 uint32_t bits = vdirty[k];
                 while (bits) {
                     const int b = __ffs(bits) - 1;
                     bits &= bits - 1;
                     const int v = (k << 5) + b;
-                    if (vdist[v] >= hi) continue;
+                    const int d0 = vdist[v];
+                    if (d0 >= hi) {
+                        mynext = d0 < mynext ? d0 : mynext;
+                        continue;
+                    }
                     atomicAnd(&dirty[k], ~(1u << b));
                     // pairs with the fence between a writer's atomicMin and atomicOr:
                     // a bit this atomicAnd cleared was set after its distance was
@@ -150,12 +152,16 @@ __global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
                             if (nd < old) {
                                 __threadfence_block();  // the new distance before the dirty bit
                                 atomicOr(&dirty[x >> 5], 1u << (x & 31));
+                                mynext = nd < mynext ? nd : mynext;
                             }
                         }
                     }
                 }
             }
+            mynext = __reduce_min_sync(0xffffffffu, mynext);
+            if (lane == 0 && mynext != INT_MAX) atomicMin(&s_next[slot], mynext);
             cta_sync();
+            lo = s_next[slot];
         }
         // 2. parents by the rule, and the root's tie flag
         int tie = converged ? 0 : 1;
@@ -193,6 +199,40 @@ __global__ void __launch_bounds__(kTreeThreads, 1) trees_kernel(TreeArgs a) {
         if (tid == 0) a.tied_out[r] = tie ? 1 : 0;
         if (!converged && tid == 0) atomicOr(a.status, ST_DIVERGED);
     }
+}
+
+// A launch shape of trees_kernel: CTA size, CTAs per SM (global form) and the
+// bucket width as a multiple of the mean edge weight, in quarters.
+struct TreeShape {
+    int threads, ctas_per_sm, delta_quarters;
+};
+
+// The bucket width of a shape on a graph whose mean slot weight is mean_w.
+inline int32_t shape_delta(const TreeShape &sh, int32_t mean_w) {
+    const long long d = ((long long)mean_w * sh.delta_quarters + 3) / 4;
+    return (int32_t)(d < 1 ? 1 : d > (1ll << 30) ? (1ll << 30) : d);
+}
+
+// Launches trees_kernel in `shape` over grid CTAs (the shared form: 1024 threads,
+// smem bytes of dynamic shared memory).
+inline cudaError_t launch_trees(bool shared, const TreeShape &shape, int grid, size_t smem, cudaStream_t st,
+                                const TreeArgs &a) {
+    if (shared) {
+        trees_kernel<true, kTreeThreads><<<grid, kTreeThreads, smem, st>>>(a);
+    } else {
+        switch (shape.threads) {
+        case 128: trees_kernel<false, 128><<<grid, 128, 0, st>>>(a); break;
+        case 256: trees_kernel<false, 256><<<grid, 256, 0, st>>>(a); break;
+        case 512: trees_kernel<false, 512><<<grid, 512, 0, st>>>(a); break;
+        default: trees_kernel<false, 1024><<<grid, 1024, 0, st>>>(a); break;
+        }
+    }
+    return cudaGetLastError();
+}
+
+inline cudaError_t set_trees_smem_limit() {
+    return cudaFuncSetAttribute(trees_kernel<true, kTreeThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)((size_t)kTreeSharedMaxN * 4 + (size_t)(kTreeSharedMaxN / 32) * 4));
 }
 
 }  // namespace

@@ -108,8 +108,8 @@ int mcbgpu_trees_create(mcbgpu_trees **out, int32_t nodes, int64_t slots, const 
     TALLOC(t->d_next, 4);
     TALLOC(t->d_status, 4);
     if (!t->shared_form) {
-        TALLOC(t->d_gdist, 4 * per_root * (size_t)t->sm_count);
-        TALLOC(t->d_gdirty, 4 * (size_t)words * (size_t)t->sm_count);
+        TALLOC(t->d_gdist, 4 * per_root * (size_t)t->sm_count * kTreeMaxCtasPerSm);
+        TALLOC(t->d_gdirty, 4 * (size_t)words * (size_t)t->sm_count * kTreeMaxCtasPerSm);
     }
 #undef TALLOC
     if (e == cudaSuccess) e = cudaMemcpy(t->d_ro, row_offsets, 4 * ((size_t)nodes + 1), cudaMemcpyHostToDevice);
@@ -120,9 +120,7 @@ int mcbgpu_trees_create(mcbgpu_trees **out, int32_t nodes, int64_t slots, const 
     }
     // the kernel's attribute is process-wide: set to the largest shared form, so that
     // handles of different sizes can be used in any order
-    if (e == cudaSuccess && t->shared_form)
-        e = cudaFuncSetAttribute(trees_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)((size_t)kTreeSharedMaxN * 4 + (size_t)(kTreeSharedMaxN / 32) * 4));
+    if (e == cudaSuccess && t->shared_form) e = set_trees_smem_limit();
     if (e != cudaSuccess) {
         const int rc = cuda_fail(e, "mcbgpu_trees_create");
         trees_free(t);
@@ -154,7 +152,8 @@ int mcbgpu_trees_run(mcbgpu_trees *t, const uint32_t *roots, int32_t count, int3
     a.w = t->d_w;
     a.rev = t->d_rev;
     a.n = t->n;
-    a.delta = t->delta;
+    const TreeShape shape = t->shared_form ? TreeShape{kTreeThreads, 1, 4} : TreeShape{256, 4, 8};
+    a.delta = shape_delta(shape, t->delta);
     a.roots = t->d_roots;
     a.count = count;
     a.dist_out = t->d_dist;
@@ -164,12 +163,9 @@ int mcbgpu_trees_run(mcbgpu_trees *t, const uint32_t *roots, int32_t count, int3
     a.gdirty = t->d_gdirty;
     a.next_root = t->d_next;
     a.status = t->d_status;
-    const int grid = count < t->sm_count ? count : t->sm_count;
-    if (t->shared_form)
-        trees_kernel<true><<<grid, kTreeThreads, t->smem, st>>>(a);
-    else
-        trees_kernel<false><<<grid, kTreeThreads, 0, st>>>(a);
-    MCB_CUDA(cudaGetLastError());
+    const int slots_ = t->sm_count * shape.ctas_per_sm;
+    const int grid = count < slots_ ? count : slots_;
+    MCB_CUDA(launch_trees(t->shared_form, shape, grid, t->smem, st, a));
     const size_t cells = (size_t)count * (size_t)t->n;
     MCB_CUDA(cudaMemcpyAsync(dist, t->d_dist, 4 * cells, cudaMemcpyDeviceToHost, st));
     MCB_CUDA(cudaMemcpyAsync(parent_slot, t->d_pedge, 4 * cells, cudaMemcpyDeviceToHost, st));
