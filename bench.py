@@ -385,6 +385,52 @@ def plain_form(solver, N, stream, sh, windows=8, width=128):
             "ms_per_iteration": [round(x * 1e3, 4) for x in per_iter]}
 
 
+def learned_form(args, g, sel0, tot0, sh):
+    """Trains the proposal network on traces of --train-graphs smaller graphs of the
+    workload's family (seeds after the workload's), then solves the workload graph
+    -> basis with the proposal's prefix.  Returns (the line's `learned` object, the
+    solver holding the prefix lists, the prefix lists' host copies, graph-to-basis
+    seconds of the learned form)."""
+    import numpy as np
+
+    from minimumcyclebasis_gb300.learned import ProposalNet, solve_with_proposal, traces, train
+    small = argparse.Namespace(**vars(args))
+    small.n = args.train_n
+    t0 = time.perf_counter()
+    xs, ys, ks = [], [], []
+    for i in range(args.train_graphs):
+        small.seed = args.seed + 1000 + i
+        x, y, res = traces(make_graph(small))
+        xs.append(x)
+        ys.append(y)
+        ks.append(res.K)
+    t_traces = time.perf_counter() - t0
+    net = ProposalNet(seed=args.seed)
+    t1 = time.perf_counter()
+    losses = train(net, xs, ys, epochs=args.train_epochs)
+    t_train = time.perf_counter() - t1
+    del xs, ys
+    untrained = ProposalNet(seed=args.seed)
+    # graph -> basis on the proposal's prefix (its lists copied to the host afterwards,
+    # for the end-to-end steps; the untrained network's prefix on the same features
+    # for comparison: neither is part of the timed solve)
+    r, lsolver, p = solve_with_proposal(g, net, margin=args.margin, stream=sh, keep_solver=True, host_lists=True,
+                                        compare=[untrained])
+    g2b = r.times["total"]
+    assert np.array_equal(r.selected, sel0) and r.total_weight == tot0, "the learned form's basis differs"
+    uk, _ = r.compared[0]
+    learned = {"skip_rate": r.skip_rate, "diffs": 0, "fallback": r.fallback, "K": r.K, "K_kept": r.K_kept,
+               "U": r.U, "nnz_kept": r.nnz_kept, "trees": r.trees, "trees_kept": r.trees_kept,
+               "margin": args.margin, "untrained_skip_rate": 1.0 - uk / max(r.K, 1),
+               "training": {"graphs": args.train_graphs, "points": args.train_n, "candidates": int(sum(ks)),
+                            "epochs": args.train_epochs, "loss_first_last": [round(losses[0], 4),
+                                                                             round(losses[-1], 4)],
+                            "traces_s": round(t_traces, 2), "train_s": round(t_train, 2)},
+               "times_s": {k: round(v, 3) for k, v in r.times.items()}}
+    untrained.close()
+    return learned, lsolver, r.lists, g2b
+
+
 def run_gpu(args, world, rank, local, pg):
     import numpy as np
     import torch
@@ -403,10 +449,12 @@ def run_gpu(args, world, rank, local, pg):
     # graph -> basis, once: preparation + solve + results
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    tree_shapes = None
     if args.prep == "device":
         dp, gen = prepare_on_device(g, threads=0, stream=sh, keep_gen=True)
         p, solver = dp.problem, dp.solver
         prep_times = dict(dp.times)
+        tree_shapes = dp.tree_shapes
     else:
         p = Problem.from_graph(g).prepare(threads=0)
         i = p.info
@@ -465,10 +513,47 @@ def run_gpu(args, world, rank, local, pg):
         ms = max_over_ranks(ms, pg)
         pg.barrier()
 
+    # the learned proposal: a network trained on traces of smaller graphs of the same
+    # family (its own kernels), then the graph -> basis solve on the proposal's
+    # prefix of the rank order, checked against the full list's basis
+    learned = None
+    lsolver = None
+    if args.learned and args.prep == "device" and args.max_iterations < 0:
+        learned, lsolver, lists_l, lg2b = learned_form(args, g, sel0, tot0, sh)
+
     plain = None
     if not args.no_plain and args.max_iterations < 0:
         plain = plain_form(solver, p.N, stream, sh, windows=args.plain_windows, width=args.plain_width)
         plain["speedup"] = plain["value"] / (ms / 1e3)
+
+    full_ms = ms
+    if lsolver is not None:
+        # the learned form's solve on its resident prefix lists, timed as above
+        for _ in range(args.warmup):
+            lsolver.reset(sh)
+            lsolver.run(-1, sh)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            lsolver.reset(sh)
+            lsolver.run(-1, sh)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        lms = ev0.elapsed_time(ev1) / args.steps
+        lsel, ltot = lsolver.results(stream=sh)
+        assert np.array_equal(lsel, sel0) and ltot == tot0, "the learned form's solve differs"
+        learned["solve_s"] = lms / 1e3
+        learned["solve_s_full_list"] = full_ms / 1e3
+        if pg:
+            lms = max_over_ranks(lms, pg)
+        if lms < ms:  # the fastest form is the line's value; its lists feed the e2e below
+            ms = lms
+            solver.close()
+            solver = lsolver
+            w, off, co = lists_l
+            learned["is_value"] = True
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
@@ -541,10 +626,13 @@ def run_gpu(args, world, rank, local, pg):
             "clocks": clocks.summary(), "e2e": e2e,
             "e2e_with_preparation": {"value": graph_to_basis, "unit": "s", "runs": 1,
                                      "preparation_s": {k: round(v, 3) for k, v in prep_times.items()},
-                                     "tied_roots_searched_on_host": tied,
+                                     "tied_roots_searched_on_host": tied, "tree_kernel_shapes": tree_shapes,
+                                     "learned_form": lg2b if learned else None,
                                      "note": "graph edge arrays in host memory -> basis in host memory: "
-                                             "preparation + solve + results, measured once"},
-            "plain_gpu": plain, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cb}
+                                             "preparation + solve + results, measured once (learned_form: the "
+                                             "same with the proposal's prefix, the network trained beforehand)"},
+            "plain_gpu": plain, "learned": learned, "gpu_launches": int(launches), "roofline": roofline,
+            "cpu_baseline": cb}
 
 
 def run_batch(args, world, rank, local, pg):
@@ -749,6 +837,12 @@ def main():
     ap.add_argument("--prep", choices=["device", "host"], default="device",
                     help="candidate generation on the GPU (default) or on the host")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-iteration form's timing")
+    ap.add_argument("--no-learned", dest="learned", action="store_false",
+                    help="skip the learned proposal's form")
+    ap.add_argument("--train-graphs", type=int, default=3, help="graphs whose traces train the proposal")
+    ap.add_argument("--train-n", type=int, default=20000, help="size (--n units) of the training graphs")
+    ap.add_argument("--train-epochs", type=int, default=20)
+    ap.add_argument("--margin", type=float, default=0.05, help="proposals: ceil(N (1 + margin)) top scores")
     ap.add_argument("--plain-windows", type=int, default=8)
     ap.add_argument("--plain-width", type=int, default=128)
     ap.add_argument("--batch-count", type=int, default=4096)

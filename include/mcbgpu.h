@@ -322,6 +322,13 @@ int mcbgpu_gen_lists(mcbgpu_gen *g, int64_t K, const int32_t *tree, const int32_
                      const int32_t *weight, int64_t *nnz, void *stream);
 int mcbgpu_gen_get_lists(const mcbgpu_gen *g, const int32_t **weight, const int64_t **offsets,
                          const int32_t **coords);
+/* The tree kernel's launch shapes (threads per CTA, CTAs per SM, bucket width in
+ * quarters of the mean edge weight; 3 int32 each, up to cap), their measured
+ * microseconds per root (-1: not tried) and the index of the one in use (-1: still
+ * tuning).  While tuning, the first calls of mcbgpu_gen_trees each try one shape
+ * on their chunk (every shape gives the same trees); then the fastest is kept. */
+int mcbgpu_gen_tree_shapes(const mcbgpu_gen *g, int32_t *shapes, double *us_per_root, int32_t cap, int32_t *count,
+                           int32_t *chosen);
 /* The lists copied into host memory: offsets (K + 1) and coordinates (nnz). */
 int mcbgpu_gen_copy_lists(const mcbgpu_gen *g, int64_t *offsets, int32_t *coords, void *stream);
 /* Frees the resident parent slots (after the lists are built). */

@@ -137,6 +137,7 @@ GPU_SYMBOLS = {
     "mcbgpu_gen_lists": (C.c_int, [vp, i64, vp, vp, vp, C.POINTER(i64), vp]),
     "mcbgpu_gen_get_lists": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
     "mcbgpu_gen_copy_lists": (C.c_int, [vp, vp, vp, vp]),
+    "mcbgpu_gen_tree_shapes": (C.c_int, [vp, vp, vp, i32, C.POINTER(i32), C.POINTER(i32)]),
     "mcbgpu_gen_release_trees": (C.c_int, [vp]),
     "mcbgpu_gen_device_bytes": (i64, [vp]),
     "mcbgpu_gen_destroy": (C.c_int, [vp]),

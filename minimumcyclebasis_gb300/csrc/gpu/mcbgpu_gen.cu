@@ -479,7 +479,13 @@ struct mcbgpu_gen {
     int sm_count = 0;
     bool shared_form = true;
     size_t smem = 0;
-    int delta = 1;
+    int delta = 1;  // the mean slot weight
+    // launch shapes of the tree kernel: while tuning, call i of mcbgpu_gen_trees
+    // runs shapes[i] and records its time per root; then the fastest is kept
+    std::vector<TreeShape> shapes;
+    std::vector<double> shape_us;  // microseconds per root, per shape tried
+    int chosen = -1;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // graph
     uint32_t *d_ro = nullptr, *d_rows = nullptr, *d_cols = nullptr, *d_rev = nullptr, *d_pairs = nullptr,
              *d_roots = nullptr;
@@ -522,6 +528,8 @@ static void gen_free_lists(mcbgpu_gen *g) {
 }
 
 static void gen_free(mcbgpu_gen *g) {
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
     void *ps[] = {g->d_ro,   g->d_rows,    g->d_cols,   g->d_rev,    g->d_pairs,  g->d_roots,  g->d_w,
                   g->d_ec,   g->d_fvs,     g->d_pedge,  g->d_dist,   g->d_code,   g->d_jump,   g->d_bits,
                   g->d_gdist, g->d_next,   g->d_gdirty, g->d_tied,   g->d_counts, g->d_coff,   g->d_cpair,
@@ -665,9 +673,19 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
     GALLOC(g->d_status, 4);
     GALLOC(g->d_nlong, 4);
     if (!g->shared_form) {
-        GALLOC(g->d_gdist, 4 * n * (size_t)g->sm_count);
-        GALLOC(g->d_gdirty, 4 * (size_t)words * (size_t)g->sm_count);
+        GALLOC(g->d_gdist, 4 * n * (size_t)g->sm_count * kTreeMaxCtasPerSm);
+        GALLOC(g->d_gdirty, 4 * (size_t)words * (size_t)g->sm_count * kTreeMaxCtasPerSm);
     }
+    // shapes the tuner tries (the shared form: one 1024-thread CTA per SM, bucket
+    // widths only); with fewer chunks than twice the shapes, the first one is kept
+    if (g->shared_form)
+        g->shapes = {{kTreeThreads, 1, 4}, {kTreeThreads, 1, 8}, {kTreeThreads, 1, 16}, {kTreeThreads, 1, 2}};
+    else
+        g->shapes = {{256, 4, 8}, {256, 4, 32}, {256, 8, 16}, {128, 8, 16}, {512, 2, 16}, {1024, 1, 4}};
+    const int nchunks = (fvs_size + g->chunk - 1) / g->chunk;
+    if (nchunks < 2 * (int)g->shapes.size()) g->chosen = 0;
+    if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&g->ev1);
 #undef GALLOC
     auto up = [&](void *dst, const void *src, size_t b) {
         if (e == cudaSuccess) e = cudaMemcpy(dst, src, b, cudaMemcpyHostToDevice);
@@ -682,9 +700,7 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
     up(g->d_pairs, pair_slot, 4 * (size_t)npairs);
     up(g->d_roots, fvs_vertices, 4 * (size_t)fvs_size);
     if (e == cudaSuccess) e = cudaMemset(g->d_status, 0, 4);
-    if (e == cudaSuccess && g->shared_form)
-        e = cudaFuncSetAttribute(trees_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)((size_t)kTreeSharedMaxN * 4 + (size_t)(kTreeSharedMaxN / 32) * 4));
+    if (e == cudaSuccess && g->shared_form) e = set_trees_smem_limit();
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(sort_long_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(int32_t) * kSortLongMax));
@@ -713,8 +729,11 @@ int mcbgpu_gen_trees(mcbgpu_gen *g, int32_t t0, int32_t count, uint8_t *tied, vo
     a.cols = g->d_cols;
     a.w = g->d_w;
     a.rev = g->d_rev;
+    // the shape of this call: the next untried one while tuning, else the chosen one
+    const int si = g->chosen >= 0 ? g->chosen : (int)g->shape_us.size();
+    const TreeShape shape = g->shapes[(size_t)si];
     a.n = g->n;
-    a.delta = g->delta;
+    a.delta = shape_delta(shape, g->delta);
     a.roots = g->d_roots + t0;
     a.count = count;
     a.dist_out = g->d_dist;
@@ -724,16 +743,24 @@ int mcbgpu_gen_trees(mcbgpu_gen *g, int32_t t0, int32_t count, uint8_t *tied, vo
     a.gdirty = g->d_gdirty;
     a.next_root = g->d_next;
     a.status = g->d_status;
-    const int grid = count < g->sm_count ? count : g->sm_count;
-    if (g->shared_form)
-        trees_kernel<true><<<grid, kTreeThreads, g->smem, st>>>(a);
-    else
-        trees_kernel<false><<<grid, kTreeThreads, 0, st>>>(a);
-    MCB_CUDA(cudaGetLastError());
+    const int cap = g->sm_count * shape.ctas_per_sm;
+    const int grid = count < cap ? count : cap;
+    MCB_CUDA(cudaEventRecord(g->ev0, st));
+    MCB_CUDA(launch_trees(g->shared_form, shape, grid, g->smem, st, a));
+    MCB_CUDA(cudaEventRecord(g->ev1, st));
     MCB_CUDA(cudaMemcpyAsync(tied, g->d_tied, (size_t)count, cudaMemcpyDeviceToHost, st));
     g->cur_t0 = t0;
     g->cur_count = count;
-    return check_status(g, st, "mcbgpu_gen_trees");
+    const int rc = check_status(g, st, "mcbgpu_gen_trees");
+    if (rc) return rc;
+    if (g->chosen < 0) {
+        float ms = 0;
+        MCB_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+        g->shape_us.push_back(1e3 * (double)ms / count);
+        if (g->shape_us.size() == g->shapes.size())
+            g->chosen = (int)(std::min_element(g->shape_us.begin(), g->shape_us.end()) - g->shape_us.begin());
+    }
+    return MCBGPU_OK;
 }
 
 int mcbgpu_gen_put_trees(mcbgpu_gen *g, const int32_t *trees, int32_t count, const int32_t *dist,
@@ -954,6 +981,23 @@ int mcbgpu_gen_release_trees(mcbgpu_gen *g) {
     cudaFree(g->d_pedge);
     g->d_pedge = nullptr;
     g->bytes -= 4ll * g->n * g->F;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_gen_tree_shapes(const mcbgpu_gen *g, int32_t *shapes, double *us_per_root, int32_t cap, int32_t *count,
+                           int32_t *chosen) {
+    if (!g || !count || !chosen || (cap > 0 && (!shapes || !us_per_root))) {
+        set_error("mcbgpu_gen_tree_shapes: invalid arguments");
+        return MCBGPU_E_ARG;
+    }
+    *count = (int32_t)g->shapes.size();
+    *chosen = g->chosen;
+    for (int32_t i = 0; i < cap && i < *count; i++) {
+        shapes[3 * i] = g->shapes[(size_t)i].threads;
+        shapes[3 * i + 1] = g->shapes[(size_t)i].ctas_per_sm;
+        shapes[3 * i + 2] = g->shapes[(size_t)i].delta_quarters;
+        us_per_root[i] = (size_t)i < g->shape_us.size() ? g->shape_us[(size_t)i] : -1.0;
+    }
     return MCBGPU_OK;
 }
 

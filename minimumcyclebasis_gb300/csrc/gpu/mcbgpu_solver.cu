@@ -1686,6 +1686,98 @@ __global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, lo
     if (lane == 0 && nb) atomicAdd(bytes, nb);
 }
 
+// The update of the next block's rows (at most 3 x 64, on the critical path: the
+// next block's transpose reads them), spread over the whole GPU in two launches
+// instead of blk_update_kernel's one warp group per 8 rows.
+// near_d_kernel: D_j = <C_sel_k, S_j> bits for every near row j, one (row, chunk of
+// kNearChunk pairs) item per warp, XOR-accumulated into Dbuf[j - row_begin] (which
+// near_apply_kernel clears after use).
+constexpr int kNearPer = 16;               // pairs per lane of an item
+constexpr int kNearChunk = 32 * kNearPer;  // pairs per item
+constexpr int kNearMaxRows = 192;
+
+__global__ void __launch_bounds__(256) near_d_kernel(const uint64_t *__restrict__ S, long long row_begin, int nrows,
+                                                    int P, const unsigned *__restrict__ pairs,
+                                                    const unsigned *__restrict__ word_end,
+                                                    unsigned long long *Dbuf, unsigned long long *bytes) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const unsigned npmax = __ldg(word_end + P);
+    const long long chunks = (npmax + kNearChunk - 1) / kNearChunk;
+    unsigned long long nb = 0;
+    for (long long it = gw; it < (long long)nrows * chunks; it += nw) {
+        const int r = (int)(it % nrows);
+        const long long ch = it / nrows;
+        const long long j = row_begin + r;
+        const int wl = (int)(j >> 6) + 1 < P ? (int)(j >> 6) + 1 : P;
+        const unsigned np = __ldg(word_end + wl);
+        const unsigned i0 = (unsigned)(ch * kNearChunk);
+        if (i0 >= np) continue;  // warp-uniform
+        const uint64_t *Sj = S + (size_t)j * P;
+        uint64_t D = 0;
+#pragma unroll
+        for (int q = 0; q < kNearPer; q++) {
+            const unsigned i = i0 + q * 32 + lane;
+            if (i < np) {
+                const unsigned pr = __ldg(pairs + i);
+                const unsigned c = pr >> 6, k = pr & 63u;
+                D ^= ((Sj[c >> 6] >> (c & 63u)) & 1ull) << k;
+            }
+        }
+        D = warp_xor64(D);
+        if (lane == 0) {
+            if (D) atomicXor(Dbuf + r, (unsigned long long)D);
+            const unsigned e = np - i0 < (unsigned)kNearChunk ? np - i0 : (unsigned)kNearChunk;
+            nb += 8ull * e;
+        }
+    }
+    if (lane == 0 && nb) atomicAdd(bytes, nb);
+}
+
+// near_apply_kernel: per near row (one CTA each), beta_k = D_k ^ <beta_{<k}, gcol_k>
+// (the sequential effect of the block's updates), written to beta_out for the
+// grouped pass's correction if given, then S_j ^= XOR_k beta_k S_{e0+k} through the
+// Four-Russians tables over the row's first Wb words.
+__global__ void __launch_bounds__(256) near_apply_kernel(uint64_t *S, long long row_begin, int nrows, int P, int b,
+                                                        int Wb, int Pt, const uint64_t *__restrict__ tab,
+                                                        const uint64_t *__restrict__ gcol, unsigned long long *Dbuf,
+                                                        uint64_t *beta_out, unsigned long long *bytes) {
+    __shared__ uint64_t sg[64];
+    __shared__ uint64_t s_beta;
+    if (threadIdx.x < 64) sg[threadIdx.x] = (int)threadIdx.x < b ? gcol[threadIdx.x] : 0;
+    cta_sync();
+    unsigned long long nb = 0;
+    for (int r = blockIdx.x; r < nrows; r += gridDim.x) {
+        if (threadIdx.x == 0) {
+            const uint64_t D = Dbuf[r];
+            Dbuf[r] = 0;  // ready for the next block
+            uint64_t beta = 0;
+            for (int k = 0; k < b; k++) beta |= ((((D >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]))) << k;
+            if (beta_out) beta_out[r] = beta;
+            s_beta = beta;
+            nb += beta ? 16ull * (unsigned long long)Wb : 0ull;
+        }
+        cta_sync();
+        const uint64_t bt = s_beta;
+        if (bt) {
+            uint64_t *Sj = S + (size_t)(row_begin + r) * P;
+            const uint64_t *t0 = tab + ((size_t)0 * 256 + ((bt >> 0) & 255)) * Pt;
+            const uint64_t *t1 = tab + ((size_t)1 * 256 + ((bt >> 8) & 255)) * Pt;
+            const uint64_t *t2 = tab + ((size_t)2 * 256 + ((bt >> 16) & 255)) * Pt;
+            const uint64_t *t3 = tab + ((size_t)3 * 256 + ((bt >> 24) & 255)) * Pt;
+            const uint64_t *t4 = tab + ((size_t)4 * 256 + ((bt >> 32) & 255)) * Pt;
+            const uint64_t *t5 = tab + ((size_t)5 * 256 + ((bt >> 40) & 255)) * Pt;
+            const uint64_t *t6 = tab + ((size_t)6 * 256 + ((bt >> 48) & 255)) * Pt;
+            const uint64_t *t7 = tab + ((size_t)7 * 256 + ((bt >> 56) & 255)) * Pt;
+            for (int w = threadIdx.x; w < Wb; w += blockDim.x)
+                Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
+        }
+        cta_sync();  // s_beta is rewritten for the next row
+    }
+    if (threadIdx.x == 0 && nb) atomicAdd(bytes, nb);
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1706,6 +1798,7 @@ struct mcbgpu_solver {
     uint64_t *d_Warr3 = nullptr;   // W of a group's third block
     uint64_t *d_Tg = nullptr;      // the group's blocks' rows transposed, kGStride words per coordinate
     uint64_t *d_beta = nullptr;    // 3 x 192: update bits of the near rows of a group's first blocks
+    unsigned long long *d_nearD = nullptr;  // kNearMaxRows: D of the near rows (zero between uses)
     uint64_t *d_masks = nullptr;   // 2 x 64: final masks of a group's first blocks
     unsigned *d_tile_epoch = nullptr;
     int32_t *d_tile_minc = nullptr;
@@ -1791,6 +1884,7 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_Warr3);
     cudaFree(s->d_Tg);
     cudaFree(s->d_beta);
+    cudaFree(s->d_nearD);
     cudaFree(s->d_masks);
     cudaFree(s->d_tile_epoch);
     cudaFree(s->d_tile_minc);
@@ -1880,6 +1974,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
         ALLOC(s->d_beta, sizeof(uint64_t) * 3 * 192);
         ALLOC(s->d_masks, sizeof(uint64_t) * 2 * 64);
     }
+    ALLOC(s->d_nearD, sizeof(unsigned long long) * kNearMaxRows);
     ALLOC(s->d_tile_epoch, sizeof(unsigned) * ntiles);
     ALLOC(s->d_tile_minc, sizeof(int32_t) * ntiles);
     ALLOC(s->d_gbar, sizeof(GridBar));
@@ -1896,6 +1991,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     if (e == cudaSuccess) e = cudaMemset(s->d_bytes, 0, sizeof(unsigned long long) * KC_COUNT);
     if (e == cudaSuccess) e = cudaMemset(s->d_tile_epoch, 0, sizeof(unsigned) * ntiles);
     if (e == cudaSuccess) e = cudaMemset(s->d_gbar, 0, sizeof(GridBar));
+    if (e == cudaSuccess) e = cudaMemset(s->d_nearD, 0, sizeof(unsigned long long) * kNearMaxRows);
     if (e == cudaSuccess) e = cudaMemset(s->d_word_end, 0, sizeof(unsigned) * 2 * ((size_t)s->P + 1));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
@@ -1949,6 +2045,7 @@ int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream) {
         Launch L(s, KC_RESET, st);
         reset_state_kernel<<<1, 32, 0, st>>>(s->d_slots, s->d_bs, s->d_status);
     }
+    MCB_CUDA(cudaMemsetAsync(s->d_nearD, 0, sizeof(unsigned long long) * kNearMaxRows, st));
     MCB_CUDA(cudaGetLastError());
     s->iters_run = 0;
     return MCBGPU_OK;
@@ -2253,9 +2350,12 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             if (wait_slot >= 0) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[wait_slot], 0));
             {
                 Launch L(s, KC_BLK_UPDATE_NEAR, st);
-                blk_update_kernel<<<grid_for(near_end - (e0 + b)), kUpdThreads, 0, st>>>(
-                    s->d_S, e0 + b, near_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes(),
-                    kGroup > 1 && pos < kGroup - 1 ? s->d_beta + (size_t)pos * 192 : nullptr);
+                const int nrows = (int)(near_end - (e0 + b));
+                uint64_t *bo = kGroup > 1 && pos < kGroup - 1 ? s->d_beta + (size_t)pos * 192 : nullptr;
+                near_d_kernel<<<sms * 4, 256, 0, st>>>(s->d_S, e0 + b, nrows, s->P, pairs, wend, s->d_nearD,
+                                                        L.bytes());
+                near_apply_kernel<<<nrows, 256, 0, st>>>(s->d_S, e0 + b, nrows, s->P, b, Wb, s->P, tab, gcol,
+                                                         s->d_nearD, bo, L.bytes());
             }
             if (near_end < far_end) {
                 const int slot = ring;

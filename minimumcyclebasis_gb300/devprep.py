@@ -93,6 +93,21 @@ class GpuGen:
                   "mcbgpu_gen_copy_lists")
         return off, co[:self.nnz]
 
+    def tree_shapes(self) -> dict:
+        """The tree kernel's tuned launch shapes: every shape tried (threads per CTA,
+        CTAs per SM, bucket width in quarters of the mean weight) with its
+        microseconds per root, and the one kept."""
+        cap = 16
+        sh = np.zeros(3 * cap, np.int32)
+        us = np.zeros(cap, np.float64)
+        cnt, ch = C.c_int32(), C.c_int32()
+        check_gpu(self.lib.mcbgpu_gen_tree_shapes(self._h, ptr(sh), ptr(us), cap, C.byref(cnt), C.byref(ch)),
+                  "mcbgpu_gen_tree_shapes")
+        tried = [{"threads": int(sh[3 * i]), "ctas_per_sm": int(sh[3 * i + 1]),
+                  "delta_x_mean_weight": sh[3 * i + 2] / 4.0, "us_per_root": round(float(us[i]), 2)}
+                 for i in range(min(cnt.value, cap)) if us[i] >= 0]
+        return {"tried": tried, "chosen": int(ch.value)}
+
     def release_trees(self) -> None:
         check_gpu(self.lib.mcbgpu_gen_release_trees(self._h), "mcbgpu_gen_release_trees")
 
@@ -120,6 +135,7 @@ class DevicePrepared:
     nnz: int
     tied_roots: int
     times: dict = field(default_factory=dict)
+    tree_shapes: dict = field(default_factory=dict)
 
 
 def prepare_on_device(src, threads: int = 0, chunk: int = 0, stream=0, make_solver: bool = True,
@@ -161,6 +177,7 @@ def prepare_on_device(src, threads: int = 0, chunk: int = 0, stream=0, make_solv
         offs.append(base + np.cumsum(counts))
         base += int(counts.sum())
     times["trees_and_candidates"] = time.perf_counter() - t2
+    shapes = gen.tree_shapes()
     times["host_searches_of_tied_roots"] = t_host_search
     t3 = time.perf_counter()
     p.rank_candidates(np.concatenate(offs), np.concatenate(pis) if pis else np.zeros(0, np.uint32),
@@ -178,7 +195,7 @@ def prepare_on_device(src, threads: int = 0, chunk: int = 0, stream=0, make_solv
         solver = Solver.from_device_lists(p.N, len(w), nnz, dw, do, dc, stream)
         times["solver_upload"] = time.perf_counter() - t5
     times["total"] = time.perf_counter() - t0
-    out = DevicePrepared(p, solver, len(w), nnz, tied_total, times)
+    out = DevicePrepared(p, solver, len(w), nnz, tied_total, times, shapes)
     if keep_gen:
         return out, gen
     gen.close()

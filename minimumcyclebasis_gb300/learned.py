@@ -154,6 +154,8 @@ class LearnedSolve:
     trees_kept: int
     fallback: bool
     times: dict = field(default_factory=dict)
+    lists: tuple | None = None
+    compared: list = field(default_factory=list)
 
     @property
     def skip_rate(self) -> float:
@@ -161,12 +163,16 @@ class LearnedSolve:
 
 
 def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.02, threads: int = 0, stream=0,
-                        keep_solver: bool = False, keep_features: bool = False, prefix: int | None = None):
+                        keep_solver: bool = False, keep_features: bool = False, prefix: int | None = None,
+                        host_lists: bool = False, compare=()):
     """Graph -> basis with the device preparation and the proposal's prefix (no
     proposal: `net` None keeps the whole list; `prefix` imposes a prefix length
     instead of the proposal's).  Returns a LearnedSolve; with keep_solver also the
     Solver and the Problem, with keep_features also the candidates' features (torch
-    (K, 16) bf16)."""
+    (K, 16) bf16); with host_lists the solved lists (weights, offsets, coordinates)
+    are copied to the host into LearnedSolve.lists; `compare` (networks) gets each
+    one's proposal prefix on the same features, (K_keep, U), in LearnedSolve.compared
+    (not solved, not timed)."""
     import torch
 
     from .devprep import GpuGen
@@ -204,10 +210,17 @@ def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.02, thre
         K_keep, U = proposal_prefix(logits.cpu().numpy(), w, N, margin)
     else:
         K_keep, U = K, int(w[-1]) if K else 0
+    times["proposal"] = time.perf_counter() - t1
+    compared = []
+    t_cmp = time.perf_counter()
+    for other in compare:
+        lg = other.forward(x, stream)
+        torch.cuda.synchronize()
+        compared.append(proposal_prefix(lg.cpu().numpy(), w, N, margin))
+    t_cmp = time.perf_counter() - t_cmp  # not part of the solve's time
     if not keep_features:
         del x
         x = None
-    times["proposal"] = time.perf_counter() - t1
     t2 = time.perf_counter()
     fallback = False
     nnz = build_lists(gen, K_keep, stream)
@@ -230,10 +243,14 @@ def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.02, thre
         solver.run(-1, stream)
         sel, tot = solver.results(stream=stream)
     times["solve"] = time.perf_counter() - t3
-    times["total"] = time.perf_counter() - t0
+    times["total"] = time.perf_counter() - t0 - t_cmp
     trees_kept = int(len(np.unique(tree[:K_keep]))) if K_keep else 0
+    lists = None
+    if host_lists:
+        off, co = gen.fetch_lists(stream)
+        lists = (np.ascontiguousarray(w[:len(off) - 1]), off, co)
     gen.close()
-    out = LearnedSolve(sel, tot, K, K_keep, U, nnz, p.F, trees_kept, fallback, times)
+    out = LearnedSolve(sel, tot, K, K_keep, U, nnz, p.F, trees_kept, fallback, times, lists, compared)
     extra = []
     if keep_solver:
         extra += [solver, p]
