@@ -143,6 +143,16 @@ int mcbgpu_solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t 
  * device candidate generation built, mcbgpu_gen_get_lists): copied on the device. */
 int mcbgpu_solver_upload_device(mcbgpu_solver *s, const int32_t *weight, const int64_t *offsets,
                                 const int32_t *coords, void *stream);
+/* No counterpart in the reference.  Re-verification of a complete run's basis on
+ * the device: the product M[i][j] = <C_i, S_j> of the selected cycles' vectors and
+ * the final support vectors, over every pair i <= j (O(N^3 / 64) word operations,
+ * an N x ceil(N/64) word scratch matrix).  A de Pina run leaves M unit lower
+ * triangular, which proves the N cycles GF(2)-independent (rank N of N); any
+ * other entry is counted in *violations, the first (row-major) at (*first_bad_i,
+ * *first_bad_j) (-1 if none; either may be NULL).  MCBGPU_E_STATE before the run
+ * is complete. */
+int mcbgpu_solver_verify(mcbgpu_solver *s, int64_t *violations, int64_t *first_bad_i, int64_t *first_bad_j,
+                         void *stream);
 /* Reset S to the unit vectors without re-uploading the candidates. */
 int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream);
 

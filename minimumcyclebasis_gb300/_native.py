@@ -96,6 +96,7 @@ GPU_SYMBOLS = {
     "mcbgpu_solver_create": (C.c_int, [C.POINTER(vp), i32, i64, i64]),
     "mcbgpu_solver_upload": (C.c_int, [vp, vp, vp, vp, vp]),
     "mcbgpu_solver_upload_device": (C.c_int, [vp, vp, vp, vp, vp]),
+    "mcbgpu_solver_verify": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), vp]),
     "mcbgpu_solver_reset": (C.c_int, [vp, vp]),
     "mcbgpu_select": (C.c_int, [vp, i32, C.POINTER(i64), vp]),
     "mcbgpu_cycle_vector": (C.c_int, [vp, i32, vp, vp]),

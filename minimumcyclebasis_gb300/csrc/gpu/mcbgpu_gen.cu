@@ -497,7 +497,7 @@ struct mcbgpu_gen {
     uint64_t *d_jump = nullptr;  // chunk x n
     uint32_t *d_bits = nullptr;  // chunk x words_per_root
     int32_t *d_gdist = nullptr, *d_next = nullptr;
-    uint32_t *d_gdirty = nullptr;
+    uint32_t *d_gdirty = nullptr, *d_gsumm = nullptr;
     uint8_t *d_tied = nullptr;
     int64_t *d_counts = nullptr, *d_coff = nullptr;  // chunk, chunk + 1
     uint32_t *d_cpair = nullptr;
@@ -532,7 +532,7 @@ static void gen_free(mcbgpu_gen *g) {
     if (g->ev1) cudaEventDestroy(g->ev1);
     void *ps[] = {g->d_ro,   g->d_rows,    g->d_cols,   g->d_rev,    g->d_pairs,  g->d_roots,  g->d_w,
                   g->d_ec,   g->d_fvs,     g->d_pedge,  g->d_dist,   g->d_code,   g->d_jump,   g->d_bits,
-                  g->d_gdist, g->d_next,   g->d_gdirty, g->d_tied,   g->d_counts, g->d_coff,   g->d_cpair,
+                  g->d_gdist, g->d_next,   g->d_gdirty, g->d_gsumm, g->d_tied,   g->d_counts, g->d_coff,   g->d_cpair,
                   g->d_cweight, g->d_nlong, g->d_status};
     for (void *p : ps) cudaFree(p);
     gen_free_lists(g);
@@ -584,6 +584,10 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
         return MCBGPU_E_ARG;
     }
     *out = nullptr;
+    if (nodes > kTreeGlobalMaxN) {
+        set_error("mcbgpu_gen_create: %d vertices after chain contraction (at most %d)", (int)nodes, kTreeGlobalMaxN);
+        return MCBGPU_E_ARG;
+    }
     // the graph is checked here once, so the kernels can index with it
     if (row_offsets[0] != 0 || (int64_t)row_offsets[nodes] != slots) {
         set_error("mcbgpu_gen_create: row offsets must run from 0 to the slot count");
@@ -643,7 +647,7 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, dev);
     const int words = (nodes + 31) / 32;
     g->shared_form = nodes <= kTreeSharedMaxN;
-    g->smem = g->shared_form ? ((((size_t)nodes * 4 + 15) & ~(size_t)15) + (size_t)words * 4) : 0;
+    g->smem = g->shared_form ? trees_smem_bytes(nodes) : 0;
     const size_t n = (size_t)nodes, C = (size_t)g->chunk;
 #define GALLOC(ptr, sz)                                            \
     do {                                                           \
@@ -675,13 +679,14 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
     if (!g->shared_form) {
         GALLOC(g->d_gdist, 4 * n * (size_t)g->sm_count * kTreeMaxCtasPerSm);
         GALLOC(g->d_gdirty, 4 * (size_t)words * (size_t)g->sm_count * kTreeMaxCtasPerSm);
+        GALLOC(g->d_gsumm, 4 * (size_t)((words + 31) / 32) * (size_t)g->sm_count * kTreeMaxCtasPerSm);
     }
     // shapes the tuner tries (the shared form: one 1024-thread CTA per SM, bucket
     // widths only); with fewer chunks than twice the shapes, the first one is kept
     if (g->shared_form)
         g->shapes = {{kTreeThreads, 1, 4}, {kTreeThreads, 1, 8}, {kTreeThreads, 1, 16}, {kTreeThreads, 1, 2}};
     else
-        g->shapes = {{256, 4, 8}, {256, 4, 32}, {256, 8, 16}, {128, 8, 16}, {512, 2, 16}, {1024, 1, 4}};
+        g->shapes = {{256, 8, 16}, {256, 8, 8}, {256, 8, 32}, {128, 16, 16}, {128, 16, 32}, {512, 4, 16}};
     const int nchunks = (fvs_size + g->chunk - 1) / g->chunk;
     if (nchunks < 2 * (int)g->shapes.size()) g->chosen = 0;
     if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);
@@ -700,7 +705,7 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
     up(g->d_pairs, pair_slot, 4 * (size_t)npairs);
     up(g->d_roots, fvs_vertices, 4 * (size_t)fvs_size);
     if (e == cudaSuccess) e = cudaMemset(g->d_status, 0, 4);
-    if (e == cudaSuccess && g->shared_form) e = set_trees_smem_limit();
+    if (e == cudaSuccess) e = set_trees_smem_limit();
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(sort_long_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(sizeof(int32_t) * kSortLongMax));
@@ -741,6 +746,7 @@ int mcbgpu_gen_trees(mcbgpu_gen *g, int32_t t0, int32_t count, uint8_t *tied, vo
     a.tied_out = g->d_tied;
     a.gdist = g->d_gdist;
     a.gdirty = g->d_gdirty;
+    a.gsumm = g->d_gsumm;
     a.next_root = g->d_next;
     a.status = g->d_status;
     const int cap = g->sm_count * shape.ctas_per_sm;

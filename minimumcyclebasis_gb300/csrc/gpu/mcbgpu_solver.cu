@@ -1778,6 +1778,89 @@ __global__ void __launch_bounds__(256) near_apply_kernel(uint64_t *S, long long 
     if (threadIdx.x == 0 && nb) atomicAdd(bytes, nb);
 }
 
+// ---- independence certificate --------------------------------------------------
+// After a complete run, the final support vectors certify the basis: S_j was made
+// orthogonal to every C_i chosen before it and is never changed after iteration j,
+// where <C_j, S_j> = 1.  So the N x N matrix M[i][j] = <C_i, S_j> is unit lower
+// triangular (M[i][j] = 0 for i < j, 1 for i = j) and has full rank, and with it the
+// N cycle vectors C_i (rank(M) <= rank(C)).  Whatever S holds, finding that
+// pattern in the product proves the selected cycles GF(2)-independent.
+// cert_rows_kernel: C as an N x P bit matrix from the selected candidates' lists.
+__global__ void cert_rows_kernel(const long long *__restrict__ selected, int N, int P, long long K,
+                                 const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
+                                 unsigned long long *C, unsigned *status) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long i = gw; i < N; i += nw) {
+        const long long r = selected[i];
+        if (r < 0 || r >= K) {
+            if (lane == 0) atomicOr(status, ST_BAD_INPUT);
+            continue;
+        }
+        for (long long q = off[r] + lane; q < off[r + 1]; q += 32) {
+            const int c = coords[q];
+            if (c >= 0 && c < N) atomicOr(C + (size_t)i * P + (c >> 6), 1ull << (c & 63));
+        }
+    }
+}
+
+// cert_check_kernel: one CTA per 64 x 64 tile (ti <= tj) of M: row i of C against row
+// j of S over the words of S_j's support (bits [0, j]); parity(XOR_w C_i[w] & S_j[w])
+// must be 1 on the diagonal and 0 above it.  Counts the pairs where it is not.
+constexpr int kCertWords = 32;
+__global__ void __launch_bounds__(256) cert_check_kernel(const unsigned long long *__restrict__ C,
+                                                        const uint64_t *__restrict__ S, int N, int P,
+                                                        unsigned long long *violations,
+                                                        unsigned long long *first_bad) {
+    const int ti = blockIdx.x, tj = blockIdx.y;
+    if (ti > tj) return;
+    __shared__ unsigned long long sC[64][kCertWords + 1], sS[64][kCertWords + 1];
+    const int t = threadIdx.x, ig = t >> 4, jg = t & 15;
+    unsigned long long acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = 0;
+    const int words = (tj + 1) < P ? tj + 1 : P;  // S_j, j < 64 (tj + 1), has no bit beyond word tj
+    for (int w0 = 0; w0 < words; w0 += kCertWords) {
+        for (int e = t; e < 64 * kCertWords; e += blockDim.x) {
+            const int row = e / kCertWords, w = w0 + e % kCertWords;
+            const long long i = 64ll * ti + row, j = 64ll * tj + row;
+            sC[row][e % kCertWords] = (i < N && w < words) ? C[(size_t)i * P + w] : 0ull;
+            sS[row][e % kCertWords] = (j < N && w < words) ? S[(size_t)j * P + w] : 0ull;
+        }
+        cta_sync();
+#pragma unroll 4
+        for (int w = 0; w < kCertWords; w++) {
+            unsigned long long ci[4], sj[4];
+#pragma unroll
+            for (int a = 0; a < 4; a++) ci[a] = sC[ig * 4 + a][w];
+#pragma unroll
+            for (int b = 0; b < 4; b++) sj[b] = sS[jg * 4 + b][w];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] ^= ci[a] & sj[b];
+        }
+        cta_sync();
+    }
+    unsigned long long bad = 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const long long i = 64ll * ti + ig * 4 + a, j = 64ll * tj + jg * 4 + b;
+            if (i >= N || j >= N || i > j) continue;
+            const unsigned bit = (unsigned)__popcll(acc[a][b]) & 1u;
+            if (bit != (i == j ? 1u : 0u)) {
+                bad++;
+                atomicMin(first_bad, (unsigned long long)i * (unsigned long long)N + (unsigned long long)j);
+            }
+        }
+    if (bad) atomicAdd(violations, bad);
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -2403,6 +2486,54 @@ int mcbgpu_solver_get_support(mcbgpu_solver *s, int32_t j, uint64_t *words, void
     MCB_CUDA(cudaMemcpyAsync(words, s->d_S + (size_t)j * s->P, sizeof(uint64_t) * (size_t)s->W,
                              cudaMemcpyDeviceToHost, st));
     MCB_CUDA(cudaStreamSynchronize(st));
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_verify(mcbgpu_solver *s, int64_t *violations, int64_t *first_bad_i, int64_t *first_bad_j,
+                         void *stream) {
+    if (!s || !violations) {
+        set_error("mcbgpu_solver_verify: invalid argument");
+        return MCBGPU_E_ARG;
+    }
+    if (s->iters_run != s->N) {
+        set_error("mcbgpu_solver_verify: the basis is not complete (%lld of %d iterations run)",
+                  (long long)s->iters_run, s->N);
+        return MCBGPU_E_STATE;
+    }
+    int rc = check_status(s, (cudaStream_t)stream);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    *violations = 0;
+    if (s->N == 0) return MCBGPU_OK;
+    unsigned long long *C = nullptr, *cnt = nullptr;
+    const size_t cbytes = sizeof(unsigned long long) * (size_t)s->N * s->P;
+    cudaError_t e = cudaMalloc((void **)&C, cbytes);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&cnt, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemsetAsync(C, 0, cbytes, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt + 1, 0xff, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) {
+        const int sms = s->sm_count > 0 ? s->sm_count : 148;
+        cert_rows_kernel<<<sms * 8, 256, 0, st>>>(s->d_selected, s->N, s->P, s->K, s->d_off, s->d_coords, C,
+                                                  s->d_status);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        const unsigned tiles = (unsigned)((s->N + 63) / 64);
+        cert_check_kernel<<<dim3(tiles, tiles), 256, 0, st>>>(C, s->d_S, s->N, s->P, cnt, cnt + 1);
+        e = cudaGetLastError();
+    }
+    unsigned long long h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, cnt, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(C);
+    cudaFree(cnt);
+    if (e != cudaSuccess) return cuda_fail(e, "mcbgpu_solver_verify");
+    rc = check_status(s, st);
+    if (rc) return rc;
+    *violations = (int64_t)h[0];
+    if (first_bad_i) *first_bad_i = h[0] ? (int64_t)(h[1] / (unsigned long long)s->N) : -1;
+    if (first_bad_j) *first_bad_j = h[0] ? (int64_t)(h[1] % (unsigned long long)s->N) : -1;
     return MCBGPU_OK;
 }
 

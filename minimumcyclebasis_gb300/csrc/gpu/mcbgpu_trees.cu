@@ -20,7 +20,7 @@ struct mcbgpu_trees {
     size_t smem = 0;
     uint32_t *d_ro = nullptr, *d_cols = nullptr, *d_rev = nullptr, *d_roots = nullptr;
     int32_t *d_w = nullptr, *d_dist = nullptr, *d_pedge = nullptr, *d_gdist = nullptr, *d_next = nullptr;
-    uint32_t *d_gdirty = nullptr;
+    uint32_t *d_gdirty = nullptr, *d_gsumm = nullptr;
     uint8_t *d_tied = nullptr;
     unsigned *d_status = nullptr;
     long long bytes = 0;
@@ -38,6 +38,7 @@ static void trees_free(mcbgpu_trees *t) {
     cudaFree(t->d_gdist);
     cudaFree(t->d_next);
     cudaFree(t->d_gdirty);
+    cudaFree(t->d_gsumm);
     cudaFree(t->d_tied);
     cudaFree(t->d_status);
     delete t;
@@ -53,6 +54,10 @@ int mcbgpu_trees_create(mcbgpu_trees **out, int32_t nodes, int64_t slots, const 
         return MCBGPU_E_ARG;
     }
     *out = nullptr;
+    if (nodes > kTreeGlobalMaxN) {
+        set_error("mcbgpu_trees_create: %d vertices after chain contraction (at most %d)", (int)nodes, kTreeGlobalMaxN);
+        return MCBGPU_E_ARG;
+    }
     if (row_offsets[0] != 0 || (int64_t)row_offsets[nodes] != slots) {
         set_error("mcbgpu_trees_create: row offsets must run from 0 to the slot count");
         return MCBGPU_E_ARG;
@@ -88,7 +93,7 @@ int mcbgpu_trees_create(mcbgpu_trees **out, int32_t nodes, int64_t slots, const 
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&t->sm_count, cudaDevAttrMultiProcessorCount, dev);
     const int words = (nodes + 31) / 32;
     t->shared_form = nodes <= kTreeSharedMaxN;
-    t->smem = t->shared_form ? ((((size_t)nodes * 4 + 15) & ~(size_t)15) + (size_t)words * 4) : 0;
+    t->smem = t->shared_form ? trees_smem_bytes(nodes) : 0;
     const size_t per_root = (size_t)nodes;
 #define TALLOC(ptr, sz)                                            \
     do {                                                           \
@@ -110,6 +115,7 @@ int mcbgpu_trees_create(mcbgpu_trees **out, int32_t nodes, int64_t slots, const 
     if (!t->shared_form) {
         TALLOC(t->d_gdist, 4 * per_root * (size_t)t->sm_count * kTreeMaxCtasPerSm);
         TALLOC(t->d_gdirty, 4 * (size_t)words * (size_t)t->sm_count * kTreeMaxCtasPerSm);
+        TALLOC(t->d_gsumm, 4 * (size_t)((words + 31) / 32) * (size_t)t->sm_count * kTreeMaxCtasPerSm);
     }
 #undef TALLOC
     if (e == cudaSuccess) e = cudaMemcpy(t->d_ro, row_offsets, 4 * ((size_t)nodes + 1), cudaMemcpyHostToDevice);
@@ -120,7 +126,7 @@ int mcbgpu_trees_create(mcbgpu_trees **out, int32_t nodes, int64_t slots, const 
     }
     // the kernel's attribute is process-wide: set to the largest shared form, so that
     // handles of different sizes can be used in any order
-    if (e == cudaSuccess && t->shared_form) e = set_trees_smem_limit();
+    if (e == cudaSuccess) e = set_trees_smem_limit();
     if (e != cudaSuccess) {
         const int rc = cuda_fail(e, "mcbgpu_trees_create");
         trees_free(t);
@@ -152,7 +158,7 @@ int mcbgpu_trees_run(mcbgpu_trees *t, const uint32_t *roots, int32_t count, int3
     a.w = t->d_w;
     a.rev = t->d_rev;
     a.n = t->n;
-    const TreeShape shape = t->shared_form ? TreeShape{kTreeThreads, 1, 4} : TreeShape{256, 4, 8};
+    const TreeShape shape = t->shared_form ? TreeShape{kTreeThreads, 1, 4} : TreeShape{256, 8, 16};
     a.delta = shape_delta(shape, t->delta);
     a.roots = t->d_roots;
     a.count = count;
@@ -161,6 +167,7 @@ int mcbgpu_trees_run(mcbgpu_trees *t, const uint32_t *roots, int32_t count, int3
     a.tied_out = t->d_tied;
     a.gdist = t->d_gdist;
     a.gdirty = t->d_gdirty;
+    a.gsumm = t->d_gsumm;
     a.next_root = t->d_next;
     a.status = t->d_status;
     const int slots_ = t->sm_count * shape.ctas_per_sm;

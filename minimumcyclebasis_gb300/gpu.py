@@ -182,6 +182,16 @@ class Solver:
                   "mcbgpu_solver_results")
         return sel[:count], tot.value
 
+    def verify(self, stream=0) -> dict:
+        """The independence certificate of a complete run (mcbgpu_solver_verify):
+        {"rank": N if every <C_i, S_j> (i <= j) is as a de Pina run leaves it, else
+        None, "violations": count, "first": (i, j) or None}."""
+        v, i, j = C.c_int64(), C.c_int64(), C.c_int64()
+        check_gpu(self.lib.mcbgpu_solver_verify(self._h, C.byref(v), C.byref(i), C.byref(j), _stream(stream)),
+                  "mcbgpu_solver_verify")
+        return {"rank": self.N if v.value == 0 else None, "violations": int(v.value),
+                "first": None if v.value == 0 else (int(i.value), int(j.value))}
+
     def support_vector(self, j: int, stream=0) -> np.ndarray:
         out = np.zeros((self.N + 63) // 64, np.uint64)
         check_gpu(self.lib.mcbgpu_solver_get_support(self._h, j, ptr(out), _stream(stream)),

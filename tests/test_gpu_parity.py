@@ -167,3 +167,45 @@ def test_upload_rejects_bad_lists():
         Solver(4, w, off, np.array([2, 1, 0], np.int32))  # not ascending
     with pytest.raises(MCBError):
         Solver(4, w, off, np.array([0, 9, 1], np.int32))  # outside [0, N)
+
+
+@pytest.mark.parametrize("name", ["grid8x8_s3", "rand300_s0", "grid32x32_s1", "planar2000_s2"])
+def test_device_independence_certificate(name):
+    # the selected cycles against the final support vectors: unit lower triangular,
+    # so rank N of N; the host's elimination agrees
+    fx, p = prep(name)
+    s = Solver.from_problem(p)
+    from minimumcyclebasis_gb300._native import MCBError
+    with pytest.raises(MCBError):  # not before the run is complete
+        s.verify()
+    s.run()
+    sel, _ = s.results()
+    v = s.verify()
+    assert v == {"rank": p.N, "violations": 0, "first": None}
+    assert p.gf2_rank(sel) == p.N
+    s.close()
+
+
+def test_device_certificate_flags_a_wrong_basis():
+    # the per-iteration form run with one selection forced to a repeated candidate is
+    # not a de Pina run: its support vectors cannot certify the basis
+    fx, p = prep("grid8x8_s3")
+    s = Solver.from_problem(p)
+    s.run()
+    good = s.verify()
+    assert good["violations"] == 0
+    # a second solver whose lists make candidate 0 appear twice in the basis: the
+    # lists of every candidate replaced by candidate 0's
+    _, _, w, _ = p.candidates()
+    off, co = p.cycle_lists()
+    n0 = int(off[1])
+    K = len(w)
+    off2 = np.arange(K + 1, dtype=np.int64) * n0
+    co2 = np.tile(co[:n0], K)
+    s2 = Solver(p.N, w, off2, co2)
+    s2.run()
+    from minimumcyclebasis_gb300._native import MCBError
+    with pytest.raises(MCBError):  # no odd candidate after the first iteration
+        s2.results()
+    s.close()
+    s2.close()
