@@ -415,13 +415,20 @@ def learned_form(args, g, sel0, tot0, sh):
     # for the end-to-end steps; the untrained network's prefix on the same features
     # for comparison: neither is part of the timed solve)
     r, lsolver, p = solve_with_proposal(g, net, margin=args.margin, stream=sh, keep_solver=True, host_lists=True,
-                                        compare=[untrained])
+                                        compare=[untrained], rule=args.proposal_rule, eps=args.eps,
+                                        keep_logits=True)
     g2b = r.times["total"]
     assert np.array_equal(r.selected, sel0) and r.total_weight == tot0, "the learned form's basis differs"
     uk, _ = r.compared[0]
+    from minimumcyclebasis_gb300.learned import proposal_table
+    _, _, wsorted, _ = p.candidates()
+    K_needed = int(np.max(sel0)) + 1  # the prefix the solve needs: up to its last selection
+    table = proposal_table(r.logits, wsorted, p.N, net.pos_weight, K_needed)
     learned = {"skip_rate": r.skip_rate, "diffs": 0, "fallback": r.fallback, "K": r.K, "K_kept": r.K_kept,
-               "U": r.U, "nnz_kept": r.nnz_kept, "trees": r.trees, "trees_kept": r.trees_kept,
-               "margin": args.margin, "untrained_skip_rate": 1.0 - uk / max(r.K, 1),
+               "K_needed": K_needed, "U": r.U, "nnz_kept": r.nnz_kept, "trees": r.trees,
+               "trees_kept": r.trees_kept, "rule": args.proposal_rule,
+               "rule_param": args.eps if args.proposal_rule == "tail" else args.margin,
+               "untrained_skip_rate": 1.0 - uk / max(r.K, 1), "rules_on_this_graph": table,
                "training": {"graphs": args.train_graphs, "points": args.train_n, "candidates": int(sum(ks)),
                             "epochs": args.train_epochs, "loss_first_last": [round(losses[0], 4),
                                                                              round(losses[-1], 4)],
@@ -840,9 +847,12 @@ def main():
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip the learned proposal's form")
     ap.add_argument("--train-graphs", type=int, default=3, help="graphs whose traces train the proposal")
-    ap.add_argument("--train-n", type=int, default=20000, help="size (--n units) of the training graphs")
+    ap.add_argument("--train-n", type=int, default=60000, help="size (--n units) of the training graphs")
     ap.add_argument("--train-epochs", type=int, default=20)
-    ap.add_argument("--margin", type=float, default=0.05, help="proposals: ceil(N (1 + margin)) top scores")
+    ap.add_argument("--proposal-rule", choices=["tail", "top"], default="tail",
+                    help="tail: expected selections beyond the prefix <= --eps; top: ceil(N (1 + margin)) top scores")
+    ap.add_argument("--eps", type=float, default=0.1)
+    ap.add_argument("--margin", type=float, default=0.05)
     ap.add_argument("--plain-windows", type=int, default=8)
     ap.add_argument("--plain-width", type=int, default=128)
     ap.add_argument("--batch-count", type=int, default=4096)

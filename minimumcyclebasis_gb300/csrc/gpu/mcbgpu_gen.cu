@@ -686,7 +686,7 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
     if (g->shared_form)
         g->shapes = {{kTreeThreads, 1, 4}, {kTreeThreads, 1, 8}, {kTreeThreads, 1, 16}, {kTreeThreads, 1, 2}};
     else
-        g->shapes = {{256, 8, 16}, {256, 8, 8}, {256, 8, 32}, {128, 16, 16}, {128, 16, 32}, {512, 4, 16}};
+        g->shapes = {{256, 8, 8}, {256, 8, 4}, {256, 8, 2}, {256, 8, 16}, {512, 4, 8}, {128, 16, 8}};
     const int nchunks = (fvs_size + g->chunk - 1) / g->chunk;
     if (nchunks < 2 * (int)g->shapes.size()) g->chosen = 0;
     if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);

@@ -1891,7 +1891,9 @@ struct mcbgpu_solver {
     unsigned *d_pairs = nullptr;     // 3 x pair_cap: resolve scratch, sorted pairs of the two block parities
     unsigned pair_cap = 0;
     unsigned *d_word_end = nullptr;  // 2 x (P + 1): sorted pairs with S word < w, by block parity
-    cudaStream_t st2 = nullptr;      // the update of the rows beyond the next block
+    cudaStream_t st1 = nullptr;      // the blocked run's critical path (highest priority)
+    cudaStream_t st2 = nullptr;      // the update of the rows beyond the next block (lowest priority)
+    cudaEvent_t ev_join = nullptr;   // the end of a blocked run, for the caller's stream
     cudaEvent_t ev_fork = nullptr, ev_tail = nullptr, ev_upd[4] = {}, ev_par[2] = {};
     IterSlot *d_slots = nullptr;   // 2
     BlockState *d_bs = nullptr;
@@ -1976,6 +1978,8 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_pairs);
     cudaFree(s->d_word_end);
     if (s->st2) cudaStreamDestroy(s->st2);
+    if (s->st1) cudaStreamDestroy(s->st1);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev_tail) cudaEventDestroy(s->ev_tail);
     for (cudaEvent_t e : s->ev_par)
@@ -2076,7 +2080,14 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     if (e == cudaSuccess) e = cudaMemset(s->d_gbar, 0, sizeof(GridBar));
     if (e == cudaSuccess) e = cudaMemset(s->d_nearD, 0, sizeof(unsigned long long) * kNearMaxRows);
     if (e == cudaSuccess) e = cudaMemset(s->d_word_end, 0, sizeof(unsigned) * 2 * ((size_t)s->P + 1));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st2, cudaStreamNonBlocking);
+    // the far update fills every SM when it runs; with the critical path (transpose,
+    // streaming pass, pivot search, near update) on a higher-priority stream, the
+    // block scheduler gives that path's CTAs the SMs as they free up
+    int prio_low = 0, prio_high = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->st2, cudaStreamNonBlocking, prio_low);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->st1, cudaStreamNonBlocking, prio_high);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_tail, cudaEventDisableTiming);
     for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&s->ev_upd[i], cudaEventDisableTiming);
@@ -2301,7 +2312,8 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         set_error("mcbgpu_solver_run: candidates not uploaded");
         return MCBGPU_E_STATE;
     }
-    cudaStream_t st = (cudaStream_t)stream;
+    cudaStream_t caller = (cudaStream_t)stream;
+    cudaStream_t st = s->st1;  // the critical path; joined back into the caller's stream at the end
     const int64_t iters = (max_iterations >= 0 && max_iterations < s->N) ? max_iterations : s->N;
     const int sms = s->sm_count > 0 ? s->sm_count : 148;
     long long ntiles = (s->K + kTile - 1) / kTile;
@@ -2321,7 +2333,8 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
     // group starts: the last block of a group updates the next kGroup x 64 rows on
     // `st`, and block i < kGroup - 1 of a group the rows of the group's later blocks
     // (their update bits go to beta slab i for the corrections).
-    MCB_CUDA(cudaEventRecord(s->ev_fork, st));
+    MCB_CUDA(cudaEventRecord(s->ev_fork, caller));
+    MCB_CUDA(cudaStreamWaitEvent(st, s->ev_fork, 0));
     MCB_CUDA(cudaStreamWaitEvent(s->st2, s->ev_fork, 0));
     struct FarRec {
         long long start;  // first row of the far update
@@ -2456,6 +2469,8 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         MCB_CUDA(cudaGetLastError());
     }
     if (nfar > 0) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[fars[nfar - 1].slot], 0));
+    MCB_CUDA(cudaEventRecord(s->ev_join, st));
+    MCB_CUDA(cudaStreamWaitEvent(caller, s->ev_join, 0));
 
     s->iters_run = iters;
     return MCBGPU_OK;

@@ -30,8 +30,10 @@
 //                        tree it does not accept itself (the result does not change);
 //                        single-graph mode (with --bcc the components are prepared on
 //                        the host in parallel)
-//   --verify             re-verify every basis by Gaussian elimination over GF(2)
-//                        (mcbh_gf2_rank): the N selected cycles must have rank N;
+//   --verify             re-verify every basis over GF(2): the N selected cycles must
+//                        have rank N; single-graph blocked solves by the device
+//                        certificate (mcbgpu_solver_verify, any N), the others by
+//                        Gaussian elimination on the host (mcbh_gf2_rank);
 //                        "GF(2) rank R of N" on stderr per problem, an error if R < N
 //
 // Exit status 0 on success; on any error a message on stderr and status 1 (the
@@ -149,6 +151,7 @@ struct Job {
     std::vector<int32_t> root, edge, weight, tree, coords;
     std::vector<int64_t> off, sel;
     long long total = 0;
+    int64_t device_rank = -1;  // rank certified on the device (--verify, single-problem solver)
 };
 
 void init_gpu_once() {
@@ -251,6 +254,17 @@ void solve_single(Job &j, const Outputs &o) {
     j.st.t_gpu = j.st.t_inspection = gpu_ms / 1000.0;
     j.st.t_main = now_s() - t1;
     j.st.total_mb = (double)mcbgpu_solver_device_bytes(s) / (1024.0 * 1024.0);
+    if (o.verify && !o.plain) {
+        // the basis against the final support vectors, on the device (exact at any N)
+        int64_t bad = 0, bi = -1, bj = -1;
+        check_gpu(mcbgpu_solver_verify(s, &bad, &bi, &bj, nullptr), "GF(2) verification on the device");
+        if (bad != 0) {
+            std::fprintf(stderr, "mcb_gb300: %lld entries of <C_i, S_j> contradict the basis (first (%lld, %lld))\n",
+                         (long long)bad, (long long)bi, (long long)bj);
+            std::exit(1);
+        }
+        j.device_rank = N;
+    }
     mcbgpu_solver_destroy(s);
 }
 
@@ -306,9 +320,12 @@ void solve_batched(std::vector<Job *> &jobs) {
 // Appends the problem's stats row and its cycle blocks.
 void emit_job(Job &j, const Outputs &o) {
     if (o.verify && !j.info.single_cycle && j.info.num_coords > 0) {
-        int64_t rank = 0;
-        check_host(mcbh_gf2_rank(j.p, j.sel.data(), (int64_t)j.sel.size(), o.threads, &rank), "GF(2) verification");
-        std::fprintf(stderr, "GF(2) rank %lld of %d\n", (long long)rank, j.info.num_coords);
+        int64_t rank = j.device_rank;
+        if (rank < 0)
+            check_host(mcbh_gf2_rank(j.p, j.sel.data(), (int64_t)j.sel.size(), o.threads, &rank),
+                       "GF(2) verification");
+        std::fprintf(stderr, "GF(2) rank %lld of %d%s\n", (long long)rank, j.info.num_coords,
+                     j.device_rank >= 0 ? " (device certificate)" : "");
         if (rank != j.info.num_coords) {
             std::fprintf(stderr, "mcb_gb300: the basis is not independent\n");
             std::exit(1);

@@ -15,8 +15,12 @@ The network proposes it.  It scores every candidate from 16 features of its cycl
 length, rank quantile, degrees; computed on the device during the cycle walk) with a
 two-layer perceptron (16 -> 64 ReLU -> 1, bf16 weights, fp32 accumulation; its first
 layer on the tensor cores) trained on (candidate, selected?) traces of solved graphs.
-The top ceil(N (1 + margin)) scores are the proposals; the heaviest proposal's weight
-U bounds the prefix (every candidate of weight <= U, ties included).  The solver runs
+Two rules turn scores into a prefix.  The tail rule (the default): the shortest prefix
+beyond which the candidates' calibrated probabilities of selection sum to at most
+eps, i.e. the expected number of selected candidates left out is at most eps.  The
+top-score rule: the top ceil(N (1 + margin)) scores are the proposals and the
+heaviest proposal's weight U bounds the prefix.  Either way the prefix ends at the
+end of a weight class (every candidate of weight <= U, ties included).  The solver runs
 on that prefix and checks itself: if some iteration finds no odd candidate in it
 (the proposals did not hold a basis), the whole list is built and the solve is run
 again on it.  Either way the result is the plain solve's, which stays the judge.  When
@@ -65,6 +69,7 @@ class ProposalNet:
         h = C.c_void_p()
         check_gpu(self.lib.mcbgpu_mlp_create(C.byref(h), ptr(p)), "mcbgpu_mlp_create")
         self._h = h
+        self.pos_weight = 1.0  # the positive weight of the training loss (set by train)
 
     def params(self) -> np.ndarray:
         out = np.empty(int(self.lib.mcbgpu_mlp_param_count()), np.float32)
@@ -129,8 +134,8 @@ def build_lists(gen, K_keep: int, stream=0) -> int:
 
 
 def proposal_prefix(logits_host: np.ndarray, weight_sorted: np.ndarray, N: int, margin: float):
-    """(K_keep, U): the top ceil(N (1 + margin)) scores' heaviest weight U and the
-    rank-order prefix of every candidate of weight <= U."""
+    """(K_keep, U) by the top-score rule: the top ceil(N (1 + margin)) scores'
+    heaviest weight U and the rank-order prefix of every candidate of weight <= U."""
     K = len(weight_sorted)
     k = int(min(K, np.ceil(N * (1.0 + margin))))
     if k >= K:
@@ -138,6 +143,48 @@ def proposal_prefix(logits_host: np.ndarray, weight_sorted: np.ndarray, N: int, 
     top = np.argpartition(-logits_host, k - 1)[:k]
     U = int(weight_sorted[top].max())
     return int(np.searchsorted(weight_sorted, U, side="right")), U
+
+
+def calibrated(logits_host: np.ndarray, pos_weight: float) -> np.ndarray:
+    """P(selected) from logits trained with positives weighted by pos_weight (the
+    weighting multiplies the odds by pos_weight)."""
+    z = np.clip(logits_host.astype(np.float64), -60, 60) - np.log(max(pos_weight, 1e-12))
+    return 1.0 / (1.0 + np.exp(-z))
+
+
+def tail_prefix(logits_host: np.ndarray, weight_sorted: np.ndarray, pos_weight: float, eps: float):
+    """(K_keep, U) by the tail rule: the shortest rank-order prefix beyond which the
+    expected number of selected candidates (calibrated probabilities summed) is at
+    most eps (so no selected candidate lies beyond it with probability >= 1 - eps),
+    extended to the end of its weight class."""
+    K = len(weight_sorted)
+    if K == 0:
+        return 0, 0
+    p = calibrated(logits_host, pos_weight)
+    tail = np.cumsum(p[::-1])[::-1]  # tail[r] = sum of p over ranks >= r
+    beyond = np.nonzero(tail <= eps)[0]
+    K1 = int(beyond[0]) if len(beyond) else K
+    if K1 >= K:
+        return K, int(weight_sorted[-1])
+    U = int(weight_sorted[max(K1 - 1, 0)])
+    return int(np.searchsorted(weight_sorted, U, side="right")), U
+
+
+def proposal_table(logits_host, weight_sorted, N: int, pos_weight: float, K_needed: int | None = None):
+    """The prefix of each rule (top-score margins, tail bounds) on one graph's
+    scores; with the prefix the solve needs (K_needed), whether each holds it."""
+    out = []
+    for rule, par in [("top", 0.05), ("top", 0.25), ("top", 1.0), ("top", 3.0), ("tail", 1.0), ("tail", 0.3),
+                      ("tail", 0.1), ("tail", 0.03)]:
+        if rule == "top":
+            k, U = proposal_prefix(logits_host, weight_sorted, N, par)
+        else:
+            k, U = tail_prefix(logits_host, weight_sorted, pos_weight, par)
+        row = {"rule": rule, "param": par, "K_keep": int(k), "U": int(U)}
+        if K_needed is not None:
+            row["holds_basis"] = bool(k >= K_needed)
+        out.append(row)
+    return out
 
 
 @dataclass
@@ -156,15 +203,17 @@ class LearnedSolve:
     times: dict = field(default_factory=dict)
     lists: tuple | None = None
     compared: list = field(default_factory=list)
+    logits: np.ndarray | None = None
 
     @property
     def skip_rate(self) -> float:
         return 1.0 - self.K_kept / self.K if self.K else 0.0
 
 
-def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.02, threads: int = 0, stream=0,
+def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.05, threads: int = 0, stream=0,
                         keep_solver: bool = False, keep_features: bool = False, prefix: int | None = None,
-                        host_lists: bool = False, compare=()):
+                        host_lists: bool = False, compare=(), rule: str = "tail", eps: float = 0.1,
+                        keep_logits: bool = False):
     """Graph -> basis with the device preparation and the proposal's prefix (no
     proposal: `net` None keeps the whole list; `prefix` imposes a prefix length
     instead of the proposal's).  Returns a LearnedSolve; with keep_solver also the
@@ -172,7 +221,9 @@ def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.02, thre
     (K, 16) bf16); with host_lists the solved lists (weights, offsets, coordinates)
     are copied to the host into LearnedSolve.lists; `compare` (networks) gets each
     one's proposal prefix on the same features, (K_keep, U), in LearnedSolve.compared
-    (not solved, not timed)."""
+    (not solved, not timed).  `rule`: "tail" (the tail rule with bound eps, on the
+    network's calibrated probabilities; the default) or "top" (the top-score rule
+    with `margin`).  keep_logits stores the scores (host) in LearnedSolve.logits."""
     import torch
 
     from .devprep import GpuGen
@@ -207,7 +258,11 @@ def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.02, thre
     elif net is not None:
         logits = net.forward(x, stream)
         torch.cuda.synchronize()
-        K_keep, U = proposal_prefix(logits.cpu().numpy(), w, N, margin)
+        lh = logits.cpu().numpy()
+        if rule == "top":
+            K_keep, U = proposal_prefix(lh, w, N, margin)
+        else:
+            K_keep, U = tail_prefix(lh, w, net.pos_weight, eps)
     else:
         K_keep, U = K, int(w[-1]) if K else 0
     times["proposal"] = time.perf_counter() - t1
@@ -216,7 +271,9 @@ def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.02, thre
     for other in compare:
         lg = other.forward(x, stream)
         torch.cuda.synchronize()
-        compared.append(proposal_prefix(lg.cpu().numpy(), w, N, margin))
+        lo = lg.cpu().numpy()
+        compared.append(proposal_prefix(lo, w, N, margin) if rule == "top" else
+                        tail_prefix(lo, w, other.pos_weight, eps))
     t_cmp = time.perf_counter() - t_cmp  # not part of the solve's time
     if not keep_features:
         del x
@@ -250,7 +307,8 @@ def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.02, thre
         off, co = gen.fetch_lists(stream)
         lists = (np.ascontiguousarray(w[:len(off) - 1]), off, co)
     gen.close()
-    out = LearnedSolve(sel, tot, K, K_keep, U, nnz, p.F, trees_kept, fallback, times, lists, compared)
+    out = LearnedSolve(sel, tot, K, K_keep, U, nnz, p.F, trees_kept, fallback, times, lists, compared,
+                       lh if (keep_logits and net is not None and prefix is None) else None)
     extra = []
     if keep_solver:
         extra += [solver, p]
@@ -282,6 +340,7 @@ def train(net: ProposalNet, xs, ys, epochs: int = 8, batch: int = 16384, lr: flo
     if pos_weight is None:
         pos = float(y.sum().item())
         pos_weight = max(1.0, (n - pos) / max(pos, 1.0))
+    net.pos_weight = float(pos_weight)
     g = torch.Generator(device="cuda")
     g.manual_seed(seed)
     losses = []

@@ -117,14 +117,16 @@ def test_bcc_mode_rings_and_bridge_without_gpu(tmp_path):
 @pytest.mark.parametrize("name", ["grid32x32_s1", "rand2000_w20_s11"])
 @pytest.mark.parametrize("bcc", [False, True])
 def test_driver_verify_reports_full_rank(tmp_path, name, bcc):
-    # --verify: every basis re-verified by GF(2) elimination, rank N of N
+    # --verify: every basis re-verified over GF(2), rank N of N (the single graph by the
+    # device certificate, the components by elimination on the host)
     fx = load_golden(name)
     r = run(fx["mtx"], tmp_path / "stats.csv", 4, "--verify", *(["--bcc"] if bcc else []))
     assert r.returncode == 0, r.stderr
     ranks = [ln.split() for ln in r.stderr.splitlines() if ln.startswith("GF(2) rank ")]
     assert ranks and all(x[2] == x[4] for x in ranks)
     if not bcc:
-        assert ranks == [["GF(2)", "rank", str(fx["G"]["num_coords"]), "of", str(fx["G"]["num_coords"])]]
+        n = str(fx["G"]["num_coords"])
+        assert ranks == [["GF(2)", "rank", n, "of", n, "(device", "certificate)"]]
 
 
 @pytest.mark.gpu
