@@ -223,6 +223,15 @@ int mcbh_write_mtx(const char *path, int32_t nodes, int64_t m, const int32_t *u,
  * own; this replaces the reference's bicc tool + per-component loop (bicc/,
  * main.sh:19-32) inside one process. */
 int64_t mcbh_bcc_split(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v, int32_t *comp_of_edge);
+/* The order in which the reference's bicc tool writes a component's edges
+ * (bicc/include/bicc.h:220-314, print_to_a_file): the slots of the input graph's CSR
+ * (include/CsrGraph.h:113-174, the 2m directed slots sorted by (row, col)) whose row
+ * exceeds their column, in slot order, each written as (row, column).  order[k] =
+ * the input edge of the k-th such slot (m entries at most; self-loops have none).
+ * Returns the number written.  A component's edges in this order, with its vertices
+ * numbered in order of first appearance (row before column, bicc/Relabeller.cpp:72-126),
+ * are the graph the reference's per-component run reads. */
+int64_t mcbh_edge_slot_order(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v, int64_t *order);
 
 #ifdef __cplusplus
 }

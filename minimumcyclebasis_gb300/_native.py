@@ -71,6 +71,7 @@ HOST_SYMBOLS = {
     "mcbh_gen_planar_chains": (i64, [i32, i32, i32, i32, i32, i32, u64, vp, vp, vp, vp]),
     "mcbh_gen_block_tree": (i64, [i32, i32, i32, i32, i32, i32, i32, u64, vp, vp, vp, vp]),
     "mcbh_bcc_split": (i64, [i32, i64, vp, vp, vp]),
+    "mcbh_edge_slot_order": (i64, [i32, i64, vp, vp, vp]),
     "mcbh_read_mtx": (i64, [C.c_char_p, vp, i64, vp, vp, vp]),
     "mcbh_write_mtx": (C.c_int, [C.c_char_p, i32, i64, vp, vp, vp]),
 }

@@ -21,7 +21,8 @@
 //   --bcc                split the graph into biconnected components first and solve
 //                        each one that has a cycle (in order of its first edge), one
 //                        stats row per component, the way the reference's bicc tool +
-//                        per-component loop (bicc/, main.sh:19-32) processes a graph;
+//                        per-component loop (bicc/, main.sh:19-32) processes a graph,
+//                        each component with the tool's edge order and numbering;
 //                        the components go through one batched solve (mcbgpu_batch);
 //                        the cycle listings give each component's basis in turn
 //   --gpu-trees          the per-root shortest-path trees computed on the GPU
@@ -421,13 +422,18 @@ int main(int argc, char **argv) {
                    "cannot read the input graph");
         const int64_t nc = mcbh_bcc_split(nodes, m, u.data(), v.data(), comp.data());
         if (nc < 0) fail("biconnected split failed", nullptr);
-        // edges of every component in input order; vertices renumbered in order of
-        // first appearance (as bicc/Relabeller.cpp numbers a component file)
+        // every component as the reference's bicc tool writes it and its Relabeller
+        // numbers it (bicc/include/bicc.h:220-314, bicc/Relabeller.cpp:72-126): its
+        // edges in the input CSR's slot order as (larger, smaller endpoint), its
+        // vertices in order of first appearance
+        std::vector<int64_t> slot_order(m > 0 ? m : 1);
+        const int64_t ns = mcbh_edge_slot_order(nodes, m, u.data(), v.data(), slot_order.data());
+        if (ns < 0) fail("slot order failed", nullptr);
         std::vector<int64_t> start(nc + 1, 0);
-        for (int64_t i = 0; i < m; i++) start[comp[i] + 1]++;
+        for (int64_t k = 0; k < ns; k++) start[comp[slot_order[k]] + 1]++;
         for (int64_t c = 0; c < nc; c++) start[c + 1] += start[c];
-        std::vector<int64_t> order(m > 0 ? m : 1), fill(start.begin(), start.end() - 1);
-        for (int64_t i = 0; i < m; i++) order[fill[comp[i]]++] = i;
+        std::vector<int64_t> order(ns > 0 ? ns : 1), fill(start.begin(), start.end() - 1);
+        for (int64_t k = 0; k < ns; k++) order[fill[comp[slot_order[k]]]++] = slot_order[k];
         std::vector<int32_t> local(nodes, -1);
         std::vector<Job> jobs;
         jobs.reserve(nc);
@@ -435,13 +441,14 @@ int main(int argc, char **argv) {
             std::vector<int32_t> cu, cv, cw, ids;
             for (int64_t k = start[c]; k < start[c + 1]; k++) {
                 const int64_t e = order[k];
-                for (int32_t x : {u[e], v[e]})
+                const int32_t hi = u[e] > v[e] ? u[e] : v[e], lo = u[e] > v[e] ? v[e] : u[e];
+                for (int32_t x : {hi, lo})
                     if (local[x] < 0) {
                         local[x] = (int32_t)ids.size();
                         ids.push_back(x);
                     }
-                cu.push_back(local[u[e]]);
-                cv.push_back(local[v[e]]);
+                cu.push_back(local[hi]);
+                cv.push_back(local[lo]);
                 cw.push_back(w[e]);
             }
             for (int32_t x : ids) local[x] = -1;

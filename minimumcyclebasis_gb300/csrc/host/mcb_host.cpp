@@ -1847,6 +1847,30 @@ int64_t mcbh_gen_block_tree(int32_t blocks, int32_t nmin, int32_t nmax, int32_t 
     return emit(out, u, v, w, nodes);
 }
 
+int64_t mcbh_edge_slot_order(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v, int64_t *order) {
+    if (nodes <= 0 || m < 0 || (m > 0 && (!u || !v || !order))) return MCBH_E_ARG;
+    for (int64_t i = 0; i < m; i++)
+        if (u[i] < 0 || u[i] >= nodes || v[i] < 0 || v[i] >= nodes) return MCBH_E_ARG;
+    try {
+        // the 2m slots as csr_graph::insert(a, b, w, false) pushes them, sorted by
+        // (row, col) with std::sort: the permutation the reference's CSR gets, parallel
+        // edges included (only the comparison outcomes decide it)
+        std::vector<EdgeSlot> s;
+        s.reserve(2 * (size_t)m);
+        for (int64_t i = 0; i < m; i++) {
+            s.push_back({(u32)u[i], (u32)v[i], 0, -1, (int)i, 0});
+            s.push_back({(u32)v[i], (u32)u[i], 0, -1, (int)i, 0});
+        }
+        std::sort(s.begin(), s.end(), RowColLess());
+        int64_t k = 0;
+        for (const EdgeSlot &e : s)
+            if (e.row > e.col) order[k++] = e.orig;
+        return k;
+    } catch (const std::bad_alloc &) {
+        return MCBH_E_NOMEM;
+    }
+}
+
 int64_t mcbh_bcc_split(int32_t nodes, int64_t m, const int32_t *u, const int32_t *v, int32_t *comp_of_edge) {
     if (nodes <= 0 || m < 0 || (m > 0 && (!u || !v || !comp_of_edge))) return MCBH_E_ARG;
     for (int64_t i = 0; i < m; i++)

@@ -132,33 +132,51 @@ def batch_graphs(count: int, nmin: int = 50, nmax: int = 5000, deg_lo: float = 2
     return out
 
 
-def bcc_split(g: Graph, keep_bridges: bool = False) -> list[Graph]:
+def bcc_split(g: Graph, keep_bridges: bool = False, with_ids: bool = False) -> list:
     """The biconnected components of g as graphs of their own, in order of their first
-    edge; a component's vertices are numbered in order of first appearance in its
-    edges (input order), as the reference's Relabeller numbers a component file
-    (bicc/Relabeller.cpp).  Components without a cycle (bridges) are dropped unless
-    keep_bridges.  The minimum cycle basis of g is the union of the components' bases."""
+    edge, each exactly as the reference's bicc tool + Relabeller hand it to the mcb
+    driver: its edges in the order the tool writes them (the input CSR's slots with
+    row > column, in slot order, as (row, column); mcbh_edge_slot_order) and its
+    vertices numbered in order of first appearance in that sequence
+    (bicc/include/bicc.h:220-314, bicc/Relabeller.cpp:72-126), so every component's
+    candidates, order and basis equal the reference's per-component run.  Components
+    without a cycle (bridges) are dropped unless keep_bridges.  The minimum cycle basis
+    of g is the union of the components' bases.  with_ids: (graph, input vertex of
+    every component vertex) pairs."""
     comp = np.empty(max(g.m, 1), np.int32)
-    nc = host_lib().mcbh_bcc_split(g.nodes, g.m, ptr(g.u), ptr(g.v), ptr(comp))
+    lib = host_lib()
+    nc = lib.mcbh_bcc_split(g.nodes, g.m, ptr(g.u), ptr(g.v), ptr(comp))
     if nc < 0:
         raise ValueError("bad graph for the biconnected split")
     comp = comp[:g.m]
-    order = np.argsort(comp, kind="stable")
-    bounds = np.searchsorted(comp[order], np.arange(nc + 1))
+    order = np.empty(max(g.m, 1), np.int64)
+    k = lib.mcbh_edge_slot_order(g.nodes, g.m, ptr(g.u), ptr(g.v), ptr(order))
+    if k < 0:
+        raise ValueError("bad graph for the slot order")
+    order = order[:k]
+    # every component's edges in slot order (a stable split of the slot sequence)
+    cs = comp[order]
+    grouped = order[np.argsort(cs, kind="stable")]
+    bounds = np.searchsorted(np.sort(cs), np.arange(nc + 1))
+    hi = np.maximum(g.u, g.v).astype(np.int32)
+    lo = np.minimum(g.u, g.v).astype(np.int32)
     out = []
     for c in range(nc):
-        idx = order[bounds[c]:bounds[c + 1]]
-        u, v, w = g.u[idx], g.v[idx], g.w[idx]
+        idx = grouped[bounds[c]:bounds[c + 1]]
+        if idx.size == 0:
+            continue
+        r, q, w = hi[idx], lo[idx], g.w[idx]
         verts = np.empty(2 * idx.size, np.int32)
-        verts[0::2], verts[1::2] = u, v
+        verts[0::2], verts[1::2] = r, q
         uniq, first = np.unique(verts, return_index=True)
+        ids = uniq[np.argsort(first, kind="stable")]  # input vertex of each component vertex
         rank = np.empty(uniq.size, np.int32)
         rank[np.argsort(first, kind="stable")] = np.arange(uniq.size, dtype=np.int32)
-        relabel = dict(zip(uniq.tolist(), rank.tolist()))
-        cu = np.fromiter((relabel[x] for x in u.tolist()), np.int32, idx.size)
-        cv = np.fromiter((relabel[x] for x in v.tolist()), np.int32, idx.size)
+        cu = rank[np.searchsorted(uniq, r)]
+        cv = rank[np.searchsorted(uniq, q)]
         if keep_bridges or idx.size >= uniq.size:
-            out.append(Graph(int(uniq.size), cu, cv, np.ascontiguousarray(w)))
+            cg = Graph(int(uniq.size), cu.astype(np.int32), cv.astype(np.int32), np.ascontiguousarray(w))
+            out.append((cg, ids.astype(np.int32)) if with_ids else cg)
     return out
 
 
