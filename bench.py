@@ -849,10 +849,10 @@ def main():
     ap.add_argument("--train-graphs", type=int, default=3, help="graphs whose traces train the proposal")
     ap.add_argument("--train-n", type=int, default=60000, help="size (--n units) of the training graphs")
     ap.add_argument("--train-epochs", type=int, default=20)
-    ap.add_argument("--proposal-rule", choices=["tail", "top"], default="tail",
-                    help="tail: expected selections beyond the prefix <= --eps; top: ceil(N (1 + margin)) top scores")
+    ap.add_argument("--proposal-rule", choices=["tail", "top"], default="top",
+                    help="top: ceil(N (1 + margin)) top scores; tail: expected selections beyond the prefix <= --eps")
     ap.add_argument("--eps", type=float, default=0.1)
-    ap.add_argument("--margin", type=float, default=0.05)
+    ap.add_argument("--margin", type=float, default=1.0)
     ap.add_argument("--plain-windows", type=int, default=8)
     ap.add_argument("--plain-width", type=int, default=128)
     ap.add_argument("--batch-count", type=int, default=4096)
