@@ -321,6 +321,15 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
                       const int32_t *edge_coord, int32_t num_coords, const int32_t *fvs_array,
                       const uint32_t *fvs_vertices, int32_t fvs_size, const uint32_t *pair_slot, int32_t chunk);
 int mcbgpu_gen_trees(mcbgpu_gen *g, int32_t t0, int32_t count, uint8_t *tied, void *stream);
+/* mcbgpu_gen_trees in two halves, so that the trees of the next chunk run while the
+ * host searches the current chunk's tied roots: submit enqueues a chunk's trees into
+ * one of two slots and returns; collect waits for the chunk submitted at t0, gives
+ * its tie flags and makes it the current chunk (for mcbgpu_gen_put_trees and
+ * mcbgpu_gen_candidates).  At most two chunks are submitted and not collected. */
+int mcbgpu_gen_trees_submit(mcbgpu_gen *g, int32_t t0, int32_t count, void *stream);
+int mcbgpu_gen_trees_collect(mcbgpu_gen *g, int32_t t0, uint8_t *tied, void *stream);
+/* 1 while the tree kernel's launch shapes are still being timed (mcbgpu_gen_tree_shapes). */
+int mcbgpu_gen_tuning(const mcbgpu_gen *g);
 int mcbgpu_gen_put_trees(mcbgpu_gen *g, const int32_t *trees, int32_t count, const int32_t *dist,
                          const int32_t *parent_slot, void *stream);
 int mcbgpu_gen_candidates(mcbgpu_gen *g, int64_t *counts, int64_t *total, void *stream);

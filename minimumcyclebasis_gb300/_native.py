@@ -131,6 +131,9 @@ GPU_SYMBOLS = {
     "mcbgpu_batch_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "mcbgpu_gen_create": (C.c_int, [C.POINTER(vp), i32, i64, vp, vp, vp, vp, vp, vp, i32, vp, vp, i32, vp, i32]),
     "mcbgpu_gen_trees": (C.c_int, [vp, i32, i32, vp, vp]),
+    "mcbgpu_gen_trees_submit": (C.c_int, [vp, i32, i32, vp]),
+    "mcbgpu_gen_trees_collect": (C.c_int, [vp, i32, vp, vp]),
+    "mcbgpu_gen_tuning": (C.c_int, [vp]),
     "mcbgpu_gen_put_trees": (C.c_int, [vp, vp, i32, vp, vp, vp]),
     "mcbgpu_gen_candidates": (C.c_int, [vp, vp, C.POINTER(i64), vp]),
     "mcbgpu_gen_fetch": (C.c_int, [vp, i64, vp, vp, vp]),

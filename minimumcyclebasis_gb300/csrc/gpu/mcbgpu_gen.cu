@@ -27,6 +27,7 @@
 // bit (MCBGPU_E_DEVICE) instead of being followed, and every walk is bounded by n'.
 #include <algorithm>
 #include <climits>
+#include <cstring>
 #include <vector>
 
 #include "mcbgpu_sssp.cuh"
@@ -485,7 +486,17 @@ struct mcbgpu_gen {
     std::vector<TreeShape> shapes;
     std::vector<double> shape_us;  // microseconds per root, per shape tried
     int chosen = -1;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // two tree slots, so that the trees of the next chunk run while the host searches
+    // the current chunk's tied roots: distances, tie flags (device and pinned host),
+    // the events around the launch, and what was submitted into each
+    int32_t *d_dist_slot[2] = {nullptr, nullptr};
+    uint8_t *d_tied_slot[2] = {nullptr, nullptr};
+    uint8_t *h_tied[2] = {nullptr, nullptr};
+    cudaEvent_t ev_begin[2] = {nullptr, nullptr}, ev_end[2] = {nullptr, nullptr};
+    int32_t slot_t0[2] = {-1, -1}, slot_count[2] = {0, 0};
+    int slot_shape[2] = {-1, -1};
+    int submitted = 0;
+    int cur_slot = 0;
     // graph
     uint32_t *d_ro = nullptr, *d_rows = nullptr, *d_cols = nullptr, *d_rev = nullptr, *d_pairs = nullptr,
              *d_roots = nullptr;
@@ -528,10 +539,15 @@ static void gen_free_lists(mcbgpu_gen *g) {
 }
 
 static void gen_free(mcbgpu_gen *g) {
-    if (g->ev0) cudaEventDestroy(g->ev0);
-    if (g->ev1) cudaEventDestroy(g->ev1);
+    for (int k = 0; k < 2; k++) {
+        if (g->ev_begin[k]) cudaEventDestroy(g->ev_begin[k]);
+        if (g->ev_end[k]) cudaEventDestroy(g->ev_end[k]);
+        if (g->h_tied[k]) cudaFreeHost(g->h_tied[k]);
+        cudaFree(g->d_tied_slot[k]);
+    }
+    cudaFree(g->d_dist_slot[1]);  // slot 0's distances are d_dist
     void *ps[] = {g->d_ro,   g->d_rows,    g->d_cols,   g->d_rev,    g->d_pairs,  g->d_roots,  g->d_w,
-                  g->d_ec,   g->d_fvs,     g->d_pedge,  g->d_dist,   g->d_code,   g->d_jump,   g->d_bits,
+                  g->d_ec,   g->d_fvs,     g->d_pedge,  g->d_dist_slot[0], g->d_code, g->d_jump, g->d_bits,
                   g->d_gdist, g->d_next,   g->d_gdirty, g->d_gsumm, g->d_tied,   g->d_counts, g->d_coff,   g->d_cpair,
                   g->d_cweight, g->d_nlong, g->d_status};
     for (void *p : ps) cudaFree(p);
@@ -667,6 +683,7 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
     GALLOC(g->d_roots, 4 * (size_t)fvs_size);
     GALLOC(g->d_pedge, 4 * n * (size_t)fvs_size);
     GALLOC(g->d_dist, 4 * n * C);
+    g->d_dist_slot[0] = g->d_dist;
     GALLOC(g->d_code, 4 * n * C);
     GALLOC(g->d_jump, 8 * n * C);
     GALLOC(g->d_bits, 4 * (size_t)g->words_per_root * C);
@@ -689,8 +706,14 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
         g->shapes = {{256, 8, 8}, {256, 8, 4}, {256, 8, 2}, {256, 8, 16}, {512, 4, 8}, {128, 16, 8}};
     const int nchunks = (fvs_size + g->chunk - 1) / g->chunk;
     if (nchunks < 2 * (int)g->shapes.size()) g->chosen = 0;
-    if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);
-    if (e == cudaSuccess) e = cudaEventCreate(&g->ev1);
+    for (int k = 0; k < 2; k++) {
+        if (e == cudaSuccess) e = cudaEventCreate(&g->ev_begin[k]);
+        if (e == cudaSuccess) e = cudaEventCreate(&g->ev_end[k]);
+        if (e == cudaSuccess) e = cudaMallocHost((void **)&g->h_tied[k], C);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&g->d_tied_slot[k], C);
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void **)&g->d_dist_slot[1], 4 * n * C);
+    g->bytes += 4ll * (long long)n * (long long)C + 2ll * (long long)C;
 #undef GALLOC
     auto up = [&](void *dst, const void *src, size_t b) {
         if (e == cudaSuccess) e = cudaMemcpy(dst, src, b, cudaMemcpyHostToDevice);
@@ -718,32 +741,45 @@ int mcbgpu_gen_create(mcbgpu_gen **out, int32_t nodes, int64_t slots, const uint
     return MCBGPU_OK;
 }
 
-int mcbgpu_gen_trees(mcbgpu_gen *g, int32_t t0, int32_t count, uint8_t *tied, void *stream) {
-    if (!g || t0 < 0 || count <= 0 || count > g->chunk || t0 + (int64_t)count > g->F || !tied) {
-        set_error("mcbgpu_gen_trees: invalid arguments");
+int mcbgpu_gen_trees_submit(mcbgpu_gen *g, int32_t t0, int32_t count, void *stream) {
+    if (!g || t0 < 0 || count <= 0 || count > g->chunk || t0 + (int64_t)count > g->F) {
+        set_error("mcbgpu_gen_trees_submit: invalid arguments");
         return MCBGPU_E_ARG;
     }
     if (!g->d_pedge) {
-        set_error("mcbgpu_gen_trees: the trees were released");
+        set_error("mcbgpu_gen_trees_submit: the trees were released");
+        return MCBGPU_E_STATE;
+    }
+    const int k = g->submitted & 1;
+    if (g->slot_t0[k] >= 0) {
+        set_error("mcbgpu_gen_trees_submit: both tree slots are taken (collect a chunk first)");
         return MCBGPU_E_STATE;
     }
     cudaStream_t st = (cudaStream_t)stream;
+    // the shape: the next untried one while tuning; once every shape has been
+    // submitted, the fastest collected so far (the chosen one once all are timed)
+    int si;
+    if (g->chosen >= 0)
+        si = g->chosen;
+    else if (g->submitted < (int)g->shapes.size())
+        si = g->submitted;
+    else
+        si = g->shape_us.empty() ? 0
+                                 : (int)(std::min_element(g->shape_us.begin(), g->shape_us.end()) - g->shape_us.begin());
+    const TreeShape shape = g->shapes[(size_t)si];
     MCB_CUDA(cudaMemsetAsync(g->d_next, 0, 4, st));
     TreeArgs a;
     a.ro = g->d_ro;
     a.cols = g->d_cols;
     a.w = g->d_w;
     a.rev = g->d_rev;
-    // the shape of this call: the next untried one while tuning, else the chosen one
-    const int si = g->chosen >= 0 ? g->chosen : (int)g->shape_us.size();
-    const TreeShape shape = g->shapes[(size_t)si];
     a.n = g->n;
     a.delta = shape_delta(shape, g->delta);
     a.roots = g->d_roots + t0;
     a.count = count;
-    a.dist_out = g->d_dist;
+    a.dist_out = g->d_dist_slot[k];
     a.pedge_out = g->d_pedge + (size_t)t0 * g->n;
-    a.tied_out = g->d_tied;
+    a.tied_out = g->d_tied_slot[k];
     a.gdist = g->d_gdist;
     a.gdirty = g->d_gdirty;
     a.gsumm = g->d_gsumm;
@@ -751,23 +787,62 @@ int mcbgpu_gen_trees(mcbgpu_gen *g, int32_t t0, int32_t count, uint8_t *tied, vo
     a.status = g->d_status;
     const int cap = g->sm_count * shape.ctas_per_sm;
     const int grid = count < cap ? count : cap;
-    MCB_CUDA(cudaEventRecord(g->ev0, st));
+    MCB_CUDA(cudaEventRecord(g->ev_begin[k], st));
     MCB_CUDA(launch_trees(g->shared_form, shape, grid, g->smem, st, a));
-    MCB_CUDA(cudaEventRecord(g->ev1, st));
-    MCB_CUDA(cudaMemcpyAsync(tied, g->d_tied, (size_t)count, cudaMemcpyDeviceToHost, st));
+    MCB_CUDA(cudaEventRecord(g->ev_end[k], st));
+    MCB_CUDA(cudaMemcpyAsync(g->h_tied[k], g->d_tied_slot[k], (size_t)count, cudaMemcpyDeviceToHost, st));
+    g->slot_t0[k] = t0;
+    g->slot_count[k] = count;
+    g->slot_shape[k] = si;
+    g->submitted++;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_gen_trees_collect(mcbgpu_gen *g, int32_t t0, uint8_t *tied, void *stream) {
+    if (!g || !tied) {
+        set_error("mcbgpu_gen_trees_collect: invalid arguments");
+        return MCBGPU_E_ARG;
+    }
+    const int k = g->slot_t0[0] == t0 ? 0 : g->slot_t0[1] == t0 ? 1 : -1;
+    if (k < 0 || t0 < 0) {
+        set_error("mcbgpu_gen_trees_collect: no chunk at tree %d was submitted", (int)t0);
+        return MCBGPU_E_STATE;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    MCB_CUDA(cudaEventSynchronize(g->ev_end[k]));
+    const int count = g->slot_count[k];
+    // the tie flags' copy follows ev_end on the same stream
+    MCB_CUDA(cudaStreamSynchronize(st));
+    std::memcpy(tied, g->h_tied[k], (size_t)count);
     g->cur_t0 = t0;
     g->cur_count = count;
+    g->cur_slot = k;
+    g->d_dist = g->d_dist_slot[k];
     const int rc = check_status(g, st, "mcbgpu_gen_trees");
     if (rc) return rc;
-    if (g->chosen < 0) {
+    const int si = g->slot_shape[k];
+    if (g->chosen < 0 && si == (int)g->shape_us.size() && si < (int)g->shapes.size()) {
         float ms = 0;
-        MCB_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+        MCB_CUDA(cudaEventElapsedTime(&ms, g->ev_begin[k], g->ev_end[k]));
         g->shape_us.push_back(1e3 * (double)ms / count);
         if (g->shape_us.size() == g->shapes.size())
             g->chosen = (int)(std::min_element(g->shape_us.begin(), g->shape_us.end()) - g->shape_us.begin());
     }
+    g->slot_t0[k] = -1;  // free for the next submission (its distances stay until then)
     return MCBGPU_OK;
 }
+
+int mcbgpu_gen_trees(mcbgpu_gen *g, int32_t t0, int32_t count, uint8_t *tied, void *stream) {
+    if (!tied) {
+        set_error("mcbgpu_gen_trees: invalid arguments");
+        return MCBGPU_E_ARG;
+    }
+    int rc = mcbgpu_gen_trees_submit(g, t0, count, stream);
+    if (rc) return rc;
+    return mcbgpu_gen_trees_collect(g, t0, tied, stream);
+}
+
+int mcbgpu_gen_tuning(const mcbgpu_gen *g) { return g && g->chosen < 0 ? 1 : 0; }
 
 int mcbgpu_gen_put_trees(mcbgpu_gen *g, const int32_t *trees, int32_t count, const int32_t *dist,
                          const int32_t *parent_slot, void *stream) {

@@ -33,9 +33,11 @@ class GpuGen:
         fa, fv = p.fvs()
         pairs = p.pairs()
         self.n, self.F, self.N = p.n, p.F, p.N
-        if chunk <= 0:  # about 4 GB of per-chunk buffers (16 bytes per vertex and root)
-            chunk = int(min(4096, max(256, (4 << 30) // max(16 * self.n + len(pairs) // 8, 1))))
+        if chunk <= 0:  # about 12 GB of per-chunk buffers (20 bytes per vertex and root)
+            chunk = int(min(8192, max(256, (12 << 30) // max(20 * self.n + len(pairs) // 8, 1))))
         self.chunk = min(chunk, self.F)
+        # chunks while the tree kernel's shapes are timed: two waves of the largest grid
+        self.tune_count = min(self.chunk, 2 * 16 * 152)
         h = C.c_void_p()
         check_gpu(self.lib.mcbgpu_gen_create(C.byref(h), self.n, len(cols), ptr(ro), ptr(rows), ptr(cols),
                                              ptr(np.ascontiguousarray(w, np.int32)), ptr(rev), ptr(ec), self.N,
@@ -46,6 +48,18 @@ class GpuGen:
         tied = np.zeros(max(count, 1), np.uint8)
         check_gpu(self.lib.mcbgpu_gen_trees(self._h, t0, count, ptr(tied), _stream(stream)), "mcbgpu_gen_trees")
         return tied[:count]
+
+    def submit(self, t0: int, count: int, stream=0) -> None:
+        check_gpu(self.lib.mcbgpu_gen_trees_submit(self._h, t0, count, _stream(stream)), "mcbgpu_gen_trees_submit")
+
+    def collect(self, t0: int, count: int, stream=0) -> np.ndarray:
+        tied = np.zeros(max(count, 1), np.uint8)
+        check_gpu(self.lib.mcbgpu_gen_trees_collect(self._h, t0, ptr(tied), _stream(stream)),
+                  "mcbgpu_gen_trees_collect")
+        return tied[:count]
+
+    def tuning(self) -> bool:
+        return bool(self.lib.mcbgpu_gen_tuning(self._h))
 
     def put_trees(self, trees, dist, parent_slot, stream=0) -> None:
         t = np.ascontiguousarray(trees, np.int32)
@@ -138,6 +152,49 @@ class DevicePrepared:
     tree_shapes: dict = field(default_factory=dict)
 
 
+def generate_candidates(p: Problem, gen: GpuGen, threads: int = 0, stream=0):
+    """Every root's tree and candidates on the device, chunk after chunk; the roots the
+    device leaves to the host (ties) are searched on the host while the next chunk's
+    trees run.  Returns (per-root offsets, pair indices, weights: the arguments of
+    Problem.rank_candidates, as lists of arrays), the number of tied roots, and the
+    seconds spent in the host searches."""
+    F = p.F
+    state = {"next": 0}
+
+    def submit():
+        t0 = state["next"]
+        if t0 >= F:
+            return None
+        cnt = min(gen.tune_count if gen.tuning() else gen.chunk, F - t0)
+        gen.submit(t0, cnt, stream)
+        state["next"] = t0 + cnt
+        return t0, cnt
+
+    offs, pis, wis = [np.zeros(1, np.int64)], [], []
+    base, tied_total, t_host = 0, 0, 0.0
+    pending = [submit()]
+    while pending:
+        t0, cnt = pending.pop(0)
+        tied = gen.collect(t0, cnt, stream)
+        nxt = submit()  # its trees run on the device while the host searches this chunk's ties
+        if nxt is not None:
+            pending.append(nxt)
+        idx = np.nonzero(tied)[0]
+        if len(idx):
+            th = time.perf_counter()
+            d, ps = p.search_trees(t0 + idx, threads=threads)
+            gen.put_trees(t0 + idx, d, ps, stream)
+            t_host += time.perf_counter() - th
+            tied_total += len(idx)
+        pi, wi, counts = gen.candidates(cnt, stream)
+        pis.append(pi)
+        wis.append(wi)
+        offs.append(base + np.cumsum(counts))
+        base += int(counts.sum())
+    return (np.concatenate(offs), np.concatenate(pis) if pis else np.zeros(0, np.uint32),
+            np.concatenate(wis) if wis else np.zeros(0, np.int32), tied_total, t_host)
+
+
 def prepare_on_device(src, threads: int = 0, chunk: int = 0, stream=0, make_solver: bool = True,
                       keep_gen: bool = False):
     """Graph (or an unprepared Problem) -> DevicePrepared: host structure, device
@@ -155,33 +212,13 @@ def prepare_on_device(src, threads: int = 0, chunk: int = 0, stream=0, make_solv
     t1 = time.perf_counter()
     gen = GpuGen(p, chunk)
     times["device_setup"] = time.perf_counter() - t1
-    offs = [np.zeros(1, np.int64)]
-    pis, wis = [], []
-    tied_total = 0
-    t_host_search = 0.0
     t2 = time.perf_counter()
-    base = 0
-    for t0_ in range(0, p.F, gen.chunk):
-        cnt = min(gen.chunk, p.F - t0_)
-        tied = gen.trees(t0_, cnt, stream)
-        idx = np.nonzero(tied)[0]
-        if len(idx):
-            th = time.perf_counter()
-            d, ps = p.search_trees(t0_ + idx, threads=threads)
-            gen.put_trees(t0_ + idx, d, ps, stream)
-            t_host_search += time.perf_counter() - th
-            tied_total += len(idx)
-        pi, wi, counts = gen.candidates(cnt, stream)
-        pis.append(pi)
-        wis.append(wi)
-        offs.append(base + np.cumsum(counts))
-        base += int(counts.sum())
+    offs, pis, wis, tied_total, t_host_search = generate_candidates(p, gen, threads, stream)
     times["trees_and_candidates"] = time.perf_counter() - t2
     shapes = gen.tree_shapes()
     times["host_searches_of_tied_roots"] = t_host_search
     t3 = time.perf_counter()
-    p.rank_candidates(np.concatenate(offs), np.concatenate(pis) if pis else np.zeros(0, np.uint32),
-                      np.concatenate(wis) if wis else np.zeros(0, np.int32), threads=threads)
+    p.rank_candidates(offs, pis, wis, threads=threads)
     _, edge, w, tree = p.candidates()
     times["ranking"] = time.perf_counter() - t3
     t4 = time.perf_counter()

@@ -226,27 +226,15 @@ def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.05, thre
     with `margin`).  keep_logits stores the scores (host) in LearnedSolve.logits."""
     import torch
 
-    from .devprep import GpuGen
+    from .devprep import GpuGen, generate_candidates
     from .host import Graph, Problem
     times = {}
     t0 = time.perf_counter()
     p = Problem.from_graph(src) if isinstance(src, Graph) else src
     p.prepare(threads=threads, structure_only=True)
     gen = GpuGen(p)
-    pis, wis, offs, base = [], [], [np.zeros(1, np.int64)], 0
-    for t0_ in range(0, p.F, gen.chunk):
-        cnt = min(gen.chunk, p.F - t0_)
-        tied = gen.trees(t0_, cnt, stream)
-        idx = np.nonzero(tied)[0]
-        if len(idx):
-            d, ps = p.search_trees(t0_ + idx, threads=threads)
-            gen.put_trees(t0_ + idx, d, ps, stream)
-        pi, wi, counts = gen.candidates(cnt, stream)
-        pis.append(pi)
-        wis.append(wi)
-        offs.append(base + np.cumsum(counts))
-        base += int(counts.sum())
-    p.rank_candidates(np.concatenate(offs), np.concatenate(pis), np.concatenate(wis), threads=threads)
+    offs, pis, wis, _, _ = generate_candidates(p, gen, threads, stream)
+    p.rank_candidates(offs, pis, wis, threads=threads)
     _, edge, w, tree = p.candidates()
     times["generation"] = time.perf_counter() - t0
     K, N = len(w), p.N
