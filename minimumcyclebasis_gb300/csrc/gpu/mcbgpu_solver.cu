@@ -1146,7 +1146,10 @@ __device__ void materialize_tables(const TailArgs &ta, const BlockState *bs, int
 #ifdef MCB_SCAN_PROFILE
 __device__ long long g_scan_prof[4];
 #endif
-__global__ void __launch_bounds__(kPivotThreads) blk_pivot_kernel(
+#ifndef MCB_PIVOT_MINB
+#define MCB_PIVOT_MINB 1  // pivot-kernel CTAs the register budget is sized for per SM
+#endif
+__global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kernel(
     long long K, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
     const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T, int bound, BlockState *bs,
     uint64_t *Warr, unsigned *tile_epoch, unsigned long long *reports, GridBar *gb, unsigned *status,
@@ -1602,6 +1605,9 @@ size_t pivot_smem_bytes(int G) {
 // D_k ^ <beta_{<k}, gcol_k> (the sequential effect of the block's 64 updates); then
 // S_j ^= XOR_k beta_k S_{e0+k} through the tables, the group's warps split the
 // row's words.
+#ifndef MCB_UPD_CTAS
+#define MCB_UPD_CTAS 8  // block update: CTAs per SM at most (each loops over row groups)
+#endif
 constexpr int kUpdThreads = 256;
 constexpr int kUpdSplit = MCB_UPD_SPLIT;
 constexpr int kUpdGroups = kUpdThreads / 32 / kUpdSplit;  // row groups per CTA
@@ -1615,8 +1621,9 @@ __global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, lo
                                                                  const uint64_t *__restrict__ gcol,
                                                                  const unsigned *__restrict__ pairs,
                                                                  const unsigned *__restrict__ word_end,
-                                                                 unsigned long long *bytes, uint64_t *beta_out) {
-    unsigned long long nb = 0;
+                                                                 unsigned long long *bytes, uint64_t *beta_out,
+                                                                 unsigned long long *diag) {
+    unsigned long long nb = 0, n_rows = 0, n_changed = 0, n_gather = 0;
     __shared__ uint64_t sg[64];
     __shared__ uint64_t sD[2][kUpdGroups][kUpdSplit][kUpdRows];
     if (threadIdx.x < 64) sg[threadIdx.x] = (int)threadIdx.x < b ? gcol[threadIdx.x] : 0;
@@ -1663,7 +1670,12 @@ __global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, lo
             // algorithmic bytes (counted by the group's first warp): the S words the
             // group's pairs touch (8 rows share each pair, counted once per row) plus,
             // when the row changes, read + write of its first Wb words
-            if (h == 0) nb += 8ull * np + (beta ? 16ull * (unsigned long long)Wb : 0ull);
+            if (h == 0) {
+                nb += 8ull * np + (beta ? 16ull * (unsigned long long)Wb : 0ull);
+                n_rows++;
+                n_changed += beta ? 1 : 0;
+                n_gather += np;
+            }
             if (beta_out && h == 0) beta_out[g0 - row_begin + lane] = beta;  // the next block's rows (paired pass)
         }
         for (int r = 0; r < rows; r++) {
@@ -1682,8 +1694,18 @@ __global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, lo
                 Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
         }
     }
-    for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
+    for (int d = 16; d > 0; d >>= 1) {
+        nb += __shfl_xor_sync(0xffffffffu, nb, d);
+        n_rows += __shfl_xor_sync(0xffffffffu, n_rows, d);
+        n_changed += __shfl_xor_sync(0xffffffffu, n_changed, d);
+        n_gather += __shfl_xor_sync(0xffffffffu, n_gather, d);
+    }
     if (lane == 0 && nb) atomicAdd(bytes, nb);
+    if (lane == 0 && diag && n_rows) {  // far rows, changed far rows, pair words gathered
+        atomicAdd(&diag[23], n_rows);
+        atomicAdd(&diag[30], n_changed);
+        atomicAdd(&diag[31], n_gather);
+    }
 }
 
 // The update of the next block's rows (at most 3 x 64, on the critical path: the
@@ -2430,7 +2452,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             const unsigned *wend = s->d_word_end + (size_t)par * (s->P + 1);
             auto grid_for = [&](long long rows) {
                 long long g = (rows + kUpdGroups * kUpdRows - 1) / (kUpdGroups * kUpdRows);
-                return (int)std::max<long long>(1, std::min<long long>(g, (long long)sms * 8));
+                return (int)std::max<long long>(1, std::min<long long>(g, (long long)sms * MCB_UPD_CTAS));
             };
             // the last earlier far update that reaches the near rows [e0 + b, near_end)
             int wait_slot = -1;
@@ -2441,7 +2463,8 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 MCB_CUDA(cudaStreamWaitEvent(s->st2, s->ev_tail, 0));
                 Launch L(s, KC_BLK_UPDATE, s->st2);
                 blk_update_kernel<<<grid_for(far_end - near_end), kUpdThreads, 0, s->st2>>>(
-                    s->d_S, near_end, far_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes(), nullptr);
+                    s->d_S, near_end, far_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes(), nullptr,
+                    s->d_diag);
             }
             if (wait_slot >= 0) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[wait_slot], 0));
             {
