@@ -385,6 +385,28 @@ def plain_form(solver, N, stream, sh, windows=8, width=128):
             "ms_per_iteration": [round(x * 1e3, 4) for x in per_iter]}
 
 
+def forward_throughput(net, x, sh, reps: int = 10):
+    """The proposal network's forward pass (mlp_forward_kernel) over the workload's
+    K x 16 bf16 features, timed with CUDA events on its stream after 3 warm-up passes:
+    ms per pass and GB/s of its algorithmic bytes (32 B of features read and a 4 B
+    logit written per candidate; the 16 x 64 weights stay in shared memory)."""
+    import torch
+    stream = torch.cuda.ExternalStream(sh)
+    for _ in range(3):
+        net.forward(x, sh)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        net.forward(x, sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    K = int(x.shape[0])
+    return {"candidates": K, "ms": round(ms, 4), "GBps": round(36.0 * K / ms / 1e6, 1),
+            "tflops_first_layer": round(2.0 * 16 * 64 * K / ms / 1e9, 2)}
+
+
 def learned_form(args, g, sel0, tot0, sh):
     """Trains the proposal network on traces of --train-graphs smaller graphs of the
     workload's family (seeds after the workload's), then solves the workload graph
@@ -414,9 +436,11 @@ def learned_form(args, g, sel0, tot0, sh):
     # graph -> basis on the proposal's prefix (its lists copied to the host afterwards,
     # for the end-to-end steps; the untrained network's prefix on the same features
     # for comparison: neither is part of the timed solve)
-    r, lsolver, p = solve_with_proposal(g, net, margin=args.margin, stream=sh, keep_solver=True, host_lists=True,
-                                        compare=[untrained], rule=args.proposal_rule, eps=args.eps,
-                                        keep_logits=True)
+    r, lsolver, p, x = solve_with_proposal(g, net, margin=args.margin, stream=sh, keep_solver=True,
+                                           host_lists=True, compare=[untrained], rule=args.proposal_rule,
+                                           eps=args.eps, keep_logits=True, keep_features=True)
+    fwd = forward_throughput(net, x, sh)
+    del x
     g2b = r.times["total"]
     assert np.array_equal(r.selected, sel0) and r.total_weight == tot0, "the learned form's basis differs"
     uk, _ = r.compared[0]
@@ -433,7 +457,7 @@ def learned_form(args, g, sel0, tot0, sh):
                             "epochs": args.train_epochs, "loss_first_last": [round(losses[0], 4),
                                                                              round(losses[-1], 4)],
                             "traces_s": round(t_traces, 2), "train_s": round(t_train, 2)},
-               "times_s": {k: round(v, 3) for k, v in r.times.items()}}
+               "times_s": {k: round(v, 3) for k, v in r.times.items()}, "forward": fwd}
     untrained.close()
     return learned, lsolver, r.lists, g2b
 

@@ -143,17 +143,25 @@ __global__ void __launch_bounds__(kFwdThreads) mlp_forward_kernel(const uint16_t
     const int64_t ntiles = (count + kTileRows - 1) / kTileRows;
     uint32_t phase = 0;
     bool ok = true;
-    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        // this thread's row of the tile: 16 bf16 = two 16-byte halves
-        const int64_t row = tile * kTileRows + tid;
-        uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
-        if (row < count) {
-            const uint4 *src = reinterpret_cast<const uint4 *>(x + row * kIn);
-            lo = src[0];
-            hi = src[1];
+    // this thread's row of a tile: 16 bf16 = two 16-byte halves; the next tile's row
+    // is loaded while the current tile is multiplied and its epilogue runs
+    auto load_row = [&](int64_t t, uint4 &lo, uint4 &hi) {
+        const int64_t r = t * kTileRows + tid;
+        lo = make_uint4(0, 0, 0, 0);
+        hi = lo;
+        if (t < ntiles && r < count) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(x + r * kIn);
+            lo = __ldg(src);
+            hi = __ldg(src + 1);
         }
-        *reinterpret_cast<uint4 *>(sA + core_off(tid, 0)) = lo;
-        *reinterpret_cast<uint4 *>(sA + core_off(tid, 8)) = hi;
+    };
+    uint4 nlo, nhi;
+    load_row(blockIdx.x, nlo, nhi);
+    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int64_t row = tile * kTileRows + tid;
+        *reinterpret_cast<uint4 *>(sA + core_off(tid, 0)) = nlo;
+        *reinterpret_cast<uint4 *>(sA + core_off(tid, 8)) = nhi;
+        load_row(tile + gridDim.x, nlo, nhi);
         fence_proxy_async_smem();  // generic-proxy writes -> visible to the tensor core
         tc_fence_before();
         cta_sync();
@@ -334,7 +342,9 @@ static int mlp_forward(mcbgpu_mlp *m, const uint16_t *x, int64_t count, float *l
                        cudaStream_t st) {
     if (count <= 0) return MCBGPU_OK;
     const int64_t tiles = (count + kTileRows - 1) / kTileRows;
-    const int grid = (int)std::min<int64_t>(tiles, (int64_t)(m->sm_count > 0 ? m->sm_count : 148) * 4);
+    // 8 CTAs per SM: 8 x 64 TMEM columns fill the SM's 512, and with the prefetch of
+    // the next tile 16 tiles of features are in flight per SM
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)(m->sm_count > 0 ? m->sm_count : 148) * 8);
     mlp_forward_kernel<<<grid, kFwdThreads, 0, st>>>(x, count, m->d_w1, m->d_params + kHid * kIn,
                                                      m->d_w2r, m->d_params + kParams - 1, logits, hidden,
                                                      m->d_status);

@@ -104,8 +104,8 @@ enum KernelClass {
     KC_BLK_UPDATE, KC_SEARCH, KC_UPDATE, KC_CYCLE, KC_RESET, KC_VALIDATE, KC_WFIX, KC_BLK_UPDATE_NEAR, KC_COUNT
 };
 const char *const kKernelNames[KC_COUNT] = {
-    "init_identity", "tile_minc", "blk_transpose", "blk_w", "blk_pivot", "blk_update", "search", "update",
-    "cycle_vector", "reset_state", "validate", "blk_wfix", "blk_update_near"};
+    "init_identity", "tile_minc", "blk_transpose", "blk_w", "blk_pivot", "far_update", "search", "update",
+    "cycle_vector", "reset_state", "validate", "blk_wfix", "near_update"};
 
 struct IterSlot {            // state of one per-iteration search
     unsigned long long best; // first odd rank (kNone until found)
@@ -1612,42 +1612,111 @@ constexpr int kUpdThreads = 256;
 constexpr int kUpdSplit = MCB_UPD_SPLIT;
 constexpr int kUpdGroups = kUpdThreads / 32 / kUpdSplit;  // row groups per CTA
 
-// Rows [row_begin, row_end) of the block that starts at e0 with b iterations; gcol,
-// tab, pairs and word_end are that block's (they are double-buffered by block
-// parity, so the next block's tail can run while these rows are updated).
-__global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, long long row_begin, long long row_end,
-                                                                 int P, int b, int Wb, int Pt,
-                                                                 const uint64_t *__restrict__ tab,
-                                                                 const uint64_t *__restrict__ gcol,
-                                                                 const unsigned *__restrict__ pairs,
-                                                                 const unsigned *__restrict__ word_end,
-                                                                 unsigned long long *bytes, uint64_t *beta_out,
-                                                                 unsigned long long *diag) {
-    unsigned long long nb = 0, n_rows = 0, n_changed = 0, n_gather = 0;
-    __shared__ uint64_t sg[64];
-    __shared__ uint64_t sD[2][kUpdGroups][kUpdSplit][kUpdRows];
-    if (threadIdx.x < 64) sg[threadIdx.x] = (int)threadIdx.x < b ? gcol[threadIdx.x] : 0;
+// beta of a row is a linear function of its D over GF(2): beta_k = D_k ^ <beta_{<k},
+// gcol_k> gives beta = D (I + G)^-1, G[i][k] = bit i of gcol_k.  Row i of that inverse,
+// V_i, is the recurrence run on D = e_i, so beta = XOR of V_i over the set bits i of
+// D; tab[g][pat] = XOR of V_{8g+i} over the bits i of pat turns that into eight
+// lookups.  Built by the whole CTA from the block's gcol (b <= 64 columns).
+__device__ void build_beta_tables(const uint64_t *__restrict__ gcol, int b, uint64_t (*tab)[256]) {
+    __shared__ uint64_t sV[64], sg[64];
+    if (threadIdx.x < 64) sg[threadIdx.x] = (int)threadIdx.x < b ? gcol[threadIdx.x] : 0ull;
     cta_sync();
+    if (threadIdx.x < 64) {
+        const int i = threadIdx.x;
+        uint64_t v = 0;
+        for (int k = 0; k < b; k++) v |= ((uint64_t)((k == i) ^ parity64(v & sg[k]))) << k;
+        sV[i] = v;
+    }
+    cta_sync();
+    for (int idx = threadIdx.x; idx < 8 * 256; idx += blockDim.x) {
+        const int g = idx >> 8;
+        uint64_t acc = 0;
+        for (unsigned m = (unsigned)(idx & 255); m; m &= m - 1) acc ^= sV[8 * g + __ffs(m) - 1];
+        tab[g][idx & 255] = acc;
+    }
+    cta_sync();
+}
+
+// The far update of a block: every row j >= row_begin (the rows past the near
+// update's) takes D_j = <C_sel_k, S_j> (k < b), beta_j = D_j (I + G)^-1 and
+// S_j ^= XOR_k beta_jk S_{e0+k} over the first Wb words.  Most far rows are still
+// their unit vector (S_j = e_j: no update has reached them yet), and for those
+// D_j bit k is simply whether coordinate j lies on the selected cycle C_sel_k.  So
+// the update runs in three launches, all on the far stream:
+//   far_scatter_kernel: every (coordinate c, k) pair of the block's selected cycles
+//     with c a unit far row sets bit k of Dfar[c] (first touch lists c);
+//   far_rows_kernel:    the non-unit far rows (a list carried from update to update)
+//     gather D from their words, as the reference's update does;
+//   far_touch_kernel:   the touched unit rows apply their scattered D.
+// A row that changes is no longer a unit vector: it leaves the unit set and joins
+// the non-unit list the next far update reads.  Far-row starts never decrease from
+// block to block (the near rows of a block are below every later far range), so a
+// listed row below the current start is dropped for good.
+// Rows in groups of kUpdRows list entries, kUpdSplit warps per group.  D_j (64 bits):
+// the group's warps split the chosen cycles' (coordinate, k) pairs, sorted by S word,
+// and each pair is applied to all rows of the group (independent gathers); pairs
+// whose word lies above the group's last row are skipped (S_j has support [0, j]).
+// The warps' partial D's meet in shared memory (two buffers by iteration parity, one
+// named barrier per group and iteration).  gcol, tab, pairs and word_end are the
+// block's (double-buffered by block parity, so the next block's tail can run while
+// these rows are updated).
+__global__ void __launch_bounds__(kUpdThreads) far_rows_kernel(uint64_t *S, long long row_begin, int P, int b,
+                                                               int Wb, int Pt, const uint64_t *__restrict__ tab,
+                                                               const uint64_t *__restrict__ gcol,
+                                                               const unsigned *__restrict__ pairs,
+                                                               const unsigned *__restrict__ word_end,
+                                                               const int32_t *__restrict__ list_in,
+                                                               const unsigned *__restrict__ n_in, int32_t *list_out,
+                                                               unsigned *n_out, unsigned long long *bytes,
+                                                               unsigned long long *diag) {
+    const unsigned nlist = *n_in;
+    const long long groups = (long long)gridDim.x * kUpdGroups;
+    if ((long long)blockIdx.x * kUpdGroups * kUpdRows >= (long long)nlist) return;  // no rows for this CTA
+    unsigned long long nb = 0, n_rows = 0, n_changed = 0, n_gather = 0, n_betabits = 0;
+    __shared__ uint64_t btab[8][256];
+    __shared__ uint64_t sD[2][kUpdGroups][kUpdSplit][kUpdRows];
+    build_beta_tables(gcol, b, btab);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gi = warp / kUpdSplit, h = warp % kUpdSplit;
-    const long long groups = (long long)gridDim.x * kUpdGroups;
     int par = 0;
-    for (long long g0 = row_begin + kUpdRows * ((long long)blockIdx.x * kUpdGroups + gi); g0 < row_end;
-         g0 += kUpdRows * groups, par ^= 1) {
-        const int rows = (int)((row_end - g0) < kUpdRows ? (row_end - g0) : kUpdRows);
-        const long long jl = g0 + rows - 1;
-        const int wl = (int)(jl >> 6) + 1 < P ? (int)(jl >> 6) + 1 : P;
+    for (long long base = kUpdRows * ((long long)blockIdx.x * kUpdGroups + gi); base < (long long)nlist;
+         base += kUpdRows * groups, par ^= 1) {
+        const int rows = (int)(((long long)nlist - base) < kUpdRows ? ((long long)nlist - base) : kUpdRows);
+        // lane r < rows: its listed row, kept if still a far row
+        const long long jr = lane < rows ? (long long)__ldg(list_in + base + lane) : -1;
+        const bool keep = jr >= row_begin;
+        const unsigned kmask = __ballot_sync(0xffffffffu, keep);
+        if (h == 0 && kmask) {  // carried over to the next far update
+            unsigned o = 0;
+            if (lane == 0) o = atomicAdd(n_out, (unsigned)__popc(kmask));
+            o = __shfl_sync(0xffffffffu, o, 0);
+            if (keep) list_out[o + __popc(kmask & ((1u << lane) - 1u))] = (int32_t)jr;
+        }
+        if (!kmask) continue;  // warp-uniform
+        long long jmax = keep ? jr : -1;
+        for (int d = 16; d > 0; d >>= 1) {
+            const long long o = __shfl_xor_sync(0xffffffffu, jmax, d);
+            jmax = o > jmax ? o : jmax;
+        }
+        const int wl = (int)(jmax >> 6) + 1 < P ? (int)(jmax >> 6) + 1 : P;
         const unsigned np = __ldg(word_end + wl);
-        const uint64_t *Sg = S + (size_t)g0 * P;
+        // the group's rows as 32-bit words: bit c of a row is bit c & 31 of word c >> 5
+        const uint32_t *Sr[kUpdRows];
+#pragma unroll
+        for (int r = 0; r < kUpdRows; r++) {
+            const long long j = __shfl_sync(0xffffffffu, jr, r);
+            Sr[r] = ((kmask >> r) & 1u) ? reinterpret_cast<const uint32_t *>(S + (size_t)j * P) : nullptr;
+        }
         uint64_t D[kUpdRows];
 #pragma unroll
         for (int r = 0; r < kUpdRows; r++) D[r] = 0;
         for (unsigned i = h * 32 + lane; i < np; i += 32 * kUpdSplit) {
             const unsigned pr = __ldg(pairs + i);
-            const unsigned c = pr >> 6, k = pr & 63u, w = c >> 6, sh = c & 63u;
+            const unsigned c = pr >> 6, q = c >> 5, sh = c & 31u;
+            const uint64_t m = 1ull << (pr & 63u);
 #pragma unroll
             for (int r = 0; r < kUpdRows; r++)
-                if (r < rows) D[r] ^= ((Sg[(size_t)r * P + w] >> sh) & 1ull) << k;
+                if (Sr[r] && ((Sr[r][q] >> sh) & 1u)) D[r] ^= m;
         }
         uint64_t Dmine = 0;
 #pragma unroll
@@ -1665,23 +1734,24 @@ __global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, lo
             }
         }
         uint64_t beta = 0;
-        if (lane < rows) {
-            for (int k = 0; k < b; k++) beta |= ((((Dmine >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]))) << k;
+        if (keep) {
+#pragma unroll
+            for (int g = 0; g < 8; g++) beta ^= btab[g][(Dmine >> (8 * g)) & 255];
             // algorithmic bytes (counted by the group's first warp): the S words the
-            // group's pairs touch (8 rows share each pair, counted once per row) plus,
-            // when the row changes, read + write of its first Wb words
+            // group's pairs touch plus, when the row changes, read + write of its
+            // first Wb words
             if (h == 0) {
                 nb += 8ull * np + (beta ? 16ull * (unsigned long long)Wb : 0ull);
                 n_rows++;
                 n_changed += beta ? 1 : 0;
                 n_gather += np;
+                n_betabits += (unsigned)__popcll(beta);
             }
-            if (beta_out && h == 0) beta_out[g0 - row_begin + lane] = beta;  // the next block's rows (paired pass)
         }
         for (int r = 0; r < rows; r++) {
             const uint64_t bt = __shfl_sync(0xffffffffu, beta, r);
             if (!bt) continue;
-            uint64_t *Sj = S + (size_t)(g0 + r) * P;
+            uint64_t *Sj = S + (size_t)__shfl_sync(0xffffffffu, jr, r) * P;
             const uint64_t *t0 = tab + ((size_t)0 * 256 + ((bt >> 0) & 255)) * Pt;
             const uint64_t *t1 = tab + ((size_t)1 * 256 + ((bt >> 8) & 255)) * Pt;
             const uint64_t *t2 = tab + ((size_t)2 * 256 + ((bt >> 16) & 255)) * Pt;
@@ -1699,18 +1769,102 @@ __global__ void __launch_bounds__(kUpdThreads) blk_update_kernel(uint64_t *S, lo
         n_rows += __shfl_xor_sync(0xffffffffu, n_rows, d);
         n_changed += __shfl_xor_sync(0xffffffffu, n_changed, d);
         n_gather += __shfl_xor_sync(0xffffffffu, n_gather, d);
+        n_betabits += __shfl_xor_sync(0xffffffffu, n_betabits, d);
     }
     if (lane == 0 && nb) atomicAdd(bytes, nb);
-    if (lane == 0 && diag && n_rows) {  // far rows, changed far rows, pair words gathered
+    if (lane == 0 && diag && n_rows) {  // gathered far rows, changed ones, pair words gathered, beta bits
         atomicAdd(&diag[23], n_rows);
         atomicAdd(&diag[30], n_changed);
         atomicAdd(&diag[31], n_gather);
+        atomicAdd(&diag[29], n_betabits);
+    }
+}
+
+// Every pair (c, k) of the block's sorted pairs with c a unit row in [row_begin,
+// row_end): bit k of Dfar[c] (a cycle's coordinates are distinct, so the bits of one
+// row come from distinct cycles and OR is XOR); a row's first touch lists it.
+__global__ void __launch_bounds__(256) far_scatter_kernel(const unsigned *__restrict__ pairs,
+                                                         const unsigned *__restrict__ word_end, int P,
+                                                         long long row_begin, long long row_end,
+                                                         const uint8_t *__restrict__ unit, unsigned long long *Dfar,
+                                                         int32_t *touch, unsigned *n_touch,
+                                                         unsigned long long *bytes) {
+    const unsigned np = __ldg(word_end + P);
+    unsigned long long nb = 0;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const unsigned pr = __ldg(pairs + i);
+        const long long c = (long long)(pr >> 6);
+        nb += 4;
+        if (c < row_begin || c >= row_end || !unit[c]) continue;
+        const unsigned long long old = atomicOr(Dfar + c, 1ull << (pr & 63u));
+        if (!old) touch[atomicAdd(n_touch, 1u)] = (int32_t)c;
+        nb += 8;
+    }
+    for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
+    if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
+}
+
+// The touched unit rows, one warp each: beta from the scattered D (never zero: the
+// map D -> beta is invertible), S_c ^= XOR_k beta_k S_{e0+k} over the first Wb words
+// (all zero in a unit row below its own word), then the row leaves the unit set and
+// joins the non-unit list.
+__global__ void __launch_bounds__(256) far_touch_kernel(uint64_t *S, int P, int b, int Wb, int Pt,
+                                                       const uint64_t *__restrict__ tab,
+                                                       const uint64_t *__restrict__ gcol,
+                                                       const int32_t *__restrict__ touch,
+                                                       const unsigned *__restrict__ n_touch,
+                                                       unsigned long long *Dfar, uint8_t *unit, int32_t *list_out,
+                                                       unsigned *n_out, unsigned long long *bytes,
+                                                       unsigned long long *diag) {
+    const unsigned nt = *n_touch;
+    const unsigned warps = blockDim.x >> 5;
+    if (blockIdx.x * warps >= nt) return;
+    __shared__ uint64_t btab[8][256];
+    build_beta_tables(gcol, b, btab);
+    const int lane = threadIdx.x & 31;
+    unsigned long long nb = 0, n_touched = 0, n_changed = 0, n_betabits = 0;
+    for (unsigned i = blockIdx.x * warps + (threadIdx.x >> 5); i < nt; i += gridDim.x * warps) {
+        const long long c = __ldg(touch + i);
+        uint64_t D = 0;
+        if (lane == 0) {
+            D = Dfar[c];
+            Dfar[c] = 0;  // ready for the next block
+            unit[c] = 0;
+            list_out[atomicAdd(n_out, 1u)] = (int32_t)c;
+        }
+        D = __shfl_sync(0xffffffffu, D, 0);
+        uint64_t bt = 0;
+#pragma unroll
+        for (int g = 0; g < 8; g++) bt ^= btab[g][(D >> (8 * g)) & 255];
+        if (lane == 0) {
+            nb += 8 + (bt ? 16ull * (unsigned long long)Wb : 0ull);
+            n_touched++;
+            n_changed += bt ? 1 : 0;
+            n_betabits += (unsigned)__popcll(bt);
+        }
+        if (!bt) continue;
+        uint64_t *Sj = S + (size_t)c * P;
+        const uint64_t *t0 = tab + ((size_t)0 * 256 + ((bt >> 0) & 255)) * Pt;
+        const uint64_t *t1 = tab + ((size_t)1 * 256 + ((bt >> 8) & 255)) * Pt;
+        const uint64_t *t2 = tab + ((size_t)2 * 256 + ((bt >> 16) & 255)) * Pt;
+        const uint64_t *t3 = tab + ((size_t)3 * 256 + ((bt >> 24) & 255)) * Pt;
+        const uint64_t *t4 = tab + ((size_t)4 * 256 + ((bt >> 32) & 255)) * Pt;
+        const uint64_t *t5 = tab + ((size_t)5 * 256 + ((bt >> 40) & 255)) * Pt;
+        const uint64_t *t6 = tab + ((size_t)6 * 256 + ((bt >> 48) & 255)) * Pt;
+        const uint64_t *t7 = tab + ((size_t)7 * 256 + ((bt >> 56) & 255)) * Pt;
+        for (int w = lane; w < Wb; w += 32) Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
+    }
+    if (lane == 0 && nb) atomicAdd(bytes, nb);
+    if (lane == 0 && diag && n_touched) {  // touched unit rows, changed ones, beta bits
+        atomicAdd(&diag[28], n_touched);
+        atomicAdd(&diag[30], n_changed);
+        atomicAdd(&diag[29], n_betabits);
     }
 }
 
 // The update of the next block's rows (at most 3 x 64, on the critical path: the
 // next block's transpose reads them), spread over the whole GPU in two launches
-// instead of blk_update_kernel's one warp group per 8 rows.
+// instead of one warp group per 8 rows.
 // near_d_kernel: D_j = <C_sel_k, S_j> bits for every near row j, one (row, chunk of
 // kNearChunk pairs) item per warp, XOR-accumulated into Dbuf[j - row_begin] (which
 // near_apply_kernel clears after use).
@@ -1904,6 +2058,13 @@ struct mcbgpu_solver {
     uint64_t *d_Tg = nullptr;      // the group's blocks' rows transposed, kGStride words per coordinate
     uint64_t *d_beta = nullptr;    // 3 x 192: update bits of the near rows of a group's first blocks
     unsigned long long *d_nearD = nullptr;  // kNearMaxRows: D of the near rows (zero between uses)
+    // far update: rows whose support vector is still the unit vector get D by scatter
+    uint8_t *d_unit = nullptr;               // N: 1 while S_j = e_j (far rows only kept exact)
+    unsigned long long *d_Dfar = nullptr;    // N: scattered D of unit far rows (zero between uses)
+    int32_t *d_rowlist[2] = {};              // N each: the non-unit far rows, read / written by turns
+    int32_t *d_touch = nullptr;              // N: unit far rows the scatter reached
+    unsigned *d_fcnt = nullptr;              // [rows in list 0, rows in list 1, touched rows]
+    int list_cur = 0;                        // the list the next far update reads
     uint64_t *d_masks = nullptr;   // 2 x 64: final masks of a group's first blocks
     unsigned *d_tile_epoch = nullptr;
     int32_t *d_tile_minc = nullptr;
@@ -1956,7 +2117,9 @@ struct Launch {
     int cls;
     cudaStream_t st;
     cudaEvent_t a = nullptr;
-    Launch(mcbgpu_solver *s_, int cls_, cudaStream_t st_) : s(s_), cls(cls_), st(st_) {
+    int kernels;  // kernel launches inside the bracket
+    Launch(mcbgpu_solver *s_, int cls_, cudaStream_t st_, int kernels_ = 1)
+        : s(s_), cls(cls_), st(st_), kernels(kernels_) {
         if (s->profiling) {
             a = pool_event(s);
             cudaEventRecord(a, st);
@@ -1968,7 +2131,7 @@ struct Launch {
             cudaEventRecord(b, st);
             s->recs.push_back({cls, a, b});
         }
-        s->launches++;
+        s->launches += kernels;
     }
     unsigned long long *bytes() const { return s->d_bytes + cls; }
 };
@@ -1992,6 +2155,12 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_Tg);
     cudaFree(s->d_beta);
     cudaFree(s->d_nearD);
+    cudaFree(s->d_unit);
+    cudaFree(s->d_Dfar);
+    cudaFree(s->d_rowlist[0]);
+    cudaFree(s->d_rowlist[1]);
+    cudaFree(s->d_touch);
+    cudaFree(s->d_fcnt);
     cudaFree(s->d_masks);
     cudaFree(s->d_tile_epoch);
     cudaFree(s->d_tile_minc);
@@ -2084,6 +2253,12 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
         ALLOC(s->d_masks, sizeof(uint64_t) * 2 * 64);
     }
     ALLOC(s->d_nearD, sizeof(unsigned long long) * kNearMaxRows);
+    ALLOC(s->d_unit, (size_t)N);
+    ALLOC(s->d_Dfar, sizeof(unsigned long long) * (size_t)N);
+    ALLOC(s->d_rowlist[0], sizeof(int32_t) * (size_t)N);
+    ALLOC(s->d_rowlist[1], sizeof(int32_t) * (size_t)N);
+    ALLOC(s->d_touch, sizeof(int32_t) * (size_t)N);
+    ALLOC(s->d_fcnt, sizeof(unsigned) * 4);
     ALLOC(s->d_tile_epoch, sizeof(unsigned) * ntiles);
     ALLOC(s->d_tile_minc, sizeof(int32_t) * ntiles);
     ALLOC(s->d_gbar, sizeof(GridBar));
@@ -2101,6 +2276,9 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     if (e == cudaSuccess) e = cudaMemset(s->d_tile_epoch, 0, sizeof(unsigned) * ntiles);
     if (e == cudaSuccess) e = cudaMemset(s->d_gbar, 0, sizeof(GridBar));
     if (e == cudaSuccess) e = cudaMemset(s->d_nearD, 0, sizeof(unsigned long long) * kNearMaxRows);
+    if (e == cudaSuccess) e = cudaMemset(s->d_Dfar, 0, sizeof(unsigned long long) * ((size_t)N > 0 ? (size_t)N : 2));
+    if (e == cudaSuccess) e = cudaMemset(s->d_unit, 1, (size_t)N > 0 ? (size_t)N : 16);
+    if (e == cudaSuccess) e = cudaMemset(s->d_fcnt, 0, sizeof(unsigned) * 4);
     if (e == cudaSuccess) e = cudaMemset(s->d_word_end, 0, sizeof(unsigned) * 2 * ((size_t)s->P + 1));
     // the far update fills every SM when it runs; with the critical path (transpose,
     // streaming pass, pivot search, near update) on a higher-priority stream, the
@@ -2162,6 +2340,12 @@ int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream) {
         reset_state_kernel<<<1, 32, 0, st>>>(s->d_slots, s->d_bs, s->d_status);
     }
     MCB_CUDA(cudaMemsetAsync(s->d_nearD, 0, sizeof(unsigned long long) * kNearMaxRows, st));
+    if (s->N > 0) {  // every row is a unit vector again; no non-unit rows, no scattered D left over
+        MCB_CUDA(cudaMemsetAsync(s->d_unit, 1, (size_t)s->N, st));
+        MCB_CUDA(cudaMemsetAsync(s->d_Dfar, 0, sizeof(unsigned long long) * (size_t)s->N, st));
+    }
+    MCB_CUDA(cudaMemsetAsync(s->d_fcnt, 0, sizeof(unsigned) * 4, st));
+    s->list_cur = 0;
     MCB_CUDA(cudaGetLastError());
     s->iters_run = 0;
     return MCBGPU_OK;
@@ -2461,14 +2645,25 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             if (near_end < far_end) {  // far rows: on st2 once this block's tail is done
                 MCB_CUDA(cudaEventRecord(s->ev_tail, st));
                 MCB_CUDA(cudaStreamWaitEvent(s->st2, s->ev_tail, 0));
-                Launch L(s, KC_BLK_UPDATE, s->st2);
-                blk_update_kernel<<<grid_for(far_end - near_end), kUpdThreads, 0, s->st2>>>(
-                    s->d_S, near_end, far_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, L.bytes(), nullptr,
-                    s->d_diag);
+                // scatter into the unit rows, gather the listed non-unit rows, apply the
+                // touched unit rows; the lists swap for the next far update
+                const int lin = s->list_cur, lout = 1 - lin;
+                MCB_CUDA(cudaMemsetAsync(s->d_fcnt + lout, 0, sizeof(unsigned), s->st2));
+                MCB_CUDA(cudaMemsetAsync(s->d_fcnt + 2, 0, sizeof(unsigned), s->st2));
+                Launch L(s, KC_BLK_UPDATE, s->st2, 3);
+                far_scatter_kernel<<<sms * 2, 256, 0, s->st2>>>(pairs, wend, s->P, near_end, far_end, s->d_unit,
+                                                                 s->d_Dfar, s->d_touch, s->d_fcnt + 2, L.bytes());
+                far_rows_kernel<<<grid_for(far_end - near_end), kUpdThreads, 0, s->st2>>>(
+                    s->d_S, near_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, s->d_rowlist[lin], s->d_fcnt + lin,
+                    s->d_rowlist[lout], s->d_fcnt + lout, L.bytes(), s->d_diag);
+                far_touch_kernel<<<sms * 2, 256, 0, s->st2>>>(s->d_S, s->P, b, Wb, s->P, tab, gcol, s->d_touch,
+                                                              s->d_fcnt + 2, s->d_Dfar, s->d_unit, s->d_rowlist[lout],
+                                                              s->d_fcnt + lout, L.bytes(), s->d_diag);
+                s->list_cur = lout;
             }
             if (wait_slot >= 0) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[wait_slot], 0));
             {
-                Launch L(s, KC_BLK_UPDATE_NEAR, st);
+                Launch L(s, KC_BLK_UPDATE_NEAR, st, 2);
                 const int nrows = (int)(near_end - (e0 + b));
                 uint64_t *bo = kGroup > 1 && pos < kGroup - 1 ? s->d_beta + (size_t)pos * 192 : nullptr;
                 near_d_kernel<<<sms * 4, 256, 0, st>>>(s->d_S, e0 + b, nrows, s->P, pairs, wend, s->d_nearD,

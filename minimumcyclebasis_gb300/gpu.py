@@ -218,8 +218,9 @@ class Solver:
                 "cycles_scan", "cycles_barrier", "cycles_merge", "timeout_cta_plus1", "timeout_step", "timeout_rank",
                 "timeout_gen", "timeout_count", "max_barriers_per_cta", "min_barriers_per_cta", "diverged",
                 "div_step", "div_cta", "div_epoch", "cycles_tail_resolve", "cycles_tail_barrier",
-                "cycles_tail_tables", "far_rows", "profile_0", "profile_1", "profile_2", "profile_3", "profile_4",
-                "profile_5", "far_rows_changed", "far_pair_words"]
+                "cycles_tail_tables", "far_rows_gathered", "profile_0", "profile_1", "profile_2", "profile_3",
+                "far_rows_touched",
+                "far_beta_bits", "far_rows_changed", "far_pair_words"]
         return dict(zip(keys, out.tolist()))
 
     @property
