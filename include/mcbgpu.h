@@ -201,7 +201,10 @@ int mcbgpu_solver_kernel_stats(mcbgpu_solver *s, mcbgpu_kernel_stat *out, int ma
  * arrivals), [14]/[15] most/fewest barriers of a CTA in one launch, [16]-[19] first
  * step at which two CTAs disagreed on the merged result (flag, step, CTA, block),
  * [20] / [21] / [22] SM clock cycles of CTA 0 in the block tail: resolve, the tail's
- * grid barrier, final rows + tables.  Synchronises the device. */
+ * grid barrier, final rows + tables; far update: [23] non-unit rows gathered,
+ * [29] update bits of the changed rows, [30] rows changed, [31] pair words gathered,
+ * [32] unit rows reached by the scatter; [24]-[28] and [33]-[37] per-phase clock
+ * counters of profiling builds.  At most 48 counters; synchronises the device. */
 int mcbgpu_solver_diagnostics(mcbgpu_solver *s, int64_t *out, int n, int reset);
 /* Kernel launches issued by this handle so far (for accounting). */
 int64_t mcbgpu_solver_launches(const mcbgpu_solver *s);

@@ -41,6 +41,7 @@ constexpr int kTile = 1024;           // candidates per tile
 constexpr int kScanThreads = 256;     // 4 candidates per thread
 constexpr int kPer = kTile / kScanThreads;
 constexpr unsigned kSpinLimit = 1u << 24;
+constexpr int kDiagWords = 48;  // counters of mcbgpu_solver_diagnostics (the pivot kernel's check area follows)
 // Shape parameters of the blocked search; each can be overridden at build time
 // (-DMCB_LMAX=... and so on) to sweep them.
 #ifndef MCB_LMAX
@@ -870,13 +871,12 @@ __device__ __forceinline__ int nth_bit(unsigned mask, unsigned j) {
 // ---- block tail, run inside the pivot kernel after its last step -------------
 struct TailArgs {
     uint64_t *S;
-    uint64_t *tab;
     long long *selected;
     const int32_t *weight;
     unsigned *pairs, *sorted, *word_end;
     unsigned pair_cap;
-    int P, e0, Wb, tables;  // tables = 0 for the last block (no later rows)
-    int par;                // block parity: which gcol / tables / sorted pairs to write
+    int P, e0, Wb;
+    int par;  // block parity: which gcol / sorted pairs to write
 };
 
 // Named CTA barrier 1 over the warps 1.. of the CTA (warp 0 is busy elsewhere);
@@ -1084,25 +1084,24 @@ __device__ bool resolve_block(BlockState *bs, int rank, const int64_t *__restric
     return true;
 }
 
-// S_{e0+k} := XOR of S^0_{e0+l} over l in mask[k], in place, words [0, Wb), and the
-// Four-Russians tables of the final rows: tab[g][pat][w] = XOR of S_{e0+8g+i} over
-// the bits i of pat.  Column groups of kMatCols words, group cg handled by CTA
-// cg mod G; `buf` is shared scratch of 2 x 64 x (kMatCols + 1) words.
+// S_{e0+k} := XOR of S^0_{e0+l} over l in mask[k], in place, words [0, Wb): the
+// block's final rows, which every later row update XORs in directly.  Column groups
+// of kMatCols words, group cg handled by CTA cg mod G; `buf` is shared scratch of
+// 64 x (kMatCols + 1) words.
 #ifndef MCB_MAT_COLS
 #define MCB_MAT_COLS 8
 #endif
 constexpr int kMatCols = MCB_MAT_COLS;
 
-__device__ void materialize_tables(const TailArgs &ta, const BlockState *bs, int b, uint64_t *buf) {
+__device__ void materialize_rows(const TailArgs &ta, const BlockState *bs, int b, uint64_t *buf) {
     uint64_t(*s0)[kMatCols + 1] = reinterpret_cast<uint64_t(*)[kMatCols + 1]>(buf);
-    uint64_t(*s1)[kMatCols + 1] = s0 + 64;
     __shared__ uint64_t sm[64];
     if (threadIdx.x < 64) sm[threadIdx.x] = (int)threadIdx.x < b ? bs->mask[threadIdx.x] : 0ull;
     const int Wb = ta.Wb, P = ta.P, e0 = ta.e0;
     const int ng = (Wb + kMatCols - 1) / kMatCols;
     for (int cg = blockIdx.x; cg < ng; cg += gridDim.x) {
         const int w0 = cg * kMatCols;
-        cta_sync();  // the masks are in place; the previous group's tables are read
+        cta_sync();  // the masks are in place; the previous group's rows are read
         for (int idx = threadIdx.x; idx < 64 * kMatCols; idx += blockDim.x) {
             const int l = idx / kMatCols, w = idx % kMatCols;
             s0[l][w] = (l < b && w0 + w < Wb) ? ta.S[(size_t)(e0 + l) * P + w0 + w] : 0ull;
@@ -1110,39 +1109,28 @@ __device__ void materialize_tables(const TailArgs &ta, const BlockState *bs, int
         cta_sync();
         for (int idx = threadIdx.x; idx < 64 * kMatCols; idx += blockDim.x) {
             const int k = idx / kMatCols, w = idx % kMatCols;
-            uint64_t acc = 0;
             if (k < b && w0 + w < Wb) {
+                uint64_t acc = 0;
                 for (uint64_t m = sm[k]; m; m &= m - 1) acc ^= s0[__ffsll((long long)m) - 1][w];
                 ta.S[(size_t)(e0 + k) * P + w0 + w] = acc;
-            }
-            s1[k][w] = acc;
-        }
-        if (!ta.tables) continue;
-        cta_sync();
-        // one thread per (word, table group, quarter of the patterns); Gray-code order
-        // inside the quarter: one XOR per entry
-        for (int idx = threadIdx.x; idx < kMatCols * 8 * 4; idx += blockDim.x) {
-            const int w = idx % kMatCols, g = (idx / kMatCols) >> 2, q = (idx / kMatCols) & 3;
-            if (w0 + w >= Wb) continue;
-            uint64_t v[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++) v[i] = s1[8 * g + i][w];
-            uint64_t *out = ta.tab + (size_t)g * 256 * P + w0 + w;
-            const int t0 = q * 64;
-            const int g0 = t0 ^ (t0 >> 1);
-            uint64_t cur = 0;
-#pragma unroll
-            for (int i = 0; i < 8; i++)
-                if ((g0 >> i) & 1) cur ^= v[i];
-            out[(size_t)g0 * P] = cur;
-            for (int t = t0 + 1; t < t0 + 64; t++) {
-                cur ^= v[__ffs(t) - 1];
-                out[(size_t)(t ^ (t >> 1)) * P] = cur;
             }
         }
     }
 }
 
+#ifdef MCB_MERGE_PROFILE
+__device__ long long g_merge_prof[5];
+#define MERGE_STAMP(i)                                                  \
+    do {                                                                \
+        const long long mp1 = clock64();                                \
+        if (threadIdx.x == 0 && c == 0) g_merge_prof[i] += mp1 - mp0;  \
+        mp0 = mp1;                                                      \
+    } while (0)
+#else
+#define MERGE_STAMP(i) \
+    do {               \
+    } while (0)
+#endif
 #ifdef MCB_SCAN_PROFILE
 __device__ long long g_scan_prof[4];
 #endif
@@ -1395,6 +1383,9 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
             }
         }
         // ---- part 2: merge (identical in every CTA) ----
+#ifdef MCB_MERGE_PROFILE
+        long long mp0 = clock64();
+#endif
         // all reports into shared memory with independent loads (one round trip)
         const unsigned words = G * (2 * kLmax + 2);
         for (unsigned i = threadIdx.x; i < words; i += blockDim.x) lr[i] = __ldcg(rep_rank + i);
@@ -1404,6 +1395,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
         unsigned long long dmin = kNone;
         for (unsigned i = threadIdx.x; i < G; i += blockDim.x) dmin = l_end[i] < dmin ? l_end[i] : dmin;
         const unsigned long long D = block_min_u64(dmin, s_dmin);
+        MERGE_STAMP(0);
         // the reports below D, CTA by CTA (a CTA's ranks ascend): per-CTA counts,
         // block prefix sum, copy
         unsigned cnt = 0;
@@ -1439,6 +1431,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
         }
         if (cnt > G * kLmax) cnt = G * kLmax;
         n_cand += cnt;
+        MERGE_STAMP(1);
         int nnew = 0;
         if (!MCB_MERGE_FAST || cnt > 0) {  // no report below D: no new pivot (uniform)
             // rank order: each candidate's position = number of smaller ranks (ranks are distinct)
@@ -1454,6 +1447,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
                 sz[pos] = fr_reduce(mw[i], gtab);
             }
             cta_sync();
+            MERGE_STAMP(2);
             // greedy echelon in rank order (warp 0): a candidate is a new global pivot iff
             // its residual is not in the span of the new pivots before it; then the new
             // vectors are brought to reduced form among themselves, latest first (lane l
@@ -1498,6 +1492,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
             }
             cta_sync();
             nnew = s_nnew;
+            MERGE_STAMP(3);
         }
         if (nnew > 0) {
             // clear the new pivot bits from the old basis vectors, append, rebuild tables
@@ -1514,6 +1509,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
             grank += nnew;
             cta_sync();
             fr_build(gtab, gbasis, gpiv, (unsigned)grank);
+            MERGE_STAMP(4);
         }
         if (nnew == 0 && D >= (unsigned long long)K) {
             if (c == 0 && threadIdx.x == 0) {
@@ -1549,7 +1545,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
             ok = false;
         } else {
             const long long c5 = clock64();
-            if (*((volatile unsigned *)&bs->tail_ok)) materialize_tables(ta, bs, b, win);
+            if (*((volatile unsigned *)&bs->tail_ok)) materialize_rows(ta, bs, b, win);
             cta_sync();
             cyc_tailbar = c5 - c4;
             cyc_mat = clock64() - c5;
@@ -1579,6 +1575,9 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
         atomicAdd(&diag[20], (unsigned long long)cyc_resolve);
         atomicAdd(&diag[21], (unsigned long long)cyc_tailbar);
         atomicAdd(&diag[22], (unsigned long long)cyc_mat);
+#ifdef MCB_MERGE_PROFILE
+        for (int i = 0; i < 5; i++) diag[33 + i] = (unsigned long long)g_merge_prof[i];
+#endif
 #ifdef MCB_SCAN_PROFILE
         for (int i = 0; i < 4; i++) diag[24 + i] = (unsigned long long)g_scan_prof[i];
 #endif
@@ -1611,6 +1610,19 @@ size_t pivot_smem_bytes(int G) {
 constexpr int kUpdThreads = 256;
 constexpr int kUpdSplit = MCB_UPD_SPLIT;
 constexpr int kUpdGroups = kUpdThreads / 32 / kUpdSplit;  // row groups per CTA
+
+// S_j ^= XOR of the block's final rows S_{e0+k} over the set bits k of bt, words
+// [w, Wb) with stride `step` (the caller's lanes split the words).  The final rows
+// are written once by the block tail and never change again, so any number of
+// rows can be updated from them at once.
+__device__ __forceinline__ void xor_final_rows(uint64_t *Sj, const uint64_t *S, int P, int e0, uint64_t bt, int w,
+                                               int Wb, int step) {
+    for (; w < Wb; w += step) {
+        uint64_t acc = 0;
+        for (uint64_t m = bt; m; m &= m - 1) acc ^= S[(size_t)(e0 + __ffsll((long long)m) - 1) * P + w];
+        Sj[w] ^= acc;
+    }
+}
 
 // beta of a row is a linear function of its D over GF(2): beta_k = D_k ^ <beta_{<k},
 // gcol_k> gives beta = D (I + G)^-1, G[i][k] = bit i of gcol_k.  Row i of that inverse,
@@ -1661,8 +1673,7 @@ __device__ void build_beta_tables(const uint64_t *__restrict__ gcol, int b, uint
 // block's (double-buffered by block parity, so the next block's tail can run while
 // these rows are updated).
 __global__ void __launch_bounds__(kUpdThreads) far_rows_kernel(uint64_t *S, long long row_begin, int P, int b,
-                                                               int Wb, int Pt, const uint64_t *__restrict__ tab,
-                                                               const uint64_t *__restrict__ gcol,
+                                                               int e0, int Wb, const uint64_t *__restrict__ gcol,
                                                                const unsigned *__restrict__ pairs,
                                                                const unsigned *__restrict__ word_end,
                                                                const int32_t *__restrict__ list_in,
@@ -1739,9 +1750,9 @@ __global__ void __launch_bounds__(kUpdThreads) far_rows_kernel(uint64_t *S, long
             for (int g = 0; g < 8; g++) beta ^= btab[g][(Dmine >> (8 * g)) & 255];
             // algorithmic bytes (counted by the group's first warp): the S words the
             // group's pairs touch plus, when the row changes, read + write of its
-            // first Wb words
+            // first Wb words and the read of the final rows its bits select
             if (h == 0) {
-                nb += 8ull * np + (beta ? 16ull * (unsigned long long)Wb : 0ull);
+                nb += 8ull * np + (beta ? (16ull + 8ull * (unsigned)__popcll(beta)) * (unsigned long long)Wb : 0ull);
                 n_rows++;
                 n_changed += beta ? 1 : 0;
                 n_gather += np;
@@ -1752,16 +1763,7 @@ __global__ void __launch_bounds__(kUpdThreads) far_rows_kernel(uint64_t *S, long
             const uint64_t bt = __shfl_sync(0xffffffffu, beta, r);
             if (!bt) continue;
             uint64_t *Sj = S + (size_t)__shfl_sync(0xffffffffu, jr, r) * P;
-            const uint64_t *t0 = tab + ((size_t)0 * 256 + ((bt >> 0) & 255)) * Pt;
-            const uint64_t *t1 = tab + ((size_t)1 * 256 + ((bt >> 8) & 255)) * Pt;
-            const uint64_t *t2 = tab + ((size_t)2 * 256 + ((bt >> 16) & 255)) * Pt;
-            const uint64_t *t3 = tab + ((size_t)3 * 256 + ((bt >> 24) & 255)) * Pt;
-            const uint64_t *t4 = tab + ((size_t)4 * 256 + ((bt >> 32) & 255)) * Pt;
-            const uint64_t *t5 = tab + ((size_t)5 * 256 + ((bt >> 40) & 255)) * Pt;
-            const uint64_t *t6 = tab + ((size_t)6 * 256 + ((bt >> 48) & 255)) * Pt;
-            const uint64_t *t7 = tab + ((size_t)7 * 256 + ((bt >> 56) & 255)) * Pt;
-            for (int w = h * 32 + lane; w < Wb; w += 32 * kUpdSplit)
-                Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
+            xor_final_rows(Sj, S, P, e0, bt, h * 32 + lane, Wb, 32 * kUpdSplit);
         }
     }
     for (int d = 16; d > 0; d >>= 1) {
@@ -1808,8 +1810,7 @@ __global__ void __launch_bounds__(256) far_scatter_kernel(const unsigned *__rest
 // map D -> beta is invertible), S_c ^= XOR_k beta_k S_{e0+k} over the first Wb words
 // (all zero in a unit row below its own word), then the row leaves the unit set and
 // joins the non-unit list.
-__global__ void __launch_bounds__(256) far_touch_kernel(uint64_t *S, int P, int b, int Wb, int Pt,
-                                                       const uint64_t *__restrict__ tab,
+__global__ void __launch_bounds__(256) far_touch_kernel(uint64_t *S, int P, int b, int e0, int Wb,
                                                        const uint64_t *__restrict__ gcol,
                                                        const int32_t *__restrict__ touch,
                                                        const unsigned *__restrict__ n_touch,
@@ -1837,37 +1838,27 @@ __global__ void __launch_bounds__(256) far_touch_kernel(uint64_t *S, int P, int 
 #pragma unroll
         for (int g = 0; g < 8; g++) bt ^= btab[g][(D >> (8 * g)) & 255];
         if (lane == 0) {
-            nb += 8 + (bt ? 16ull * (unsigned long long)Wb : 0ull);
+            nb += 8 + (bt ? (16ull + 8ull * (unsigned)__popcll(bt)) * (unsigned long long)Wb : 0ull);
             n_touched++;
             n_changed += bt ? 1 : 0;
             n_betabits += (unsigned)__popcll(bt);
         }
         if (!bt) continue;
-        uint64_t *Sj = S + (size_t)c * P;
-        const uint64_t *t0 = tab + ((size_t)0 * 256 + ((bt >> 0) & 255)) * Pt;
-        const uint64_t *t1 = tab + ((size_t)1 * 256 + ((bt >> 8) & 255)) * Pt;
-        const uint64_t *t2 = tab + ((size_t)2 * 256 + ((bt >> 16) & 255)) * Pt;
-        const uint64_t *t3 = tab + ((size_t)3 * 256 + ((bt >> 24) & 255)) * Pt;
-        const uint64_t *t4 = tab + ((size_t)4 * 256 + ((bt >> 32) & 255)) * Pt;
-        const uint64_t *t5 = tab + ((size_t)5 * 256 + ((bt >> 40) & 255)) * Pt;
-        const uint64_t *t6 = tab + ((size_t)6 * 256 + ((bt >> 48) & 255)) * Pt;
-        const uint64_t *t7 = tab + ((size_t)7 * 256 + ((bt >> 56) & 255)) * Pt;
-        for (int w = lane; w < Wb; w += 32) Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
+        xor_final_rows(S + (size_t)c * P, S, P, e0, bt, lane, Wb, 32);
     }
     if (lane == 0 && nb) atomicAdd(bytes, nb);
     if (lane == 0 && diag && n_touched) {  // touched unit rows, changed ones, beta bits
-        atomicAdd(&diag[28], n_touched);
+        atomicAdd(&diag[32], n_touched);
         atomicAdd(&diag[30], n_changed);
         atomicAdd(&diag[29], n_betabits);
     }
 }
 
 // The update of the next block's rows (at most 3 x 64, on the critical path: the
-// next block's transpose reads them), spread over the whole GPU in two launches
-// instead of one warp group per 8 rows.
+// next block's transpose reads them), spread over the whole GPU in two launches.
 // near_d_kernel: D_j = <C_sel_k, S_j> bits for every near row j, one (row, chunk of
-// kNearChunk pairs) item per warp, XOR-accumulated into Dbuf[j - row_begin] (which
-// near_apply_kernel clears after use).
+// kNearChunk pairs) item per warp, XOR-accumulated into Dbuf[j - row_begin] (one of
+// two buffers by block parity; the next block's near_apply_kernel clears it).
 constexpr int kNearPer = 16;               // pairs per lane of an item
 constexpr int kNearChunk = 32 * kNearPer;  // pairs per item
 constexpr int kNearMaxRows = 192;
@@ -1911,47 +1902,60 @@ __global__ void __launch_bounds__(256) near_d_kernel(const uint64_t *__restrict_
     if (lane == 0 && nb) atomicAdd(bytes, nb);
 }
 
-// near_apply_kernel: per near row (one CTA each), beta_k = D_k ^ <beta_{<k}, gcol_k>
-// (the sequential effect of the block's updates), written to beta_out for the
-// grouped pass's correction if given, then S_j ^= XOR_k beta_k S_{e0+k} through the
-// Four-Russians tables over the row's first Wb words.
+// near_apply_kernel: every CTA computes beta_k = D_k ^ <beta_{<k}, gcol_k> (the
+// sequential effect of the block's updates) of every near row (CTA 0 writes them to
+// beta_out for the grouped pass's correction and clears the other parity's D
+// buffer for the next block), then takes columns [w0, w0 + kNearCols) of the block's
+// final rows into shared memory and applies S_j ^= XOR_k beta_k S_{e0+k} there to
+// every near row: one read of the final rows in all, the near rows read and written
+// once, column-contiguous.
+constexpr int kNearCols = 32;
+
 __global__ void __launch_bounds__(256) near_apply_kernel(uint64_t *S, long long row_begin, int nrows, int P, int b,
-                                                        int Wb, int Pt, const uint64_t *__restrict__ tab,
-                                                        const uint64_t *__restrict__ gcol, unsigned long long *Dbuf,
-                                                        uint64_t *beta_out, unsigned long long *bytes) {
+                                                        int e0, int Wb, const uint64_t *__restrict__ gcol,
+                                                        const unsigned long long *__restrict__ Dbuf,
+                                                        unsigned long long *Dnext, uint64_t *beta_out,
+                                                        unsigned long long *bytes) {
     __shared__ uint64_t sg[64];
-    __shared__ uint64_t s_beta;
+    __shared__ uint64_t sbeta[kNearMaxRows];
+    __shared__ uint64_t srow[64][kNearCols];
     if (threadIdx.x < 64) sg[threadIdx.x] = (int)threadIdx.x < b ? gcol[threadIdx.x] : 0;
     cta_sync();
     unsigned long long nb = 0;
-    for (int r = blockIdx.x; r < nrows; r += gridDim.x) {
-        if (threadIdx.x == 0) {
-            const uint64_t D = Dbuf[r];
-            Dbuf[r] = 0;  // ready for the next block
-            uint64_t beta = 0;
-            for (int k = 0; k < b; k++) beta |= ((((D >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]))) << k;
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+        const uint64_t D = Dbuf[r];
+        uint64_t beta = 0;
+        for (int k = 0; k < b; k++) beta |= ((((D >> k) & 1ull) ^ (uint64_t)parity64(beta & sg[k]))) << k;
+        sbeta[r] = beta;
+        if (blockIdx.x == 0) {
             if (beta_out) beta_out[r] = beta;
-            s_beta = beta;
             nb += beta ? 16ull * (unsigned long long)Wb : 0ull;
         }
-        cta_sync();
-        const uint64_t bt = s_beta;
-        if (bt) {
-            uint64_t *Sj = S + (size_t)(row_begin + r) * P;
-            const uint64_t *t0 = tab + ((size_t)0 * 256 + ((bt >> 0) & 255)) * Pt;
-            const uint64_t *t1 = tab + ((size_t)1 * 256 + ((bt >> 8) & 255)) * Pt;
-            const uint64_t *t2 = tab + ((size_t)2 * 256 + ((bt >> 16) & 255)) * Pt;
-            const uint64_t *t3 = tab + ((size_t)3 * 256 + ((bt >> 24) & 255)) * Pt;
-            const uint64_t *t4 = tab + ((size_t)4 * 256 + ((bt >> 32) & 255)) * Pt;
-            const uint64_t *t5 = tab + ((size_t)5 * 256 + ((bt >> 40) & 255)) * Pt;
-            const uint64_t *t6 = tab + ((size_t)6 * 256 + ((bt >> 48) & 255)) * Pt;
-            const uint64_t *t7 = tab + ((size_t)7 * 256 + ((bt >> 56) & 255)) * Pt;
-            for (int w = threadIdx.x; w < Wb; w += blockDim.x)
-                Sj[w] ^= t0[w] ^ t1[w] ^ t2[w] ^ t3[w] ^ t4[w] ^ t5[w] ^ t6[w] ^ t7[w];
-        }
-        cta_sync();  // s_beta is rewritten for the next row
     }
-    if (threadIdx.x == 0 && nb) atomicAdd(bytes, nb);
+    if (blockIdx.x == 0)
+        for (int r = threadIdx.x; r < kNearMaxRows; r += blockDim.x) Dnext[r] = 0;
+    cta_sync();
+    const int w = threadIdx.x % kNearCols, rs = threadIdx.x / kNearCols, rstep = blockDim.x / kNearCols;
+    for (int w0 = blockIdx.x * kNearCols; w0 < Wb; w0 += gridDim.x * kNearCols) {
+        for (int idx = threadIdx.x; idx < 64 * kNearCols; idx += blockDim.x) {
+            const int l = idx / kNearCols, x = idx % kNearCols;
+            srow[l][x] = (l < b && w0 + x < Wb) ? S[(size_t)(e0 + l) * P + w0 + x] : 0ull;
+        }
+        if (threadIdx.x == 0) nb += 8ull * (unsigned long long)b * (unsigned long long)min(kNearCols, Wb - w0);
+        cta_sync();
+        if (w0 + w < Wb) {
+            for (int r = rs; r < nrows; r += rstep) {
+                const uint64_t bt = sbeta[r];
+                if (!bt) continue;
+                uint64_t acc = 0;
+                for (uint64_t m = bt; m; m &= m - 1) acc ^= srow[__ffsll((long long)m) - 1][w];
+                S[(size_t)(row_begin + r) * P + w0 + w] ^= acc;
+            }
+        }
+        cta_sync();  // srow is refilled for the next column chunk
+    }
+    for (int d = 16; d > 0; d >>= 1) nb += __shfl_xor_sync(0xffffffffu, nb, d);
+    if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
 }
 
 // ---- independence certificate --------------------------------------------------
@@ -2051,13 +2055,12 @@ struct mcbgpu_solver {
     uint64_t *d_S = nullptr;
     uint64_t *d_C = nullptr;       // cycle vector buffer (W words)
     uint64_t *d_T = nullptr;       // 64 * P words
-    uint64_t *d_tab = nullptr;     // 8 * 256 * P words
     uint64_t *d_Warr = nullptr;    // W per candidate (tiles * 1024)
     uint64_t *d_Warr2 = nullptr;   // W of a group's second block (the grouped pass, then its correction)
     uint64_t *d_Warr3 = nullptr;   // W of a group's third block
     uint64_t *d_Tg = nullptr;      // the group's blocks' rows transposed, kGStride words per coordinate
     uint64_t *d_beta = nullptr;    // 3 x 192: update bits of the near rows of a group's first blocks
-    unsigned long long *d_nearD = nullptr;  // kNearMaxRows: D of the near rows (zero between uses)
+    unsigned long long *d_nearD = nullptr;  // 2 x kNearMaxRows: D of the near rows by block parity (zero between uses)
     // far update: rows whose support vector is still the unit vector get D by scatter
     uint8_t *d_unit = nullptr;               // N: 1 while S_j = e_j (far rows only kept exact)
     unsigned long long *d_Dfar = nullptr;    // N: scattered D of unit far rows (zero between uses)
@@ -2148,7 +2151,6 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_S);
     cudaFree(s->d_C);
     cudaFree(s->d_T);
-    cudaFree(s->d_tab);
     cudaFree(s->d_Warr);
     cudaFree(s->d_Warr2);
     cudaFree(s->d_Warr3);
@@ -2243,7 +2245,6 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_S, sizeof(uint64_t) * (size_t)N * s->P);
     ALLOC(s->d_C, sizeof(uint64_t) * (size_t)s->P);
     ALLOC(s->d_T, sizeof(uint64_t) * 64 * (size_t)s->P);
-    ALLOC(s->d_tab, sizeof(uint64_t) * 2 * 8 * 256 * (size_t)s->P);
     ALLOC(s->d_Warr, sizeof(uint64_t) * (size_t)kTile * ntiles);
     if (kGroup > 1) {
         ALLOC(s->d_Warr2, sizeof(uint64_t) * (size_t)kTile * ntiles);
@@ -2252,7 +2253,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
         ALLOC(s->d_beta, sizeof(uint64_t) * 3 * 192);
         ALLOC(s->d_masks, sizeof(uint64_t) * 2 * 64);
     }
-    ALLOC(s->d_nearD, sizeof(unsigned long long) * kNearMaxRows);
+    ALLOC(s->d_nearD, sizeof(unsigned long long) * 2 * kNearMaxRows);
     ALLOC(s->d_unit, (size_t)N);
     ALLOC(s->d_Dfar, sizeof(unsigned long long) * (size_t)N);
     ALLOC(s->d_rowlist[0], sizeof(int32_t) * (size_t)N);
@@ -2269,13 +2270,13 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_status, sizeof(unsigned));
     ALLOC(s->d_bytes, sizeof(unsigned long long) * KC_COUNT);
     ALLOC(s->d_check, sizeof(unsigned) * 2);
-    ALLOC(s->d_diag, sizeof(unsigned long long) * (32 + 8 * 1024));
+    ALLOC(s->d_diag, sizeof(unsigned long long) * (kDiagWords + 8 * 1024));
 #undef ALLOC
-    if (e == cudaSuccess) e = cudaMemset(s->d_diag, 0, sizeof(unsigned long long) * 32);
+    if (e == cudaSuccess) e = cudaMemset(s->d_diag, 0, sizeof(unsigned long long) * kDiagWords);
     if (e == cudaSuccess) e = cudaMemset(s->d_bytes, 0, sizeof(unsigned long long) * KC_COUNT);
     if (e == cudaSuccess) e = cudaMemset(s->d_tile_epoch, 0, sizeof(unsigned) * ntiles);
     if (e == cudaSuccess) e = cudaMemset(s->d_gbar, 0, sizeof(GridBar));
-    if (e == cudaSuccess) e = cudaMemset(s->d_nearD, 0, sizeof(unsigned long long) * kNearMaxRows);
+    if (e == cudaSuccess) e = cudaMemset(s->d_nearD, 0, sizeof(unsigned long long) * 2 * kNearMaxRows);
     if (e == cudaSuccess) e = cudaMemset(s->d_Dfar, 0, sizeof(unsigned long long) * ((size_t)N > 0 ? (size_t)N : 2));
     if (e == cudaSuccess) e = cudaMemset(s->d_unit, 1, (size_t)N > 0 ? (size_t)N : 16);
     if (e == cudaSuccess) e = cudaMemset(s->d_fcnt, 0, sizeof(unsigned) * 4);
@@ -2339,7 +2340,7 @@ int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream) {
         Launch L(s, KC_RESET, st);
         reset_state_kernel<<<1, 32, 0, st>>>(s->d_slots, s->d_bs, s->d_status);
     }
-    MCB_CUDA(cudaMemsetAsync(s->d_nearD, 0, sizeof(unsigned long long) * kNearMaxRows, st));
+    MCB_CUDA(cudaMemsetAsync(s->d_nearD, 0, sizeof(unsigned long long) * 2 * kNearMaxRows, st));
     if (s->N > 0) {  // every row is a unit vector again; no non-unit rows, no scattered D left over
         MCB_CUDA(cudaMemsetAsync(s->d_unit, 1, (size_t)s->N, st));
         MCB_CUDA(cudaMemsetAsync(s->d_Dfar, 0, sizeof(unsigned long long) * (size_t)s->N, st));
@@ -2608,10 +2609,9 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             unsigned long long *rp = s->d_reports;
             unsigned long long *nb = L.bytes();
             unsigned long long *dg = s->d_diag;
-            unsigned long long *db = s->d_diag + 32;
+            unsigned long long *db = s->d_diag + kDiagWords;
             TailArgs ta;
             ta.S = s->d_S;
-            ta.tab = s->d_tab + (size_t)par * 8 * 256 * s->P;
             ta.selected = s->d_selected;
             ta.weight = s->d_weight;
             ta.pairs = s->d_pairs;
@@ -2621,7 +2621,6 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             ta.P = s->P;
             ta.e0 = (int)e0;
             ta.Wb = Wb;
-            ta.tables = e0 + b < s->N ? 1 : 0;
             ta.par = par;
             void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db, &ta};
             MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kPivotThreads),
@@ -2630,7 +2629,6 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         if (e0 + b < s->N) {
             const int near_rows = kGroup == 1 ? 64 : pos == kGroup - 1 ? 64 * kGroup : 64 * (kGroup - 1 - pos);
             const long long near_end = std::min<long long>(e0 + b + near_rows, s->N), far_end = s->N;
-            const uint64_t *tab = s->d_tab + (size_t)par * 8 * 256 * s->P;
             const uint64_t *gcol = reinterpret_cast<const uint64_t *>(&s->d_bs->gcol[par][0]);
             const unsigned *pairs = s->d_pairs + (size_t)(1 + par) * s->pair_cap;
             const unsigned *wend = s->d_word_end + (size_t)par * (s->P + 1);
@@ -2654,9 +2652,9 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 far_scatter_kernel<<<sms * 2, 256, 0, s->st2>>>(pairs, wend, s->P, near_end, far_end, s->d_unit,
                                                                  s->d_Dfar, s->d_touch, s->d_fcnt + 2, L.bytes());
                 far_rows_kernel<<<grid_for(far_end - near_end), kUpdThreads, 0, s->st2>>>(
-                    s->d_S, near_end, s->P, b, Wb, s->P, tab, gcol, pairs, wend, s->d_rowlist[lin], s->d_fcnt + lin,
+                    s->d_S, near_end, s->P, b, (int)e0, Wb, gcol, pairs, wend, s->d_rowlist[lin], s->d_fcnt + lin,
                     s->d_rowlist[lout], s->d_fcnt + lout, L.bytes(), s->d_diag);
-                far_touch_kernel<<<sms * 2, 256, 0, s->st2>>>(s->d_S, s->P, b, Wb, s->P, tab, gcol, s->d_touch,
+                far_touch_kernel<<<sms * 2, 256, 0, s->st2>>>(s->d_S, s->P, b, (int)e0, Wb, gcol, s->d_touch,
                                                               s->d_fcnt + 2, s->d_Dfar, s->d_unit, s->d_rowlist[lout],
                                                               s->d_fcnt + lout, L.bytes(), s->d_diag);
                 s->list_cur = lout;
@@ -2666,10 +2664,12 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 Launch L(s, KC_BLK_UPDATE_NEAR, st, 2);
                 const int nrows = (int)(near_end - (e0 + b));
                 uint64_t *bo = kGroup > 1 && pos < kGroup - 1 ? s->d_beta + (size_t)pos * 192 : nullptr;
-                near_d_kernel<<<sms * 4, 256, 0, st>>>(s->d_S, e0 + b, nrows, s->P, pairs, wend, s->d_nearD,
-                                                        L.bytes());
-                near_apply_kernel<<<nrows, 256, 0, st>>>(s->d_S, e0 + b, nrows, s->P, b, Wb, s->P, tab, gcol,
-                                                         s->d_nearD, bo, L.bytes());
+                unsigned long long *Dn = s->d_nearD + (size_t)par * kNearMaxRows;
+                unsigned long long *Dn_next = s->d_nearD + (size_t)(par ^ 1) * kNearMaxRows;
+                const int agrid = (int)std::min<long long>((Wb + kNearCols - 1) / kNearCols, (long long)sms * 2);
+                near_d_kernel<<<sms * 4, 256, 0, st>>>(s->d_S, e0 + b, nrows, s->P, pairs, wend, Dn, L.bytes());
+                near_apply_kernel<<<agrid, 256, 0, st>>>(s->d_S, e0 + b, nrows, s->P, b, (int)e0, Wb, gcol, Dn,
+                                                         Dn_next, bo, L.bytes());
             }
             if (near_end < far_end) {
                 const int slot = ring;
@@ -2818,11 +2818,11 @@ int mcbgpu_solver_kernel_stats(mcbgpu_solver *s, mcbgpu_kernel_stat *out, int ma
 }
 
 int mcbgpu_solver_diagnostics(mcbgpu_solver *s, int64_t *out, int n, int reset) {
-    if (!s || (!out && n > 0) || n > 32) {
+    if (!s || (!out && n > 0) || n > kDiagWords) {
         set_error("mcbgpu_solver_diagnostics: invalid argument");
         return MCBGPU_E_ARG;
     }
-    unsigned long long v[32];
+    unsigned long long v[kDiagWords];
     MCB_CUDA(cudaDeviceSynchronize());
     MCB_CUDA(cudaMemcpy(v, s->d_diag, sizeof v, cudaMemcpyDeviceToHost));
     for (int i = 0; i < n; i++) out[i] = (int64_t)v[i];

@@ -212,15 +212,15 @@ class Solver:
 
     def diagnostics(self, reset: bool = True) -> dict:
         """Counters of the blocked search since the last reset."""
-        out = np.zeros(32, np.int64)
-        check_gpu(self.lib.mcbgpu_solver_diagnostics(self._h, ptr(out), 32, int(reset)), "mcbgpu_solver_diagnostics")
+        out = np.zeros(48, np.int64)
+        check_gpu(self.lib.mcbgpu_solver_diagnostics(self._h, ptr(out), 48, int(reset)), "mcbgpu_solver_diagnostics")
         keys = ["pivot_steps", "local_pivots", "merge_candidates", "tiles_loaded", "tiles_computed", "blocks",
                 "cycles_scan", "cycles_barrier", "cycles_merge", "timeout_cta_plus1", "timeout_step", "timeout_rank",
                 "timeout_gen", "timeout_count", "max_barriers_per_cta", "min_barriers_per_cta", "diverged",
                 "div_step", "div_cta", "div_epoch", "cycles_tail_resolve", "cycles_tail_barrier",
                 "cycles_tail_tables", "far_rows_gathered", "profile_0", "profile_1", "profile_2", "profile_3",
-                "far_rows_touched",
-                "far_beta_bits", "far_rows_changed", "far_pair_words"]
+                "profile_4", "far_beta_bits", "far_rows_changed", "far_pair_words", "far_rows_touched",
+                "merge_profile_0", "merge_profile_1", "merge_profile_2", "merge_profile_3", "merge_profile_4"]
         return dict(zip(keys, out.tolist()))
 
     @property
