@@ -1436,28 +1436,27 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
         if (!MCB_MERGE_FAST || cnt > 0) {  // no report below D: no new pivot (uniform)
             // rank order: each candidate's position = number of smaller ranks (ranks are distinct)
             unsigned long long *sr = mr + cnt;  // sorted ranks
-            uint64_t *sz = mw + cnt;            // sorted residuals against the global basis
-            uint64_t *sw = sz + cnt;            // sorted W
+            uint64_t *sw = mw + cnt;            // sorted W
             for (unsigned i = threadIdx.x; i < cnt; i += blockDim.x) {
                 const unsigned long long r = mr[i];
                 unsigned pos = 0;
                 for (unsigned j = 0; j < cnt; j++) pos += mr[j] < r;
                 sr[pos] = r;
                 sw[pos] = mw[i];
-                sz[pos] = fr_reduce(mw[i], gtab);
             }
             cta_sync();
             MERGE_STAMP(2);
-            // greedy echelon in rank order (warp 0): a candidate is a new global pivot iff
-            // its residual is not in the span of the new pivots before it; then the new
-            // vectors are brought to reduced form among themselves, latest first (lane l
-            // holds vectors l and l + 32)
-            if (threadIdx.x < 32) {
-                int nn = 0;
-                for (unsigned base = 0; base < cnt && grank + nn < b; base += 32) {
-                    uint64_t z = base + lane < cnt ? sz[base + lane] : 0ull;
-                    for (int j = 0; j < nn; j++)
-                        if ((z >> s_newq[j]) & 1ull) z ^= s_newv[j];
+            // greedy echelon in rank order, 32 candidates at a time.  Warp 0 reduces the
+            // chunk against the basis (its Four-Russians tables hold every pivot
+            // accepted so far, this step's included), accepts in order the candidates
+            // whose residual is not in the span of the basis and of the chunk's accepted
+            // ones before them, and brings those to reduced form among themselves
+            // (latest first); then the whole CTA clears their pivot bits from the basis,
+            // appends them and rebuilds the tables for the next chunk.
+            for (unsigned base = 0; base < cnt && grank < b; base += 32) {
+                if (threadIdx.x < 32) {
+                    int nn = 0;
+                    uint64_t z = base + lane < cnt ? fr_reduce(sw[base + lane], gtab) : 0ull;
                     for (;;) {
                         const unsigned bal = __ballot_sync(0xffffffffu, z != 0);
                         if (!bal || grank + nn >= b) break;
@@ -1476,40 +1475,38 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
                         if ((z >> qb) & 1ull) z ^= v;
                     }
                     __syncwarp();
+                    uint64_t va = lane < (unsigned)nn ? s_newv[lane] : 0ull;  // nn <= 32
+                    for (int j = nn - 1; j >= 1; j--) {
+                        const uint64_t vj = __shfl_sync(0xffffffffu, va, j);
+                        const unsigned qj = s_newq[j];
+                        if ((int)lane < j && ((va >> qj) & 1ull)) va ^= vj;
+                    }
+                    __syncwarp();
+                    if (lane < (unsigned)nn) s_newv[lane] = va;
+                    if (lane == 0) s_nnew = nn;
                 }
-                uint64_t va = lane < (unsigned)nn ? s_newv[lane] : 0ull;
-                uint64_t vb = lane + 32 < (unsigned)nn ? s_newv[lane + 32] : 0ull;
-                for (int j = nn - 1; j >= 1; j--) {
-                    const uint64_t vj = __shfl_sync(0xffffffffu, j < 32 ? va : vb, j & 31);
-                    const unsigned qj = s_newq[j];
-                    if ((int)lane < j && ((va >> qj) & 1ull)) va ^= vj;
-                    if ((int)lane + 32 < j && ((vb >> qj) & 1ull)) vb ^= vj;
+                cta_sync();
+                const int nc = s_nnew;
+                if (nc > 0) {
+                    if (threadIdx.x < (unsigned)grank) {
+                        uint64_t v = gbasis[threadIdx.x];
+                        for (int j = 0; j < nc; j++)
+                            if ((v >> s_newq[j]) & 1ull) v ^= s_newv[j];
+                        gbasis[threadIdx.x] = v;
+                    }
+                    if (threadIdx.x < (unsigned)nc && grank + threadIdx.x < 64) {
+                        gbasis[grank + threadIdx.x] = s_newv[threadIdx.x];
+                        gpiv[grank + threadIdx.x] = s_newq[threadIdx.x];
+                    }
+                    grank += nc;
+                    nnew += nc;
+                    cta_sync();
+                    fr_build(gtab, gbasis, gpiv, (unsigned)grank);  // ends with a barrier: s_new* are free
+                } else {
+                    cta_sync();  // s_nnew is read by every thread before warp 0 writes it again
                 }
-                __syncwarp();
-                if (lane < (unsigned)nn) s_newv[lane] = va;
-                if (lane + 32 < (unsigned)nn) s_newv[lane + 32] = vb;
-                if (lane == 0) s_nnew = nn;
             }
-            cta_sync();
-            nnew = s_nnew;
             MERGE_STAMP(3);
-        }
-        if (nnew > 0) {
-            // clear the new pivot bits from the old basis vectors, append, rebuild tables
-            if (threadIdx.x < (unsigned)grank) {
-                uint64_t v = gbasis[threadIdx.x];
-                for (int j = 0; j < nnew; j++)
-                    if ((v >> s_newq[j]) & 1ull) v ^= s_newv[j];
-                gbasis[threadIdx.x] = v;
-            }
-            if (threadIdx.x < (unsigned)nnew && grank + threadIdx.x < 64) {
-                gbasis[grank + threadIdx.x] = s_newv[threadIdx.x];
-                gpiv[grank + threadIdx.x] = s_newq[threadIdx.x];
-            }
-            grank += nnew;
-            cta_sync();
-            fr_build(gtab, gbasis, gpiv, (unsigned)grank);
-            MERGE_STAMP(4);
         }
         if (nnew == 0 && D >= (unsigned long long)K) {
             if (c == 0 && threadIdx.x == 0) {
@@ -1614,13 +1611,23 @@ constexpr int kUpdGroups = kUpdThreads / 32 / kUpdSplit;  // row groups per CTA
 // S_j ^= XOR of the block's final rows S_{e0+k} over the set bits k of bt, words
 // [w, Wb) with stride `step` (the caller's lanes split the words).  The final rows
 // are written once by the block tail and never change again, so any number of
-// rows can be updated from them at once.
-__device__ __forceinline__ void xor_final_rows(uint64_t *Sj, const uint64_t *S, int P, int e0, uint64_t bt, int w,
+// rows can be updated from them at once.  The bits go in batches of eight rows
+// whose loads are independent (one memory round trip per word and batch).
+__device__ __forceinline__ void xor_final_rows(uint64_t *Sj, const uint64_t *S, int P, int e0, uint64_t bt, int w0,
                                                int Wb, int step) {
-    for (; w < Wb; w += step) {
-        uint64_t acc = 0;
-        for (uint64_t m = bt; m; m &= m - 1) acc ^= S[(size_t)(e0 + __ffsll((long long)m) - 1) * P + w];
-        Sj[w] ^= acc;
+    while (bt) {
+        const uint64_t *r[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            r[q] = bt ? S + (size_t)(e0 + __ffsll((long long)bt) - 1) * P : nullptr;
+            bt &= bt - 1;
+        }
+        for (int w = w0; w < Wb; w += step) {
+            uint64_t x[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) x[q] = r[q] ? r[q][w] : 0ull;
+            Sj[w] ^= ((x[0] ^ x[1]) ^ (x[2] ^ x[3])) ^ ((x[4] ^ x[5]) ^ (x[6] ^ x[7]));
+        }
     }
 }
 
@@ -1918,7 +1925,7 @@ __global__ void __launch_bounds__(256) near_apply_kernel(uint64_t *S, long long 
                                                         unsigned long long *bytes) {
     __shared__ uint64_t sg[64];
     __shared__ uint64_t sbeta[kNearMaxRows];
-    __shared__ uint64_t srow[64][kNearCols];
+    __shared__ uint64_t srow[65][kNearCols];  // row 64: zeros, the padding of a short batch of bits
     if (threadIdx.x < 64) sg[threadIdx.x] = (int)threadIdx.x < b ? gcol[threadIdx.x] : 0;
     cta_sync();
     unsigned long long nb = 0;
@@ -1937,7 +1944,7 @@ __global__ void __launch_bounds__(256) near_apply_kernel(uint64_t *S, long long 
     cta_sync();
     const int w = threadIdx.x % kNearCols, rs = threadIdx.x / kNearCols, rstep = blockDim.x / kNearCols;
     for (int w0 = blockIdx.x * kNearCols; w0 < Wb; w0 += gridDim.x * kNearCols) {
-        for (int idx = threadIdx.x; idx < 64 * kNearCols; idx += blockDim.x) {
+        for (int idx = threadIdx.x; idx < 65 * kNearCols; idx += blockDim.x) {
             const int l = idx / kNearCols, x = idx % kNearCols;
             srow[l][x] = (l < b && w0 + x < Wb) ? S[(size_t)(e0 + l) * P + w0 + x] : 0ull;
         }
@@ -1945,11 +1952,26 @@ __global__ void __launch_bounds__(256) near_apply_kernel(uint64_t *S, long long 
         cta_sync();
         if (w0 + w < Wb) {
             for (int r = rs; r < nrows; r += rstep) {
-                const uint64_t bt = sbeta[r];
+                uint64_t bt = sbeta[r];
                 if (!bt) continue;
-                uint64_t acc = 0;
-                for (uint64_t m = bt; m; m &= m - 1) acc ^= srow[__ffsll((long long)m) - 1][w];
-                S[(size_t)(row_begin + r) * P + w0 + w] ^= acc;
+                // four independent accumulators: the shared-memory reads of a row's
+                // bits overlap instead of waiting one after the other
+                uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+                while (bt) {
+                    const int k0 = __ffsll((long long)bt) - 1;
+                    bt &= bt - 1;
+                    const int k1 = bt ? __ffsll((long long)bt) - 1 : 64;
+                    bt &= bt - 1;
+                    const int k2 = bt ? __ffsll((long long)bt) - 1 : 64;
+                    bt &= bt - 1;
+                    const int k3 = bt ? __ffsll((long long)bt) - 1 : 64;
+                    bt &= bt - 1;
+                    a0 ^= srow[k0][w];
+                    a1 ^= srow[k1][w];
+                    a2 ^= srow[k2][w];
+                    a3 ^= srow[k3][w];
+                }
+                S[(size_t)(row_begin + r) * P + w0 + w] ^= (a0 ^ a1) ^ (a2 ^ a3);
             }
         }
         cta_sync();  // srow is refilled for the next column chunk
