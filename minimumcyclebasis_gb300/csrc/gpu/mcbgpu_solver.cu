@@ -38,6 +38,7 @@ using namespace mcbgpu;
 namespace {
 
 constexpr int kTile = 1024;           // candidates per tile
+constexpr int kHead = 8;              // coordinates of a list's head (one aligned 32-byte slot per candidate)
 constexpr int kScanThreads = 256;     // 4 candidates per thread
 constexpr int kPer = kTile / kScanThreads;
 constexpr unsigned kSpinLimit = 1u << 24;
@@ -89,6 +90,9 @@ constexpr int kGStride = kGroup == 3 ? 4 : kGroup;  // words per coordinate in t
 #endif
 #ifndef MCB_TAIL_RANK
 #define MCB_TAIL_RANK 60
+#endif
+#ifndef MCB_MERGE_CHUNKED
+#define MCB_MERGE_CHUNKED 0  // merge echelon by chunks of 32 with a table rebuild per chunk (1) or serially (0)
 #endif
 #ifndef MCB_MERGE_FAST
 #define MCB_MERGE_FAST 1  // merge: skip the sort and echelon when no report lies below D
@@ -183,6 +187,22 @@ __global__ void validate_kernel(const int64_t *__restrict__ off, const int32_t *
 
 // Smallest first coordinate per tile of 1024 candidates (lists are ascending, so a
 // tile whose value is >= the block's bound has W = 0 for every candidate).
+// head[r] = the first kHead coordinates of candidate r's list, INT_MAX past its end:
+// one aligned 32-byte slot per candidate, read by the W walks before (and mostly
+// instead of) the list itself.
+__global__ void head_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ coords, long long K,
+                            int32_t *head) {
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < K; r += (long long)gridDim.x * blockDim.x) {
+        const int64_t a = off[r], e = off[r + 1];
+        int v[kHead];
+#pragma unroll
+        for (int q = 0; q < kHead; q++) v[q] = a + q < e ? coords[a + q] : 0x7fffffff;
+        int4 *h = reinterpret_cast<int4 *>(head + (size_t)r * kHead);
+        h[0] = make_int4(v[0], v[1], v[2], v[3]);
+        h[1] = make_int4(v[4], v[5], v[6], v[7]);
+    }
+}
+
 __global__ void tile_minc_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ coords, long long K,
                                  int32_t *tile_minc, long long ntiles) {
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -493,59 +513,100 @@ __device__ bool grid_barrier(GridBar *gb, unsigned nctas, unsigned &gen_local) {
 // ends the walk, and its coordinates >= bound gather nothing.  `nread` counts the
 // coordinates read.
 constexpr int kWChunk = MCB_W_CHUNK;
+static_assert(kWChunk == kHead, "the first chunk of a W walk is the list's head");
 
+// The first kHead coordinates of candidate r (INT_MAX past the end of its list), from
+// the head array: consecutive candidates' heads are consecutive 32-byte slots, so a
+// warp's first chunks are one coalesced read, and no offset is needed unless the
+// list goes on below the bound.
+__device__ __forceinline__ void load_head(const int32_t *__restrict__ head, long long r, int (&cv)[kHead]) {
+    const int4 *h = reinterpret_cast<const int4 *>(head + (size_t)r * kHead);
+    const int4 a = __ldg(h), b = __ldg(h + 1);
+    cv[0] = a.x;
+    cv[1] = a.y;
+    cv[2] = a.z;
+    cv[3] = a.w;
+    cv[4] = b.x;
+    cv[5] = b.y;
+    cv[6] = b.z;
+    cv[7] = b.w;
+}
+
+__device__ __forceinline__ uint64_t w_chunk(const int (&cv)[kWChunk], const uint64_t *__restrict__ T, int bound) {
+    uint64_t tv[kWChunk];
+#pragma unroll
+    for (int q = 0; q < kWChunk; q++) tv[q] = cv[q] < bound ? __ldg(T + cv[q]) : 0ull;
+    uint64_t W = 0;
+#pragma unroll
+    for (int q = 0; q < kWChunk; q++) W ^= tv[q];
+    return W;
+}
+
+// W_r = XOR of T[c] over the coordinates c < bound of candidate r's list.  The head
+// gives the first kHead coordinates; a list whose head ends below the bound goes on
+// from its offset, kWChunk coordinates at a time (independent loads), then their T
+// words (independent loads).  The list is ascending: a chunk whose last coordinate
+// is >= bound ends the walk, and its coordinates >= bound gather nothing.  `nread`
+// counts the 4-byte words read (head, offsets, further coordinates).
 __device__ __forceinline__ uint64_t w_of_candidate(long long r, const int64_t *__restrict__ off,
                                                    const int32_t *__restrict__ coords,
+                                                   const int32_t *__restrict__ head,
                                                    const uint64_t *__restrict__ T, int bound, unsigned &nread) {
-    int64_t i = __ldg(off + r);
-    const int64_t e = __ldg(off + r + 1);
-    uint64_t W = 0;
-    while (i < e) {
-        int cv[kWChunk];
+    int cv[kWChunk];
+    load_head(head, r, cv);
+    uint64_t W = w_chunk(cv, T, bound);
+    nread += kHead;
+    if (cv[kHead - 1] < bound) {
+        int64_t i = __ldg(off + r) + kHead;
+        const int64_t e = __ldg(off + r + 1);
+        nread += 2;
+        while (i < e) {
 #pragma unroll
-        for (int q = 0; q < kWChunk; q++) cv[q] = i + q < e ? __ldg(coords + i + q) : 0x7fffffff;
-        uint64_t tv[kWChunk];
-#pragma unroll
-        for (int q = 0; q < kWChunk; q++) tv[q] = cv[q] < bound ? __ldg(T + cv[q]) : 0ull;
-#pragma unroll
-        for (int q = 0; q < kWChunk; q++) W ^= tv[q];
-        nread += (unsigned)(e - i < kWChunk ? e - i : kWChunk);
-        if (cv[kWChunk - 1] >= bound) break;
-        i += kWChunk;
+            for (int q = 0; q < kWChunk; q++) cv[q] = i + q < e ? __ldg(coords + i + q) : 0x7fffffff;
+            W ^= w_chunk(cv, T, bound);
+            nread += (unsigned)(e - i < kWChunk ? e - i : kWChunk);
+            if (cv[kWChunk - 1] >= bound) break;
+            i += kWChunk;
+        }
     }
     return W;
 }
 
 // W of two candidates walked in lockstep (their loads overlap); rb < 0: only ra.
 __device__ __forceinline__ void w_of_two(long long ra, long long rb, const int64_t *__restrict__ off,
-                                         const int32_t *__restrict__ coords, const uint64_t *__restrict__ T,
-                                         int bound, unsigned &nread, uint64_t &Wa, uint64_t &Wb) {
-    int64_t ia = __ldg(off + ra), ea = __ldg(off + ra + 1);
-    int64_t ib = 0, eb = 0;
+                                         const int32_t *__restrict__ coords, const int32_t *__restrict__ head,
+                                         const uint64_t *__restrict__ T, int bound, unsigned &nread, uint64_t &Wa,
+                                         uint64_t &Wb) {
+    int ca[kWChunk], cb[kWChunk];
+    load_head(head, ra, ca);
     if (rb >= 0) {
-        ib = __ldg(off + rb);
-        eb = __ldg(off + rb + 1);
+        load_head(head, rb, cb);
+    } else {
+#pragma unroll
+        for (int q = 0; q < kWChunk; q++) cb[q] = 0x7fffffff;
     }
-    Wa = 0;
-    Wb = 0;
+    Wa = w_chunk(ca, T, bound);
+    Wb = w_chunk(cb, T, bound);
+    nread += rb >= 0 ? 2 * kHead : kHead;
+    int64_t ia = 0, ea = 0, ib = 0, eb = 0;
+    if (ca[kHead - 1] < bound) {
+        ia = __ldg(off + ra) + kHead;
+        ea = __ldg(off + ra + 1);
+        nread += 2;
+    }
+    if (rb >= 0 && cb[kHead - 1] < bound) {
+        ib = __ldg(off + rb) + kHead;
+        eb = __ldg(off + rb + 1);
+        nread += 2;
+    }
     while (ia < ea || ib < eb) {
-        int ca[kWChunk], cb[kWChunk];
 #pragma unroll
         for (int q = 0; q < kWChunk; q++) {
             ca[q] = ia + q < ea ? __ldg(coords + ia + q) : 0x7fffffff;
             cb[q] = ib + q < eb ? __ldg(coords + ib + q) : 0x7fffffff;
         }
-        uint64_t ta[kWChunk], tb[kWChunk];
-#pragma unroll
-        for (int q = 0; q < kWChunk; q++) {
-            ta[q] = ca[q] < bound ? __ldg(T + ca[q]) : 0ull;
-            tb[q] = cb[q] < bound ? __ldg(T + cb[q]) : 0ull;
-        }
-#pragma unroll
-        for (int q = 0; q < kWChunk; q++) {
-            Wa ^= ta[q];
-            Wb ^= tb[q];
-        }
+        Wa ^= w_chunk(ca, T, bound);
+        Wb ^= w_chunk(cb, T, bound);
         if (ia < ea) nread += (unsigned)(ea - ia < kWChunk ? ea - ia : kWChunk);
         if (ib < eb) nread += (unsigned)(eb - ib < kWChunk ? eb - ib : kWChunk);
         ia = ca[kWChunk - 1] >= bound ? ea : ia + kWChunk;
@@ -555,43 +616,56 @@ __device__ __forceinline__ void w_of_two(long long ra, long long rb, const int64
 
 // W of one candidate for the kG blocks of a group at once: W[0] against this block's
 // rows (coordinates below bd[0]), W[j] against the group's j-th later block's rows as
-// they are now (below bd[j], ascending), one walk of the list; Tg holds kGStride
-// words per coordinate (one 16- or 32-byte gather).
+// they are now (below bd[j], ascending), one walk of the list (head first); Tg holds
+// kGStride words per coordinate (one 16- or 32-byte gather).
+template <int kG>
+__device__ __forceinline__ void w_group_chunk(const int (&cv)[kWChunk], const uint64_t *__restrict__ Tg,
+                                              const int (&bd)[3], uint64_t (&W)[kG]) {
+    const int last = bd[kG - 1];
+    uint64_t tv[kWChunk][kG];
+#pragma unroll
+    for (int q = 0; q < kWChunk; q++) {
+        const bool in = cv[q] < last;
+        const ulonglong2 t01 = in ? __ldg(reinterpret_cast<const ulonglong2 *>(Tg + (size_t)kGStride * cv[q]))
+                                  : make_ulonglong2(0ull, 0ull);
+        tv[q][0] = cv[q] < bd[0] ? t01.x : 0ull;
+        tv[q][1] = cv[q] < bd[1] ? t01.y : 0ull;
+        if (kG == 3) {
+            const ulonglong2 t23 = in ? __ldg(reinterpret_cast<const ulonglong2 *>(Tg + (size_t)kGStride * cv[q] + 2))
+                                      : make_ulonglong2(0ull, 0ull);
+            tv[q][kG - 1] = t23.x;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kWChunk; q++)
+#pragma unroll
+        for (int g = 0; g < kG; g++) W[g] ^= tv[q][g];
+}
+
 template <int kG>
 __device__ __forceinline__ void w_of_group(long long r, const int64_t *__restrict__ off,
-                                           const int32_t *__restrict__ coords, const uint64_t *__restrict__ Tg,
-                                           const int (&bd)[3], unsigned &nread, uint64_t (&W)[kG]) {
-    int64_t i = __ldg(off + r);
-    const int64_t e = __ldg(off + r + 1);
+                                           const int32_t *__restrict__ coords, const int32_t *__restrict__ head,
+                                           const uint64_t *__restrict__ Tg, const int (&bd)[3], unsigned &nread,
+                                           uint64_t (&W)[kG]) {
     const int last = bd[kG - 1];
 #pragma unroll
     for (int g = 0; g < kG; g++) W[g] = 0;
-    while (i < e) {
-        int cv[kWChunk];
+    int cv[kWChunk];
+    load_head(head, r, cv);
+    w_group_chunk<kG>(cv, Tg, bd, W);
+    nread += kHead;
+    if (cv[kHead - 1] < last) {
+        int64_t i = __ldg(off + r) + kHead;
+        const int64_t e = __ldg(off + r + 1);
+        nread += 2;
+        while (i < e) {
 #pragma unroll
-        for (int q = 0; q < kWChunk; q++) cv[q] = i + q < e ? __ldg(coords + i + q) : 0x7fffffff;
-        uint64_t tv[kWChunk][kG];
-#pragma unroll
-        for (int q = 0; q < kWChunk; q++) {
-            const bool in = cv[q] < last;
-            const ulonglong2 t01 = in ? __ldg(reinterpret_cast<const ulonglong2 *>(Tg + (size_t)kGStride * cv[q]))
-                                      : make_ulonglong2(0ull, 0ull);
-            tv[q][0] = cv[q] < bd[0] ? t01.x : 0ull;
-            tv[q][1] = cv[q] < bd[1] ? t01.y : 0ull;
-            if (kG == 3) {
-                const ulonglong2 t23 =
-                    in ? __ldg(reinterpret_cast<const ulonglong2 *>(Tg + (size_t)kGStride * cv[q] + 2))
-                       : make_ulonglong2(0ull, 0ull);
-                tv[q][kG - 1] = t23.x;
-            }
+            for (int q = 0; q < kWChunk; q++) cv[q] = i + q < e ? __ldg(coords + i + q) : 0x7fffffff;
+            w_group_chunk<kG>(cv, Tg, bd, W);
+            nread += (unsigned)(e - i < kWChunk ? e - i : kWChunk);
+            if (cv[kWChunk - 1] >= last) break;
+            i += kWChunk;
         }
-#pragma unroll
-        for (int q = 0; q < kWChunk; q++)
-#pragma unroll
-            for (int g = 0; g < kG; g++) W[g] ^= tv[q][g];
-        nread += (unsigned)(e - i < kWChunk ? e - i : kWChunk);
-        if (cv[kWChunk - 1] >= last) break;
-        i += kWChunk;
     }
 }
 
@@ -606,6 +680,7 @@ __device__ __forceinline__ void w_of_group(long long r, const int64_t *__restric
 template <int kG>
 __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, const int64_t *__restrict__ off,
                                                     const int32_t *__restrict__ coords,
+                                                    const int32_t *__restrict__ head,
                                                     const int32_t *__restrict__ tile_minc,
                                                     const uint64_t *__restrict__ T, int bound, const BlockState *bs,
                                                     uint64_t *Warr, unsigned *tile_epoch, unsigned long long *bytes,
@@ -619,13 +694,9 @@ __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, c
         const int last = bd[kG - 1];
         for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
 #if MCB_W_PREFETCH
-            if (threadIdx.x == 0 && t + gridDim.x < ntiles) {  // this CTA's next tile into L2
+            if (threadIdx.x == 0 && t + gridDim.x < ntiles) {  // this CTA's next tile's heads into L2
                 const long long r0 = (t + gridDim.x) * kTile, r1 = min(r0 + kTile, K);
-                if (r0 < r1) {
-                    prefetch_l2(off + r0, 8ull * (unsigned long long)(r1 - r0 + 1));
-                    const long long c0 = off[r0], c1 = off[r1];
-                    prefetch_l2(coords + c0, 4ull * (unsigned long long)(c1 - c0));
-                }
+                if (r0 < r1) prefetch_l2(head + (size_t)r0 * kHead, 4ull * kHead * (unsigned long long)(r1 - r0));
             }
 #endif
             if (tile_minc[t] >= last) {  // every W of the tile is 0
@@ -638,8 +709,8 @@ __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, c
             for (int g = 0; g < kG; g++) W[g] = 0;
             unsigned nread = 0;
             if (r < K) {
-                w_of_group<kG>(r, off, coords, Tg, bd, nread, W);
-                nb += 8 + 8ull * kG + 4ull * nread;  // offset, kG W writes, coordinates read
+                w_of_group<kG>(r, off, coords, head, Tg, bd, nread, W);
+                nb += 8ull * kG + 4ull * nread;  // kG W writes, head / offsets / coordinates read
             }
             Warr[r] = W[0];
             Wl1[r] = W[1];
@@ -663,8 +734,8 @@ __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, c
         uint64_t W = 0;
         unsigned nread = 0;
         if (r < K) {
-            W = w_of_candidate(r, off, coords, T, bound, nread);
-            nb += 8 + 8 + 4ull * nread;  // offset, W write, coordinates read
+            W = w_of_candidate(r, off, coords, head, T, bound, nread);
+            nb += 8 + 4ull * nread;  // W write, head / offsets / coordinates read
         }
         Warr[r] = W;
     }
@@ -1139,7 +1210,8 @@ __device__ long long g_scan_prof[4];
 #endif
 __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kernel(
     long long K, const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
-    const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T, int bound, BlockState *bs,
+    const int32_t *__restrict__ head, const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T,
+    int bound, BlockState *bs,
     uint64_t *Warr, unsigned *tile_epoch, unsigned long long *reports, GridBar *gb, unsigned *status,
     unsigned long long *bytes, unsigned long long *diag, unsigned long long *dbg, TailArgs ta) {
     // dynamic shared memory: global tables | local tables | window W's | merge buffers | report staging
@@ -1266,7 +1338,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
                     if (!(rb < K && tile_minc[tb_] < bound)) rb = -2;
                 }
                 uint64_t Wa = 0, Wb = 0;
-                if (va || rb >= 0) w_of_two(va ? ra : rb, va ? (rb >= 0 ? rb : -1) : -1, off, coords, T, bound, nread, Wa, Wb);
+                if (va || rb >= 0) w_of_two(va ? ra : rb, va ? (rb >= 0 ? rb : -1) : -1, off, coords, head, T, bound, nread, Wa, Wb);
                 if (!va) {  // the walk ran on rb alone
                     Wb = Wa;
                     Wa = 0;
@@ -1285,7 +1357,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
                 const long long t = tf + (long long)m * G;
                 const long long r = t * kTile + i;
                 uint64_t W = 0;
-                if (r < K && tile_minc[t] < bound) W = w_of_candidate(r, off, coords, T, bound, nread);
+                if (r < K && tile_minc[t] < bound) W = w_of_candidate(r, off, coords, head, T, bound, nread);
                 win[(size_t)m * kTile + i] = W;
                 Warr[r] = W;
             }
@@ -1433,6 +1505,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
         n_cand += cnt;
         MERGE_STAMP(1);
         int nnew = 0;
+#if MCB_MERGE_CHUNKED
         if (!MCB_MERGE_FAST || cnt > 0) {  // no report below D: no new pivot (uniform)
             // rank order: each candidate's position = number of smaller ranks (ranks are distinct)
             unsigned long long *sr = mr + cnt;  // sorted ranks
@@ -1508,6 +1581,86 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
             }
             MERGE_STAMP(3);
         }
+#else
+        if (!MCB_MERGE_FAST || cnt > 0) {  // no report below D: no new pivot (uniform)
+            // rank order: each candidate's position = number of smaller ranks (ranks are distinct)
+            unsigned long long *sr = mr + cnt;  // sorted ranks
+            uint64_t *sz = mw + cnt;            // sorted residuals against the global basis
+            uint64_t *sw = sz + cnt;            // sorted W
+            for (unsigned i = threadIdx.x; i < cnt; i += blockDim.x) {
+                const unsigned long long r = mr[i];
+                unsigned pos = 0;
+                for (unsigned j = 0; j < cnt; j++) pos += mr[j] < r;
+                sr[pos] = r;
+                sw[pos] = mw[i];
+                sz[pos] = fr_reduce(mw[i], gtab);
+            }
+            cta_sync();
+            MERGE_STAMP(2);
+            // greedy echelon in rank order (warp 0): a candidate is a new global pivot iff
+            // its residual is not in the span of the new pivots before it; then the new
+            // vectors are brought to reduced form among themselves, latest first (lane l
+            // holds vectors l and l + 32)
+            if (threadIdx.x < 32) {
+                int nn = 0;
+                for (unsigned base = 0; base < cnt && grank + nn < b; base += 32) {
+                    uint64_t z = base + lane < cnt ? sz[base + lane] : 0ull;
+                    for (int j = 0; j < nn; j++)
+                        if ((z >> s_newq[j]) & 1ull) z ^= s_newv[j];
+                    for (;;) {
+                        const unsigned bal = __ballot_sync(0xffffffffu, z != 0);
+                        if (!bal || grank + nn >= b) break;
+                        const int pl = __ffs(bal) - 1;
+                        const uint64_t v = __shfl_sync(0xffffffffu, z, pl);
+                        const unsigned qb = (unsigned)(__ffsll((long long)v) - 1);
+                        if (lane == 0) {
+                            s_newv[nn] = v;
+                            s_newq[nn] = qb;
+                            if (c == 0) {
+                                bs->pivrank[grank + nn] = (long long)sr[base + pl];
+                                bs->pivW[grank + nn] = sw[base + pl];
+                            }
+                        }
+                        nn++;
+                        if ((z >> qb) & 1ull) z ^= v;
+                    }
+                    __syncwarp();
+                }
+                uint64_t va = lane < (unsigned)nn ? s_newv[lane] : 0ull;
+                uint64_t vb = lane + 32 < (unsigned)nn ? s_newv[lane + 32] : 0ull;
+                for (int j = nn - 1; j >= 1; j--) {
+                    const uint64_t vj = __shfl_sync(0xffffffffu, j < 32 ? va : vb, j & 31);
+                    const unsigned qj = s_newq[j];
+                    if ((int)lane < j && ((va >> qj) & 1ull)) va ^= vj;
+                    if ((int)lane + 32 < j && ((vb >> qj) & 1ull)) vb ^= vj;
+                }
+                __syncwarp();
+                if (lane < (unsigned)nn) s_newv[lane] = va;
+                if (lane + 32 < (unsigned)nn) s_newv[lane + 32] = vb;
+                if (lane == 0) s_nnew = nn;
+            }
+            cta_sync();
+            nnew = s_nnew;
+            MERGE_STAMP(3);
+        }
+        if (nnew > 0) {
+            // clear the new pivot bits from the old basis vectors, append, rebuild tables
+            if (threadIdx.x < (unsigned)grank) {
+                uint64_t v = gbasis[threadIdx.x];
+                for (int j = 0; j < nnew; j++)
+                    if ((v >> s_newq[j]) & 1ull) v ^= s_newv[j];
+                gbasis[threadIdx.x] = v;
+            }
+            if (threadIdx.x < (unsigned)nnew && grank + threadIdx.x < 64) {
+                gbasis[grank + threadIdx.x] = s_newv[threadIdx.x];
+                gpiv[grank + threadIdx.x] = s_newq[threadIdx.x];
+            }
+            grank += nnew;
+            cta_sync();
+            fr_build(gtab, gbasis, gpiv, (unsigned)grank);
+            MERGE_STAMP(4);
+        }
+#endif
         if (nnew == 0 && D >= (unsigned long long)K) {
             if (c == 0 && threadIdx.x == 0) {
                 atomicOr(status, ST_RANK_DEFICIT);
@@ -2074,6 +2227,7 @@ struct mcbgpu_solver {
     int32_t *d_weight = nullptr;
     int64_t *d_off = nullptr;
     int32_t *d_coords = nullptr;
+    int32_t *d_head = nullptr;     // K x kHead: each list's first coordinates (INT_MAX past its end)
     uint64_t *d_S = nullptr;
     uint64_t *d_C = nullptr;       // cycle vector buffer (W words)
     uint64_t *d_T = nullptr;       // 64 * P words
@@ -2170,6 +2324,7 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_weight);
     cudaFree(s->d_off);
     cudaFree(s->d_coords);
+    cudaFree(s->d_head);
     cudaFree(s->d_S);
     cudaFree(s->d_C);
     cudaFree(s->d_T);
@@ -2264,6 +2419,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_weight, sizeof(int32_t) * (size_t)K);
     ALLOC(s->d_off, sizeof(int64_t) * (size_t)(K + 1));
     ALLOC(s->d_coords, sizeof(int32_t) * (size_t)(nnz + 16));  // aligned 16-byte loads read up to 11 past the end
+    ALLOC(s->d_head, sizeof(int32_t) * kHead * (size_t)K);
     ALLOC(s->d_S, sizeof(uint64_t) * (size_t)N * s->P);
     ALLOC(s->d_C, sizeof(uint64_t) * (size_t)s->P);
     ALLOC(s->d_T, sizeof(uint64_t) * 64 * (size_t)s->P);
@@ -2415,6 +2571,11 @@ static int solver_upload(mcbgpu_solver *s, const int32_t *weight, const int64_t 
     }
     const long long ntiles = (s->K + kTile - 1) / kTile;
     if (ntiles > 0) {
+        {
+            Launch L(s, KC_VALIDATE, st);
+            const int hgrid = (int)std::min<long long>((s->K + 255) / 256, (long long)(s->sm_count > 0 ? s->sm_count : 148) * 16);
+            head_kernel<<<hgrid, 256, 0, st>>>(s->d_off, s->d_coords, s->K, s->d_head);
+        }
         int grid = (int)std::min<long long>(ntiles, (long long)(s->sm_count > 0 ? s->sm_count : 148) * 8);
         {
             Launch L(s, KC_TILE_MINC, st);
@@ -2602,15 +2763,15 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         } else if (ntiles > 0) {
             Launch L(s, KC_WSTREAM, st);
             if (nl == 2)
-                blk_w_kernel<3><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                blk_w_kernel<3><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_head, s->d_tile_minc, s->d_T, bound,
                                                            s->d_bs, Wpos[0], s->d_tile_epoch, L.bytes(), s->d_Tg, bd1,
                                                            bd2, Wpos[1], Wpos[2]);
             else if (nl == 1)
-                blk_w_kernel<2><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                blk_w_kernel<2><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_head, s->d_tile_minc, s->d_T, bound,
                                                            s->d_bs, Wpos[0], s->d_tile_epoch, L.bytes(), s->d_Tg, bd1,
                                                            bd1, Wpos[1], nullptr);
             else
-                blk_w_kernel<1><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_tile_minc, s->d_T, bound,
+                blk_w_kernel<1><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_head, s->d_tile_minc, s->d_T, bound,
                                                            s->d_bs, Wpos[0], s->d_tile_epoch, L.bytes(), nullptr, 0, 0,
                                                            nullptr, nullptr);
         }
@@ -2621,6 +2782,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             long long K = s->K;
             const int64_t *off = s->d_off;
             const int32_t *co = s->d_coords;
+            const int32_t *hd = s->d_head;
             const int32_t *tm = s->d_tile_minc;
             const uint64_t *T = s->d_T;
             BlockState *bs = s->d_bs;
@@ -2644,7 +2806,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             ta.e0 = (int)e0;
             ta.Wb = Wb;
             ta.par = par;
-            void *args[] = {&K, &off, &co, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db, &ta};
+            void *args[] = {&K, &off, &co, &hd, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db, &ta};
             MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kPivotThreads),
                                                  args, pivot_smem_bytes(s->pivot_grid), st));
         }
