@@ -1761,108 +1761,146 @@ constexpr int kUpdThreads = 256;
 constexpr int kUpdSplit = MCB_UPD_SPLIT;
 constexpr int kUpdGroups = kUpdThreads / 32 / kUpdSplit;  // row groups per CTA
 
-// S_j ^= XOR of the block's final rows S_{e0+k} over the set bits k of bt, words
-// [w, Wb) with stride `step` (the caller's lanes split the words).  The final rows
-// are written once by the block tail and never change again, so any number of
-// rows can be updated from them at once.  The bits go in batches of eight rows
-// whose loads are independent (one memory round trip per word and batch).
-__device__ __forceinline__ void xor_final_rows(uint64_t *Sj, const uint64_t *S, int P, int e0, uint64_t bt, int w0,
-                                               int Wb, int step) {
-    while (bt) {
-        const uint64_t *r[8];
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            r[q] = bt ? S + (size_t)(e0 + __ffsll((long long)bt) - 1) * P : nullptr;
-            bt &= bt - 1;
-        }
-        for (int w = w0; w < Wb; w += step) {
-            uint64_t x[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) x[q] = r[q] ? r[q][w] : 0ull;
-            Sj[w] ^= ((x[0] ^ x[1]) ^ (x[2] ^ x[3])) ^ ((x[4] ^ x[5]) ^ (x[6] ^ x[7]));
-        }
-    }
+// beta of one row from its D: beta_k = D_k ^ <beta_{<k}, gcol_k> (the sequential
+// effect of the block's updates; beta = D (I + G)^-1, G[i][k] = bit i of gcol_k, an
+// invertible map, so beta = 0 exactly when D = 0).  Far rows rarely change (a few
+// dozen per block against thousands tested on the planar-chain family), so the rows
+// that do run the b-step recurrence in one lane.
+__device__ __forceinline__ uint64_t beta_of(uint64_t D, const uint64_t *__restrict__ gcol, int b) {
+    uint64_t beta = 0;
+    for (int k = 0; k < b; k++)
+        beta |= (((D >> k) & 1ull) ^ (uint64_t)parity64(beta & __ldg(gcol + k))) << k;
+    return beta;
 }
 
-// beta of a row is a linear function of its D over GF(2): beta_k = D_k ^ <beta_{<k},
-// gcol_k> gives beta = D (I + G)^-1, G[i][k] = bit i of gcol_k.  Row i of that inverse,
-// V_i, is the recurrence run on D = e_i, so beta = XOR of V_i over the set bits i of
-// D; tab[g][pat] = XOR of V_{8g+i} over the bits i of pat turns that into eight
-// lookups.  Built by the whole CTA from the block's gcol (b <= 64 columns).
-__device__ void build_beta_tables(const uint64_t *__restrict__ gcol, int b, uint64_t (*tab)[256]) {
-    __shared__ uint64_t sV[64], sg[64];
-    if (threadIdx.x < 64) sg[threadIdx.x] = (int)threadIdx.x < b ? gcol[threadIdx.x] : 0ull;
-    cta_sync();
-    if (threadIdx.x < 64) {
-        const int i = threadIdx.x;
-        uint64_t v = 0;
-        for (int k = 0; k < b; k++) v |= ((uint64_t)((k == i) ^ parity64(v & sg[k]))) << k;
-        sV[i] = v;
+// Appends v to list (counter *count) for the lanes with pred: one atomic per warp.
+// All 32 lanes call it.
+__device__ __forceinline__ unsigned warp_append(bool pred, int32_t v, int32_t *list, unsigned *count) {
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (!m) return 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == lead) base = atomicAdd(count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, lead);
+    const unsigned pos = base + (unsigned)__popc(m & ((1u << lane) - 1u));
+    if (pred) list[pos] = v;
+    return pos;
+}
+
+// Far rows that are no longer unit vectors are kept as lists of their nonzero
+// 64-bit words.  A far row j (j >= the far start, so j / 64 >= Wb) has support in
+// [0, Wb) (the XORs of earlier blocks' final rows) and in its own word j / 64 (bit j
+// alone): its list is its nonzero words below Wb plus j / 64, in any order.  D_j
+// then only needs the chosen cycles' pairs that fall into those words (the pairs
+// are sorted by S word, word_end[w] .. word_end[w + 1] being word w's), instead of
+// every pair up to the row.  On the planar-chain family the support vectors stay
+// local: a non-unit far row has 3 nonzero words at the median and rarely more than
+// a few dozen of its thousands.  A row with more than kNzCap words is dense and goes
+// through the gather of every pair (dense list).
+#ifndef MCB_NZ_CAP
+#define MCB_NZ_CAP 32  // words listed per sparse far row; beyond that the row is dense
+#endif
+constexpr int kNzCap = MCB_NZ_CAP;
+constexpr uint16_t kDenseRow = 0xFFFFu;
+static_assert(kNzCap >= 2 && kNzCap < 0xFFFF, "MCB_NZ_CAP out of range");
+
+// D of a sparse far row from its word list: for each listed word that holds pairs
+// of this block, the row's word is read once and tested against them.  List entries
+// in batches of four (independent loads).
+__device__ __forceinline__ uint64_t sparse_D(const uint64_t *S, long long j, int P, unsigned cnt, const uint32_t *nzw,
+                                             const unsigned *__restrict__ word_end, const unsigned *__restrict__ pairs,
+                                             unsigned long long &tests, unsigned long long &words) {
+    const uint32_t *L = nzw + (size_t)j * kNzCap;
+    const uint64_t *Sj = S + (size_t)j * P;
+    uint64_t D = 0;
+    for (unsigned i = 0; i < cnt; i += 4) {
+        uint32_t w[4];
+        unsigned lo[4], hi[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) w[q] = i + q < cnt ? L[i + q] : 0xFFFFFFFFu;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            lo[q] = w[q] != 0xFFFFFFFFu ? __ldg(word_end + w[q]) : 0u;
+            hi[q] = w[q] != 0xFFFFFFFFu ? __ldg(word_end + w[q] + 1) : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (lo[q] >= hi[q]) continue;
+            const uint64_t x = Sj[w[q]];
+            words++;
+            for (unsigned p = lo[q]; p < hi[q]; p++) {
+                const unsigned pr = __ldg(pairs + p);
+                D ^= ((x >> ((pr >> 6) & 63u)) & 1ull) << (pr & 63u);
+            }
+            tests += hi[q] - lo[q];
+        }
     }
-    cta_sync();
-    for (int idx = threadIdx.x; idx < 8 * 256; idx += blockDim.x) {
-        const int g = idx >> 8;
-        uint64_t acc = 0;
-        for (unsigned m = (unsigned)(idx & 255); m; m &= m - 1) acc ^= sV[8 * g + __ffs(m) - 1];
-        tab[g][idx & 255] = acc;
-    }
-    cta_sync();
+    return D;
 }
 
 // The far update of a block: every row j >= row_begin (the rows past the near
 // update's) takes D_j = <C_sel_k, S_j> (k < b), beta_j = D_j (I + G)^-1 and
 // S_j ^= XOR_k beta_jk S_{e0+k} over the first Wb words.  Most far rows are still
 // their unit vector (S_j = e_j: no update has reached them yet), and for those
-// D_j bit k is simply whether coordinate j lies on the selected cycle C_sel_k.  So
-// the update runs in three launches, all on the far stream:
+// D_j bit k is simply whether coordinate j lies on the selected cycle C_sel_k.  Few
+// rows change, so finding them and changing them are separate launches, all on the
+// far stream:
 //   far_scatter_kernel: every (coordinate c, k) pair of the block's selected cycles
 //     with c a unit far row sets bit k of Dfar[c] (first touch lists c);
-//   far_rows_kernel:    the non-unit far rows (a list carried from update to update)
-//     gather D from their words, as the reference's update does;
-//   far_touch_kernel:   the touched unit rows apply their scattered D.
-// A row that changes is no longer a unit vector: it leaves the unit set and joins
-// the non-unit list the next far update reads.  Far-row starts never decrease from
-// block to block (the near rows of a block are below every later far range), so a
-// listed row below the current start is dropped for good.
-// Rows in groups of kUpdRows list entries, kUpdSplit warps per group.  D_j (64 bits):
-// the group's warps split the chosen cycles' (coordinate, k) pairs, sorted by S word,
-// and each pair is applied to all rows of the group (independent gathers); pairs
-// whose word lies above the group's last row are skipped (S_j has support [0, j]).
-// The warps' partial D's meet in shared memory (two buffers by iteration parity, one
-// named barrier per group and iteration).  gcol, tab, pairs and word_end are the
-// block's (double-buffered by block parity, so the next block's tail can run while
-// these rows are updated).
-__global__ void __launch_bounds__(kUpdThreads) far_rows_kernel(uint64_t *S, long long row_begin, int P, int b,
-                                                               int e0, int Wb, const uint64_t *__restrict__ gcol,
+//   far_rows_kernel:    D and beta of the non-unit far rows (lists carried from update
+//     to update; sparse rows test the pairs of their listed words, one row per lane;
+//     dense rows gather every pair up to their own word, as the reference's update
+//     does) and of the touched unit rows; unchanged rows are carried over, changed
+//     rows go to a (row, beta) list;
+//   far_apply_kernel:   one CTA per changed row: S_j ^= XOR_k beta_k S_{e0+k} spread
+//     over the CTA's threads, then the row is relisted (sparse or dense).
+// Far-row starts never decrease from block to block (the near rows of a block are
+// below every later far range), so a listed row below the current start is dropped
+// for good.
+// Dense rows in groups of kUpdRows list entries, kUpdSplit warps per group.  D_j (64
+// bits): the group's warps split the chosen cycles' (coordinate, k) pairs, sorted by
+// S word, and each pair is applied to all rows of the group (independent gathers);
+// pairs whose word lies above the group's last row are skipped (S_j has support [0,
+// j]).  The warps' partial D's meet in shared memory (two buffers by iteration
+// parity, one named barrier per group and iteration).  gcol, pairs and word_end are
+// the block's (double-buffered by block parity, so the next block's tail can run
+// while these rows are updated).
+struct FarLists {
+    const int32_t *sp_in, *dn_in;
+    const unsigned *n_in;     // [sparse, dense]
+    int32_t *sp_out, *dn_out;
+    unsigned *n_out;          // [sparse, dense, touched, changed]
+    const int32_t *touch;     // touched unit rows (count n_out[2])
+    int32_t *chg_row;         // changed rows (count n_out[3])
+    unsigned long long *chg_beta;
+    uint16_t *nzc;            // per row: listed words, or kDenseRow
+    uint32_t *nzw;            // per row: kNzCap word indices
+};
+
+__global__ void __launch_bounds__(kUpdThreads) far_rows_kernel(const uint64_t *__restrict__ S, long long row_begin,
+                                                               int P, int b, const uint64_t *__restrict__ gcol,
                                                                const unsigned *__restrict__ pairs,
-                                                               const unsigned *__restrict__ word_end,
-                                                               const int32_t *__restrict__ list_in,
-                                                               const unsigned *__restrict__ n_in, int32_t *list_out,
-                                                               unsigned *n_out, unsigned long long *bytes,
-                                                               unsigned long long *diag) {
-    const unsigned nlist = *n_in;
-    const long long groups = (long long)gridDim.x * kUpdGroups;
-    if ((long long)blockIdx.x * kUpdGroups * kUpdRows >= (long long)nlist) return;  // no rows for this CTA
-    unsigned long long nb = 0, n_rows = 0, n_changed = 0, n_gather = 0, n_betabits = 0;
-    __shared__ uint64_t btab[8][256];
-    __shared__ uint64_t sD[2][kUpdGroups][kUpdSplit][kUpdRows];
-    build_beta_tables(gcol, b, btab);
+                                                               const unsigned *__restrict__ word_end, FarLists fl,
+                                                               unsigned long long *Dfar, uint8_t *unit,
+                                                               unsigned long long *bytes, unsigned long long *diag) {
+    const unsigned nsparse = fl.n_in[0], ndense = fl.n_in[1], ntouch = fl.n_out[2];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long groups = (long long)gridDim.x * kUpdGroups;
+    const bool dense_work = (long long)blockIdx.x * kUpdGroups * kUpdRows < (long long)ndense;
+    const bool sparse_work = (long long)blockIdx.x * kUpdThreads < (long long)nsparse + ntouch;
+    if (!dense_work && !sparse_work) return;  // CTA-uniform
+    unsigned long long nb = 0, n_rows = 0, n_changed = 0, n_gather = 0, n_betabits = 0;
+    unsigned long long n_sparse = 0, n_words = 0, n_tests = 0, n_swords = 0, n_touched = 0;
+    __shared__ uint64_t sD[2][kUpdGroups][kUpdSplit][kUpdRows];
     const int gi = warp / kUpdSplit, h = warp % kUpdSplit;
     int par = 0;
-    for (long long base = kUpdRows * ((long long)blockIdx.x * kUpdGroups + gi); base < (long long)nlist;
+    for (long long base = kUpdRows * ((long long)blockIdx.x * kUpdGroups + gi); base < (long long)ndense;
          base += kUpdRows * groups, par ^= 1) {
-        const int rows = (int)(((long long)nlist - base) < kUpdRows ? ((long long)nlist - base) : kUpdRows);
+        const int rows = (int)(((long long)ndense - base) < kUpdRows ? ((long long)ndense - base) : kUpdRows);
         // lane r < rows: its listed row, kept if still a far row
-        const long long jr = lane < rows ? (long long)__ldg(list_in + base + lane) : -1;
+        const long long jr = lane < rows ? (long long)__ldg(fl.dn_in + base + lane) : -1;
         const bool keep = jr >= row_begin;
         const unsigned kmask = __ballot_sync(0xffffffffu, keep);
-        if (h == 0 && kmask) {  // carried over to the next far update
-            unsigned o = 0;
-            if (lane == 0) o = atomicAdd(n_out, (unsigned)__popc(kmask));
-            o = __shfl_sync(0xffffffffu, o, 0);
-            if (keep) list_out[o + __popc(kmask & ((1u << lane) - 1u))] = (int32_t)jr;
-        }
         if (!kmask) continue;  // warp-uniform
         long long jmax = keep ? jr : -1;
         for (int d = 16; d > 0; d >>= 1) {
@@ -1904,41 +1942,81 @@ __global__ void __launch_bounds__(kUpdThreads) far_rows_kernel(uint64_t *S, long
                 for (int q = 0; q < kUpdSplit; q++) Dmine ^= sD[par][gi][q][lane];
             }
         }
-        uint64_t beta = 0;
+        if (h != 0) continue;  // the group's first warp carries the rows over
+        if (!keep) Dmine = 0;
+        // an unchanged row stays in the dense list; a changed one goes to the apply
+        warp_append(keep && Dmine == 0, (int32_t)jr, fl.dn_out, fl.n_out + 1);
+        const uint64_t beta = Dmine ? beta_of(Dmine, gcol, b) : 0ull;
+        const unsigned pos = warp_append(beta != 0, (int32_t)jr, fl.chg_row, fl.n_out + 3);
+        if (beta) fl.chg_beta[pos] = beta;
         if (keep) {
-#pragma unroll
-            for (int g = 0; g < 8; g++) beta ^= btab[g][(Dmine >> (8 * g)) & 255];
-            // algorithmic bytes (counted by the group's first warp): the S words the
-            // group's pairs touch plus, when the row changes, read + write of its
-            // first Wb words and the read of the final rows its bits select
-            if (h == 0) {
-                nb += 8ull * np + (beta ? (16ull + 8ull * (unsigned)__popcll(beta)) * (unsigned long long)Wb : 0ull);
-                n_rows++;
-                n_changed += beta ? 1 : 0;
-                n_gather += np;
-                n_betabits += (unsigned)__popcll(beta);
-            }
-        }
-        for (int r = 0; r < rows; r++) {
-            const uint64_t bt = __shfl_sync(0xffffffffu, beta, r);
-            if (!bt) continue;
-            uint64_t *Sj = S + (size_t)__shfl_sync(0xffffffffu, jr, r) * P;
-            xor_final_rows(Sj, S, P, e0, bt, h * 32 + lane, Wb, 32 * kUpdSplit);
+            nb += 8ull * np;
+            n_rows++;
+            n_changed += beta ? 1 : 0;
+            n_gather += np;
+            n_betabits += (unsigned)__popcll(beta);
         }
     }
+    // sparse rows, then the touched unit rows, one per lane
+    const long long gw = (long long)blockIdx.x * (kUpdThreads / 32) + warp;
+    const long long nwarps = (long long)gridDim.x * (kUpdThreads / 32);
+    const long long nall = (long long)nsparse + ntouch;
+    for (long long base = gw * 32; base < nall; base += nwarps * 32) {
+        const long long i = base + lane;
+        const bool touched = i >= (long long)nsparse && i < nall;
+        long long j = -1;
+        if (i < (long long)nsparse)
+            j = __ldg(fl.sp_in + i);
+        else if (touched)
+            j = __ldg(fl.touch + (i - nsparse));
+        const bool keep = !touched && j >= row_begin;
+        uint64_t D = 0;
+        if (keep) {
+            const unsigned cnt = fl.nzc[j];
+            D = sparse_D(S, j, P, cnt, fl.nzw, word_end, pairs, n_tests, n_swords);
+            n_sparse++;
+            n_words += cnt;
+            nb += 4ull + 2ull + 12ull * cnt;  // list entry, count, listed words + their two word_end entries
+        } else if (touched) {  // a unit row the scatter reached: D was scattered (never zero)
+            D = Dfar[j];
+            Dfar[j] = 0;  // ready for the next block
+            unit[j] = 0;
+            n_touched++;
+            nb += 4ull + 16ull;
+        }
+        warp_append(keep && D == 0, (int32_t)j, fl.sp_out, fl.n_out);
+        const uint64_t beta = D ? beta_of(D, gcol, b) : 0ull;
+        const unsigned pos = warp_append(beta != 0, (int32_t)j, fl.chg_row, fl.n_out + 3);
+        if (beta) {
+            fl.chg_beta[pos] = beta;
+            n_changed++;
+            n_betabits += (unsigned)__popcll(beta);
+        }
+    }
+    nb += 8ull * n_swords + 4ull * n_tests;
     for (int d = 16; d > 0; d >>= 1) {
         nb += __shfl_xor_sync(0xffffffffu, nb, d);
         n_rows += __shfl_xor_sync(0xffffffffu, n_rows, d);
         n_changed += __shfl_xor_sync(0xffffffffu, n_changed, d);
         n_gather += __shfl_xor_sync(0xffffffffu, n_gather, d);
         n_betabits += __shfl_xor_sync(0xffffffffu, n_betabits, d);
+        n_sparse += __shfl_xor_sync(0xffffffffu, n_sparse, d);
+        n_words += __shfl_xor_sync(0xffffffffu, n_words, d);
+        n_tests += __shfl_xor_sync(0xffffffffu, n_tests, d);
+        n_touched += __shfl_xor_sync(0xffffffffu, n_touched, d);
     }
     if (lane == 0 && nb) atomicAdd(bytes, nb);
-    if (lane == 0 && diag && n_rows) {  // gathered far rows, changed ones, pair words gathered, beta bits
+    if (lane == 0 && diag && (n_rows || n_sparse || n_touched)) {
+        // dense rows gathered, changed rows, pair words gathered, beta bits, touched
+        // unit rows; sparse rows tested, their listed words, pair tests
         atomicAdd(&diag[23], n_rows);
         atomicAdd(&diag[30], n_changed);
         atomicAdd(&diag[31], n_gather);
         atomicAdd(&diag[29], n_betabits);
+        atomicAdd(&diag[32], n_touched);
+        atomicAdd(&diag[38], n_sparse);
+        atomicAdd(&diag[39], n_words);
+        atomicAdd(&diag[40], n_tests);
     }
 }
 
@@ -1966,52 +2044,73 @@ __global__ void __launch_bounds__(256) far_scatter_kernel(const unsigned *__rest
     if ((threadIdx.x & 31) == 0 && nb) atomicAdd(bytes, nb);
 }
 
-// The touched unit rows, one warp each: beta from the scattered D (never zero: the
-// map D -> beta is invertible), S_c ^= XOR_k beta_k S_{e0+k} over the first Wb words
-// (all zero in a unit row below its own word), then the row leaves the unit set and
-// joins the non-unit list.
-__global__ void __launch_bounds__(256) far_touch_kernel(uint64_t *S, int P, int b, int e0, int Wb,
-                                                       const uint64_t *__restrict__ gcol,
-                                                       const int32_t *__restrict__ touch,
-                                                       const unsigned *__restrict__ n_touch,
-                                                       unsigned long long *Dfar, uint8_t *unit, int32_t *list_out,
-                                                       unsigned *n_out, unsigned long long *bytes,
-                                                       unsigned long long *diag) {
-    const unsigned nt = *n_touch;
-    const unsigned warps = blockDim.x >> 5;
-    if (blockIdx.x * warps >= nt) return;
-    __shared__ uint64_t btab[8][256];
-    build_beta_tables(gcol, b, btab);
-    const int lane = threadIdx.x & 31;
-    unsigned long long nb = 0, n_touched = 0, n_changed = 0, n_betabits = 0;
-    for (unsigned i = blockIdx.x * warps + (threadIdx.x >> 5); i < nt; i += gridDim.x * warps) {
-        const long long c = __ldg(touch + i);
-        uint64_t D = 0;
-        if (lane == 0) {
-            D = Dfar[c];
-            Dfar[c] = 0;  // ready for the next block
-            unit[c] = 0;
-            list_out[atomicAdd(n_out, 1u)] = (int32_t)c;
-        }
-        D = __shfl_sync(0xffffffffu, D, 0);
-        uint64_t bt = 0;
+// The changed far rows, one CTA each: S_j ^= XOR_k beta_k S_{e0+k} over words [0, Wb)
+// (the final rows are written once by the block tail and never change again), four
+// words per thread at a time so their loads overlap; the nonzero words are counted
+// and listed as they are written (shared counter, any order), then the row's own
+// word j / 64 joins the list and the row goes to the sparse list, or to the dense
+// list past kNzCap words.
+constexpr int kApplyThreads = 256;
+
+__global__ void __launch_bounds__(kApplyThreads) far_apply_kernel(uint64_t *S, int P, int e0, int Wb, FarLists fl,
+                                                                 unsigned long long *bytes) {
+    const unsigned nchg = fl.n_out[3];
+    if (blockIdx.x >= nchg) return;
+    __shared__ int sk[64];
+    __shared__ unsigned s_cnt;
+    unsigned long long nb = 0;
+    for (unsigned item = blockIdx.x; item < nchg; item += gridDim.x) {
+        const long long j = fl.chg_row[item];
+        const uint64_t bt = fl.chg_beta[item];
+        const int nbits = __popcll(bt);
+        if (threadIdx.x < 64) sk[threadIdx.x] = (bt >> threadIdx.x) & 1ull ? __popcll(bt & ((1ull << threadIdx.x) - 1ull)) : -1;
+        if (threadIdx.x == 0) s_cnt = 0;
+        cta_sync();
+        __shared__ int skl[64];
+        if (threadIdx.x < 64 && sk[threadIdx.x] >= 0) skl[sk[threadIdx.x]] = (int)threadIdx.x;
+        cta_sync();
+        uint64_t *Sj = S + (size_t)j * P;
+        uint32_t *L = fl.nzw + (size_t)j * kNzCap;
+        for (int w0 = threadIdx.x; w0 < Wb; w0 += 4 * kApplyThreads) {
+            uint64_t acc[4] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll 4
+            for (int i = 0; i < nbits; i++) {
+                const uint64_t *F = S + (size_t)(e0 + skl[i]) * P;
 #pragma unroll
-        for (int g = 0; g < 8; g++) bt ^= btab[g][(D >> (8 * g)) & 255];
-        if (lane == 0) {
-            nb += 8 + (bt ? (16ull + 8ull * (unsigned)__popcll(bt)) * (unsigned long long)Wb : 0ull);
-            n_touched++;
-            n_changed += bt ? 1 : 0;
-            n_betabits += (unsigned)__popcll(bt);
+                for (int q = 0; q < 4; q++) {
+                    const int w = w0 + q * kApplyThreads;
+                    if (w < Wb) acc[q] ^= F[w];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int w = w0 + q * kApplyThreads;
+                if (w < Wb) {
+                    const uint64_t x = Sj[w] ^ acc[q];
+                    Sj[w] = x;
+                    if (x) {
+                        const unsigned pos = atomicAdd(&s_cnt, 1u);
+                        if (pos < (unsigned)kNzCap) L[pos] = (uint32_t)w;
+                    }
+                }
+            }
         }
-        if (!bt) continue;
-        xor_final_rows(S + (size_t)c * P, S, P, e0, bt, lane, Wb, 32);
+        cta_sync();
+        if (threadIdx.x == 0) {
+            unsigned cnt = s_cnt;
+            if (cnt < (unsigned)kNzCap) L[cnt] = (uint32_t)(j >> 6);
+            cnt++;
+            const bool dense = cnt > (unsigned)kNzCap;
+            fl.nzc[j] = dense ? kDenseRow : (uint16_t)cnt;
+            if (dense)
+                fl.dn_out[atomicAdd(fl.n_out + 1, 1u)] = (int32_t)j;
+            else
+                fl.sp_out[atomicAdd(fl.n_out, 1u)] = (int32_t)j;
+            nb += (16ull + 8ull * (unsigned)nbits) * (unsigned long long)Wb + 4ull * (cnt < kNzCap ? cnt : kNzCap);
+        }
+        cta_sync();  // sk, skl and s_cnt are reset for the next row
     }
-    if (lane == 0 && nb) atomicAdd(bytes, nb);
-    if (lane == 0 && diag && n_touched) {  // touched unit rows, changed ones, beta bits
-        atomicAdd(&diag[32], n_touched);
-        atomicAdd(&diag[30], n_changed);
-        atomicAdd(&diag[29], n_betabits);
-    }
+    if (threadIdx.x == 0 && nb) atomicAdd(bytes, nb);
 }
 
 // The update of the next block's rows (at most 3 x 64, on the critical path: the
@@ -2240,10 +2339,16 @@ struct mcbgpu_solver {
     // far update: rows whose support vector is still the unit vector get D by scatter
     uint8_t *d_unit = nullptr;               // N: 1 while S_j = e_j (far rows only kept exact)
     unsigned long long *d_Dfar = nullptr;    // N: scattered D of unit far rows (zero between uses)
-    int32_t *d_rowlist[2] = {};              // N each: the non-unit far rows, read / written by turns
+    int32_t *d_rowlist[2] = {};              // N each: the sparse non-unit far rows, read / written by turns
+    int32_t *d_denselist[2] = {};            // N each: the dense non-unit far rows, the same way
+    uint16_t *d_nzc = nullptr;               // N: listed nonzero words of a sparse far row, or kDenseRow
+    uint32_t *d_nzw = nullptr;               // N x kNzCap: those words
     int32_t *d_touch = nullptr;              // N: unit far rows the scatter reached
-    unsigned *d_fcnt = nullptr;              // [rows in list 0, rows in list 1, touched rows]
-    int list_cur = 0;                        // the list the next far update reads
+    int32_t *d_chg_row = nullptr;            // N: far rows that change in this block's update
+    unsigned long long *d_chg_beta = nullptr;  // N: their update bits
+    unsigned *d_fcnt = nullptr;              // per list set l: [4l] sparse rows, [4l + 1] dense rows, [4l + 2] touched,
+                                             // [4l + 3] changed
+    int list_cur = 0;                        // the list set the next far update reads
     uint64_t *d_masks = nullptr;   // 2 x 64: final masks of a group's first blocks
     unsigned *d_tile_epoch = nullptr;
     int32_t *d_tile_minc = nullptr;
@@ -2338,7 +2443,13 @@ void free_solver(mcbgpu_solver *s) {
     cudaFree(s->d_Dfar);
     cudaFree(s->d_rowlist[0]);
     cudaFree(s->d_rowlist[1]);
+    cudaFree(s->d_denselist[0]);
+    cudaFree(s->d_denselist[1]);
+    cudaFree(s->d_nzc);
+    cudaFree(s->d_nzw);
     cudaFree(s->d_touch);
+    cudaFree(s->d_chg_row);
+    cudaFree(s->d_chg_beta);
     cudaFree(s->d_fcnt);
     cudaFree(s->d_masks);
     cudaFree(s->d_tile_epoch);
@@ -2436,8 +2547,14 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     ALLOC(s->d_Dfar, sizeof(unsigned long long) * (size_t)N);
     ALLOC(s->d_rowlist[0], sizeof(int32_t) * (size_t)N);
     ALLOC(s->d_rowlist[1], sizeof(int32_t) * (size_t)N);
+    ALLOC(s->d_denselist[0], sizeof(int32_t) * (size_t)N);
+    ALLOC(s->d_denselist[1], sizeof(int32_t) * (size_t)N);
+    ALLOC(s->d_nzc, sizeof(uint16_t) * (size_t)N);
+    ALLOC(s->d_nzw, sizeof(uint32_t) * kNzCap * (size_t)N);
     ALLOC(s->d_touch, sizeof(int32_t) * (size_t)N);
-    ALLOC(s->d_fcnt, sizeof(unsigned) * 4);
+    ALLOC(s->d_chg_row, sizeof(int32_t) * (size_t)N);
+    ALLOC(s->d_chg_beta, sizeof(unsigned long long) * (size_t)N);
+    ALLOC(s->d_fcnt, sizeof(unsigned) * 8);
     ALLOC(s->d_tile_epoch, sizeof(unsigned) * ntiles);
     ALLOC(s->d_tile_minc, sizeof(int32_t) * ntiles);
     ALLOC(s->d_gbar, sizeof(GridBar));
@@ -2457,7 +2574,7 @@ int mcbgpu_solver_create(mcbgpu_solver **out, int32_t N, int64_t K, int64_t nnz)
     if (e == cudaSuccess) e = cudaMemset(s->d_nearD, 0, sizeof(unsigned long long) * 2 * kNearMaxRows);
     if (e == cudaSuccess) e = cudaMemset(s->d_Dfar, 0, sizeof(unsigned long long) * ((size_t)N > 0 ? (size_t)N : 2));
     if (e == cudaSuccess) e = cudaMemset(s->d_unit, 1, (size_t)N > 0 ? (size_t)N : 16);
-    if (e == cudaSuccess) e = cudaMemset(s->d_fcnt, 0, sizeof(unsigned) * 4);
+    if (e == cudaSuccess) e = cudaMemset(s->d_fcnt, 0, sizeof(unsigned) * 8);
     if (e == cudaSuccess) e = cudaMemset(s->d_word_end, 0, sizeof(unsigned) * 2 * ((size_t)s->P + 1));
     // the far update fills every SM when it runs; with the critical path (transpose,
     // streaming pass, pivot search, near update) on a higher-priority stream, the
@@ -2523,7 +2640,7 @@ int mcbgpu_solver_reset(mcbgpu_solver *s, void *stream) {
         MCB_CUDA(cudaMemsetAsync(s->d_unit, 1, (size_t)s->N, st));
         MCB_CUDA(cudaMemsetAsync(s->d_Dfar, 0, sizeof(unsigned long long) * (size_t)s->N, st));
     }
-    MCB_CUDA(cudaMemsetAsync(s->d_fcnt, 0, sizeof(unsigned) * 4, st));
+    MCB_CUDA(cudaMemsetAsync(s->d_fcnt, 0, sizeof(unsigned) * 8, st));
     s->list_cur = 0;
     MCB_CUDA(cudaGetLastError());
     s->iters_run = 0;
@@ -2830,17 +2947,26 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 // scatter into the unit rows, gather the listed non-unit rows, apply the
                 // touched unit rows; the lists swap for the next far update
                 const int lin = s->list_cur, lout = 1 - lin;
-                MCB_CUDA(cudaMemsetAsync(s->d_fcnt + lout, 0, sizeof(unsigned), s->st2));
-                MCB_CUDA(cudaMemsetAsync(s->d_fcnt + 2, 0, sizeof(unsigned), s->st2));
+                MCB_CUDA(cudaMemsetAsync(s->d_fcnt + 4 * lout, 0, sizeof(unsigned) * 4, s->st2));
+                FarLists fl;
+                fl.sp_in = s->d_rowlist[lin];
+                fl.dn_in = s->d_denselist[lin];
+                fl.n_in = s->d_fcnt + 4 * lin;
+                fl.sp_out = s->d_rowlist[lout];
+                fl.dn_out = s->d_denselist[lout];
+                fl.n_out = s->d_fcnt + 4 * lout;
+                fl.touch = s->d_touch;
+                fl.chg_row = s->d_chg_row;
+                fl.chg_beta = s->d_chg_beta;
+                fl.nzc = s->d_nzc;
+                fl.nzw = s->d_nzw;
                 Launch L(s, KC_BLK_UPDATE, s->st2, 3);
                 far_scatter_kernel<<<sms * 2, 256, 0, s->st2>>>(pairs, wend, s->P, near_end, far_end, s->d_unit,
-                                                                 s->d_Dfar, s->d_touch, s->d_fcnt + 2, L.bytes());
+                                                                 s->d_Dfar, s->d_touch, s->d_fcnt + 4 * lout + 2,
+                                                                 L.bytes());
                 far_rows_kernel<<<grid_for(far_end - near_end), kUpdThreads, 0, s->st2>>>(
-                    s->d_S, near_end, s->P, b, (int)e0, Wb, gcol, pairs, wend, s->d_rowlist[lin], s->d_fcnt + lin,
-                    s->d_rowlist[lout], s->d_fcnt + lout, L.bytes(), s->d_diag);
-                far_touch_kernel<<<sms * 2, 256, 0, s->st2>>>(s->d_S, s->P, b, (int)e0, Wb, gcol, s->d_touch,
-                                                              s->d_fcnt + 2, s->d_Dfar, s->d_unit, s->d_rowlist[lout],
-                                                              s->d_fcnt + lout, L.bytes(), s->d_diag);
+                    s->d_S, near_end, s->P, b, gcol, pairs, wend, fl, s->d_Dfar, s->d_unit, L.bytes(), s->d_diag);
+                far_apply_kernel<<<sms * 2, kApplyThreads, 0, s->st2>>>(s->d_S, s->P, (int)e0, Wb, fl, L.bytes());
                 s->list_cur = lout;
             }
             if (wait_slot >= 0) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_upd[wait_slot], 0));

@@ -220,7 +220,8 @@ class Solver:
                 "div_step", "div_cta", "div_epoch", "cycles_tail_resolve", "cycles_tail_barrier",
                 "cycles_tail_tables", "far_rows_gathered", "profile_0", "profile_1", "profile_2", "profile_3",
                 "profile_4", "far_beta_bits", "far_rows_changed", "far_pair_words", "far_rows_touched",
-                "merge_profile_0", "merge_profile_1", "merge_profile_2", "merge_profile_3", "merge_profile_4"]
+                "merge_profile_0", "merge_profile_1", "merge_profile_2", "merge_profile_3", "merge_profile_4",
+                "far_sparse_rows", "far_sparse_words", "far_sparse_tests"]
         return dict(zip(keys, out.tolist()))
 
     @property
