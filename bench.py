@@ -14,8 +14,9 @@ as part of the graph-to-basis time (`e2e_with_preparation`).
 
 One step = one complete de Pina solve (all N iterations) on the GPU: reset S to the
 unit vectors, then the blocked device loop.  The rank-ordered candidates and their
-coordinate lists stay resident in HBM (7.7 GB at the default size, larger than the
-129 MB L2, so no flush is needed between steps).
+coordinate lists stay resident in HBM.  The reset writes the whole support matrix
+(10.4 GB at the default size), larger than the 129 MB L2, so every step starts with
+a flushed L2.
 
   value       mean seconds per solve (CUDA events on the solver's stream)
   plain_gpu   the per-iteration device form (one odd-candidate search and one update
@@ -29,7 +30,9 @@ coordinate lists stay resident in HBM (7.7 GB at the default size, larger than t
   roofline    the kernel class with the largest time share, algorithmic bytes per
               launch / mean event-timed launch duration vs the measured HBM peak;
               the launch durations come from a second pass of the same K solves
-              with an event pair around every launch (out of the timed region)
+              of the solver that gives `value`, with an event pair around every
+              launch (out of the timed region); `search`: the same over the
+              search kernels (streaming pass, correction, pivot search) together
   cpu_baseline  the reference's CPU main loop (oracle port of mcb/mcb_non_cpu_rd.cpp)
               on this host's cores: a label pass over a sample of the FVS trees
               and the full-width update over a sample of rows, extrapolated to the
@@ -332,6 +335,11 @@ def run_reference(args, world, rank, pg):
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def solver_words(N):
+    """64-bit words of one support-vector row in the solver (ceil(N / 64) rounded up to 4)."""
+    return ((N + 63) // 64 + 3) // 4 * 4
+
+
 def pinned_like(a):
     """A pinned host copy of numpy array `a` (cudaMallocHost through the C ABI)."""
     import ctypes as C
@@ -532,14 +540,6 @@ def run_gpu(args, world, rank, local, pg):
     launches = solver.launches - launches0
     sel, tot = solver.results(stream=sh)
     assert np.array_equal(sel, sel0) and tot == tot0, "timed solves differ from the first"
-    # per-kernel durations: the same K solves again, with an event pair around
-    # every launch on the solver's stream (kept out of the timed region above)
-    solver.set_profiling(True)
-    for _ in range(args.steps):
-        solve_once()
-    torch.cuda.synchronize()
-    stats = solver.kernel_stats()
-    solver.set_profiling(False)
     if pg:
         ms = max_over_ranks(ms, pg)
         pg.barrier()
@@ -555,7 +555,6 @@ def run_gpu(args, world, rank, local, pg):
     plain = None
     if not args.no_plain and args.max_iterations < 0:
         plain = plain_form(solver, p.N, stream, sh, windows=args.plain_windows, width=args.plain_width)
-        plain["speedup"] = plain["value"] / (ms / 1e3)
 
     full_ms = ms
     if lsolver is not None:
@@ -566,6 +565,7 @@ def run_gpu(args, world, rank, local, pg):
         torch.cuda.synchronize()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
+        l0 = lsolver.launches
         ev0.record(stream)
         for _ in range(args.steps):
             lsolver.reset(sh)
@@ -573,6 +573,7 @@ def run_gpu(args, world, rank, local, pg):
         ev1.record(stream)
         torch.cuda.synchronize()
         lms = ev0.elapsed_time(ev1) / args.steps
+        llaunches = lsolver.launches - l0
         lsel, ltot = lsolver.results(stream=sh)
         assert np.array_equal(lsel, sel0) and ltot == tot0, "the learned form's solve differs"
         learned["solve_s"] = lms / 1e3
@@ -581,10 +582,30 @@ def run_gpu(args, world, rank, local, pg):
             lms = max_over_ranks(lms, pg)
         if lms < ms:  # the fastest form is the line's value; its lists feed the e2e below
             ms = lms
+            launches = llaunches
             solver.close()
             solver = lsolver
             w, off, co = lists_l
             learned["is_value"] = True
+        else:
+            lsolver.close()
+
+    if plain is not None:  # the per-iteration form against the fastest form
+        plain["speedup"] = plain["value"] / (ms / 1e3)
+        plain["speedup_vs_full_list"] = plain["value"] / (full_ms / 1e3)
+
+    # per-kernel durations of the solver that gives `value`: K solves again, with an
+    # event pair around every launch on its streams (kept out of the timed region),
+    # and its search counters
+    solver.diagnostics(reset=True)
+    solver.set_profiling(True)
+    for _ in range(args.steps):
+        solver.reset(sh)
+        solver.run(args.max_iterations, sh)
+    torch.cuda.synchronize()
+    stats = solver.kernel_stats()
+    solver.set_profiling(False)
+    diag = solver.diagnostics(reset=True)
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
@@ -635,9 +656,26 @@ def run_gpu(args, world, rank, local, pg):
         if rec:  # captured on this workload (or scaled to it; see the file)
             traffic = rec.get(name)
     total_ms = sum(v["ms"] for v in stats.values())
+    # the search phase (streaming pass, its correction, the pivot search): the part of
+    # the metric's "search HBM GB/s" -- their algorithmic bytes over their event time
+    srch = [stats[k] for k in ("blk_w", "blk_wfix", "blk_pivot") if k in stats]
+    s_ms = sum(v["ms"] for v in srch)
+    s_b = sum(v["bytes"] for v in srch)
+    blocks = max(int(diag.get("blocks", 0)), 1)
+    search = {"kernels": ["blk_w", "blk_wfix", "blk_pivot"], "GBps": s_b / (s_ms / 1e3) / 1e9 if s_ms > 0 else None,
+              "frac": (s_b / (s_ms / 1e3) / 1e9) / peak if s_ms > 0 else None, "ms_per_solve": s_ms / args.steps,
+              "pivot_steps_per_block": diag.get("pivot_steps", 0) / blocks,
+              "tiles_loaded_per_block": diag.get("tiles_loaded", 0) / blocks,
+              "tiles_computed_per_block": diag.get("tiles_computed", 0) / blocks}
+    far = {"dense_rows_per_block": diag.get("far_rows_gathered", 0) / blocks,
+           "sparse_rows_per_block": diag.get("far_sparse_rows", 0) / blocks,
+           "listed_words_per_sparse_row": diag.get("far_sparse_words", 0) / max(diag.get("far_sparse_rows", 0), 1),
+           "changed_rows_per_block": diag.get("far_rows_changed", 0) / blocks,
+           "touched_unit_rows_per_block": diag.get("far_rows_touched", 0) / blocks}
     roofline = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                 "bytes_per_launch": per_launch_b, "launch_ms": per_launch_s * 1e3, "share": st["ms"] / total_ms,
+                "search": search, "far_update": far,
                 "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
                                 "GBps": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 and v["bytes"] else None}
                             for k, v in sorted(stats.items(), key=lambda kv: -kv[1]["ms"])}}
@@ -649,8 +687,9 @@ def run_gpu(args, world, rank, local, pg):
         return None
     extra = {"total_weight": tot, "total_weight_pinned": pin, "solves_per_s_all_ranks": world * 1e3 / ms,
              "cycle_nnz": int(off[-1]), "preparation": args.prep,
-             "l2": ("inputs (cycle lists %.2f GB) larger than the 129 MB L2; no flush" % (int(off[-1]) * 4 / 1e9))
-             if int(off[-1]) * 4 > 129e6 else "small case: inputs fit in L2"}
+             "l2": ("every solve starts by writing the %.1f GB support matrix (reset to unit vectors), larger than "
+                    "the 129 MB L2, which flushes it between steps; cycle lists %.2f GB"
+                    % (8.0 * p.N * solver_words(p.N) / 1e9, int(off[-1]) * 4 / 1e9))}
     return {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic", "config": config_of(p, args, extra),
