@@ -519,6 +519,13 @@ def run_gpu(args, world, rank, local, pg):
         solver.reset(sh)
         solver.run(args.max_iterations, sh)
 
+    # search shapes: one tuning solve (the candidate shapes take turns group by group;
+    # each quarter of the solve keeps its fastest), checked like any other solve
+    shapes = None
+    if args.max_iterations < 0 and args.tune:
+        shapes = solver.tune(sh)
+        sel, tot = solver.results(stream=sh)
+        assert np.array_equal(sel, sel0) and tot == tot0, "the tuning solve differs from the first"
     for i in range(args.warmup):
         solve_once()
     sel, tot = solver.results(stream=sh)
@@ -558,7 +565,13 @@ def run_gpu(args, world, rank, local, pg):
 
     full_ms = ms
     if lsolver is not None:
-        # the learned form's solve on its resident prefix lists, timed as above
+        # the learned form's solve on its resident prefix lists, timed as above (its
+        # own tuning solve first)
+        lshapes = None
+        if args.tune:
+            lshapes = lsolver.tune(sh)
+            lsel, ltot = lsolver.results(stream=sh)
+            assert np.array_equal(lsel, sel0) and ltot == tot0, "the learned form's tuning solve differs"
         for _ in range(args.warmup):
             lsolver.reset(sh)
             lsolver.run(-1, sh)
@@ -583,6 +596,7 @@ def run_gpu(args, world, rank, local, pg):
         if lms < ms:  # the fastest form is the line's value; its lists feed the e2e below
             ms = lms
             launches = llaunches
+            shapes = lshapes
             solver.close()
             solver = lsolver
             w, off, co = lists_l
@@ -686,6 +700,7 @@ def run_gpu(args, world, rank, local, pg):
     if rank != 0:
         return None
     extra = {"total_weight": tot, "total_weight_pinned": pin, "solves_per_s_all_ranks": world * 1e3 / ms,
+             "search_shapes": shapes,
              "cycle_nnz": int(off[-1]), "preparation": args.prep,
              "l2": ("every solve starts by writing the %.1f GB support matrix (reset to unit vectors), larger than "
                     "the 129 MB L2, which flushes it between steps; cycle lists %.2f GB"
@@ -907,6 +922,8 @@ def main():
     ap.add_argument("--prep", choices=["device", "host"], default="device",
                     help="candidate generation on the GPU (default) or on the host")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-iteration form's timing")
+    ap.add_argument("--no-tune", dest="tune", action="store_false",
+                    help="keep the default search shape (no tuning solve)")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="skip the learned proposal's form")
     ap.add_argument("--train-graphs", type=int, default=3, help="graphs whose traces train the proposal")

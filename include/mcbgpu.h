@@ -201,11 +201,38 @@ int mcbgpu_solver_kernel_stats(mcbgpu_solver *s, mcbgpu_kernel_stat *out, int ma
  * arrivals), [14]/[15] most/fewest barriers of a CTA in one launch, [16]-[19] first
  * step at which two CTAs disagreed on the merged result (flag, step, CTA, block),
  * [20] / [21] / [22] SM clock cycles of CTA 0 in the block tail: resolve, the tail's
- * grid barrier, final rows + tables; far update: [23] non-unit rows gathered,
+ * grid barrier, final rows + tables; far update: [23] dense non-unit rows gathered,
  * [29] update bits of the changed rows, [30] rows changed, [31] pair words gathered,
- * [32] unit rows reached by the scatter; [24]-[28] and [33]-[37] per-phase clock
+ * [32] unit rows reached by the scatter, [38] sparse non-unit rows tested, [39]
+ * their listed words, [40] their pair tests; [24]-[28] and [33]-[37] per-phase clock
  * counters of profiling builds.  At most 48 counters; synchronises the device. */
 int mcbgpu_solver_diagnostics(mcbgpu_solver *s, int64_t *out, int n, int reset);
+/* Search shapes of the blocked run (no counterpart in the reference, whose host scan
+ * has no shape).  A shape sets the pivot search's window (W tiles a CTA scans per
+ * step, by how many of the block's 64 pivots are known), the local pivots after
+ * which a CTA ends its step, and how far past the previous block's last pivot the
+ * streaming pass reaches.  Every shape gives the same result; only the time
+ * differs.  A solve is cut into MCBGPU_SHAPE_SEGMENTS segments of 64-iteration
+ * blocks, each with its own shape (candidate 0, the built-in default, until tuned).
+ *
+ * tune: one complete blocked run from a reset, the candidate shapes taking turns
+ *   group by group (the blocks that share one streaming pass); each segment then
+ *   keeps the shape with the least mean search time per block (event-timed on the
+ *   device, from a group's first transpose to the end of its last pivot search).
+ *   The run's results are valid like those of mcbgpu_solver_run.  Synchronises
+ *   `stream`.  ms_per_block (may be NULL): MCBGPU_SHAPE_SEGMENTS x n_shapes means;
+ *   chosen (may be NULL): the shape of each segment.  With fewer than 4 groups per
+ *   segment and shape the default stays.
+ * set_shape: force one candidate for every block (-1: back to the per-segment choice).
+ * shapes: the candidates' parameters, MCBGPU_SHAPE_INTS each (window early, rank it
+ *   ends at, window middle, rank the tail window starts at, window tail, local-pivot
+ *   limit, streaming reach in percent), their number, and each segment's shape. */
+#define MCBGPU_SHAPE_SEGMENTS 4
+#define MCBGPU_SHAPE_INTS 7
+int mcbgpu_solver_tune(mcbgpu_solver *s, double *ms_per_block, int32_t *chosen, void *stream);
+int mcbgpu_solver_set_shape(mcbgpu_solver *s, int32_t shape);
+int mcbgpu_solver_shapes(const mcbgpu_solver *s, int32_t *params, int32_t max_shapes, int32_t *n_shapes,
+                         int32_t *segment_shape);
 /* Kernel launches issued by this handle so far (for accounting). */
 int64_t mcbgpu_solver_launches(const mcbgpu_solver *s);
 /* Device bytes held by the handle. */

@@ -109,6 +109,9 @@ GPU_SYMBOLS = {
     "mcbgpu_solver_set_profiling": (C.c_int, [vp, C.c_int]),
     "mcbgpu_solver_kernel_stats": (C.c_int, [vp, vp, C.c_int, C.POINTER(C.c_int)]),
     "mcbgpu_solver_diagnostics": (C.c_int, [vp, vp, C.c_int, C.c_int]),
+    "mcbgpu_solver_tune": (C.c_int, [vp, vp, vp, vp]),
+    "mcbgpu_solver_set_shape": (C.c_int, [vp, i32]),
+    "mcbgpu_solver_shapes": (C.c_int, [vp, vp, i32, C.POINTER(i32), vp]),
     "mcbgpu_solver_launches": (i64, [vp]),
     "mcbgpu_solver_device_bytes": (i64, [vp]),
     "mcbgpu_solver_destroy": (C.c_int, [vp]),

@@ -71,25 +71,36 @@ def build_host(force: bool = False) -> str:
     return out
 
 
+def _defines() -> list[str]:
+    """Tuning macros for the GPU library (MCB_DEFINES="-DMCB_NZ_CAP=64 ..."); only -D
+    options are taken.  The default build uses none."""
+    return [d for d in os.environ.get("MCB_DEFINES", "").split() if d.startswith("-D")]
+
+
 def build_gpu(force: bool = False) -> str:
     out = os.path.join(LIB, "libmcbgpu.so")
     srcs = [os.path.join(CSRC, "gpu", f) for f in GPU_SOURCES]
-    if not (force or _stale(out, srcs + _headers())):
-        return out
-    nvcc = _nvcc()
     objdir = os.path.join(LIB, "obj")
     os.makedirs(objdir, exist_ok=True)
+    stamp = os.path.join(objdir, "defines.txt")
+    defines = _defines()
+    same = os.path.exists(stamp) and open(stamp).read() == " ".join(defines)
+    if not (force or not same or _stale(out, srcs + _headers())):
+        return out
+    nvcc = _nvcc()
     objs = []
 
     def compile_one(src: str) -> str:
         obj = os.path.join(objdir, os.path.basename(src).replace(".cu", ".o"))
         _run([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INC,
-              "-I" + os.path.join(CSRC, "gpu"), "-c", src, "-o", obj])
+              "-I" + os.path.join(CSRC, "gpu"), *defines, "-c", src, "-o", obj])
         return obj
 
     with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(compile_one, srcs))
     _run([nvcc, *ARCH, "-shared", "-o", out, *objs, "-lcudart"])
+    with open(stamp, "w") as f:
+        f.write(" ".join(defines))
     return out
 
 

@@ -97,8 +97,31 @@ constexpr int kGStride = kGroup == 3 ? 4 : kGroup;  // words per coordinate in t
 #ifndef MCB_MERGE_FAST
 #define MCB_MERGE_FAST 1  // merge: skip the sort and echelon when no report lies below D
 #endif
-constexpr int kLmax = MCB_LMAX;           // local pivots a CTA reports per pivot step
-constexpr int kWinTiles = MCB_WIN_TILES;  // tiles a CTA scans per pivot step (<= 32)
+#ifndef MCB_LMAX_CAP
+#define MCB_LMAX_CAP 8  // report slots per CTA and step: the largest local-pivot limit a shape may use
+#endif
+#ifndef MCB_WIN_CAP
+#define MCB_WIN_CAP 12  // the largest window (tiles per CTA and step) a shape may use
+#endif
+constexpr int kLmax = MCB_LMAX_CAP;       // report slots per CTA and pivot step
+constexpr int kWinTiles = MCB_WIN_TILES;  // tiles a CTA scans per pivot step (default shape)
+static_assert(MCB_LMAX >= 1 && MCB_LMAX <= kLmax, "MCB_LMAX above MCB_LMAX_CAP");
+static_assert(MCB_EARLY_WIN <= MCB_WIN_CAP && MCB_WIN_TILES <= MCB_WIN_CAP && MCB_TAIL_WIN <= MCB_WIN_CAP &&
+                  MCB_WIN_CAP <= 32, "a window above MCB_WIN_CAP (at most 32)");
+
+// The runtime shape of the blocked search (blk_pivot_kernel and the streaming pass's
+// reach).  Every shape gives the same pivots (the search is exact for any window
+// and local-pivot limit); only the time differs, by graph and by how far a solve has
+// got, so a solver can time several on its own graph (mcbgpu_solver_tune).
+struct PivotShape {
+    int win_early, rank_early;  // tiles per CTA and step while fewer than rank_early pivots are known
+    int win_mid;                // ... from rank_early on
+    int rank_tail, win_tail;    // ... once rank_tail pivots are known
+    int lmax;                   // local pivots after which a CTA ends its step (<= kLmax)
+    int stream_pct;             // the streaming pass reaches this percent past the last block's last pivot
+};
+constexpr PivotShape kDefaultShape = {MCB_EARLY_WIN, MCB_EARLY_RANK, MCB_WIN_TILES, MCB_TAIL_RANK,
+                                      MCB_TAIL_WIN,  MCB_LMAX,       25};
 constexpr int kUpdRows = MCB_UPD_ROWS;    // rows per warp group in the block update (<= 32)
 constexpr unsigned long long kNone = 0xFFFFFFFFFFFFFFFFull;
 constexpr unsigned kNoIndex = 0xFFFFFFFFu;
@@ -376,8 +399,8 @@ __device__ __forceinline__ void transpose_rows(const uint64_t *__restrict__ S, i
 
 __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int e0, int b, int Wb,
                                      uint64_t *__restrict__ T, BlockState *bs, long long ntiles,
-                                     GridBar *gb, long long window_tiles, uint64_t *__restrict__ Tg, int b1,
-                                     int Wb1, int b2, int Wb2) {
+                                     GridBar *gb, long long window_tiles, int stream_pct,
+                                     uint64_t *__restrict__ Tg, int b1, int Wb1, int b2, int Wb2) {
     if (*(volatile const unsigned *)&bs->failed) {  // set by an earlier block's pivot kernel (same stream)
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             bs->pred_tiles = 0;  // the streaming pass and its correction then cover no tile
@@ -391,12 +414,12 @@ __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int 
         bs->rank = 0;
         bs->epoch = bs->epoch + 1;
         bs->b = (unsigned)b;
-        // stream 25% past the previous block's deepest pivot; the pivot kernel
-        // computes any further tile it needs
+        // stream stream_pct percent past the previous block's deepest pivot; the
+        // pivot kernel computes any further tile it needs
         long long pred = ntiles;
         if (e0 != 0) {
             const long long lp = bs->last_pivot + 1;
-            const long long a = (lp + lp / 4) / kTile + 1, m = bs->max_tile + 1;
+            const long long a = (lp + lp * stream_pct / 100) / kTile + 1, m = bs->max_tile + 1;
             pred = (a > m ? a : m) + window_tiles;
         }
         const int later = (b1 > 0 ? 1 : 0) + (b2 > 0 ? 1 : 0);  // the pass serves the group's later blocks too
@@ -844,9 +867,10 @@ __global__ void __launch_bounds__(kTile) blk_wfix_kernel(const int32_t *__restri
 // earlier W's.
 //
 // Step, part 1 (no communication): CTA c scans its own tiles t = c (mod G) from s
-// on, up to kWinTiles of them.  It keeps a local basis B ∪ L_c and, in rank order,
-// turns every candidate whose residual against B ∪ L_c is non-zero into a local
-// pivot (appended to L_c).  It stops early after kLmax local pivots.  It reports
+// on, up to the shape's window of them.  It keeps a local basis B ∪ L_c and, in rank
+// order, turns every candidate whose residual against B ∪ L_c is non-zero into a
+// local pivot (appended to L_c).  It stops early after the shape's lmax local
+// pivots.  It reports
 // its local pivots (rank, W) and `end`: every candidate of its tiles below `end`
 // has been processed.
 // Part 2, after one grid barrier, in every CTA identically: D = min over CTAs of
@@ -862,7 +886,7 @@ __global__ void __launch_bounds__(kTile) blk_wfix_kernel(const int32_t *__restri
 // the next call that writes the same slots.
 constexpr int kPivotThreads = 512;        // threads of a pivot-kernel CTA
 constexpr int kWarps = kPivotThreads / 32;
-constexpr int kWinMax = MCB_TAIL_WIN > kWinTiles ? MCB_TAIL_WIN : kWinTiles;  // largest window
+constexpr int kWinMax = MCB_WIN_CAP;  // largest window
 constexpr int kWinW = kWinMax * kTile;  // W's the window buffer holds
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
@@ -1213,7 +1237,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
     const int32_t *__restrict__ head, const int32_t *__restrict__ tile_minc, const uint64_t *__restrict__ T,
     int bound, BlockState *bs,
     uint64_t *Warr, unsigned *tile_epoch, unsigned long long *reports, GridBar *gb, unsigned *status,
-    unsigned long long *bytes, unsigned long long *diag, unsigned long long *dbg, TailArgs ta) {
+    unsigned long long *bytes, unsigned long long *diag, unsigned long long *dbg, TailArgs ta, PivotShape sh) {
     // dynamic shared memory: global tables | local tables | window W's | merge buffers | report staging
     extern __shared__ __align__(128) unsigned char dsm[];
     const unsigned G = gridDim.x;
@@ -1288,9 +1312,9 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
     do {              \
     } while (0)
 #endif
-        const int wsz = grank < MCB_EARLY_RANK ? MCB_EARLY_WIN
-                        : grank >= MCB_TAIL_RANK ? MCB_TAIL_WIN
-                                                 : kWinTiles;  // same in every CTA
+        const int wsz = grank < sh.rank_early ? sh.win_early
+                        : grank >= sh.rank_tail ? sh.win_tail
+                                                : sh.win_mid;  // same in every CTA
         const int nwin = tf >= ntiles ? 0 : (int)min((long long)wsz, (ntiles - 1 - tf) / G + 1);
         if (threadIdx.x < (unsigned)nwin) s_tag[threadIdx.x] = ld_acquire_u32(&tile_epoch[tf + (long long)threadIdx.x * G]);
         cta_sync();
@@ -1407,7 +1431,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
             basis_add(ltab, lbasis, lpiv, lrank, x, s_chg);
             nloc++;
             from = p + 1;
-            if (nloc == kLmax) {
+            if (nloc == sh.lmax) {
                 end = rank + 1;
                 trunc = true;
                 break;
@@ -1738,7 +1762,7 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
 }
 
 // Dynamic shared memory of blk_pivot_kernel for a grid of G CTAs: two sets of
-// Four-Russians tables, the window of kWinTiles tiles of W's, the merge buffers
+// Four-Russians tables, the window of kWinMax tiles of W's, the merge buffers
 // (5 x G x kLmax words) and the report staging (G x (2 kLmax + 2) words).
 size_t pivot_smem_bytes(int G) {
     return 32768 + 8 * (size_t)kWinW + 8 * 5 * (size_t)G * kLmax + 8 * (size_t)G * (2 * kLmax + 2);
@@ -2318,6 +2342,25 @@ __global__ void __launch_bounds__(256) cert_check_kernel(const unsigned long lon
 }  // namespace
 
 // ===========================================================================
+// The candidate search shapes a solver times (mcbgpu_solver_tune): the compiled-in
+// default, more local pivots per step, wider windows, deeper streaming passes.  A
+// solve is cut into kShapeSegs segments of blocks, each with its own shape (the
+// pivots of later blocks lie deeper in the rank order).  On the 1M-vertex
+// planar-chain graph the wider windows with 8 local pivots take 0.105-0.116 ms per
+// block against 0.129-0.185 ms for the default (a one-tile early window was 10x
+// slower there and is not a candidate).
+constexpr int kShapeSegs = 4;
+constexpr int kShapeInts = 7;  // ints per shape in mcbgpu_solver_shapes
+const PivotShape kCandidateShapes[] = {
+    kDefaultShape,
+    {2, 48, 6, 60, 8, 8, 25},
+    {4, 48, 8, 56, 12, 8, 25},
+    {3, 40, 8, 56, 12, 8, 60},
+    {2, 40, 8, 56, 12, 8, 40},
+    {3, 40, 8, 56, 12, 8, 40},
+};
+constexpr int kNumShapes = (int)(sizeof(kCandidateShapes) / sizeof(kCandidateShapes[0]));
+
 struct mcbgpu_solver {
     int N = 0, W = 0, P = 0, words_cap = 0;
     long long K = 0, nnz = 0;
@@ -2382,6 +2425,19 @@ struct mcbgpu_solver {
     size_t pool_next = 0;
     unsigned long long *d_bytes = nullptr;  // KC_COUNT counters
     unsigned long long *d_diag = nullptr;   // pivot-kernel counters (see mcbgpu_solver_diagnostics)
+    // search shapes: the shape of each segment of a solve (0 = the default until a
+    // tuning run picks), a shape forced for every block (-1: none), and while a
+    // tuning run is on, the blocks' search times (transpose to pivot-kernel end on
+    // the critical stream) by segment and shape
+    int seg_shape[kShapeSegs] = {};
+    int forced_shape = -1;
+    bool tuning = false;
+    struct TuneRec {
+        int seg, shape, blocks;  // a group of `blocks` blocks
+        cudaEvent_t a, b;
+    };
+    std::vector<TuneRec> tune_recs;
+    std::vector<cudaEvent_t> tpool;
 };
 
 namespace {
@@ -2426,6 +2482,7 @@ namespace {
 
 void free_solver(mcbgpu_solver *s) {
     if (!s) return;
+    for (cudaEvent_t e : s->tpool) cudaEventDestroy(e);
     cudaFree(s->d_weight);
     cudaFree(s->d_off);
     cudaFree(s->d_coords);
@@ -2822,6 +2879,9 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
     cudaStream_t caller = (cudaStream_t)stream;
     cudaStream_t st = s->st1;  // the critical path; joined back into the caller's stream at the end
     const int64_t iters = (max_iterations >= 0 && max_iterations < s->N) ? max_iterations : s->N;
+    const int64_t nblocks = (iters + 63) / 64;
+    size_t tnext = 0;             // tuning events used
+    cudaEvent_t tev_a = nullptr;  // start of the group being timed
     const int sms = s->sm_count > 0 ? s->sm_count : 148;
     long long ntiles = (s->K + kTile - 1) / kTile;
     // The update of a block is split: the next rows on `st` (the next block's
@@ -2863,11 +2923,30 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         const int nl = (bl[0] > 0 ? 1 : 0) + (bl[1] > 0 ? 1 : 0);
         const int bd1 = (int)(e0 + 64 + bl[0]), bd2 = (int)(e0 + 128 + bl[1]);
         const int Wb1 = bl[0] > 0 ? (bd1 + 63) / 64 : 0, Wb2 = bl[1] > 0 ? (bd2 + 63) / 64 : 0;
+        // this block's search shape: by segment (tuned or default), forced, or while
+        // tuning every candidate in turn, group by group (a group's blocks share one
+        // streaming pass, so a group is the unit that is timed: from its first
+        // transpose to its last pivot search)
+        const int64_t blk = e0 / 64;
+        const int seg = (int)(blk * kShapeSegs / nblocks);
+        const int shp = s->tuning ? (int)((blk / kGroup) % kNumShapes)
+                        : s->forced_shape >= 0 ? s->forced_shape
+                                               : s->seg_shape[seg];
+        const PivotShape sh = kCandidateShapes[shp];
+        if (s->tuning && pos == 0) {
+            while (s->tpool.size() < tnext + 2) {
+                cudaEvent_t ev = nullptr;
+                MCB_CUDA(cudaEventCreate(&ev));
+                s->tpool.push_back(ev);
+            }
+            tev_a = s->tpool[tnext++];
+            MCB_CUDA(cudaEventRecord(tev_a, st));
+        }
         {
             Launch L(s, KC_TRANSPOSE, st);
             blk_transpose_kernel<<<(std::max(Wb, std::max(Wb1, Wb2)) + 7) / 8, 256, 0, st>>>(
-                s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles, s->d_gbar, (long long)s->pivot_grid * kWinTiles,
-                s->d_Tg, bl[0], Wb1, bl[1], Wb2);
+                s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles, s->d_gbar,
+                (long long)s->pivot_grid * sh.win_mid, sh.stream_pct, s->d_Tg, bl[0], Wb1, bl[1], Wb2);
         }
         if (ntiles > 0 && pos > 0) {
             Launch L(s, KC_WFIX, st);
@@ -2923,9 +3002,16 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             ta.e0 = (int)e0;
             ta.Wb = Wb;
             ta.par = par;
-            void *args[] = {&K, &off, &co, &hd, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db, &ta};
+            PivotShape shv = sh;
+            void *args[] = {&K, &off, &co, &hd, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db, &ta,
+                            &shv};
             MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kPivotThreads),
                                                  args, pivot_smem_bytes(s->pivot_grid), st));
+        }
+        if (s->tuning && (pos == kGroup - 1 || e0 + b >= iters)) {  // the group's last block
+            cudaEvent_t tev_b = s->tpool[tnext++];
+            MCB_CUDA(cudaEventRecord(tev_b, st));
+            s->tune_recs.push_back({seg, shp, (int)(blk % kGroup) + 1, tev_a, tev_b});
         }
         if (e0 + b < s->N) {
             const int near_rows = kGroup == 1 ? 64 : pos == kGroup - 1 ? 64 * kGroup : 64 * (kGroup - 1 - pos);
@@ -3140,6 +3226,79 @@ int mcbgpu_solver_diagnostics(mcbgpu_solver *s, int64_t *out, int n, int reset) 
         MCB_CUDA(cudaMemset(s->d_diag, 0, sizeof v));
         MCB_CUDA(cudaMemset(s->d_diag + 15, 0xff, sizeof(unsigned long long)));
     }
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_tune(mcbgpu_solver *s, double *ms_per_block, int32_t *chosen, void *stream) {
+    if (!s) {
+        set_error("mcbgpu_solver_tune: NULL handle");
+        return MCBGPU_E_ARG;
+    }
+    if (!s->uploaded) {
+        set_error("mcbgpu_solver_tune: candidates not uploaded");
+        return MCBGPU_E_STATE;
+    }
+    const int64_t nblocks = ((int64_t)s->N + 63) / 64;
+    // a few groups of every shape in every segment, else the default shape stays
+    const bool enough = nblocks >= 4LL * kGroup * kNumShapes * kShapeSegs;
+    int rc = mcbgpu_solver_reset(s, stream);
+    if (rc) return rc;
+    s->tune_recs.clear();
+    s->tuning = enough;
+    rc = mcbgpu_solver_run(s, -1, stream);
+    s->tuning = false;
+    if (rc) return rc;
+    MCB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    double sum[kShapeSegs][kNumShapes] = {};
+    long long cnt[kShapeSegs][kNumShapes] = {};
+    for (const auto &r : s->tune_recs) {
+        float t = 0;
+        MCB_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+        sum[r.seg][r.shape] += t;
+        cnt[r.seg][r.shape] += r.blocks;
+    }
+    s->tune_recs.clear();
+    for (int g = 0; g < kShapeSegs; g++) {
+        int best = -1;
+        double bt = 0;
+        for (int k = 0; k < kNumShapes; k++) {
+            const double m = cnt[g][k] ? sum[g][k] / (double)cnt[g][k] : 0.0;
+            if (ms_per_block) ms_per_block[g * kNumShapes + k] = m;
+            if (cnt[g][k] && (best < 0 || m < bt)) {
+                best = k;
+                bt = m;
+            }
+        }
+        if (enough && best >= 0) s->seg_shape[g] = best;
+        if (chosen) chosen[g] = s->seg_shape[g];
+    }
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_set_shape(mcbgpu_solver *s, int32_t shape) {
+    if (!s || shape < -1 || shape >= kNumShapes) {
+        set_error("mcbgpu_solver_set_shape: invalid argument");
+        return MCBGPU_E_ARG;
+    }
+    s->forced_shape = shape;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_shapes(const mcbgpu_solver *s, int32_t *params, int32_t max_shapes, int32_t *n_shapes,
+                         int32_t *segment_shape) {
+    if (!s || (!params && max_shapes > 0)) {
+        set_error("mcbgpu_solver_shapes: invalid argument");
+        return MCBGPU_E_ARG;
+    }
+    for (int k = 0; k < kNumShapes && k < max_shapes; k++) {
+        const PivotShape &h = kCandidateShapes[k];
+        const int32_t v[kShapeInts] = {h.win_early, h.rank_early, h.win_mid, h.rank_tail, h.win_tail, h.lmax,
+                                       h.stream_pct};
+        for (int i = 0; i < kShapeInts; i++) params[k * kShapeInts + i] = v[i];
+    }
+    if (n_shapes) *n_shapes = kNumShapes;
+    if (segment_shape)
+        for (int g = 0; g < kShapeSegs; g++) segment_shape[g] = s->forced_shape >= 0 ? s->forced_shape : s->seg_shape[g];
     return MCBGPU_OK;
 }
 

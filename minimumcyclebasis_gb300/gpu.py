@@ -224,6 +224,36 @@ class Solver:
                 "far_sparse_rows", "far_sparse_words", "far_sparse_tests"]
         return dict(zip(keys, out.tolist()))
 
+    SHAPE_SEGMENTS = 4
+    SHAPE_INTS = 7
+    SHAPE_FIELDS = ("win_early", "rank_early", "win_mid", "rank_tail", "win_tail", "lmax", "stream_pct")
+
+    def shapes(self) -> dict:
+        """The candidate search shapes and the shape each segment of a solve uses."""
+        n = C.c_int32()
+        params = np.zeros(16 * self.SHAPE_INTS, np.int32)
+        seg = np.zeros(self.SHAPE_SEGMENTS, np.int32)
+        check_gpu(self.lib.mcbgpu_solver_shapes(self._h, ptr(params), 16, C.byref(n), ptr(seg)), "mcbgpu_solver_shapes")
+        cands = [dict(zip(self.SHAPE_FIELDS, params[k * self.SHAPE_INTS:(k + 1) * self.SHAPE_INTS].tolist()))
+                 for k in range(min(n.value, 16))]
+        return {"candidates": cands, "segment_shape": seg.tolist()}
+
+    def tune(self, stream=0) -> dict:
+        """One complete blocked run with the candidate shapes taking turns group by group;
+        each segment of the solve keeps the fastest.  The run's results stay readable."""
+        info = self.shapes()
+        n = len(info["candidates"])
+        ms = np.zeros(self.SHAPE_SEGMENTS * n, np.float64)
+        chosen = np.zeros(self.SHAPE_SEGMENTS, np.int32)
+        check_gpu(self.lib.mcbgpu_solver_tune(self._h, ptr(ms), ptr(chosen), _stream(stream)), "mcbgpu_solver_tune")
+        info["ms_per_block"] = ms.reshape(self.SHAPE_SEGMENTS, n).round(4).tolist()
+        info["segment_shape"] = chosen.tolist()
+        return info
+
+    def set_shape(self, shape: int) -> None:
+        """Force one candidate shape for every block (-1: the per-segment choice)."""
+        check_gpu(self.lib.mcbgpu_solver_set_shape(self._h, int(shape)), "mcbgpu_solver_set_shape")
+
     @property
     def launches(self) -> int:
         return int(self.lib.mcbgpu_solver_launches(self._h))
