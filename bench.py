@@ -519,6 +519,36 @@ def run_gpu(args, world, rank, local, pg):
         solver.reset(sh)
         solver.run(args.max_iterations, sh)
 
+    def timed(s, step):
+        """args.steps solves by step() after args.warmup untimed ones: CUDA events on the
+        solver's stream, clocks sampled meanwhile, the results checked.  Returns (ms per
+        solve, launches in the timed region, clock summary)."""
+        for _ in range(args.warmup):
+            step()
+        r_sel, r_tot = s.results(stream=sh)
+        assert np.array_equal(r_sel, sel0) and r_tot == tot0, "warm-up solve differs from the first"
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+        l0 = s.launches
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            e_a = torch.cuda.Event(enable_timing=True)
+            e_b = torch.cuda.Event(enable_timing=True)
+            e_a.record(stream)
+            for _ in range(args.steps):
+                step()
+            e_b.record(stream)
+            torch.cuda.synchronize()
+        t_ms = e_a.elapsed_time(e_b) / args.steps
+        n_l = s.launches - l0
+        r_sel, r_tot = s.results(stream=sh)
+        assert np.array_equal(r_sel, sel0) and r_tot == tot0, "timed solves differ from the first"
+        if pg:
+            t_ms = max_over_ranks(t_ms, pg)
+            pg.barrier()
+        return t_ms, n_l, clk.summary()
+
     # search shapes: one tuning solve (the candidate shapes take turns group by group;
     # each quarter of the solve keeps its fastest), checked like any other solve
     shapes = None
@@ -526,30 +556,7 @@ def run_gpu(args, world, rank, local, pg):
         shapes = solver.tune(sh)
         sel, tot = solver.results(stream=sh)
         assert np.array_equal(sel, sel0) and tot == tot0, "the tuning solve differs from the first"
-    for i in range(args.warmup):
-        solve_once()
-    sel, tot = solver.results(stream=sh)
-    assert np.array_equal(sel, sel0) and tot == tot0, "warm-up solve differs from the first"
-    torch.cuda.synchronize()
-    if pg:
-        pg.barrier()
-    launches0 = solver.launches
-    with ClockSampler(local) as clocks:
-        torch.cuda.synchronize()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        for _ in range(args.steps):
-            solve_once()
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    launches = solver.launches - launches0
-    sel, tot = solver.results(stream=sh)
-    assert np.array_equal(sel, sel0) and tot == tot0, "timed solves differ from the first"
-    if pg:
-        ms = max_over_ranks(ms, pg)
-        pg.barrier()
+    ms, launches, clocks = timed(solver, solve_once)
 
     # the learned proposal: a network trained on traces of smaller graphs of the same
     # family (its own kernels), then the graph -> basis solve on the proposal's
@@ -572,30 +579,17 @@ def run_gpu(args, world, rank, local, pg):
             lshapes = lsolver.tune(sh)
             lsel, ltot = lsolver.results(stream=sh)
             assert np.array_equal(lsel, sel0) and ltot == tot0, "the learned form's tuning solve differs"
-        for _ in range(args.warmup):
+        def lsolve():
             lsolver.reset(sh)
             lsolver.run(-1, sh)
-        torch.cuda.synchronize()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        l0 = lsolver.launches
-        ev0.record(stream)
-        for _ in range(args.steps):
-            lsolver.reset(sh)
-            lsolver.run(-1, sh)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        lms = ev0.elapsed_time(ev1) / args.steps
-        llaunches = lsolver.launches - l0
-        lsel, ltot = lsolver.results(stream=sh)
-        assert np.array_equal(lsel, sel0) and ltot == tot0, "the learned form's solve differs"
+
+        lms, llaunches, lclocks = timed(lsolver, lsolve)
         learned["solve_s"] = lms / 1e3
         learned["solve_s_full_list"] = full_ms / 1e3
-        if pg:
-            lms = max_over_ranks(lms, pg)
         if lms < ms:  # the fastest form is the line's value; its lists feed the e2e below
             ms = lms
             launches = llaunches
+            clocks = lclocks
             shapes = lshapes
             solver.close()
             solver = lsolver
@@ -603,6 +597,25 @@ def run_gpu(args, world, rank, local, pg):
             learned["is_value"] = True
         else:
             lsolver.close()
+
+    # the same solve (reset + blocked run) as one CUDA graph, captured once and
+    # replayed; the faster launch form gives the value
+    launch_form = {"form": "streams", "stream_ms": ms}
+    use_graph = False
+    if args.cuda_graph:
+        from minimumcyclebasis_gb300._native import MCBError
+        try:
+            t_c = time.perf_counter()
+            solver.run_graph(args.max_iterations, sh)
+            torch.cuda.synchronize()
+            capture_s = time.perf_counter() - t_c
+            gms, glaunches, gclocks = timed(solver, lambda: solver.run_graph(args.max_iterations, sh))
+            launch_form.update({"graph_ms": gms, "capture_and_first_replay_s": capture_s})
+            if gms < ms:
+                ms, launches, clocks, use_graph = gms, glaunches, gclocks, True
+                launch_form["form"] = "graph"
+        except MCBError as exc:
+            launch_form["graph"] = "unavailable: %s" % exc
 
     if plain is not None:  # the per-iteration form against the fastest form
         plain["speedup"] = plain["value"] / (ms / 1e3)
@@ -636,7 +649,10 @@ def run_gpu(args, world, rank, local, pg):
 
         def e2e_once():
             solver.upload(sh, pw, po, pc)
-            solver.run(args.max_iterations, sh)
+            if use_graph:  # the graph reads the handle's buffers the upload refills
+                solver.run_graph(args.max_iterations, sh)
+            else:
+                solver.run(args.max_iterations, sh)
             check_gpu(lib.mcbgpu_solver_results(solver._h, C.c_void_p(psel.ctypes.data), p.N, C.byref(tot_c),
                                                 C.c_void_p(sh)), "mcbgpu_solver_results")
 
@@ -700,7 +716,7 @@ def run_gpu(args, world, rank, local, pg):
     if rank != 0:
         return None
     extra = {"total_weight": tot, "total_weight_pinned": pin, "solves_per_s_all_ranks": world * 1e3 / ms,
-             "search_shapes": shapes,
+             "search_shapes": shapes, "launch_form": launch_form,
              "cycle_nnz": int(off[-1]), "preparation": args.prep,
              "l2": ("every solve starts by writing the %.1f GB support matrix (reset to unit vectors), larger than "
                     "the 129 MB L2, which flushes it between steps; cycle lists %.2f GB"
@@ -708,7 +724,7 @@ def run_gpu(args, world, rank, local, pg):
     return {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic", "config": config_of(p, args, extra),
-            "clocks": clocks.summary(), "e2e": e2e,
+            "clocks": clocks, "e2e": e2e,
             "e2e_with_preparation": {"value": graph_to_basis, "unit": "s", "runs": 1,
                                      "preparation_s": {k: round(v, 3) for k, v in prep_times.items()},
                                      "tied_roots_searched_on_host": tied, "tree_kernel_shapes": tree_shapes,
@@ -922,6 +938,8 @@ def main():
     ap.add_argument("--prep", choices=["device", "host"], default="device",
                     help="candidate generation on the GPU (default) or on the host")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-iteration form's timing")
+    ap.add_argument("--no-cuda-graph", dest="cuda_graph", action="store_false",
+                    help="time the solve with stream launches only (no CUDA graph form)")
     ap.add_argument("--no-tune", dest="tune", action="store_false",
                     help="keep the default search shape (no tuning solve)")
     ap.add_argument("--no-learned", dest="learned", action="store_false",

@@ -171,6 +171,15 @@ int mcbgpu_update(mcbgpu_solver *s, int32_t e, void *stream);
  * enqueued on `stream` without host synchronisation.  Results via
  * mcbgpu_solver_results. */
 int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream);
+/* A complete solve (reset of S to the unit vectors, then the blocked run over
+ * iterations [0, min(max_iterations, N))) as one CUDA graph, launched on `stream`.
+ * The first call (and the first after a tuning run, a shape change or another
+ * max_iterations) captures the solve on a stream of the handle and instantiates it;
+ * later calls replay it.  The graph reads the handle's buffers, so a new upload
+ * (same sizes) is solved by the same graph.  Results via mcbgpu_solver_results, as
+ * after mcbgpu_solver_run.  Not with profiling on.  No counterpart in the reference
+ * (its loop is host code). */
+int mcbgpu_solver_run_graph(mcbgpu_solver *s, int64_t max_iterations, void *stream);
 /* Per-iteration form over all iterations, enqueued without host synchronisation
  * (select + update per iteration). */
 int mcbgpu_solver_run_plain(mcbgpu_solver *s, int64_t max_iterations, void *stream);

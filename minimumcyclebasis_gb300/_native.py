@@ -103,6 +103,7 @@ GPU_SYMBOLS = {
     "mcbgpu_cycle_vector": (C.c_int, [vp, i32, vp, vp]),
     "mcbgpu_update": (C.c_int, [vp, i32, vp]),
     "mcbgpu_solver_run": (C.c_int, [vp, i64, vp]),
+    "mcbgpu_solver_run_graph": (C.c_int, [vp, i64, vp]),
     "mcbgpu_solver_run_plain": (C.c_int, [vp, i64, vp]),
     "mcbgpu_solver_results": (C.c_int, [vp, vp, i64, C.POINTER(i64), vp]),
     "mcbgpu_solver_get_support": (C.c_int, [vp, i32, vp, vp]),

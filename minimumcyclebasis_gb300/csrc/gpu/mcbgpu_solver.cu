@@ -1052,26 +1052,30 @@ __device__ bool resolve_block(BlockState *bs, int rank, const int64_t *__restric
                     a1 = row;
             }
         }
+        // The loop carries only what the next iteration needs (row k + 1 after this
+        // iteration's XORs); the selections stay in the lane of their iteration and
+        // gcol is read off the final rows afterwards.
         uint64_t m0 = 1ull << lane, m1 = 1ull << (32 + lane);
         uint64_t used = 0;
+        int psel0 = 0, psel1 = 0;  // lane l: the pivots of iterations l and l + 32
+        bool fail = false;
         for (int k = 0; k < b; k++) {
             const uint64_t ak = __shfl_sync(0xffffffffu, k < 32 ? a0 : a1, k & 31);
             const uint64_t mk = __shfl_sync(0xffffffffu, k < 32 ? m0 : m1, k & 31);
             const uint64_t cand = ak & ~used;
-            if (!cand) {
-                if (lane == 0) s_fail = 1;
+            if (!cand) {  // warp-uniform
+                fail = true;
                 break;
             }
             const int p = __ffsll((long long)cand) - 1;
             used |= 1ull << p;
-            const bool h0 = (a0 >> p) & 1ull, h1 = (a1 >> p) & 1ull;
-            const unsigned g0 = __ballot_sync(0xffffffffu, lane < k && h0);
-            const unsigned g1 = __ballot_sync(0xffffffffu, 32 + lane < k && h1);
-            if (lane == 0) {
-                s_sel[k] = p;
-                s_kof[p] = k;
-                bs->gcol[ta.par][k] = (uint64_t)g0 | ((uint64_t)g1 << 32);
+            if (lane == (k & 31)) {
+                if (k < 32)
+                    psel0 = p;
+                else
+                    psel1 = p;
             }
+            const bool h0 = (a0 >> p) & 1ull, h1 = (a1 >> p) & 1ull;
             if (lane > k && h0) {
                 a0 ^= ak;
                 m0 ^= mk;
@@ -1079,6 +1083,37 @@ __device__ bool resolve_block(BlockState *bs, int rank, const int64_t *__restric
             if (32 + lane > k && h1) {
                 a1 ^= ak;
                 m1 ^= mk;
+            }
+        }
+        if (fail) {
+            if (lane == 0) s_fail = 1;
+        } else {
+            // rows i < k do not change after iteration i, so gcol[k] bit i = A[i][p_k] of
+            // the final rows: column c of A (lane c & 31 keeps columns c and c + 32),
+            // then iteration k (lane k & 31) fetches column p_k
+            uint64_t col0 = 0, col1 = 0;
+            for (int cc = 0; cc < 64; cc++) {
+                const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(a0 >> cc) & 1u);
+                const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(a1 >> cc) & 1u);
+                const uint64_t col = (uint64_t)lo | ((uint64_t)hi << 32);
+                if (lane == (cc & 31)) {
+                    if (cc < 32)
+                        col0 = col;
+                    else
+                        col1 = col;
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int k = lane + 32 * h;
+                const int p = h ? psel1 : psel0;
+                const uint64_t c0 = __shfl_sync(0xffffffffu, col0, p & 31);
+                const uint64_t c1 = __shfl_sync(0xffffffffu, col1, p & 31);
+                if (k < b) {
+                    s_sel[k] = p;
+                    s_kof[p] = k;
+                    bs->gcol[ta.par][k] = (p < 32 ? c0 : c1) & ((1ull << k) - 1ull);
+                }
             }
         }
         bs->mask[lane] = m0;
@@ -2438,6 +2473,12 @@ struct mcbgpu_solver {
     };
     std::vector<TuneRec> tune_recs;
     std::vector<cudaEvent_t> tpool;
+    // a complete solve (reset + blocked run) captured as one CUDA graph
+    cudaStream_t cap = nullptr;      // the stream the capture starts on
+    cudaGraphExec_t gexec = nullptr;
+    int64_t gexec_iters = -1;        // iterations the graph runs
+    long long gexec_launches = 0;    // kernel launches per replay
+    int gexec_list_end = 0;          // list set the replay leaves current
 };
 
 namespace {
@@ -2480,8 +2521,16 @@ struct Launch {
 
 namespace {
 
+void drop_graph(mcbgpu_solver *s) {
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+    s->gexec_iters = -1;
+}
+
 void free_solver(mcbgpu_solver *s) {
     if (!s) return;
+    drop_graph(s);
+    if (s->cap) cudaStreamDestroy(s->cap);
     for (cudaEvent_t e : s->tpool) cudaEventDestroy(e);
     cudaFree(s->d_weight);
     cudaFree(s->d_off);
@@ -3241,6 +3290,7 @@ int mcbgpu_solver_tune(mcbgpu_solver *s, double *ms_per_block, int32_t *chosen, 
     const int64_t nblocks = ((int64_t)s->N + 63) / 64;
     // a few groups of every shape in every segment, else the default shape stays
     const bool enough = nblocks >= 4LL * kGroup * kNumShapes * kShapeSegs;
+    drop_graph(s);  // the shapes change
     int rc = mcbgpu_solver_reset(s, stream);
     if (rc) return rc;
     s->tune_recs.clear();
@@ -3280,7 +3330,56 @@ int mcbgpu_solver_set_shape(mcbgpu_solver *s, int32_t shape) {
         set_error("mcbgpu_solver_set_shape: invalid argument");
         return MCBGPU_E_ARG;
     }
+    if (s->forced_shape != shape) drop_graph(s);
     s->forced_shape = shape;
+    return MCBGPU_OK;
+}
+
+int mcbgpu_solver_run_graph(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
+    if (!s) {
+        set_error("mcbgpu_solver_run_graph: NULL handle");
+        return MCBGPU_E_ARG;
+    }
+    if (!s->uploaded || s->profiling || s->tuning) {
+        set_error("mcbgpu_solver_run_graph: candidates not uploaded, or profiling on");
+        return MCBGPU_E_STATE;
+    }
+    const int64_t iters = (max_iterations >= 0 && max_iterations < s->N) ? max_iterations : s->N;
+    if (!s->gexec || s->gexec_iters != iters) {
+        drop_graph(s);
+        if (!s->cap) MCB_CUDA(cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking));
+        // the solver's streams must be idle: their work joins the capture through events
+        MCB_CUDA(cudaStreamSynchronize(s->st1));
+        MCB_CUDA(cudaStreamSynchronize(s->st2));
+        const long long l0 = s->launches;
+        MCB_CUDA(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
+        int rc = mcbgpu_solver_reset(s, s->cap);
+        if (rc == MCBGPU_OK) rc = mcbgpu_solver_run(s, iters, s->cap);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(s->cap, &g);
+        const long long per = s->launches - l0;
+        s->launches = l0;
+        if (rc != MCBGPU_OK || ec != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            (void)cudaGetLastError();
+            if (rc == MCBGPU_OK) return ::mcbgpu::cuda_fail(ec != cudaSuccess ? ec : cudaErrorStreamCaptureInvalidated,
+                                                            "cudaStreamEndCapture (solve graph)");
+            return rc;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&s->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            s->gexec = nullptr;
+            return ::mcbgpu::cuda_fail(ei, "cudaGraphInstantiate (solve graph)");
+        }
+        s->gexec_iters = iters;
+        s->gexec_launches = per;
+        s->gexec_list_end = s->list_cur;  // the host state a replay ends in (the capture ran the loop once)
+    }
+    MCB_CUDA(cudaGraphLaunch(s->gexec, (cudaStream_t)stream));
+    s->launches += s->gexec_launches;
+    s->list_cur = s->gexec_list_end;
+    s->iters_run = iters;
     return MCBGPU_OK;
 }
 

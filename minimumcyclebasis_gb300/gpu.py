@@ -169,6 +169,11 @@ class Solver:
     def run(self, max_iterations: int = -1, stream=0) -> None:
         check_gpu(self.lib.mcbgpu_solver_run(self._h, max_iterations, _stream(stream)), "mcbgpu_solver_run")
 
+    def run_graph(self, max_iterations: int = -1, stream=0) -> None:
+        """Reset + blocked run as one CUDA graph (captured on the first call, replayed after)."""
+        check_gpu(self.lib.mcbgpu_solver_run_graph(self._h, max_iterations, _stream(stream)),
+                  "mcbgpu_solver_run_graph")
+
     def run_plain(self, max_iterations: int = -1, stream=0) -> None:
         check_gpu(self.lib.mcbgpu_solver_run_plain(self._h, max_iterations, _stream(stream)),
                   "mcbgpu_solver_run_plain")
