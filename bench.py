@@ -663,7 +663,7 @@ def run_gpu(args, world, rank, local, pg):
             e2e_once()
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
         iters = p.N if args.max_iterations < 0 else min(args.max_iterations, p.N)
-        assert np.array_equal(psel[:iters], sel[:iters]) and tot_c.value == tot, "e2e results differ"
+        assert np.array_equal(psel[:iters], sel0[:iters]) and tot_c.value == tot0, "e2e results differ"
         e2e = {"value": e2e_s, "unit": "s", "steps": args.e2e_steps,
                "h2d_bytes_per_step": int(w.nbytes + off.nbytes + co.nbytes),
                "d2h_bytes_per_step": int(8 * p.N + 8 + 4)}
@@ -715,7 +715,7 @@ def run_gpu(args, world, rank, local, pg):
         cb = cpu_baseline(p, args, args.cpu_threads)
     if rank != 0:
         return None
-    extra = {"total_weight": tot, "total_weight_pinned": pin, "solves_per_s_all_ranks": world * 1e3 / ms,
+    extra = {"total_weight": tot0, "total_weight_pinned": pin, "solves_per_s_all_ranks": world * 1e3 / ms,
              "search_shapes": shapes, "launch_form": launch_form,
              "cycle_nnz": int(off[-1]), "preparation": args.prep,
              "l2": ("every solve starts by writing the %.1f GB support matrix (reset to unit vectors), larger than "
