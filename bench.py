@@ -456,7 +456,8 @@ def learned_form(args, g, sel0, tot0, sh):
     _, _, wsorted, _ = p.candidates()
     K_needed = int(np.max(sel0)) + 1  # the prefix the solve needs: up to its last selection
     table = proposal_table(r.logits, wsorted, p.N, net.pos_weight, K_needed)
-    learned = {"skip_rate": r.skip_rate, "diffs": 0, "fallback": r.fallback, "K": r.K, "K_kept": r.K_kept,
+    learned = {"skip_rate": r.skip_rate, "proposed_skip_rate": r.proposed_skip_rate, "diffs": 0,
+               "fallback": r.fallback, "K": r.K, "K_kept": r.K_kept,
                "K_needed": K_needed, "U": r.U, "nnz_kept": r.nnz_kept, "trees": r.trees,
                "trees_kept": r.trees_kept, "rule": args.proposal_rule,
                "rule_param": args.eps if args.proposal_rule == "tail" else args.margin,

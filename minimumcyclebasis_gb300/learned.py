@@ -206,8 +206,15 @@ class LearnedSolve:
     logits: np.ndarray | None = None
 
     @property
-    def skip_rate(self) -> float:
+    def proposed_skip_rate(self) -> float:
+        """Share of the candidates beyond the proposal's prefix."""
         return 1.0 - self.K_kept / self.K if self.K else 0.0
+
+    @property
+    def skip_rate(self) -> float:
+        """Share of the candidates the solve did without: none after a fallback to the
+        whole list (the prefix did not hold the basis)."""
+        return 0.0 if self.fallback else self.proposed_skip_rate
 
 
 def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.05, threads: int = 0, stream=0,

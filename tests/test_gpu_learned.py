@@ -123,6 +123,7 @@ def test_a_short_prefix_falls_back_to_the_whole_list():
     # of candidates, says so, and is run again on the whole list
     r = solve_with_proposal(g, None, threads=4, prefix=len(want_sel) // 2)
     assert r.fallback and r.K_kept < r.K
+    assert r.skip_rate == 0.0 and r.proposed_skip_rate > 0.4  # the whole list was solved after all
     assert np.array_equal(r.selected, want_sel) and r.total_weight == want_tot
     # a prefix that holds the basis needs no fallback
     last = int(want_sel.max()) + 1
