@@ -2141,13 +2141,18 @@ __global__ void __launch_bounds__(kApplyThreads) far_apply_kernel(uint64_t *S, i
                     if (w < Wb) acc[q] ^= F[w];
                 }
             }
+            uint64_t x[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {  // the row's four words loaded together, then stored
+                const int w = w0 + q * kApplyThreads;
+                x[q] = w < Wb ? Sj[w] ^ acc[q] : 0ull;
+            }
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const int w = w0 + q * kApplyThreads;
                 if (w < Wb) {
-                    const uint64_t x = Sj[w] ^ acc[q];
-                    Sj[w] = x;
-                    if (x) {
+                    Sj[w] = x[q];
+                    if (x[q]) {
                         const unsigned pos = atomicAdd(&s_cnt, 1u);
                         if (pos < (unsigned)kNzCap) L[pos] = (uint32_t)w;
                     }
@@ -2228,6 +2233,7 @@ __global__ void __launch_bounds__(256) near_d_kernel(const uint64_t *__restrict_
 // every near row: one read of the final rows in all, the near rows read and written
 // once, column-contiguous.
 constexpr int kNearCols = 32;
+constexpr int kNearBatch = 8;  // near rows per thread whose words are loaded together
 
 __global__ void __launch_bounds__(256) near_apply_kernel(uint64_t *S, long long row_begin, int nrows, int P, int b,
                                                         int e0, int Wb, const uint64_t *__restrict__ gcol,
@@ -2262,27 +2268,42 @@ __global__ void __launch_bounds__(256) near_apply_kernel(uint64_t *S, long long 
         if (threadIdx.x == 0) nb += 8ull * (unsigned long long)b * (unsigned long long)min(kNearCols, Wb - w0);
         cta_sync();
         if (w0 + w < Wb) {
-            for (int r = rs; r < nrows; r += rstep) {
-                uint64_t bt = sbeta[r];
-                if (!bt) continue;
-                // four independent accumulators: the shared-memory reads of a row's
-                // bits overlap instead of waiting one after the other
-                uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-                while (bt) {
-                    const int k0 = __ffsll((long long)bt) - 1;
-                    bt &= bt - 1;
-                    const int k1 = bt ? __ffsll((long long)bt) - 1 : 64;
-                    bt &= bt - 1;
-                    const int k2 = bt ? __ffsll((long long)bt) - 1 : 64;
-                    bt &= bt - 1;
-                    const int k3 = bt ? __ffsll((long long)bt) - 1 : 64;
-                    bt &= bt - 1;
-                    a0 ^= srow[k0][w];
-                    a1 ^= srow[k1][w];
-                    a2 ^= srow[k2][w];
-                    a3 ^= srow[k3][w];
+            // rows in batches of eight: their XORs from shared memory, then the eight
+            // row words loaded together (one memory round trip per batch, not per
+            // row), then stored
+            for (int r0 = rs; r0 < nrows; r0 += kNearBatch * rstep) {
+                uint64_t acc[kNearBatch], old[kNearBatch];
+                bool act[kNearBatch];
+#pragma unroll
+                for (int q = 0; q < kNearBatch; q++) {
+                    const int r = r0 + q * rstep;
+                    uint64_t bt = r < nrows ? sbeta[r] : 0ull;
+                    act[q] = bt != 0;
+                    // four independent accumulators: the shared-memory reads of a row's
+                    // bits overlap instead of waiting one after the other
+                    uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+                    while (bt) {
+                        const int k0 = __ffsll((long long)bt) - 1;
+                        bt &= bt - 1;
+                        const int k1 = bt ? __ffsll((long long)bt) - 1 : 64;
+                        bt &= bt - 1;
+                        const int k2 = bt ? __ffsll((long long)bt) - 1 : 64;
+                        bt &= bt - 1;
+                        const int k3 = bt ? __ffsll((long long)bt) - 1 : 64;
+                        bt &= bt - 1;
+                        a0 ^= srow[k0][w];
+                        a1 ^= srow[k1][w];
+                        a2 ^= srow[k2][w];
+                        a3 ^= srow[k3][w];
+                    }
+                    acc[q] = (a0 ^ a1) ^ (a2 ^ a3);
                 }
-                S[(size_t)(row_begin + r) * P + w0 + w] ^= (a0 ^ a1) ^ (a2 ^ a3);
+#pragma unroll
+                for (int q = 0; q < kNearBatch; q++)
+                    old[q] = act[q] ? S[(size_t)(row_begin + r0 + q * rstep) * P + w0 + w] : 0ull;
+#pragma unroll
+                for (int q = 0; q < kNearBatch; q++)
+                    if (act[q]) S[(size_t)(row_begin + r0 + q * rstep) * P + w0 + w] = old[q] ^ acc[q];
             }
         }
         cta_sync();  // srow is refilled for the next column chunk
