@@ -131,6 +131,16 @@ __device__ __forceinline__ uint64_t warp_xor64(uint64_t v) {
 // kernel of this library uses these instead of __syncthreads().
 __device__ __forceinline__ void cta_sync() { asm volatile("barrier.sync 0;" ::: "memory"); }
 
+// Programmatic dependent launch.  A kernel launched with the programmatic
+// stream-serialisation attribute may be scheduled while its predecessor in the stream
+// is still running: griddep_wait() blocks until that predecessor has completed and its
+// memory operations are visible (it returns at once for a kernel launched without the
+// attribute), and griddep_launch() lets the successor be scheduled once every CTA of
+// this kernel has issued it.  A kernel that waits first thing reads nothing of its
+// predecessor early, so only the launch latency overlaps.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // cta_sync that also returns whether `v` holds in every thread of the CTA.
 __device__ __forceinline__ bool cta_sync_and(bool v) {
     unsigned r;

@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "mcbgpu_internal.cuh"
@@ -90,6 +91,9 @@ constexpr int kGStride = kGroup == 3 ? 4 : kGroup;  // words per coordinate in t
 #endif
 #ifndef MCB_TAIL_RANK
 #define MCB_TAIL_RANK 60
+#endif
+#ifndef MCB_PDL
+#define MCB_PDL 1  // blocked run: critical-path kernels launched with programmatic stream serialisation
 #endif
 #ifndef MCB_MERGE_CHUNKED
 #define MCB_MERGE_CHUNKED 0  // merge echelon by chunks of 32 with a table rebuild per chunk (1) or serially (0)
@@ -401,6 +405,8 @@ __global__ void blk_transpose_kernel(const uint64_t *__restrict__ S, int P, int 
                                      uint64_t *__restrict__ T, BlockState *bs, long long ntiles,
                                      GridBar *gb, long long window_tiles, int stream_pct,
                                      uint64_t *__restrict__ Tg, int b1, int Wb1, int b2, int Wb2) {
+    griddep_wait();
+    griddep_launch();
     if (*(volatile const unsigned *)&bs->failed) {  // set by an earlier block's pivot kernel (same stream)
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             bs->pred_tiles = 0;  // the streaming pass and its correction then cover no tile
@@ -709,6 +715,8 @@ __global__ void __launch_bounds__(kTile, MCB_W_MINB) blk_w_kernel(long long K, c
                                                     uint64_t *Warr, unsigned *tile_epoch, unsigned long long *bytes,
                                                     const uint64_t *__restrict__ Tg, int bound1, int bound2,
                                                     uint64_t *Wl1, uint64_t *Wl2) {
+    griddep_wait();
+    griddep_launch();
     const unsigned epoch = bs->epoch;
     const long long ntiles = bs->pred_tiles;
     unsigned long long nb = (blockIdx.x == 0 && threadIdx.x == 0) ? 8ull * (unsigned long long)bound : 0ull;
@@ -785,6 +793,8 @@ __global__ void __launch_bounds__(kTile) blk_wfix_kernel(const int32_t *__restri
                                                          unsigned long long *bytes) {
     __shared__ uint64_t s_m[64], s_g[64], s_col[64];
     __shared__ uint64_t s_tab[kJ][8][256];
+    griddep_wait();
+    griddep_launch();
     const unsigned epoch = bs->epoch;
     const long long ntiles = bs->pair_tiles;
     const int tid = threadIdx.x;
@@ -1293,6 +1303,8 @@ __global__ void __launch_bounds__(kPivotThreads, MCB_PIVOT_MINB) blk_pivot_kerne
     __shared__ int s_nnew;
     __shared__ unsigned long long sr_rank[kLmax], sr_w[kLmax];
 
+    griddep_wait();
+    griddep_launch();
     // an earlier block ran out of candidates (flag written by an earlier launch, so
     // every CTA reads the same value and none waits at a grid barrier)
     if (*(volatile const unsigned *)&bs->failed) return;
@@ -2190,6 +2202,8 @@ __global__ void __launch_bounds__(256) near_d_kernel(const uint64_t *__restrict_
                                                     int P, const unsigned *__restrict__ pairs,
                                                     const unsigned *__restrict__ word_end,
                                                     unsigned long long *Dbuf, unsigned long long *bytes) {
+    griddep_wait();
+    griddep_launch();
     const int lane = threadIdx.x & 31;
     const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -2243,6 +2257,8 @@ __global__ void __launch_bounds__(256) near_apply_kernel(uint64_t *S, long long 
     __shared__ uint64_t sg[64];
     __shared__ uint64_t sbeta[kNearMaxRows];
     __shared__ uint64_t srow[65][kNearCols];  // row 64: zeros, the padding of a short batch of bits
+    griddep_wait();
+    griddep_launch();
     if (threadIdx.x < 64) sg[threadIdx.x] = (int)threadIdx.x < b ? gcol[threadIdx.x] : 0;
     cta_sync();
     unsigned long long nb = 0;
@@ -2487,6 +2503,7 @@ struct mcbgpu_solver {
     // the critical stream) by segment and shape
     int seg_shape[kShapeSegs] = {};
     int forced_shape = -1;
+    bool pdl = MCB_PDL != 0;  // critical-path kernels with programmatic dependent launch
     bool tuning = false;
     struct TuneRec {
         int seg, shape, blocks;  // a group of `blocks` blocks
@@ -2503,6 +2520,45 @@ struct mcbgpu_solver {
 };
 
 namespace {
+
+// A launch on the critical stream of the blocked run: with programmatic stream
+// serialisation when the handle uses it (the kernel is scheduled while its
+// predecessor finishes and waits for it in griddep_wait), cooperative when asked.
+template <typename... Exp, typename... Act>
+cudaError_t launch_k(bool pdl, void (*kern)(Exp...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     Act &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    if (pdl) {
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+    }
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Act>(args)...);
+}
+
+cudaError_t launch_coop(bool pdl, const void *kern, dim3 grid, dim3 block, void **args, size_t smem,
+                        cudaStream_t st) {
+    if (!pdl) return cudaLaunchCooperativeKernel(kern, grid, block, args, smem, st);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 2;
+    return cudaLaunchKernelExC(&cfg, kern, args);
+}
 
 cudaEvent_t pool_event(mcbgpu_solver *s) {
     if (s->pool_next == s->pool.size()) {
@@ -2950,6 +3006,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
     cudaStream_t st = s->st1;  // the critical path; joined back into the caller's stream at the end
     const int64_t iters = (max_iterations >= 0 && max_iterations < s->N) ? max_iterations : s->N;
     const int64_t nblocks = (iters + 63) / 64;
+    const bool pdl = s->pdl;
     size_t tnext = 0;             // tuning events used
     cudaEvent_t tev_a = nullptr;  // start of the group being timed
     const int sms = s->sm_count > 0 ? s->sm_count : 148;
@@ -3014,32 +3071,38 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
         }
         {
             Launch L(s, KC_TRANSPOSE, st);
-            blk_transpose_kernel<<<(std::max(Wb, std::max(Wb1, Wb2)) + 7) / 8, 256, 0, st>>>(
-                s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles, s->d_gbar,
-                (long long)s->pivot_grid * sh.win_mid, sh.stream_pct, s->d_Tg, bl[0], Wb1, bl[1], Wb2);
+            MCB_CUDA(launch_k(pdl, blk_transpose_kernel, dim3((std::max(Wb, std::max(Wb1, Wb2)) + 7) / 8), dim3(256), 0,
+                              st, (const uint64_t *)s->d_S, s->P, (int)e0, b, Wb, s->d_T, s->d_bs, ntiles, s->d_gbar,
+                              (long long)s->pivot_grid * sh.win_mid, sh.stream_pct, s->d_Tg, bl[0], Wb1, bl[1],
+                              Wb2));
         }
         if (ntiles > 0 && pos > 0) {
             Launch L(s, KC_WFIX, st);
             if (pos == 1)
-                blk_wfix_kernel<1><<<sms, kTile, 0, st>>>(s->d_tile_minc, bound, s->d_bs, s->d_beta, s->d_masks, b,
-                                                          Wpos[0], Wpos[1], Wpos[1], s->d_tile_epoch, L.bytes());
+                MCB_CUDA(launch_k(pdl, blk_wfix_kernel<1>, dim3(sms), dim3(kTile), 0, st, (const int32_t *)s->d_tile_minc,
+                                  bound, s->d_bs, (const uint64_t *)s->d_beta, s->d_masks, b, Wpos[0], Wpos[1], Wpos[1],
+                                  s->d_tile_epoch, L.bytes()));
             else
-                blk_wfix_kernel<2><<<sms, kTile, 0, st>>>(s->d_tile_minc, bound, s->d_bs, s->d_beta, s->d_masks, b,
-                                                          Wpos[0], Wpos[1], Wpos[2], s->d_tile_epoch, L.bytes());
+                MCB_CUDA(launch_k(pdl, blk_wfix_kernel<2>, dim3(sms), dim3(kTile), 0, st, (const int32_t *)s->d_tile_minc,
+                                  bound, s->d_bs, (const uint64_t *)s->d_beta, s->d_masks, b, Wpos[0], Wpos[1], Wpos[2],
+                                  s->d_tile_epoch, L.bytes()));
         } else if (ntiles > 0) {
             Launch L(s, KC_WSTREAM, st);
+            const int64_t *woff = s->d_off;
+            const int32_t *wco = s->d_coords, *whd = s->d_head, *wtm = s->d_tile_minc;
+            const uint64_t *wT = s->d_T, *wTg = s->d_Tg;
+            const BlockState *wbs = s->d_bs;
+            uint64_t *nul = nullptr;
             if (nl == 2)
-                blk_w_kernel<3><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_head, s->d_tile_minc, s->d_T, bound,
-                                                           s->d_bs, Wpos[0], s->d_tile_epoch, L.bytes(), s->d_Tg, bd1,
-                                                           bd2, Wpos[1], Wpos[2]);
+                MCB_CUDA(launch_k(pdl, blk_w_kernel<3>, dim3(sms * 2), dim3(kTile), 0, st, s->K, woff, wco, whd, wtm, wT,
+                                  bound, wbs, Wpos[0], s->d_tile_epoch, L.bytes(), wTg, bd1, bd2, Wpos[1], Wpos[2]));
             else if (nl == 1)
-                blk_w_kernel<2><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_head, s->d_tile_minc, s->d_T, bound,
-                                                           s->d_bs, Wpos[0], s->d_tile_epoch, L.bytes(), s->d_Tg, bd1,
-                                                           bd1, Wpos[1], nullptr);
+                MCB_CUDA(launch_k(pdl, blk_w_kernel<2>, dim3(sms * 2), dim3(kTile), 0, st, s->K, woff, wco, whd, wtm, wT,
+                                  bound, wbs, Wpos[0], s->d_tile_epoch, L.bytes(), wTg, bd1, bd1, Wpos[1], nul));
             else
-                blk_w_kernel<1><<<sms * 2, kTile, 0, st>>>(s->K, s->d_off, s->d_coords, s->d_head, s->d_tile_minc, s->d_T, bound,
-                                                           s->d_bs, Wpos[0], s->d_tile_epoch, L.bytes(), nullptr, 0, 0,
-                                                           nullptr, nullptr);
+                MCB_CUDA(launch_k(pdl, blk_w_kernel<1>, dim3(sms * 2), dim3(kTile), 0, st, s->K, woff, wco, whd, wtm, wT,
+                                  bound, wbs, Wpos[0], s->d_tile_epoch, L.bytes(), (const uint64_t *)nullptr, 0, 0, nul,
+                                  nul));
         }
         // this block's tail rewrites the parity buffers the far update two blocks back reads
         if (par_far[par]) MCB_CUDA(cudaStreamWaitEvent(st, s->ev_par[par], 0));
@@ -3075,8 +3138,8 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
             PivotShape shv = sh;
             void *args[] = {&K, &off, &co, &hd, &tm, &T, (void *)&bound, &bs, &Wa, &te, &rp, &gb, &stt, &nb, &dg, &db, &ta,
                             &shv};
-            MCB_CUDA(cudaLaunchCooperativeKernel((const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kPivotThreads),
-                                                 args, pivot_smem_bytes(s->pivot_grid), st));
+            MCB_CUDA(launch_coop(pdl, (const void *)blk_pivot_kernel, dim3(s->pivot_grid), dim3(kPivotThreads), args,
+                                 pivot_smem_bytes(s->pivot_grid), st));
         }
         if (s->tuning && (pos == kGroup - 1 || e0 + b >= iters)) {  // the group's last block
             cudaEvent_t tev_b = s->tpool[tnext++];
@@ -3133,9 +3196,10 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 unsigned long long *Dn = s->d_nearD + (size_t)par * kNearMaxRows;
                 unsigned long long *Dn_next = s->d_nearD + (size_t)(par ^ 1) * kNearMaxRows;
                 const int agrid = (int)std::min<long long>((Wb + kNearCols - 1) / kNearCols, (long long)sms * 2);
-                near_d_kernel<<<sms * 4, 256, 0, st>>>(s->d_S, e0 + b, nrows, s->P, pairs, wend, Dn, L.bytes());
-                near_apply_kernel<<<agrid, 256, 0, st>>>(s->d_S, e0 + b, nrows, s->P, b, (int)e0, Wb, gcol, Dn,
-                                                         Dn_next, bo, L.bytes());
+                MCB_CUDA(launch_k(pdl, near_d_kernel, dim3(sms * 4), dim3(256), 0, st, (const uint64_t *)s->d_S,
+                                  (long long)(e0 + b), nrows, s->P, pairs, wend, Dn, L.bytes()));
+                MCB_CUDA(launch_k(pdl, near_apply_kernel, dim3(agrid), dim3(256), 0, st, s->d_S, (long long)(e0 + b), nrows,
+                                  s->P, b, (int)e0, Wb, gcol, (const unsigned long long *)Dn, Dn_next, bo, L.bytes()));
             }
             if (near_end < far_end) {
                 const int slot = ring;
