@@ -877,9 +877,9 @@ def run_batch(args, world, rank, local, pg):
     nnz = int(bs.offsets[-1])
     scanned = int(prof[:, 6].sum())
     K = int(bs.weight.shape[0])
-    # the scan reads, per scanned candidate, its two offsets and its coordinate list
-    # (lists are walked to the block's bound; the full list is the upper bound used here)
-    scan_bytes = scanned * (8 + 4.0 * nnz / max(K, 1))
+    # the scan reads, per scanned candidate, its two offsets and its coordinate list up
+    # to the block's bound: the bytes the kernel counted as it walked them
+    scan_bytes = float(prof[:, 12].sum())
     peak, peak_kind = measured_peaks()
     achieved = scan_bytes / (ms / 1e3) / 1e9
     return {"metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -906,8 +906,8 @@ def run_batch(args, world, rank, local, pg):
             "roofline": {"kernel": "batch_solve", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                          "bytes_per_launch": scan_bytes, "launch_ms": ms,
-                         "note": "scan bytes (offsets + lists of the scanned candidates) per batched solve; the "
-                                 "kernel is latency-bound on the per-problem critical path"},
+                         "note": "scan bytes (offsets + coordinates the list walks read, counted by the kernel) "
+                                 "per batched solve; the kernel is latency-bound on the per-problem critical path"},
             "cpu_baseline": cb}
 
 

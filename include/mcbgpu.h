@@ -285,13 +285,13 @@ int mcbgpu_batch_results(mcbgpu_batch *b, int64_t *selected, int64_t *total_weig
 /* S_j of problem `problem` after the run (ceil(N/64) words, synchronous). */
 int mcbgpu_batch_get_support(mcbgpu_batch *b, int32_t problem, int32_t j, uint64_t *words, void *stream);
 /* Optional per-problem profile of the following runs: set_profiling(1) makes the
- * kernel record, for problem i, out[12i..12i+11] = wall ns from its start to its
+ * kernel record, for problem i, out[13i..13i+12] = wall ns from its start to its
  * end, SM clock cycles of its CTA in the transposes, the pivot scans, the resolves,
  * the final rows + pairs and the updates of later rows, the candidates scanned, the
  * SM it ran on, the cycles of the scans' list walks (part of the pivot scans), the
- * pivot rounds (CTA-wide searches for the next pivot), and the cycles warp 0 spent
- * in the update forming D and beta, and writing rows.  profile synchronises the
- * device. */
+ * pivot rounds (CTA-wide searches for the next pivot), the cycles warp 0 spent in
+ * the update forming D and beta, and writing rows, and the bytes the scans' list
+ * walks read (offsets and coordinates).  profile synchronises the device. */
 int mcbgpu_batch_set_profiling(mcbgpu_batch *b, int enable);
 int mcbgpu_batch_profile(mcbgpu_batch *b, int64_t *out);
 int64_t mcbgpu_batch_launches(const mcbgpu_batch *b);

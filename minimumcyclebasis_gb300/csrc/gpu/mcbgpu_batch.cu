@@ -57,6 +57,8 @@ constexpr size_t kSmemBudget = 220 * 1024;  // dynamic shared memory per CTA at 
 constexpr int kClasses = 3;
 constexpr int kClassMaxN[kClasses] = {1024, 4096, kBatchMaxN};
 
+constexpr int kBProf = 13;  // profile words per problem (mcbgpu_batch_profile)
+
 struct BatchGraph {
     long long cand;  // first candidate (index into weight / offsets)
     long long K;     // candidates
@@ -69,11 +71,13 @@ __device__ __forceinline__ int ffs64(uint64_t x) { return __ffsll((long long)x) 
 
 // W of the kBQ consecutive candidates r0 .. r0 + kBQ - 1 (0 past K) from the block's
 // T in shared memory.  The lists are walked in lockstep, kBChunk coordinates of each
-// per step, so kBQ x kBChunk independent loads are in flight per thread.
+// per step, so kBQ x kBChunk independent loads are in flight per thread.  `walked`
+// counts the offsets and coordinates read (for the profile's byte count).
 template <int kBQ>
 __device__ __forceinline__ void w_smem_q(long long r0, long long K, long long cand,
                                          const int64_t *__restrict__ off, const int32_t *__restrict__ coords,
-                                         const uint64_t *T, int bound, uint64_t (&W)[kBQ]) {
+                                         const uint64_t *T, int bound, uint64_t (&W)[kBQ],
+                                         unsigned long long &walked) {
     long long ia[kBQ], ea[kBQ];
 #pragma unroll
     for (int q = 0; q < kBQ; q++) {
@@ -82,6 +86,7 @@ __device__ __forceinline__ void w_smem_q(long long r0, long long K, long long ca
         if (r0 + q < K) {
             ia[q] = __ldg(off + cand + r0 + q);
             ea[q] = __ldg(off + cand + r0 + q + 1);
+            walked += 16;
         }
     }
     for (;;) {
@@ -96,6 +101,7 @@ __device__ __forceinline__ void w_smem_q(long long r0, long long K, long long ca
             for (int t = 0; t < kBChunk; t++) cv[q][t] = ia[q] + t < ea[q] ? __ldg(coords + ia[q] + t) : 0x7fffffff;
 #pragma unroll
         for (int q = 0; q < kBQ; q++) {
+            walked += 4ull * (unsigned long long)min((long long)kBChunk, ea[q] - ia[q] > 0 ? ea[q] - ia[q] : 0);
 #pragma unroll
             for (int t = 0; t < kBChunk; t++)
                 if (cv[q][t] < bound) W[q] ^= T[cv[q][t]];
@@ -135,6 +141,7 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
     // scanned; cycles of the scan's list walks; pivot rounds; cycles of warp 0 in the
     // update's D + beta and in its row writes
     __shared__ long long pc[10];
+    __shared__ unsigned long long s_walked;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned full = 0xffffffffu;
@@ -176,6 +183,8 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
         }
         long long tot = 0;
         unsigned long long t_start = 0;
+        unsigned long long walked = 0;  // this thread's list-walk bytes (offsets + coordinates)
+        if (prof && tid == 0) s_walked = 0;
         if (prof && tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
         if (tid == 0) {
             sFail = 0;
@@ -237,7 +246,7 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
                 const long long cw = prof ? clock64() : 0;
                 bool first_round = true;
                 uint64_t W[kBQ], res[kBQ];
-                w_smem_q<kBQ>(base + (long long)tid * kBQ, K, cand, off, coords, T, bound, W);
+                w_smem_q<kBQ>(base + (long long)tid * kBQ, K, cand, off, coords, T, bound, W, walked);
 #pragma unroll
                 for (int q = 0; q < kBQ; q++) {
                     res[q] = W[q];
@@ -483,12 +492,16 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
             // tot lives in lane 0 of warp 0
             if (lane == 0) total[gx] = sFail ? -1 : tot;
         }
+        if (prof) {
+            atomicAdd(&s_walked, walked);
+            cta_sync();
+        }
         if (prof && tid == 0) {
             unsigned long long t_end;
             asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
             unsigned smid;
             asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-            long long *o = prof + (size_t)gx * 12;
+            long long *o = prof + (size_t)gx * kBProf;
             o[0] = (long long)(t_end - t_start);
             for (int q = 0; q < 6; q++) o[1 + q] = pc[q];
             o[7] = smid;
@@ -496,6 +509,7 @@ __global__ void __launch_bounds__(kBThreads, kMinBlocks) batch_solve_kernel(
             o[9] = pc[7];
             o[10] = pc[8];
             o[11] = pc[9];
+            o[12] = (long long)s_walked;
         }
     }
 }
@@ -866,8 +880,8 @@ int mcbgpu_batch_set_profiling(mcbgpu_batch *b, int enable) {
         return MCBGPU_E_ARG;
     }
     if (enable && !b->d_prof) {
-        MCB_CUDA(cudaMalloc((void **)&b->d_prof, sizeof(long long) * 12 * (size_t)std::max(b->count, 1)));
-        MCB_CUDA(cudaMemset(b->d_prof, 0, sizeof(long long) * 12 * (size_t)std::max(b->count, 1)));
+        MCB_CUDA(cudaMalloc((void **)&b->d_prof, sizeof(long long) * kBProf * (size_t)std::max(b->count, 1)));
+        MCB_CUDA(cudaMemset(b->d_prof, 0, sizeof(long long) * kBProf * (size_t)std::max(b->count, 1)));
     } else if (!enable && b->d_prof) {
         MCB_CUDA(cudaFree(b->d_prof));
         b->d_prof = nullptr;
@@ -881,7 +895,7 @@ int mcbgpu_batch_profile(mcbgpu_batch *b, int64_t *out) {
         return MCBGPU_E_ARG;
     }
     MCB_CUDA(cudaDeviceSynchronize());
-    MCB_CUDA(cudaMemcpy(out, b->d_prof, sizeof(long long) * 12 * (size_t)b->count, cudaMemcpyDeviceToHost));
+    MCB_CUDA(cudaMemcpy(out, b->d_prof, sizeof(long long) * kBProf * (size_t)b->count, cudaMemcpyDeviceToHost));
     return MCBGPU_OK;
 }
 

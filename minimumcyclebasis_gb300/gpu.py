@@ -371,8 +371,9 @@ class BatchSolver:
 
     def profile(self) -> np.ndarray:
         """Per problem: [ns, cycles in T, scan, resolve, final rows, update, candidates scanned, SM,
-        cycles of the scan's list walks, pivot rounds, warp 0's update cycles in D + beta, in row writes]."""
-        out = np.zeros((max(self.count, 1), 12), np.int64)
+        cycles of the scan's list walks, pivot rounds, warp 0's update cycles in D + beta, in row writes,
+        bytes the list walks read]."""
+        out = np.zeros((max(self.count, 1), 13), np.int64)
         check_gpu(self.lib.mcbgpu_batch_profile(self._h, ptr(out)), "mcbgpu_batch_profile")
         return out[: self.count]
 

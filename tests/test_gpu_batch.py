@@ -139,9 +139,15 @@ def test_per_problem_profile():
     b.set_profiling(True)
     b.run()
     pr = b.profile()
-    assert pr.shape == (len(probs), 12)
+    assert pr.shape == (len(probs), 13)
     assert (pr[:, 0] > 0).all() and (pr[:, 2] > 0).all()  # wall time, scan cycles
     assert (pr[:, 6] > 0).all()  # candidates scanned
+    # bytes walked: at least the offsets of every candidate of the first scan round of
+    # every block, at most every list read in full by every block
+    for p, walked in zip(probs, pr[:, 12]):
+        off = p.cycle_lists()[0]
+        blocks = (p.N + 63) // 64
+        assert 16 * min(p.K, 64) <= walked <= blocks * (16 * p.K + 4 * int(off[-1]) + 4 * 8 * p.K)
     assert (pr[:, 9] >= np.array([(p.N + 63) // 64 for p in probs])).all()  # at least one pivot round per block
     b.set_profiling(False)
     sels, tots = b.results()
