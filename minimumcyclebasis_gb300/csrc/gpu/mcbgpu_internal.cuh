@@ -141,6 +141,36 @@ __device__ __forceinline__ void cta_sync() { asm volatile("barrier.sync 0;" ::: 
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// 64 x 64 bit transpose across a warp: lane l holds rows l (r0) and l + 32 (r1), bit j
+// of a row being column j; afterwards r0 = column l and r1 = column l + 32 (bit i =
+// row i).  The 32 x 32 blocks off the diagonal are swapped in each lane, then both
+// halves of the words are transposed as two 32 x 32 matrices at once by the
+// recursive block swap (blocks of 16, 8, 4, 2, 1: rows r and r + j exchange with one
+// shuffle), five shuffles per word instead of 64 ballots.
+__device__ __forceinline__ void warp_transpose64(uint64_t &r0, uint64_t &r1) {
+    const int lane = threadIdx.x & 31;
+    uint64_t u0 = (r0 & 0x00000000FFFFFFFFull) | (r1 << 32);
+    uint64_t u1 = (r0 >> 32) | (r1 & 0xFFFFFFFF00000000ull);
+    const uint64_t masks[5] = {0x0000FFFF0000FFFFull, 0x00FF00FF00FF00FFull, 0x0F0F0F0F0F0F0F0Full,
+                               0x3333333333333333ull, 0x5555555555555555ull};
+#pragma unroll
+    for (int s = 0; s < 5; s++) {
+        const int j = 16 >> s;
+        const uint64_t m = masks[s];
+        const uint64_t p0 = __shfl_xor_sync(0xffffffffu, u0, j);
+        const uint64_t p1 = __shfl_xor_sync(0xffffffffu, u1, j);
+        if ((lane & j) == 0) {
+            u0 ^= (((u0 >> j) ^ p0) & m) << j;
+            u1 ^= (((u1 >> j) ^ p1) & m) << j;
+        } else {
+            u0 ^= ((p0 >> j) ^ u0) & m;
+            u1 ^= ((p1 >> j) ^ u1) & m;
+        }
+    }
+    r0 = u0;
+    r1 = u1;
+}
+
 // cta_sync that also returns whether `v` holds in every thread of the CTA.
 __device__ __forceinline__ bool cta_sync_and(bool v) {
     unsigned r;

@@ -377,19 +377,9 @@ __device__ __forceinline__ void transpose_rows(const uint64_t *__restrict__ S, i
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < Wb; w += warps) {
-        uint64_t lo = lane < b ? S[(size_t)(r0 + lane) * P + w] : 0ull;
-        uint64_t hi = (32 + lane) < b ? S[(size_t)(r0 + 32 + lane) * P + w] : 0ull;
-        uint64_t a = 0, c = 0;
-        for (int i = 0; i < 64; i++) {
-            unsigned blo = __ballot_sync(0xffffffffu, (unsigned)(lo >> i) & 1u);
-            unsigned bhi = __ballot_sync(0xffffffffu, (unsigned)(hi >> i) & 1u);
-            uint64_t v = (uint64_t)blo | ((uint64_t)bhi << 32);
-            if (i < 32) {
-                if (lane == i) a = v;
-            } else {
-                if (lane == i - 32) c = v;
-            }
-        }
+        uint64_t a = lane < b ? S[(size_t)(r0 + lane) * P + w] : 0ull;
+        uint64_t c = (32 + lane) < b ? S[(size_t)(r0 + 32 + lane) * P + w] : 0ull;
+        warp_transpose64(a, c);  // a: column 64w + lane, c: column 64w + 32 + lane
         if (T) {
             T[(size_t)w * 64 + lane] = a;
             T[(size_t)w * 64 + 32 + lane] = c;
@@ -814,14 +804,11 @@ __global__ void __launch_bounds__(kTile) blk_wfix_kernel(const int32_t *__restri
             s_g[tid] = g;
         }
         cta_sync();
-        if (tid < 64) {  // col_t bit r = bit t of gamma_r: a 64x64 bit transpose by ballots (warps 0, 1)
-            const int lane = tid & 31, half = tid >> 5;
-            const uint64_t g0 = s_g[lane], g1 = s_g[lane + 32];
-            for (int t = half * 32; t < half * 32 + 32; t++) {
-                const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(g0 >> t) & 1u);
-                const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(g1 >> t) & 1u);
-                if (lane == (t & 31)) s_col[t] = (uint64_t)lo | ((uint64_t)hi << 32);
-            }
+        if (tid < 32) {  // col_t bit r = bit t of gamma_r: a 64x64 bit transpose (warp 0)
+            uint64_t g0 = s_g[tid], g1 = s_g[tid + 32];
+            warp_transpose64(g0, g1);
+            s_col[tid] = g0;
+            s_col[tid + 32] = g1;
         }
         if (tid < 8) s_tab[i][tid][0] = 0;
         cta_sync();
@@ -1049,19 +1036,8 @@ __device__ bool resolve_block(BlockState *bs, int rank, const int64_t *__restric
         // p_k = the first unused p with A[k][p] = 1; every later row j with
         // A[j][p_k] = 1 takes row k (m_j ^= m_k, and A[j] ^= A[k] with it).  Rows
         // i < k are final, so gcol[k] bit i = A[i][p_k].
-        const uint64_t w0 = s_w[lane], w1 = s_w[32 + lane];
-        uint64_t a0 = 0, a1 = 0;
-        for (int j = 0; j < 64; j++) {
-            const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(w0 >> j) & 1u);
-            const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(w1 >> j) & 1u);
-            const uint64_t row = (uint64_t)lo | ((uint64_t)hi << 32);
-            if (lane == (j & 31)) {
-                if (j < 32)
-                    a0 = row;
-                else
-                    a1 = row;
-            }
-        }
+        uint64_t a0 = s_w[lane], a1 = s_w[32 + lane];
+        warp_transpose64(a0, a1);  // row j of A = bit j of every W
         // The loop carries only what the next iteration needs (row k + 1 after this
         // iteration's XORs); the selections stay in the lane of their iteration and
         // gcol is read off the final rows afterwards.
@@ -1101,18 +1077,8 @@ __device__ bool resolve_block(BlockState *bs, int rank, const int64_t *__restric
             // rows i < k do not change after iteration i, so gcol[k] bit i = A[i][p_k] of
             // the final rows: column c of A (lane c & 31 keeps columns c and c + 32),
             // then iteration k (lane k & 31) fetches column p_k
-            uint64_t col0 = 0, col1 = 0;
-            for (int cc = 0; cc < 64; cc++) {
-                const unsigned lo = __ballot_sync(0xffffffffu, (unsigned)(a0 >> cc) & 1u);
-                const unsigned hi = __ballot_sync(0xffffffffu, (unsigned)(a1 >> cc) & 1u);
-                const uint64_t col = (uint64_t)lo | ((uint64_t)hi << 32);
-                if (lane == (cc & 31)) {
-                    if (cc < 32)
-                        col0 = col;
-                    else
-                        col1 = col;
-                }
-            }
+            uint64_t col0 = a0, col1 = a1;
+            warp_transpose64(col0, col1);
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 const int k = lane + 32 * h;
