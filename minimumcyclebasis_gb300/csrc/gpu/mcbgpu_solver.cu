@@ -3149,7 +3149,9 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 far_scatter_kernel<<<sms * 2, 256, 0, s->st2>>>(pairs, wend, s->P, near_end, far_end, s->d_unit,
                                                                  s->d_Dfar, s->d_touch, s->d_fcnt + 4 * lout + 2,
                                                                  L.bytes());
-                far_rows_kernel<<<grid_for(far_end - near_end), kUpdThreads, 0, s->st2>>>(
+                // grid-stride over the listed rows: two CTAs per SM cover ~78k sparse rows per
+                // pass (a block lists ~12k at the 1M-vertex graph); more CTAs would mostly exit
+                far_rows_kernel<<<std::min(grid_for(far_end - near_end), sms * 2), kUpdThreads, 0, s->st2>>>(
                     s->d_S, near_end, s->P, b, gcol, pairs, wend, fl, s->d_Dfar, s->d_unit, L.bytes(), s->d_diag);
                 far_apply_kernel<<<sms * 2, kApplyThreads, 0, s->st2>>>(s->d_S, s->P, (int)e0, Wb, fl, L.bytes());
                 s->list_cur = lout;
@@ -3162,7 +3164,7 @@ int mcbgpu_solver_run(mcbgpu_solver *s, int64_t max_iterations, void *stream) {
                 unsigned long long *Dn = s->d_nearD + (size_t)par * kNearMaxRows;
                 unsigned long long *Dn_next = s->d_nearD + (size_t)(par ^ 1) * kNearMaxRows;
                 const int agrid = (int)std::min<long long>((Wb + kNearCols - 1) / kNearCols, (long long)sms * 2);
-                MCB_CUDA(launch_k(pdl, near_d_kernel, dim3(sms * 4), dim3(256), 0, st, (const uint64_t *)s->d_S,
+                MCB_CUDA(launch_k(pdl, near_d_kernel, dim3(sms), dim3(256), 0, st, (const uint64_t *)s->d_S,
                                   (long long)(e0 + b), nrows, s->P, pairs, wend, Dn, L.bytes()));
                 MCB_CUDA(launch_k(pdl, near_apply_kernel, dim3(agrid), dim3(256), 0, st, s->d_S, (long long)(e0 + b), nrows,
                                   s->P, b, (int)e0, Wb, gcol, (const unsigned long long *)Dn, Dn_next, bo, L.bytes()));
