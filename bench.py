@@ -423,29 +423,37 @@ def learned_form(args, g, sel0, tot0, sh):
     seconds of the learned form)."""
     import numpy as np
 
-    from minimumcyclebasis_gb300.learned import ProposalNet, solve_with_proposal, traces, train
+    from minimumcyclebasis_gb300.learned import (ProposalNet, calibrate_margin, needed_margin, solve_with_proposal,
+                                                 traces, train)
     small = argparse.Namespace(**vars(args))
     small.n = args.train_n
     t0 = time.perf_counter()
-    xs, ys, ks = [], [], []
+    xs, ys, ks, rs = [], [], [], []
     for i in range(args.train_graphs):
         small.seed = args.seed + 1000 + i
         x, y, res = traces(make_graph(small))
         xs.append(x)
         ys.append(y)
         ks.append(res.K)
+        rs.append(res)
     t_traces = time.perf_counter() - t0
     net = ProposalNet(seed=args.seed)
     t1 = time.perf_counter()
     losses = train(net, xs, ys, epochs=args.train_epochs)
     t_train = time.perf_counter() - t1
-    del xs, ys
+    # the top-score margin each training graph needed with the trained network, and
+    # the margin calibrated from them for the unseen workload graph
+    needed = [needed_margin(net.forward(x, sh).cpu().numpy(), r.weight_sorted, len(r.selected), r.K_needed)
+              for x, r in zip(xs, rs)]
+    margin = calibrate_margin(needed) if args.proposal_rule == "calibrated" else args.margin
+    rule = "top" if args.proposal_rule == "calibrated" else args.proposal_rule
+    del xs, ys, rs
     untrained = ProposalNet(seed=args.seed)
     # graph -> basis on the proposal's prefix (its lists copied to the host afterwards,
     # for the end-to-end steps; the untrained network's prefix on the same features
     # for comparison: neither is part of the timed solve)
-    r, lsolver, p, x = solve_with_proposal(g, net, margin=args.margin, stream=sh, keep_solver=True,
-                                           host_lists=True, compare=[untrained], rule=args.proposal_rule,
+    r, lsolver, p, x = solve_with_proposal(g, net, margin=margin, stream=sh, keep_solver=True,
+                                           host_lists=True, compare=[untrained], rule=rule,
                                            eps=args.eps, keep_logits=True, keep_features=True)
     fwd = forward_throughput(net, x, sh)
     del x
@@ -460,7 +468,8 @@ def learned_form(args, g, sel0, tot0, sh):
                "fallback": r.fallback, "K": r.K, "K_kept": r.K_kept,
                "K_needed": K_needed, "U": r.U, "nnz_kept": r.nnz_kept, "trees": r.trees,
                "trees_kept": r.trees_kept, "rule": args.proposal_rule,
-               "rule_param": args.eps if args.proposal_rule == "tail" else args.margin,
+               "rule_param": args.eps if args.proposal_rule == "tail" else margin,
+               "training_needed_margins": [round(m, 4) for m in needed],
                "untrained_skip_rate": 1.0 - uk / max(r.K, 1), "rules_on_this_graph": table,
                "training": {"graphs": args.train_graphs, "points": args.train_n, "candidates": int(sum(ks)),
                             "epochs": args.train_epochs, "loss_first_last": [round(losses[0], 4),
@@ -948,8 +957,9 @@ def main():
     ap.add_argument("--train-graphs", type=int, default=3, help="graphs whose traces train the proposal")
     ap.add_argument("--train-n", type=int, default=60000, help="size (--n units) of the training graphs")
     ap.add_argument("--train-epochs", type=int, default=20)
-    ap.add_argument("--proposal-rule", choices=["tail", "top"], default="top",
-                    help="top: ceil(N (1 + margin)) top scores; tail: expected selections beyond the prefix <= --eps")
+    ap.add_argument("--proposal-rule", choices=["calibrated", "tail", "top"], default="calibrated",
+                    help="top: ceil(N (1 + margin)) top scores; tail: expected selections beyond the prefix <= --eps; "
+                         "calibrated (default): the top rule with the margin the training graphs needed, x 1.25 + 0.05")
     ap.add_argument("--eps", type=float, default=0.1)
     ap.add_argument("--margin", type=float, default=1.0)
     ap.add_argument("--plain-windows", type=int, default=8)

@@ -145,6 +145,27 @@ def proposal_prefix(logits_host: np.ndarray, weight_sorted: np.ndarray, N: int, 
     return int(np.searchsorted(weight_sorted, U, side="right")), U
 
 
+def needed_margin(logits_host: np.ndarray, weight_sorted: np.ndarray, N: int, K_needed: int) -> float:
+    """The smallest top-score margin whose prefix holds the first K_needed candidates of
+    the rank order: the proposals (the top ceil(N (1 + margin)) scores) must include a
+    candidate at least as heavy as the last needed one, whose weight class then ends
+    the prefix at or past it."""
+    K = len(weight_sorted)
+    if K == 0 or K_needed <= 0 or N <= 0:
+        return 0.0
+    w_star = weight_sorted[min(K_needed, K) - 1]
+    order = np.argsort(-logits_host, kind="stable")
+    heavy = np.nonzero(weight_sorted[order] >= w_star)[0]
+    first = int(heavy[0]) + 1  # proposals needed to reach a heavy enough candidate
+    return max(first / N - 1.0, 0.0)
+
+
+def calibrate_margin(margins, scale: float = 1.25, slack: float = 0.05) -> float:
+    """The top-score margin for unseen graphs: the largest margin the training graphs
+    needed, scaled and padded (a margin is relative to N, so it carries over sizes)."""
+    return float(max(margins, default=0.0)) * scale + slack
+
+
 def calibrated(logits_host: np.ndarray, pos_weight: float) -> np.ndarray:
     """P(selected) from logits trained with positives weighted by pos_weight (the
     weighting multiplies the odds by pos_weight)."""
@@ -202,8 +223,14 @@ class LearnedSolve:
     fallback: bool
     times: dict = field(default_factory=dict)
     lists: tuple | None = None
+    weight_sorted: np.ndarray | None = None
     compared: list = field(default_factory=list)
     logits: np.ndarray | None = None
+
+    @property
+    def K_needed(self) -> int:
+        """The rank-order prefix the basis needs: up to its last selected candidate."""
+        return int(np.max(self.selected)) + 1 if len(self.selected) else 0
 
     @property
     def proposed_skip_rate(self) -> float:
@@ -302,8 +329,8 @@ def solve_with_proposal(src, net: ProposalNet | None, margin: float = 0.05, thre
         off, co = gen.fetch_lists(stream)
         lists = (np.ascontiguousarray(w[:len(off) - 1]), off, co)
     gen.close()
-    out = LearnedSolve(sel, tot, K, K_keep, U, nnz, p.F, trees_kept, fallback, times, lists, compared,
-                       lh if (keep_logits and net is not None and prefix is None) else None)
+    out = LearnedSolve(sel, tot, K, K_keep, U, nnz, p.F, trees_kept, fallback, times, lists, np.asarray(w),
+                       compared, lh if (keep_logits and net is not None and prefix is None) else None)
     extra = []
     if keep_solver:
         extra += [solver, p]
