@@ -2384,9 +2384,10 @@ __global__ void __launch_bounds__(256) cert_check_kernel(const unsigned long lon
 // default, more local pivots per step, wider windows, deeper streaming passes.  A
 // solve is cut into kShapeSegs segments of blocks, each with its own shape (the
 // pivots of later blocks lie deeper in the rank order).  On the 1M-vertex
-// planar-chain graph the wider windows with 8 local pivots take 0.105-0.116 ms per
-// block against 0.129-0.185 ms for the default (a one-tile early window was 10x
-// slower there and is not a candidate).
+// planar-chain graph's prefix solve the wider windows with 8 local pivots (candidate
+// 2) take 0.113-0.146 ms per block against 0.128-0.164 ms for the default, from the
+// first quarter of the solve to the last (a one-tile early window was 10x slower
+// there and is not a candidate).
 constexpr int kShapeSegs = 4;
 constexpr int kShapeInts = 7;  // ints per shape in mcbgpu_solver_shapes
 const PivotShape kCandidateShapes[] = {
