@@ -312,3 +312,112 @@ def test_grouped_pass_correction_identity_three_blocks():
                     S[j] ^= S[e0 + k]
         hist.append((e0, Wb, m, betas))
     assert checked > 20
+
+
+def blocked_select_wordlists(prob, B, ww, cap):
+    """blocked_select with the far update of the blocked run's word-list form: the B
+    rows after a block are near rows (D gathered directly); every later ("far") row is
+    either still its unit vector (D from membership of its own coordinate in the
+    selected cycles: the scatter), or listed by its nonzero ww-bit words (D from the
+    pairs in those words only), or dense past `cap` listed words (D gathered
+    directly).  Every far row's D is checked against the direct one at every block,
+    and the rows are relisted after they change.  Returns the selected ranks."""
+    N, K = prob.N, prob.K
+    off, co = prob.cycle_lists()
+    lists = [co[off[r]:off[r + 1]].tolist() for r in range(K)]
+    S = [1 << j for j in range(N)]
+    dot = lambda s, r: sum((s >> c) & 1 for c in lists[r]) & 1  # noqa: E731
+    unit = [True] * N
+    words = [None] * N  # listed words of a non-unit far row, or "dense"
+    mask = (1 << ww) - 1
+
+    def relist(j, Wb):
+        nz = [w for w in range(Wb) if (S[j] >> (ww * w)) & mask]
+        own = j // ww
+        assert own >= Wb and (S[j] >> (ww * own)) & mask == 1 << (j % ww)  # the row's own word: bit j alone
+        assert S[j] >> (ww * Wb) == (S[j] >> (ww * own)) << (ww * (own - Wb))  # nothing else above Wb
+        nz.append(own)
+        words[j] = nz if len(nz) <= cap else "dense"
+
+    sel = []
+    checked = {"unit": 0, "sparse": 0, "dense": 0}
+    for e0 in range(0, N, B):
+        b = min(B, N - e0)
+        echelon, piv = {}, []
+        for r in range(K):
+            W = sum(dot(S[e0 + k], r) << k for k in range(b))
+            x = W
+            while x:
+                p = (x & -x).bit_length() - 1
+                if p in echelon:
+                    x ^= echelon[p]
+                else:
+                    echelon[p] = x
+                    piv.append((r, W))
+                    break
+            if len(piv) == b:
+                break
+        m = [1 << k for k in range(b)]
+        g, chosen, used = [], [], set()
+        for k in range(b):
+            p = next(i for i in range(b) if i not in used and parity(piv[i][1] & m[k]))
+            used.add(p)
+            chosen.append(p)
+            wp = piv[p][1]
+            g.append(sum(parity(wp & m[i]) << i for i in range(k)))
+            for j in range(k + 1, b):
+                if parity(wp & m[j]):
+                    m[j] ^= m[k]
+        S0 = [S[e0 + l] for l in range(b)]
+        for k in range(b):
+            v = 0
+            for l in range(b):
+                if (m[k] >> l) & 1:
+                    v ^= S0[l]
+            S[e0 + k] = v
+        sel += [piv[c][0] for c in chosen]
+        # the selected cycles' (coordinate, k) pairs, by word
+        pairs = [(c, k) for k in range(b) for c in lists[piv[chosen[k]][0]]]
+        by_word = {}
+        for c, k in pairs:
+            by_word.setdefault(c // ww, []).append((c, k))
+        Wb = (e0 + b + ww - 1) // ww
+        far_start = e0 + b + B
+        for j in range(e0 + b, N):
+            D = sum(dot(S[j], piv[chosen[k]][0]) << k for k in range(b))
+            if j >= far_start:
+                if unit[j]:
+                    Dw = sum(1 << k for c, k in pairs if c == j)
+                    checked["unit"] += 1
+                elif words[j] == "dense":
+                    Dw = D
+                    checked["dense"] += 1
+                else:
+                    Dw = 0
+                    for w in words[j]:
+                        for c, k in by_word.get(w, []):
+                            Dw ^= ((S[j] >> c) & 1) << k
+                    checked["sparse"] += 1
+                assert Dw == D, (e0, j)
+            beta = 0
+            for k in range(b):
+                beta |= (((D >> k) & 1) ^ parity(beta & g[k])) << k
+            for k in range(b):
+                if (beta >> k) & 1:
+                    S[j] ^= S[e0 + k]
+            if j >= far_start and beta:
+                unit[j] = False
+                relist(j, Wb)
+    return sel, checked
+
+
+@pytest.mark.parametrize("graph,B,cap", [(random_graph(200, 400, 1, 20, 2), 8, 3),
+                                         (random_graph(200, 400, 1, 20, 2), 8, 64),
+                                         (random_graph(300, 700, 1, 5, 5), 8, 2)])
+def test_far_update_by_word_lists(graph, B, cap):
+    p = Problem.from_graph(graph).prepare(threads=2, keep_trees=True)
+    ref, _, _ = oracle.solve(p, threads=2)
+    sel, checked = blocked_select_wordlists(p, B, 8, cap)
+    assert sel == ref.tolist()
+    assert checked["unit"] > 0 and checked["sparse"] > 0  # all three kinds of far row met
+    assert (checked["dense"] > 0) == (cap < 8)
