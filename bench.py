@@ -687,14 +687,7 @@ def run_gpu(args, world, rank, local, pg):
     per_launch_s = st["ms"] / 1e3 / max(st["launches"], 1)
     per_launch_b = st["bytes"] / max(st["launches"], 1)
     achieved = per_launch_b / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            tj = json.load(f)
-        rec = tj.get("%s:%d" % (args.graph, args.n))
-        if rec:  # captured on this workload (or scaled to it; see the file)
-            traffic = rec.get(name)
+    traffic = None  # DRAM bytes per launch need an ncu capture; the ncu summaries are under profiles/
     total_ms = sum(v["ms"] for v in stats.values())
     # the search phase (streaming pass, its correction, the pivot search): the part of
     # the metric's "search HBM GB/s" -- their algorithmic bytes over their event time
