@@ -71,3 +71,20 @@ def test_reference_arm_of_the_planar_workload_prints_one_line():
     assert d["config"]["workload"].startswith("planar-like graph from 1500 triangulated points")
     assert "label pass over 40 of the" in d["cpu_baseline"]["sample"]
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_sampled_cpu_baseline_tracks_a_full_oracle_solve():
+    # the single-graph CPU baseline extrapolates a sampled label pass and a sampled
+    # update to a whole solve; on a graph the oracle solves in a second the estimate
+    # must land near the measured loop (it leaves out the list scan: slightly low)
+    import argparse
+
+    import bench
+    import oracle
+    from minimumcyclebasis_gb300 import Problem, planar_chain_graph
+    g = planar_chain_graph(1500, 30, 30, 8, 1, 1000, 7)
+    p = Problem.from_graph(g).prepare(threads=4, keep_trees=True)
+    _, _, loop_s = oracle.solve(p, threads=4)
+    ps = Problem.from_graph(g).prepare(threads=4, structure_only=True)
+    est = bench.cpu_baseline(ps, argparse.Namespace(cpu_sample_roots=2000), 4)
+    assert 0.5 < est["value"] / loop_s < 2.0, (est["value"], loop_s)
