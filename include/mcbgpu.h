@@ -210,7 +210,7 @@ int mcbgpu_solver_kernel_stats(mcbgpu_solver *s, mcbgpu_kernel_stat *out, int ma
  * arrivals), [14]/[15] most/fewest barriers of a CTA in one launch, [16]-[19] first
  * step at which two CTAs disagreed on the merged result (flag, step, CTA, block),
  * [20] / [21] / [22] SM clock cycles of CTA 0 in the block tail: resolve, the tail's
- * grid barrier, final rows + tables; far update: [23] dense non-unit rows gathered,
+ * grid barrier, final rows; far update: [23] dense non-unit rows gathered,
  * [29] update bits of the changed rows, [30] rows changed, [31] pair words gathered,
  * [32] unit rows reached by the scatter, [38] sparse non-unit rows tested, [39]
  * their listed words, [40] their pair tests; [24]-[28] and [33]-[37] per-phase clock
