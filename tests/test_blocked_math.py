@@ -421,3 +421,116 @@ def test_far_update_by_word_lists(graph, B, cap):
     assert sel == ref.tolist()
     assert checked["unit"] > 0 and checked["sparse"] > 0  # all three kinds of far row met
     assert (checked["dense"] > 0) == (cap < 8)
+
+
+def sequential_pivots(W, b):
+    """The first b candidates, in rank order, whose W is independent of every earlier
+    W (the pivots of a block)."""
+    echelon, piv = {}, []
+    for r, w in enumerate(W):
+        x = w
+        while x:
+            p = (x & -x).bit_length() - 1
+            if p in echelon:
+                x ^= echelon[p]
+            else:
+                echelon[p] = x
+                piv.append(r)
+                break
+        if len(piv) == b:
+            break
+    return piv
+
+
+def reduce_by(x, echelon):
+    while x:
+        p = (x & -x).bit_length() - 1
+        if p not in echelon:
+            return x, p
+        x ^= echelon[p]
+    return 0, -1
+
+
+def windowed_pivots(W, b, G, tile, shape):
+    """The pivot search of blk_pivot_kernel restated step by step: G CTAs, CTA c owning
+    the tiles t = c (mod G); per step each CTA scans its next window of tiles from the
+    scan start s (the shape's window for the number of pivots known), turns every
+    candidate independent of the basis and its own local pivots into a local pivot,
+    stops after the shape's local-pivot limit, and reports its local pivots and `end`
+    (every one of its candidates below end scanned); the merge takes D = min end and
+    accepts, in rank order, the reported local pivots below D independent of the
+    basis and of those accepted before them; s = D.  Returns the pivots and the steps."""
+    win_early, rank_early, win_mid, rank_tail, win_tail, lmax = shape
+    K = len(W)
+    ntiles = (K + tile - 1) // tile
+    basis, piv, s, steps = {}, [], 0, 0
+    while len(piv) < b:
+        steps += 1
+        wsz = win_early if len(piv) < rank_early else win_tail if len(piv) >= rank_tail else win_mid
+        t0 = s // tile
+        reports, ends = [], []
+        for c in range(G):
+            tf = t0 + ((c - t0 % G) % G)
+            tiles = [t for t in (tf + m * G for m in range(wsz)) if t < ntiles]
+            local = dict(basis)
+            nloc, end, trunc = 0, K, False
+            for t in tiles:
+                lo = max(t * tile, s)
+                for r in range(lo, min((t + 1) * tile, K)):
+                    x, p = reduce_by(W[r], local)
+                    if x:
+                        local[p] = x
+                        reports.append((r, W[r]))
+                        nloc += 1
+                        if nloc == lmax:
+                            end, trunc = r + 1, True
+                            break
+                if trunc:
+                    break
+            if not trunc and len(tiles) == wsz:
+                end = min((tiles[-1] + 1) * tile, K)
+            ends.append(end)
+        D = min(ends)
+        for r, w in sorted(x for x in reports if x[0] < D):
+            x, p = reduce_by(w, basis)
+            if x and len(piv) < b:
+                basis[p] = x
+                piv.append(r)
+        if D >= K and len(piv) < b:
+            break  # the candidates do not span
+        s = D
+    return piv, steps
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_windowed_pivot_search_is_exact_for_every_shape(seed):
+    # W's of a block with its pivots spread over the rank order (each pivot brings a
+    # new direction; every other candidate is zero or a combination of the directions
+    # seen so far, the common case in a de Pina block): the step-wise search gives the
+    # sequential pivots for every window, local-pivot limit and grid size
+    rng = np.random.default_rng(seed)
+    b, K = 16, 2500
+    at = sorted(rng.choice(np.arange(1, K), size=b - 1, replace=False).tolist()) + [0]
+    at = sorted(at)
+    W, dirs = [], []
+    for r in range(K):
+        if at and r == at[0]:
+            at.pop(0)
+            v = (1 << len(dirs)) | (int(rng.integers(0, 1 << len(dirs))) if dirs else 0)
+            dirs.append(v)
+            W.append(v)
+        elif dirs and rng.random() < 0.6:
+            w = 0
+            for i in rng.choice(len(dirs), size=int(rng.integers(1, 4))):
+                w ^= dirs[int(i)]
+            W.append(w)
+        else:
+            W.append(0)
+    want = sequential_pivots(W, b)
+    assert len(want) == b
+    for G in (1, 3, 7):
+        for tile in (16, 64):
+            for shape in ((2, 8, 6, 12, 8, 6), (1, 4, 4, 12, 12, 8), (4, 8, 8, 12, 12, 1), (3, 5, 2, 9, 1, 3)):
+                got, steps = windowed_pivots(W, b, G, tile, shape)
+                assert got == want, (G, tile, shape)
+                assert steps >= 1
