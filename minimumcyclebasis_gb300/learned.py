@@ -23,7 +23,7 @@ heaviest proposal's weight U bounds the prefix.  Either way the prefix ends at t
 end of a weight class (every candidate of weight <= U, ties included).  The solver runs
 on that prefix and checks itself: if some iteration finds no odd candidate in it
 (the proposals did not hold a basis), the whole list is built and the solve is run
-again on it.  Either way the result is the plain solve's, which stays the judge.  When
+again on it.  Either way the result is the plain solve's, which stays the arbiter.  When
 the prefix suffices, its heaviest selected weight is an exact upper bound of the
 minimum basis's heaviest cycle (a matroid's greedy basis minimises its largest
 element).
