@@ -15,11 +15,13 @@ The network proposes it.  It scores every candidate from 16 features of its cycl
 length, rank quantile, degrees; computed on the device during the cycle walk) with a
 two-layer perceptron (16 -> 64 ReLU -> 1, bf16 weights, fp32 accumulation; its first
 layer on the tensor cores) trained on (candidate, selected?) traces of solved graphs.
-Two rules turn scores into a prefix.  The tail rule (the default): the shortest prefix
-beyond which the candidates' calibrated probabilities of selection sum to at most
-eps, i.e. the expected number of selected candidates left out is at most eps.  The
-top-score rule: the top ceil(N (1 + margin)) scores are the proposals and the
-heaviest proposal's weight U bounds the prefix.  Either way the prefix ends at the
+Two rules turn scores into a prefix.  The tail rule (solve_with_proposal's default):
+the shortest prefix beyond which the candidates' calibrated probabilities of
+selection sum to at most eps, i.e. the expected number of selected candidates left
+out is at most eps.  The top-score rule: the top ceil(N (1 + margin)) scores are the
+proposals and the heaviest proposal's weight U bounds the prefix; its margin can be
+calibrated on the training graphs (needed_margin, calibrate_margin), which is how
+the benchmark uses it.  Either way the prefix ends at the
 end of a weight class (every candidate of weight <= U, ties included).  The solver runs
 on that prefix and checks itself: if some iteration finds no odd candidate in it
 (the proposals did not hold a basis), the whole list is built and the solve is run
